@@ -1,0 +1,145 @@
+/*
+ * tecs_gpu.h -- C ABI of the GB300 (sm_103a) cell-step library.
+ *
+ * The TECS reference exposes its hot path as C++ templates (Simulation,
+ * pair finders, integrators, com fixers).  This header is the thin C layer
+ * beneath those templates: plain pointers and sizes, no C++ or torch types,
+ * so a ctypes / cffi / cgo / JNI stub can bind it directly.  Each entry point
+ * names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns 0 on success and a negative status on failure;
+ *     tecs_last_error() then holds a message for the calling thread.
+ *   - "host" pointers are ordinary CPU memory (pinned or pageable); "device"
+ *     pointers are CUDA global memory on the simulation's device.
+ *   - Positions are AoS float[n][dims] (the byte layout of the reference's
+ *     View<VectorN<float, dims>>); polarities are float[n][2] (theta, phi),
+ *     the layout of View<Polarity_<float>>.
+ *   - Work is queued on the simulation's CUDA stream; download/count calls
+ *     synchronise it.
+ */
+#ifndef TECS_GPU_H
+#define TECS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Pair finders: include/pair_finders/{naive_all_pairs,binned_all_pairs,naive_gabriel,binned_gabriel}.hpp */
+enum tecs_finder {
+  TECS_FINDER_NAIVE_ALL_PAIRS = 0,
+  TECS_FINDER_BINNED_ALL_PAIRS = 1,
+  TECS_FINDER_NAIVE_GABRIEL = 2,
+  TECS_FINDER_BINNED_GABRIEL = 3
+};
+
+/* Integrators: include/integrators/euler.hpp, heun.hpp */
+enum tecs_integrator { TECS_EULER = 0, TECS_HEUN = 1 };
+
+/* Built-in pairwise force descriptors (the C layer cannot take user lambdas). */
+enum tecs_force {
+  TECS_FORCE_NONE = 0,      /* no deltas (pair capture only)                                       */
+  TECS_FORCE_SPRING2R = 1,  /* F = k_rep*max(r_rep-d,0) - k_adh*max(d-r_adh,0); covers forces::Spring
+                               and forces::PiecewiseLinear (include/forces/predefined.hpp:60-144)   */
+  TECS_FORCE_POLARITY = 2   /* spring2r + k_pol*(Polarity_::bending_force + bidirectional alignment)
+                               (include/types/polarity.hpp:131-198); dims must be 3                  */
+};
+
+/* Simulation description.  Field names and defaults follow Simulation::Settings
+ * (include/simulation.hpp:76-98) and BinnedGabriel::Settings
+ * (include/pair_finders/binned_gabriel.hpp:20-26). */
+typedef struct tecs_sim_desc {
+  int dims;                     /* 2 or 3                                                         */
+  int finder;                   /* enum tecs_finder                                               */
+  int symmetric;                /* 1 = the *Symmetric finder variants (j<i, +d to i, -d to j)     */
+  float cutoff;                 /* Settings::cutoff_distance                                      */
+  float gabriel_coefficient;    /* default 0.8                                                    */
+  float min_bounds[3];          /* default -20                                                    */
+  float max_bounds[3];          /* default +20                                                    */
+  float bin_size_scale;         /* default 1                                                      */
+  int rebuild_every_n;          /* default 0 (rebuild on every full step)                         */
+  int integrator;               /* enum tecs_integrator                                           */
+  int com_fix;                  /* 0 = com_fixers::NoComFixer, 1 = com_fixers::GlobalComFixer     */
+  int force;                    /* enum tecs_force                                                */
+  float k_rep, r_rep, k_adh, r_adh, k_pol;
+  int has_polarity;             /* second field (Polarity) present                                */
+  unsigned capacity;            /* Settings::capacity (>= agent count; COM divides by it)         */
+  double division_probability;  /* per cell per step; 0 disables division                         */
+  float division_offset;        /* daughter = parent + offset * random unit vector                */
+  uint64_t seed;                /* Settings::seed                                                 */
+  int device;                   /* CUDA device ordinal                                            */
+} tecs_sim_desc;
+
+typedef struct tecs_sim tecs_sim;
+
+/* Fill *desc with the reference defaults (dims 3, binned Gabriel, Heun, no COM). */
+int tecs_sim_desc_default(tecs_sim_desc* desc);
+
+/* Simulation(Settings) constructor: allocates the device state for desc->capacity cells.
+ * Replaces include/simulation.hpp:133-153. */
+int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out);
+
+/* Frees every device buffer of the simulation. */
+int tecs_sim_destroy(tecs_sim* sim);
+
+/* Initial state from host memory (n <= capacity); resets the step counters
+ * as Simulation::set_agent_count does (include/simulation.hpp:295-302). */
+int tecs_sim_upload(tecs_sim* sim, const float* positions, const float* polarity, unsigned n);
+
+/* Same from device memory on the simulation's device (no host copy). */
+int tecs_sim_upload_device(tecs_sim* sim, const float* d_positions, const float* d_polarity, unsigned n);
+
+/* Simulation::take_step(dt, force) repeated n_steps times
+ * (include/simulation.hpp:548-556 -> integrators/{euler,heun}.hpp::integrate),
+ * followed by cell division when enabled.  Asynchronous. */
+int tecs_sim_step(tecs_sim* sim, double dt, int n_steps);
+
+/* Wait for the simulation's queued work. */
+int tecs_sim_synchronize(tecs_sim* sim);
+
+/* Current agent count (synchronises). */
+int tecs_sim_count(tecs_sim* sim, unsigned* n);
+
+/* Copy the state back in cell-id order (synchronises).  The host side of
+ * View::sync_host + HDF5_Writer::write (include/io/hdf5_writer.hpp:306-321).
+ * positions: capacity*dims floats; polarity: capacity*2 floats or NULL. */
+int tecs_sim_download(tecs_sim* sim, float* positions, float* polarity, unsigned* n);
+
+/* Test hook: one full-step force evaluation of the current state with a
+ * fresh grid (PairFinder::evaluate_force, e.g. binned_gabriel.hpp:71-362).
+ * Writes per-cell deltas in cell-id order (dpos: n*dims, dpol: n*2 or NULL)
+ * and, when pairs != NULL, up to pair_capacity directed (self, other) id
+ * pairs in unspecified order; *n_pairs receives the total.  Synchronises. */
+int tecs_sim_evaluate(tecs_sim* sim, float* dpos, float* dpol, uint32_t* pairs, size_t pair_capacity,
+                      size_t* n_pairs);
+
+/* The simulation's CUDA stream (a cudaStream_t). */
+void* tecs_sim_stream(tecs_sim* sim);
+
+/* Capture each step as a CUDA graph and replay it (default on). */
+int tecs_sim_set_graph(tecs_sim* sim, int enable);
+
+/* Bracket every kernel of a step with CUDA events (recorded as event nodes
+ * inside the step's graph).  Changing the setting re-captures the graph. */
+int tecs_sim_set_profiling(tecs_sim* sim, int enable);
+
+/* Per-kernel durations (ms) of the most recently completed step, in launch
+ * order; *count receives the number of kernels (synchronises). */
+int tecs_sim_last_step_profile(tecs_sim* sim, float* ms, int capacity, int* count);
+
+/* Name of kernel `index` of that profile (static string), or NULL. */
+const char* tecs_sim_profile_name(tecs_sim* sim, int index);
+
+/* Number of kernels one step launches (for launch accounting). */
+int tecs_sim_kernels_per_step(tecs_sim* sim, int* kernels);
+
+/* Message of the last failing call on this thread. */
+const char* tecs_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TECS_GPU_H */

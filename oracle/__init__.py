@@ -1,0 +1,165 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle is the checker the CUDA path is compared against.  Only the test
+suite, ``__graft_entry__.smoke()`` and the benchmark's CPU-baseline leg import
+this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libtecs_oracle.so"
+
+NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL = 0, 1, 2, 3
+FORCE_NONE, FORCE_SPRING2R, FORCE_POLARITY = 0, 1, 2
+EULER, HEUN = 0, 1
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int),
+        ("finder", ctypes.c_int),
+        ("symmetric", ctypes.c_int),
+        ("cutoff", ctypes.c_float),
+        ("gabriel_coefficient", ctypes.c_float),
+        ("min_bounds", ctypes.c_float * 3),
+        ("max_bounds", ctypes.c_float * 3),
+        ("bin_size_scale", ctypes.c_float),
+        ("rebuild_every_n", ctypes.c_int),
+        ("integrator", ctypes.c_int),
+        ("com_fix", ctypes.c_int),
+        ("force", ctypes.c_int),
+        ("k_rep", ctypes.c_float),
+        ("r_rep", ctypes.c_float),
+        ("k_adh", ctypes.c_float),
+        ("r_adh", ctypes.c_float),
+        ("k_pol", ctypes.c_float),
+        ("has_polarity", ctypes.c_int),
+        ("capacity", ctypes.c_uint),
+        ("division_probability", ctypes.c_double),
+        ("division_offset", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+def build(force: bool = False) -> Path:
+    """Compile the C restatement into oracle/_build/libtecs_oracle.so."""
+    src = HERE / "tecs_oracle.c"
+    if LIB.exists() and not force and LIB.stat().st_mtime >= src.stat().st_mtime:
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-fopenmp", str(src), "-o", str(LIB), "-lm"]
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        L.tecs_oracle_create.restype = ctypes.c_void_p
+        L.tecs_oracle_create.argtypes = [ctypes.POINTER(Desc)]
+        L.tecs_oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.tecs_oracle_set_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint]
+        L.tecs_oracle_count.restype = ctypes.c_uint
+        L.tecs_oracle_count.argtypes = [ctypes.c_void_p]
+        L.tecs_oracle_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.tecs_oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.tecs_oracle_evaluate.restype = ctypes.c_long
+        L.tecs_oracle_evaluate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_long, ctypes.c_int]
+        L.tecs_oracle_hash.restype = ctypes.c_uint64
+        L.tecs_oracle_hash.argtypes = [ctypes.c_uint64] * 4
+        L.tecs_oracle_last_error.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """One simulation held by the CPU restatement."""
+
+    def __init__(self, *, dims=3, finder=BINNED_GABRIEL, symmetric=False, cutoff=1.0,
+                 gabriel_coefficient=0.8, min_bounds=(-20, -20, -20), max_bounds=(20, 20, 20),
+                 bin_size_scale=1.0, rebuild_every_n=0, integrator=HEUN, com_fix=False,
+                 force=FORCE_SPRING2R, k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8, k_pol=0.0,
+                 has_polarity=False, capacity=0, division_probability=0.0, division_offset=0.25,
+                 seed=2807):
+        d = Desc()
+        d.dims, d.finder, d.symmetric = dims, finder, int(symmetric)
+        d.cutoff, d.gabriel_coefficient = cutoff, gabriel_coefficient
+        for k in range(3):
+            d.min_bounds[k] = float(min_bounds[k]) if k < len(min_bounds) else 0.0
+            d.max_bounds[k] = float(max_bounds[k]) if k < len(max_bounds) else 0.0
+        d.bin_size_scale, d.rebuild_every_n = bin_size_scale, rebuild_every_n
+        d.integrator, d.com_fix, d.force = integrator, int(com_fix), force
+        d.k_rep, d.r_rep, d.k_adh, d.r_adh, d.k_pol = k_rep, r_rep, k_adh, r_adh, k_pol
+        d.has_polarity, d.capacity = int(has_polarity), capacity
+        d.division_probability, d.division_offset, d.seed = division_probability, division_offset, seed
+        self.desc = d
+        self.dims = dims
+        self.has_polarity = has_polarity
+        self._h = lib().tecs_oracle_create(ctypes.byref(d))
+        if not self._h:
+            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().tecs_oracle_destroy(h)
+            self._h = None
+
+    def set_state(self, positions, polarity=None):
+        x = np.ascontiguousarray(positions, dtype=np.float32)
+        p = None if polarity is None else np.ascontiguousarray(polarity, dtype=np.float32)
+        if lib().tecs_oracle_set_state(self._h, _ptr(x), _ptr(p), x.shape[0]) != 0:
+            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+
+    @property
+    def count(self):
+        return lib().tecs_oracle_count(self._h)
+
+    def get_state(self):
+        n = self.count
+        x = np.empty((n, self.dims), np.float32)
+        p = np.empty((n, 2), np.float32) if self.has_polarity else None
+        lib().tecs_oracle_get_state(self._h, _ptr(x), _ptr(p))
+        return x, p
+
+    def step(self, dt, n_steps=1, threads=1):
+        lib().tecs_oracle_step(self._h, dt, n_steps, threads)
+
+    def evaluate(self, want_pairs=True, threads=1):
+        """Deltas of one full-step force pass and the directed pairs in evaluation order."""
+        n = self.count
+        dx = np.zeros((n, self.dims), np.float32)
+        dp = np.zeros((n, 2), np.float32) if self.has_polarity else None
+        if not want_pairs:
+            lib().tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), None, 0, threads)
+            return dx, dp, None
+        cap = max(1024, 64 * n)
+        while True:
+            pairs = np.zeros((cap, 2), np.uint32)
+            cnt = lib().tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), _ptr(pairs), cap, threads)
+            if cnt <= cap:
+                return dx, dp, pairs[:cnt]
+            cap = cnt
+
+
+def hash64(seed, step, cell, stream):
+    return lib().tecs_oracle_hash(seed, step, cell, stream)

@@ -1,0 +1,649 @@
+// kernels.cuh -- device kernels of one cell step on sm_103a.
+//
+// State layout in HBM (per simulation, capacity-sized):
+//   A      float4[cap]  x, y, z, cell id (uint bits)   state between steps
+//   B      float4[cap]  A reordered by (bin, cell id)   working copy of a step
+//   Xt     float4[cap]  Heun predictor x~ (sorted order)
+//   d1,d2  float4[cap]  pass-1 / pass-2 position deltas (sorted order)
+//   PA,PB,Pt,dp1,dp2    float2 polarity counterparts
+//   key,rank,src        uint[cap] bin key, tentative rank, sorted -> unsorted slot
+//   cnt,off             uint[nbins+1] bin counts (zero between steps), offsets
+#pragma once
+
+#include "common.cuh"
+#include "forces.cuh"
+
+namespace tecs {
+
+enum PassMode : int {
+  kStore = 0,       // d_out[i] = sum of pair deltas
+  kEulerFused = 1,  // A[i] = B[i] + sum * dt                               (euler.hpp:52-68, no COM)
+  kHeun1Fused = 2,  // d_out[i] = sum; Xt[i] = B[i] + sum * dt             (heun.hpp:54-68, no COM)
+  kHeun2Fused = 3   // A[i] = B[i] + ((d1[i] + sum) * 0.5) * dt            (heun.hpp:78-98, no COM)
+};
+
+struct Counters {
+  unsigned n;           // active cells
+  unsigned div_count;   // daughters requested this step
+  unsigned done[2];     // last-block counters of the two COM reductions
+  unsigned error;       // bit 0: capacity overflow on division
+  unsigned pad;
+  unsigned long long step;        // integrator steps taken (keys the division RNG)
+  unsigned long long pair_count;  // pairs recorded by the capture hook
+};
+
+struct PassArgs {
+  const float4* X;      // positions read by the pass (B or Xt)
+  const float2* P;      // polarities read by the pass (PB or Pt) or null
+  const unsigned* off;  // bin offsets
+  Counters* ctr;
+  // outputs
+  float4* d_out;
+  float2* dp_out;
+  // fused epilogues
+  const float4* Bx;     // x_n (sorted) for the fused updates
+  const float2* Bp;
+  const float4* d1;     // pass-1 deltas (Heun pass 2)
+  const float2* dp1;
+  float4* A;            // state written by the fused Euler / Heun-2 epilogue
+  float2* PA;
+  float4* Xt;           // predictor written by the fused Heun-1 epilogue
+  float2* Pt;
+  float dt;
+  int mode;
+  // centre-of-mass reduction (GlobalComFixer) fused into kStore
+  double* com_part;     // 3 doubles per block
+  float* com_out;       // 3 floats
+  int com_slot;         // 0 or 1 (which done counter)
+  unsigned capacity;
+  // division (fused into kEulerFused / kHeun2Fused)
+  double div_p;
+  float div_offset;
+  unsigned long long seed;
+  unsigned* div_parent;
+  unsigned* div_slot;
+  // pair capture hook
+  uint2* pairs;
+  unsigned long long pair_cap;
+};
+
+// ---------------------------------------------------------------------------
+// binning: key + count, exclusive scan, scatter, per-bin id sort + gather
+
+__global__ void k_count(const float4* __restrict__ A, const Counters* __restrict__ ctr, GridP g, int dims,
+                        unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = A[s];
+    float p[3] = {v.x, v.y, v.z};
+    int c[3] = {0, 0, 0};
+    unsigned b;
+    if (dims == 3) { bin_coords_div<3>(g, p, c); b = flatten<3>(g, c); }
+    else { bin_coords_div<2>(g, p, c); b = flatten<2>(g, c); }
+    key[s] = b;
+    rank[s] = atomicAdd(&cnt[b], 1u);
+  }
+}
+
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 16;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+__device__ __forceinline__ unsigned block_sum(unsigned v, unsigned* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0u;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sh[0] = t;
+  __syncthreads();
+  t = sh[0];
+  __syncthreads();
+  return t;
+}
+
+// Per-chunk totals of cnt[0..len).
+__global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned len, unsigned* __restrict__ part) {
+  __shared__ unsigned sh[32];
+  const unsigned base = blockIdx.x * kScanChunk;
+  unsigned v = 0;
+  for (int k = 0; k < kScanPer; ++k) {
+    unsigned idx = base + k * kScanThreads + threadIdx.x;
+    if (idx < len) v += cnt[idx];
+  }
+  unsigned t = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Exclusive scan of cnt into off, zeroing cnt for the next step.
+__global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, const unsigned* __restrict__ part,
+                             unsigned* __restrict__ off) {
+  __shared__ unsigned sh[32];
+  __shared__ unsigned wsum[kScanThreads / 32];
+  // prefix of all earlier chunks
+  unsigned pre = 0;
+  for (unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += part[b];
+  pre = block_sum(pre, sh);
+  // each thread owns kScanPer consecutive elements
+  const unsigned base = blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+  unsigned vals[kScanPer];
+  unsigned local = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    unsigned idx = base + k;
+    vals[k] = idx < len ? cnt[idx] : 0u;
+    local += vals[k];
+  }
+  // block exclusive scan of the per-thread totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned w = lane < (kScanThreads / 32) ? wsum[lane] : 0u;
+    unsigned wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < (kScanThreads / 32)) wsum[lane] = wi - w;
+  }
+  __syncthreads();
+  unsigned run = pre + wsum[warp] + (incl - local);
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    unsigned idx = base + k;
+    if (idx < len) {
+      off[idx] = run;
+      cnt[idx] = 0u;
+    }
+    run += vals[k];
+  }
+}
+
+__global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
+                          const unsigned* __restrict__ rank, const unsigned* __restrict__ off,
+                          unsigned* __restrict__ src) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    src[off[key[s]] + rank[s]] = s;
+}
+
+// One thread per bin: order the bin's cells by id (the Serial BinSort order,
+// Kokkos_Sort binning loop in ascending index) and gather them into B.
+constexpr int kSortLocal = 24;
+__global__ void k_sort_gather(unsigned nbins, const unsigned* __restrict__ off, unsigned* __restrict__ src,
+                              const float4* __restrict__ A, const float2* __restrict__ PA, float4* __restrict__ B,
+                              float2* __restrict__ PB) {
+  const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  const unsigned lo = off[b], hi = off[b + 1];
+  const unsigned m = hi - lo;
+  if (m == 0) return;
+  if (m <= (unsigned)kSortLocal) {
+    unsigned sl[kSortLocal], id[kSortLocal];
+    for (unsigned r = 0; r < m; ++r) {
+      unsigned s = src[lo + r];
+      unsigned v = id_of(A[s]);
+      unsigned q = r;
+      while (q > 0 && id[q - 1] > v) { id[q] = id[q - 1]; sl[q] = sl[q - 1]; --q; }
+      id[q] = v; sl[q] = s;
+    }
+    for (unsigned r = 0; r < m; ++r) {
+      B[lo + r] = A[sl[r]];
+      if (PB) PB[lo + r] = PA[sl[r]];
+    }
+  } else {
+    // crowded bin: insertion sort in place on src (bounded by m*m/2 steps)
+    for (unsigned r = 1; r < m; ++r) {
+      unsigned s = src[lo + r];
+      unsigned v = id_of(A[s]);
+      unsigned q = r;
+      while (q > 0 && id_of(A[src[lo + q - 1]]) > v) { src[lo + q] = src[lo + q - 1]; --q; }
+      src[lo + q] = s;
+    }
+    for (unsigned r = 0; r < m; ++r) {
+      unsigned s = src[lo + r];
+      B[lo + r] = A[s];
+      if (PB) PB[lo + r] = PA[s];
+    }
+  }
+}
+
+// Naive finders keep the working copy in cell-id order.
+__global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __restrict__ A,
+                             const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = A[s];
+    unsigned id = id_of(v);
+    B[id] = v;
+    if (PB) PB[id] = PA[s];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// block reduction of the COM partials + last-block finalisation
+
+__device__ void com_reduce_block(const PassArgs& a, double x, double y, double z) {
+  __shared__ double sh[3][32];
+  __shared__ bool last;
+  for (int o = 16; o > 0; o >>= 1) {
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+    y += __shfl_xor_sync(0xffffffffu, y, o);
+    z += __shfl_xor_sync(0xffffffffu, z, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { sh[0][warp] = x; sh[1][warp] = y; sh[2][warp] = z; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sx = 0, sy = 0, sz = 0;
+    for (int w = 0; w < nw; ++w) { sx += sh[0][w]; sy += sh[1][w]; sz += sh[2][w]; }
+    a.com_part[3 * blockIdx.x + 0] = sx;
+    a.com_part[3 * blockIdx.x + 1] = sy;
+    a.com_part[3 * blockIdx.x + 2] = sz;
+    __threadfence();
+    unsigned prev = atomicAdd(&a.ctr->done[a.com_slot], 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  // fixed summation order over blocks: deterministic result
+  double sx = 0, sy = 0, sz = 0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    sx += __ldcg(&a.com_part[3 * b + 0]);
+    sy += __ldcg(&a.com_part[3 * b + 1]);
+    sz += __ldcg(&a.com_part[3 * b + 2]);
+  }
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
+  }
+  if (lane == 0) { sh[0][warp] = sx; sh[1][warp] = sy; sh[2][warp] = sz; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tx = 0, ty = 0, tz = 0;
+    for (int w = 0; w < nw; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
+    // com_fixers.hpp:43: mean over the stage view's extent, i.e. the capacity
+    const double cap = (double)a.capacity;
+    a.com_out[0] = (float)(tx / cap);
+    a.com_out[1] = (float)(ty / cap);
+    a.com_out[2] = (float)(tz / cap);
+    a.ctr->done[a.com_slot] = 0u;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// division: decide (RNG keyed by cell id and step), append daughter at A[n + k]
+
+template <int D>
+__device__ __forceinline__ void maybe_divide(const PassArgs& a, unsigned n, unsigned id, const float* xnew,
+                                             float2 pnew, unsigned long long step) {
+  if (a.div_p <= 0.0) return;
+  double u = u01(hash64(a.seed, step, id, 0));
+  if (u > a.div_p) return;
+  unsigned k = atomicAdd(&a.ctr->div_count, 1u);
+  unsigned slot = n + k;
+  if (slot >= a.capacity) { atomicOr(&a.ctr->error, 1u); return; }
+  double th = acos(2.0 * u01(hash64(a.seed, step, id, 1)) - 1.0);
+  double ph = u01(hash64(a.seed, step, id, 2)) * 2.0 * 3.14159265358979323846;
+  float v[3];
+  pol_to_vec3((float)th, (float)ph, v);
+  float4 o = make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));
+  o.x = xnew[0] + a.div_offset * v[0];
+  if (D >= 2) o.y = xnew[1] + a.div_offset * v[1];
+  if (D >= 3) o.z = xnew[2] + a.div_offset * v[2];
+  a.A[slot] = o;
+  if (a.PA) a.PA[slot] = pnew;
+  a.div_parent[k] = id;
+  a.div_slot[k] = slot;
+}
+
+// Daughter ids: n + rank of the parent id among this step's parents.
+__global__ void k_div_fixup(Counters* __restrict__ ctr, unsigned capacity, const unsigned* __restrict__ parent,
+                            const unsigned* __restrict__ slot, float4* __restrict__ A) {
+  const unsigned n = ctr->n;
+  unsigned k = ctr->div_count;
+  if (k > capacity - n) k = capacity - n;
+  for (unsigned d = blockIdx.x * blockDim.x + threadIdx.x; d < k; d += gridDim.x * blockDim.x) {
+    const unsigned p = parent[d];
+    unsigned r = 0;
+    for (unsigned e = 0; e < k; ++e) r += parent[e] < p ? 1u : 0u;
+    A[slot[d]].w = __uint_as_float(n + r);
+  }
+}
+__global__ void k_div_commit(Counters* __restrict__ ctr, unsigned capacity) {
+  const unsigned n = ctr->n;
+  unsigned k = ctr->div_count;
+  if (k > capacity - n) k = capacity - n;
+  ctr->n = n + k;
+  ctr->div_count = 0u;
+  ctr->step += 1ull;
+}
+__global__ void k_step_commit(Counters* __restrict__ ctr) { ctr->step += 1ull; }
+
+// ---------------------------------------------------------------------------
+// the force pass
+
+// Gabriel witness test over the bins that overlap the ball around the
+// midpoint (binned_gabriel.hpp:133-209).  true = some k blocks the pair.
+template <int D>
+__device__ __forceinline__ bool gabriel_blocked(const GridP& g, const ForceP& fp, const float4* __restrict__ X,
+                                                const unsigned* __restrict__ off, unsigned i, unsigned j,
+                                                const float* xi, const float* disp, float d2) {
+  float m[3];
+#pragma unroll
+  for (int d = 0; d < D; ++d) m[d] = xi[d] - disp[d] * 0.5f;
+  const float rsq = d2 * fp.gab_factor;
+  const float r = sqrtf(rsq);
+  int mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    mn[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1);
+    mx[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1);
+  }
+  const int z0 = D >= 3 ? mn[2] : 0, z1 = D >= 3 ? mx[2] : 0;
+  for (int z = z0; z <= z1; ++z) {
+    for (int y = mn[1]; y <= mx[1]; ++y) {
+      // a row of bins along x is one contiguous segment in sorted order
+      int c0[3] = {mn[0], y, z}, c1[3] = {mx[0], y, z};
+      const unsigned lo = off[flatten<D>(g, c0)], hi = off[flatten<D>(g, c1) + 1];
+      for (unsigned k = lo; k < hi; ++k) {
+        if (k == i || k == j) continue;
+        const float4 v = X[k];
+        const float e0 = v.x - m[0], e1 = v.y - m[1];
+        float s = e0 * e0 + e1 * e1;
+        if (D >= 3) { const float e2 = v.z - m[2]; s = s + e2 * e2; }
+        if (s < rsq) return true;
+      }
+    }
+  }
+  return false;
+}
+
+// naive_gabriel.hpp:71-80: every k, radius (d2 * 0.25) * c^2
+template <int D>
+__device__ __forceinline__ bool gabriel_blocked_naive(const ForceP& fp, const float4* __restrict__ X, unsigned n,
+                                                      unsigned i, unsigned j, const float* xi, const float* disp,
+                                                      float d2) {
+  float m[3];
+#pragma unroll
+  for (int d = 0; d < D; ++d) m[d] = xi[d] - disp[d] * 0.5f;
+  const float rsq = d2 * 0.25f * fp.gab_csq;
+  for (unsigned k = 0; k < n; ++k) {
+    if (k == i || k == j) continue;
+    const float4 v = X[k];
+    const float e0 = v.x - m[0], e1 = v.y - m[1];
+    float s = e0 * e0 + e1 * e1;
+    if (D >= 3) { const float e2 = v.z - m[2]; s = s + e2 * e2; }
+    if (s < rsq) return true;
+  }
+  return false;
+}
+
+template <int D, int FINDER, int FORCE>
+__device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+                                      unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi) {
+  const float4 vj = a.X[j];
+  float disp[3];
+  disp[0] = xi[0] - vj.x;
+  if (D >= 2) disp[1] = xi[1] - vj.y;
+  if (D >= 3) disp[2] = xi[2] - vj.z;
+  float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+  if (D >= 3) d2 = d2 + disp[2] * disp[2];
+  if (d2 >= fp.rc2) return;
+  if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
+  if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
+  if (a.pairs) {
+    unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(vj));
+  }
+  const float dist = sqrtf(d2);
+  const float2 pj = (FORCE == 2 && a.P) ? a.P[j] : make_float2(0.f, 0.f);
+  pair_force<D, FORCE>(fp, disp, dist, pi, pj, acc);
+}
+
+template <int D, int FINDER, int FORCE>
+__global__ void __launch_bounds__(128) k_pass(GridP g, ForceP fp, PassArgs a) {
+  const unsigned n = a.ctr->n;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  float xi[3] = {0.f, 0.f, 0.f};
+  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 pi = make_float2(0.f, 0.f);
+  if (active) {
+    vi = a.X[i];
+    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
+    if (a.P) pi = a.P[i];
+    const unsigned idi = id_of(vi);
+    if (FINDER == 1 || FINDER == 3) {
+      int bc[3] = {0, 0, 0};
+      if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
+      else bin_coords_div<D>(g, xi, bc);
+      // neighbour bins in the reference's task order (x fastest); each row of
+      // bins along x is one contiguous range of the sorted arrays
+      const int R = g.R;
+      const int z0 = D >= 3 ? -R : 0, z1 = D >= 3 ? R : 0;
+      for (int dz = z0; dz <= z1; ++dz) {
+        const int cz = D >= 3 ? bc[2] + dz : 0;
+        if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+        for (int dy = -R; dy <= R; ++dy) {
+          const int cy = bc[1] + dy;
+          if (cy < 0 || cy >= g.ext[1]) continue;
+          const int x0 = max(bc[0] - R, 0), x1 = min(bc[0] + R, g.ext[0] - 1);
+          int c0[3] = {x0, cy, cz}, c1[3] = {x1, cy, cz};
+          const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
+          for (unsigned j = lo; j < hi; ++j) {
+            if (j == i) continue;
+            visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
+          }
+        }
+      }
+    } else {
+      for (unsigned j = 0; j < n; ++j) {
+        if (j == i) continue;
+        visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
+      }
+    }
+  }
+  // commit: out(i) = 0 + sum (views(i) += values on cleared stage buffers);
+  // the drag term adds exactly zero for the built-in laws (pairwise_drag = 0)
+  float s[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
+  const float sp0 = 0.0f + acc.p[0], sp1 = 0.0f + acc.p[1];
+  if (a.mode == kStore) {
+    if (active) {
+      a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
+      if (a.dp_out) a.dp_out[i] = make_float2(sp0, sp1);
+    }
+    if (a.com_part) com_reduce_block(a, active ? (double)s[0] : 0.0, active ? (double)s[1] : 0.0,
+                                     active ? (double)s[2] : 0.0);
+    return;
+  }
+  if (!active) return;
+  const float dt = a.dt;
+  if (a.mode == kHeun1Fused) {
+    a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
+    a.Xt[i] = make_float4(xi[0] + s[0] * dt, xi[1] + s[1] * dt, xi[2] + s[2] * dt, vi.w);
+    if (a.P) {
+      a.dp_out[i] = make_float2(sp0, sp1);
+      a.Pt[i] = make_float2(pi.x + sp0 * dt, pi.y + sp1 * dt);
+    }
+    return;
+  }
+  // kEulerFused / kHeun2Fused: write the next state into A
+  const float4 xb = a.Bx[i];
+  float xn[3];
+  float2 pn = make_float2(0.f, 0.f);
+  if (a.mode == kEulerFused) {
+    xn[0] = xb.x + s[0] * dt; xn[1] = xb.y + s[1] * dt; xn[2] = xb.z + s[2] * dt;
+    if (a.P) { const float2 pb = a.Bp[i]; pn = make_float2(pb.x + sp0 * dt, pb.y + sp1 * dt); }
+  } else {
+    const float4 d1 = a.d1[i];
+    const float h0 = d1.x + s[0], h1 = d1.y + s[1], h2 = d1.z + s[2];
+    xn[0] = xb.x + (h0 * 0.5f) * dt; xn[1] = xb.y + (h1 * 0.5f) * dt; xn[2] = xb.z + (h2 * 0.5f) * dt;
+    if (a.P) {
+      const float2 pb = a.Bp[i], q1 = a.dp1[i];
+      const float g0 = q1.x + sp0, g1 = q1.y + sp1;
+      pn = make_float2(pb.x + (g0 * 0.5f) * dt, pb.y + (g1 * 0.5f) * dt);
+    }
+  }
+  if (D < 3) xn[2] = 0.f;
+  a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
+  if (a.PA) a.PA[i] = pn;
+  maybe_divide<D>(a, n, id_of(xb), xn, pn, a.ctr->step);
+}
+
+// Symmetric finders (…_symmetric.hpp): only j with a smaller id, +delta to the
+// evaluating cell and -delta to j for every field.  Float atomics: the
+// accumulation order is not fixed, results agree to rounding.
+template <int D, int FINDER, int FORCE>
+__global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a) {
+  const unsigned n = a.ctr->n;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 vi = a.X[i];
+  const float xi[3] = {vi.x, vi.y, vi.z};
+  const float2 pi = a.P ? a.P[i] : make_float2(0.f, 0.f);
+  const unsigned idi = id_of(vi);
+  auto one = [&](unsigned j) {
+    if (id_of(a.X[j]) >= idi) return;
+    Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+    const unsigned long long before = a.pairs ? 1ull : 0ull;
+    (void)before;
+    // pair (self = i, other = j)
+    const float4 vj = a.X[j];
+    float disp[3];
+    disp[0] = xi[0] - vj.x;
+    disp[1] = xi[1] - vj.y;
+    disp[2] = D >= 3 ? xi[2] - vj.z : 0.f;
+    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+    if (D >= 3) d2 = d2 + disp[2] * disp[2];
+    if (d2 >= fp.rc2) return;
+    if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
+    if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
+    if (a.pairs) {
+      unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(vj));
+    }
+    const float dist = sqrtf(d2);
+    const float2 pj = (FORCE == 2 && a.P) ? a.P[j] : make_float2(0.f, 0.f);
+    pair_force<D, FORCE>(fp, disp, dist, pi, pj, acc);
+    for (int d = 0; d < D; ++d) {
+      atomicAdd(&((float*)&a.d_out[i])[d], acc.x[d]);
+      atomicAdd(&((float*)&a.d_out[j])[d], -acc.x[d]);
+    }
+    if (a.dp_out) {
+      atomicAdd(&a.dp_out[i].x, acc.p[0]); atomicAdd(&a.dp_out[i].y, acc.p[1]);
+      atomicAdd(&a.dp_out[j].x, -acc.p[0]); atomicAdd(&a.dp_out[j].y, -acc.p[1]);
+    }
+  };
+  if (FINDER == 1 || FINDER == 3) {
+    int bc[3] = {0, 0, 0};
+    bin_coords_div<D>(g, xi, bc);
+    const int R = g.R;
+    const int z0 = D >= 3 ? -R : 0, z1 = D >= 3 ? R : 0;
+    for (int dz = z0; dz <= z1; ++dz) {
+      const int cz = D >= 3 ? bc[2] + dz : 0;
+      if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+      for (int dy = -R; dy <= R; ++dy) {
+        const int cy = bc[1] + dy;
+        if (cy < 0 || cy >= g.ext[1]) continue;
+        const int x0 = max(bc[0] - R, 0), x1 = min(bc[0] + R, g.ext[0] - 1);
+        int c0[3] = {x0, cy, cz}, c1[3] = {x1, cy, cz};
+        const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
+        for (unsigned j = lo; j < hi; ++j) one(j);
+      }
+    }
+  } else {
+    for (unsigned j = 0; j < n; ++j) one(j);
+  }
+}
+
+// Plain COM reduction over a delta buffer (used after the symmetric pass).
+__global__ void k_com(const float4* __restrict__ d, PassArgs a) {
+  const unsigned n = a.ctr->n;
+  double x = 0, y = 0, z = 0;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = d[i];
+    x += v.x; y += v.y; z += v.z;
+  }
+  com_reduce_block(a, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// integrator epilogues when the COM fix (or the symmetric finder) forbids
+// fusing them into the pass
+
+// heun.hpp:54-68: d1 -= c; x~ = x + d1 * dt (every field)
+__global__ void k_predict(const Counters* __restrict__ ctr, const float* __restrict__ com, float dt,
+                          const float4* __restrict__ B, const float2* __restrict__ PB, float4* __restrict__ d1,
+                          const float2* __restrict__ dp1, float4* __restrict__ Xt, float2* __restrict__ Pt) {
+  const unsigned n = ctr->n;
+  const float c0 = com[0], c1 = com[1], c2 = com[2];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 v = d1[i];
+    v.x = v.x - c0; v.y = v.y - c1; v.z = v.z - c2;
+    d1[i] = v;
+    const float4 x = B[i];
+    Xt[i] = make_float4(x.x + v.x * dt, x.y + v.y * dt, x.z + v.z * dt, x.w);
+    if (Pt) {
+      const float2 p = PB[i], q = dp1[i];
+      Pt[i] = make_float2(p.x + q.x * dt, p.y + q.y * dt);
+    }
+  }
+}
+
+// heun.hpp:78-98 (corrector) and euler.hpp:49-69 with the COM subtraction,
+// plus division.  Heun: s = d1 + (d2 - c); x += (s * 0.5) * dt.
+// Euler:  s = d1 - c; x += s * dt.
+template <int D>
+__global__ void k_finish(int heun, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
+                         const float2* __restrict__ dp2) {
+  const unsigned n = a.ctr->n;
+  const float c0 = com[0], c1 = com[1], c2 = com[2];
+  const float dt = a.dt;
+  const unsigned long long step = a.ctr->step;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 xb = a.Bx[i];
+    const float4 v1 = a.d1[i];
+    float xn[3];
+    float2 pn = make_float2(0.f, 0.f);
+    if (heun) {
+      const float4 v2 = d2[i];
+      const float e0 = v2.x - c0, e1 = v2.y - c1, e2 = v2.z - c2;
+      const float h0 = v1.x + e0, h1 = v1.y + e1, h2 = v1.z + e2;
+      xn[0] = xb.x + (h0 * 0.5f) * dt; xn[1] = xb.y + (h1 * 0.5f) * dt; xn[2] = xb.z + (h2 * 0.5f) * dt;
+      if (a.PA) {
+        const float2 pb = a.Bp[i], q1 = a.dp1[i], q2 = dp2[i];
+        const float g0 = q1.x + q2.x, g1 = q1.y + q2.y;
+        pn = make_float2(pb.x + (g0 * 0.5f) * dt, pb.y + (g1 * 0.5f) * dt);
+      }
+    } else {
+      const float e0 = v1.x - c0, e1 = v1.y - c1, e2 = v1.z - c2;
+      xn[0] = xb.x + e0 * dt; xn[1] = xb.y + e1 * dt; xn[2] = xb.z + e2 * dt;
+      if (a.PA) {
+        const float2 pb = a.Bp[i], q1 = a.dp1[i];
+        pn = make_float2(pb.x + q1.x * dt, pb.y + q1.y * dt);
+      }
+    }
+    if (D < 3) xn[2] = 0.f;
+    a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
+    if (a.PA) a.PA[i] = pn;
+    maybe_divide<D>(a, n, id_of(xb), xn, pn, step);
+  }
+}
+
+}  // namespace tecs

@@ -1,0 +1,683 @@
+// tecs_gpu.cu -- C ABI of the GB300 cell-step library (include/tecs_gpu.h).
+//
+// One tecs_sim owns the device state of one simulation and a CUDA stream.
+// tecs_sim_step queues one integrator step as a fixed kernel sequence:
+//
+//   rebuild   k_count -> k_scan_reduce -> k_scan_apply -> k_scatter -> k_sort_gather
+//   Euler     k_pass(kEulerFused)                                   [no COM]
+//             k_pass(kStore + COM) -> k_finish                      [COM]
+//   Heun      k_pass(kHeun1Fused) -> k_pass(kHeun2Fused)            [no COM]
+//             k_pass(kStore + COM) -> k_predict -> k_pass(kStore + COM) -> k_finish
+//   division  k_div_fixup -> k_div_commit
+//
+// and, by default, captures that sequence once as a CUDA graph and replays it.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tecs_gpu.h"
+#include "kernels.cuh"
+
+using namespace tecs;
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(const std::string& m) {
+  g_last_error = m;
+  return -1;
+}
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+unsigned ceil_div(unsigned long long a, unsigned b) { return (unsigned)((a + b - 1) / b); }
+
+// pack AoS float[n][dims] into float4 (x, y, z, id)
+__global__ void k_pack(const float* __restrict__ in, unsigned n, int dims, float4* __restrict__ A) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = make_float4(0.f, 0.f, 0.f, __uint_as_float(s));
+    v.x = in[(size_t)s * dims];
+    if (dims >= 2) v.y = in[(size_t)s * dims + 1];
+    if (dims >= 3) v.z = in[(size_t)s * dims + 2];
+    A[s] = v;
+  }
+}
+__global__ void k_pack4(const float4* __restrict__ in, unsigned n, float4* __restrict__ A) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = in[s];
+    v.w = __uint_as_float(s);
+    A[s] = v;
+  }
+}
+// scatter slot-ordered float4 values into cell-id order AoS float[n][dims]
+__global__ void k_unpack(const float4* __restrict__ ids, const float4* __restrict__ val, unsigned n, int dims,
+                         float* __restrict__ out) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const unsigned id = id_of(ids[s]);
+    const float4 v = val[s];
+    out[(size_t)id * dims] = v.x;
+    if (dims >= 2) out[(size_t)id * dims + 1] = v.y;
+    if (dims >= 3) out[(size_t)id * dims + 2] = v.z;
+  }
+}
+__global__ void k_unpack2(const float4* __restrict__ ids, const float2* __restrict__ val, unsigned n,
+                          float2* __restrict__ out) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    out[id_of(ids[s])] = val[s];
+}
+}  // namespace
+
+struct tecs_sim {
+  tecs_sim_desc d{};
+  GridP g{};
+  ForceP fp{};
+  cudaStream_t stream = nullptr;
+  bool binned = false;
+  float4 *A = nullptr, *B = nullptr, *Xt = nullptr, *d1 = nullptr, *d2 = nullptr;
+  float2 *PA = nullptr, *PB = nullptr, *Pt = nullptr, *dp1 = nullptr, *dp2 = nullptr;
+  unsigned *key = nullptr, *rank = nullptr, *src = nullptr, *cnt = nullptr, *off = nullptr, *part = nullptr;
+  unsigned *div_parent = nullptr, *div_slot = nullptr;
+  Counters* ctr = nullptr;
+  double* com_part = nullptr;
+  float* com = nullptr;  // [0..2] pass 1, [4..6] pass 2
+  float* stage = nullptr;
+  unsigned n_host = 0;
+  int step_count = 0;
+  bool use_graph = true;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  float gdt[2] = {0.f, 0.f};
+  int kernels[2] = {0, 0};
+  int last_kernels = 0;
+  // per-kernel CUDA events (external event-record nodes when captured in a graph)
+  bool profiling = false;
+  static constexpr int kMaxProf = 32;
+  cudaEvent_t ev[2 * kMaxProf] = {};
+  const char* prof_name[kMaxProf] = {};
+  int prof_n = 0;       // kernels marked while queueing the current step
+  int prof_last = 0;    // kernels marked in the step that was last queued
+};
+
+namespace {
+
+unsigned launch_count(const tecs_sim* s) {
+  return s->d.division_probability > 0.0 ? s->d.capacity : s->n_host;
+}
+
+using PassFn = void (*)(GridP, ForceP, PassArgs);
+
+thread_local bool g_capturing = false;
+
+int prof_mark(tecs_sim* s, int which, const char* name) {
+  if (!s->profiling) return 0;
+  const int k = s->prof_n;
+  if (k >= tecs_sim::kMaxProf) return 0;
+  cudaEvent_t& e = s->ev[2 * k + which];
+  if (!e) CK(cudaEventCreate(&e));
+  if (g_capturing) CK(cudaEventRecordWithFlags(e, s->stream, cudaEventRecordExternal));
+  else CK(cudaEventRecord(e, s->stream));
+  if (which == 1) {
+    s->prof_name[k] = name;
+    s->prof_n = k + 1;
+  }
+  return 0;
+}
+#define PROF_BEGIN(s) \
+  if (prof_mark((s), 0, nullptr)) return -1
+#define PROF_END(s, name) \
+  if (prof_mark((s), 1, (name))) return -1
+
+PassFn pass_fn(const tecs_sim* s, bool sym) {
+  const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
+#define PICK(DD, FF)                                                            \
+  if (D == DD && F == FF) {                                                     \
+    if (sym) {                                                                  \
+      if (FO == 0) return k_pass_sym<DD, FF, 0>;                                \
+      if (FO == 1) return k_pass_sym<DD, FF, 1>;                                \
+      if (DD == 3) return k_pass_sym<DD, FF, 2>;                                \
+    } else {                                                                    \
+      if (FO == 0) return k_pass<DD, FF, 0>;                                    \
+      if (FO == 1) return k_pass<DD, FF, 1>;                                    \
+      if (DD == 3) return k_pass<DD, FF, 2>;                                    \
+    }                                                                           \
+  }
+  PICK(3, 0) PICK(3, 1) PICK(3, 2) PICK(3, 3) PICK(2, 0) PICK(2, 1) PICK(2, 2) PICK(2, 3)
+#undef PICK
+  return nullptr;
+}
+
+PassArgs base_args(const tecs_sim* s, float dt) {
+  PassArgs a{};
+  a.off = s->off;
+  a.ctr = s->ctr;
+  a.dt = dt;
+  a.capacity = s->d.capacity;
+  a.div_p = s->d.division_probability;
+  a.div_offset = s->d.division_offset;
+  a.seed = s->d.seed;
+  a.div_parent = s->div_parent;
+  a.div_slot = s->div_slot;
+  a.A = s->A;
+  a.PA = s->d.has_polarity ? s->PA : nullptr;
+  return a;
+}
+
+// Rebuild B (working copy) from A: bins sorted by (bin, id), or id order for naive finders.
+int enqueue_rebuild(tecs_sim* s, int& K) {
+  const unsigned L = launch_count(s);
+  const unsigned gb = ceil_div(L ? L : 1, 256);
+  float2* PA = s->d.has_polarity ? s->PA : nullptr;
+  float2* PB = s->d.has_polarity ? s->PB : nullptr;
+  if (s->binned) {
+    const unsigned len = s->g.nbins + 1;
+    const unsigned chunks = ceil_div(len, kScanChunk);
+    PROF_BEGIN(s);
+    k_count<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+    PROF_END(s, "k_count");
+    PROF_BEGIN(s);
+    k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
+    PROF_END(s, "k_scan_reduce");
+    PROF_BEGIN(s);
+    k_scan_apply<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part, s->off);
+    PROF_END(s, "k_scan_apply");
+    PROF_BEGIN(s);
+    k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
+    PROF_END(s, "k_scatter");
+    PROF_BEGIN(s);
+    k_sort_gather<<<ceil_div(s->g.nbins, 256), 256, 0, s->stream>>>(s->g.nbins, s->off, s->src, s->A, PA, s->B,
+                                                                    PB);
+    PROF_END(s, "k_sort_gather");
+    K += 5;
+  } else {
+    PROF_BEGIN(s);
+    k_id_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, PA, s->B, PB);
+    PROF_END(s, "k_id_scatter");
+    K += 1;
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
+  const bool sym = s->d.symmetric != 0;
+  PassFn fn = pass_fn(s, sym);
+  if (!fn) return fail("unsupported finder/force/dims combination");
+  const unsigned L = launch_count(s);
+  const unsigned blocks = ceil_div(L ? L : 1, 128);
+  PROF_BEGIN(s);
+  fn<<<blocks, 128, 0, s->stream>>>(s->g, s->fp, a);
+  PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
+              : a.mode == kHeun1Fused ? "k_pass_heun1" : "k_pass_heun2");
+  K += 1;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// One integrator step (plus division), queued on the stream.
+int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
+  const bool pol = s->d.has_polarity != 0;
+  const bool sym = s->d.symmetric != 0;
+  const bool com = s->d.com_fix != 0;
+  const bool fused = !com && !sym;
+  const unsigned L = launch_count(s);
+  const unsigned gb = ceil_div(L ? L : 1, 256);
+  const int D = s->d.dims;
+  if (rebuild || !s->binned) {
+    if (enqueue_rebuild(s, K)) return -1;
+  } else {
+    CK(cudaMemcpyAsync(s->B, s->A, sizeof(float4) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
+    if (pol) CK(cudaMemcpyAsync(s->PB, s->PA, sizeof(float2) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  PassArgs a = base_args(s, dt);
+  auto store_args = [&](PassArgs& p, float4* dout, float2* dpout, int slot) {
+    p.mode = kStore;
+    p.d_out = dout;
+    p.dp_out = pol ? dpout : nullptr;
+    p.com_part = (com && !sym) ? s->com_part : nullptr;
+    p.com_out = s->com + 4 * slot;
+    p.com_slot = slot;
+  };
+  auto sym_zero = [&](float4* dout, float2* dpout) -> int {
+    if (!sym) return 0;
+    CK(cudaMemsetAsync(dout, 0, sizeof(float4) * s->d.capacity, s->stream));
+    if (pol) CK(cudaMemsetAsync(dpout, 0, sizeof(float2) * s->d.capacity, s->stream));
+    return 0;
+  };
+  auto sym_com = [&](const float4* dout, int slot) {
+    if (!(sym && com)) return;
+    PassArgs c = base_args(s, dt);
+    c.com_part = s->com_part;
+    c.com_out = s->com + 4 * slot;
+    c.com_slot = slot;
+    prof_mark(s, 0, nullptr);
+    k_com<<<ceil_div(L ? L : 1, 128), 128, 0, s->stream>>>(dout, c);
+    prof_mark(s, 1, "k_com");
+    K += 1;
+  };
+  PassArgs fin = base_args(s, dt);
+  fin.Bx = s->B;
+  fin.Bp = pol ? s->PB : nullptr;
+  fin.d1 = s->d1;
+  fin.dp1 = pol ? s->dp1 : nullptr;
+
+  if (s->d.integrator == TECS_EULER) {
+    PassArgs p = a;
+    p.X = s->B;
+    p.P = pol ? s->PB : nullptr;
+    if (fused) {
+      p.mode = kEulerFused;
+      p.Bx = s->B;
+      p.Bp = p.P;
+      if (enqueue_pass(s, p, K)) return -1;
+    } else {
+      store_args(p, s->d1, s->dp1, 0);
+      if (sym_zero(s->d1, s->dp1)) return -1;
+      if (enqueue_pass(s, p, K)) return -1;
+      sym_com(s->d1, 0);
+      PROF_BEGIN(s);
+      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(0, fin, s->com, nullptr, nullptr);
+      else k_finish<2><<<gb, 256, 0, s->stream>>>(0, fin, s->com, nullptr, nullptr);
+      PROF_END(s, "k_finish");
+      K += 1;
+    }
+  } else {
+    PassArgs p1 = a;
+    p1.X = s->B;
+    p1.P = pol ? s->PB : nullptr;
+    if (fused) {
+      p1.mode = kHeun1Fused;
+      p1.d_out = s->d1;
+      p1.dp_out = pol ? s->dp1 : nullptr;
+      p1.Xt = s->Xt;
+      p1.Pt = pol ? s->Pt : nullptr;
+      if (enqueue_pass(s, p1, K)) return -1;
+    } else {
+      store_args(p1, s->d1, s->dp1, 0);
+      if (sym_zero(s->d1, s->dp1)) return -1;
+      if (enqueue_pass(s, p1, K)) return -1;
+      sym_com(s->d1, 0);
+      PROF_BEGIN(s);
+      k_predict<<<gb, 256, 0, s->stream>>>(s->ctr, s->com, dt, s->B, pol ? s->PB : nullptr, s->d1,
+                                           pol ? s->dp1 : nullptr, s->Xt, pol ? s->Pt : nullptr);
+      PROF_END(s, "k_predict");
+      K += 1;
+    }
+    PassArgs p2 = a;
+    p2.X = s->Xt;
+    p2.P = pol ? s->Pt : nullptr;
+    if (fused) {
+      p2.mode = kHeun2Fused;
+      p2.Bx = s->B;
+      p2.Bp = pol ? s->PB : nullptr;
+      p2.d1 = s->d1;
+      p2.dp1 = pol ? s->dp1 : nullptr;
+      if (enqueue_pass(s, p2, K)) return -1;
+    } else {
+      store_args(p2, s->d2, s->dp2, 1);
+      if (sym_zero(s->d2, s->dp2)) return -1;
+      if (enqueue_pass(s, p2, K)) return -1;
+      sym_com(s->d2, 1);
+      PROF_BEGIN(s);
+      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(1, fin, s->com + 4, s->d2, pol ? s->dp2 : nullptr);
+      else k_finish<2><<<gb, 256, 0, s->stream>>>(1, fin, s->com + 4, s->d2, pol ? s->dp2 : nullptr);
+      PROF_END(s, "k_finish");
+      K += 1;
+    }
+  }
+  if (s->d.division_probability > 0.0) {
+    PROF_BEGIN(s);
+    k_div_fixup<<<32, 256, 0, s->stream>>>(s->ctr, s->d.capacity, s->div_parent, s->div_slot, s->A);
+    PROF_END(s, "k_div_fixup");
+    PROF_BEGIN(s);
+    k_div_commit<<<1, 1, 0, s->stream>>>(s->ctr, s->d.capacity);
+    PROF_END(s, "k_div_commit");
+    K += 2;
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+void drop_graphs(tecs_sim* s) {
+  for (int k = 0; k < 2; ++k) {
+    if (s->gexec[k]) cudaGraphExecDestroy(s->gexec[k]);
+    s->gexec[k] = nullptr;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tecs_last_error(void) { return g_last_error.c_str(); }
+
+int tecs_sim_desc_default(tecs_sim_desc* d) {
+  if (!d) return fail("null desc");
+  std::memset(d, 0, sizeof *d);
+  d->dims = 3;
+  d->finder = TECS_FINDER_BINNED_GABRIEL;
+  d->cutoff = 1.0f;
+  d->gabriel_coefficient = 0.8f;
+  for (int k = 0; k < 3; ++k) { d->min_bounds[k] = -20.f; d->max_bounds[k] = 20.f; }
+  d->bin_size_scale = 1.0f;
+  d->integrator = TECS_HEUN;
+  d->force = TECS_FORCE_SPRING2R;
+  d->k_rep = 2.0f; d->r_rep = 0.7f; d->k_adh = 0.5f; d->r_adh = 0.8f;
+  d->division_offset = 0.25f;
+  d->seed = 2807;
+  return 0;
+}
+
+int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
+  if (!desc || !out) return fail("null argument");
+  *out = nullptr;
+  if (desc->dims != 2 && desc->dims != 3) return fail("dims must be 2 or 3");
+  if (desc->capacity == 0) return fail("capacity must be > 0");
+  if (desc->finder < 0 || desc->finder > 3) return fail("unknown finder");
+  if (desc->force < 0 || desc->force > 2) return fail("unknown force");
+  if (desc->force == TECS_FORCE_POLARITY && (desc->dims != 3 || !desc->has_polarity))
+    return fail("the polarity force needs dims 3 and a polarity field");
+  if (!(desc->cutoff > 0.f) || !(desc->bin_size_scale > 0.f)) return fail("cutoff and bin_size_scale must be > 0");
+  tecs_sim* s = new tecs_sim();
+  s->d = *desc;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    delete s;
+    return fail("no CUDA device");
+  }
+  if (cudaSetDevice(desc->device) != cudaSuccess) {
+    delete s;
+    return fail("cudaSetDevice failed");
+  }
+  // grid: binned_gabriel.hpp:28-42, grid.hpp:201-215
+  GridP& g = s->g;
+  g.bin_size = desc->bin_size_scale * desc->cutoff;
+  g.inv_bin = 1.0f / g.bin_size;
+  g.R = (int)std::ceil(desc->cutoff * g.inv_bin);
+  unsigned long long nb = 1;
+  for (int k = 0; k < 3; ++k) { g.mn[k] = 0.f; g.ext[k] = 1; }
+  for (int k = 0; k < desc->dims; ++k) {
+    g.mn[k] = desc->min_bounds[k];
+    g.ext[k] = (int)std::ceil((desc->max_bounds[k] - desc->min_bounds[k]) / g.bin_size);
+    if (g.ext[k] < 1) { delete s; return fail("max_bounds must exceed min_bounds"); }
+    nb *= (unsigned long long)g.ext[k];
+  }
+  if (nb > (1ull << 31)) { delete s; return fail("bin grid too large"); }
+  g.nbins = (unsigned)nb;
+  ForceP& f = s->fp;
+  f.force = desc->force;
+  f.k_rep = desc->k_rep; f.r_rep = desc->r_rep; f.k_adh = desc->k_adh; f.r_adh = desc->r_adh; f.k_pol = desc->k_pol;
+  f.rc2 = desc->cutoff * desc->cutoff;
+  f.gab_factor = desc->gabriel_coefficient * desc->gabriel_coefficient * 0.25f;
+  f.gab_csq = desc->gabriel_coefficient * desc->gabriel_coefficient;
+  s->binned = desc->finder == TECS_FINDER_BINNED_ALL_PAIRS || desc->finder == TECS_FINDER_BINNED_GABRIEL;
+
+  const size_t cap = desc->capacity;
+  auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
+  bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && alloc((void**)&s->A, cap * 16) && alloc((void**)&s->B, cap * 16) && alloc((void**)&s->Xt, cap * 16) &&
+       alloc((void**)&s->d1, cap * 16) && alloc((void**)&s->d2, cap * 16);
+  if (desc->has_polarity)
+    ok = ok && alloc((void**)&s->PA, cap * 8) && alloc((void**)&s->PB, cap * 8) && alloc((void**)&s->Pt, cap * 8) &&
+         alloc((void**)&s->dp1, cap * 8) && alloc((void**)&s->dp2, cap * 8);
+  ok = ok && alloc((void**)&s->key, cap * 4) && alloc((void**)&s->rank, cap * 4) && alloc((void**)&s->src, cap * 4);
+  ok = ok && alloc((void**)&s->div_parent, cap * 4) && alloc((void**)&s->div_slot, cap * 4);
+  if (s->binned) {
+    const size_t len = (size_t)g.nbins + 1;
+    ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
+         alloc((void**)&s->part, (size_t)ceil_div(len, kScanChunk) * 4);
+  }
+  const size_t pass_blocks = ceil_div(cap, 128);
+  ok = ok && alloc((void**)&s->ctr, sizeof(Counters)) && alloc((void**)&s->com_part, pass_blocks * 3 * 8) &&
+       alloc((void**)&s->com, 8 * 4) && alloc((void**)&s->stage, cap * 4 * 4);
+  if (ok && s->cnt) ok = cudaMemset(s->cnt, 0, ((size_t)g.nbins + 1) * 4) == cudaSuccess;
+  if (ok) ok = cudaMemset(s->ctr, 0, sizeof(Counters)) == cudaSuccess && cudaMemset(s->com, 0, 32) == cudaSuccess;
+  if (!ok) {
+    std::string m = std::string("device allocation failed: ") + cudaGetErrorString(cudaGetLastError());
+    tecs_sim_destroy(s);
+    return fail(m);
+  }
+  *out = s;
+  return 0;
+}
+
+int tecs_sim_destroy(tecs_sim* s) {
+  if (!s) return 0;
+  cudaSetDevice(s->d.device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  drop_graphs(s);
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e);
+  void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
+                  s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return 0;
+}
+
+static int upload_common(tecs_sim* s, unsigned n) {
+  const size_t cap = s->d.capacity;
+  CK(cudaMemsetAsync(s->d1, 0, cap * 16, s->stream));
+  CK(cudaMemsetAsync(s->d2, 0, cap * 16, s->stream));
+  if (s->d.has_polarity) {
+    CK(cudaMemsetAsync(s->dp1, 0, cap * 8, s->stream));
+    CK(cudaMemsetAsync(s->dp2, 0, cap * 8, s->stream));
+  }
+  Counters c{};
+  c.n = n;
+  CK(cudaMemcpyAsync(s->ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_host = n;
+  s->step_count = 0;
+  drop_graphs(s);
+  return 0;
+}
+
+int tecs_sim_upload(tecs_sim* s, const float* pos, const float* pol, unsigned n) {
+  if (!s || (!pos && n)) return fail("null argument");
+  if (n > s->d.capacity) return fail("agent count exceeds capacity");
+  if (s->d.has_polarity && n && !pol) return fail("simulation has a polarity field: polarity required");
+  CK(cudaSetDevice(s->d.device));
+  CK(cudaStreamSynchronize(s->stream));
+  const int D = s->d.dims;
+  if (n) {
+    CK(cudaMemcpyAsync(s->stage, pos, (size_t)n * D * 4, cudaMemcpyHostToDevice, s->stream));
+    k_pack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->stage, n, D, s->A);
+    CK(cudaGetLastError());
+    if (s->d.has_polarity) CK(cudaMemcpyAsync(s->PA, pol, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
+  }
+  return upload_common(s, n);
+}
+
+int tecs_sim_upload_device(tecs_sim* s, const float* dpos, const float* dpol, unsigned n) {
+  if (!s || (!dpos && n)) return fail("null argument");
+  if (n > s->d.capacity) return fail("agent count exceeds capacity");
+  if (s->d.has_polarity && n && !dpol) return fail("simulation has a polarity field: polarity required");
+  CK(cudaSetDevice(s->d.device));
+  CK(cudaStreamSynchronize(s->stream));
+  const int D = s->d.dims;
+  if (n) {
+    k_pack<<<ceil_div(n, 256), 256, 0, s->stream>>>(dpos, n, D, s->A);
+    CK(cudaGetLastError());
+    if (s->d.has_polarity) CK(cudaMemcpyAsync(s->PA, dpol, (size_t)n * 8, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  return upload_common(s, n);
+}
+
+int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
+  if (!s) return fail("null simulation");
+  if (n_steps < 0) return fail("negative step count");
+  CK(cudaSetDevice(s->d.device));
+  const float fdt = (float)dt;  // VectorN * Scalar narrows dt (vector.hpp:264-267)
+  for (int it = 0; it < n_steps; ++it) {
+    // binned_gabriel.hpp:83-89: rebuild when step_count == 0 || step_count >= rebuild_every_n;
+    // division resets the counter every step (set_agent_count, :61-64)
+    const bool rebuild = s->step_count == 0 || s->step_count >= s->d.rebuild_every_n;
+    const int gk = rebuild ? 0 : 1;
+    if (rebuild) s->step_count = 0;
+    s->step_count++;
+    if (s->d.division_probability > 0.0) s->step_count = 0;
+    if (!s->use_graph) {
+      int K = 0;
+      s->prof_n = 0;
+      if (enqueue_step(s, fdt, rebuild, K)) return -1;
+      s->last_kernels = K;
+      s->prof_last = s->prof_n;
+      continue;
+    }
+    if (!s->gexec[gk] || s->gdt[gk] != fdt) {
+      if (s->gexec[gk]) { cudaGraphExecDestroy(s->gexec[gk]); s->gexec[gk] = nullptr; }
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      int K = 0;
+      s->prof_n = 0;
+      g_capturing = true;
+      int rc = enqueue_step(s, fdt, rebuild, K);
+      g_capturing = false;
+      s->prof_last = s->prof_n;
+      cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+      if (rc) return -1;
+      if (e != cudaSuccess) return fail(std::string("graph capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&s->gexec[gk], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return fail(std::string("graph instantiate: ") + cudaGetErrorString(e));
+      s->gdt[gk] = fdt;
+      s->kernels[gk] = K;
+    }
+    CK(cudaGraphLaunch(s->gexec[gk], s->stream));
+    s->last_kernels = s->kernels[gk];
+  }
+  return 0;
+}
+
+int tecs_sim_synchronize(tecs_sim* s) {
+  if (!s) return fail("null simulation");
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+int tecs_sim_count(tecs_sim* s, unsigned* n) {
+  if (!s || !n) return fail("null argument");
+  Counters c;
+  CK(cudaMemcpyAsync(&c, s->ctr, sizeof c, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (c.error & 1u) return fail("capacity exceeded by cell division");
+  *n = c.n;
+  return 0;
+}
+
+int tecs_sim_download(tecs_sim* s, float* pos, float* pol, unsigned* n_out) {
+  if (!s || !pos) return fail("null argument");
+  unsigned n = 0;
+  if (tecs_sim_count(s, &n)) return -1;
+  const int D = s->d.dims;
+  if (n) {
+    // Xt is free between steps; unpack into it in id order
+    k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->A, n, D, (float*)s->Xt);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(pos, s->Xt, (size_t)n * D * 4, cudaMemcpyDeviceToHost, s->stream));
+    if (pol && s->d.has_polarity) {
+      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->PA, n, s->Pt);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(pol, s->Pt, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  if (n_out) *n_out = n;
+  return 0;
+}
+
+int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, size_t pair_cap, size_t* n_pairs) {
+  if (!s) return fail("null simulation");
+  CK(cudaSetDevice(s->d.device));
+  unsigned n = 0;
+  if (tecs_sim_count(s, &n)) return -1;
+  const bool pol = s->d.has_polarity != 0;
+  int K = 0;
+  if (enqueue_rebuild(s, K)) return -1;
+  uint2* dpairs = nullptr;
+  if (pairs && pair_cap) CK(cudaMalloc(&dpairs, pair_cap * sizeof(uint2)));
+  CK(cudaMemsetAsync(&s->ctr->pair_count, 0, 8, s->stream));
+  if (s->d.symmetric) {
+    CK(cudaMemsetAsync(s->d1, 0, sizeof(float4) * s->d.capacity, s->stream));
+    if (pol) CK(cudaMemsetAsync(s->dp1, 0, sizeof(float2) * s->d.capacity, s->stream));
+  }
+  PassArgs a = base_args(s, 0.f);
+  a.X = s->B;
+  a.P = pol ? s->PB : nullptr;
+  a.mode = kStore;
+  a.d_out = s->d1;
+  a.dp_out = pol ? s->dp1 : nullptr;
+  a.pairs = dpairs;
+  a.pair_cap = dpairs ? pair_cap : 0;
+  int rc = enqueue_pass(s, a, K);
+  if (rc == 0 && n) {
+    if (dpos) {
+      k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->d1, n, s->d.dims, (float*)s->Xt);
+      cudaMemcpyAsync(dpos, s->Xt, (size_t)n * s->d.dims * 4, cudaMemcpyDeviceToHost, s->stream);
+    }
+    if (dpol && pol) {
+      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->dp1, n, s->Pt);
+      cudaMemcpyAsync(dpol, s->Pt, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream);
+    }
+  }
+  unsigned long long cnt = 0;
+  cudaMemcpyAsync(&cnt, &s->ctr->pair_count, 8, cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (rc == 0 && e == cudaSuccess && dpairs) {
+    size_t m = cnt < pair_cap ? (size_t)cnt : pair_cap;
+    e = cudaMemcpy(pairs, dpairs, m * sizeof(uint2), cudaMemcpyDeviceToHost);
+  }
+  if (dpairs) cudaFree(dpairs);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(std::string("evaluate: ") + cudaGetErrorString(e));
+  if (n_pairs) *n_pairs = (size_t)cnt;
+  return 0;
+}
+
+void* tecs_sim_stream(tecs_sim* s) { return s ? (void*)s->stream : nullptr; }
+
+int tecs_sim_set_graph(tecs_sim* s, int enable) {
+  if (!s) return fail("null simulation");
+  s->use_graph = enable != 0;
+  if (!s->use_graph) drop_graphs(s);
+  return 0;
+}
+
+int tecs_sim_set_profiling(tecs_sim* s, int enable) {
+  if (!s) return fail("null simulation");
+  if ((enable != 0) != s->profiling) drop_graphs(s);
+  s->profiling = enable != 0;
+  return 0;
+}
+
+int tecs_sim_last_step_profile(tecs_sim* s, float* ms, int capacity, int* count) {
+  if (!s || !count) return fail("null argument");
+  if (!s->profiling) return fail("profiling is off");
+  CK(cudaStreamSynchronize(s->stream));
+  const int k = s->prof_last;
+  *count = k;
+  for (int i = 0; i < k && i < capacity; ++i) CK(cudaEventElapsedTime(&ms[i], s->ev[2 * i], s->ev[2 * i + 1]));
+  return 0;
+}
+
+const char* tecs_sim_profile_name(tecs_sim* s, int index) {
+  if (!s || index < 0 || index >= s->prof_last) return nullptr;
+  return s->prof_name[index];
+}
+
+int tecs_sim_kernels_per_step(tecs_sim* s, int* kernels) {
+  if (!s || !kernels) return fail("null argument");
+  *kernels = s->last_kernels;
+  return 0;
+}
+
+}  // extern "C"
