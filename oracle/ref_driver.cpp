@@ -1,0 +1,250 @@
+// ref_driver.cpp -- runs the TECS reference's own headers (compiled unmodified
+// against oracle/kokkos_shim) on a raw input file and writes raw outputs.
+// Used only to generate the golden vectors that pin the oracle
+// (tests/golden/make_golden.py); never part of the product.
+//
+//   ref_driver <scenario> <in.bin> <out_prefix> <steps> <dt>
+//
+// in.bin: uint32 n, uint32 dims, uint32 has_polarity, float32 params[16],
+//         float32 positions[n*dims], float32 polarity[n*2] (if present)
+// params: cutoff, gabriel_c, min_x, min_y, min_z, max_x, max_y, max_z,
+//         k_rep, r_rep, k_adh, r_adh, k_pol, capacity, bin_size_scale, spare
+// outputs: <out>.pairs (uint32 pairs, evaluation order), <out>.dpos, <out>.dpol
+//          (one full-step pass from a fresh finder), <out>.pos / <out>.pol
+//          (state after <steps> take_step calls).
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+// the reference's umbrella include order (include/tecs.hpp:1-57) minus the CLI helper
+#include <utils/utils.hpp>
+#include <types/vector.hpp>
+#include <types/polarity.hpp>
+#include <types/plane.hpp>
+#include <types/link.hpp>
+#include <types/view.hpp>
+#include <types/device_var.hpp>
+#include <integrators/base.hpp>
+#include <forces/detail.hpp>
+#include <forces/kernel_fuser.hpp>
+#include <simulation.hpp>
+#include <pair_finders/binned_all_pairs.hpp>
+#include <pair_finders/binned_all_pairs_symmetric.hpp>
+#include <pair_finders/binned_gabriel.hpp>
+#include <pair_finders/binned_gabriel_symmetric.hpp>
+#include <pair_finders/naive_all_pairs.hpp>
+#include <pair_finders/naive_all_pairs_symmetric.hpp>
+#include <pair_finders/naive_gabriel.hpp>
+#include <pair_finders/naive_gabriel_symmetric.hpp>
+#include <integrators/euler.hpp>
+#include <integrators/heun.hpp>
+#include <com_fixers/com_fixers.hpp>
+#include <io/dummy.hpp>
+
+struct Input {
+  unsigned n = 0, dims = 0, has_pol = 0;
+  float prm[16] = {};
+  std::vector<float> x, p;
+};
+
+static Input read_input(const char* path) {
+  Input in;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) { std::perror(path); std::exit(2); }
+  unsigned hdr[3];
+  if (std::fread(hdr, 4, 3, f) != 3) std::exit(2);
+  in.n = hdr[0]; in.dims = hdr[1]; in.has_pol = hdr[2];
+  if (std::fread(in.prm, 4, 16, f) != 16) std::exit(2);
+  in.x.resize((size_t)in.n * in.dims);
+  if (in.n && std::fread(in.x.data(), 4, in.x.size(), f) != in.x.size()) std::exit(2);
+  if (in.has_pol) {
+    in.p.resize((size_t)in.n * 2);
+    if (in.n && std::fread(in.p.data(), 4, in.p.size(), f) != in.p.size()) std::exit(2);
+  }
+  std::fclose(f);
+  return in;
+}
+
+static void write_raw(const std::string& path, const void* data, size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { std::perror(path.c_str()); std::exit(2); }
+  if (bytes) std::fwrite(data, 1, bytes, f);
+  std::fclose(f);
+}
+
+// --- force laws, written as user PAIRWISE_FORCE lambdas -------------------
+// spring2r: F(d) = k_rep*max(r_rep-d,0) - k_adh*max(d-r_adh,0), zero at d == 0
+#define TECS_DRIVER_SPRING                                                                              \
+  if (capture) {                                                                                        \
+    const int slot = Kokkos::atomic_fetch_add(counter.data(), 1);                                       \
+    pairs(2 * slot) = i;                                                                                \
+    pairs(2 * slot + 1) = j;                                                                            \
+  }                                                                                                     \
+  if (distance != Scalar(0)) {                                                                          \
+    const Scalar F = k_rep * Kokkos::fmax(r_rep - distance, Scalar(0)) -                                \
+                     k_adh * Kokkos::fmax(distance - r_adh, Scalar(0));                                 \
+    ctx.position.delta += displacement * F / distance;                                                 \
+  }
+
+// polarity: spring2r + k_pol * (bending_force + bidirectional_polarization_force)
+#define TECS_DRIVER_POLARITY                                                                            \
+  TECS_DRIVER_SPRING                                                                                    \
+  auto bend = ctx.polarity.self.bending_force(displacement, ctx.polarity.other, distance);             \
+  ctx.position.delta += bend.vector * k_pol;                                                            \
+  ctx.polarity.delta += bend.polarity * k_pol;                                                          \
+  ctx.polarity.delta += ctx.polarity.self.bidirectional_polarization_force(ctx.polarity.other) * k_pol;
+
+// --- one scenario per (finder, integrator, com fixer, fields, dims) -------
+#define TECS_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER, DIMS, POLAR)                                    \
+  namespace NAME {                                                                                      \
+  CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
+                                       CONFIG_COM_FIXER(COMFIXER) CONFIG_DIMENSIONS(DIMS)                \
+                                           CONFIG_WRITER(tecs::io::Dummy) TECS_FIELDS_##POLAR)           \
+  EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)                                                            \
+  static int run(const Input& in, const std::string& out, int steps, double dt) {                       \
+    return tecs_driver_run<Config, PairFinder, Scalar, Vector, Random, PairwiseForceFields, POLAR>(     \
+        in, out, steps, dt);                                                                            \
+  }                                                                                                     \
+  }
+
+#define TECS_FIELDS_0 CONFIG_FIELDS((Vector, position))
+#define TECS_FIELDS_1 CONFIG_FIELDS((Vector, position), (Polarity, polarity))
+
+template <class Sim, class Settings>
+static void fill_settings(Settings& s, const Input& in) {
+  s.cutoff_distance = in.prm[0];
+  s.capacity = (unsigned)in.prm[13] > in.n ? (unsigned)in.prm[13] : in.n;
+}
+
+template <class PFS>
+static void fill_finder_settings(PFS& pfs, const Input& in) {
+  if constexpr (requires { pfs.gabriel_coefficient; }) pfs.gabriel_coefficient = in.prm[1];
+  if constexpr (requires { pfs.min_bounds; }) {
+    for (unsigned d = 0; d < in.dims; ++d) {
+      pfs.min_bounds[d] = in.prm[2 + d];
+      pfs.max_bounds[d] = in.prm[5 + d];
+    }
+  }
+  if constexpr (requires { pfs.bin_size_scale; }) pfs.bin_size_scale = in.prm[14];
+}
+
+template <class Config, class PairFinder, class Scalar, class Vector, class Random, class PairwiseForceFields,
+          int POLAR>
+static int tecs_driver_run(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11], k_pol = in.prm[12];
+  (void)k_pol;
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2 * (size_t)n * (n < 4096 ? n : 64) + 2);
+  DeviceVar<int> counter = 0;
+  bool capture = true;
+
+  auto make_force = [&]() {
+    if constexpr (POLAR) {
+      return PAIRWISE_FORCE(TECS_DRIVER_POLARITY)();
+    } else {
+      return PAIRWISE_FORCE(TECS_DRIVER_SPRING)();
+    }
+  };
+
+  // (1) one full-step pass with a fresh finder: PairFinder::evaluate_force
+  {
+    typename PairFinder::Settings pfs{};
+    fill_finder_settings(pfs, in);
+    PairFinder finder(n, in.prm[0], pfs);
+    using PV = Kokkos::View<Vector*>;
+    PV x("position", n), dx("position", n), vold("old_velocities", n);
+    for (unsigned i = 0; i < n; ++i)
+      for (unsigned d = 0; d < in.dims; ++d) x(i)[d] = in.x[(size_t)i * in.dims + d];
+    Kokkos::Random_XorShift64_Pool<> pool(2807);
+    auto force = make_force();
+    if constexpr (POLAR) {
+      using PolV = Kokkos::View<Polarity_<Scalar>*>;
+      PolV p("polarity", n), dp("polarity", n);
+      for (unsigned i = 0; i < n; ++i) { p(i)[0] = in.p[2 * i]; p(i)[1] = in.p[2 * i + 1]; }
+      detail::ViewPack<PV, PolV> ip(x, p), op(dx, dp);
+      finder.template evaluate_force<decltype(pool), decltype(force.force), PairwiseForceFields>(ip, op, vold, pool,
+                                                                                                force.force, true);
+      write_raw(out + ".dpol", dp.data(), (size_t)n * 8);
+    } else {
+      detail::ViewPack<PV> ip(x), op(dx);
+      finder.template evaluate_force<decltype(pool), decltype(force.force), PairwiseForceFields>(ip, op, vold, pool,
+                                                                                                force.force, true);
+    }
+    std::vector<float> flat((size_t)n * in.dims);
+    for (unsigned i = 0; i < n; ++i)
+      for (unsigned d = 0; d < in.dims; ++d) flat[(size_t)i * in.dims + d] = dx(i)[d];
+    write_raw(out + ".dpos", flat.data(), flat.size() * 4);
+    const int np = counter;
+    write_raw(out + ".pairs", pairs.data(), (size_t)np * 8);
+  }
+
+  // (2) Simulation::take_step, steps times
+  capture = false;
+  {
+    typename Simulation<Config>::Settings st(n, "unused");
+    fill_settings<Simulation<Config>>(st, in);
+    fill_finder_settings(st.pair_finder_settings, in);
+    Simulation<Config> sim(st);
+    auto& pos = sim.template get_view<FIELD(Vector, position)>();
+    for (unsigned i = 0; i < n; ++i)
+      for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+    if constexpr (POLAR) {
+      auto& pol = sim.template get_view<FIELD(Polarity_<Scalar>, polarity)>();
+      for (unsigned i = 0; i < n; ++i) { pol(i)[0] = in.p[2 * i]; pol(i)[1] = in.p[2 * i + 1]; }
+    }
+    auto force = make_force();
+    for (int s = 0; s < steps; ++s) sim.take_step(dt, force);
+    std::vector<float> flat((size_t)n * in.dims);
+    for (unsigned i = 0; i < n; ++i)
+      for (unsigned d = 0; d < in.dims; ++d) flat[(size_t)i * in.dims + d] = pos(i)[d];
+    write_raw(out + ".pos", flat.data(), flat.size() * 4);
+    if constexpr (POLAR) {
+      auto& pol = sim.template get_view<FIELD(Polarity_<Scalar>, polarity)>();
+      std::vector<float> pf((size_t)n * 2);
+      for (unsigned i = 0; i < n; ++i) { pf[2 * i] = pol(i)[0]; pf[2 * i + 1] = pol(i)[1]; }
+      write_raw(out + ".pol", pf.data(), pf.size() * 4);
+    }
+  }
+  return 0;
+}
+
+using namespace tecs;
+TECS_SCENARIO(ba_euler_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(ba_heun_com_3, pair_finders::BinnedAllPairs, integrators::Heun, com_fixers::GlobalComFixer, 3, 0)
+TECS_SCENARIO(bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(bg_heun_com_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::GlobalComFixer, 3, 0)
+TECS_SCENARIO(bg_euler_com_3, pair_finders::BinnedGabriel, integrators::Euler, com_fixers::GlobalComFixer, 3, 0)
+TECS_SCENARIO(na_heun_3, pair_finders::NaiveAllPairs, integrators::Heun, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(ng_heun_3, pair_finders::NaiveGabriel, integrators::Heun, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(bgs_euler_com_3, pair_finders::BinnedGabrielSymmetric, integrators::Euler, com_fixers::GlobalComFixer,
+              3, 0)
+TECS_SCENARIO(bas_heun_3, pair_finders::BinnedAllPairsSymmetric, integrators::Heun, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(ngs_euler_3, pair_finders::NaiveGabrielSymmetric, integrators::Euler, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(bg_heun_pol_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 3, 1)
+TECS_SCENARIO(ng_euler_2, pair_finders::NaiveGabriel, integrators::Euler, com_fixers::NoComFixer, 2, 0)
+TECS_SCENARIO(bg_heun_2, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 2, 0)
+
+int main(int argc, char** argv) {
+  if (argc < 6) {
+    std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
+    return 2;
+  }
+  Kokkos::initialize();
+  const std::string sc = argv[1];
+  const Input in = read_input(argv[2]);
+  const std::string out = argv[3];
+  const int steps = std::atoi(argv[4]);
+  const double dt = std::atof(argv[5]);
+  int rc = 3;
+#define DISPATCH(NAME) \
+  if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
+  DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
+  DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
+  DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2)
+#undef DISPATCH
+  if (rc == 3) std::fprintf(stderr, "unknown scenario %s\n", sc.c_str());
+  return rc;
+}

@@ -1,0 +1,167 @@
+#!/usr/bin/env python
+"""Generate the golden fixtures that pin the oracle to the TECS reference.
+
+Runs oracle/_ref/ref_driver -- the reference's own headers compiled unmodified
+against oracle/kokkos_shim (recipe: oracle/Makefile) -- on seeded inputs and
+stores inputs and outputs as compressed .npz files next to this script:
+
+  x0, p0          initial positions / polarities
+  prm             cutoff, gabriel_c, min[3], max[3], k_rep, r_rep, k_adh, r_adh, k_pol, capacity, bin_scale
+  pairs           directed (self, other) pairs of one full-step pass, in the reference's evaluation order
+  dpos, dpol      per-cell deltas of that pass
+  pos, pol        state after `steps` Simulation::take_step(dt) calls
+
+Needs the reference sources (default /root/reference, override with
+TECS_REFERENCE); run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from tecs_gb300 import workloads as wl  # noqa: E402
+
+REF = Path(os.environ.get("TECS_REFERENCE", "/root/reference"))
+DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
+
+# name: (driver scenario, oracle finder, symmetric, integrator, com, dims, polarity)
+SCENARIOS = {
+    "c1_small_euler": ("ba_euler_3", 1, 0, 0, 0, 3, 0),
+    "bg_heun": ("bg_heun_3", 3, 0, 1, 0, 3, 0),
+    "bg_heun_com": ("bg_heun_com_3", 3, 0, 1, 1, 3, 0),
+    "bg_heun_clamped": ("bg_heun_3", 3, 0, 1, 0, 3, 0),
+    "ba_heun_com": ("ba_heun_com_3", 1, 0, 1, 1, 3, 0),
+    "bg_euler_com": ("bg_euler_com_3", 3, 0, 0, 1, 3, 0),
+    "na_heun": ("na_heun_3", 0, 0, 1, 0, 3, 0),
+    "ng_heun": ("ng_heun_3", 2, 0, 1, 0, 3, 0),
+    "bgs_euler_com": ("bgs_euler_com_3", 3, 1, 0, 1, 3, 0),
+    "bas_heun": ("bas_heun_3", 1, 1, 1, 0, 3, 0),
+    "ngs_euler": ("ngs_euler_3", 2, 1, 0, 0, 3, 0),
+    "bg_heun_polarity": ("bg_heun_pol_3", 3, 0, 1, 0, 3, 1),
+    "ng_euler_2d_points11": ("ng_euler_2", 2, 0, 0, 0, 2, 0),
+    "bg_heun_2d": ("bg_heun_2", 3, 0, 1, 0, 2, 0),
+}
+
+
+def main_cpp_points():
+    """The 11-point 2-D table of the reference's main.cpp (its Gabriel demo fixture)."""
+    text = (REF / "main.cpp").read_text()
+    block = text[text.index("pos[n_cells][2]"):]
+    block = block[: block.index("};")]
+    pts = re.findall(r"\{\s*(-?\d+\.\d+),\s*(-?\d+\.\d+)\s*\}", block)
+    return np.array(pts, dtype=np.float32)
+
+
+def inputs(name):
+    """(x0, p0, prm, steps, dt) for one scenario."""
+    prm = np.zeros(16, np.float32)
+    prm[0], prm[1] = 1.0, 0.8
+    prm[8:13] = (2.0, 0.7, 0.5, 0.8, 0.0)
+    prm[14] = 1.0
+    p0 = None
+    if name == "c1_small_euler":
+        x = wl.ball(1000, 0, radius=5.0)
+        mn, mx, steps, dt = (-6,) * 3, (6,) * 3, 1000, 0.1
+    elif name in ("bg_heun", "bg_heun_com"):
+        x = wl.ball(3000, 1)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 20, 0.05
+        if name == "bg_heun_com":
+            prm[13] = 3150
+    elif name == "bg_heun_clamped":
+        # the default +-20 grid around a ball of radius 26: outside cells land in edge bins
+        x = wl.ball(2000, 12, radius=26.0)
+        mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 5, 0.05
+    elif name in ("ba_heun_com", "bg_euler_com", "bgs_euler_com", "bas_heun"):
+        seed = {"ba_heun_com": 3, "bg_euler_com": 4, "bgs_euler_com": 7, "bas_heun": 8}[name]
+        x = wl.ball(2000, seed)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = (10, 0.05) if name in ("ba_heun_com", "bg_euler_com") else (5, 0.05)
+        if name in ("ba_heun_com", "bgs_euler_com"):
+            prm[13] = 2100
+    elif name == "na_heun":
+        x = wl.ball(600, 5)
+        mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 5, 0.05
+    elif name in ("ng_heun", "ngs_euler"):
+        x = wl.ball(400 if name == "ng_heun" else 300, 6 if name == "ng_heun" else 9)
+        mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
+    elif name == "bg_heun_polarity":
+        x = wl.sheet(2000, 10)
+        p0 = wl.outward_polarity(x, 10)
+        mn, mx = wl.bounds_for(x)
+        prm[12] = 0.2
+        steps, dt = 5, 0.05
+    elif name == "ng_euler_2d_points11":
+        x = main_cpp_points()
+        prm[0] = 2.5
+        mn, mx, steps, dt = (-20, -20, 0), (20, 20, 0), 3, 0.01
+    elif name == "bg_heun_2d":
+        x = np.ascontiguousarray(wl.ball(1500, 13)[:, :2] * 0.4)
+        m = float(np.ceil(np.abs(x).max() + 2))
+        mn, mx, steps, dt = (-m, -m, 0), (m, m, 0), 10, 0.05
+    else:
+        raise KeyError(name)
+    prm[2:5] = mn
+    prm[5:8] = mx
+    return np.ascontiguousarray(x, np.float32), p0, prm, steps, dt
+
+
+def run(name):
+    scen, *_rest, dims, pol = SCENARIOS[name]
+    x, p0, prm, steps, dt = inputs(name)
+    with tempfile.TemporaryDirectory() as td:
+        inp = Path(td) / "in.bin"
+        with open(inp, "wb") as f:
+            np.array([len(x), dims, 1 if p0 is not None else 0], np.uint32).tofile(f)
+            prm.tofile(f)
+            x.tofile(f)
+            if p0 is not None:
+                p0.astype(np.float32).tofile(f)
+        out = Path(td) / "out"
+        subprocess.run([str(DRIVER), scen, str(inp), str(out), str(steps), repr(dt)], check=True)
+        res = {
+            "x0": x, "prm": prm, "steps": np.int64(steps), "dt": np.float64(dt),
+            "pairs": np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2),
+            "dpos": np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims),
+            "pos": np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims),
+        }
+        if p0 is not None:
+            res["p0"] = p0
+            res["dpol"] = np.fromfile(f"{out}.dpol", np.float32).reshape(-1, 2)
+            res["pol"] = np.fromfile(f"{out}.pol", np.float32).reshape(-1, 2)
+    np.savez_compressed(HERE / f"{name}.npz", **res)
+    return res
+
+
+def main():
+    if not REF.exists():
+        sys.exit(f"reference sources not found at {REF}")
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    names = sys.argv[1:] or list(SCENARIOS)
+    manifest = {}
+    for name in names:
+        r = run(name)
+        manifest[name] = {"scenario": SCENARIOS[name][0], "cells": int(len(r["x0"])), "pairs": int(len(r["pairs"])),
+                          "steps": int(r["steps"]), "dt": float(r["dt"])}
+        print(name, manifest[name])
+    old = {}
+    mf = HERE / "manifest.json"
+    if mf.exists():
+        old = json.loads(mf.read_text())
+    old.update(manifest)
+    mf.write_text(json.dumps(old, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main()

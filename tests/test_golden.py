@@ -1,0 +1,96 @@
+"""Pin the oracle (C restatement) to the TECS reference.
+
+The fixtures in tests/golden/ were produced by the reference's own headers,
+compiled unmodified against oracle/kokkos_shim (tests/golden/make_golden.py).
+The restatement must reproduce them bit for bit: the directed pair lists in the
+reference's evaluation order, the per-cell deltas of one full-step pass, and
+the state after the recorded number of Simulation::take_step calls.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+MANIFEST = json.loads((GOLDEN / "manifest.json").read_text())
+
+# name -> (finder, symmetric, integrator, com, dims, polarity), mirrors make_golden.SCENARIOS
+KIND = {
+    "c1_small_euler": (1, 0, 0, 0, 3, 0),
+    "bg_heun": (3, 0, 1, 0, 3, 0),
+    "bg_heun_com": (3, 0, 1, 1, 3, 0),
+    "bg_heun_clamped": (3, 0, 1, 0, 3, 0),
+    "ba_heun_com": (1, 0, 1, 1, 3, 0),
+    "bg_euler_com": (3, 0, 0, 1, 3, 0),
+    "na_heun": (0, 0, 1, 0, 3, 0),
+    "ng_heun": (2, 0, 1, 0, 3, 0),
+    "bgs_euler_com": (3, 1, 0, 1, 3, 0),
+    "bas_heun": (1, 1, 1, 0, 3, 0),
+    "ngs_euler": (2, 1, 0, 0, 3, 0),
+    "bg_heun_polarity": (3, 0, 1, 0, 3, 1),
+    "ng_euler_2d_points11": (2, 0, 0, 0, 2, 0),
+    "bg_heun_2d": (3, 0, 1, 0, 2, 0),
+}
+
+
+def load(name):
+    return dict(np.load(GOLDEN / f"{name}.npz"))
+
+
+def make_oracle(name, g):
+    finder, sym, integ, com, dims, pol = KIND[name]
+    prm = g["prm"]
+    n = len(g["x0"])
+    cap = max(int(prm[13]), n)
+    o = oracle.Oracle(dims=dims, finder=finder, symmetric=bool(sym), cutoff=float(prm[0]),
+                      gabriel_coefficient=float(prm[1]), min_bounds=tuple(prm[2:5]), max_bounds=tuple(prm[5:8]),
+                      bin_size_scale=float(prm[14]), integrator=integ, com_fix=bool(com),
+                      force=oracle.FORCE_POLARITY if pol else oracle.FORCE_SPRING2R, k_rep=float(prm[8]),
+                      r_rep=float(prm[9]), k_adh=float(prm[10]), r_adh=float(prm[11]), k_pol=float(prm[12]),
+                      has_polarity=bool(pol), capacity=cap)
+    o.set_state(g["x0"], g.get("p0"))
+    return o
+
+
+def test_manifest_covers_every_fixture():
+    assert set(MANIFEST) == set(KIND)
+    for name in KIND:
+        assert (GOLDEN / f"{name}.npz").exists()
+
+
+@pytest.mark.parametrize("name", sorted(KIND))
+def test_pairs_and_deltas_match_reference(name):
+    g = load(name)
+    o = make_oracle(name, g)
+    dx, dp, pairs = o.evaluate()
+    assert len(g["pairs"]) == MANIFEST[name]["pairs"]
+    # the directed pair list in the reference's Serial evaluation order
+    np.testing.assert_array_equal(pairs, g["pairs"])
+    np.testing.assert_array_equal(dx, g["dpos"])
+    if "dpol" in g:
+        np.testing.assert_array_equal(dp, g["dpol"])
+
+
+@pytest.mark.parametrize("name", sorted(KIND))
+def test_steps_match_reference(name):
+    g = load(name)
+    o = make_oracle(name, g)
+    o.step(float(g["dt"]), int(g["steps"]))
+    x, p = o.get_state()
+    np.testing.assert_array_equal(x, g["pos"])
+    if "pol" in g:
+        np.testing.assert_array_equal(p, g["pol"])
+
+
+def test_points11_gabriel_neighbour_counts():
+    # main.cpp's 2-D demo counts Gabriel neighbours per cell over both pair directions
+    g = load("ng_euler_2d_points11")
+    pairs = g["pairs"]
+    counts = np.bincount(pairs[:, 0], minlength=11)
+    # the graph is undirected: every (i, j) appears with (j, i)
+    s = {tuple(p) for p in pairs.tolist()}
+    assert all((j, i) in s for i, j in s)
+    assert counts.sum() == len(pairs) and counts.min() >= 1
