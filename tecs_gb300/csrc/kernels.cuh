@@ -27,7 +27,7 @@ struct Counters {
   unsigned div_count;   // daughters requested this step
   unsigned done[2];     // last-block counters of the two COM reductions
   unsigned error;       // bit 0: capacity overflow on division
-  unsigned pad;
+  unsigned done_div;    // last-block counter of the division fixup
   unsigned long long step;        // integrator steps taken (keys the division RNG)
   unsigned long long pair_count;  // pairs recorded by the capture hook
 };
@@ -65,6 +65,13 @@ struct PassArgs {
   // pair capture hook
   uint2* pairs;
   unsigned long long pair_cap;
+  // Gabriel fast path allowed (gabriel_coefficient <= 0.9 and bin size >= cutoff)
+  int gabriel_fast;
+  // bin count of the next step's rebuild, fused into the state write
+  int count_next;
+  unsigned* key;
+  unsigned* rank;
+  unsigned* cnt;
 };
 
 // ---------------------------------------------------------------------------
@@ -119,53 +126,43 @@ __global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned len, un
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// Exclusive scan of cnt into off, zeroing cnt for the next step.
+// Exclusive scan of cnt into off, zeroing cnt for the next step.  Each warp
+// owns 512 consecutive counts, read 32 at a time (coalesced): a first sweep
+// forms the warp totals, the block combines them with the earlier chunks'
+// totals, a second sweep (L1 hits) scans and writes.
 __global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, const unsigned* __restrict__ part,
                              unsigned* __restrict__ off) {
   __shared__ unsigned sh[32];
-  __shared__ unsigned wsum[kScanThreads / 32];
-  // prefix of all earlier chunks
+  __shared__ unsigned wtot[kScanThreads / 32];
   unsigned pre = 0;
   for (unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += part[b];
   pre = block_sum(pre, sh);
-  // each thread owns kScanPer consecutive elements
-  const unsigned base = blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
-  unsigned vals[kScanPer];
-  unsigned local = 0;
-#pragma unroll
-  for (int k = 0; k < kScanPer; ++k) {
-    unsigned idx = base + k;
-    vals[k] = idx < len ? cnt[idx] : 0u;
-    local += vals[k];
-  }
-  // block exclusive scan of the per-thread totals
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned incl = local;
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
+  constexpr int kPerWarp = kScanChunk / (kScanThreads / 32);
+  const unsigned base = blockIdx.x * kScanChunk + warp * kPerWarp;
+  unsigned tot = 0;
+  for (int it = 0; it < kPerWarp / 32; ++it) {
+    const unsigned idx = base + it * 32 + lane;
+    tot += idx < len ? cnt[idx] : 0u;
   }
-  if (lane == 31) wsum[warp] = incl;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (lane == 0) wtot[warp] = tot;
   __syncthreads();
-  if (warp == 0) {
-    unsigned w = lane < (kScanThreads / 32) ? wsum[lane] : 0u;
-    unsigned wi = w;
+  unsigned carry = pre;
+  for (int w = 0; w < warp; ++w) carry += wtot[w];
+  for (int it = 0; it < kPerWarp / 32; ++it) {
+    const unsigned idx = base + it * 32 + lane;
+    const unsigned v = idx < len ? cnt[idx] : 0u;
+    unsigned incl = v;
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += y;
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
     }
-    if (lane < (kScanThreads / 32)) wsum[lane] = wi - w;
-  }
-  __syncthreads();
-  unsigned run = pre + wsum[warp] + (incl - local);
-#pragma unroll
-  for (int k = 0; k < kScanPer; ++k) {
-    unsigned idx = base + k;
     if (idx < len) {
-      off[idx] = run;
+      off[idx] = carry + incl - v;
       cnt[idx] = 0u;
     }
-    run += vals[k];
+    carry += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 
@@ -177,44 +174,29 @@ __global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __re
     src[off[key[s]] + rank[s]] = s;
 }
 
-// One thread per bin: order the bin's cells by id (the Serial BinSort order,
-// Kokkos_Sort binning loop in ascending index) and gather them into B.
-constexpr int kSortLocal = 24;
-__global__ void k_sort_gather(unsigned nbins, const unsigned* __restrict__ off, unsigned* __restrict__ src,
-                              const float4* __restrict__ A, const float2* __restrict__ PA, float4* __restrict__ B,
-                              float2* __restrict__ PB) {
-  const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbins) return;
-  const unsigned lo = off[b], hi = off[b + 1];
-  const unsigned m = hi - lo;
-  if (m == 0) return;
-  if (m <= (unsigned)kSortLocal) {
-    unsigned sl[kSortLocal], id[kSortLocal];
-    for (unsigned r = 0; r < m; ++r) {
-      unsigned s = src[lo + r];
-      unsigned v = id_of(A[s]);
-      unsigned q = r;
-      while (q > 0 && id[q - 1] > v) { id[q] = id[q - 1]; sl[q] = sl[q - 1]; --q; }
-      id[q] = v; sl[q] = s;
+// One thread per sorted slot: the cell that the scatter put at slot t moves to
+// lo + (number of cells of its bin with a smaller id), so every bin lists its
+// cells in ascending id -- the order of Kokkos BinSort's binning loop on the
+// Serial backend.  Single-cell bins (most of them) copy straight through.
+__global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
+                               const unsigned* __restrict__ off, const unsigned* __restrict__ src,
+                               const float4* __restrict__ A, const float2* __restrict__ PA, float4* __restrict__ B,
+                               float2* __restrict__ PB) {
+  const unsigned n = ctr->n;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const unsigned s = src[t];
+    const unsigned b = key[s];
+    const unsigned lo = off[b], hi = off[b + 1];
+    const float4 v = A[s];
+    unsigned dst = t;
+    if (hi - lo > 1u) {
+      const unsigned me = id_of(v);
+      unsigned r = 0;
+      for (unsigned k = lo; k < hi; ++k) r += id_of(A[src[k]]) < me ? 1u : 0u;
+      dst = lo + r;
     }
-    for (unsigned r = 0; r < m; ++r) {
-      B[lo + r] = A[sl[r]];
-      if (PB) PB[lo + r] = PA[sl[r]];
-    }
-  } else {
-    // crowded bin: insertion sort in place on src (bounded by m*m/2 steps)
-    for (unsigned r = 1; r < m; ++r) {
-      unsigned s = src[lo + r];
-      unsigned v = id_of(A[s]);
-      unsigned q = r;
-      while (q > 0 && id_of(A[src[lo + q - 1]]) > v) { src[lo + q] = src[lo + q - 1]; --q; }
-      src[lo + q] = s;
-    }
-    for (unsigned r = 0; r < m; ++r) {
-      unsigned s = src[lo + r];
-      B[lo + r] = A[s];
-      if (PB) PB[lo + r] = PA[s];
-    }
+    B[dst] = v;
+    if (PB) PB[dst] = PA[s];
   }
 }
 
@@ -283,12 +265,23 @@ __device__ void com_reduce_block(const PassArgs& a, double x, double y, double z
   }
 }
 
+// Bin key and tentative rank of a freshly written cell for the next rebuild
+// (what k_count does, fused into the state write).
+template <int D>
+__device__ __forceinline__ void count_cell(const GridP& g, const PassArgs& a, unsigned slot, const float* x) {
+  int c[3] = {0, 0, 0};
+  bin_coords_div<D>(g, x, c);
+  const unsigned b = flatten<D>(g, c);
+  a.key[slot] = b;
+  a.rank[slot] = atomicAdd(&a.cnt[b], 1u);
+}
+
 // ---------------------------------------------------------------------------
 // division: decide (RNG keyed by cell id and step), append daughter at A[n + k]
 
 template <int D>
-__device__ __forceinline__ void maybe_divide(const PassArgs& a, unsigned n, unsigned id, const float* xnew,
-                                             float2 pnew, unsigned long long step) {
+__device__ __forceinline__ void maybe_divide(const GridP& g, const PassArgs& a, unsigned n, unsigned id,
+                                             const float* xnew, float2 pnew, unsigned long long step) {
   if (a.div_p <= 0.0) return;
   double u = u01(hash64(a.seed, step, id, 0));
   if (u > a.div_p) return;
@@ -307,11 +300,17 @@ __device__ __forceinline__ void maybe_divide(const PassArgs& a, unsigned n, unsi
   if (a.PA) a.PA[slot] = pnew;
   a.div_parent[k] = id;
   a.div_slot[k] = slot;
+  if (a.count_next) {
+    const float xd[3] = {o.x, o.y, o.z};
+    count_cell<D>(g, a, slot, xd);
+  }
 }
 
-// Daughter ids: n + rank of the parent id among this step's parents.
-__global__ void k_div_fixup(Counters* __restrict__ ctr, unsigned capacity, const unsigned* __restrict__ parent,
-                            const unsigned* __restrict__ slot, float4* __restrict__ A) {
+// Daughter ids: n + rank of the parent id among this step's parents, then
+// (last block) n += daughters.  Deterministic: ids depend only on parent ids.
+__global__ void k_divide_commit(Counters* __restrict__ ctr, unsigned capacity, const unsigned* __restrict__ parent,
+                                const unsigned* __restrict__ slot, float4* __restrict__ A) {
+  __shared__ bool last;
   const unsigned n = ctr->n;
   unsigned k = ctr->div_count;
   if (k > capacity - n) k = capacity - n;
@@ -321,14 +320,18 @@ __global__ void k_div_fixup(Counters* __restrict__ ctr, unsigned capacity, const
     for (unsigned e = 0; e < k; ++e) r += parent[e] < p ? 1u : 0u;
     A[slot[d]].w = __uint_as_float(n + r);
   }
-}
-__global__ void k_div_commit(Counters* __restrict__ ctr, unsigned capacity) {
-  const unsigned n = ctr->n;
-  unsigned k = ctr->div_count;
-  if (k > capacity - n) k = capacity - n;
-  ctr->n = n + k;
-  ctr->div_count = 0u;
-  ctr->step += 1ull;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&ctr->done_div, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    ctr->n = n + k;
+    ctr->div_count = 0u;
+    ctr->step += 1ull;
+    ctr->done_div = 0u;
+  }
 }
 __global__ void k_step_commit(Counters* __restrict__ ctr) { ctr->step += 1ull; }
 
@@ -413,52 +416,12 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
   pair_force<D, FORCE>(fp, disp, dist, pi, pj, acc);
 }
 
-template <int D, int FINDER, int FORCE>
-__global__ void __launch_bounds__(128) k_pass(GridP g, ForceP fp, PassArgs a) {
-  const unsigned n = a.ctr->n;
-  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = i < n;
-  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
-  float xi[3] = {0.f, 0.f, 0.f};
-  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
-  float2 pi = make_float2(0.f, 0.f);
-  if (active) {
-    vi = a.X[i];
-    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
-    if (a.P) pi = a.P[i];
-    const unsigned idi = id_of(vi);
-    if (FINDER == 1 || FINDER == 3) {
-      int bc[3] = {0, 0, 0};
-      if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
-      else bin_coords_div<D>(g, xi, bc);
-      // neighbour bins in the reference's task order (x fastest); each row of
-      // bins along x is one contiguous range of the sorted arrays
-      const int R = g.R;
-      const int z0 = D >= 3 ? -R : 0, z1 = D >= 3 ? R : 0;
-      for (int dz = z0; dz <= z1; ++dz) {
-        const int cz = D >= 3 ? bc[2] + dz : 0;
-        if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
-        for (int dy = -R; dy <= R; ++dy) {
-          const int cy = bc[1] + dy;
-          if (cy < 0 || cy >= g.ext[1]) continue;
-          const int x0 = max(bc[0] - R, 0), x1 = min(bc[0] + R, g.ext[0] - 1);
-          int c0[3] = {x0, cy, cz}, c1[3] = {x1, cy, cz};
-          const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
-          for (unsigned j = lo; j < hi; ++j) {
-            if (j == i) continue;
-            visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
-          }
-        }
-      }
-    } else {
-      for (unsigned j = 0; j < n; ++j) {
-        if (j == i) continue;
-        visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
-      }
-    }
-  }
-  // commit: out(i) = 0 + sum (views(i) += values on cleared stage buffers);
-  // the drag term adds exactly zero for the built-in laws (pairwise_drag = 0)
+// Commit of one cell: out(i) = 0 + sum (views(i) += values on cleared stage
+// buffers); the drag term adds exactly zero for the built-in laws
+// (pairwise_drag = 0).  Then the fused integrator epilogue of the mode.
+template <int D>
+__device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
+                                              const float* xi, const float4& vi, const float2& pi, const Acc& acc) {
   float s[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
@@ -503,7 +466,393 @@ __global__ void __launch_bounds__(128) k_pass(GridP g, ForceP fp, PassArgs a) {
   if (D < 3) xn[2] = 0.f;
   a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
   if (a.PA) a.PA[i] = pn;
-  maybe_divide<D>(a, n, id_of(xb), xn, pn, a.ctr->step);
+  if (a.count_next) count_cell<D>(g, a, i, xn);
+  maybe_divide<D>(g, a, n, id_of(xb), xn, pn, a.ctr->step);
+}
+
+
+// ---------------------------------------------------------------------------
+// Gabriel fast path.
+//
+// A witness k that blocks the pair (i, j) lies inside the ball of radius
+// r = c*d/2 around the midpoint m, and |x_i - m| = d/2, so |x_k - x_i| < d(1+c)/2.
+// For c <= 0.9 and d < cutoff that is < 0.95 * cutoff: every witness is itself
+// one of i's in-cutoff neighbours, found in i's 27 candidate bins.  The pass
+// therefore collects i's in-cutoff neighbours (candidate order = the
+// reference's summation order) into shared memory and tests each pair against
+// the others, keeping the reference's bin-range restriction on k exactly
+// (binned_gabriel.hpp:142-207).  If a cell has more than kMaxNb neighbours, or
+// a ball's bin range leaves i's 3x3x3 block, the cell takes the general path.
+constexpr int kMaxNb = 16;
+constexpr int kPassThreads = 128;
+
+template <int D, int FORCE>
+__device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned i,
+                                                  const float* xi, float2 pi, unsigned idi, Acc& acc,
+                                                  float4* nb) {
+  int bc[3] = {0, 0, 0};
+  bin_coords_div<D>(g, xi, bc);
+  int cnt = 0;
+  const int z0 = D >= 3 ? -1 : 0, z1 = D >= 3 ? 1 : 0;
+  for (int dz = z0; dz <= z1; ++dz) {
+    const int cz = D >= 3 ? bc[2] + dz : 0;
+    if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int cy = bc[1] + dy;
+      if (cy < 0 || cy >= g.ext[1]) continue;
+      const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
+      int c0[3] = {x0, cy, cz};
+      const unsigned b0 = flatten<D>(g, c0);
+      // boundaries of the (up to) three bins of this row
+      const unsigned o0 = __ldg(&a.off[b0]);
+      const unsigned o1 = __ldg(&a.off[b0 + 1]);
+      const unsigned o2 = x1 >= x0 + 1 ? __ldg(&a.off[b0 + 2]) : o1;
+      const unsigned o3 = x1 >= x0 + 2 ? __ldg(&a.off[b0 + 3]) : o2;
+      for (unsigned j = o0; j < o3; ++j) {
+        if (j == i) continue;
+        const float4 vj = __ldg(&a.X[j]);
+        const float e0 = xi[0] - vj.x, e1 = xi[1] - vj.y;
+        float d2 = e0 * e0 + e1 * e1;
+        if (D >= 3) { const float e2 = xi[2] - vj.z; d2 = d2 + e2 * e2; }
+        if (d2 >= fp.rc2) continue;
+        if (cnt == kMaxNb) return false;
+        const int rx = x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0];
+        const unsigned code = (unsigned)(rx + 1) | ((unsigned)(dy + 1) << 2) | ((unsigned)(dz + 1) << 4);
+        nb[cnt * kPassThreads] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 6) | code));
+        ++cnt;
+      }
+    }
+  }
+  // pass over the pairs: Gabriel test against the other neighbours
+  unsigned accepted = 0u;
+  for (int q = 0; q < cnt; ++q) {
+    const float4 vj = nb[q * kPassThreads];
+    float disp[3];
+    disp[0] = xi[0] - vj.x;
+    disp[1] = xi[1] - vj.y;
+    disp[2] = D >= 3 ? xi[2] - vj.z : 0.f;
+    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+    if (D >= 3) d2 = d2 + disp[2] * disp[2];
+    // midpoint ball and its bin range, relative to i's bin
+    float m[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) m[d] = xi[d] - disp[d] * 0.5f;
+    const float rsq = d2 * fp.gab_factor;
+    const float r = sqrtf(rsq);
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      lo[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - bc[d];
+      hi[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - bc[d];
+      if (lo[d] < -1 || hi[d] > 1) return false;
+    }
+    bool blocked = false;
+    for (int w = 0; w < cnt && !blocked; ++w) {
+      if (w == q) continue;
+      const float4 vk = nb[w * kPassThreads];
+      const unsigned code = __float_as_uint(vk.w) & 63u;
+      const int rx = (int)(code & 3u) - 1, ry = (int)((code >> 2) & 3u) - 1, rz = (int)((code >> 4) & 3u) - 1;
+      if (rx < lo[0] || rx > hi[0] || ry < lo[1] || ry > hi[1]) continue;
+      if (D >= 3 && (rz < lo[2] || rz > hi[2])) continue;
+      const float f0 = vk.x - m[0], f1 = vk.y - m[1];
+      float s = f0 * f0 + f1 * f1;
+      if (D >= 3) { const float f2 = vk.z - m[2]; s = s + f2 * f2; }
+      if (s < rsq) blocked = true;
+    }
+    if (!blocked) accepted |= 1u << q;
+  }
+  // forces of the accepted pairs, in candidate (= reference summation) order
+  Acc loc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  while (accepted) {
+    const int q = __ffs(accepted) - 1;
+    accepted &= accepted - 1u;
+    const float4 vj = nb[q * kPassThreads];
+    const unsigned j = __float_as_uint(vj.w) >> 6;
+    float disp[3];
+    disp[0] = xi[0] - vj.x;
+    disp[1] = xi[1] - vj.y;
+    disp[2] = D >= 3 ? xi[2] - vj.z : 0.f;
+    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+    if (D >= 3) d2 = d2 + disp[2] * disp[2];
+    if (a.pairs) {
+      unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(__ldg(&a.X[j])));
+    }
+    const float dist = sqrtf(d2);
+    const float2 pj = (FORCE == 2 && a.P) ? __ldg(&a.P[j]) : make_float2(0.f, 0.f);
+    pair_force<D, FORCE>(fp, disp, dist, pi, pj, loc);
+  }
+  acc = loc;
+  return true;
+}
+
+template <int D, int FINDER, int FORCE>
+__device__ __noinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+                                          const float* xi, float2 pi, unsigned idi, Acc& acc);
+
+template <int D, int FINDER, int FORCE>
+__global__ void __launch_bounds__(kPassThreads) k_pass(GridP g, ForceP fp, PassArgs a) {
+  const unsigned n = a.ctr->n;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  float xi[3] = {0.f, 0.f, 0.f};
+  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 pi = make_float2(0.f, 0.f);
+  if (active) {
+    vi = a.X[i];
+    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
+    if (a.P) pi = a.P[i];
+    const unsigned idi = id_of(vi);
+    if (FINDER == 3 && a.gabriel_fast) {
+      __shared__ float4 nbuf[kMaxNb * kPassThreads];
+      if (!gabriel_cell_fast<D, FORCE>(g, fp, a, i, xi, pi, idi, acc, &nbuf[threadIdx.x])) {
+        // nothing was recorded or accumulated yet: redo the cell the general way
+        cell_general<D, FINDER, FORCE>(g, fp, a, n, i, xi, pi, idi, acc);
+      }
+    } else {
+      cell_general<D, FINDER, FORCE>(g, fp, a, n, i, xi, pi, idi, acc);
+    }
+  }
+  pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+}
+
+// The general path: the reference's loops (27 bins, then the ball's bins per pair).
+template <int D, int FINDER, int FORCE>
+__device__ __noinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+                                          const float* xi, float2 pi, unsigned idi, Acc& acc) {
+    if (FINDER == 1 || FINDER == 3) {
+      int bc[3] = {0, 0, 0};
+      if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
+      else bin_coords_div<D>(g, xi, bc);
+      // neighbour bins in the reference's task order (x fastest); each row of
+      // bins along x is one contiguous range of the sorted arrays
+      const int R = g.R;
+      const int z0 = D >= 3 ? -R : 0, z1 = D >= 3 ? R : 0;
+      for (int dz = z0; dz <= z1; ++dz) {
+        const int cz = D >= 3 ? bc[2] + dz : 0;
+        if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+        for (int dy = -R; dy <= R; ++dy) {
+          const int cy = bc[1] + dy;
+          if (cy < 0 || cy >= g.ext[1]) continue;
+          const int x0 = max(bc[0] - R, 0), x1 = min(bc[0] + R, g.ext[0] - 1);
+          int c0[3] = {x0, cy, cz}, c1[3] = {x1, cy, cz};
+          const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
+          for (unsigned j = lo; j < hi; ++j) {
+            if (j == i) continue;
+            visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
+          }
+        }
+      }
+    } else {
+      for (unsigned j = 0; j < n; ++j) {
+        if (j == i) continue;
+        visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
+      }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block-cooperative Gabriel pass (spring laws).
+//
+// Same pair semantics as gabriel_cell_fast, reorganised so that the lanes stay
+// busy: (1) each thread collects its cell's in-cutoff neighbours into shared
+// memory; (2) the block lists every (cell, neighbour) pair and the threads
+// take pairs round-robin for the Gabriel test; (3) the same for the pair
+// forces, each written over its candidate slot; (4) each thread adds its
+// cell's accepted contributions in candidate order -- the reference's
+// summation order, so the sums stay bit-identical.  Cells with more than
+// kMaxNb neighbours, or whose witness ball leaves the 3x3x3 bin block, take
+// the general path in phase 4.
+template <int D>
+__device__ __forceinline__ unsigned ball_mask27(const int* lo, const int* hi) {
+  // bit (rx+1) + 3(ry+1) + 9(rz+1) set when the bin offset (rx, ry, rz) lies in [lo, hi]
+  unsigned m3[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (d < D) m3[d] = ((1u << (hi[d] + 2)) - 1u) & ~((1u << (lo[d] + 1)) - 1u);
+    else m3[d] = 2u;  // unused dimension: offset 0 only
+  }
+  const unsigned plane = ((m3[1] & 1u) ? m3[0] : 0u) | ((m3[1] & 2u) ? m3[0] << 3 : 0u) |
+                         ((m3[1] & 4u) ? m3[0] << 6 : 0u);
+  return ((m3[2] & 1u) ? plane : 0u) | ((m3[2] & 2u) ? plane << 9 : 0u) | ((m3[2] & 4u) ? plane << 18 : 0u);
+}
+
+template <int D, int FORCE>
+__global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
+  static_assert(FORCE <= 1, "the block-cooperative pass serves the spring laws");
+  __shared__ float4 cand[kMaxNb * kPassThreads];            // [q][t]: position, w = (slot << 5) | bin code
+  __shared__ float4 home[kPassThreads];                     // position, w = packed bin coords
+  __shared__ unsigned short pinfo[kMaxNb * kPassThreads];   // (t << 4) | q, bit 15 = accepted
+  __shared__ int pofs[kPassThreads + 1];
+  __shared__ int wsum[kPassThreads / 32];
+  __shared__ unsigned char ncnt[kPassThreads];
+  __shared__ unsigned char fallback[kPassThreads];
+
+  const unsigned n = a.ctr->n;
+  const int t = threadIdx.x;
+  const unsigned i = blockIdx.x * kPassThreads + t;
+  const bool active = i < n;
+  float xi[3] = {0.f, 0.f, 0.f};
+  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 pi = make_float2(0.f, 0.f);
+  int bc[3] = {0, 0, 0};
+  int cnt = 0;
+  bool fb = false;
+  // ---- phase 1: in-cutoff neighbours of this thread's cell
+  if (active) {
+    vi = __ldg(&a.X[i]);
+    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
+    if (a.P) pi = a.P[i];
+    bin_coords_div<D>(g, xi, bc);
+    const int z0 = D >= 3 ? -1 : 0, z1 = D >= 3 ? 1 : 0;
+    for (int dz = z0; dz <= z1 && !fb; ++dz) {
+      const int cz = D >= 3 ? bc[2] + dz : 0;
+      if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+      for (int dy = -1; dy <= 1 && !fb; ++dy) {
+        const int cy = bc[1] + dy;
+        if (cy < 0 || cy >= g.ext[1]) continue;
+        const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
+        int c0[3] = {x0, cy, cz};
+        const unsigned b0 = flatten<D>(g, c0);
+        const unsigned o0 = __ldg(&a.off[b0]);
+        const unsigned o1 = __ldg(&a.off[b0 + 1]);
+        const unsigned o2 = x1 >= x0 + 1 ? __ldg(&a.off[b0 + 2]) : o1;
+        const unsigned o3 = x1 >= x0 + 2 ? __ldg(&a.off[b0 + 3]) : o2;
+        const unsigned rowcode = 3u * (unsigned)(dy + 1) + 9u * (unsigned)(D >= 3 ? dz + 1 : 1);
+        for (unsigned j = o0; j < o3; ++j) {
+          if (j == i) continue;
+          const float4 vj = __ldg(&a.X[j]);
+          const float e0 = xi[0] - vj.x, e1 = xi[1] - vj.y;
+          float d2 = e0 * e0 + e1 * e1;
+          if (D >= 3) { const float e2 = xi[2] - vj.z; d2 = d2 + e2 * e2; }
+          if (d2 >= fp.rc2) continue;
+          if (cnt == kMaxNb) { fb = true; break; }
+          const unsigned rx = (unsigned)(x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0] + 1);
+          cand[cnt * kPassThreads + t] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 5) | (rowcode + rx)));
+          ++cnt;
+        }
+      }
+    }
+  }
+  if (fb) cnt = 0;
+  home[t] = make_float4(xi[0], xi[1], xi[2],
+                        __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
+  ncnt[t] = (unsigned char)cnt;
+  fallback[t] = fb ? 1 : 0;
+  // exclusive scan of the neighbour counts -> pair offsets
+  {
+    const int lane = t & 31, warp = t >> 5;
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += wsum[w];
+    pofs[t] = base + incl - cnt;
+    if (t == kPassThreads - 1) pofs[kPassThreads] = base + incl;
+  }
+  for (int q = 0; q < cnt; ++q) pinfo[pofs[t] + q] = (unsigned short)((t << 4) | q);
+  __syncthreads();
+  const int P = pofs[kPassThreads];
+  // ---- phase 2: Gabriel test, one pair per thread at a time
+  for (int p = t; p < P; p += kPassThreads) {
+    const unsigned info = pinfo[p];
+    const int c = (int)(info >> 4), q = (int)(info & 15u);
+    const float4 h = home[c];
+    const float4 vj = cand[q * kPassThreads + c];
+    const unsigned hb = __float_as_uint(h.w);
+    const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
+    const float hx[3] = {h.x, h.y, h.z};
+    float disp[3];
+    disp[0] = hx[0] - vj.x;
+    disp[1] = hx[1] - vj.y;
+    disp[2] = D >= 3 ? hx[2] - vj.z : 0.f;
+    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+    if (D >= 3) d2 = d2 + disp[2] * disp[2];
+    float m[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) m[d] = hx[d] - disp[d] * 0.5f;
+    const float rsq = d2 * fp.gab_factor;
+    const float r = sqrtf(rsq);
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    bool out = false;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      lo[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+      hi[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+      out = out || lo[d] < -1 || hi[d] > 1;
+    }
+    if (out) {
+      fallback[c] = 1;
+      continue;
+    }
+    const unsigned mask = ball_mask27<D>(lo, hi);
+    const int cc = ncnt[c];
+    bool blocked = false;
+    for (int w = 0; w < cc; ++w) {
+      if (w == q) continue;
+      const float4 vk = cand[w * kPassThreads + c];
+      if (!((mask >> (__float_as_uint(vk.w) & 31u)) & 1u)) continue;
+      const float f0 = vk.x - m[0], f1 = vk.y - m[1];
+      float s = f0 * f0 + f1 * f1;
+      if (D >= 3) { const float f2 = vk.z - m[2]; s = s + f2 * f2; }
+      if (s < rsq) { blocked = true; break; }
+    }
+    if (!blocked) pinfo[p] = (unsigned short)(info | 0x8000u);
+  }
+  __syncthreads();
+  // ---- phase 3: pair forces, written over the candidate slot
+  for (int p = t; p < P; p += kPassThreads) {
+    const unsigned info = pinfo[p];
+    const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
+    if (!(info & 0x8000u) || fallback[c]) continue;
+    const float4 h = home[c];
+    const float4 vj = cand[q * kPassThreads + c];
+    float disp[3];
+    disp[0] = h.x - vj.x;
+    disp[1] = h.y - vj.y;
+    disp[2] = D >= 3 ? h.z - vj.z : 0.f;
+    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+    if (D >= 3) d2 = d2 + disp[2] * disp[2];
+    if (a.pairs) {
+      const unsigned j = __float_as_uint(vj.w) >> 5;
+      const unsigned ci = blockIdx.x * kPassThreads + c;
+      unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(id_of(__ldg(&a.X[ci])), id_of(__ldg(&a.X[j])));
+    }
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float dist = sqrtf(d2);
+    if (FORCE == 1 && dist != 0.0f) {
+      // (displacement * F) / distance, forces/predefined.hpp:134-143
+      const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
+      f.x = (disp[0] * F) / dist;
+      f.y = (disp[1] * F) / dist;
+      if (D >= 3) f.z = (disp[2] * F) / dist;
+    }
+    cand[q * kPassThreads + c] = f;
+  }
+  __syncthreads();
+  // ---- phase 4: ordered per-cell sums
+  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  if (active) {
+    if (fallback[t]) {
+      cell_general<D, 3, FORCE>(g, fp, a, n, i, xi, pi, id_of(vi), acc);
+    } else {
+      const int base = pofs[t];
+      for (int q = 0; q < cnt; ++q) {
+        if (!(pinfo[base + q] & 0x8000u)) continue;
+        const float4 f = cand[q * kPassThreads + t];
+        acc.x[0] = acc.x[0] + f.x;
+        acc.x[1] = acc.x[1] + f.y;
+        if (D >= 3) acc.x[2] = acc.x[2] + f.z;
+      }
+    }
+  }
+  pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
 }
 
 // Symmetric finders (…_symmetric.hpp): only j with a smaller id, +delta to the
@@ -587,16 +936,16 @@ __global__ void k_com(const float4* __restrict__ d, PassArgs a) {
 // integrator epilogues when the COM fix (or the symmetric finder) forbids
 // fusing them into the pass
 
-// heun.hpp:54-68: d1 -= c; x~ = x + d1 * dt (every field)
+// heun.hpp:54-68: d1' = d1 - c1; x~ = x + d1' * dt (every field).  d1' is not
+// stored: the corrector forms it again with the same operations.
 __global__ void k_predict(const Counters* __restrict__ ctr, const float* __restrict__ com, float dt,
-                          const float4* __restrict__ B, const float2* __restrict__ PB, float4* __restrict__ d1,
+                          const float4* __restrict__ B, const float2* __restrict__ PB, const float4* __restrict__ d1,
                           const float2* __restrict__ dp1, float4* __restrict__ Xt, float2* __restrict__ Pt) {
   const unsigned n = ctr->n;
   const float c0 = com[0], c1 = com[1], c2 = com[2];
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 v = d1[i];
-    v.x = v.x - c0; v.y = v.y - c1; v.z = v.z - c2;
-    d1[i] = v;
+    v.x = v.x - c0; v.y = v.y - c1; v.z = v.z - c2;  // d1 - c1 (re-formed by k_finish)
     const float4 x = B[i];
     Xt[i] = make_float4(x.x + v.x * dt, x.y + v.y * dt, x.z + v.z * dt, x.w);
     if (Pt) {
@@ -610,10 +959,12 @@ __global__ void k_predict(const Counters* __restrict__ ctr, const float* __restr
 // plus division.  Heun: s = d1 + (d2 - c); x += (s * 0.5) * dt.
 // Euler:  s = d1 - c; x += s * dt.
 template <int D>
-__global__ void k_finish(int heun, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
+__global__ void k_finish(int heun, GridP g, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
                          const float2* __restrict__ dp2) {
   const unsigned n = a.ctr->n;
-  const float c0 = com[0], c1 = com[1], c2 = com[2];
+  // Euler: com = c (slot 0).  Heun: com = c1 (slot 0), com + 4 = c2 (slot 1)
+  const float c0 = com[heun ? 4 : 0], c1 = com[heun ? 5 : 1], c2 = com[heun ? 6 : 2];
+  const float p0 = com[0], p1 = com[1], p2 = com[2];
   const float dt = a.dt;
   const unsigned long long step = a.ctr->step;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -623,8 +974,9 @@ __global__ void k_finish(int heun, PassArgs a, const float* __restrict__ com, co
     float2 pn = make_float2(0.f, 0.f);
     if (heun) {
       const float4 v2 = d2[i];
-      const float e0 = v2.x - c0, e1 = v2.y - c1, e2 = v2.z - c2;
-      const float h0 = v1.x + e0, h1 = v1.y + e1, h2 = v1.z + e2;
+      const float f0 = v1.x - p0, f1 = v1.y - p1, f2 = v1.z - p2;  // d1 - c1 (predictor)
+      const float e0 = v2.x - c0, e1 = v2.y - c1, e2 = v2.z - c2;  // d2 - c2 (corrector)
+      const float h0 = f0 + e0, h1 = f1 + e1, h2 = f2 + e2;
       xn[0] = xb.x + (h0 * 0.5f) * dt; xn[1] = xb.y + (h1 * 0.5f) * dt; xn[2] = xb.z + (h2 * 0.5f) * dt;
       if (a.PA) {
         const float2 pb = a.Bp[i], q1 = a.dp1[i], q2 = dp2[i];
@@ -642,7 +994,8 @@ __global__ void k_finish(int heun, PassArgs a, const float* __restrict__ com, co
     if (D < 3) xn[2] = 0.f;
     a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
     if (a.PA) a.PA[i] = pn;
-    maybe_divide<D>(a, n, id_of(xb), xn, pn, step);
+    if (a.count_next) count_cell<D>(g, a, i, xn);
+    maybe_divide<D>(g, a, n, id_of(xb), xn, pn, step);
   }
 }
 

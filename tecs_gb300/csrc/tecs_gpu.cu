@@ -3,12 +3,14 @@
 // One tecs_sim owns the device state of one simulation and a CUDA stream.
 // tecs_sim_step queues one integrator step as a fixed kernel sequence:
 //
-//   rebuild   k_count -> k_scan_reduce -> k_scan_apply -> k_scatter -> k_sort_gather
+//   rebuild   [k_count] -> k_scan_reduce -> k_scan_apply -> k_scatter -> k_order_gather
+//             (k_count is fused into the previous step's state write when every
+//              step rebuilds)
 //   Euler     k_pass(kEulerFused)                                   [no COM]
 //             k_pass(kStore + COM) -> k_finish                      [COM]
 //   Heun      k_pass(kHeun1Fused) -> k_pass(kHeun2Fused)            [no COM]
 //             k_pass(kStore + COM) -> k_predict -> k_pass(kStore + COM) -> k_finish
-//   division  k_div_fixup -> k_div_commit
+//   division  k_divide_commit
 //
 // and, by default, captures that sequence once as a CUDA graph and replays it.
 #include <cuda_runtime.h>
@@ -47,13 +49,6 @@ __global__ void k_pack(const float* __restrict__ in, unsigned n, int dims, float
     v.x = in[(size_t)s * dims];
     if (dims >= 2) v.y = in[(size_t)s * dims + 1];
     if (dims >= 3) v.z = in[(size_t)s * dims + 2];
-    A[s] = v;
-  }
-}
-__global__ void k_pack4(const float4* __restrict__ in, unsigned n, float4* __restrict__ A) {
-  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    float4 v = in[s];
-    v.w = __uint_as_float(s);
     A[s] = v;
   }
 }
@@ -96,6 +91,10 @@ struct tecs_sim {
   float gdt[2] = {0.f, 0.f};
   int kernels[2] = {0, 0};
   int last_kernels = 0;
+  // the next rebuild's bin count is done by the state-writing kernel
+  bool fuse_count = false;
+  // block-cooperative Gabriel pass enabled (off only for comparison runs)
+  bool use_coop = true;
   // per-kernel CUDA events (external event-record nodes when captured in a graph)
   bool profiling = false;
   static constexpr int kMaxProf = 32;
@@ -136,6 +135,11 @@ int prof_mark(tecs_sim* s, int which, const char* name) {
 
 PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
+  // the block-cooperative Gabriel pass needs the fast-path geometry and packs
+  // bin coordinates in 10 bits and slots in 27 bits
+  const bool coop = s->d.gabriel_coefficient <= 0.9f && s->g.R == 1 && s->g.bin_size >= s->d.cutoff &&
+                    s->g.ext[0] <= 1024 && s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 &&
+                    s->d.capacity < (1u << 27) && s->use_coop;
 #define PICK(DD, FF)                                                            \
   if (D == DD && F == FF) {                                                     \
     if (sym) {                                                                  \
@@ -143,6 +147,8 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
       if (FO == 1) return k_pass_sym<DD, FF, 1>;                                \
       if (DD == 3) return k_pass_sym<DD, FF, 2>;                                \
     } else {                                                                    \
+      if (FF == 3 && coop && FO == 0) return k_pass_gabriel<DD, 0>;             \
+      if (FF == 3 && coop && FO == 1) return k_pass_gabriel<DD, 1>;             \
       if (FO == 0) return k_pass<DD, FF, 0>;                                    \
       if (FO == 1) return k_pass<DD, FF, 1>;                                    \
       if (DD == 3) return k_pass<DD, FF, 2>;                                    \
@@ -166,11 +172,18 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.div_slot = s->div_slot;
   a.A = s->A;
   a.PA = s->d.has_polarity ? s->PA : nullptr;
+  // the fast Gabriel path needs every witness inside i's cutoff ball and 3x3x3 bin block
+  a.gabriel_fast = (s->d.gabriel_coefficient <= 0.9f && s->g.R == 1 && s->g.bin_size >= s->d.cutoff) ? 1 : 0;
+  a.count_next = s->fuse_count ? 1 : 0;
+  a.key = s->key;
+  a.rank = s->rank;
+  a.cnt = s->cnt;
   return a;
 }
 
 // Rebuild B (working copy) from A: bins sorted by (bin, id), or id order for naive finders.
-int enqueue_rebuild(tecs_sim* s, int& K) {
+// With run_count false the bin counts of A were already made by the kernel that wrote A.
+int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
   const unsigned L = launch_count(s);
   const unsigned gb = ceil_div(L ? L : 1, 256);
   float2* PA = s->d.has_polarity ? s->PA : nullptr;
@@ -178,9 +191,12 @@ int enqueue_rebuild(tecs_sim* s, int& K) {
   if (s->binned) {
     const unsigned len = s->g.nbins + 1;
     const unsigned chunks = ceil_div(len, kScanChunk);
-    PROF_BEGIN(s);
-    k_count<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
-    PROF_END(s, "k_count");
+    if (run_count) {
+      PROF_BEGIN(s);
+      k_count<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+      PROF_END(s, "k_count");
+      K += 1;
+    }
     PROF_BEGIN(s);
     k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
     PROF_END(s, "k_scan_reduce");
@@ -191,10 +207,9 @@ int enqueue_rebuild(tecs_sim* s, int& K) {
     k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
-    k_sort_gather<<<ceil_div(s->g.nbins, 256), 256, 0, s->stream>>>(s->g.nbins, s->off, s->src, s->A, PA, s->B,
-                                                                    PB);
-    PROF_END(s, "k_sort_gather");
-    K += 5;
+    k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB);
+    PROF_END(s, "k_order_gather");
+    K += 4;
   } else {
     PROF_BEGIN(s);
     k_id_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, PA, s->B, PB);
@@ -230,7 +245,7 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
   const unsigned gb = ceil_div(L ? L : 1, 256);
   const int D = s->d.dims;
   if (rebuild || !s->binned) {
-    if (enqueue_rebuild(s, K)) return -1;
+    if (enqueue_rebuild(s, K, !s->fuse_count)) return -1;
   } else {
     CK(cudaMemcpyAsync(s->B, s->A, sizeof(float4) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
     if (pol) CK(cudaMemcpyAsync(s->PB, s->PA, sizeof(float2) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
@@ -282,8 +297,8 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
       if (enqueue_pass(s, p, K)) return -1;
       sym_com(s->d1, 0);
       PROF_BEGIN(s);
-      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(0, fin, s->com, nullptr, nullptr);
-      else k_finish<2><<<gb, 256, 0, s->stream>>>(0, fin, s->com, nullptr, nullptr);
+      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(0, s->g, fin, s->com, nullptr, nullptr);
+      else k_finish<2><<<gb, 256, 0, s->stream>>>(0, s->g, fin, s->com, nullptr, nullptr);
       PROF_END(s, "k_finish");
       K += 1;
     }
@@ -325,20 +340,17 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
       if (enqueue_pass(s, p2, K)) return -1;
       sym_com(s->d2, 1);
       PROF_BEGIN(s);
-      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(1, fin, s->com + 4, s->d2, pol ? s->dp2 : nullptr);
-      else k_finish<2><<<gb, 256, 0, s->stream>>>(1, fin, s->com + 4, s->d2, pol ? s->dp2 : nullptr);
+      if (D == 3) k_finish<3><<<gb, 256, 0, s->stream>>>(1, s->g, fin, s->com, s->d2, pol ? s->dp2 : nullptr);
+      else k_finish<2><<<gb, 256, 0, s->stream>>>(1, s->g, fin, s->com, s->d2, pol ? s->dp2 : nullptr);
       PROF_END(s, "k_finish");
       K += 1;
     }
   }
   if (s->d.division_probability > 0.0) {
     PROF_BEGIN(s);
-    k_div_fixup<<<32, 256, 0, s->stream>>>(s->ctr, s->d.capacity, s->div_parent, s->div_slot, s->A);
-    PROF_END(s, "k_div_fixup");
-    PROF_BEGIN(s);
-    k_div_commit<<<1, 1, 0, s->stream>>>(s->ctr, s->d.capacity);
-    PROF_END(s, "k_div_commit");
-    K += 2;
+    k_divide_commit<<<32, 256, 0, s->stream>>>(s->ctr, s->d.capacity, s->div_parent, s->div_slot, s->A);
+    PROF_END(s, "k_divide_commit");
+    K += 1;
   }
   CK(cudaGetLastError());
   return 0;
@@ -417,6 +429,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   f.gab_factor = desc->gabriel_coefficient * desc->gabriel_coefficient * 0.25f;
   f.gab_csq = desc->gabriel_coefficient * desc->gabriel_coefficient;
   s->binned = desc->finder == TECS_FINDER_BINNED_ALL_PAIRS || desc->finder == TECS_FINDER_BINNED_GABRIEL;
+  s->fuse_count = s->binned && (desc->division_probability > 0.0 || desc->rebuild_every_n <= 1);
 
   const size_t cap = desc->capacity;
   auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
@@ -474,6 +487,12 @@ static int upload_common(tecs_sim* s, unsigned n) {
   Counters c{};
   c.n = n;
   CK(cudaMemcpyAsync(s->ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+  if (s->fuse_count) {
+    // the first rebuild expects the bin counts of A to be made already
+    CK(cudaMemsetAsync(s->cnt, 0, ((size_t)s->g.nbins + 1) * 4, s->stream));
+    if (n) k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(s->stream));
   s->n_host = n;
   s->step_count = 0;
@@ -602,7 +621,7 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   if (tecs_sim_count(s, &n)) return -1;
   const bool pol = s->d.has_polarity != 0;
   int K = 0;
-  if (enqueue_rebuild(s, K)) return -1;
+  if (enqueue_rebuild(s, K, !s->fuse_count)) return -1;
   uint2* dpairs = nullptr;
   if (pairs && pair_cap) CK(cudaMalloc(&dpairs, pair_cap * sizeof(uint2)));
   CK(cudaMemsetAsync(&s->ctr->pair_count, 0, 8, s->stream));
@@ -618,7 +637,12 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   a.dp_out = pol ? s->dp1 : nullptr;
   a.pairs = dpairs;
   a.pair_cap = dpairs ? pair_cap : 0;
+  a.count_next = 0;
   int rc = enqueue_pass(s, a, K);
+  if (rc == 0 && s->fuse_count && n) {
+    // A is unchanged: count it again for the next step's rebuild
+    k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+  }
   if (rc == 0 && n) {
     if (dpos) {
       k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->d1, n, s->d.dims, (float*)s->Xt);

@@ -259,3 +259,27 @@ def test_full_size_million_cells_pairs_and_deltas():
     dc, _, pc = c.evaluate(threads=0)
     np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
     np.testing.assert_array_equal(dg, dc)
+
+
+@pytest.mark.parametrize("gab", [0.95, 1.0, 0.5])
+def test_gabriel_coefficients_general_path(gab):
+    # c > 0.9 takes the reference-shaped general path; c = 0.5 the fast paths
+    x = ball(4000, seed=16)
+    g, c = make_pair(x, finder="binned_gabriel", gab=gab)
+    dg, _, pg = g.evaluate()
+    dc, _, pc = c.evaluate()
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
+    np.testing.assert_array_equal(dg, dc)
+
+
+def test_dense_packing_neighbour_overflow():
+    # ~3x the headline density: many cells exceed the 16-neighbour fast-path list
+    x = ball(6000, seed=17, radius=8.0)
+    g, c = make_pair(x, finder="binned_gabriel", integrator="heun")
+    dg, _, pg = g.evaluate()
+    dc, _, pc = c.evaluate()
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
+    np.testing.assert_array_equal(dg, dc)
+    g.take_step(0.05, 3)
+    c.step(0.05, 3)
+    np.testing.assert_array_equal(g.get_state()[0], c.get_state()[0])
