@@ -136,6 +136,26 @@ const char* tecs_sim_profile_name(tecs_sim* sim, int index);
 /* Number of kernels one step launches (for launch accounting). */
 int tecs_sim_kernels_per_step(tecs_sim* sim, int* kernels);
 
+/* Limits of tecs_force_pass_noalloc (its scratch is a fixed static device array). */
+#define TECS_NOALLOC_MAX_CELLS 65536u
+#define TECS_NOALLOC_MAX_BINS 262144u
+
+/* No counterpart in the reference: an allocation-free form of the one-pass
+ * force evaluation of tecs_sim_evaluate, for callers that may not allocate
+ * device memory (a host runtime that owns the GPU memory budget, a serving
+ * loop that must not stall on or fragment the allocator).  Reads positions
+ * (device, float[n][dims]), writes per-cell deltas (device, float[n][dims],
+ * input order) for a binned, non-symmetric finder with the spring law or no
+ * force, queued on `stream` (a cudaStream_t, 0 = legacy default).  Allocates
+ * nothing: its scratch is a static device array of about 6 MB that every GPU
+ * loading the library keeps until exit.  Rejects more than
+ * TECS_NOALLOC_MAX_CELLS cells or TECS_NOALLOC_MAX_BINS bins.  The first call
+ * on a device looks up the array's device address (once per device), so make
+ * that first call before any stream capture.  All calls on a device share the
+ * array: calls whose GPU work overlaps race and must be serialised. */
+int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d_positions, unsigned n, float* d_deltas,
+                            void* stream);
+
 /* Message of the last failing call on this thread. */
 const char* tecs_last_error(void);
 

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -705,3 +706,150 @@ int tecs_sim_kernels_per_step(tecs_sim* s, int* kernels) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free force pass.
+//
+// Some callers cannot call cudaMalloc: code that hands this library a fixed
+// device-memory budget and forbids allocation after start-up (a host runtime
+// that owns the GPU's memory pool, a serving loop that must never stall on the
+// allocator or fragment HBM between requests), or code already inside a region
+// where allocating is not allowed.  For them, tecs_force_pass_noalloc runs the
+// same one-pass force evaluation as tecs_sim_evaluate on caller-owned device
+// buffers and takes all of its scratch from the file-scope array below.
+//
+// The array is part of the library's device image: every GPU that loads the
+// library holds it (kNoallocScratchBytes) until the process exits.  All calls
+// on one device share it and each call starts by clearing what must start at
+// zero, so calls whose GPU work overlaps (two streams, two host threads) race
+// on it and must be serialised by the caller.
+namespace {
+constexpr unsigned kNoallocMaxCells = TECS_NOALLOC_MAX_CELLS;
+constexpr unsigned kNoallocMaxBins = TECS_NOALLOC_MAX_BINS;
+constexpr size_t kNoallocAlign = 256;
+constexpr size_t align_up(size_t v) { return (v + kNoallocAlign - 1) / kNoallocAlign * kNoallocAlign; }
+// layout of the scratch array
+constexpr size_t kOffCtr = 0;
+constexpr size_t kOffA = align_up(kOffCtr + sizeof(Counters));
+constexpr size_t kOffB = align_up(kOffA + (size_t)kNoallocMaxCells * sizeof(float4));
+constexpr size_t kOffD = align_up(kOffB + (size_t)kNoallocMaxCells * sizeof(float4));
+constexpr size_t kOffKey = align_up(kOffD + (size_t)kNoallocMaxCells * sizeof(float4));
+constexpr size_t kOffRank = align_up(kOffKey + (size_t)kNoallocMaxCells * 4);
+constexpr size_t kOffSrc = align_up(kOffRank + (size_t)kNoallocMaxCells * 4);
+constexpr size_t kOffCnt = align_up(kOffSrc + (size_t)kNoallocMaxCells * 4);
+constexpr size_t kOffOff = align_up(kOffCnt + ((size_t)kNoallocMaxBins + 1) * 4);
+constexpr size_t kOffPart = align_up(kOffOff + ((size_t)kNoallocMaxBins + 1) * 4);
+constexpr size_t kNoallocScratchBytes =
+    align_up(kOffPart + ((size_t)kNoallocMaxBins + 1 + kScanChunk - 1) / kScanChunk * 4);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+__global__ void k_noalloc_reset(Counters* ctr, unsigned n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Counters c{};
+    c.n = n;
+    *ctr = c;
+  }
+}
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current.  The host-side name of the array is only a stand-in; kernels
+// must be given this address.
+int noalloc_scratch(int device, unsigned char** out) {
+  static std::mutex mu;
+  static unsigned char* addr[64] = {};
+  if (device < 0 || device >= 64) return fail("device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    addr[device] = (unsigned char*)p;
+  }
+  *out = addr[device];
+  return 0;
+}
+}  // namespace
+
+extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d_positions, unsigned n,
+                                       float* d_deltas, void* stream) {
+  if (!desc || (n && (!d_positions || !d_deltas))) return fail("null argument");
+  if (desc->dims != 2 && desc->dims != 3) return fail("dims must be 2 or 3");
+  if (desc->finder != TECS_FINDER_BINNED_ALL_PAIRS && desc->finder != TECS_FINDER_BINNED_GABRIEL)
+    return fail("the allocation-free pass serves the binned finders");
+  if (desc->symmetric) return fail("the allocation-free pass serves the non-symmetric finders");
+  if (desc->has_polarity || desc->force == TECS_FORCE_POLARITY)
+    return fail("the allocation-free pass serves the spring laws without a polarity field");
+  if (desc->force != TECS_FORCE_NONE && desc->force != TECS_FORCE_SPRING2R) return fail("unknown force");
+  if (!(desc->cutoff > 0.f) || !(desc->bin_size_scale > 0.f)) return fail("cutoff and bin_size_scale must be > 0");
+  if (n > kNoallocMaxCells)
+    return fail("tecs_force_pass_noalloc: " + std::to_string(n) + " cells exceed the allocation-free limit of " +
+                std::to_string(kNoallocMaxCells));
+  // grid of binned_gabriel.hpp:28-42 / grid.hpp:201-215
+  tecs_sim s;
+  s.d = *desc;
+  GridP& g = s.g;
+  g.bin_size = desc->bin_size_scale * desc->cutoff;
+  g.inv_bin = 1.0f / g.bin_size;
+  g.R = (int)std::ceil(desc->cutoff * g.inv_bin);
+  unsigned long long nb = 1;
+  for (int k = 0; k < 3; ++k) { g.mn[k] = 0.f; g.ext[k] = 1; }
+  for (int k = 0; k < desc->dims; ++k) {
+    g.mn[k] = desc->min_bounds[k];
+    g.ext[k] = (int)std::ceil((desc->max_bounds[k] - desc->min_bounds[k]) / g.bin_size);
+    if (g.ext[k] < 1) return fail("max_bounds must exceed min_bounds");
+    nb *= (unsigned long long)g.ext[k];
+  }
+  if (nb > kNoallocMaxBins)
+    return fail("tecs_force_pass_noalloc: " + std::to_string(nb) + " bins exceed the allocation-free limit of " +
+                std::to_string(kNoallocMaxBins));
+  g.nbins = (unsigned)nb;
+  ForceP& f = s.fp;
+  f.force = desc->force;
+  f.k_rep = desc->k_rep; f.r_rep = desc->r_rep; f.k_adh = desc->k_adh; f.r_adh = desc->r_adh; f.k_pol = 0.f;
+  f.rc2 = desc->cutoff * desc->cutoff;
+  f.gab_factor = desc->gabriel_coefficient * desc->gabriel_coefficient * 0.25f;
+  f.gab_csq = desc->gabriel_coefficient * desc->gabriel_coefficient;
+  s.binned = true;
+  s.fuse_count = false;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  unsigned char* base = nullptr;
+  if (noalloc_scratch(dev, &base)) return -1;
+  s.stream = (cudaStream_t)stream;
+  s.d.capacity = n ? n : 1;
+  s.d.division_probability = 0.0;
+  s.n_host = n;
+  s.ctr = (Counters*)(base + kOffCtr);
+  s.A = (float4*)(base + kOffA);
+  s.B = (float4*)(base + kOffB);
+  s.d1 = (float4*)(base + kOffD);
+  s.key = (unsigned*)(base + kOffKey);
+  s.rank = (unsigned*)(base + kOffRank);
+  s.src = (unsigned*)(base + kOffSrc);
+  s.cnt = (unsigned*)(base + kOffCnt);
+  s.off = (unsigned*)(base + kOffOff);
+  s.part = (unsigned*)(base + kOffPart);
+  // what must start at zero: the counters and the bin counts
+  k_noalloc_reset<<<1, 32, 0, s.stream>>>(s.ctr, n);
+  CK(cudaMemsetAsync(s.cnt, 0, ((size_t)g.nbins + 1) * 4, s.stream));
+  if (n == 0) {
+    CK(cudaGetLastError());
+    return 0;
+  }
+  k_pack<<<ceil_div(n, 256), 256, 0, s.stream>>>(d_positions, n, desc->dims, s.A);
+  int K = 0;
+  s.stream = (cudaStream_t)stream;
+  if (enqueue_rebuild(&s, K, true)) return -1;
+  PassArgs a = base_args(&s, 0.f);
+  a.X = s.B;
+  a.P = nullptr;
+  a.mode = kStore;
+  a.d_out = s.d1;
+  a.dp_out = nullptr;
+  a.count_next = 0;
+  if (enqueue_pass(&s, a, K)) return -1;
+  k_unpack<<<ceil_div(n, 256), 256, 0, s.stream>>>(s.B, s.d1, n, desc->dims, d_deltas);
+  CK(cudaGetLastError());
+  return 0;
+}
