@@ -67,6 +67,10 @@ struct PassArgs {
   unsigned long long pair_cap;
   // Gabriel fast path allowed (gabriel_coefficient <= 0.9 and bin size >= cutoff)
   int gabriel_fast;
+  // packed bin coordinates of the sorted cells (x | y << 10 | z << 20), or null
+  const unsigned* binc;
+  // 1 when X is not the array the bins were built from (Heun pass 2)
+  int stale_bins;
   // bin count of the next step's rebuild, fused into the state write
   int count_next;
   unsigned* key;
@@ -178,10 +182,10 @@ __global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __re
 // lo + (number of cells of its bin with a smaller id), so every bin lists its
 // cells in ascending id -- the order of Kokkos BinSort's binning loop on the
 // Serial backend.  Single-cell bins (most of them) copy straight through.
-__global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
+__global__ void k_order_gather(GridP g, const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
                                const unsigned* __restrict__ off, const unsigned* __restrict__ src,
                                const float4* __restrict__ A, const float2* __restrict__ PA, float4* __restrict__ B,
-                               float2* __restrict__ PB) {
+                               float2* __restrict__ PB, unsigned* __restrict__ binc) {
   const unsigned n = ctr->n;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const unsigned s = src[t];
@@ -197,6 +201,11 @@ __global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned*
     }
     B[dst] = v;
     if (PB) PB[dst] = PA[s];
+    if (binc) {
+      const unsigned e0 = (unsigned)g.ext[0], e1 = (unsigned)g.ext[1];
+      const unsigned bx = b % e0, q = b / e0;
+      binc[dst] = bx | ((q % e1) << 10) | ((q / e1) << 20);
+    }
   }
 }
 
@@ -664,19 +673,9 @@ __device__ __noinline__ void cell_general(const GridP& g, const ForceP& fp, cons
 // summation order, so the sums stay bit-identical.  Cells with more than
 // kMaxNb neighbours, or whose witness ball leaves the 3x3x3 bin block, take
 // the general path in phase 4.
-template <int D>
-__device__ __forceinline__ unsigned ball_mask27(const int* lo, const int* hi) {
-  // bit (rx+1) + 3(ry+1) + 9(rz+1) set when the bin offset (rx, ry, rz) lies in [lo, hi]
-  unsigned m3[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    if (d < D) m3[d] = ((1u << (hi[d] + 2)) - 1u) & ~((1u << (lo[d] + 1)) - 1u);
-    else m3[d] = 2u;  // unused dimension: offset 0 only
-  }
-  const unsigned plane = ((m3[1] & 1u) ? m3[0] : 0u) | ((m3[1] & 2u) ? m3[0] << 3 : 0u) |
-                         ((m3[1] & 4u) ? m3[0] << 6 : 0u);
-  return ((m3[2] & 1u) ? plane : 0u) | ((m3[2] & 2u) ? plane << 9 : 0u) | ((m3[2] & 4u) ? plane << 18 : 0u);
-}
+// candidate slot (q, cell c) in shared memory, XOR-swizzled so that threads
+// reading different q of the same cell hit different banks
+__device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c ^ q); }
 
 template <int D, int FORCE>
 __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
@@ -704,7 +703,13 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
     vi = __ldg(&a.X[i]);
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
-    bin_coords_div<D>(g, xi, bc);
+    if (a.binc && !a.stale_bins) {
+      // the sort already binned this position with the same formula
+      const unsigned pb = __ldg(&a.binc[i]);
+      bc[0] = (int)(pb & 1023u); bc[1] = (int)((pb >> 10) & 1023u); bc[2] = (int)(pb >> 20);
+    } else {
+      bin_coords_div<D>(g, xi, bc);
+    }
     const int z0 = D >= 3 ? -1 : 0, z1 = D >= 3 ? 1 : 0;
     for (int dz = z0; dz <= z1 && !fb; ++dz) {
       const int cz = D >= 3 ? bc[2] + dz : 0;
@@ -716,9 +721,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
         int c0[3] = {x0, cy, cz};
         const unsigned b0 = flatten<D>(g, c0);
         const unsigned o0 = __ldg(&a.off[b0]);
-        const unsigned o1 = __ldg(&a.off[b0 + 1]);
-        const unsigned o2 = x1 >= x0 + 1 ? __ldg(&a.off[b0 + 2]) : o1;
-        const unsigned o3 = x1 >= x0 + 2 ? __ldg(&a.off[b0 + 3]) : o2;
+        const unsigned o3 = __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]);
         const unsigned rowcode = 3u * (unsigned)(dy + 1) + 9u * (unsigned)(D >= 3 ? dz + 1 : 1);
         for (unsigned j = o0; j < o3; ++j) {
           if (j == i) continue;
@@ -728,8 +731,15 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
           if (D >= 3) { const float e2 = xi[2] - vj.z; d2 = d2 + e2 * e2; }
           if (d2 >= fp.rc2) continue;
           if (cnt == kMaxNb) { fb = true; break; }
-          const unsigned rx = (unsigned)(x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0] + 1);
-          cand[cnt * kPassThreads + t] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 5) | (rowcode + rx)));
+          unsigned rx;
+          if (a.binc) {
+            rx = (unsigned)((int)(__ldg(&a.binc[j]) & 1023u) - bc[0] + 1);
+          } else {
+            const unsigned o1 = __ldg(&a.off[b0 + 1]);
+            const unsigned o2 = x1 >= x0 + 1 ? __ldg(&a.off[b0 + 2]) : o1;
+            rx = (unsigned)(x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0] + 1);
+          }
+          cand[cix(cnt, t)] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 5) | (rowcode + rx)));
           ++cnt;
         }
       }
@@ -758,14 +768,15 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
   for (int q = 0; q < cnt; ++q) pinfo[pofs[t] + q] = (unsigned short)((t << 4) | q);
   __syncthreads();
   const int P = pofs[kPassThreads];
-  // ---- phase 2: Gabriel test, one pair per thread at a time
+  // ---- phase 2: Gabriel test, one pair per thread at a time.  A witness k
+  // blocks (i, j) when it is inside the ball (|x_k - m|^2 < r^2) and its bin
+  // lies in the ball's bin range; the range (sqrt + floors) is only worked out
+  // for the rare k that pass the distance test.
   for (int p = t; p < P; p += kPassThreads) {
     const unsigned info = pinfo[p];
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const float4 h = home[c];
-    const float4 vj = cand[q * kPassThreads + c];
-    const unsigned hb = __float_as_uint(h.w);
-    const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
+    const float4 vj = cand[cix(q, c)];
     const float hx[3] = {h.x, h.y, h.z};
     float disp[3];
     disp[0] = hx[0] - vj.x;
@@ -777,30 +788,29 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
 #pragma unroll
     for (int d = 0; d < D; ++d) m[d] = hx[d] - disp[d] * 0.5f;
     const float rsq = d2 * fp.gab_factor;
-    const float r = sqrtf(rsq);
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    bool out = false;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      lo[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-      hi[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-      out = out || lo[d] < -1 || hi[d] > 1;
-    }
-    if (out) {
-      fallback[c] = 1;
-      continue;
-    }
-    const unsigned mask = ball_mask27<D>(lo, hi);
     const int cc = ncnt[c];
     bool blocked = false;
     for (int w = 0; w < cc; ++w) {
       if (w == q) continue;
-      const float4 vk = cand[w * kPassThreads + c];
-      if (!((mask >> (__float_as_uint(vk.w) & 31u)) & 1u)) continue;
+      const float4 vk = cand[cix(w, c)];
       const float f0 = vk.x - m[0], f1 = vk.y - m[1];
-      float s = f0 * f0 + f1 * f1;
-      if (D >= 3) { const float f2 = vk.z - m[2]; s = s + f2 * f2; }
-      if (s < rsq) { blocked = true; break; }
+      float sd = f0 * f0 + f1 * f1;
+      if (D >= 3) { const float f2 = vk.z - m[2]; sd = sd + f2 * f2; }
+      if (!(sd < rsq)) continue;
+      // binned_gabriel.hpp:142-153: the bins overlapping the ball
+      const unsigned hb = __float_as_uint(h.w);
+      const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
+      const unsigned code = __float_as_uint(vk.w) & 31u;
+      const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
+      const float r = sqrtf(rsq);
+      bool inside = true;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const int lo = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+        const int hi = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+        inside = inside && rel[d] >= lo && rel[d] <= hi;
+      }
+      if (inside) { blocked = true; break; }
     }
     if (!blocked) pinfo[p] = (unsigned short)(info | 0x8000u);
   }
@@ -811,7 +821,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
     if (!(info & 0x8000u) || fallback[c]) continue;
     const float4 h = home[c];
-    const float4 vj = cand[q * kPassThreads + c];
+    const float4 vj = cand[cix(q, c)];
     float disp[3];
     disp[0] = h.x - vj.x;
     disp[1] = h.y - vj.y;
@@ -833,7 +843,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
       f.y = (disp[1] * F) / dist;
       if (D >= 3) f.z = (disp[2] * F) / dist;
     }
-    cand[q * kPassThreads + c] = f;
+    cand[cix(q, c)] = f;
   }
   __syncthreads();
   // ---- phase 4: ordered per-cell sums
@@ -845,7 +855,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
       const int base = pofs[t];
       for (int q = 0; q < cnt; ++q) {
         if (!(pinfo[base + q] & 0x8000u)) continue;
-        const float4 f = cand[q * kPassThreads + t];
+        const float4 f = cand[cix(q, t)];
         acc.x[0] = acc.x[0] + f.x;
         acc.x[1] = acc.x[1] + f.y;
         if (D >= 3) acc.x[2] = acc.x[2] + f.z;

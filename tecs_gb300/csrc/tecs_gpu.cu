@@ -81,6 +81,7 @@ struct tecs_sim {
   float2 *PA = nullptr, *PB = nullptr, *Pt = nullptr, *dp1 = nullptr, *dp2 = nullptr;
   unsigned *key = nullptr, *rank = nullptr, *src = nullptr, *cnt = nullptr, *off = nullptr, *part = nullptr;
   unsigned *div_parent = nullptr, *div_slot = nullptr;
+  unsigned* binc = nullptr;  // packed bin coordinates of B's cells
   Counters* ctr = nullptr;
   double* com_part = nullptr;
   float* com = nullptr;  // [0..2] pass 1, [4..6] pass 2
@@ -176,6 +177,8 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   // the fast Gabriel path needs every witness inside i's cutoff ball and 3x3x3 bin block
   a.gabriel_fast = (s->d.gabriel_coefficient <= 0.9f && s->g.R == 1 && s->g.bin_size >= s->d.cutoff) ? 1 : 0;
   a.count_next = s->fuse_count ? 1 : 0;
+  a.binc = s->binc;
+  a.stale_bins = 0;
   a.key = s->key;
   a.rank = s->rank;
   a.cnt = s->cnt;
@@ -208,7 +211,7 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
-    k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB);
+    k_order_gather<<<gb, 256, 0, s->stream>>>(s->g, s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->binc);
     PROF_END(s, "k_order_gather");
     K += 4;
   } else {
@@ -252,6 +255,9 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     if (pol) CK(cudaMemcpyAsync(s->PB, s->PA, sizeof(float2) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
   }
   PassArgs a = base_args(s, dt);
+  // positions no longer match the bins they were sorted by: a step without a
+  // rebuild (rebuild_every_n > 1), and every Heun second pass
+  a.stale_bins = rebuild ? 0 : 1;
   auto store_args = [&](PassArgs& p, float4* dout, float2* dpout, int slot) {
     p.mode = kStore;
     p.d_out = dout;
@@ -328,6 +334,7 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     PassArgs p2 = a;
     p2.X = s->Xt;
     p2.P = pol ? s->Pt : nullptr;
+    p2.stale_bins = 1;
     if (fused) {
       p2.mode = kHeun2Fused;
       p2.Bx = s->B;
@@ -442,6 +449,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
          alloc((void**)&s->dp1, cap * 8) && alloc((void**)&s->dp2, cap * 8);
   ok = ok && alloc((void**)&s->key, cap * 4) && alloc((void**)&s->rank, cap * 4) && alloc((void**)&s->src, cap * 4);
   ok = ok && alloc((void**)&s->div_parent, cap * 4) && alloc((void**)&s->div_slot, cap * 4);
+  if (s->binned && g.ext[0] <= 1024 && g.ext[1] <= 1024 && g.ext[2] <= 1024) ok = ok && alloc((void**)&s->binc, cap * 4);
   if (s->binned) {
     const size_t len = (size_t)g.nbins + 1;
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
@@ -469,7 +477,8 @@ int tecs_sim_destroy(tecs_sim* s) {
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
-                  s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage};
+                  s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
+                  s->binc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
