@@ -56,8 +56,10 @@ struct PassArgs {
   float* com_out;       // 3 floats
   int com_slot;         // 0 or 1 (which done counter)
   unsigned capacity;
-  // division (fused into kEulerFused / kHeun2Fused)
-  double div_p;
+  // division (fused into kEulerFused / kHeun2Fused): a cell divides when
+  // (hash >> 11) <= div_thresh = floor(p * 2^53), i.e. u01(hash) <= p exactly
+  int div_enabled;
+  unsigned long long div_thresh;
   float div_offset;
   unsigned long long seed;
   unsigned* div_parent;
@@ -224,8 +226,16 @@ __global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __r
 // ---------------------------------------------------------------------------
 // block reduction of the COM partials + last-block finalisation
 
-__device__ void com_reduce_block(const PassArgs& a, double x, double y, double z) {
-  __shared__ double sh[3][32];
+// Centre-of-mass partial sums in 64-bit fixed point (2^-32 units): integer
+// addition is associative, so the sum -- and the mean -- is the same whatever
+// order the blocks finish in, and no FP64 (slow on this part) is needed.  Each
+// block adds its totals to three global accumulators; the last block forms
+// mean = sum / capacity (com_fixers.hpp:43 divides by the stage view's extent,
+// i.e. the capacity) and clears the accumulators for the next use.
+__device__ __forceinline__ long long com_fixed(float v) { return __float2ll_rn(v * 4294967296.0f); }
+
+__device__ void com_reduce_block(const PassArgs& a, long long x, long long y, long long z) {
+  __shared__ long long sh[3][32];
   __shared__ bool last;
   for (int o = 16; o > 0; o >>= 1) {
     x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -235,41 +245,24 @@ __device__ void com_reduce_block(const PassArgs& a, double x, double y, double z
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (lane == 0) { sh[0][warp] = x; sh[1][warp] = y; sh[2][warp] = z; }
   __syncthreads();
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(a.com_part) + 3 * a.com_slot;
   if (threadIdx.x == 0) {
-    double sx = 0, sy = 0, sz = 0;
+    long long sx = 0, sy = 0, sz = 0;
     for (int w = 0; w < nw; ++w) { sx += sh[0][w]; sy += sh[1][w]; sz += sh[2][w]; }
-    a.com_part[3 * blockIdx.x + 0] = sx;
-    a.com_part[3 * blockIdx.x + 1] = sy;
-    a.com_part[3 * blockIdx.x + 2] = sz;
+    atomicAdd(&acc[0], (unsigned long long)sx);
+    atomicAdd(&acc[1], (unsigned long long)sy);
+    atomicAdd(&acc[2], (unsigned long long)sz);
     __threadfence();
-    unsigned prev = atomicAdd(&a.ctr->done[a.com_slot], 1u);
-    last = (prev == gridDim.x - 1);
+    last = atomicAdd(&a.ctr->done[a.com_slot], 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last) return;
-  // fixed summation order over blocks: deterministic result
-  double sx = 0, sy = 0, sz = 0;
-  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-    sx += __ldcg(&a.com_part[3 * b + 0]);
-    sy += __ldcg(&a.com_part[3 * b + 1]);
-    sz += __ldcg(&a.com_part[3 * b + 2]);
-  }
-  __syncthreads();
-  for (int o = 16; o > 0; o >>= 1) {
-    sx += __shfl_xor_sync(0xffffffffu, sx, o);
-    sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    sz += __shfl_xor_sync(0xffffffffu, sz, o);
-  }
-  if (lane == 0) { sh[0][warp] = sx; sh[1][warp] = sy; sh[2][warp] = sz; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double tx = 0, ty = 0, tz = 0;
-    for (int w = 0; w < nw; ++w) { tx += sh[0][w]; ty += sh[1][w]; tz += sh[2][w]; }
-    // com_fixers.hpp:43: mean over the stage view's extent, i.e. the capacity
-    const double cap = (double)a.capacity;
-    a.com_out[0] = (float)(tx / cap);
-    a.com_out[1] = (float)(ty / cap);
-    a.com_out[2] = (float)(tz / cap);
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const double scale = 1.0 / (4294967296.0 * (double)a.capacity);
+    for (int d = 0; d < 3; ++d) {
+      const long long v = (long long)atomicExch(&acc[d], 0ull);
+      a.com_out[d] = (float)((double)v * scale);
+    }
     a.ctr->done[a.com_slot] = 0u;
   }
 }
@@ -291,9 +284,8 @@ __device__ __forceinline__ void count_cell(const GridP& g, const PassArgs& a, un
 template <int D>
 __device__ __forceinline__ void maybe_divide(const GridP& g, const PassArgs& a, unsigned n, unsigned id,
                                              const float* xnew, float2 pnew, unsigned long long step) {
-  if (a.div_p <= 0.0) return;
-  double u = u01(hash64(a.seed, step, id, 0));
-  if (u > a.div_p) return;
+  if (!a.div_enabled) return;
+  if ((hash64(a.seed, step, id, 0) >> 11) > a.div_thresh) return;
   unsigned k = atomicAdd(&a.ctr->div_count, 1u);
   unsigned slot = n + k;
   if (slot >= a.capacity) { atomicOr(&a.ctr->error, 1u); return; }
@@ -440,8 +432,8 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
       a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
       if (a.dp_out) a.dp_out[i] = make_float2(sp0, sp1);
     }
-    if (a.com_part) com_reduce_block(a, active ? (double)s[0] : 0.0, active ? (double)s[1] : 0.0,
-                                     active ? (double)s[2] : 0.0);
+    if (a.com_part) com_reduce_block(a, active ? com_fixed(s[0]) : 0ll, active ? com_fixed(s[1]) : 0ll,
+                                     active ? com_fixed(s[2]) : 0ll);
     return;
   }
   if (!active) return;
@@ -596,7 +588,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
 }
 
 template <int D, int FINDER, int FORCE>
-__device__ __noinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+__device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
                                           const float* xi, float2 pi, unsigned idi, Acc& acc);
 
 template <int D, int FINDER, int FORCE>
@@ -628,7 +620,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(GridP g, ForceP fp, PassA
 
 // The general path: the reference's loops (27 bins, then the ball's bins per pair).
 template <int D, int FINDER, int FORCE>
-__device__ __noinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+__device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
                                           const float* xi, float2 pi, unsigned idi, Acc& acc) {
     if (FINDER == 1 || FINDER == 3) {
       int bc[3] = {0, 0, 0};
@@ -934,10 +926,10 @@ __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a
 // Plain COM reduction over a delta buffer (used after the symmetric pass).
 __global__ void k_com(const float4* __restrict__ d, PassArgs a) {
   const unsigned n = a.ctr->n;
-  double x = 0, y = 0, z = 0;
+  long long x = 0, y = 0, z = 0;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 v = d[i];
-    x += v.x; y += v.y; z += v.z;
+    x += com_fixed(v.x); y += com_fixed(v.y); z += com_fixed(v.z);
   }
   com_reduce_block(a, x, y, z);
 }

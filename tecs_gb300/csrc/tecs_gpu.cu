@@ -15,6 +15,7 @@
 // and, by default, captures that sequence once as a CUDA graph and replays it.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -167,7 +168,11 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.ctr = s->ctr;
   a.dt = dt;
   a.capacity = s->d.capacity;
-  a.div_p = s->d.division_probability;
+  a.div_enabled = s->d.division_probability > 0.0 ? 1 : 0;
+  {
+    const double p = s->d.division_probability;
+    a.div_thresh = p >= 1.0 ? ~0ull : (p > 0.0 ? (unsigned long long)std::floor(p * 9007199254740992.0) : 0ull);
+  }
   a.div_offset = s->d.division_offset;
   a.seed = s->d.seed;
   a.div_parent = s->div_parent;
@@ -455,11 +460,13 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
          alloc((void**)&s->part, (size_t)ceil_div(len, kScanChunk) * 4);
   }
-  const size_t pass_blocks = ceil_div(cap, 128);
+  // COM accumulators: 3 per reduction slot, two slots (Heun's two passes)
+  const size_t pass_blocks = std::max<size_t>(ceil_div(cap, 128), 2);
   ok = ok && alloc((void**)&s->ctr, sizeof(Counters)) && alloc((void**)&s->com_part, pass_blocks * 3 * 8) &&
        alloc((void**)&s->com, 8 * 4) && alloc((void**)&s->stage, cap * 4 * 4);
   if (ok && s->cnt) ok = cudaMemset(s->cnt, 0, ((size_t)g.nbins + 1) * 4) == cudaSuccess;
-  if (ok) ok = cudaMemset(s->ctr, 0, sizeof(Counters)) == cudaSuccess && cudaMemset(s->com, 0, 32) == cudaSuccess;
+  if (ok) ok = cudaMemset(s->ctr, 0, sizeof(Counters)) == cudaSuccess && cudaMemset(s->com, 0, 32) == cudaSuccess &&
+               cudaMemset(s->com_part, 0, pass_blocks * 3 * 8) == cudaSuccess;
   if (!ok) {
     std::string m = std::string("device allocation failed: ") + cudaGetErrorString(cudaGetLastError());
     tecs_sim_destroy(s);
