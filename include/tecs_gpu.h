@@ -136,6 +136,55 @@ const char* tecs_sim_profile_name(tecs_sim* sim, int index);
 /* Number of kernels one step launches (for launch accounting). */
 int tecs_sim_kernels_per_step(tecs_sim* sim, int* kernels);
 
+/* ------------------------------------------------------------------------
+ * Engine: many independent simulations advanced together (batched ensemble,
+ * served requests).  No counterpart in the reference, which runs one
+ * Simulation after another (include/utils/runtime_guard.hpp:26-99 shares the
+ * runtime, nothing more).  Each resident simulation is described by the same
+ * tecs_sim_desc as a single one (3-D, binned finder, non-symmetric, no COM
+ * fix, no division; bin_size_scale >= 1) and evolves exactly as a
+ * tecs_sim_step run of it would.  One tecs_engine_step advances every
+ * resident simulation by one step of its own integrator in one CUDA graph.
+ * ------------------------------------------------------------------------ */
+typedef struct tecs_engine_desc {
+  unsigned cell_capacity;   /* cells of all resident simulations together */
+  unsigned bin_capacity;    /* bins of all resident simulations together  */
+  unsigned max_sims;        /* resident simulations at most               */
+  int device;
+} tecs_engine_desc;
+
+typedef struct tecs_engine tecs_engine;
+
+int tecs_engine_desc_default(tecs_engine_desc* desc);
+int tecs_engine_create(const tecs_engine_desc* desc, tecs_engine** out);
+int tecs_engine_destroy(tecs_engine* engine);
+/* Bins a simulation described by desc occupies in the engine. */
+int tecs_engine_bins_needed(const tecs_sim_desc* desc, unsigned* nbins);
+/* Free cells and the largest free run of bins (admission by free capacity). */
+int tecs_engine_free(tecs_engine* engine, unsigned* free_cells, unsigned* largest_free_bins);
+/* Admit a simulation with its initial state (host memory); *slot names it. */
+int tecs_engine_add(tecs_engine* engine, const tecs_sim_desc* desc, const float* positions, const float* polarity,
+                    unsigned n, int* slot);
+/* Retire a simulation; its cells and bins are released by the next step. */
+int tecs_engine_remove(tecs_engine* engine, int slot);
+/* n_steps steps of every resident simulation (asynchronous). */
+int tecs_engine_step(tecs_engine* engine, double dt, int n_steps);
+int tecs_engine_synchronize(tecs_engine* engine);
+/* Resident cells and simulations. */
+int tecs_engine_count(tecs_engine* engine, unsigned* cells, unsigned* sims);
+/* One simulation's state in cell-id order (synchronises). */
+int tecs_engine_download(tecs_engine* engine, int slot, float* positions, float* polarity, unsigned* n);
+/* Snapshot into pinned host buffers without stalling the step stream: the
+ * cells are unpacked on the device (into staging cells [stage_offset,
+ * stage_offset + n)) and copied on a side stream; *event (a cudaEvent_t)
+ * completes when the host buffers hold the data. */
+int tecs_engine_snapshot_async(tecs_engine* engine, int slot, float* pinned_positions, float* pinned_polarity,
+                               unsigned stage_offset, void** event);
+int tecs_engine_event_query(void* event, int* ready);
+int tecs_engine_event_destroy(void* event);
+int tecs_engine_kernels_per_step(tecs_engine* engine, int* kernels);
+void* tecs_engine_stream(tecs_engine* engine);
+
 /* Limits of tecs_force_pass_noalloc (its scratch is a fixed static device array). */
 #define TECS_NOALLOC_MAX_CELLS 65536u
 #define TECS_NOALLOC_MAX_BINS 262144u

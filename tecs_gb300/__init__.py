@@ -169,6 +169,41 @@ class Settings:
     pair_finder_settings: PairFinderSettings = field(default_factory=PairFinderSettings)
 
 
+def make_desc(settings: Settings, *, dims: int = 3, pair_finder: str = "binned_gabriel", symmetric: bool = False,
+              integrator: str = "heun", com_fixer: Optional[str] = None, force=Spring2R(), polarity: bool = False,
+              division: Division = Division(), device: int = 0) -> SimDesc:
+    """tecs_sim_desc for a configuration named the reference's way."""
+    L = load()
+    d = SimDesc()
+    _check(L.tecs_sim_desc_default(ctypes.byref(d)))
+    pf = settings.pair_finder_settings
+    d.dims = dims
+    d.finder = FINDERS[pair_finder]
+    d.symmetric = int(symmetric)
+    d.cutoff = settings.cutoff_distance
+    d.gabriel_coefficient = pf.gabriel_coefficient
+    for k in range(3):
+        d.min_bounds[k] = float(pf.min_bounds[k]) if k < len(pf.min_bounds) else 0.0
+        d.max_bounds[k] = float(pf.max_bounds[k]) if k < len(pf.max_bounds) else 0.0
+    d.bin_size_scale = pf.bin_size_scale
+    d.rebuild_every_n = pf.rebuild_every_n
+    d.integrator = INTEGRATORS[integrator]
+    d.com_fix = 1 if com_fixer else 0
+    if force is None:
+        d.force = FORCE_NONE
+    else:
+        d.force = FORCE_POLARITY if isinstance(force, PolaritySpring) else FORCE_SPRING2R
+        d.k_rep, d.r_rep, d.k_adh, d.r_adh = force.k_rep, force.r_rep, force.k_adh, force.r_adh
+        d.k_pol = getattr(force, "k_pol", 0.0)
+    d.has_polarity = int(polarity)
+    d.capacity = max(settings.capacity, settings.agent_count)
+    d.division_probability = division.probability
+    d.division_offset = division.offset
+    d.seed = settings.seed
+    d.device = device
+    return d
+
+
 class Simulation:
     """One simulation resident on a GB300: the reference's Simulation<Config>.
 
@@ -182,33 +217,8 @@ class Simulation:
                  force=Spring2R(), polarity: bool = False, division: Division = Division(), device: int = 0,
                  graph: bool = True):
         L = load()
-        d = SimDesc()
-        _check(L.tecs_sim_desc_default(ctypes.byref(d)))
-        pf = settings.pair_finder_settings
-        d.dims = dims
-        d.finder = FINDERS[pair_finder]
-        d.symmetric = int(symmetric)
-        d.cutoff = settings.cutoff_distance
-        d.gabriel_coefficient = pf.gabriel_coefficient
-        for k in range(3):
-            d.min_bounds[k] = float(pf.min_bounds[k]) if k < len(pf.min_bounds) else 0.0
-            d.max_bounds[k] = float(pf.max_bounds[k]) if k < len(pf.max_bounds) else 0.0
-        d.bin_size_scale = pf.bin_size_scale
-        d.rebuild_every_n = pf.rebuild_every_n
-        d.integrator = INTEGRATORS[integrator]
-        d.com_fix = 1 if com_fixer else 0
-        if force is None:
-            d.force = FORCE_NONE
-        else:
-            d.force = FORCE_POLARITY if isinstance(force, PolaritySpring) else FORCE_SPRING2R
-            d.k_rep, d.r_rep, d.k_adh, d.r_adh = force.k_rep, force.r_rep, force.k_adh, force.r_adh
-            d.k_pol = getattr(force, "k_pol", 0.0)
-        d.has_polarity = int(polarity)
-        d.capacity = max(settings.capacity, settings.agent_count)
-        d.division_probability = division.probability
-        d.division_offset = division.offset
-        d.seed = settings.seed
-        d.device = device
+        d = make_desc(settings, dims=dims, pair_finder=pair_finder, symmetric=symmetric, integrator=integrator,
+                      com_fixer=com_fixer, force=force, polarity=polarity, division=division, device=device)
         self.desc = d
         self.dims = dims
         self.polarity = polarity

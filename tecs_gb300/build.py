@@ -38,8 +38,21 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     newest = max(p.stat().st_mtime for p in sources())
     if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
         return LIB
+    # one object per translation unit, compiled in parallel, then one shared library
+    units = sorted(CSRC.glob("*.cu"))
+    objs, procs = [], []
+    for u in units:
+        obj = BUILD / (u.stem + ".o")
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS[:-1], "-c", str(u), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append(subprocess.Popen(cmd))
+        objs.append(obj)
+    failed = [p.wait() for p in procs]
+    if any(failed):
+        raise subprocess.CalledProcessError(max(failed), "nvcc")
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, str(CSRC / "tecs_gpu.cu"), "-o", str(tmp)]
+    cmd = [nvcc(), *ARCH, "-shared", *map(str, objs), "-o", str(tmp)]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.run(cmd, check=True)

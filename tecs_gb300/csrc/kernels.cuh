@@ -69,10 +69,9 @@ struct PassArgs {
   unsigned long long pair_cap;
   // Gabriel fast path allowed (gabriel_coefficient <= 0.9 and bin size >= cutoff)
   int gabriel_fast;
-  // packed bin coordinates of the sorted cells (x | y << 10 | z << 20), or null
-  const unsigned* binc;
-  // 1 when X is not the array the bins were built from (Heun pass 2)
-  int stale_bins;
+  // cell ids of the sorted slots (binned finders keep the bin key in X.w);
+  // null when X.w holds the id (naive finders)
+  const unsigned* Bid;
   // bin count of the next step's rebuild, fused into the state write
   int count_next;
   unsigned* key;
@@ -83,7 +82,7 @@ struct PassArgs {
 // ---------------------------------------------------------------------------
 // binning: key + count, exclusive scan, scatter, per-bin id sort + gather
 
-__global__ void k_count(const float4* __restrict__ A, const Counters* __restrict__ ctr, GridP g, int dims,
+static __global__ void k_count(const float4* __restrict__ A, const Counters* __restrict__ ctr, GridP g, int dims,
                         unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt) {
   const unsigned n = ctr->n;
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -120,7 +119,7 @@ __device__ __forceinline__ unsigned block_sum(unsigned v, unsigned* sh) {
 }
 
 // Per-chunk totals of cnt[0..len).
-__global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned len, unsigned* __restrict__ part) {
+static __global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned len, unsigned* __restrict__ part) {
   __shared__ unsigned sh[32];
   const unsigned base = blockIdx.x * kScanChunk;
   unsigned v = 0;
@@ -136,7 +135,7 @@ __global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned len, un
 // owns 512 consecutive counts, read 32 at a time (coalesced): a first sweep
 // forms the warp totals, the block combines them with the earlier chunks'
 // totals, a second sweep (L1 hits) scans and writes.
-__global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, const unsigned* __restrict__ part,
+static __global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, const unsigned* __restrict__ part,
                              unsigned* __restrict__ off) {
   __shared__ unsigned sh[32];
   __shared__ unsigned wtot[kScanThreads / 32];
@@ -172,7 +171,7 @@ __global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, const uns
   }
 }
 
-__global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
+static __global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
                           const unsigned* __restrict__ rank, const unsigned* __restrict__ off,
                           unsigned* __restrict__ src) {
   const unsigned n = ctr->n;
@@ -180,14 +179,19 @@ __global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __re
     src[off[key[s]] + rank[s]] = s;
 }
 
+// id of sorted slot j
+__device__ __forceinline__ unsigned id_at(const float4* X, const unsigned* Bid, unsigned j) {
+  return Bid ? __ldg(&Bid[j]) : id_of(__ldg(&X[j]));
+}
+
 // One thread per sorted slot: the cell that the scatter put at slot t moves to
 // lo + (number of cells of its bin with a smaller id), so every bin lists its
 // cells in ascending id -- the order of Kokkos BinSort's binning loop on the
 // Serial backend.  Single-cell bins (most of them) copy straight through.
-__global__ void k_order_gather(GridP g, const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
-                               const unsigned* __restrict__ off, const unsigned* __restrict__ src,
-                               const float4* __restrict__ A, const float2* __restrict__ PA, float4* __restrict__ B,
-                               float2* __restrict__ PB, unsigned* __restrict__ binc) {
+static __global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
+                                      const unsigned* __restrict__ off, const unsigned* __restrict__ src,
+                                      const float4* __restrict__ A, const float2* __restrict__ PA,
+                                      float4* __restrict__ B, float2* __restrict__ PB, unsigned* __restrict__ Bid) {
   const unsigned n = ctr->n;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const unsigned s = src[t];
@@ -201,18 +205,28 @@ __global__ void k_order_gather(GridP g, const Counters* __restrict__ ctr, const 
       for (unsigned k = lo; k < hi; ++k) r += id_of(A[src[k]]) < me ? 1u : 0u;
       dst = lo + r;
     }
-    B[dst] = v;
+    // the sorted copy carries the bin key in w (read by the passes with the
+    // position); the id moves to Bid
+    B[dst] = make_float4(v.x, v.y, v.z, __uint_as_float(b));
+    Bid[dst] = id_of(v);
     if (PB) PB[dst] = PA[s];
-    if (binc) {
-      const unsigned e0 = (unsigned)g.ext[0], e1 = (unsigned)g.ext[1];
-      const unsigned bx = b % e0, q = b / e0;
-      binc[dst] = bx | ((q % e1) << 10) | ((q / e1) << 20);
-    }
+  }
+}
+
+// A step without a rebuild (rebuild_every_n > 1): the working copy takes the
+// new positions in the same slot order and keeps each slot's bin key in w.
+static __global__ void k_refresh(const Counters* __restrict__ ctr, const float4* __restrict__ A,
+                                 const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const float4 v = A[s];
+    B[s] = make_float4(v.x, v.y, v.z, B[s].w);
+    if (PB) PB[s] = PA[s];
   }
 }
 
 // Naive finders keep the working copy in cell-id order.
-__global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __restrict__ A,
+static __global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __restrict__ A,
                              const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB) {
   const unsigned n = ctr->n;
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -234,7 +248,7 @@ __global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __r
 // i.e. the capacity) and clears the accumulators for the next use.
 __device__ __forceinline__ long long com_fixed(float v) { return __float2ll_rn(v * 4294967296.0f); }
 
-__device__ void com_reduce_block(const PassArgs& a, long long x, long long y, long long z) {
+static __device__ void com_reduce_block(const PassArgs& a, long long x, long long y, long long z) {
   __shared__ long long sh[3][32];
   __shared__ bool last;
   for (int o = 16; o > 0; o >>= 1) {
@@ -309,7 +323,7 @@ __device__ __forceinline__ void maybe_divide(const GridP& g, const PassArgs& a, 
 
 // Daughter ids: n + rank of the parent id among this step's parents, then
 // (last block) n += daughters.  Deterministic: ids depend only on parent ids.
-__global__ void k_divide_commit(Counters* __restrict__ ctr, unsigned capacity, const unsigned* __restrict__ parent,
+static __global__ void k_divide_commit(Counters* __restrict__ ctr, unsigned capacity, const unsigned* __restrict__ parent,
                                 const unsigned* __restrict__ slot, float4* __restrict__ A) {
   __shared__ bool last;
   const unsigned n = ctr->n;
@@ -334,7 +348,7 @@ __global__ void k_divide_commit(Counters* __restrict__ ctr, unsigned capacity, c
     ctr->done_div = 0u;
   }
 }
-__global__ void k_step_commit(Counters* __restrict__ ctr) { ctr->step += 1ull; }
+static __global__ void k_step_commit(Counters* __restrict__ ctr) { ctr->step += 1ull; }
 
 // ---------------------------------------------------------------------------
 // the force pass
@@ -410,7 +424,7 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
   if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
   if (a.pairs) {
     unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(vj));
+    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_at(a.X, a.Bid, j));
   }
   const float dist = sqrtf(d2);
   const float2 pj = (FORCE == 2 && a.P) ? a.P[j] : make_float2(0.f, 0.f);
@@ -447,8 +461,9 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
     }
     return;
   }
-  // kEulerFused / kHeun2Fused: write the next state into A
+  // kEulerFused / kHeun2Fused: write the next state into A (w = cell id)
   const float4 xb = a.Bx[i];
+  const unsigned idb = a.Bid ? a.Bid[i] : id_of(xb);
   float xn[3];
   float2 pn = make_float2(0.f, 0.f);
   if (a.mode == kEulerFused) {
@@ -465,10 +480,10 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
     }
   }
   if (D < 3) xn[2] = 0.f;
-  a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
+  a.A[i] = make_float4(xn[0], xn[1], xn[2], __uint_as_float(idb));
   if (a.PA) a.PA[i] = pn;
   if (a.count_next) count_cell<D>(g, a, i, xn);
-  maybe_divide<D>(g, a, n, id_of(xb), xn, pn, a.ctr->step);
+  maybe_divide<D>(g, a, n, idb, xn, pn, a.ctr->step);
 }
 
 
@@ -577,7 +592,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
     if (D >= 3) d2 = d2 + disp[2] * disp[2];
     if (a.pairs) {
       unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(__ldg(&a.X[j])));
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_at(a.X, a.Bid, j));
     }
     const float dist = sqrtf(d2);
     const float2 pj = (FORCE == 2 && a.P) ? __ldg(&a.P[j]) : make_float2(0.f, 0.f);
@@ -592,7 +607,7 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
                                           const float* xi, float2 pi, unsigned idi, Acc& acc);
 
 template <int D, int FINDER, int FORCE>
-__global__ void __launch_bounds__(kPassThreads) k_pass(GridP g, ForceP fp, PassArgs a) {
+static __global__ void __launch_bounds__(kPassThreads) k_pass(GridP g, ForceP fp, PassArgs a) {
   const unsigned n = a.ctr->n;
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n;
@@ -604,7 +619,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(GridP g, ForceP fp, PassA
     vi = a.X[i];
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
-    const unsigned idi = id_of(vi);
+    const unsigned idi = id_at(a.X, a.Bid, i);
     if (FINDER == 3 && a.gabriel_fast) {
       __shared__ float4 nbuf[kMaxNb * kPassThreads];
       if (!gabriel_cell_fast<D, FORCE>(g, fp, a, i, xi, pi, idi, acc, &nbuf[threadIdx.x])) {
@@ -670,7 +685,7 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c ^ q); }
 
 template <int D, int FORCE>
-__global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
+static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
   static_assert(FORCE <= 1, "the block-cooperative pass serves the spring laws");
   __shared__ float4 cand[kMaxNb * kPassThreads];            // [q][t]: position, w = (slot << 5) | bin code
   __shared__ float4 home[kPassThreads];                     // position, w = packed bin coords
@@ -690,48 +705,50 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
   int bc[3] = {0, 0, 0};
   int cnt = 0;
   bool fb = false;
-  // ---- phase 1: in-cutoff neighbours of this thread's cell
+  // ---- phase 1: in-cutoff neighbours of this thread's cell.  The row
+  // offsets of all 3x3 neighbour rows are fetched first and the candidates
+  // four at a time, so each thread keeps several loads in flight; a
+  // candidate's bin comes with its position (B.w holds the bin key).
   if (active) {
     vi = __ldg(&a.X[i]);
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
-    if (a.binc && !a.stale_bins) {
-      // the sort already binned this position with the same formula
-      const unsigned pb = __ldg(&a.binc[i]);
-      bc[0] = (int)(pb & 1023u); bc[1] = (int)((pb >> 10) & 1023u); bc[2] = (int)(pb >> 20);
-    } else {
-      bin_coords_div<D>(g, xi, bc);
+    bin_coords_div<D>(g, xi, bc);
+    constexpr int kRows = D >= 3 ? 9 : 3;
+    unsigned rlo[kRows], rhi[kRows], rb0[kRows];
+    int rx0[kRows];
+    const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const int dy = r % 3 - 1, dz = D >= 3 ? r / 3 - 1 : 0;
+      const int cy = bc[1] + dy, cz = D >= 3 ? bc[2] + dz : 0;
+      const bool ok = cy >= 0 && cy < g.ext[1] && (D < 3 || (cz >= 0 && cz < g.ext[2]));
+      int c0[3] = {x0, ok ? cy : 0, ok ? cz : 0};
+      const unsigned b0 = flatten<D>(g, c0);
+      rb0[r] = b0;
+      rx0[r] = x0 - bc[0] + 1;
+      rlo[r] = ok ? __ldg(&a.off[b0]) : 0u;
+      rhi[r] = ok ? __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]) : 0u;
     }
-    const int z0 = D >= 3 ? -1 : 0, z1 = D >= 3 ? 1 : 0;
-    for (int dz = z0; dz <= z1 && !fb; ++dz) {
-      const int cz = D >= 3 ? bc[2] + dz : 0;
-      if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
-      for (int dy = -1; dy <= 1 && !fb; ++dy) {
-        const int cy = bc[1] + dy;
-        if (cy < 0 || cy >= g.ext[1]) continue;
-        const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
-        int c0[3] = {x0, cy, cz};
-        const unsigned b0 = flatten<D>(g, c0);
-        const unsigned o0 = __ldg(&a.off[b0]);
-        const unsigned o3 = __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]);
-        const unsigned rowcode = 3u * (unsigned)(dy + 1) + 9u * (unsigned)(D >= 3 ? dz + 1 : 1);
-        for (unsigned j = o0; j < o3; ++j) {
-          if (j == i) continue;
-          const float4 vj = __ldg(&a.X[j]);
-          const float e0 = xi[0] - vj.x, e1 = xi[1] - vj.y;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(D >= 3 ? r / 3 : 1);
+      for (unsigned j0 = rlo[r]; j0 < rhi[r] && !fb; j0 += 4u) {
+        float4 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          v[k] = (j0 + k < rhi[r]) ? __ldg(&a.X[j0 + k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const unsigned j = j0 + k;
+          if (j >= rhi[r] || j == i || fb) continue;
+          const float e0 = xi[0] - v[k].x, e1 = xi[1] - v[k].y;
           float d2 = e0 * e0 + e1 * e1;
-          if (D >= 3) { const float e2 = xi[2] - vj.z; d2 = d2 + e2 * e2; }
+          if (D >= 3) { const float e2 = xi[2] - v[k].z; d2 = d2 + e2 * e2; }
           if (d2 >= fp.rc2) continue;
-          if (cnt == kMaxNb) { fb = true; break; }
-          unsigned rx;
-          if (a.binc) {
-            rx = (unsigned)((int)(__ldg(&a.binc[j]) & 1023u) - bc[0] + 1);
-          } else {
-            const unsigned o1 = __ldg(&a.off[b0 + 1]);
-            const unsigned o2 = x1 >= x0 + 1 ? __ldg(&a.off[b0 + 2]) : o1;
-            rx = (unsigned)(x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0] + 1);
-          }
-          cand[cix(cnt, t)] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 5) | (rowcode + rx)));
+          if (cnt == kMaxNb) { fb = true; continue; }
+          const unsigned rx = (unsigned)((int)(__float_as_uint(v[k].w) - rb0[r]) + rx0[r]);
+          cand[cix(cnt, t)] = make_float4(v[k].x, v[k].y, v[k].z, __uint_as_float((j << 5) | (rowcode + rx)));
           ++cnt;
         }
       }
@@ -824,7 +841,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
       const unsigned j = __float_as_uint(vj.w) >> 5;
       const unsigned ci = blockIdx.x * kPassThreads + c;
       unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-      if (s < a.pair_cap) a.pairs[s] = make_uint2(id_of(__ldg(&a.X[ci])), id_of(__ldg(&a.X[j])));
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(id_at(a.X, a.Bid, ci), id_at(a.X, a.Bid, j));
     }
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
     const float dist = sqrtf(d2);
@@ -842,7 +859,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
   if (active) {
     if (fallback[t]) {
-      cell_general<D, 3, FORCE>(g, fp, a, n, i, xi, pi, id_of(vi), acc);
+      cell_general<D, 3, FORCE>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc);
     } else {
       const int base = pofs[t];
       for (int q = 0; q < cnt; ++q) {
@@ -861,16 +878,16 @@ __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP f
 // evaluating cell and -delta to j for every field.  Float atomics: the
 // accumulation order is not fixed, results agree to rounding.
 template <int D, int FINDER, int FORCE>
-__global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a) {
+static __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a) {
   const unsigned n = a.ctr->n;
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 vi = a.X[i];
   const float xi[3] = {vi.x, vi.y, vi.z};
   const float2 pi = a.P ? a.P[i] : make_float2(0.f, 0.f);
-  const unsigned idi = id_of(vi);
+  const unsigned idi = id_at(a.X, a.Bid, i);
   auto one = [&](unsigned j) {
-    if (id_of(a.X[j]) >= idi) return;
+    if (id_at(a.X, a.Bid, j) >= idi) return;
     Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
     const unsigned long long before = a.pairs ? 1ull : 0ull;
     (void)before;
@@ -887,7 +904,7 @@ __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a
     if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
     if (a.pairs) {
       unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_of(vj));
+      if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_at(a.X, a.Bid, j));
     }
     const float dist = sqrtf(d2);
     const float2 pj = (FORCE == 2 && a.P) ? a.P[j] : make_float2(0.f, 0.f);
@@ -924,7 +941,7 @@ __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, PassArgs a
 }
 
 // Plain COM reduction over a delta buffer (used after the symmetric pass).
-__global__ void k_com(const float4* __restrict__ d, PassArgs a) {
+static __global__ void k_com(const float4* __restrict__ d, PassArgs a) {
   const unsigned n = a.ctr->n;
   long long x = 0, y = 0, z = 0;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -940,7 +957,7 @@ __global__ void k_com(const float4* __restrict__ d, PassArgs a) {
 
 // heun.hpp:54-68: d1' = d1 - c1; x~ = x + d1' * dt (every field).  d1' is not
 // stored: the corrector forms it again with the same operations.
-__global__ void k_predict(const Counters* __restrict__ ctr, const float* __restrict__ com, float dt,
+static __global__ void k_predict(const Counters* __restrict__ ctr, const float* __restrict__ com, float dt,
                           const float4* __restrict__ B, const float2* __restrict__ PB, const float4* __restrict__ d1,
                           const float2* __restrict__ dp1, float4* __restrict__ Xt, float2* __restrict__ Pt) {
   const unsigned n = ctr->n;
@@ -961,7 +978,7 @@ __global__ void k_predict(const Counters* __restrict__ ctr, const float* __restr
 // plus division.  Heun: s = d1 + (d2 - c); x += (s * 0.5) * dt.
 // Euler:  s = d1 - c; x += s * dt.
 template <int D>
-__global__ void k_finish(int heun, GridP g, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
+static __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
                          const float2* __restrict__ dp2) {
   const unsigned n = a.ctr->n;
   // Euler: com = c (slot 0).  Heun: com = c1 (slot 0), com + 4 = c2 (slot 1)
@@ -994,10 +1011,11 @@ __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __restrict_
       }
     }
     if (D < 3) xn[2] = 0.f;
-    a.A[i] = make_float4(xn[0], xn[1], xn[2], xb.w);
+    const unsigned idb = a.Bid ? a.Bid[i] : id_of(xb);
+    a.A[i] = make_float4(xn[0], xn[1], xn[2], __uint_as_float(idb));
     if (a.PA) a.PA[i] = pn;
     if (a.count_next) count_cell<D>(g, a, i, xn);
-    maybe_divide<D>(g, a, n, id_of(xb), xn, pn, step);
+    maybe_divide<D>(g, a, n, idb, xn, pn, step);
   }
 }
 

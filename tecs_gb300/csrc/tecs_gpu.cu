@@ -43,6 +43,14 @@ int fail(const std::string& m) {
   } while (0)
 
 unsigned ceil_div(unsigned long long a, unsigned b) { return (unsigned)((a + b - 1) / b); }
+}  // namespace
+
+// shared with engine.cu: the thread's last error message
+namespace tecs {
+int set_last_error(const std::string& m) { return fail(m); }
+}  // namespace tecs
+
+namespace {
 
 // pack AoS float[n][dims] into float4 (x, y, z, id)
 __global__ void k_pack(const float* __restrict__ in, unsigned n, int dims, float4* __restrict__ A) {
@@ -55,20 +63,20 @@ __global__ void k_pack(const float* __restrict__ in, unsigned n, int dims, float
   }
 }
 // scatter slot-ordered float4 values into cell-id order AoS float[n][dims]
-__global__ void k_unpack(const float4* __restrict__ ids, const float4* __restrict__ val, unsigned n, int dims,
-                         float* __restrict__ out) {
+__global__ void k_unpack(const float4* __restrict__ idw, const unsigned* __restrict__ ids,
+                         const float4* __restrict__ val, unsigned n, int dims, float* __restrict__ out) {
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    const unsigned id = id_of(ids[s]);
+    const unsigned id = ids ? ids[s] : id_of(idw[s]);
     const float4 v = val[s];
     out[(size_t)id * dims] = v.x;
     if (dims >= 2) out[(size_t)id * dims + 1] = v.y;
     if (dims >= 3) out[(size_t)id * dims + 2] = v.z;
   }
 }
-__global__ void k_unpack2(const float4* __restrict__ ids, const float2* __restrict__ val, unsigned n,
-                          float2* __restrict__ out) {
+__global__ void k_unpack2(const float4* __restrict__ idw, const unsigned* __restrict__ ids,
+                          const float2* __restrict__ val, unsigned n, float2* __restrict__ out) {
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
-    out[id_of(ids[s])] = val[s];
+    out[ids ? ids[s] : id_of(idw[s])] = val[s];
 }
 }  // namespace
 
@@ -82,7 +90,7 @@ struct tecs_sim {
   float2 *PA = nullptr, *PB = nullptr, *Pt = nullptr, *dp1 = nullptr, *dp2 = nullptr;
   unsigned *key = nullptr, *rank = nullptr, *src = nullptr, *cnt = nullptr, *off = nullptr, *part = nullptr;
   unsigned *div_parent = nullptr, *div_slot = nullptr;
-  unsigned* binc = nullptr;  // packed bin coordinates of B's cells
+  unsigned* Bid = nullptr;  // cell ids of B's slots (B.w holds the bin key)
   Counters* ctr = nullptr;
   double* com_part = nullptr;
   float* com = nullptr;  // [0..2] pass 1, [4..6] pass 2
@@ -182,8 +190,7 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   // the fast Gabriel path needs every witness inside i's cutoff ball and 3x3x3 bin block
   a.gabriel_fast = (s->d.gabriel_coefficient <= 0.9f && s->g.R == 1 && s->g.bin_size >= s->d.cutoff) ? 1 : 0;
   a.count_next = s->fuse_count ? 1 : 0;
-  a.binc = s->binc;
-  a.stale_bins = 0;
+  a.Bid = s->binned ? s->Bid : nullptr;
   a.key = s->key;
   a.rank = s->rank;
   a.cnt = s->cnt;
@@ -216,7 +223,7 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
-    k_order_gather<<<gb, 256, 0, s->stream>>>(s->g, s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->binc);
+    k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid);
     PROF_END(s, "k_order_gather");
     K += 4;
   } else {
@@ -256,13 +263,12 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
   if (rebuild || !s->binned) {
     if (enqueue_rebuild(s, K, !s->fuse_count)) return -1;
   } else {
-    CK(cudaMemcpyAsync(s->B, s->A, sizeof(float4) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
-    if (pol) CK(cudaMemcpyAsync(s->PB, s->PA, sizeof(float2) * s->d.capacity, cudaMemcpyDeviceToDevice, s->stream));
+    PROF_BEGIN(s);
+    k_refresh<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, pol ? s->PA : nullptr, s->B, pol ? s->PB : nullptr);
+    PROF_END(s, "k_refresh");
+    K += 1;
   }
   PassArgs a = base_args(s, dt);
-  // positions no longer match the bins they were sorted by: a step without a
-  // rebuild (rebuild_every_n > 1), and every Heun second pass
-  a.stale_bins = rebuild ? 0 : 1;
   auto store_args = [&](PassArgs& p, float4* dout, float2* dpout, int slot) {
     p.mode = kStore;
     p.d_out = dout;
@@ -339,7 +345,6 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     PassArgs p2 = a;
     p2.X = s->Xt;
     p2.P = pol ? s->Pt : nullptr;
-    p2.stale_bins = 1;
     if (fused) {
       p2.mode = kHeun2Fused;
       p2.Bx = s->B;
@@ -454,7 +459,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
          alloc((void**)&s->dp1, cap * 8) && alloc((void**)&s->dp2, cap * 8);
   ok = ok && alloc((void**)&s->key, cap * 4) && alloc((void**)&s->rank, cap * 4) && alloc((void**)&s->src, cap * 4);
   ok = ok && alloc((void**)&s->div_parent, cap * 4) && alloc((void**)&s->div_slot, cap * 4);
-  if (s->binned && g.ext[0] <= 1024 && g.ext[1] <= 1024 && g.ext[2] <= 1024) ok = ok && alloc((void**)&s->binc, cap * 4);
+  if (s->binned) ok = ok && alloc((void**)&s->Bid, cap * 4);
   if (s->binned) {
     const size_t len = (size_t)g.nbins + 1;
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
@@ -485,7 +490,7 @@ int tecs_sim_destroy(tecs_sim* s) {
     if (e) cudaEventDestroy(e);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
-                  s->binc};
+                  s->Bid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -617,11 +622,11 @@ int tecs_sim_download(tecs_sim* s, float* pos, float* pol, unsigned* n_out) {
   const int D = s->d.dims;
   if (n) {
     // Xt is free between steps; unpack into it in id order
-    k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->A, n, D, (float*)s->Xt);
+    k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, nullptr, s->A, n, D, (float*)s->Xt);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(pos, s->Xt, (size_t)n * D * 4, cudaMemcpyDeviceToHost, s->stream));
     if (pol && s->d.has_polarity) {
-      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->PA, n, s->Pt);
+      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, nullptr, s->PA, n, s->Pt);
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(pol, s->Pt, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream));
     }
@@ -662,11 +667,12 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   }
   if (rc == 0 && n) {
     if (dpos) {
-      k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->d1, n, s->d.dims, (float*)s->Xt);
+      k_unpack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->binned ? s->Bid : nullptr, s->d1, n, s->d.dims,
+                                                         (float*)s->Xt);
       cudaMemcpyAsync(dpos, s->Xt, (size_t)n * s->d.dims * 4, cudaMemcpyDeviceToHost, s->stream);
     }
     if (dpol && pol) {
-      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->dp1, n, s->Pt);
+      k_unpack2<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->B, s->binned ? s->Bid : nullptr, s->dp1, n, s->Pt);
       cudaMemcpyAsync(dpol, s->Pt, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream);
     }
   }
@@ -752,7 +758,8 @@ constexpr size_t kOffD = align_up(kOffB + (size_t)kNoallocMaxCells * sizeof(floa
 constexpr size_t kOffKey = align_up(kOffD + (size_t)kNoallocMaxCells * sizeof(float4));
 constexpr size_t kOffRank = align_up(kOffKey + (size_t)kNoallocMaxCells * 4);
 constexpr size_t kOffSrc = align_up(kOffRank + (size_t)kNoallocMaxCells * 4);
-constexpr size_t kOffCnt = align_up(kOffSrc + (size_t)kNoallocMaxCells * 4);
+constexpr size_t kOffBid = align_up(kOffSrc + (size_t)kNoallocMaxCells * 4);
+constexpr size_t kOffCnt = align_up(kOffBid + (size_t)kNoallocMaxCells * 4);
 constexpr size_t kOffOff = align_up(kOffCnt + ((size_t)kNoallocMaxBins + 1) * 4);
 constexpr size_t kOffPart = align_up(kOffOff + ((size_t)kNoallocMaxBins + 1) * 4);
 constexpr size_t kNoallocScratchBytes =
@@ -843,6 +850,7 @@ extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d
   s.key = (unsigned*)(base + kOffKey);
   s.rank = (unsigned*)(base + kOffRank);
   s.src = (unsigned*)(base + kOffSrc);
+  s.Bid = (unsigned*)(base + kOffBid);
   s.cnt = (unsigned*)(base + kOffCnt);
   s.off = (unsigned*)(base + kOffOff);
   s.part = (unsigned*)(base + kOffPart);
@@ -865,7 +873,7 @@ extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d
   a.dp_out = nullptr;
   a.count_next = 0;
   if (enqueue_pass(&s, a, K)) return -1;
-  k_unpack<<<ceil_div(n, 256), 256, 0, s.stream>>>(s.B, s.d1, n, desc->dims, d_deltas);
+  k_unpack<<<ceil_div(n, 256), 256, 0, s.stream>>>(s.B, s.Bid, s.d1, n, desc->dims, d_deltas);
   CK(cudaGetLastError());
   return 0;
 }
