@@ -335,6 +335,42 @@ def run_gb300(args):
     return 0
 
 
+def run_ensemble(args):
+    """Batched form vs the plain drop-in run sequentially, on the 256-simulation ensemble."""
+    import torch
+
+    from tecs_gb300 import batched
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    members = batched.ensemble(args.sims, 2)
+    cells = sum(len(m.x) for m in members)
+    scales, timings = ({}, {}) if args.no_tune else batched.autotune(members)
+    eng, _ = batched.build_engine(members, scales, device=local)
+    with Clocks(local) as clocks:
+        t_b = batched.time_engine_steps(eng, args.steps, warmup=args.warmup)
+    kpl = eng.kernels_per_step()
+    eng.close()
+    t_p = batched.run_plain_steps_only(members, args.steps)
+    v_b = cells * args.steps / t_b
+    v_p = cells * args.steps / t_p
+    line = {
+        "metric": "cell-steps/s, 256-simulation ensemble (batched)", "value": v_b, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_b / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(members)} simulations, cells log-uniform in [500, 200000] (seed 2), "
+                               "density-1 balls, 50% Gabriel / 50% binned all-pairs, Heun dt 0.05",
+                   "cells": cells, "l2": "state larger than L2", "bin_size_scale": scales,
+                   "autotune_seconds_per_4_steps": timings},
+        "plain_sequential": {"value": v_p, "ms_per_step_all_sims": 1e3 * t_p / args.steps},
+        "speedup_vs_plain": v_b / v_p,
+        "gpu_launches": kpl * args.steps,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -344,11 +380,19 @@ def main():
     ap.add_argument("--cells", type=int, default=1_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="spheroid", choices=["spheroid", "ensemble", "served"])
+    ap.add_argument("--sims", type=int, default=256)
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
+    if args.workload == "served":
+        from tecs_gb300 import served
+        return served.bench_main(args)
     return run_gb300(args)
 
 
