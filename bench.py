@@ -383,6 +383,8 @@ def main():
     ap.add_argument("--workload", default="spheroid", choices=["spheroid", "ensemble", "served"])
     ap.add_argument("--sims", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--requests", type=int, default=200, help="served workload: number of requests")
+    ap.add_argument("--time-scale", type=float, default=1.0, help="served workload: arrival-time compression")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

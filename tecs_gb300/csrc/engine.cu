@@ -775,6 +775,8 @@ int tecs_engine_download(tecs_engine* e, int slot, float* positions, float* pola
   const tecs_engine::Info& I = e->info[slot];
   if (!I.active) return fail("simulation was removed");
   const unsigned n = I.n;
+  // pending snapshot copies read the staging buffer this reuses
+  ECK(cudaStreamSynchronize(e->side));
   if (n) {
     k_erange<<<1, 1, 0, e->stream>>>(e->off, I.bin_base, I.appended_at, I.sorted ? 1 : 0, e->range);
     k_eunpack<<<cdiv(n, 256), 256, 0, e->stream>>>(e->range, n, e->A, e->PA, e->stage,

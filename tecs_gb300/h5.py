@@ -1,0 +1,396 @@
+"""Minimal HDF5 reader and writer for cell snapshots (no libhdf5 needed).
+
+The reference writes snapshots with HighFive/libhdf5 (include/io/hdf5_writer.hpp:
+120-129 write_single, :306-321 write): one group "t<step>" per call holding one
+dataset per field, named by the field's label ("position", "polarity", ...),
+shaped [active_count, components], little-endian float32, plus an XDMF
+sidecar.  libhdf5 is not available here, so this module writes and reads that
+subset of the HDF5 file format itself, following the public format
+specification (version 0 superblock, version 1 object headers, symbol-table
+groups built from a version 1 B-tree, a symbol table node and a local heap,
+contiguous datasets described by dataspace v1, datatype v1, fill value v2 and
+layout v3 messages) and laid out the way the HDF5 library lays out the
+reference's own fixture files (examples/data/sphere_ic.h5).
+
+Writer: snapshots are appended as they arrive (data and the new group's
+metadata at the end of the file; the root group's heap, symbol table nodes and
+B-tree live in fixed, pre-sized places and are rewritten in place), so a
+running simulation streams into one file.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import threading
+from pathlib import Path
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+UNDEF = 0xFFFFFFFFFFFFFFFF
+SIG = b"\x89HDF\r\n\x1a\n"
+LEAF_K = 4          # group leaf node K: a symbol table node holds 2K entries
+INTERNAL_K = 16     # group internal node K: a B-tree node holds 2K children
+SNOD_ENTRIES = 2 * LEAF_K
+ENTRY_SIZE = 40
+SNOD_SIZE = 8 + SNOD_ENTRIES * ENTRY_SIZE
+BTREE_SIZE = 24 + (2 * INTERNAL_K + 1) * 8 + 2 * INTERNAL_K * 8
+ROOT_HEAP_DATA = 8192
+
+
+def _pad8(n: int) -> int:
+    return (n + 7) & ~7
+
+
+# ---------------------------------------------------------------------------
+# messages
+
+def _msg(mtype: int, body: bytes, flags: int = 0) -> bytes:
+    body = body + b"\0" * (_pad8(len(body)) - len(body))
+    return struct.pack("<HHB3x", mtype, len(body), flags) + body
+
+
+def _dataspace(shape: Tuple[int, ...]) -> bytes:
+    body = struct.pack("<BBB5x", 1, len(shape), 1)
+    body += b"".join(struct.pack("<Q", d) for d in shape)   # dimensions
+    body += b"".join(struct.pack("<Q", d) for d in shape)   # maximum dimensions
+    return _msg(0x0001, body)
+
+
+def _datatype(dtype: np.dtype) -> bytes:
+    dtype = np.dtype(dtype)
+    if dtype == np.float32:
+        # version 1, class 1 (floating point); little endian, IEEE layout
+        body = bytes([0x11, 0x20, 0x1F, 0x00]) + struct.pack("<I", 4)
+        body += struct.pack("<HHBBBBI", 0, 32, 23, 8, 0, 23, 127)
+    elif dtype == np.float64:
+        body = bytes([0x11, 0x20, 0x3F, 0x00]) + struct.pack("<I", 8)
+        body += struct.pack("<HHBBBBI", 0, 64, 52, 11, 0, 52, 1023)
+    elif dtype in (np.int32, np.uint32, np.int64, np.uint64):
+        signed = 0x08 if dtype.kind == "i" else 0x00
+        body = bytes([0x10, signed, 0x00, 0x00]) + struct.pack("<I", dtype.itemsize)
+        body += struct.pack("<HH", 0, 8 * dtype.itemsize)
+    else:
+        raise TypeError(f"unsupported dtype {dtype}")
+    return _msg(0x0003, body, flags=1)
+
+
+def _fill_value() -> bytes:
+    # version 2, allocation time late, fill written if set, defined with size 0
+    # (the library's default, as in the reference's fixture files)
+    return _msg(0x0005, struct.pack("<BBBBI", 2, 2, 2, 1, 0), flags=1)
+
+
+def _layout_contiguous(addr: int, size: int) -> bytes:
+    return _msg(0x0008, struct.pack("<BBQQ", 3, 1, addr, size))
+
+
+def _symbol_table_msg(btree: int, heap: int) -> bytes:
+    return _msg(0x0011, struct.pack("<QQ", btree, heap))
+
+
+def _object_header(messages: List[bytes], min_size: int = 0) -> bytes:
+    body = b"".join(messages)
+    if len(body) < min_size:  # a NIL message pads the header like the library does
+        pad = min_size - len(body)
+        if pad < 8:
+            pad += 8
+        body += struct.pack("<HHB3x", 0, pad - 8, 0) + b"\0" * (pad - 8)
+        n = len(messages) + 1
+    else:
+        n = len(messages)
+    return struct.pack("<BBHII4x", 1, 0, n, 1, len(body)) + body
+
+
+def _entry(name_off: int, ohdr: int, btree: Optional[int] = None, heap: Optional[int] = None) -> bytes:
+    if btree is None:
+        return struct.pack("<QQII16x", name_off, ohdr, 0, 0)
+    return struct.pack("<QQIIQQ", name_off, ohdr, 1, 0, btree, heap)
+
+
+def _snod(entries: List[bytes]) -> bytes:
+    out = b"SNOD" + struct.pack("<BBH", 1, 0, len(entries)) + b"".join(entries)
+    return out + b"\0" * (SNOD_SIZE - len(out))
+
+
+def _btree(keys: List[int], children: List[int]) -> bytes:
+    out = b"TREE" + struct.pack("<BBHQQ", 0, 0, len(children), UNDEF, UNDEF)
+    for k in range(len(children)):
+        out += struct.pack("<QQ", keys[k], children[k])
+    out += struct.pack("<Q", keys[len(children)])
+    return out + b"\0" * (BTREE_SIZE - len(out))
+
+
+def _heap_header(data_size: int, free_off: int, data_addr: int) -> bytes:
+    return b"HEAP" + struct.pack("<B3xQQQ", 0, data_size, free_off, data_addr)
+
+
+class _Heap:
+    """Local heap data segment: NUL-terminated names, each padded to 8 bytes."""
+
+    def __init__(self, size: int):
+        self.size = size
+        self.data = bytearray(8)  # offset 0: the empty name
+
+    def add(self, name: str) -> int:
+        off = len(self.data)
+        raw = name.encode() + b"\0"
+        self.data += raw + b"\0" * (_pad8(len(raw)) - len(raw))
+        if len(self.data) + 16 > self.size:
+            raise ValueError("group name heap full")
+        return off
+
+    def segment(self) -> Tuple[bytes, int]:
+        """(data bytes of the full segment, free-list head offset)"""
+        used = len(self.data)
+        free = self.size - used
+        out = bytes(self.data)
+        if free >= 16:
+            out += struct.pack("<QQ", 1, free) + b"\0" * (free - 16)  # one free block, last in list
+            return out, used
+        return out + b"\0" * free, UNDEF
+
+
+# ---------------------------------------------------------------------------
+# writer
+
+class H5Writer:
+    """Append-only HDF5 file of groups of float32 datasets (t<step>/<field>)."""
+
+    def __init__(self, path: str | os.PathLike):
+        self.path = Path(path)
+        self.f = open(self.path, "wb+")
+        self.names: Dict[str, Tuple[int, int, int, int]] = {}  # group name -> (name_off, ohdr, btree, heap)
+        self.heap = _Heap(ROOT_HEAP_DATA)
+        # fixed metadata region: superblock, root object header, B-tree, heap header + data, first SNODs
+        self.root_ohdr = 96                     # after the 96-byte superblock
+        self.root_btree = self.root_ohdr + 40   # object header prefix + symbol table message
+        self.root_heap = self.root_btree + BTREE_SIZE
+        self.root_heap_data = self.root_heap + 32
+        self.snods: List[int] = []
+        self.eof = self.root_heap_data + ROOT_HEAP_DATA
+        self._write_root()
+
+    def _write_at(self, addr: int, data: bytes):
+        self.f.seek(addr)
+        self.f.write(data)
+
+    def _alloc(self, size: int) -> int:
+        addr = self.eof
+        self.eof = _pad8(self.eof + size)
+        return addr
+
+    def _superblock(self) -> bytes:
+        sb = SIG + struct.pack("<BBBBBBBB", 0, 0, 0, 0, 0, 8, 8, 0)
+        sb += struct.pack("<HHI", LEAF_K, INTERNAL_K, 0)
+        sb += struct.pack("<QQQQ", 0, UNDEF, self.eof, UNDEF)
+        sb += _entry(0, self.root_ohdr, self.root_btree, self.root_heap)
+        return sb
+
+    def _write_root(self):
+        ordered = sorted(self.names.items())
+        entries = [_entry(v[0], v[1], v[2], v[3]) for _, v in ordered]
+        chunks = [entries[k:k + SNOD_ENTRIES] for k in range(0, len(entries), SNOD_ENTRIES)] or [[]]
+        while len(self.snods) < len(chunks):
+            self.snods.append(self._alloc(SNOD_SIZE))
+        if len(chunks) > 2 * INTERNAL_K:
+            raise ValueError("too many groups for a one-level group B-tree")
+        keys = [0]
+        for k, chunk in enumerate(chunks):
+            self._write_at(self.snods[k], _snod(chunk))
+            last = ordered[min(len(ordered) - 1, (k + 1) * SNOD_ENTRIES - 1)][1][0] if ordered else 0
+            keys.append(last)
+        self._write_at(self.root_btree, _btree(keys, self.snods[: len(chunks)]))
+        seg, free = self.heap.segment()
+        self._write_at(self.root_heap, _heap_header(ROOT_HEAP_DATA, free, self.root_heap_data))
+        self._write_at(self.root_heap_data, seg)
+        self._write_at(self.root_ohdr, _object_header([_symbol_table_msg(self.root_btree, self.root_heap)]))
+        self._write_at(0, self._superblock())
+
+    def write_group(self, group: str, datasets: Dict[str, np.ndarray]):
+        """One group of datasets, like HDF5_Writer::write for one step."""
+        if group in self.names:
+            raise ValueError(f"group {group} exists")
+        if len(datasets) > SNOD_ENTRIES:
+            raise ValueError("at most 8 datasets per group")
+        # the group's own heap with the dataset names
+        gheap = _Heap(_pad8(8 + sum(_pad8(len(k) + 1) for k in datasets) + 16))
+        name_offs = {k: gheap.add(k) for k in datasets}
+        ds_entries = []
+        for name in sorted(datasets):
+            arr = np.ascontiguousarray(datasets[name])
+            if arr.dtype == np.float64:
+                arr = arr.astype(np.float32)
+            data_addr = self._alloc(max(arr.nbytes, 1))
+            self._write_at(data_addr, arr.tobytes())
+            ohdr = _object_header([_dataspace(arr.shape), _datatype(arr.dtype), _fill_value(),
+                                   _layout_contiguous(data_addr if arr.nbytes else UNDEF, arr.nbytes)],
+                                  min_size=216)
+            oaddr = self._alloc(len(ohdr))
+            self._write_at(oaddr, ohdr)
+            ds_entries.append(_entry(name_offs[name], oaddr))
+        snod = self._alloc(SNOD_SIZE)
+        self._write_at(snod, _snod(ds_entries))
+        btree = self._alloc(BTREE_SIZE)
+        last = name_offs[sorted(datasets)[-1]] if datasets else 0
+        self._write_at(btree, _btree([0, last], [snod]))
+        seg, free = gheap.segment()
+        heap = self._alloc(32)
+        heap_data = self._alloc(len(seg))
+        self._write_at(heap, _heap_header(len(seg), free, heap_data))
+        self._write_at(heap_data, seg)
+        gohdr = _object_header([_symbol_table_msg(btree, heap)], min_size=24)
+        gaddr = self._alloc(len(gohdr))
+        self._write_at(gaddr, gohdr)
+        self.names[group] = (self.heap.add(group), gaddr, btree, heap)
+        self._write_root()
+        self.f.flush()
+
+    def close(self):
+        if self.f:
+            self._write_at(0, self._superblock())
+            self.f.truncate(self.eof)
+            self.f.close()
+            self.f = None
+
+
+# ---------------------------------------------------------------------------
+# reader
+
+class H5File:
+    """Reads symbol-table groups and contiguous / compact datasets of fixed-size numeric types."""
+
+    def __init__(self, path: str | os.PathLike):
+        self.b = Path(path).read_bytes()
+        if self.b[:8] != SIG:
+            raise ValueError("not an HDF5 file")
+        if self.b[8] != 0:
+            raise ValueError(f"superblock version {self.b[8]} not supported")
+        if self.b[13] != 8 or self.b[14] != 8:
+            raise ValueError("only 8-byte offsets and lengths are supported")
+        self.root = struct.unpack_from("<Q", self.b, 64)[0]
+
+    def _messages(self, addr: int):
+        b = self.b
+        ver, _, nmsg, _, hsize = struct.unpack_from("<BBHII", b, addr)
+        if ver != 1:
+            raise ValueError(f"object header version {ver} not supported")
+        blocks = [(addr + 16, hsize)]
+        out = []
+        while blocks:
+            off, size = blocks.pop(0)
+            end = off + size
+            while off + 8 <= end:
+                mtype, msize, _ = struct.unpack_from("<HHB", b, off)
+                body = b[off + 8: off + 8 + msize]
+                if mtype == 0x0010:
+                    blocks.append(struct.unpack_from("<QQ", body, 0))
+                else:
+                    out.append((mtype, body))
+                off += 8 + msize
+        return out
+
+    def _group_entries(self, ohdr: int) -> Dict[str, int]:
+        msgs = dict(self._messages(ohdr))
+        if 0x0011 not in msgs:
+            raise ValueError("not a symbol-table group")
+        btree, heap = struct.unpack_from("<QQ", msgs[0x0011], 0)
+        b = self.b
+        if b[heap:heap + 4] != b"HEAP":
+            raise ValueError("bad local heap")
+        _, _, data_addr = struct.unpack_from("<QQQ", b, heap + 8)
+        out = {}
+
+        def walk(node):
+            if b[node:node + 4] != b"TREE":
+                raise ValueError("bad B-tree node")
+            ntype, level, nent = struct.unpack_from("<BBH", b, node + 4)
+            for k in range(nent):
+                child = struct.unpack_from("<Q", b, node + 24 + 16 * k + 8)[0]
+                if level > 0:
+                    walk(child)
+                    continue
+                if b[child:child + 4] != b"SNOD":
+                    raise ValueError("bad symbol table node")
+                nsym = struct.unpack_from("<H", b, child + 6)[0]
+                for e in range(nsym):
+                    name_off, oaddr = struct.unpack_from("<QQ", b, child + 8 + ENTRY_SIZE * e)
+                    end = b.index(b"\0", data_addr + name_off)
+                    out[b[data_addr + name_off:end].decode()] = oaddr
+
+        walk(btree)
+        return out
+
+    def _resolve(self, path: str) -> int:
+        addr = self.root
+        for part in [p for p in path.strip("/").split("/") if p]:
+            entries = self._group_entries(addr)
+            if part not in entries:
+                raise KeyError(path)
+            addr = entries[part]
+        return addr
+
+    def keys(self, path: str = "/") -> List[str]:
+        return sorted(self._group_entries(self._resolve(path)))
+
+    def read(self, path: str) -> np.ndarray:
+        msgs = dict(self._messages(self._resolve(path)))
+        ds = msgs[0x0001]
+        ver, rank = ds[0], ds[1]
+        off = 8 if ver == 1 else 4
+        shape = tuple(struct.unpack_from("<Q", ds, off + 8 * k)[0] for k in range(rank))
+        dt = msgs[0x0003]
+        cls = dt[0] & 0x0F
+        size = struct.unpack_from("<I", dt, 4)[0]
+        if dt[1] & 0x01:
+            raise ValueError("big-endian data not supported")
+        if cls == 1:
+            dtype = {4: np.float32, 8: np.float64}[size]
+        elif cls == 0:
+            dtype = np.dtype(("i" if dt[1] & 0x08 else "u") + str(size))
+        else:
+            raise ValueError(f"datatype class {cls} not supported")
+        lay = msgs[0x0008]
+        if lay[0] != 3:
+            raise ValueError("only layout message version 3 is supported")
+        count = int(np.prod(shape)) if shape else 1
+        if lay[1] == 1:  # contiguous
+            addr, nbytes = struct.unpack_from("<QQ", lay, 2)
+            if addr == UNDEF:
+                return np.zeros(shape, dtype)
+            raw = self.b[addr:addr + nbytes]
+        elif lay[1] == 0:  # compact
+            nbytes = struct.unpack_from("<H", lay, 2)[0]
+            raw = lay[4:4 + nbytes]
+        else:
+            raise ValueError("chunked datasets are not supported")
+        return np.frombuffer(raw, dtype=dtype, count=count).reshape(shape).copy()
+
+
+# ---------------------------------------------------------------------------
+# snapshot sink used by the served loop
+
+class SnapshotSink:
+    """One HDF5 file per request, one t<step> group per snapshot (position, polarity)."""
+
+    def __init__(self, directory: str | os.PathLike):
+        self.dir = Path(directory)
+        self.dir.mkdir(parents=True, exist_ok=True)
+        self.files: Dict[int, H5Writer] = {}
+        self.lock = threading.Lock()
+
+    def __call__(self, request: int, step: int, positions: np.ndarray, polarity: Optional[np.ndarray]):
+        with self.lock:
+            w = self.files.get(request)
+            if w is None:
+                w = self.files[request] = H5Writer(self.dir / f"request_{request:05d}.h5")
+        ds = {"position": positions}
+        if polarity is not None:
+            ds["polarity"] = polarity
+        w.write_group(f"t{step}", ds)
+
+    def close(self):
+        with self.lock:
+            for w in self.files.values():
+                w.close()
+            self.files.clear()

@@ -1,0 +1,283 @@
+"""Served form: a continuous-batching request loop over the engine.
+
+Requests (simulation shape, model, integrator, step count) arrive on a
+Poisson clock.  The loop admits a waiting request as soon as the engine has
+free cells and a free run of bins for it (the engine's capacity is sized from
+the GPU's free HBM), so requests that arrive while others are on the GPU join
+the very next step and share every step's kernel launches with them.  Each
+simulation's state stays on the device; every `snapshot_every` steps it is
+unpacked on the device and copied to pinned host memory on a side stream, and
+a writer thread stores it (HDF5 via tecs_gb300.h5) without stalling the steps.
+A simulation that reaches its step count is downloaded, retired, and its
+time-to-completion (arrival -> result on the host) recorded.
+"""
+from __future__ import annotations
+
+import collections
+import json
+import math
+import os
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+import tecs_gb300 as tg
+from tecs_gb300 import workloads as wl
+from tecs_gb300.engine import Engine, bins_needed
+
+BYTES_PER_CELL = 140  # device bytes the engine keeps per cell (positions, deltas, polarity, sort scratch)
+BYTES_PER_BIN = 8
+
+
+def request_sim(req: wl.Request, max_cells: Optional[int] = None):
+    """(positions, polarity, desc) for a request: a density-1 ball, or a polarised sheet."""
+    n = req.n if max_cells is None else min(req.n, max_cells)
+    if req.model == "polarity":
+        x = wl.sheet(n, req.seed)
+        p = wl.outward_polarity(x, req.seed)
+        force = tg.PolaritySpring(k_pol=0.2)
+    else:
+        x = wl.ball(n, req.seed)
+        p = None
+        force = tg.Spring2R()
+    mn, mx = wl.bounds_for(x)
+    settings = tg.Settings(agent_count=n, capacity=n,
+                           pair_finder_settings=tg.PairFinderSettings(min_bounds=mn, max_bounds=mx))
+    d = tg.make_desc(settings, pair_finder="binned_gabriel", integrator=req.integrator, force=force,
+                     polarity=p is not None)
+    return x, p, d, settings, force
+
+
+@dataclass
+class Live:
+    req: wl.Request
+    slot: int
+    n: int
+    has_pol: bool
+    steps_done: int = 0
+    admitted_at: float = 0.0
+    req_index: int = -1
+
+
+@dataclass
+class Result:
+    index: int
+    n: int
+    steps: int
+    arrival: float
+    admitted: float
+    completed: float
+    positions: Optional[np.ndarray] = None
+    polarity: Optional[np.ndarray] = None
+
+    @property
+    def latency(self):
+        return self.completed - self.arrival
+
+
+class SnapshotWriter(threading.Thread):
+    """Waits for each snapshot's copy event, then hands the pinned buffer to the sink."""
+
+    def __init__(self, sink: Optional[Callable] = None):
+        super().__init__(daemon=True)
+        self.q = queue.Queue()
+        self.sink = sink
+        self.written = 0
+        self.errors: List[str] = []
+
+    def run(self):
+        while True:
+            item = self.q.get()
+            if item is None:
+                return
+            ev, req_index, step, pos, pol, release = item
+            while not Engine.event_ready(ev):
+                time.sleep(0.0002)
+            Engine.event_destroy(ev)
+            try:
+                if self.sink:
+                    self.sink(req_index, step, pos, pol)
+                self.written += 1
+            except Exception as exc:  # a failing sink fails that snapshot, not the server
+                self.errors.append(f"request {req_index} step {step}: {exc}")
+            release()
+
+
+class PinnedPool:
+    """Reusable pinned host buffers (so snapshots do not allocate per copy)."""
+
+    def __init__(self):
+        import torch
+
+        self.torch = torch
+        self.free: Dict[tuple, list] = collections.defaultdict(list)
+        self.lock = threading.Lock()
+
+    def get(self, n: int, width: int):
+        key = (n, width)
+        with self.lock:
+            if self.free[key]:
+                return self.free[key].pop()
+        return self.torch.empty((n, width), dtype=self.torch.float32, pin_memory=True)
+
+    def put(self, t):
+        with self.lock:
+            self.free[(t.shape[0], t.shape[1])].append(t)
+
+
+class Server:
+    def __init__(self, cell_capacity: int, bin_capacity: int, max_sims: int = 1024, snapshot_every: int = 100,
+                 dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0):
+        self.engine = Engine(cell_capacity, bin_capacity, max_sims, device)
+        self.cell_capacity = cell_capacity
+        self.dt = dt
+        self.snapshot_every = snapshot_every
+        self.writer = SnapshotWriter(sink)
+        self.writer.start()
+        self.pool = PinnedPool()
+        self.keep_results = keep_results
+        self.stage_next = 0
+        self.cell_steps = 0
+        self.steps = 0
+
+    @staticmethod
+    def capacity_from_free_hbm(fraction: float = 0.5, bins_per_cell: float = 3.0):
+        import torch
+
+        free, _ = torch.cuda.mem_get_info()
+        budget = free * fraction
+        cells = int(budget / (BYTES_PER_CELL + bins_per_cell * BYTES_PER_BIN))
+        return max(cells, 1 << 16), int(max(cells, 1 << 16) * bins_per_cell)
+
+    def _snapshot(self, live: Live, step: int):
+        pos = self.pool.get(live.n, 3)
+        pol = self.pool.get(live.n, 2) if live.has_pol else None
+        if self.stage_next + live.n > self.cell_capacity:
+            self.stage_next = 0
+            self.engine.synchronize()  # staging reused: let queued copies finish
+        ev = self.engine.snapshot_async(live.slot, pos.data_ptr(), None if pol is None else pol.data_ptr(),
+                                        self.stage_next)
+        self.stage_next += live.n
+
+        def release(pos=pos, pol=pol):
+            self.pool.put(pos)
+            if pol is not None:
+                self.pool.put(pol)
+
+        self.writer.q.put((ev, live.req_index, step, pos.numpy(), None if pol is None else pol.numpy(), release))
+
+    def run(self, requests: List[wl.Request], time_scale: float = 1.0, max_cells: Optional[int] = None,
+            prebuild: bool = True):
+        """Serve the requests; arrival times are divided by time_scale.  Returns the results."""
+        reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival_s)
+        built = {}
+        if prebuild:
+            for idx, r in reqs:
+                built[idx] = request_sim(r, max_cells)
+        waiting = collections.deque()
+        live: Dict[int, Live] = {}
+        results: List[Result] = []
+        arrival = {idx: r.arrival_s / time_scale for idx, r in reqs}
+        k = 0
+        t0 = time.perf_counter()
+        while k < len(reqs) or waiting or live:
+            now = time.perf_counter() - t0
+            while k < len(reqs) and arrival[reqs[k][0]] <= now:
+                waiting.append(reqs[k][0])
+                k += 1
+            # admission: first come, first served, while cells and bins are free
+            while waiting:
+                idx = waiting[0]
+                x, p, d, _, _ = built[idx] if idx in built else request_sim(requests[idx], max_cells)
+                free_cells, free_bins = self.engine.free()
+                if len(x) > free_cells or bins_needed(d) > free_bins:
+                    break
+                waiting.popleft()
+                slot = self.engine.add(d, x, p)
+                live[slot] = Live(requests[idx], slot, len(x), p is not None, 0, time.perf_counter() - t0, idx)
+            if not live:
+                if k < len(reqs):
+                    time.sleep(max(0.0, min(0.01, arrival[reqs[k][0]] - (time.perf_counter() - t0))))
+                continue
+            # one step of every resident simulation
+            self.engine.step(self.dt, 1)
+            self.steps += 1
+            for lv in live.values():
+                lv.steps_done += 1
+                self.cell_steps += lv.n
+            done = []
+            for slot, lv in live.items():
+                if lv.steps_done % self.snapshot_every == 0 and lv.steps_done < lv.req.steps:
+                    self._snapshot(lv, lv.steps_done)
+                if lv.steps_done >= lv.req.steps:
+                    done.append(slot)
+            for slot in done:
+                lv = live.pop(slot)
+                xf, pf = self.engine.download(slot)
+                self.engine.remove(slot)
+                res = Result(lv.req_index, lv.n, lv.req.steps, arrival[lv.req_index], lv.admitted_at,
+                             time.perf_counter() - t0)
+                if self.keep_results:
+                    res.positions, res.polarity = xf, pf
+                results.append(res)
+        self.engine.synchronize()
+        self.makespan = time.perf_counter() - t0
+        return results
+
+    def close(self):
+        self.writer.q.put(None)
+        self.writer.join(timeout=60)
+        self.engine.close()
+
+
+def summarize(results: List[Result], makespan: float, cell_steps: int):
+    lat = np.array([r.latency for r in results])
+    return {
+        "requests": len(results),
+        "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+        "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+        "mean_s": float(lat.mean()) if len(lat) else None,
+        "cell_steps_per_s": cell_steps / makespan if makespan > 0 else None,
+        "makespan_s": makespan,
+    }
+
+
+def bench_main(args):
+    """bench.py --workload served: the served stream on one GPU."""
+    import torch
+
+    from tecs_gb300 import h5
+
+    rank, world, local = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(
+        os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    n_req = args.requests
+    reqs = wl.served_stream(n_req, seed=3)
+    cells, bins = Server.capacity_from_free_hbm(0.4)
+    out_dir = Path(os.environ.get("TECS_SNAPSHOT_DIR", "/tmp/tecs_snapshots"))
+    out_dir.mkdir(parents=True, exist_ok=True)
+    sink = h5.SnapshotSink(out_dir)
+    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink)
+    res = srv.run(reqs, time_scale=args.time_scale)
+    summ = summarize(res, srv.makespan, srv.cell_steps)
+    written = srv.writer.written
+    srv.close()
+    sink.close()
+    line = {
+        "metric": "cell-steps/s, served stream (continuous batching)", "value": summ["cell_steps_per_s"],
+        "unit": "cell-steps/s", "n_gpus": 1, "steps": srv.steps, "warmup": 0,
+        "ms_per_step": 1e3 * srv.makespan / max(srv.steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n_req} requests, Poisson 20/s (seed 3) with arrivals compressed x{args.time_scale}, "
+                               "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
+                               "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins},
+        "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"]},
+        "snapshots_written": written, "makespan_s": srv.makespan,
+    }
+    print(json.dumps(line), flush=True)
+    return 0

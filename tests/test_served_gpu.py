@@ -1,0 +1,69 @@
+"""The served loop: continuous batching over the engine (GB300).
+
+Requests arriving while others run are admitted at the next step and share
+its launches; each request's result must equal the same simulation run alone
+(the plain drop-in path) -- bit for bit, since the per-cell arithmetic and
+summation order do not depend on what else is resident.  Snapshots stream to
+HDF5 files through pinned buffers on a side stream.
+"""
+import numpy as np
+import pytest
+
+import tecs_gb300 as tg
+from tecs_gb300 import h5
+from tecs_gb300 import workloads as wl
+from tecs_gb300.served import Server, request_sim, summarize
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(req, max_cells):
+    x, p, d, settings, force = request_sim(req, max_cells)
+    s = tg.Simulation(settings, pair_finder="binned_gabriel", integrator=req.integrator, force=force,
+                      polarity=p is not None)
+    s.set_state(x, p)
+    s.take_step(0.05, req.steps)
+    return s.get_state()
+
+
+def test_results_same_alone_and_in_the_mix(tmp_path):
+    reqs = wl.served_stream(14, seed=5, rate_hz=200.0, lo=800, hi=12000, steps_lo=20, steps_hi=130)
+    sink = h5.SnapshotSink(tmp_path)
+    # capacity for about three requests at a time: admissions wait for retirements
+    srv = Server(cell_capacity=30000, bin_capacity=160000, max_sims=16, snapshot_every=50, sink=sink,
+                 keep_results=True)
+    res = srv.run(reqs, time_scale=1.0)
+    srv.close()
+    sink.close()
+    assert len(res) == len(reqs)
+    assert max(r.admitted for r in res) > min(r.completed for r in res)  # some admitted while others ran
+    for r in res:
+        x_alone, p_alone = alone(reqs[r.index], None)
+        np.testing.assert_array_equal(r.positions, x_alone)
+        if p_alone is not None:
+            np.testing.assert_array_equal(r.polarity, p_alone)
+    # snapshots: one group per 50 steps before the last, with the right shapes
+    assert not srv.writer.errors
+    for r in res:
+        want = [f"t{k}" for k in range(50, reqs[r.index].steps, 50)]
+        if not want:
+            continue
+        f = h5.H5File(tmp_path / f"request_{r.index:05d}.h5")
+        assert sorted(f.keys()) == sorted(want)
+        assert f.read(f"{want[0]}/position").shape == (reqs[r.index].n, 3)
+    s = summarize(res, srv.makespan, srv.cell_steps)
+    assert s["p99_s"] >= s["p50_s"] > 0
+
+
+def test_failing_snapshot_sink_fails_only_that_snapshot(tmp_path):
+    reqs = wl.served_stream(4, seed=6, rate_hz=1000.0, lo=1000, hi=3000, steps_lo=60, steps_hi=60)
+
+    def sink(request, step, pos, pol):
+        if request == 1:
+            raise OSError(28, "No space left on device")
+
+    srv = Server(cell_capacity=20000, bin_capacity=100000, max_sims=8, snapshot_every=25, sink=sink)
+    res = srv.run(reqs)
+    srv.close()
+    assert len(res) == 4
+    assert srv.writer.errors and all("request 1" in e for e in srv.writer.errors)
