@@ -1,19 +1,29 @@
 #!/usr/bin/env python
-"""Cell-step throughput of the GB300 path on the headline spheroid workload.
+"""Cell-step throughput of the GB300 path.
 
-Workload (default): 1,000,000 cells uniform in a ball at density 1 (seed 1),
-binned Gabriel finder (cutoff 1.0, c = 0.8), spring force
-F = 2*max(0.7-d,0) - 0.5*max(d-0.8,0), Heun dt = 0.05, GlobalComFixer every
-step, cell division p = 1e-4 per cell per step (daughter at 0.25 * random unit
-vector), capacity 1.05 N.  A step is one Heun step of the whole simulation.
+Workloads (--workload):
+  spheroid (default, the headline): 1,000,000 cells uniform in a ball at
+      density 1 (seed 1), binned Gabriel finder (cutoff 1.0, c = 0.8), spring
+      force F = 2*max(0.7-d,0) - 0.5*max(d-0.8,0), Heun dt = 0.05,
+      GlobalComFixer every step, cell division p = 1e-4 per cell per step
+      (daughter at 0.25 * random unit vector), capacity 1.05 N.
+  sheet: 100,000 cells on a sphere of radius sqrt(N/4pi)*0.8 (jitter 0.02),
+      outward polarity + N(0, 0.1), binned Gabriel, spring + 0.2 (bending +
+      alignment), Heun dt = 0.05.
+  small: 1,000 cells in a ball of radius 5 (seed 0), binned all-pairs, spring,
+      Euler dt = 0.1.
+  ensemble: 256 simulations in one engine vs the plain path one after another.
+  served: the continuous-batching request loop (tecs_gb300.served).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--cells N]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload W] [--cells N]
 
 Prints one JSON line (rank 0).  value = cell-steps/s with the state resident
 in HBM, each step timed with CUDA events on the simulation's stream and the L2
 flushed (256 MiB memset) between steps; e2e = the same metric through the C
-ABI with host buffers (pinned upload, per-step agent-count read, download).
-Under torchrun every rank runs its own replica (weak scaling, no collective).
+ABI with host buffers (every step: pinned upload of the state, the step, and
+the download of the new state).  --impl reference times the reference's
+algorithm (the oracle's C restatement, OpenMP) on the host cores.  Under
+torchrun every rank runs its own replica (weak scaling, no collective).
 """
 from __future__ import annotations
 
@@ -36,11 +46,64 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-steps/s at 1M cells (Gabriel+Heun)"
 UNIT = "cell-steps/s"
-# algorithmic bytes per cell of one force pass: read position (float4) + write delta (float4);
-# neighbour re-reads are cache reuse and not counted
-PASS_BYTES_PER_CELL = 32
-# whole Heun + COM step, per cell: bin+reorder 60 + pass 1 32 + pass 2 48 + corrector 64
-STEP_BYTES_PER_CELL = 204
+
+# Algorithmic bytes per cell of one force-pass launch, by pass kind: each
+# cell's own state read once and its outputs written once (float4 position /
+# delta, float2 polarity); neighbour re-reads are cache reuse and not counted.
+PASS_BYTES = {
+    "k_pass_store": (32, 16),   # read x, write delta             (+ read p, write dp)
+    "k_pass_euler": (32, 16),   # read x, write x'                (+ p, p')
+    "k_pass_heun1": (48, 24),   # read x, write d1, x~            (+ p, dp1, p~)
+    "k_pass_heun2": (64, 32),   # read x~, x, d1, write x'        (+ p~, p, dp1, p')
+}
+
+
+def _ball_workload(n):
+    from tecs_gb300 import workloads as wl
+
+    x = wl.ball(n, 1)
+    mn, mx = wl.bounds_for(x, margin=2.0)
+    return x, None, mn, mx
+
+
+def _sheet_workload(n):
+    from tecs_gb300 import workloads as wl
+
+    x = wl.sheet(n, 1)
+    p = wl.outward_polarity(x, 1)
+    mn, mx = wl.bounds_for(x, margin=2.0)
+    return x, p, mn, mx
+
+
+def _small_workload(n):
+    from tecs_gb300 import workloads as wl
+
+    x = wl.ball(n, 0, radius=5.0)
+    return x, None, (-6.0,) * 3, (6.0,) * 3
+
+
+# The configurations this benchmark runs.  spheroid is the headline (the
+# metric's 1M-cell Gabriel + Heun step); sheet and small are the epithelial
+# sheet with polarity and the small plain configuration.
+WORKLOADS = {
+    "spheroid": dict(
+        metric=METRIC, cells=1_000_000, make=_ball_workload, finder="binned_gabriel", integrator="heun", com=True,
+        division=1e-4, polarity=False, dt=0.05, capacity=1.05,
+        desc="spheroid {n} cells, binned Gabriel, spring, Heun dt 0.05, COM, division 1e-4",
+        step_bytes=204),  # bin+reorder 60, pass 1 32, pass 2 48, corrector 64
+    "sheet": dict(
+        metric="cell-steps/s, 100k-cell epithelial sheet (Gabriel + polarity, Heun)", cells=100_000,
+        make=_sheet_workload, finder="binned_gabriel", integrator="heun", com=False, division=0.0, polarity=True,
+        dt=0.05, capacity=1.0,
+        desc="sheet {n} cells on a sphere (R = sqrt(N/4pi)*0.8, jitter 0.02), binned Gabriel, spring + "
+             "0.2 (bending + alignment), Heun dt 0.05",
+        step_bytes=212),  # Heun without COM 156 + polarity 56
+    "small": dict(
+        metric="cell-steps/s, 1k-cell plain small (binned all-pairs, Euler)", cells=1000, make=_small_workload,
+        finder="binned_all_pairs", integrator="euler", com=False, division=0.0, polarity=False, dt=0.1,
+        capacity=1.0, desc="ball {n} cells radius 5 (seed 0), binned all-pairs, spring, Euler dt 0.1",
+        step_bytes=92),
+}
 
 
 def peaks():
@@ -55,23 +118,28 @@ def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def workload(n_cells: int):
-    from tecs_gb300 import workloads as wl
-
-    x = wl.ball(n_cells, 1)
-    mn, mx = wl.bounds_for(x, margin=2.0)
-    return x, mn, mx
-
-
-def make_sim(n, mn, mx, device=0):
+def make_sim(w, n, mn, mx, device=0):
     import tecs_gb300 as tg
 
     pf = tg.PairFinderSettings(gabriel_coefficient=0.8, min_bounds=mn, max_bounds=mx)
-    cap = int(math.ceil(n * 1.05))
+    cap = int(math.ceil(n * w["capacity"]))
+    force = tg.PolaritySpring(k_pol=0.2) if w["polarity"] else tg.Spring2R(k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8)
     return tg.Simulation(tg.Settings(agent_count=n, capacity=cap, cutoff_distance=1.0, seed=1, pair_finder_settings=pf),
-                         pair_finder="binned_gabriel", integrator="heun", com_fixer="global",
-                         force=tg.Spring2R(k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8),
-                         division=tg.Division(probability=1e-4, offset=0.25), device=device)
+                         pair_finder=w["finder"], integrator=w["integrator"],
+                         com_fixer="global" if w["com"] else None, force=force, polarity=w["polarity"],
+                         division=tg.Division(probability=w["division"], offset=0.25), device=device)
+
+
+def make_oracle(w, n, mn, mx):
+    import oracle
+
+    cap = int(math.ceil(n * w["capacity"]))
+    finder = oracle.BINNED_GABRIEL if w["finder"] == "binned_gabriel" else oracle.BINNED_ALL_PAIRS
+    return oracle.Oracle(finder=finder, integrator=oracle.HEUN if w["integrator"] == "heun" else oracle.EULER,
+                         com_fix=w["com"], min_bounds=mn, max_bounds=mx, capacity=cap,
+                         force=oracle.FORCE_POLARITY if w["polarity"] else oracle.FORCE_SPRING2R,
+                         k_pol=0.2 if w["polarity"] else 0.0, has_polarity=w["polarity"],
+                         division_probability=w["division"], division_offset=0.25, seed=1)
 
 
 class Clocks:
@@ -91,11 +159,34 @@ class Clocks:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # wait for the sampler's first line so that the timed region is covered
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 10.0 and self._lines() == 0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+        self.lo, self.hi = 0, None
         return self
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return sum(1 for line in f if line.endswith("\n"))
+        except OSError:
+            return 0
+
+    def start(self):
+        """Mark the start of the timed region (samples before it are ignored)."""
+        self.lo = self._lines()
+
+    def stop(self):
+        """Mark the end of the timed region, letting the sampler record at least one line inside it."""
+        t0 = time.perf_counter()
+        while self.proc and self._lines() <= self.lo and time.perf_counter() - t0 < 1.0:
+            time.sleep(0.01)
+        self.hi = self._lines()
 
     def __exit__(self, *exc):
         if self.proc:
@@ -110,7 +201,8 @@ class Clocks:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        lines = [line for line in open(self.path) if line.endswith("\n")]
+        for line in lines[self.lo:self.hi]:
             f = [t.strip() for t in line.split(",")]
             if len(f) < 9:
                 continue
@@ -129,75 +221,51 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def traffic_per_pass():
-    """DRAM bytes per k_pass launch from the committed ncu capture, scaled to 1M cells."""
+def traffic_per_pass(workload: str):
+    """DRAM bytes per cell of one force-pass launch, from the committed ncu capture of this workload."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
-        d = json.loads(p.read_text())
-        return d.get("k_pass_store_bytes_per_cell")
+        return json.loads(p.read_text()).get(workload, {}).get("pass_dram_bytes_per_cell")
     except Exception:
         return None
 
 
-def cpu_baseline(n_cells, steps, threads, budget_s=20.0):
-    """The oracle (C restatement, OpenMP) on a bounded sample of the same workload."""
-    import oracle
-    from tecs_gb300 import workloads as wl
-
-    x, mn, mx = workload(n_cells)
-    cap = int(math.ceil(n_cells * 1.05))
-    o = oracle.Oracle(finder=oracle.BINNED_GABRIEL, integrator=oracle.HEUN, com_fix=True, min_bounds=mn,
-                      max_bounds=mx, capacity=cap, division_probability=1e-4, division_offset=0.25, seed=1)
-    o.set_state(x)
+def cpu_steps(w, n, mn, mx, x, p, steps, threads, budget_s):
+    """Time up to `steps` oracle steps (about budget_s seconds) after one warm-up step."""
+    o = make_oracle(w, n, mn, mx)
+    o.set_state(x, p)
     t0 = time.perf_counter()
-    o.step(0.05, 1, threads)  # warm-up
+    o.step(w["dt"], 1, threads)
     first = time.perf_counter() - t0
-    k = max(1, min(steps, int(budget_s / max(first, 1e-3))))
+    k = max(1, min(steps, int(budget_s / max(first, 1e-4))))
     cs = 0
     t0 = time.perf_counter()
     for _ in range(k):
-        n = o.count
-        o.step(0.05, 1, threads)
-        cs += n
+        cs += o.count
+        o.step(w["dt"], 1, threads)
     dt = time.perf_counter() - t0
     return cs / dt, k, dt
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle's C restatement with OpenMP."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
+    w = WORKLOADS[args.workload]
+    n = args.cells or w["cells"]
     threads = os.cpu_count() or 1
-    n = args.cells
-    # the reference's algorithm on the host cores: the oracle's C restatement with OpenMP
-    x, mn, mx = workload(n)
-    import oracle
-
-    cap = int(math.ceil(n * 1.05))
-    o = oracle.Oracle(finder=oracle.BINNED_GABRIEL, integrator=oracle.HEUN, com_fix=True, min_bounds=mn,
-                      max_bounds=mx, capacity=cap, division_probability=1e-4, division_offset=0.25, seed=1)
-    o.set_state(x)
-    for _ in range(args.warmup):
-        o.step(0.05, 1, threads)
-    # bounded sample: at most --steps steps and about 60 s
-    cs, k = 0, 0
-    t0 = time.perf_counter()
-    while k < args.steps and (time.perf_counter() - t0) < 60.0:
-        cs += o.count
-        o.step(0.05, 1, threads)
-        k += 1
-    dt = time.perf_counter() - t0
-    v = cs / dt
+    x, p, mn, mx = w["make"](n)
+    v, k, dt = cpu_steps(w, n, mn, mx, x, p, max(args.steps, 1), threads, 60.0)
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
-        "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(k, 1), "higher_is_better": True, "scaling": "weak",
+        "impl": "reference", "metric": w["metric"], "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
+        "warmup": 1, "ms_per_step": 1e3 * dt / max(k, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"spheroid {n} cells, binned Gabriel, spring, Heun dt 0.05, COM, division 1e-4",
-                   "cells": n, "l2": "n/a (host)"},
+        "config": {"workload": w["desc"].format(n=n), "cells": n, "l2": "n/a (host)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{k} Heun steps of the {n}-cell spheroid after {args.warmup} warm-up"},
+                         "sample": f"{k} steps of the {n}-cell workload after 1 warm-up step ({dt:.1f} s, OpenMP)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -215,18 +283,22 @@ def run_gb300(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    n = args.cells
-    x, mn, mx = workload(n)
-    sim = make_sim(n, mn, mx, device=local)
+    w = WORKLOADS[args.workload]
+    n = args.cells or w["cells"]
+    pol = w["polarity"]
+    x, p, mn, mx = w["make"](n)
+    sim = make_sim(w, n, mn, mx, device=local)
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     xd = torch.from_numpy(x).to("cuda")
+    pd = torch.from_numpy(p).to("cuda") if pol else None
     torch.cuda.synchronize()
-    sim.set_state_device(xd.data_ptr(), None, n)
+    sim.set_state_device(xd.data_ptr(), pd.data_ptr() if pol else None, n)
     sim.set_profiling(True)
+    dt = w["dt"]
 
     for _ in range(args.warmup):
-        sim.take_step(0.05)
+        sim.take_step(dt)
     sim.synchronize()
 
     if world > 1:
@@ -235,6 +307,7 @@ def run_gb300(args):
     step_ms, kern = [], {}
     cell_steps = 0
     with Clocks(local) as clocks:
+        clocks.start()
         for _ in range(args.steps):
             nb = sim.get_agent_count()
             with torch.cuda.stream(stream):
@@ -242,7 +315,7 @@ def run_gb300(args):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            sim.take_step(0.05)
+            sim.take_step(dt)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
@@ -250,6 +323,7 @@ def run_gb300(args):
             for name, ms in sim.last_step_profile():
                 kern.setdefault(name, []).append(ms)
             cell_steps += nb
+        clocks.stop()
     torch.cuda.synchronize()
     total_s = sum(step_ms) / 1e3
     if world > 1:
@@ -265,30 +339,37 @@ def run_gb300(args):
     value = cell_steps_all / total_s
     kpl = sim.kernels_per_step()
 
-    # end to end through the C ABI with host buffers
+    # End to end through the C ABI with host buffers: every step uploads the
+    # state from pinned host memory, steps, and downloads the new state.
     e2e = None
     if not args.no_e2e:
         L = tg.load()
         cap = sim.desc.capacity
-        hx = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
-        hx.numpy()[:] = x
-        hout = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
-        nn = ctypes.c_uint()
+        hx = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+        hx.numpy()[:n] = x
+        hp = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True) if pol else None
+        if pol:
+            hp.numpy()[:n] = p
+        nn = ctypes.c_uint(n)
+        h2d = d2h = 0
+        cs = 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        tg._check(L.tecs_sim_upload(sim._h, ctypes.c_void_p(hx.data_ptr()), None, n))
-        cs = 0
         for _ in range(args.steps):
-            tg._check(L.tecs_sim_count(sim._h, ctypes.byref(nn)))
-            cs += nn.value
-            tg._check(L.tecs_sim_step(sim._h, 0.05, 1))
-        tg._check(L.tecs_sim_download(sim._h, ctypes.c_void_p(hout.data_ptr()), None, ctypes.byref(nn)))
+            m = nn.value
+            tg._check(L.tecs_sim_upload(sim._h, ctypes.c_void_p(hx.data_ptr()),
+                                        ctypes.c_void_p(hp.data_ptr()) if pol else None, m))
+            h2d += m * (20 if pol else 12)
+            tg._check(L.tecs_sim_step(sim._h, dt, 1))
+            tg._check(L.tecs_sim_download(sim._h, ctypes.c_void_p(hx.data_ptr()),
+                                          ctypes.c_void_p(hp.data_ptr()) if pol else None, ctypes.byref(nn)))
+            d2h += nn.value * (20 if pol else 12)
+            cs += m
         t1 = time.perf_counter()
-        e2e = {"value": cs / (t1 - t0), "unit": UNIT,
-               "h2d_bytes_per_step": int(n * 12 / args.steps),
-               "d2h_bytes_per_step": int(4 + nn.value * 12 / args.steps),
-               "note": "pinned upload of the initial state and final download amortised over the steps; "
-                       "agent count read back every step"}
+        e2e = {"value": cs / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(d2h / args.steps),
+               "note": "each step: pinned host state -> device (tecs_sim_upload), tecs_sim_step, "
+                       "device -> pinned host state (tecs_sim_download)"}
 
     if rank != 0:
         if world > 1:
@@ -296,33 +377,39 @@ def run_gb300(args):
         return 0
 
     hbm, peak_kind = peaks()
-    passes = [ms for name, v in kern.items() if name.startswith("k_pass") for ms in v]
     n_avg = cell_steps / max(args.steps, 1)
-    pass_ms = statistics.mean(passes) if passes else float("nan")
-    achieved = PASS_BYTES_PER_CELL * n_avg / (pass_ms / 1e3) / 1e9
-    tpc = traffic_per_pass()
+    pass_bytes, pass_s, pass_launches = 0.0, 0.0, 0
+    for name, v in kern.items():
+        if name in PASS_BYTES:
+            b = PASS_BYTES[name][0] + (PASS_BYTES[name][1] if pol else 0)
+            pass_bytes += b * n_avg * len(v)
+            pass_s += sum(v) / 1e3
+            pass_launches += len(v)
+    achieved = pass_bytes / pass_s / 1e9 if pass_s else float("nan")
+    tpc = traffic_per_pass(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": (tpc * n_avg if tpc else None), "kernel": "k_pass (Gabriel + spring force pass)",
-                "bytes_per_cell": PASS_BYTES_PER_CELL, "peak_kind": f"{peak_kind} hbm_gbs",
-                "avg_launch_ms": pass_ms}
-    step_achieved = STEP_BYTES_PER_CELL * n_avg / (statistics.mean(step_ms) / 1e3) / 1e9
+                "traffic": (tpc * n_avg if tpc else None),
+                "kernel": "force pass (k_pass_*: pair finding + force + fused integrator epilogue)",
+                "bytes_per_launch": pass_bytes / max(pass_launches, 1),
+                "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_s / max(pass_launches, 1)}
+    step_achieved = w["step_bytes"] * n_avg / (statistics.mean(step_ms) / 1e3) / 1e9
     kernel_table = {k: {"launches": len(v), "mean_ms": statistics.mean(v), "share": sum(v) / max(sum(step_ms), 1e-9)}
                     for k, v in kern.items()}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         threads = os.cpu_count() or 1
-        v, k, dt = cpu_baseline(n, 64, threads)
+        v, k, sec = cpu_steps(w, n, mn, mx, x, p, 1000, threads, 15.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{k} Heun steps of the {n}-cell spheroid after 1 warm-up ({dt:.1f} s, OpenMP)"}
+               "sample": f"{k} steps of the {n}-cell workload after 1 warm-up step ({sec:.1f} s, OpenMP)"}
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"spheroid {n} cells, binned Gabriel, spring, Heun dt 0.05, COM, division 1e-4",
-                   "cells": n, "capacity": sim.desc.capacity, "bins": None,
+        "metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"].format(n=n), "cells": n, "capacity": sim.desc.capacity,
                    "l2": "flushed between timed steps (256 MiB memset)", "parallelism": f"replicas x{world}"},
         "roofline": roofline,
-        "step_roofline": {"bytes_per_cell": STEP_BYTES_PER_CELL, "achieved": step_achieved, "frac": step_achieved / hbm},
+        "step_roofline": {"bytes_per_cell": w["step_bytes"], "achieved": step_achieved,
+                          "frac": step_achieved / hbm},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": kpl * args.steps,
@@ -374,13 +461,13 @@ def run_ensemble(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cells", type=int, default=1_000_000)
+    ap.add_argument("--cells", type=int, default=0, help="cell count (default: the workload's)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="spheroid", choices=["spheroid", "ensemble", "served"])
+    ap.add_argument("--workload", default="spheroid", choices=["spheroid", "sheet", "small", "ensemble", "served"])
     ap.add_argument("--sims", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--requests", type=int, default=200, help="served workload: number of requests")
@@ -389,6 +476,9 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
+        if args.workload not in WORKLOADS:
+            print(json.dumps({"impl": "reference", "unavailable": f"the reference has no {args.workload} form"}))
+            return 0
         return run_reference(args)
     if args.workload == "ensemble":
         return run_ensemble(args)

@@ -28,12 +28,14 @@
 extern "C" {
 #endif
 
-/* Pair finders: include/pair_finders/{naive_all_pairs,binned_all_pairs,naive_gabriel,binned_gabriel}.hpp */
+/* Pair finders: include/pair_finders/{naive_all_pairs,binned_all_pairs,naive_gabriel,binned_gabriel,
+ *               naive_delaunay}.hpp */
 enum tecs_finder {
   TECS_FINDER_NAIVE_ALL_PAIRS = 0,
   TECS_FINDER_BINNED_ALL_PAIRS = 1,
   TECS_FINDER_NAIVE_GABRIEL = 2,
-  TECS_FINDER_BINNED_GABRIEL = 3
+  TECS_FINDER_BINNED_GABRIEL = 3,
+  TECS_FINDER_NAIVE_DELAUNAY = 4    /* naive_delaunay.hpp:31-294; capacity <= 4096, non-symmetric */
 };
 
 /* Integrators: include/integrators/euler.hpp, heun.hpp */
@@ -118,6 +120,11 @@ int tecs_sim_evaluate(tecs_sim* sim, float* dpos, float* dpol, uint32_t* pairs, 
 
 /* The simulation's CUDA stream (a cudaStream_t). */
 void* tecs_sim_stream(tecs_sim* sim);
+
+/* Change the pairwise force law between steps: take_step(dt, force) with a
+ * different force functor (include/simulation.hpp:548-556).  No-op when the
+ * law and its constants are unchanged; otherwise waits for queued steps. */
+int tecs_sim_set_force(tecs_sim* sim, int force, float k_rep, float r_rep, float k_adh, float r_adh, float k_pol);
 
 /* Capture each step as a CUDA graph and replay it (default on). */
 int tecs_sim_set_graph(tecs_sim* sim, int enable);

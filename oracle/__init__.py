@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libtecs_oracle.so"
 
-NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL = 0, 1, 2, 3
+NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL, NAIVE_DELAUNAY = 0, 1, 2, 3, 4
 FORCE_NONE, FORCE_SPRING2R, FORCE_POLARITY = 0, 1, 2
 EULER, HEUN = 0, 1
 

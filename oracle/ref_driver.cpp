@@ -38,6 +38,7 @@
 #include <pair_finders/naive_all_pairs_symmetric.hpp>
 #include <pair_finders/naive_gabriel.hpp>
 #include <pair_finders/naive_gabriel_symmetric.hpp>
+#include <pair_finders/naive_delaunay.hpp>
 #include <integrators/euler.hpp>
 #include <integrators/heun.hpp>
 #include <com_fixers/com_fixers.hpp>
@@ -137,7 +138,9 @@ static int tecs_driver_run(const Input& in, const std::string& out, int steps, d
   const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11], k_pol = in.prm[12];
   (void)k_pol;
   const unsigned n = in.n;
-  Kokkos::View<unsigned*> pairs("pairs", 2 * (size_t)n * (n < 4096 ? n : 64) + 2);
+  // the Delaunay finder applies a pair once per accepted triangle/tetrahedron
+  const size_t per_cell = n <= 256 ? (size_t)n * n : (n < 4096 ? n : 64);
+  Kokkos::View<unsigned*> pairs("pairs", 2 * (size_t)n * per_cell + 2);
   DeviceVar<int> counter = 0;
   bool capture = true;
 
@@ -226,6 +229,8 @@ TECS_SCENARIO(ngs_euler_3, pair_finders::NaiveGabrielSymmetric, integrators::Eul
 TECS_SCENARIO(bg_heun_pol_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 3, 1)
 TECS_SCENARIO(ng_euler_2, pair_finders::NaiveGabriel, integrators::Euler, com_fixers::NoComFixer, 2, 0)
 TECS_SCENARIO(bg_heun_2, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 2, 0)
+TECS_SCENARIO(nd_euler_2, pair_finders::NaiveDelaunay, integrators::Euler, com_fixers::NoComFixer, 2, 0)
+TECS_SCENARIO(nd_heun_3, pair_finders::NaiveDelaunay, integrators::Heun, com_fixers::NoComFixer, 3, 0)
 
 int main(int argc, char** argv) {
   if (argc < 6) {
@@ -243,7 +248,7 @@ int main(int argc, char** argv) {
   if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
-  DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2)
+  DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2) DISPATCH(nd_euler_2) DISPATCH(nd_heun_3)
 #undef DISPATCH
   if (rc == 3) std::fprintf(stderr, "unknown scenario %s\n", sc.c_str());
   return rc;

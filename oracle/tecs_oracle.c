@@ -64,6 +64,10 @@ static double u01(uint64_t h) { return (double)(h >> 11) * (1.0 / 90071992547409
 tecs_oracle* tecs_oracle_create(const tecs_oracle_desc* desc) {
   if (!desc || (desc->dims != 2 && desc->dims != 3)) { set_err("dims must be 2 or 3"); return NULL; }
   if (desc->capacity == 0) { set_err("capacity must be > 0"); return NULL; }
+  if (desc->finder < 0 || desc->finder > TECS_O_NAIVE_DELAUNAY) { set_err("unknown finder"); return NULL; }
+  if (desc->finder == TECS_O_NAIVE_DELAUNAY && desc->symmetric) {
+    set_err("the Delaunay finder has no symmetric variant"); return NULL;
+  }
   tecs_oracle* o = (tecs_oracle*)calloc(1, sizeof *o);
   o->d = *desc;
   const size_t cap = desc->capacity, D = (size_t)desc->dims;
@@ -319,8 +323,86 @@ static int gabriel_blocked_naive(const tecs_oracle* o, const float* xin, unsigne
   return 0;
 }
 
+static float dist2(const float* a, const float* b, int D) {  /* vector.hpp distance_to_squared */
+  float s = 0.0f;
+  for (int d = 0; d < D; ++d) { float e = a[d] - b[d]; s = s + e * e; }
+  return s;
+}
+
+/* naive_delaunay.hpp: how many times the pair (i, j) is applied.
+ * 2-D (:45-99): once per third point k whose circumcircle through i, j, k is
+ * non-degenerate (|den| > eps) and holds no other point (<= r^2 rejects).
+ * 3-D (:158-292): once per third point k for which some l > k gives a
+ * non-degenerate tetrahedron whose circumsphere holds no other point (the
+ * axis-aligned prefilter |p_m - c| > r skips a point before its distance test). */
+static int delaunay_count(const tecs_oracle* o, const float* xin, unsigned i, unsigned j) {
+  const int D = o->d.dims;
+  const unsigned n = o->n;
+  const float eps = FLT_EPSILON;
+  const float* pi = xin + (size_t)i * D;
+  const float* pj = xin + (size_t)j * D;
+  int count = 0;
+  if (D == 2) {
+    const float li = dist2(pi, (const float[3]){0, 0, 0}, 2), lj = dist2(pj, (const float[3]){0, 0, 0}, 2);
+    for (unsigned k = 0; k < n; ++k) {
+      if (k == i || k == j) continue;
+      const float* pk = xin + (size_t)k * 2;
+      const float den = 2.0f * (pi[0] * (pj[1] - pk[1]) + pj[0] * (pk[1] - pi[1]) + pk[0] * (pi[1] - pj[1]));
+      if (fabsf(den) <= eps) continue;
+      const float lk = dist2(pk, (const float[3]){0, 0, 0}, 2);
+      float c[2];
+      c[0] = (li * (pj[1] - pk[1]) + lj * (pk[1] - pi[1]) + lk * (pi[1] - pj[1])) / den;
+      c[1] = (li * (pk[0] - pj[0]) + lj * (pi[0] - pk[0]) + lk * (pj[0] - pi[0])) / den;
+      const float r2 = dist2(pi, c, 2);
+      int ok = 1;
+      for (unsigned m = 0; m < n && ok; ++m) {
+        if (m == i || m == j || m == k) continue;
+        if (dist2(xin + (size_t)m * 2, c, 2) <= r2) ok = 0;
+      }
+      count += ok;
+    }
+    return count;
+  }
+  const float zero[3] = {0, 0, 0};
+  const float li = dist2(pi, zero, 3), lj = dist2(pj, zero, 3);
+  for (unsigned k = 0; k < n; ++k) {
+    if (k == i || k == j) continue;
+    const float* pk = xin + (size_t)k * 3;
+    const float lk = dist2(pk, zero, 3);
+    for (unsigned l = k + 1; l < n; ++l) {
+      if (l == i || l == j) continue;
+      const float* pl = xin + (size_t)l * 3;
+      float e1[3], e2[3], e3[3];
+      for (int d = 0; d < 3; ++d) { e1[d] = pj[d] - pi[d]; e2[d] = pk[d] - pi[d]; e3[d] = pl[d] - pi[d]; }
+      const float den = 2.0f * (e1[0] * (e2[1] * e3[2] - e2[2] * e3[1]) - e1[1] * (e2[0] * e3[2] - e2[2] * e3[0]) +
+                                e1[2] * (e2[0] * e3[1] - e2[1] * e3[0]));
+      if (fabsf(den) <= eps) continue;
+      const float ll = dist2(pl, zero, 3);
+      const float b1 = lj - li, b2 = lk - li, b3 = ll - li;
+      float c[3];
+      c[0] = pi[0] + (b1 * (e2[1] * e3[2] - e2[2] * e3[1]) - e1[1] * (b2 * e3[2] - e2[2] * b3) +
+                      e1[2] * (b2 * e3[1] - e2[1] * b3)) / den;
+      c[1] = pi[1] + (e1[0] * (b2 * e3[2] - e2[2] * b3) - b1 * (e2[0] * e3[2] - e2[2] * e3[0]) +
+                      e1[2] * (e2[0] * b3 - b2 * e3[0])) / den;
+      c[2] = pi[2] + (e1[0] * (e2[1] * b3 - b2 * e3[1]) - e1[1] * (e2[0] * b3 - b2 * e3[0]) +
+                      b1 * (e2[0] * e3[1] - e2[1] * e3[0])) / den;
+      const float r2 = dist2(pi, c, 3);
+      const float r = sqrtf(r2);
+      int ok = 1;
+      for (unsigned m = 0; m < n; ++m) {
+        if (m == i || m == j || m == k || m == l) continue;
+        const float* pm = xin + (size_t)m * 3;
+        if (fabsf(pm[0] - c[0]) > r || fabsf(pm[1] - c[1]) > r || fabsf(pm[2] - c[2]) > r) continue;
+        if (dist2(pm, c, 3) <= r2) { ok = 0; break; }
+      }
+      if (ok) { ++count; break; }
+    }
+  }
+  return count;
+}
+
 /* Candidate j for cell i: cutoff + Gabriel predicate, then the force.
- * Returns 1 when the pair is accepted. */
+ * Returns how many times the pair is applied: 0 or 1, or the Delaunay count. */
 static int visit_pair(const tecs_oracle* o, const float* xin, const float* pin, unsigned i, unsigned j,
                       const float* xi, acc_t* a) {
   const int D = o->d.dims;
@@ -333,9 +415,13 @@ static int visit_pair(const tecs_oracle* o, const float* xin, const float* pin, 
   if (d2 >= rc2) return 0;
   if (o->d.finder == TECS_O_BINNED_GABRIEL && gabriel_blocked_binned(o, xin, i, j, xi, disp, d2)) return 0;
   if (o->d.finder == TECS_O_NAIVE_GABRIEL && gabriel_blocked_naive(o, xin, i, j, xi, disp, d2)) return 0;
+  int reps = 1;
+  if (o->d.finder == TECS_O_NAIVE_DELAUNAY && (reps = delaunay_count(o, xin, i, j)) == 0) return 0;
   float dist = sqrtf(d2);
-  pair_force(o, disp, dist, pin ? pin + (size_t)i * 2 : NULL, pin ? pin + (size_t)j * 2 : NULL, a);
-  return 1;
+  /* each application adds into the cell's delta in turn (naive_delaunay.hpp:86-99) */
+  for (int r = 0; r < reps; ++r)
+    pair_force(o, disp, dist, pin ? pin + (size_t)i * 2 : NULL, pin ? pin + (size_t)j * 2 : NULL, a);
+  return reps;
 }
 
 /* One pass of finder.evaluate_force: in = (xin, pin), out = (ox, op).
@@ -435,9 +521,11 @@ static void eval_pass(tecs_oracle* o, const float* xin, const float* pin, float*
     } else {
       for (unsigned j = 0; j < n; ++j) {
         if (j == i) continue;
-        if (!visit_pair(o, xin, pin, i, j, xi, &a)) continue;
-        if (sink) { if (sink->count < sink->cap) { sink->pairs[2 * sink->count] = i; sink->pairs[2 * sink->count + 1] = j; } sink->count++; }
-        for (int d = 0; d < D; ++d) tvel[d] = tvel[d] + 0.0f * o->vold[(size_t)j * D + d];
+        const int reps = visit_pair(o, xin, pin, i, j, xi, &a);
+        for (int r = 0; r < reps; ++r) {
+          if (sink) { if (sink->count < sink->cap) { sink->pairs[2 * sink->count] = i; sink->pairs[2 * sink->count + 1] = j; } sink->count++; }
+          for (int d = 0; d < D; ++d) tvel[d] = tvel[d] + 0.0f * o->vold[(size_t)j * D + d];
+        }
       }
     }
     /* commit: views(i) += total; first(i) += total_velocity / fmax(total_drag, eps) */

@@ -29,7 +29,8 @@ enum {
   TECS_O_NAIVE_ALL_PAIRS = 0,   /* naive_all_pairs.hpp:41-103          */
   TECS_O_BINNED_ALL_PAIRS = 1,  /* binned_all_pairs.hpp:66-183         */
   TECS_O_NAIVE_GABRIEL = 2,     /* naive_gabriel.hpp:36-120            */
-  TECS_O_BINNED_GABRIEL = 3     /* binned_gabriel.hpp:71-362           */
+  TECS_O_BINNED_GABRIEL = 3,    /* binned_gabriel.hpp:71-362           */
+  TECS_O_NAIVE_DELAUNAY = 4     /* naive_delaunay.hpp:31-294           */
 };
 
 /* Built-in pairwise force laws. */

@@ -182,7 +182,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   if (run && !fb) {
     const GridP& g = sl.g;
     const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
-    unsigned rlo[9], rhi[9], rb0[9];
+    unsigned rlo[9], rhi[9], rb0[9], rmask[9];
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
       const int cy = bc[1] + r % 3 - 1, cz = bc[2] + r / 3 - 1;
@@ -195,25 +195,39 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     }
     const int rxo = x0 - bc[0] + 1;
     const float rc2 = sl.fp.rc2;
+    int total = 0;
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
-      const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(r / 3);
-      for (unsigned j0 = rlo[r]; j0 < rhi[r] && !fb; j0 += 4u) {
+      unsigned m = 0u;
+      if (rhi[r] - rlo[r] > 32u) { fb = true; rmask[r] = 0u; continue; }
+      for (unsigned j0 = rlo[r]; j0 < rhi[r]; j0 += 4u) {
         float4 v[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          v[k] = (j0 + k < rhi[r]) ? __ldg(&e.X[j0 + k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < 4; ++k) v[k] = __ldg(&e.X[min(j0 + k, rhi[r] - 1u)]);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const unsigned j = j0 + k;
-          if (j >= rhi[r] || j == i || fb) continue;
           const float e0 = xi[0] - v[k].x, e1 = xi[1] - v[k].y, e2 = xi[2] - v[k].z;
           float d2 = e0 * e0 + e1 * e1;
           d2 = d2 + e2 * e2;
-          if (d2 >= rc2) continue;
-          if (cnt == kMaxNb) { fb = true; continue; }
-          const unsigned rx = (unsigned)((int)(__float_as_uint(v[k].w) - rb0[r]) + rxo);
-          cand[cix(cnt, t)] = make_float4(v[k].x, v[k].y, v[k].z, __uint_as_float((j << 5) | (rowcode + rx)));
+          if (j < rhi[r] && j != i && d2 < rc2) m |= 1u << (j - rlo[r]);
+        }
+      }
+      rmask[r] = m;
+      total += __popc(m);
+    }
+    if (total > kMaxNb) fb = true;
+    if (!fb) {
+#pragma unroll
+      for (int r = 0; r < 9; ++r) {
+        const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(r / 3);
+        unsigned m = rmask[r];
+        while (m) {
+          const unsigned j = rlo[r] + (unsigned)(__ffs(m) - 1);
+          m &= m - 1u;
+          const float4 v = __ldg(&e.X[j]);
+          const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
+          cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
           ++cnt;
         }
       }
@@ -445,6 +459,7 @@ struct tecs_engine {
   std::vector<int> pending_free;
   cudaGraphExec_t graph = nullptr;
   float gdt = 0.f;
+  unsigned gC = 0, gNB = 0;  // the extents the captured graph covers (cells, bins)
   int kernels = 7;
 };
 
@@ -479,20 +494,30 @@ void bins_free(tecs_engine* e, unsigned base, unsigned nb) {
   }
 }
 
+// The step's grids cover a power-of-two class of the resident cells and of the
+// highest allocated bin, not the whole capacity: a server sized for hundreds of
+// millions of cells then pays per step only for what it holds.  The graph is
+// captured again when a class changes.
+unsigned extent_class(unsigned long long v, unsigned cap) {
+  unsigned long long p = 4096;
+  while (p < v && p < cap) p <<= 1;
+  return (unsigned)std::min<unsigned long long>(p, cap);
+}
+
 int enqueue_engine_step(tecs_engine* e, float dt) {
-  const unsigned gb = cdiv(e->C, 256);
-  const unsigned len = e->NB + 1;
+  const unsigned gb = cdiv(e->gC, 256);
+  const unsigned len = e->gNB + 1;
   const unsigned chunks = cdiv(len, kScanChunk);
   k_ecount<<<gb, 256, 0, e->stream>>>(e->A, e->Asim, e->ctr, e->table, e->key, e->rank, e->cnt);
   k_scan_reduce<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part);
   k_scan_apply<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part, e->off);
   k_escatter<<<gb, 256, 0, e->stream>>>(e->ctr, e->key, e->rank, e->off, e->src);
-  k_eorder_gather<<<gb, 256, 0, e->stream>>>(e->off, e->NB, e->key, e->src, e->A, e->PA, e->Asim, e->B, e->PB,
+  k_eorder_gather<<<gb, 256, 0, e->stream>>>(e->off, e->gNB, e->key, e->src, e->A, e->PA, e->Asim, e->B, e->PB,
                                              e->Bid, e->Bsim);
   EngArgs a{};
   a.table = e->table;
   a.off = e->off;
-  a.nb_total = e->NB;
+  a.nb_total = e->gNB;
   a.Bx = e->B;
   a.Bp = e->PB;
   a.Bid = e->Bid;
@@ -508,11 +533,11 @@ int enqueue_engine_step(tecs_engine* e, float dt) {
   EngArgs a1 = a;
   a1.X = e->B;
   a1.P = e->PB;
-  k_epass<1><<<cdiv(e->C, kPassThreads), kPassThreads, 0, e->stream>>>(a1);
+  k_epass<1><<<cdiv(e->gC, kPassThreads), kPassThreads, 0, e->stream>>>(a1);
   EngArgs a2 = a;
   a2.X = e->Xt;
   a2.P = e->Pt;
-  k_epass<2><<<cdiv(e->C, kPassThreads), kPassThreads, 0, e->stream>>>(a2);
+  k_epass<2><<<cdiv(e->gC, kPassThreads), kPassThreads, 0, e->stream>>>(a2);
   ECK(cudaGetLastError());
   return 0;
 }
@@ -700,6 +725,22 @@ int tecs_engine_remove(tecs_engine* e, int slot) {
   e->htable[slot].active = 0;
   e->table_dirty = true;
   e->pending_free.push_back(slot);
+  // Cells and bins of removed simulations are returned by the next step's sort.
+  // With none active, nothing resident is needed: return everything now, so an
+  // idle engine admits again without a step.
+  bool any = false;
+  for (unsigned k = 0; k < e->S && !any; ++k) any = e->info[k].used && e->info[k].active;
+  if (!any) {
+    for (int k : e->pending_free) {
+      tecs_engine::Info& J = e->info[k];
+      bins_free(e, J.bin_base, J.nbins);
+      J = tecs_engine::Info{};
+      e->htable[k] = SimSlot{};
+    }
+    e->pending_free.clear();
+    e->n_resident = 0;
+    e->n_dirty = true;
+  }
   return 0;
 }
 
@@ -721,8 +762,14 @@ int tecs_engine_step(tecs_engine* e, double dt, int n_steps) {
       ECK(cudaMemcpyAsync(&e->ctr->n, &e->hctr->n, 4, cudaMemcpyHostToDevice, e->stream));
       e->n_dirty = false;
     }
-    if (!e->graph || e->gdt != fdt) {
+    unsigned hwm = 0;
+    for (unsigned k = 0; k < e->S; ++k)
+      if (e->info[k].used) hwm = std::max(hwm, e->info[k].bin_base + e->info[k].nbins);
+    const unsigned wantC = extent_class(e->n_resident, e->C), wantNB = extent_class(hwm, e->NB);
+    if (!e->graph || e->gdt != fdt || wantC != e->gC || wantNB != e->gNB) {
       if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+      e->gC = wantC;
+      e->gNB = wantNB;
       cudaGraph_t g;
       ECK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_engine_step(e, fdt);

@@ -10,6 +10,8 @@
 //   cnt,off             uint[nbins+1] bin counts (zero between steps), offsets
 #pragma once
 
+#include <cfloat>
+
 #include "common.cuh"
 #include "forces.cuh"
 
@@ -52,7 +54,7 @@ struct PassArgs {
   float dt;
   int mode;
   // centre-of-mass reduction (GlobalComFixer) fused into kStore
-  double* com_part;     // 3 doubles per block
+  double* com_part;     // fixed-point (2^-32) int64 sums, 3 per slot, reused as such
   float* com_out;       // 3 floats
   int com_slot;         // 0 or 1 (which done counter)
   unsigned capacity;
@@ -77,6 +79,8 @@ struct PassArgs {
   unsigned* key;
   unsigned* rank;
   unsigned* cnt;
+  // naive Delaunay: how many times each directed pair is applied, row i at i * capacity
+  const unsigned short* dmult;
 };
 
 // ---------------------------------------------------------------------------
@@ -409,6 +413,121 @@ __device__ __forceinline__ bool gabriel_blocked_naive(const ForceP& fp, const fl
   return false;
 }
 
+// ---------------------------------------------------------------------------
+// Naive Delaunay (naive_delaunay.hpp).  The reference applies the pair (i, j)
+// once per accepted simplex: in 2-D per third point k whose circumcircle
+// through i, j, k is non-degenerate (|den| > FLT_EPSILON) and holds no other
+// point (distance^2 <= r^2 rejects); in 3-D per third point k for which some
+// l > k spans a non-degenerate tetrahedron with an empty circumsphere (a point
+// outside the axis-aligned box |p - c| <= r is skipped before its distance
+// test).  k_delaunay_mult counts the applications of every in-cutoff pair,
+// one block per cell i with the threads spread over k; the force pass then
+// adds the pair's force that many times, in j order -- the Serial order.
+template <int D>
+__device__ __forceinline__ float sq_len(const float4& v) {
+  float s = v.x * v.x + v.y * v.y;
+  if (D >= 3) s = s + v.z * v.z;
+  return s;
+}
+
+template <int D>
+__device__ __forceinline__ float sq_dist(const float4& v, const float* c) {
+  const float e0 = v.x - c[0], e1 = v.y - c[1];
+  float s = e0 * e0 + e1 * e1;
+  if (D >= 3) { const float e2 = v.z - c[2]; s = s + e2 * e2; }
+  return s;
+}
+
+__device__ __forceinline__ bool delaunay_triangle_empty(const float4* __restrict__ X, unsigned n, unsigned i,
+                                                        unsigned j, unsigned k, const float4& pi, const float4& pj,
+                                                        float li, float lj) {
+  const float4 pk = __ldg(&X[k]);
+  const float den = 2.0f * (pi.x * (pj.y - pk.y) + pj.x * (pk.y - pi.y) + pk.x * (pi.y - pj.y));
+  if (fabsf(den) <= FLT_EPSILON) return false;
+  const float lk = sq_len<2>(pk);
+  float c[2];
+  c[0] = (li * (pj.y - pk.y) + lj * (pk.y - pi.y) + lk * (pi.y - pj.y)) / den;
+  c[1] = (li * (pk.x - pj.x) + lj * (pi.x - pk.x) + lk * (pj.x - pi.x)) / den;
+  const float r2 = sq_dist<2>(pi, c);
+  for (unsigned m = 0; m < n; ++m) {
+    if (m == i || m == j || m == k) continue;
+    if (sq_dist<2>(__ldg(&X[m]), c) <= r2) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool delaunay_any_tetrahedron(const float4* __restrict__ X, unsigned n, unsigned i,
+                                                         unsigned j, unsigned k, const float4& pi, const float4& pj,
+                                                         float li, float lj) {
+  const float4 pk = __ldg(&X[k]);
+  const float lk = sq_len<3>(pk);
+  for (unsigned l = k + 1; l < n; ++l) {
+    if (l == i || l == j) continue;
+    const float4 pl = __ldg(&X[l]);
+    const float e1[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+    const float e2[3] = {pk.x - pi.x, pk.y - pi.y, pk.z - pi.z};
+    const float e3[3] = {pl.x - pi.x, pl.y - pi.y, pl.z - pi.z};
+    const float den = 2.0f * (e1[0] * (e2[1] * e3[2] - e2[2] * e3[1]) - e1[1] * (e2[0] * e3[2] - e2[2] * e3[0]) +
+                              e1[2] * (e2[0] * e3[1] - e2[1] * e3[0]));
+    if (fabsf(den) <= FLT_EPSILON) continue;
+    const float b1 = lj - li, b2 = lk - li, b3 = sq_len<3>(pl) - li;
+    float c[3];
+    c[0] = pi.x + (b1 * (e2[1] * e3[2] - e2[2] * e3[1]) - e1[1] * (b2 * e3[2] - e2[2] * b3) +
+                   e1[2] * (b2 * e3[1] - e2[1] * b3)) / den;
+    c[1] = pi.y + (e1[0] * (b2 * e3[2] - e2[2] * b3) - b1 * (e2[0] * e3[2] - e2[2] * e3[0]) +
+                   e1[2] * (e2[0] * b3 - b2 * e3[0])) / den;
+    c[2] = pi.z + (e1[0] * (e2[1] * b3 - b2 * e3[1]) - e1[1] * (e2[0] * b3 - b2 * e3[0]) +
+                   b1 * (e2[0] * e3[1] - e2[1] * e3[0])) / den;
+    const float r2 = sq_dist<3>(pi, c);
+    const float r = sqrtf(r2);
+    bool ok = true;
+    for (unsigned m = 0; m < n; ++m) {
+      if (m == i || m == j || m == k || m == l) continue;
+      const float4 pm = __ldg(&X[m]);
+      if (fabsf(pm.x - c[0]) > r || fabsf(pm.y - c[1]) > r || fabsf(pm.z - c[2]) > r) continue;
+      if (sq_dist<3>(pm, c) <= r2) { ok = false; break; }
+    }
+    if (ok) return true;
+  }
+  return false;
+}
+
+constexpr int kDelaunayThreads = 128;
+constexpr unsigned kDelaunayMaxCells = 4096;  // the pair-count table is capacity^2 x 2 bytes
+
+template <int D>
+static __global__ void __launch_bounds__(kDelaunayThreads)
+k_delaunay_mult(const float4* __restrict__ X, const Counters* __restrict__ ctr, float rc2, unsigned stride,
+                unsigned short* __restrict__ mult) {
+  __shared__ unsigned cnt;
+  const unsigned n = ctr->n;
+  const unsigned i = blockIdx.x;
+  if (i >= n) return;
+  const float4 pi = __ldg(&X[i]);
+  const float li = sq_len<D>(pi);
+  for (unsigned j = 0; j < n; ++j) {
+    if (j == i) continue;
+    const float4 pj = __ldg(&X[j]);
+    const float e0 = pi.x - pj.x, e1 = pi.y - pj.y;
+    float d2 = e0 * e0 + e1 * e1;
+    if (D >= 3) { const float e2 = pi.z - pj.z; d2 = d2 + e2 * e2; }
+    if (d2 >= rc2) continue;  // the same test, on the same values, in every thread
+    if (threadIdx.x == 0) cnt = 0u;
+    __syncthreads();
+    const float lj = sq_len<D>(pj);
+    unsigned local = 0;
+    for (unsigned k = threadIdx.x; k < n; k += kDelaunayThreads) {
+      if (k == i || k == j) continue;
+      local += (D == 2 ? delaunay_triangle_empty(X, n, i, j, k, pi, pj, li, lj)
+                       : delaunay_any_tetrahedron(X, n, i, j, k, pi, pj, li, lj)) ? 1u : 0u;
+    }
+    if (local) atomicAdd(&cnt, local);
+    __syncthreads();
+    if (threadIdx.x == 0) mult[(size_t)i * stride + j] = (unsigned short)cnt;
+    __syncthreads();
+  }
+}
+
 template <int D, int FINDER, int FORCE>
 __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
                                       unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi) {
@@ -422,13 +541,16 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
   if (d2 >= fp.rc2) return;
   if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
   if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
+  unsigned reps = 1;
+  if (FINDER == 4 && (reps = a.dmult[(size_t)i * a.capacity + j]) == 0u) return;
   if (a.pairs) {
-    unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, id_at(a.X, a.Bid, j));
+    unsigned long long s = atomicAdd(&a.ctr->pair_count, (unsigned long long)reps);
+    for (unsigned r = 0; r < reps; ++r)
+      if (s + r < a.pair_cap) a.pairs[s + r] = make_uint2(idi, id_at(a.X, a.Bid, j));
   }
   const float dist = sqrtf(d2);
   const float2 pj = (FORCE == 2 && a.P) ? a.P[j] : make_float2(0.f, 0.f);
-  pair_force<D, FORCE>(fp, disp, dist, pi, pj, acc);
+  for (unsigned r = 0; r < reps; ++r) pair_force<D, FORCE>(fp, disp, dist, pi, pj, acc);
 }
 
 // Commit of one cell: out(i) = 0 + sum (views(i) += values on cleared stage
@@ -715,8 +837,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     if (a.P) pi = a.P[i];
     bin_coords_div<D>(g, xi, bc);
     constexpr int kRows = D >= 3 ? 9 : 3;
-    unsigned rlo[kRows], rhi[kRows], rb0[kRows];
-    int rx0[kRows];
+    unsigned rlo[kRows], rhi[kRows], rb0[kRows], rmask[kRows];
     const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
 #pragma unroll
     for (int r = 0; r < kRows; ++r) {
@@ -726,29 +847,45 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       int c0[3] = {x0, ok ? cy : 0, ok ? cz : 0};
       const unsigned b0 = flatten<D>(g, c0);
       rb0[r] = b0;
-      rx0[r] = x0 - bc[0] + 1;
       rlo[r] = ok ? __ldg(&a.off[b0]) : 0u;
       rhi[r] = ok ? __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]) : 0u;
     }
+    // 1a: test every candidate, remembering the in-cutoff ones as bits per row
+    int total = 0;
 #pragma unroll
     for (int r = 0; r < kRows; ++r) {
-      const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(D >= 3 ? r / 3 : 1);
-      for (unsigned j0 = rlo[r]; j0 < rhi[r] && !fb; j0 += 4u) {
+      unsigned m = 0u;
+      if (rhi[r] - rlo[r] > 32u) { fb = true; rmask[r] = 0u; continue; }
+      for (unsigned j0 = rlo[r]; j0 < rhi[r]; j0 += 4u) {
         float4 v[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          v[k] = (j0 + k < rhi[r]) ? __ldg(&a.X[j0 + k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < 4; ++k) v[k] = __ldg(&a.X[min(j0 + k, rhi[r] - 1u)]);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const unsigned j = j0 + k;
-          if (j >= rhi[r] || j == i || fb) continue;
           const float e0 = xi[0] - v[k].x, e1 = xi[1] - v[k].y;
           float d2 = e0 * e0 + e1 * e1;
           if (D >= 3) { const float e2 = xi[2] - v[k].z; d2 = d2 + e2 * e2; }
-          if (d2 >= fp.rc2) continue;
-          if (cnt == kMaxNb) { fb = true; continue; }
-          const unsigned rx = (unsigned)((int)(__float_as_uint(v[k].w) - rb0[r]) + rx0[r]);
-          cand[cix(cnt, t)] = make_float4(v[k].x, v[k].y, v[k].z, __uint_as_float((j << 5) | (rowcode + rx)));
+          if (j < rhi[r] && j != i && d2 < fp.rc2) m |= 1u << (j - rlo[r]);
+        }
+      }
+      rmask[r] = m;
+      total += __popc(m);
+    }
+    if (total > kMaxNb) fb = true;
+    // 1b: append the in-cutoff candidates in candidate order (the summation order)
+    if (!fb) {
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(D >= 3 ? r / 3 : 1);
+        const int rxo = x0 - bc[0] + 1;
+        unsigned m = rmask[r];
+        while (m) {
+          const unsigned j = rlo[r] + (unsigned)(__ffs(m) - 1);
+          m &= m - 1u;
+          const float4 v = __ldg(&a.X[j]);
+          const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
+          cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
           ++cnt;
         }
       }

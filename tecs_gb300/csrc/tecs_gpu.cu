@@ -91,6 +91,7 @@ struct tecs_sim {
   unsigned *key = nullptr, *rank = nullptr, *src = nullptr, *cnt = nullptr, *off = nullptr, *part = nullptr;
   unsigned *div_parent = nullptr, *div_slot = nullptr;
   unsigned* Bid = nullptr;  // cell ids of B's slots (B.w holds the bin key)
+  unsigned short* dmult = nullptr;  // naive Delaunay: applications per directed pair, capacity x capacity
   Counters* ctr = nullptr;
   double* com_part = nullptr;
   float* com = nullptr;  // [0..2] pass 1, [4..6] pass 2
@@ -167,6 +168,13 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
   }
   PICK(3, 0) PICK(3, 1) PICK(3, 2) PICK(3, 3) PICK(2, 0) PICK(2, 1) PICK(2, 2) PICK(2, 3)
 #undef PICK
+  if (F == TECS_FINDER_NAIVE_DELAUNAY && !sym) {
+    if (D == 3 && FO == 0) return k_pass<3, 4, 0>;
+    if (D == 3 && FO == 1) return k_pass<3, 4, 1>;
+    if (D == 3 && FO == 2) return k_pass<3, 4, 2>;
+    if (D == 2 && FO == 0) return k_pass<2, 4, 0>;
+    if (D == 2 && FO == 1) return k_pass<2, 4, 1>;
+  }
   return nullptr;
 }
 
@@ -194,6 +202,7 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.key = s->key;
   a.rank = s->rank;
   a.cnt = s->cnt;
+  a.dmult = s->dmult;
   return a;
 }
 
@@ -242,6 +251,16 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   if (!fn) return fail("unsupported finder/force/dims combination");
   const unsigned L = launch_count(s);
   const unsigned blocks = ceil_div(L ? L : 1, 128);
+  if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY) {
+    // applications per pair on this pass's positions, then the pass
+    PROF_BEGIN(s);
+    if (s->d.dims == 3) k_delaunay_mult<3><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2,
+                                                                                         s->d.capacity, s->dmult);
+    else k_delaunay_mult<2><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2, s->d.capacity,
+                                                                             s->dmult);
+    PROF_END(s, "k_delaunay_mult");
+    K += 1;
+  }
   PROF_BEGIN(s);
   fn<<<blocks, 128, 0, s->stream>>>(s->g, s->fp, a);
   PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
@@ -409,7 +428,11 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   *out = nullptr;
   if (desc->dims != 2 && desc->dims != 3) return fail("dims must be 2 or 3");
   if (desc->capacity == 0) return fail("capacity must be > 0");
-  if (desc->finder < 0 || desc->finder > 3) return fail("unknown finder");
+  if (desc->finder < 0 || desc->finder > TECS_FINDER_NAIVE_DELAUNAY) return fail("unknown finder");
+  if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY && desc->symmetric)
+    return fail("the Delaunay finder has no symmetric variant");
+  if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY && desc->capacity > kDelaunayMaxCells)
+    return fail("the naive Delaunay finder holds at most 4096 cells");
   if (desc->force < 0 || desc->force > 2) return fail("unknown force");
   if (desc->force == TECS_FORCE_POLARITY && (desc->dims != 3 || !desc->has_polarity))
     return fail("the polarity force needs dims 3 and a polarity field");
@@ -460,6 +483,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   ok = ok && alloc((void**)&s->key, cap * 4) && alloc((void**)&s->rank, cap * 4) && alloc((void**)&s->src, cap * 4);
   ok = ok && alloc((void**)&s->div_parent, cap * 4) && alloc((void**)&s->div_slot, cap * 4);
   if (s->binned) ok = ok && alloc((void**)&s->Bid, cap * 4);
+  if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY) ok = ok && alloc((void**)&s->dmult, cap * cap * 2);
   if (s->binned) {
     const size_t len = (size_t)g.nbins + 1;
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
@@ -490,7 +514,7 @@ int tecs_sim_destroy(tecs_sim* s) {
     if (e) cudaEventDestroy(e);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
-                  s->Bid};
+                  s->Bid, s->dmult};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -696,6 +720,25 @@ int tecs_sim_set_graph(tecs_sim* s, int enable) {
   if (!s) return fail("null simulation");
   s->use_graph = enable != 0;
   if (!s->use_graph) drop_graphs(s);
+  return 0;
+}
+
+int tecs_sim_set_force(tecs_sim* s, int force, float k_rep, float r_rep, float k_adh, float r_adh, float k_pol) {
+  if (!s) return fail("null simulation");
+  if (force < 0 || force > 2) return fail("unknown force");
+  if (force == TECS_FORCE_POLARITY && (s->d.dims != 3 || !s->d.has_polarity))
+    return fail("the polarity force needs dims 3 and a polarity field");
+  ForceP& f = s->fp;
+  if (f.force == force && f.k_rep == k_rep && f.r_rep == r_rep && f.k_adh == k_adh && f.r_adh == r_adh &&
+      f.k_pol == k_pol)
+    return 0;
+  // queued steps read the old constants through their graph's kernel arguments
+  CK(cudaStreamSynchronize(s->stream));
+  s->d.force = force;
+  s->d.k_rep = k_rep; s->d.r_rep = r_rep; s->d.k_adh = k_adh; s->d.r_adh = r_adh; s->d.k_pol = k_pol;
+  f.force = force;
+  f.k_rep = k_rep; f.r_rep = r_rep; f.k_adh = k_adh; f.r_adh = r_adh; f.k_pol = k_pol;
+  drop_graphs(s);
   return 0;
 }
 

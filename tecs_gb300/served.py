@@ -135,6 +135,7 @@ class Server:
                  dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0):
         self.engine = Engine(cell_capacity, bin_capacity, max_sims, device)
         self.cell_capacity = cell_capacity
+        self.bin_capacity = bin_capacity
         self.dt = dt
         self.snapshot_every = snapshot_every
         self.writer = SnapshotWriter(sink)
@@ -176,9 +177,13 @@ class Server:
         """Serve the requests; arrival times are divided by time_scale.  Returns the results."""
         reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival_s)
         built = {}
-        if prebuild:
-            for idx, r in reqs:
-                built[idx] = request_sim(r, max_cells)
+        for idx, r in reqs:
+            sim = request_sim(r, max_cells)
+            if len(sim[0]) > self.cell_capacity or bins_needed(sim[2]) > self.bin_capacity:
+                raise ValueError(f"request {idx} ({len(sim[0])} cells, {bins_needed(sim[2])} bins) "
+                                 f"exceeds the engine ({self.cell_capacity} cells, {self.bin_capacity} bins)")
+            if prebuild:
+                built[idx] = sim
         waiting = collections.deque()
         live: Dict[int, Live] = {}
         results: List[Result] = []
@@ -201,6 +206,8 @@ class Server:
                 slot = self.engine.add(d, x, p)
                 live[slot] = Live(requests[idx], slot, len(x), p is not None, 0, time.perf_counter() - t0, idx)
             if not live:
+                if waiting:  # an idle engine holds nothing: the head request must fit
+                    raise RuntimeError(f"request {waiting[0]} cannot be admitted into an idle engine")
                 if k < len(reqs):
                     time.sleep(max(0.0, min(0.01, arrival[reqs[k][0]] - (time.perf_counter() - t0))))
                 continue

@@ -51,6 +51,9 @@ SCENARIOS = {
     "bg_heun_polarity": ("bg_heun_pol_3", 3, 0, 1, 0, 3, 1),
     "ng_euler_2d_points11": ("ng_euler_2", 2, 0, 0, 0, 2, 0),
     "bg_heun_2d": ("bg_heun_2", 3, 0, 1, 0, 2, 0),
+    "nd_euler_2d": ("nd_euler_2", 4, 0, 0, 0, 2, 0),
+    "nd_euler_2d_points11": ("nd_euler_2", 4, 0, 0, 0, 2, 0),
+    "nd_heun_3d": ("nd_heun_3", 4, 0, 1, 0, 3, 0),
 }
 
 
@@ -102,7 +105,7 @@ def inputs(name):
         mn, mx = wl.bounds_for(x)
         prm[12] = 0.2
         steps, dt = 5, 0.05
-    elif name == "ng_euler_2d_points11":
+    elif name in ("ng_euler_2d_points11", "nd_euler_2d_points11"):
         x = main_cpp_points()
         prm[0] = 2.5
         mn, mx, steps, dt = (-20, -20, 0), (20, 20, 0), 3, 0.01
@@ -110,6 +113,12 @@ def inputs(name):
         x = np.ascontiguousarray(wl.ball(1500, 13)[:, :2] * 0.4)
         m = float(np.ceil(np.abs(x).max() + 2))
         mn, mx, steps, dt = (-m, -m, 0), (m, m, 0), 10, 0.05
+    elif name == "nd_euler_2d":
+        x = np.ascontiguousarray(wl.ball(120, 14)[:, :2])
+        mn, mx, steps, dt = (-20, -20, 0), (20, 20, 0), 4, 0.02
+    elif name == "nd_heun_3d":
+        x = wl.ball(48, 15)
+        mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
     else:
         raise KeyError(name)
     prm[2:5] = mn

@@ -113,3 +113,21 @@ def test_engine_rejects_what_it_cannot_run():
     eng.add(d, x)
     with pytest.raises(tg.TecsError, match="capacity"):
         eng.add(d, x)
+
+
+def test_idle_engine_returns_everything_at_remove():
+    a = spec(3000, 51, "binned_gabriel", "heun")
+    b = spec(2000, 52, "binned_all_pairs", "euler")
+    nb = bins_needed(a[2]) + bins_needed(b[2])
+    eng = Engine(cell_capacity=5000, bin_capacity=nb, max_sims=4)
+    sa = eng.add(a[2], a[0])
+    sb = eng.add(b[2], b[0])
+    eng.step(0.05, 2)
+    eng.remove(sa)
+    assert eng.free()[0] == 0  # cells of a removed simulation leave at the next sort
+    eng.remove(sb)
+    assert eng.free() == (5000, nb)  # nothing active: all returned without a step
+    sc = eng.add(a[2], a[0])
+    eng.step(0.05, 3)
+    xc, _ = eng.download(sc)
+    np.testing.assert_array_equal(xc, plain_run(a[0], None, a[3], "binned_gabriel", "heun", a[4], False, 3)[0])

@@ -33,6 +33,9 @@ KIND = {
     "bg_heun_polarity": (3, 0, 1, 0, 3, 1),
     "ng_euler_2d_points11": (2, 0, 0, 0, 2, 0),
     "bg_heun_2d": (3, 0, 1, 0, 2, 0),
+    "nd_euler_2d": (4, 0, 0, 0, 2, 0),
+    "nd_euler_2d_points11": (4, 0, 0, 0, 2, 0),
+    "nd_heun_3d": (4, 0, 1, 0, 3, 0),
 }
 
 
@@ -94,3 +97,20 @@ def test_points11_gabriel_neighbour_counts():
     s = {tuple(p) for p in pairs.tolist()}
     assert all((j, i) in s for i, j in s)
     assert counts.sum() == len(pairs) and counts.min() >= 1
+
+
+def test_delaunay_applies_a_pair_once_per_empty_simplex():
+    # naive_delaunay.hpp applies (i, j) once per accepted triangle (2-D) or per
+    # third point with an accepted tetrahedron (3-D): pairs repeat, and every
+    # repeated application is still a directed pair within the cutoff
+    for name in ("nd_euler_2d", "nd_heun_3d"):
+        g = load(name)
+        pairs = g["pairs"]
+        uniq, counts = np.unique(pairs, axis=0, return_counts=True)
+        assert counts.max() >= 2
+        x = g["x0"]
+        d2 = ((x[uniq[:, 0]] - x[uniq[:, 1]]) ** 2).sum(1)
+        assert (d2 < float(g["prm"][0]) ** 2).all()
+    # in 2-D an edge borders at most two triangles of points in general position
+    u, c = np.unique(load("nd_euler_2d")["pairs"], axis=0, return_counts=True)
+    assert c.max() <= 2

@@ -26,6 +26,7 @@ FINDER_MAP = {
     "binned_all_pairs": oracle.BINNED_ALL_PAIRS,
     "naive_gabriel": oracle.NAIVE_GABRIEL,
     "binned_gabriel": oracle.BINNED_GABRIEL,
+    "naive_delaunay": oracle.NAIVE_DELAUNAY,
 }
 
 
@@ -283,3 +284,53 @@ def test_dense_packing_neighbour_overflow():
     g.take_step(0.05, 3)
     c.step(0.05, 3)
     np.testing.assert_array_equal(g.get_state()[0], c.get_state()[0])
+
+
+# ---------------------------------------------------------------------------
+# naive Delaunay (naive_delaunay.hpp): a pair is applied once per accepted
+# simplex, so pair lists are compared as multisets and sums stay in j order
+
+@pytest.mark.parametrize("dims,n,integrator,steps", [(2, 300, "euler", 4), (3, 90, "heun", 2)])
+def test_delaunay_pairs_deltas_and_steps_bit_exact(dims, n, integrator, steps):
+    x = ball(n, seed=21)
+    if dims == 2:
+        x = np.ascontiguousarray(x[:, :2])
+    bounds = ((-20,) * 3, (20,) * 3)
+    g, c = make_pair(x, finder="naive_delaunay", dims=dims, integrator=integrator, bounds=bounds)
+    dg, _, pg = g.evaluate()
+    dc, _, pc = c.evaluate()
+    assert len(np.unique(pc, axis=0)) < len(pc)  # some pairs apply more than once
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
+    np.testing.assert_array_equal(dg, dc)
+    g.take_step(0.02, steps)
+    c.step(0.02, steps)
+    np.testing.assert_array_equal(g.get_state()[0], c.get_state()[0])
+
+
+@pytest.mark.parametrize("name", ["nd_euler_2d", "nd_euler_2d_points11", "nd_heun_3d"])
+def test_delaunay_matches_reference_fixtures(name):
+    # the fixtures hold the reference's own outputs (tests/golden/make_golden.py)
+    from pathlib import Path
+    gold = dict(np.load(Path(__file__).resolve().parent / "golden" / f"{name}.npz"))
+    prm = gold["prm"]
+    dims = gold["x0"].shape[1]
+    x = gold["x0"]
+    pf = tg.PairFinderSettings(min_bounds=tuple(prm[2:5]), max_bounds=tuple(prm[5:8]))
+    integ = "heun" if name.endswith("3d") else "euler"
+    s = tg.Simulation(tg.Settings(agent_count=len(x), capacity=len(x), cutoff_distance=float(prm[0]),
+                                  pair_finder_settings=pf), dims=dims, pair_finder="naive_delaunay",
+                      integrator=integ, force=tg.Spring2R())
+    s.set_state(x)
+    dg, _, pg = s.evaluate()
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(gold["pairs"]))
+    np.testing.assert_array_equal(dg, gold["dpos"])
+    s.take_step(float(gold["dt"]), int(gold["steps"]))
+    np.testing.assert_array_equal(s.get_state()[0], gold["pos"])
+
+
+def test_delaunay_rejects_symmetric_and_large_capacity():
+    x = ball(50, seed=2)
+    with pytest.raises(tg.TecsError):
+        make_pair(x, finder="naive_delaunay", symmetric=True)
+    with pytest.raises(tg.TecsError, match="4096"):
+        make_pair(x, finder="naive_delaunay", capacity=5000)
