@@ -1,0 +1,152 @@
+// tecs/components.hpp -- the pair finders, integrators, centre-of-mass fixers
+// and force laws a simulation config selects, as the C++20 drop-in layer
+// names them.
+//
+// The reference's components are class templates that do the work
+// themselves; here each one is a selector that keeps the reference's name,
+// template signature and Settings (field names and defaults), and carries the
+// enum of the CUDA implementation behind include/tecs_gpu.h:
+//
+//   pair_finders::NaiveAllPairs, BinnedAllPairs, NaiveGabriel, BinnedGabriel,
+//     their *Symmetric variants, NaiveDelaunay    include/pair_finders/*.hpp
+//   integrators::Euler, Heun                      include/integrators/{euler,heun}.hpp
+//   com_fixers::NoComFixer, GlobalComFixer        include/com_fixers/com_fixers.hpp:11-45
+//   forces::Spring2R, PolaritySpring              the built-in pairwise laws
+#ifndef TECS_CXX_COMPONENTS_HPP
+#define TECS_CXX_COMPONENTS_HPP
+
+#include "../tecs_gpu.h"
+#include "vector.hpp"
+
+namespace tecs {
+
+namespace pair_finders {
+
+namespace detail {
+template <int Id, bool Sym>
+struct Tag {
+  static constexpr int finder_id = Id;
+  static constexpr bool symmetric = Sym;
+  static constexpr bool binned = Id == TECS_FINDER_BINNED_ALL_PAIRS || Id == TECS_FINDER_BINNED_GABRIEL;
+  static constexpr bool gabriel = Id == TECS_FINDER_NAIVE_GABRIEL || Id == TECS_FINDER_BINNED_GABRIEL;
+};
+
+// Settings of the naive finders: none (naive_all_pairs.hpp, naive_delaunay.hpp)
+template <typename Scalar, int dimensions>
+struct NoSettings {};
+
+// naive_gabriel.hpp: the Gabriel coefficient only
+template <typename Scalar, int dimensions>
+struct GabrielSettings {
+  Scalar gabriel_coefficient = Scalar(0.8);
+};
+
+// binned_all_pairs.hpp:20-25
+template <typename Scalar, int dimensions>
+struct BinnedSettings {
+  VectorN<Scalar, dimensions> min_bounds = VectorN<Scalar, dimensions>(Scalar(-20));
+  VectorN<Scalar, dimensions> max_bounds = VectorN<Scalar, dimensions>(Scalar(20));
+  Scalar bin_size_scale = Scalar(1);
+  int rebuild_every_n = 0;
+};
+
+// binned_gabriel.hpp:20-26
+template <typename Scalar, int dimensions>
+struct BinnedGabrielSettings {
+  Scalar gabriel_coefficient = Scalar(0.8);
+  VectorN<Scalar, dimensions> min_bounds = VectorN<Scalar, dimensions>(Scalar(-20));
+  VectorN<Scalar, dimensions> max_bounds = VectorN<Scalar, dimensions>(Scalar(20));
+  Scalar bin_size_scale = Scalar(1);
+  int rebuild_every_n = 0;
+};
+}  // namespace detail
+
+#define TECS_CXX_FINDER(NAME, ID, SYM, SETTINGS)                                 \
+  template <typename PositionsView, typename Scalar, int dimensions>             \
+  struct NAME : detail::Tag<ID, SYM> {                                           \
+    using positions_view_type = PositionsView;                                   \
+    using Settings = detail::SETTINGS<Scalar, dimensions>;                       \
+  };
+
+TECS_CXX_FINDER(NaiveAllPairs, TECS_FINDER_NAIVE_ALL_PAIRS, false, NoSettings)
+TECS_CXX_FINDER(NaiveAllPairsSymmetric, TECS_FINDER_NAIVE_ALL_PAIRS, true, NoSettings)
+TECS_CXX_FINDER(BinnedAllPairs, TECS_FINDER_BINNED_ALL_PAIRS, false, BinnedSettings)
+TECS_CXX_FINDER(BinnedAllPairsSymmetric, TECS_FINDER_BINNED_ALL_PAIRS, true, BinnedSettings)
+TECS_CXX_FINDER(NaiveGabriel, TECS_FINDER_NAIVE_GABRIEL, false, GabrielSettings)
+TECS_CXX_FINDER(NaiveGabrielSymmetric, TECS_FINDER_NAIVE_GABRIEL, true, GabrielSettings)
+TECS_CXX_FINDER(BinnedGabriel, TECS_FINDER_BINNED_GABRIEL, false, BinnedGabrielSettings)
+TECS_CXX_FINDER(BinnedGabrielSymmetric, TECS_FINDER_BINNED_GABRIEL, true, BinnedGabrielSettings)
+TECS_CXX_FINDER(NaiveDelaunay, TECS_FINDER_NAIVE_DELAUNAY, false, NoSettings)
+#undef TECS_CXX_FINDER
+
+}  // namespace pair_finders
+
+namespace integrators {
+// Any template arguments are accepted (the reference's integrators take the
+// finder, fixer, force-field and view types); only the method matters here.
+template <typename... Ts>
+struct Euler {
+  static constexpr int integrator_id = TECS_EULER;
+};
+template <typename... Ts>
+struct Heun {
+  static constexpr int integrator_id = TECS_HEUN;
+};
+}  // namespace integrators
+
+namespace com_fixers {
+template <typename SimulationConfig>
+struct NoComFixer {
+  static constexpr int com_fix = 0;
+};
+// subtracts sum(delta) / capacity from every delta (com_fixers.hpp:24-45)
+template <typename SimulationConfig>
+struct GlobalComFixer {
+  static constexpr int com_fix = 1;
+};
+}  // namespace com_fixers
+
+namespace forces {
+// Built-in pairwise force laws.  A pair at distance d < cutoff gets
+// displacement * F(d) / d (zero at d == 0) with
+//   F(d) = k_rep * max(r_rep - d, 0) - k_adh * max(d - r_adh, 0),
+// the two-radius spring of the spheroid and ensemble workloads; with r_rep ==
+// r_adh it is forces::PiecewiseLinear / forces::Spring's linear spring
+// (include/forces/predefined.hpp:60-144).
+struct Spring2R {
+  float k_rep = 2.0f, r_rep = 0.7f, k_adh = 0.5f, r_adh = 0.8f;
+  static constexpr int force_id = TECS_FORCE_SPRING2R;
+  static constexpr bool needs_polarity = false;
+  float k_pol_value() const { return 0.0f; }
+};
+
+// Spring2R plus k_pol * (Polarity_::bending_force + bidirectional alignment)
+// on a (position, polarity) config, as the epithelium examples write it
+// (include/types/polarity.hpp:131-198).
+struct PolaritySpring {
+  float k_rep = 2.0f, r_rep = 0.7f, k_adh = 0.5f, r_adh = 0.8f, k_pol = 0.2f;
+  static constexpr int force_id = TECS_FORCE_POLARITY;
+  static constexpr bool needs_polarity = true;
+  float k_pol_value() const { return k_pol; }
+};
+
+// Pairs found, no deltas: the neighbour-counting use of main.cpp.
+struct NoForce {
+  float k_rep = 0.0f, r_rep = 0.0f, k_adh = 0.0f, r_adh = 0.0f;
+  static constexpr int force_id = TECS_FORCE_NONE;
+  static constexpr bool needs_polarity = false;
+  float k_pol_value() const { return 0.0f; }
+};
+}  // namespace forces
+
+namespace io {
+// The reference's no-op writer (include/io/dummy.hpp).
+template <typename... Ts>
+struct Dummy {
+  static constexpr bool writes = false;
+};
+}  // namespace io
+
+}  // namespace tecs
+
+#endif  // TECS_CXX_COMPONENTS_HPP

@@ -1,0 +1,140 @@
+// tecs/config.hpp -- simulation configs for the C++20 drop-in layer.
+//
+// A config is a struct deriving from DefaultSimulationConfig that overrides
+// members through the reference's CONFIG_* macros and ends with
+// RESOLVE_TECS_CONFIG(), or is made in one go with CREATE_SIMULATION_CONFIG;
+// user programs name them, so the macro names and what they declare
+// (Scalar, dimensions, PairFinderT, IntegratorT, ComFixerT, WriterT, Fields,
+// Vector, Polarity) follow include/simulation_config.hpp:212-379 and
+// include/utils/utils.hpp:319-344.  The field list is resolved against the
+// final Scalar and dimensions when RESOLVE_TECS_CONFIG() runs, so overrides
+// may come in any order before it.
+#ifndef TECS_CXX_CONFIG_HPP
+#define TECS_CXX_CONFIG_HPP
+
+#include <cstddef>
+#include <string_view>
+
+#include "components.hpp"
+#include "vector.hpp"
+
+namespace tecs {
+
+template <typename T>
+class View;
+
+namespace detail {
+
+// a string literal usable as a template argument (the field's name)
+template <std::size_t N>
+struct FixedString {
+  char text[N] = {};
+  constexpr FixedString(const char (&s)[N]) {
+    for (std::size_t k = 0; k < N; ++k) text[k] = s[k];
+  }
+  constexpr std::string_view view() const { return {text, N - 1}; }
+};
+
+template <typename T, FixedString Name>
+struct Field {
+  using value_type = T;
+  static constexpr std::string_view name = Name.view();
+};
+
+template <typename... Fs>
+struct FieldList {
+  static constexpr std::size_t size = sizeof...(Fs);
+};
+
+// bind a finder template to the config's position view, scalar and dimensions
+template <template <typename, typename, int> class Finder, typename Config>
+using pair_finder_t =
+    Finder<View<VectorN<typename Config::Scalar, Config::dimensions>>, typename Config::Scalar, Config::dimensions>;
+
+}  // namespace detail
+}  // namespace tecs
+
+#define FIELD(TYPE, NAME) tecs::detail::Field<TYPE, #NAME>
+
+#define CONFIG_SCALAR(S) using Scalar = S;
+#define CONFIG_DIMENSIONS(D) static constexpr int dimensions = D;
+// one random stream per simulation is part of the CUDA library (counter-based)
+#define CONFIG_RANDOM_POOL(POOL)
+#define CONFIG_INTEGRATOR(I) \
+  template <typename SimulationConfig_> \
+  using IntegratorT = I<SimulationConfig_>;
+#define CONFIG_PAIR_FINDER(F) \
+  template <typename SimulationConfig_> \
+  using PairFinderT = tecs::detail::pair_finder_t<F, SimulationConfig_>;
+#define CONFIG_COM_FIXER(C) \
+  template <typename SimulationConfig_> \
+  using ComFixerT = C<SimulationConfig_>;
+#define CONFIG_WRITER(W) \
+  template <typename SimulationConfig_> \
+  using WriterT = W<SimulationConfig_>;
+
+// (Type, name) pairs; Type is Vector, Polarity or Scalar of the final config
+#define TECS_CXX_CAT(a, b) TECS_CXX_CAT_(a, b)
+#define TECS_CXX_CAT_(a, b) a##b
+#define TECS_CXX_NARG(...) TECS_CXX_NARG_(__VA_ARGS__, 4, 3, 2, 1, 0)
+#define TECS_CXX_NARG_(a, b, c, d, n, ...) n
+#define TECS_CXX_TYPE_Vector(S, D) tecs::VectorN<S, D>
+#define TECS_CXX_TYPE_Polarity(S, D) tecs::Polarity_<S>
+#define TECS_CXX_TYPE_Scalar(S, D) S
+#define TECS_CXX_FIELD_OF(T, N) tecs::detail::Field<TECS_CXX_TYPE_##T(TecsScalar_, TecsDims_), #N>
+#define TECS_CXX_APPLY(P) TECS_CXX_FIELD_OF P
+#define TECS_CXX_LIST_1(a) TECS_CXX_APPLY(a)
+#define TECS_CXX_LIST_2(a, b) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b)
+#define TECS_CXX_LIST_3(a, b, c) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b), TECS_CXX_APPLY(c)
+#define TECS_CXX_LIST_4(a, b, c, d) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b), TECS_CXX_APPLY(c), TECS_CXX_APPLY(d)
+
+#define CONFIG_FIELDS(...)                                                                            \
+  template <typename TecsScalar_, int TecsDims_>                                                      \
+  struct TecsFieldsOf_ {                                                                              \
+    using type = tecs::detail::FieldList<TECS_CXX_CAT(TECS_CXX_LIST_, TECS_CXX_NARG(__VA_ARGS__))(__VA_ARGS__)>; \
+  };
+
+#define RESOLVE_TECS_CONFIG()                                   \
+  using Vector = tecs::VectorN<Scalar, dimensions>;             \
+  using Polarity = tecs::Polarity_<Scalar>;                     \
+  using VectorView = tecs::View<Vector>;                        \
+  using Fields = typename TecsFieldsOf_<Scalar, dimensions>::type;
+
+namespace tecs {
+
+struct DefaultSimulationConfig {
+  CONFIG_DIMENSIONS(3)
+  CONFIG_SCALAR(float)
+  CONFIG_PAIR_FINDER(tecs::pair_finders::NaiveAllPairs)
+  CONFIG_COM_FIXER(tecs::com_fixers::NoComFixer)
+  CONFIG_INTEGRATOR(tecs::integrators::Heun)
+  CONFIG_WRITER(tecs::io::Dummy)
+  CONFIG_FIELDS((Vector, position))
+  RESOLVE_TECS_CONFIG()
+};
+
+}  // namespace tecs
+
+#define CREATE_SIMULATION_CONFIG(NAME, ...)                \
+  struct NAME : public tecs::DefaultSimulationConfig {     \
+    __VA_ARGS__                                            \
+    RESOLVE_TECS_CONFIG()                                  \
+  };
+
+#define EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                          \
+  using Scalar = typename C::Scalar;                                     \
+  static constexpr int dimensions = C::dimensions;                       \
+  using Vector = tecs::VectorN<Scalar, dimensions>;                      \
+  using VectorI = tecs::VectorN<int, dimensions>;                        \
+  using VectorView = tecs::View<Vector>;                                 \
+  using Polarity = tecs::Polarity_<Scalar>;
+
+#define EXTRACT_ALL_FROM_SIMULATION_CONFIG(C)                            \
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                \
+  using Fields = typename C::Fields;                                     \
+  using Integrator = typename C::template IntegratorT<C>;                \
+  using PairFinder = typename C::template PairFinderT<C>;                \
+  using ComFixer = typename C::template ComFixerT<C>;                    \
+  using Writer = typename C::template WriterT<C>;
+
+#endif  // TECS_CXX_CONFIG_HPP

@@ -1,0 +1,357 @@
+// tecs/simulation.hpp -- Simulation<Config> of the C++20 drop-in layer.
+//
+// Keeps the reference's Simulation interface for the per-timestep path
+// (include/simulation.hpp:76-153 constructors and Settings, :231-302 views and
+// counts, :548-556 take_step) and runs every step in the CUDA library through
+// the C ABI of include/tecs_gpu.h.  The device holds the state; a field's
+// View is a host mirror that is refreshed from the device when the program
+// asks for it after steps and uploaded again before the next step if the
+// program may have written it -- the DualView modified-flag protocol of
+// include/types/view.hpp:47-266, with the host side explicit.
+//
+// Errors: every C-ABI failure throws tecs::Error with tecs_last_error().
+#ifndef TECS_CXX_SIMULATION_HPP
+#define TECS_CXX_SIMULATION_HPP
+
+#include <cmath>
+#include <cstdint>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../tecs_gpu.h"
+#include "components.hpp"
+#include "config.hpp"
+#include "vector.hpp"
+
+namespace tecs {
+
+struct Error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+inline void check(int rc) {
+  if (rc != 0) throw Error(tecs_last_error());
+}
+
+// A field's values for the active agents, on the host.
+template <typename T>
+class View {
+ public:
+  using value_type = T;
+  using non_const_value_type = std::remove_const_t<T>;
+
+  View() = default;
+  View(const std::string& label, std::size_t n) : label_(label), data_(n), active_(static_cast<unsigned>(n)) {}
+
+  T& operator()(std::size_t i) { return data_[i]; }
+  const T& operator()(std::size_t i) const { return data_[i]; }
+  std::size_t extent(int) const { return data_.size(); }
+  T* data() { return data_.data(); }
+  const T* data() const { return data_.data(); }
+  unsigned get_active_count() const { return active_; }
+  void set_active_count(unsigned n) { active_ = n; }
+  const std::string& label() const { return label_; }
+
+  void resize(std::size_t n) { data_.resize(n); }
+
+ private:
+  std::string label_;
+  std::vector<T> data_;
+  unsigned active_ = 0;
+};
+
+// Cell division after each step (the pattern of examples/growth_w_wall.cpp:119-136,
+// done on the device): each active cell divides with this probability per step;
+// its daughter is placed at offset * a random unit vector and appended.
+struct DivisionSettings {
+  double probability = 0.0;
+  float offset = 0.25f;
+};
+
+template <typename Config>
+class Simulation {
+ public:
+  using Scalar = typename Config::Scalar;
+  static constexpr int dimensions = Config::dimensions;
+  using Vector = VectorN<Scalar, dimensions>;
+  using Polarity = Polarity_<Scalar>;
+  using Fields = typename Config::Fields;
+  using PairFinder = typename Config::template PairFinderT<Config>;
+  using Integrator = typename Config::template IntegratorT<Config>;
+  using ComFixer = typename Config::template ComFixerT<Config>;
+  using Writer = typename Config::template WriterT<Config>;
+
+  static_assert(std::is_same_v<Scalar, float>, "the GB300 path computes in float");
+  static_assert(dimensions == 2 || dimensions == 3, "2 or 3 dimensions");
+
+ private:
+  template <typename F>
+  static constexpr bool is_position_field = std::is_same_v<typename F::value_type, Vector> && F::name == "position";
+  template <typename F>
+  static constexpr bool is_polarity_field = std::is_same_v<typename F::value_type, Polarity> && F::name == "polarity";
+
+  template <typename L>
+  struct FieldShape;
+  template <typename F0, typename... Fs>
+  struct FieldShape<detail::FieldList<F0, Fs...>> {
+    static constexpr int n = 1 + static_cast<int>(sizeof...(Fs));
+    static constexpr bool first_is_position = is_position_field<F0>;
+    static constexpr bool polarity = (false || ... || is_polarity_field<Fs>);
+    static constexpr bool only_known = (true && ... && is_polarity_field<Fs>);
+  };
+  using Shape = FieldShape<Fields>;
+  static_assert(Shape::first_is_position, "the first field must be (Vector, position)");
+  static_assert(Shape::only_known && Shape::n <= 2,
+                "the GB300 path carries a (Vector, position) field and an optional (Polarity, polarity) field");
+
+ public:
+  static constexpr bool has_polarity = Shape::polarity;
+
+  struct Settings {
+    Settings(unsigned agent_count_, const std::string& output_path_)
+        : agent_count(agent_count_), output_path(output_path_), capacity(agent_count_) {}
+    unsigned agent_count;
+    std::string output_path;
+    unsigned capacity;
+    Scalar cutoff_distance = Scalar(1'000'000);
+    std::uint64_t seed = 2807;
+    typename PairFinder::Settings pair_finder_settings = {};
+    // extension: device-side cell division after every step
+    DivisionSettings division = {};
+    int device = 0;
+  };
+
+  // legacy positional constructor (include/simulation.hpp:110-126)
+  Simulation(unsigned agent_count, const std::string& output_path, Scalar cutoff_distance = Scalar(1'000'000),
+             const typename PairFinder::Settings& pair_finder_settings = {}, std::uint64_t seed = 2807)
+      : Simulation(make_settings(agent_count, output_path, cutoff_distance, pair_finder_settings, seed)) {}
+
+  explicit Simulation(const Settings& s) : agent_count(s.agent_count), capacity(s.capacity), settings_(s) {
+    if (s.capacity < s.agent_count) throw Error("capacity must be >= agent_count");
+    tecs_sim_desc d{};
+    check(tecs_sim_desc_default(&d));
+    d.dims = dimensions;
+    d.finder = PairFinder::finder_id;
+    d.symmetric = PairFinder::symmetric ? 1 : 0;
+    d.cutoff = s.cutoff_distance;
+    apply_finder_settings(d, s.pair_finder_settings);
+    d.integrator = Integrator::integrator_id;
+    d.com_fix = ComFixer::com_fix;
+    d.force = TECS_FORCE_NONE;
+    d.has_polarity = has_polarity ? 1 : 0;
+    d.capacity = s.capacity;
+    d.division_probability = s.division.probability;
+    d.division_offset = s.division.offset;
+    d.seed = s.seed;
+    d.device = s.device;
+    check(tecs_sim_create(&d, &handle_));
+    positions_ = View<Vector>("position", s.capacity);
+    positions_.set_active_count(s.agent_count);
+    if constexpr (has_polarity) {
+      polarity_ = View<Polarity>("polarity", s.capacity);
+      polarity_.set_active_count(s.agent_count);
+    }
+    host_valid_ = true;  // zero-initialised, as Kokkos views are
+    host_dirty_ = true;
+  }
+
+  Simulation(const Simulation&) = delete;
+  Simulation& operator=(const Simulation&) = delete;
+  ~Simulation() {
+    if (handle_) tecs_sim_destroy(handle_);
+  }
+
+  // -- views ----------------------------------------------------------------
+  // The returned view may be written: it is uploaded before the next step.
+  template <typename Field>
+  View<typename Field::value_type>& get_view() {
+    refresh_host();
+    host_dirty_ = true;
+    return view_of<Field>();
+  }
+  template <typename Field>
+  const View<typename Field::value_type>& get_view() const {
+    const_cast<Simulation*>(this)->refresh_host();
+    return const_cast<Simulation*>(this)->template view_of<Field>();
+  }
+  View<Vector>& get_positions_view() { return get_view<FIELD(Vector, position)>(); }
+
+  unsigned get_capacity() const { return capacity; }
+  unsigned get_agent_count() const {
+    if (!host_valid_) {
+      unsigned n = 0;
+      check(tecs_sim_count(handle_, &n));
+      const_cast<Simulation*>(this)->agent_count = n;
+    }
+    return agent_count;
+  }
+  // Simulation::set_agent_count (include/simulation.hpp:295-302): the next
+  // step starts from the first n host values and resets the finder's counter
+  void set_agent_count(unsigned n) {
+    if (n > capacity) throw Error("agent count exceeds capacity");
+    refresh_host();
+    agent_count = n;
+    positions_.set_active_count(n);
+    if constexpr (has_polarity) polarity_.set_active_count(n);
+    host_dirty_ = true;
+  }
+
+  // -- stepping ---------------------------------------------------------------
+  // take_step(dt, force): one integrator step with the given built-in law
+  template <typename Force>
+  void take_step(double dt, const Force& force) {
+    static_assert(!Force::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
+    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
+                             force.k_pol_value()));
+    upload_if_dirty();
+    check(tecs_sim_step(handle_, dt, 1));
+    host_valid_ = false;
+    ++current_step;
+    last_dt = dt;
+  }
+  // n steps queued at once (one graph replay each)
+  template <typename Force>
+  void take_steps(double dt, int n, const Force& force) {
+    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
+                             force.k_pol_value()));
+    upload_if_dirty();
+    check(tecs_sim_step(handle_, dt, n));
+    host_valid_ = false;
+    current_step += static_cast<unsigned>(n);
+    last_dt = dt;
+  }
+
+  // One full-step force evaluation of the current state without moving it:
+  // per-cell deltas and the directed (self, other) pairs found.
+  template <typename Force>
+  std::vector<std::pair<unsigned, unsigned>> evaluate(const Force& force, std::vector<Vector>* deltas = nullptr) {
+    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
+                             force.k_pol_value()));
+    upload_if_dirty();
+    const unsigned n = get_agent_count();
+    std::vector<Vector> dx(n ? n : 1);
+    std::vector<std::uint32_t> raw(2 * std::size_t(64) * (n ? n : 1));
+    std::size_t count = 0;
+    for (;;) {
+      check(tecs_sim_evaluate(handle_, reinterpret_cast<float*>(dx.data()), nullptr, raw.data(), raw.size() / 2,
+                              &count));
+      if (count <= raw.size() / 2) break;
+      raw.resize(2 * count);
+    }
+    if (deltas) deltas->assign(dx.begin(), dx.begin() + n);
+    std::vector<std::pair<unsigned, unsigned>> pairs(count);
+    for (std::size_t k = 0; k < count; ++k) pairs[k] = {raw[2 * k], raw[2 * k + 1]};
+    return pairs;
+  }
+
+  void synchronize() { check(tecs_sim_synchronize(handle_)); }
+
+  // -- initialisers (subset of include/initializers) -------------------------
+  // Uniform in a ball of the given radius (initializers/spheres.hpp's
+  // random filled sphere; the stream is this library's own).
+  void init_random_filled_sphere(Scalar radius) {
+    std::mt19937_64 rng(settings_.seed);
+    std::uniform_real_distribution<double> u(-1.0, 1.0);
+    refresh_host();
+    for (unsigned i = 0; i < agent_count; ++i) {
+      double p[3] = {0, 0, 0}, r2;
+      do {
+        r2 = 0;
+        for (int d = 0; d < dimensions; ++d) { p[d] = u(rng); r2 += p[d] * p[d]; }
+      } while (r2 > 1.0);
+      for (int d = 0; d < dimensions; ++d) positions_(i)[d] = static_cast<Scalar>(p[d] * radius);
+    }
+    host_dirty_ = true;
+  }
+  // Uniform on a sphere surface of the given radius (random hollow sphere).
+  void init_random_hollow_sphere(Scalar radius) {
+    std::mt19937_64 rng(settings_.seed);
+    std::normal_distribution<double> g(0.0, 1.0);
+    refresh_host();
+    for (unsigned i = 0; i < agent_count; ++i) {
+      double p[3] = {0, 0, 0}, r2 = 0;
+      for (int d = 0; d < dimensions; ++d) { p[d] = g(rng); r2 += p[d] * p[d]; }
+      const double s = radius / std::sqrt(r2);
+      for (int d = 0; d < dimensions; ++d) positions_(i)[d] = static_cast<Scalar>(p[d] * s);
+    }
+    host_dirty_ = true;
+  }
+
+  // The writer of the config: io::Dummy writes nothing.
+  template <typename... Extra>
+  void write(double /*time*/, Extra&&...) {}
+
+  tecs_sim* handle() const { return handle_; }
+
+  unsigned agent_count;
+  unsigned capacity;
+  unsigned current_step = 0;
+  double last_dt = 0.0;
+
+ private:
+  static Settings make_settings(unsigned n, const std::string& path, Scalar cutoff,
+                                const typename PairFinder::Settings& pfs, std::uint64_t seed) {
+    Settings s(n, path);
+    s.cutoff_distance = cutoff;
+    s.pair_finder_settings = pfs;
+    s.seed = seed;
+    return s;
+  }
+
+  template <typename PFS>
+  static void apply_finder_settings(tecs_sim_desc& d, const PFS& p) {
+    if constexpr (requires { p.gabriel_coefficient; }) d.gabriel_coefficient = p.gabriel_coefficient;
+    if constexpr (requires { p.min_bounds; }) {
+      for (int k = 0; k < 3; ++k) {
+        d.min_bounds[k] = k < dimensions ? p.min_bounds[k] : 0.0f;
+        d.max_bounds[k] = k < dimensions ? p.max_bounds[k] : 0.0f;
+      }
+    }
+    if constexpr (requires { p.bin_size_scale; }) d.bin_size_scale = p.bin_size_scale;
+    if constexpr (requires { p.rebuild_every_n; }) d.rebuild_every_n = p.rebuild_every_n;
+  }
+
+  template <typename Field>
+  View<typename Field::value_type>& view_of() {
+    if constexpr (is_position_field<Field>) {
+      return positions_;
+    } else {
+      static_assert(has_polarity && is_polarity_field<Field>, "no such field in this config");
+      return polarity_;
+    }
+  }
+
+  void refresh_host() {
+    if (host_valid_) return;
+    unsigned n = 0;
+    check(tecs_sim_download(handle_, reinterpret_cast<float*>(positions_.data()),
+                            has_polarity ? reinterpret_cast<float*>(polarity_.data()) : nullptr, &n));
+    agent_count = n;
+    positions_.set_active_count(n);
+    if constexpr (has_polarity) polarity_.set_active_count(n);
+    host_valid_ = true;
+    host_dirty_ = false;
+  }
+
+  void upload_if_dirty() {
+    if (!host_dirty_) return;
+    check(tecs_sim_upload(handle_, reinterpret_cast<const float*>(positions_.data()),
+                          has_polarity ? reinterpret_cast<const float*>(polarity_.data()) : nullptr, agent_count));
+    host_dirty_ = false;
+  }
+
+  Settings settings_;
+  tecs_sim* handle_ = nullptr;
+  View<Vector> positions_;
+  View<Polarity> polarity_;
+  bool host_valid_ = false;  // the host mirror holds the device state
+  bool host_dirty_ = false;  // the host mirror may differ from the device state
+};
+
+}  // namespace tecs
+
+#endif  // TECS_CXX_SIMULATION_HPP

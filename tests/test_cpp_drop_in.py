@@ -1,0 +1,121 @@
+"""The C++20 drop-in layer (include/tecs/) against the reference's outputs.
+
+tests/cpp/drop_in_driver.cpp is a program written the way the reference's
+programs are (a config struct, Simulation<Config>, get_view, take_step); it is
+compiled here with g++ against include/tecs/tecs.hpp and linked with the CUDA
+library.  On a GB300 it runs on the inputs of the golden fixtures -- which hold
+the reference's own outputs -- and must reproduce them: pair lists and spring
+runs bit for bit, the COM fix and the polarity law within the parity
+tolerance (|gpu - ref| <= 1e-5 |ref| + 1e-6 rms(ref)).
+"""
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import tecs_gb300 as tg
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = Path(__file__).resolve().parent / "golden"
+SOURCE = Path(__file__).resolve().parent / "cpp" / "drop_in_driver.cpp"
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    lib = Path(tg.library_path())
+    out = tmp_path_factory.mktemp("cpp") / "drop_in_driver"
+    cmd = ["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(SOURCE),
+           f"-L{lib.parent}", "-l" + lib.stem[3:], f"-Wl,-rpath,{lib.parent}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_config_machinery_and_defaults(tmp_path):
+    """tests/cpp/config_checks.cpp holds static_asserts on configs and Settings defaults."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = Path(__file__).resolve().parent / "cpp" / "config_checks.cpp"
+    lib = Path(tg.library_path())
+    out = tmp_path / "config_checks"
+    r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                        f"-L{lib.parent}", "-l" + lib.stem[3:], f"-Wl,-rpath,{lib.parent}", "-o", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(out)]).returncode == 0
+
+
+def write_input(path, g):
+    x0 = g["x0"]
+    p0 = g.get("p0")
+    with open(path, "wb") as f:
+        np.array([len(x0), x0.shape[1], 1 if p0 is not None else 0], np.uint32).tofile(f)
+        g["prm"].astype(np.float32).tofile(f)
+        x0.astype(np.float32).tofile(f)
+        if p0 is not None:
+            p0.astype(np.float32).tofile(f)
+
+
+def run_driver(driver, scenario, name, tmp_path):
+    g = dict(np.load(GOLDEN / f"{name}.npz"))
+    inp = tmp_path / "in.bin"
+    write_input(inp, g)
+    out = tmp_path / "out"
+    r = subprocess.run([str(driver), scenario, str(inp), str(out), str(int(g["steps"])), repr(float(g["dt"]))],
+                       capture_output=True, text=True, timeout=600)
+    return g, out, r
+
+
+def test_driver_builds_and_fails_cleanly_without_a_device(driver, tmp_path):
+    """Compiles with -Wall -Wextra -Werror; with no GPU the C ABI's error surfaces as tecs::Error."""
+    import os
+
+    if os.path.exists("/dev/nvidia0"):
+        pytest.skip("a GPU is present")
+    _, _, r = run_driver(driver, "bg_heun", "bg_heun", tmp_path)
+    assert r.returncode == 1
+    assert "tecs error" in r.stderr
+
+
+def close(a, b, rtol=1e-5, atol=1e-6):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.sqrt(np.mean(b ** 2)) if b.size else 0.0
+    return bool((np.abs(a - b) <= rtol * np.abs(b) + atol * scale).all())
+
+
+CASES = [
+    # (scenario in the driver, fixture, exact)
+    ("ba_euler", "c1_small_euler", True),
+    ("bg_heun", "bg_heun", True),
+    ("bg_heun", "bg_heun_clamped", True),
+    ("bg_heun_com", "bg_heun_com", False),
+    ("bg_heun_pol", "bg_heun_polarity", False),
+    ("nd_euler_2d", "nd_euler_2d", True),
+    ("nd_euler_2d", "nd_euler_2d_points11", True),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scenario,name,exact", CASES)
+def test_drop_in_program_reproduces_reference(driver, tmp_path, scenario, name, exact):
+    g, out, r = run_driver(driver, scenario, name, tmp_path)
+    assert r.returncode == 0, r.stderr
+    dims = g["x0"].shape[1]
+    pairs = np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2)
+    np.testing.assert_array_equal(tg.canonical_pairs(pairs), tg.canonical_pairs(g["pairs"]))
+    dpos = np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims)
+    pos = np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims)
+    if exact:
+        np.testing.assert_array_equal(dpos, g["dpos"])
+        np.testing.assert_array_equal(pos, g["pos"])
+    else:
+        assert close(dpos, g["dpos"])
+        assert close(pos, g["pos"])
+    if "pol" in g:
+        pol = np.fromfile(f"{out}.pol", np.float32).reshape(-1, 2)
+        assert close(pol, g["pol"])
