@@ -1,10 +1,11 @@
 // tecs/vector.hpp -- host-side value types of the C++20 drop-in layer.
 //
-// VectorN<Scalar, D> and Polarity_<Scalar> keep the reference's names and
-// memory layout (D, respectively 2, contiguous scalars; include/types/vector.hpp:34-436,
-// include/types/polarity.hpp:28-198), so a View<VectorN<float, 3>> is exactly
-// the AoS float[n][3] array the C ABI (tecs_gpu.h) uploads and downloads.
-// They are host types: the arithmetic of a step runs in the CUDA library.
+// VectorN<Scalar, D> and Polarity_<Scalar> keep the reference's names,
+// operators and memory layout (D, respectively 2, contiguous scalars;
+// include/types/vector.hpp:34-436, include/types/polarity.hpp:28-124), so a
+// View<VectorN<float, 3>> is exactly the AoS float[n][3] array the C ABI
+// (tecs_gpu.h) uploads and downloads.  They are host types: the arithmetic of
+// a step runs in the CUDA library.
 #ifndef TECS_CXX_VECTOR_HPP
 #define TECS_CXX_VECTOR_HPP
 
@@ -16,9 +17,8 @@ namespace tecs {
 
 template <typename Scalar, int dimensions>
 struct VectorN {
-  static_assert(dimensions >= 1 && dimensions <= 3, "VectorN holds 1 to 3 components");
+  static_assert(dimensions >= 1 && dimensions <= 4, "VectorN holds 1 to 4 components");
   using value_type = Scalar;
-  static constexpr int size = dimensions;
 
   Scalar data_[dimensions] = {};
 
@@ -31,6 +31,7 @@ struct VectorN {
     requires(sizeof...(Ts) == dimensions && dimensions > 1 && (std::is_arithmetic_v<Ts> && ...))
   constexpr VectorN(Ts... v) : data_{static_cast<Scalar>(v)...} {}
 
+  static constexpr int size() { return dimensions; }
   constexpr Scalar& operator[](int d) { return data_[d]; }
   constexpr const Scalar& operator[](int d) const { return data_[d]; }
   constexpr Scalar& x() { return data_[0]; }
@@ -39,32 +40,36 @@ struct VectorN {
   constexpr const Scalar& y() const requires(dimensions >= 2) { return data_[1]; }
   constexpr Scalar& z() requires(dimensions >= 3) { return data_[2]; }
   constexpr const Scalar& z() const requires(dimensions >= 3) { return data_[2]; }
+  constexpr Scalar& w() requires(dimensions >= 4) { return data_[3]; }
+  constexpr const Scalar& w() const requires(dimensions >= 4) { return data_[3]; }
 
-  constexpr VectorN& operator+=(const VectorN& o) {
-    for (int d = 0; d < dimensions; ++d) data_[d] += o.data_[d];
-    return *this;
+  // component-wise with a vector or a scalar
+#define TECS_CXX_VEC_OP(OP)                                          \
+  constexpr VectorN& operator OP##=(const VectorN& o) {              \
+    for (int d = 0; d < dimensions; ++d) data_[d] OP## = o.data_[d]; \
+    return *this;                                                    \
+  }                                                                  \
+  constexpr VectorN& operator OP##=(Scalar s) {                      \
+    for (int d = 0; d < dimensions; ++d) data_[d] OP## = s;          \
+    return *this;                                                    \
+  }                                                                  \
+  friend constexpr VectorN operator OP(VectorN a, const VectorN& b) { return a OP## = b; } \
+  friend constexpr VectorN operator OP(VectorN a, Scalar s) { return a OP## = s; }        \
+  friend constexpr VectorN operator OP(Scalar s, VectorN a) {        \
+    for (int d = 0; d < dimensions; ++d) a.data_[d] = s OP a.data_[d]; \
+    return a;                                                        \
   }
-  constexpr VectorN& operator-=(const VectorN& o) {
-    for (int d = 0; d < dimensions; ++d) data_[d] -= o.data_[d];
-    return *this;
-  }
-  constexpr VectorN& operator*=(Scalar s) {
-    for (int d = 0; d < dimensions; ++d) data_[d] *= s;
-    return *this;
-  }
-  constexpr VectorN& operator/=(Scalar s) {
-    for (int d = 0; d < dimensions; ++d) data_[d] /= s;
-    return *this;
-  }
-  friend constexpr VectorN operator+(VectorN a, const VectorN& b) { return a += b; }
-  friend constexpr VectorN operator-(VectorN a, const VectorN& b) { return a -= b; }
+  TECS_CXX_VEC_OP(+)
+  TECS_CXX_VEC_OP(-)
+  TECS_CXX_VEC_OP(*)
+  TECS_CXX_VEC_OP(/)
+#undef TECS_CXX_VEC_OP
+
   friend constexpr VectorN operator-(VectorN a) {
     for (int d = 0; d < dimensions; ++d) a.data_[d] = -a.data_[d];
     return a;
   }
-  friend constexpr VectorN operator*(VectorN a, Scalar s) { return a *= s; }
-  friend constexpr VectorN operator*(Scalar s, VectorN a) { return a *= s; }
-  friend constexpr VectorN operator/(VectorN a, Scalar s) { return a /= s; }
+  friend constexpr VectorN operator+(const VectorN& a) { return a; }
   friend constexpr bool operator==(const VectorN& a, const VectorN& b) {
     for (int d = 0; d < dimensions; ++d)
       if (a.data_[d] != b.data_[d]) return false;
@@ -88,34 +93,46 @@ struct VectorN {
     return r;
   }
   Scalar distance_to(const VectorN& o) const { return std::sqrt(distance_to_squared(o)); }
+  VectorN normalized() const { return *this / length(); }
+  constexpr VectorN cross(const VectorN& o) const requires(dimensions == 3) {
+    return VectorN(data_[1] * o.data_[2] - data_[2] * o.data_[1], data_[2] * o.data_[0] - data_[0] * o.data_[2],
+                   data_[0] * o.data_[1] - data_[1] * o.data_[0]);
+  }
 };
+
+template <typename Scalar>
+using Vector3 = VectorN<Scalar, 3>;
 
 // Apical-basal polarity as spherical angles (theta, phi).
 template <typename Scalar>
-struct Polarity_ {
-  using value_type = Scalar;
-  Scalar data_[2] = {};
+struct Polarity_ : VectorN<Scalar, 2> {
+  using Base = VectorN<Scalar, 2>;
 
   constexpr Polarity_() = default;
-  constexpr Polarity_(Scalar theta, Scalar phi) : data_{theta, phi} {}
-  // from a direction: theta = acos(z / |v|), phi = atan2(y, x) (types/polarity.hpp:74-77)
-  explicit Polarity_(const VectorN<Scalar, 3>& v) {
-    const Scalar len = v.length();
-    data_[0] = std::acos(v[2] / len);
-    data_[1] = std::atan2(v[1], v[0]);
+  constexpr explicit Polarity_(Scalar v) : Base(v) {}
+  constexpr Polarity_(Scalar theta, Scalar phi) : Base(theta, phi) {}
+  // the direction of v (polarity.hpp:74-77)
+  explicit Polarity_(const Vector3<Scalar>& v) : Polarity_(from_vector3(v)) {}
+
+  constexpr Scalar& theta() { return this->data_[0]; }
+  constexpr const Scalar& theta() const { return this->data_[0]; }
+  constexpr Scalar& phi() { return this->data_[1]; }
+  constexpr const Scalar& phi() const { return this->data_[1]; }
+
+  // theta = acos(clamp(z / |v|, -1, 1)), phi = atan2(y, x) (polarity.hpp:62-76)
+  static Polarity_ from_vector3(const Vector3<Scalar>& v, Scalar length) {
+    return Polarity_(std::acos(std::fmin(Scalar(1), std::fmax(Scalar(-1), v[2] / length))), std::atan2(v[1], v[0]));
   }
-
-  constexpr Scalar& operator[](int d) { return data_[d]; }
-  constexpr const Scalar& operator[](int d) const { return data_[d]; }
-  constexpr Scalar& theta() { return data_[0]; }
-  constexpr const Scalar& theta() const { return data_[0]; }
-  constexpr Scalar& phi() { return data_[1]; }
-  constexpr const Scalar& phi() const { return data_[1]; }
-
-  // unit vector of the angles
-  VectorN<Scalar, 3> to_vector3() const {
-    return VectorN<Scalar, 3>(std::sin(data_[0]) * std::cos(data_[1]), std::sin(data_[0]) * std::sin(data_[1]),
-                              std::cos(data_[0]));
+  static Polarity_ from_vector3(const Vector3<Scalar>& v) { return from_vector3(v, v.length()); }
+  static Vector3<Scalar> to_vector3(const Polarity_& p) {
+    return Vector3<Scalar>(std::sin(p.theta()) * std::cos(p.phi()), std::sin(p.theta()) * std::sin(p.phi()),
+                           std::cos(p.theta()));
+  }
+  Vector3<Scalar> to_vector3() const { return to_vector3(*this); }
+  // cosine of the angle between the two directions (polarity.hpp:132-136)
+  Scalar dot(const Polarity_& o) const {
+    return std::sin(theta()) * std::sin(o.theta()) * std::cos(phi() - o.phi()) +
+           std::cos(theta()) * std::cos(o.theta());
   }
 };
 

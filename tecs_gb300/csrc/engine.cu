@@ -143,16 +143,24 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 // ---------------------------------------------------------------------------
 // the force pass over all slots (block-cooperative, as k_pass_gabriel)
 
-template <int PASS>
+// POL: some resident simulation carries polarity; their cells then take the
+// cooperative path with the polarity law (as k_pass_gabriel<3, 2>), which
+// needs more shared memory -- spring-only engines use the leaner instance.
+template <int PASS, bool POL>
 static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
-  __shared__ float4 cand[kMaxNb * kPassThreads];
+  // neighbour slots per cell (the polarity law needs room for a fifth float per pair)
+  constexpr int NB = POL ? 12 : kMaxNb;
+  __shared__ float4 cand[NB * kPassThreads];
   __shared__ float4 home[kPassThreads];
-  __shared__ unsigned short pinfo[kMaxNb * kPassThreads];
+  __shared__ unsigned short pinfo[NB * kPassThreads];
   __shared__ int pofs[kPassThreads + 1];
   __shared__ int wsum[kPassThreads / 32];
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
   __shared__ unsigned hsim[kPassThreads];
+  __shared__ float2 hpol[POL ? kPassThreads : 1];
+  __shared__ PolTrig htrig[POL ? kPassThreads : 1];
+  __shared__ float pext[POL ? NB * kPassThreads : 1];
 
   const unsigned n = e.off[e.nb_total];
   const int t = threadIdx.x;
@@ -169,7 +177,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   float2 pi = make_float2(0.f, 0.f);
   int bc[3] = {0, 0, 0};
   int cnt = 0;
-  bool fb = polar || (run && gab && !sl.gabriel_fast);
+  bool fb = (polar && !POL) || (run && gab && !sl.gabriel_fast);
   if (run) {
     vi = __ldg(&e.X[i]);
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
@@ -216,7 +224,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       rmask[r] = m;
       total += __popc(m);
     }
-    if (total > kMaxNb) fb = true;
+    if (total > NB) fb = true;
     if (!fb) {
 #pragma unroll
       for (int r = 0; r < 9; ++r) {
@@ -239,6 +247,10 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   hsim[t] = sim;
   ncnt[t] = (unsigned char)cnt;
   fallback[t] = fb ? 1 : 0;
+  if (POL) {
+    hpol[t] = pi;
+    if (cnt && polar) htrig[t] = pol_trig(pi);
+  }
   {
     const int lane = t & 31, warp = t >> 5;
     int incl = cnt;
@@ -321,6 +333,17 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       f.y = (disp[1] * F) / dist;
       f.z = (disp[2] * F) / dist;
     }
+    if (POL && cs.fp.force == TECS_FORCE_POLARITY) {
+      // as k_pass_gabriel<3, 2>: spring + bending vector, and the polarity terms, pre-added per pair
+      float bv[3], bp[2], al[2];
+      const float2 pj = __ldg(&e.P[__float_as_uint(vj.w) >> 5]);
+      polarity_terms(cs.fp, disp, dist, hpol[c], htrig[c], pj, pol_trig(pj), bv, bp, al);
+      f.x = f.x + bv[0];
+      f.y = f.y + bv[1];
+      f.z = f.z + bv[2];
+      f.w = bp[0] + al[0];
+      pext[cix(q, c)] = bp[1] + al[1];
+    }
     cand[cix(q, c)] = f;
   }
   __syncthreads();
@@ -334,6 +357,10 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       acc.x[0] = acc.x[0] + f.x;
       acc.x[1] = acc.x[1] + f.y;
       acc.x[2] = acc.x[2] + f.z;
+      if (POL && polar && sl.fp.force == TECS_FORCE_POLARITY) {
+        acc.p[0] = acc.p[0] + f.w;
+        acc.p[1] = acc.p[1] + pext[cix(q, t)];
+      }
     }
   }
   // every thread has read its sums: the candidate array is free again and
@@ -350,7 +377,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     const int force = sl.fp.force;
     if (gab) {
       if (force == TECS_FORCE_POLARITY) {
-        if (!(sl.gabriel_fast && gabriel_cell_fast<3, 2>(sl.g, sl.fp, pa, i, xi, pi, idi, acc, &cand[t])))
+        if (!(sl.gabriel_fast && gabriel_cell_fast<3, 2, NB>(sl.g, sl.fp, pa, i, xi, pi, idi, acc, &cand[t])))
           cell_general<3, 3, 2>(sl.g, sl.fp, pa, n, i, xi, pi, idi, acc);
       } else if (force == TECS_FORCE_SPRING2R) {
         cell_general<3, 3, 1>(sl.g, sl.fp, pa, n, i, xi, pi, idi, acc);
@@ -460,6 +487,7 @@ struct tecs_engine {
   cudaGraphExec_t graph = nullptr;
   float gdt = 0.f;
   unsigned gC = 0, gNB = 0;  // the extents the captured graph covers (cells, bins)
+  bool gpol = false;         // the captured graph runs the polarity-capable pass
   int kernels = 7;
 };
 
@@ -533,11 +561,17 @@ int enqueue_engine_step(tecs_engine* e, float dt) {
   EngArgs a1 = a;
   a1.X = e->B;
   a1.P = e->PB;
-  k_epass<1><<<cdiv(e->gC, kPassThreads), kPassThreads, 0, e->stream>>>(a1);
   EngArgs a2 = a;
   a2.X = e->Xt;
   a2.P = e->Pt;
-  k_epass<2><<<cdiv(e->gC, kPassThreads), kPassThreads, 0, e->stream>>>(a2);
+  const unsigned blocks = cdiv(e->gC, kPassThreads);
+  if (e->gpol) {
+    k_epass<1, true><<<blocks, kPassThreads, 0, e->stream>>>(a1);
+    k_epass<2, true><<<blocks, kPassThreads, 0, e->stream>>>(a2);
+  } else {
+    k_epass<1, false><<<blocks, kPassThreads, 0, e->stream>>>(a1);
+    k_epass<2, false><<<blocks, kPassThreads, 0, e->stream>>>(a2);
+  }
   ECK(cudaGetLastError());
   return 0;
 }
@@ -763,13 +797,18 @@ int tecs_engine_step(tecs_engine* e, double dt, int n_steps) {
       e->n_dirty = false;
     }
     unsigned hwm = 0;
+    bool pol = false;
     for (unsigned k = 0; k < e->S; ++k)
-      if (e->info[k].used) hwm = std::max(hwm, e->info[k].bin_base + e->info[k].nbins);
+      if (e->info[k].used) {
+        hwm = std::max(hwm, e->info[k].bin_base + e->info[k].nbins);
+        pol = pol || e->htable[k].has_pol;
+      }
     const unsigned wantC = extent_class(e->n_resident, e->C), wantNB = extent_class(hwm, e->NB);
-    if (!e->graph || e->gdt != fdt || wantC != e->gC || wantNB != e->gNB) {
+    if (!e->graph || e->gdt != fdt || wantC != e->gC || wantNB != e->gNB || pol != e->gpol) {
       if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
       e->gC = wantC;
       e->gNB = wantNB;
+      e->gpol = pol;
       cudaGraph_t g;
       ECK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_engine_step(e, fdt);

@@ -624,7 +624,8 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
 constexpr int kMaxNb = 16;
 constexpr int kPassThreads = 128;
 
-template <int D, int FORCE>
+// nb: room for MAXN neighbours at a stride of kPassThreads
+template <int D, int FORCE, int MAXN = kMaxNb>
 __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned i,
                                                   const float* xi, float2 pi, unsigned idi, Acc& acc,
                                                   float4* nb) {
@@ -653,7 +654,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
         float d2 = e0 * e0 + e1 * e1;
         if (D >= 3) { const float e2 = xi[2] - vj.z; d2 = d2 + e2 * e2; }
         if (d2 >= fp.rc2) continue;
-        if (cnt == kMaxNb) return false;
+        if (cnt == MAXN) return false;
         const int rx = x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0];
         const unsigned code = (unsigned)(rx + 1) | ((unsigned)(dy + 1) << 2) | ((unsigned)(dz + 1) << 4);
         nb[cnt * kPassThreads] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 6) | code));
@@ -808,14 +809,22 @@ __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c 
 
 template <int D, int FORCE>
 static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
-  static_assert(FORCE <= 1, "the block-cooperative pass serves the spring laws");
-  __shared__ float4 cand[kMaxNb * kPassThreads];            // [q][t]: position, w = (slot << 5) | bin code
+  static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
+  constexpr bool POL = FORCE == 2;
+  // neighbour slots per cell (the polarity law needs room for a fifth float per pair)
+  constexpr int NB = POL ? 12 : kMaxNb;
+  __shared__ float4 cand[NB * kPassThreads];            // [q][t]: position, w = (slot << 5) | bin code
   __shared__ float4 home[kPassThreads];                     // position, w = packed bin coords
-  __shared__ unsigned short pinfo[kMaxNb * kPassThreads];   // (t << 4) | q, bit 15 = accepted
+  __shared__ unsigned short pinfo[NB * kPassThreads];   // (t << 4) | q, bit 15 = accepted
   __shared__ int pofs[kPassThreads + 1];
   __shared__ int wsum[kPassThreads / 32];
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
+  // polarity law: the home cells' angles and their sin/cos, and the second
+  // polarity component of each pair's force (the first rides in cand.w)
+  __shared__ float2 hpol[POL ? kPassThreads : 1];
+  __shared__ PolTrig htrig[POL ? kPassThreads : 1];
+  __shared__ float pext[POL ? NB * kPassThreads : 1];
 
   const unsigned n = a.ctr->n;
   const int t = threadIdx.x;
@@ -872,7 +881,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       rmask[r] = m;
       total += __popc(m);
     }
-    if (total > kMaxNb) fb = true;
+    if (total > NB) fb = true;
     // 1b: append the in-cutoff candidates in candidate order (the summation order)
     if (!fb) {
 #pragma unroll
@@ -896,6 +905,10 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
                         __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
   ncnt[t] = (unsigned char)cnt;
   fallback[t] = fb ? 1 : 0;
+  if (POL) {
+    hpol[t] = pi;
+    if (cnt) htrig[t] = pol_trig(pi);
+  }
   // exclusive scan of the neighbour counts -> pair offsets
   {
     const int lane = t & 31, warp = t >> 5;
@@ -989,6 +1002,16 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       f.y = (disp[1] * F) / dist;
       if (D >= 3) f.z = (disp[2] * F) / dist;
     }
+    if (POL) {
+      // the spring and bending vector terms of the pair, and its two polarity
+      // terms, each pre-added (phase 4 adds one sum per pair)
+      float sv[3], bv[3], bp[2], al[2];
+      spring_term<3>(fp, disp, dist, sv);
+      const float2 pj = __ldg(&a.P[__float_as_uint(vj.w) >> 5]);
+      polarity_terms(fp, disp, dist, hpol[c], htrig[c], pj, pol_trig(pj), bv, bp, al);
+      f = make_float4(sv[0] + bv[0], sv[1] + bv[1], sv[2] + bv[2], bp[0] + al[0]);
+      pext[cix(q, c)] = bp[1] + al[1];
+    }
     cand[cix(q, c)] = f;
   }
   __syncthreads();
@@ -1005,6 +1028,10 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
         acc.x[0] = acc.x[0] + f.x;
         acc.x[1] = acc.x[1] + f.y;
         if (D >= 3) acc.x[2] = acc.x[2] + f.z;
+        if (POL) {
+          acc.p[0] = acc.p[0] + f.w;
+          acc.p[1] = acc.p[1] + pext[cix(q, t)];
+        }
       }
     }
   }

@@ -161,6 +161,7 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
     } else {                                                                    \
       if (FF == 3 && coop && FO == 0) return k_pass_gabriel<DD, 0>;             \
       if (FF == 3 && coop && FO == 1) return k_pass_gabriel<DD, 1>;             \
+      if (FF == 3 && coop && FO == 2 && DD == 3) return k_pass_gabriel<3, 2>;   \
       if (FO == 0) return k_pass<DD, FF, 0>;                                    \
       if (FO == 1) return k_pass<DD, FF, 1>;                                    \
       if (DD == 3) return k_pass<DD, FF, 2>;                                    \

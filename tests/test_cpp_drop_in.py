@@ -49,6 +49,19 @@ def test_config_machinery_and_defaults(tmp_path):
     assert subprocess.run([str(out)]).returncode == 0
 
 
+def test_value_types_known_answers(tmp_path):
+    """tests/cpp/value_types.cpp: the known answers of the reference's vector and polarity tests."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = Path(__file__).resolve().parent / "cpp" / "value_types.cpp"
+    out = tmp_path / "value_types"
+    r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                        "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def write_input(path, g):
     x0 = g["x0"]
     p0 = g.get("p0")
