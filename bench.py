@@ -351,6 +351,18 @@ def run_gb300(args):
         if pol:
             hp.numpy()[:n] = p
         nn = ctypes.c_uint(n)
+        # the user-facing path: no per-kernel events; one untimed round trip
+        # captures the step graph
+        sim.set_profiling(False)
+        tg._check(L.tecs_sim_upload(sim._h, ctypes.c_void_p(hx.data_ptr()),
+                                    ctypes.c_void_p(hp.data_ptr()) if pol else None, n))
+        tg._check(L.tecs_sim_step(sim._h, dt, 1))
+        tg._check(L.tecs_sim_download(sim._h, ctypes.c_void_p(hx.data_ptr()),
+                                      ctypes.c_void_p(hp.data_ptr()) if pol else None, ctypes.byref(nn)))
+        hx.numpy()[:n] = x
+        if pol:
+            hp.numpy()[:n] = p
+        nn = ctypes.c_uint(n)
         h2d = d2h = 0
         cs = 0
         torch.cuda.synchronize()

@@ -148,7 +148,9 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 // needs more shared memory -- spring-only engines use the leaner instance.
 template <int PASS, bool POL>
 static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
-  // neighbour slots per cell (the polarity law needs room for a fifth float per pair)
+  // neighbour slots per cell; the polarity law's extra per-pair float only
+  // fits in the static shared memory with 12 (cells with more in-cutoff
+  // neighbours take the per-thread path)
   constexpr int NB = POL ? 12 : kMaxNb;
   __shared__ float4 cand[NB * kPassThreads];
   __shared__ float4 home[kPassThreads];

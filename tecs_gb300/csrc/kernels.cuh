@@ -811,13 +811,15 @@ template <int D, int FORCE>
 static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
   static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
   constexpr bool POL = FORCE == 2;
-  // neighbour slots per cell (the polarity law needs room for a fifth float per pair)
+  // neighbour slots per cell; the polarity law's extra per-pair float only
+  // fits in the static shared memory with 12 (cells with more in-cutoff
+  // neighbours take the per-thread path)
   constexpr int NB = POL ? 12 : kMaxNb;
-  __shared__ float4 cand[NB * kPassThreads];            // [q][t]: position, w = (slot << 5) | bin code
-  __shared__ float4 home[kPassThreads];                     // position, w = packed bin coords
-  __shared__ unsigned short pinfo[NB * kPassThreads];   // (t << 4) | q, bit 15 = accepted
-  __shared__ int pofs[kPassThreads + 1];
-  __shared__ int wsum[kPassThreads / 32];
+  __shared__ float4 cand[NB * kPassThreads];           // [q][t]: position, w = (slot << 5) | bin code
+  __shared__ float4 home[kPassThreads];                // position, w = packed bin coords
+  __shared__ unsigned short pinfo[NB * kPassThreads];  // the block's pairs: (t << 4) | q
+  __shared__ unsigned wpk[kPassThreads / 32];          // per-warp pair counts, three classes packed
+  __shared__ unsigned amask[kPassThreads];             // accepted pairs of each cell, bit q
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
   // polarity law: the home cells' angles and their sin/cos, and the second
@@ -837,16 +839,17 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   int cnt = 0;
   bool fb = false;
   // ---- phase 1: in-cutoff neighbours of this thread's cell.  The row
-  // offsets of all 3x3 neighbour rows are fetched first and the candidates
-  // four at a time, so each thread keeps several loads in flight; a
-  // candidate's bin comes with its position (B.w holds the bin key).
+  // offsets of all 3x3 neighbour rows are fetched first, then the three rows
+  // of each z-plane are scanned together two candidates at a time, so each
+  // thread keeps several loads in flight; a candidate's bin comes with its
+  // position (B.w holds the bin key).
   if (active) {
     vi = __ldg(&a.X[i]);
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
     bin_coords_div<D>(g, xi, bc);
     constexpr int kRows = D >= 3 ? 9 : 3;
-    unsigned rlo[kRows], rhi[kRows], rb0[kRows], rmask[kRows];
+    unsigned rlo[kRows], rhi[kRows], rb0[kRows];
     const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
 #pragma unroll
     for (int r = 0; r < kRows; ++r) {
@@ -859,39 +862,50 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       rlo[r] = ok ? __ldg(&a.off[b0]) : 0u;
       rhi[r] = ok ? __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]) : 0u;
     }
-    // 1a: test every candidate, remembering the in-cutoff ones as bits per row
-    int total = 0;
+    // 1: test the candidates three rows (one z-plane) at a time and append
+    // the in-cutoff ones at once: rows are visited in the reference's task
+    // order and positions ascend within a row, so the list is in candidate order
+    const int rxo = x0 - bc[0] + 1;
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      unsigned m = 0u;
-      if (rhi[r] - rlo[r] > 32u) { fb = true; rmask[r] = 0u; continue; }
-      for (unsigned j0 = rlo[r]; j0 < rhi[r]; j0 += 4u) {
-        float4 v[4];
+    for (int g0 = 0; g0 < kRows; g0 += 3) {
+      unsigned len[3];
+      unsigned lmax = 0u;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) v[k] = __ldg(&a.X[min(j0 + k, rhi[r] - 1u)]);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const unsigned j = j0 + k;
-          const float e0 = xi[0] - v[k].x, e1 = xi[1] - v[k].y;
-          float d2 = e0 * e0 + e1 * e1;
-          if (D >= 3) { const float e2 = xi[2] - v[k].z; d2 = d2 + e2 * e2; }
-          if (j < rhi[r] && j != i && d2 < fp.rc2) m |= 1u << (j - rlo[r]);
-        }
+      for (int q = 0; q < 3; ++q) {
+        len[q] = rhi[g0 + q] - rlo[g0 + q];
+        lmax = max(lmax, len[q]);
       }
-      rmask[r] = m;
-      total += __popc(m);
-    }
-    if (total > NB) fb = true;
-    // 1b: append the in-cutoff candidates in candidate order (the summation order)
-    if (!fb) {
+      if (lmax > 32u) fb = true;
+      if (fb) continue;
+      unsigned m[3] = {0u, 0u, 0u};
+      for (unsigned o = 0; o < lmax; o += 2u) {
+        float4 v[3][2];
 #pragma unroll
-      for (int r = 0; r < kRows; ++r) {
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+            v[q][k] = __ldg(&a.X[len[q] ? rlo[g0 + q] + min(o + k, len[q] - 1u) : i]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const unsigned j = rlo[g0 + q] + o + k;
+            const float e0 = xi[0] - v[q][k].x, e1 = xi[1] - v[q][k].y;
+            float d2 = e0 * e0 + e1 * e1;
+            if (D >= 3) { const float e2 = xi[2] - v[q][k].z; d2 = d2 + e2 * e2; }
+            if (o + k < len[q] && j != i && d2 < fp.rc2) m[q] |= 1u << (o + k);
+          }
+      }
+      // append this plane's rows in order
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int r = g0 + q;
         const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(D >= 3 ? r / 3 : 1);
-        const int rxo = x0 - bc[0] + 1;
-        unsigned m = rmask[r];
-        while (m) {
-          const unsigned j = rlo[r] + (unsigned)(__ffs(m) - 1);
-          m &= m - 1u;
+        unsigned mm = m[q];
+        if (cnt + __popc(mm) > NB) { fb = true; break; }
+        while (mm) {
+          const unsigned j = rlo[r] + (unsigned)(__ffs(mm) - 1);
+          mm &= mm - 1u;
           const float4 v = __ldg(&a.X[j]);
           const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
           cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
@@ -909,24 +923,37 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     hpol[t] = pi;
     if (cnt) htrig[t] = pol_trig(pi);
   }
-  // exclusive scan of the neighbour counts -> pair offsets
+  // pair offsets: pairs grouped by their cell's neighbour count (<= 4, <= 8,
+  // more), so that the Gabriel loops of a warp's pairs run similar lengths;
+  // three 10-bit per-class sums packed in one word per scan
+  int P = 0;
   {
     const int lane = t & 31, warp = t >> 5;
-    int incl = cnt;
+    const int cls = cnt <= 4 ? 0 : (cnt <= 8 ? 1 : 2);
+    unsigned incl = (unsigned)cnt << (10 * cls);
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    if (lane == 31) wsum[warp] = incl;
+    if (lane == 31) wpk[warp] = incl;
+    amask[t] = 0u;
     __syncthreads();
-    int base = 0;
-    for (int w = 0; w < warp; ++w) base += wsum[w];
-    pofs[t] = base + incl - cnt;
-    if (t == kPassThreads - 1) pofs[kPassThreads] = base + incl;
+    int tot[3] = {0, 0, 0}, before = 0;
+#pragma unroll
+    for (int w = 0; w < kPassThreads / 32; ++w) {
+      const unsigned v = wpk[w];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) tot[f] += (int)((v >> (10 * f)) & 1023u);
+      if (w < warp) before += (int)((v >> (10 * cls)) & 1023u);
+    }
+    int base = before + (int)((incl >> (10 * cls)) & 1023u) - cnt;
+    if (cls >= 1) base += tot[0];
+    if (cls >= 2) base += tot[1];
+    P = tot[0] + tot[1] + tot[2];
+    for (int q = 0; q < cnt; ++q) pinfo[base + q] = (unsigned short)((t << 4) | q);
   }
-  for (int q = 0; q < cnt; ++q) pinfo[pofs[t] + q] = (unsigned short)((t << 4) | q);
   __syncthreads();
-  const int P = pofs[kPassThreads];
+
   // ---- phase 2: Gabriel test, one pair per thread at a time.  A witness k
   // blocks (i, j) when it is inside the ball (|x_k - m|^2 < r^2) and its bin
   // lies in the ball's bin range; the range (sqrt + floors) is only worked out
@@ -971,14 +998,14 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       }
       if (inside) { blocked = true; break; }
     }
-    if (!blocked) pinfo[p] = (unsigned short)(info | 0x8000u);
+    if (!blocked) atomicOr(&amask[c], 1u << q);
   }
   __syncthreads();
   // ---- phase 3: pair forces, written over the candidate slot
   for (int p = t; p < P; p += kPassThreads) {
     const unsigned info = pinfo[p];
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
-    if (!(info & 0x8000u) || fallback[c]) continue;
+    if (!((amask[c] >> q) & 1u) || fallback[c]) continue;
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
     float disp[3];
@@ -1021,9 +1048,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     if (fallback[t]) {
       cell_general<D, 3, FORCE>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc);
     } else {
-      const int base = pofs[t];
       for (int q = 0; q < cnt; ++q) {
-        if (!(pinfo[base + q] & 0x8000u)) continue;
+        if (!((amask[t] >> q) & 1u)) continue;
         const float4 f = cand[cix(q, t)];
         acc.x[0] = acc.x[0] + f.x;
         acc.x[1] = acc.x[1] + f.y;

@@ -541,9 +541,12 @@ static int upload_common(tecs_sim* s, unsigned n) {
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(s->stream));
+  // the captured step graphs depend on the state only through their grid
+  // size: keep them unless that changes
+  const unsigned old_launch = launch_count(s);
   s->n_host = n;
   s->step_count = 0;
-  drop_graphs(s);
+  if (launch_count(s) != old_launch) drop_graphs(s);
   return 0;
 }
 
