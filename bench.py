@@ -6,7 +6,8 @@ Workloads (--workload):
       density 1 (seed 1), binned Gabriel finder (cutoff 1.0, c = 0.8), spring
       force F = 2*max(0.7-d,0) - 0.5*max(d-0.8,0), Heun dt = 0.05,
       GlobalComFixer every step, cell division p = 1e-4 per cell per step
-      (daughter at 0.25 * random unit vector), capacity 1.05 N.
+      (daughter at 0.25 * random unit vector), capacity 1.05 N (grown when a
+      run's expected divisions need more).
   sheet: 100,000 cells on a sphere of radius sqrt(N/4pi)*0.8 (jitter 0.02),
       outward polarity + N(0, 0.1), binned Gabriel, spring + 0.2 (bending +
       alignment), Heun dt = 0.05.
@@ -118,11 +119,18 @@ def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def make_sim(w, n, mn, mx, device=0):
+def capacity_for(w, n, steps=0):
+    """The workload's capacity (>= its stated fraction of n), grown to hold the
+    expected divisions over `steps` steps with 2 % to spare."""
+    grow = (1.0 + w["division"]) ** steps * 1.02 if w["division"] > 0 else 1.0
+    return int(math.ceil(n * max(w["capacity"], grow)))
+
+
+def make_sim(w, n, mn, mx, device=0, steps=0):
     import tecs_gb300 as tg
 
     pf = tg.PairFinderSettings(gabriel_coefficient=0.8, min_bounds=mn, max_bounds=mx)
-    cap = int(math.ceil(n * w["capacity"]))
+    cap = capacity_for(w, n, steps)
     force = tg.PolaritySpring(k_pol=0.2) if w["polarity"] else tg.Spring2R(k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8)
     return tg.Simulation(tg.Settings(agent_count=n, capacity=cap, cutoff_distance=1.0, seed=1, pair_finder_settings=pf),
                          pair_finder=w["finder"], integrator=w["integrator"],
@@ -130,10 +138,10 @@ def make_sim(w, n, mn, mx, device=0):
                          division=tg.Division(probability=w["division"], offset=0.25), device=device)
 
 
-def make_oracle(w, n, mn, mx):
+def make_oracle(w, n, mn, mx, steps=0):
     import oracle
 
-    cap = int(math.ceil(n * w["capacity"]))
+    cap = capacity_for(w, n, steps)
     finder = oracle.BINNED_GABRIEL if w["finder"] == "binned_gabriel" else oracle.BINNED_ALL_PAIRS
     return oracle.Oracle(finder=finder, integrator=oracle.HEUN if w["integrator"] == "heun" else oracle.EULER,
                          com_fix=w["com"], min_bounds=mn, max_bounds=mx, capacity=cap,
@@ -234,7 +242,7 @@ def traffic_per_pass(workload: str):
 
 def cpu_steps(w, n, mn, mx, x, p, steps, threads, budget_s):
     """Time up to `steps` oracle steps (about budget_s seconds) after one warm-up step."""
-    o = make_oracle(w, n, mn, mx)
+    o = make_oracle(w, n, mn, mx, steps + 2)
     o.set_state(x, p)
     t0 = time.perf_counter()
     o.step(w["dt"], 1, threads)
@@ -287,14 +295,15 @@ def run_gb300(args):
     n = args.cells or w["cells"]
     pol = w["polarity"]
     x, p, mn, mx = w["make"](n)
-    sim = make_sim(w, n, mn, mx, device=local)
+    # steps before the end-to-end leg re-uploads the initial state: warm-up,
+    # timed, and the profiled run
+    sim = make_sim(w, n, mn, mx, device=local, steps=args.warmup + args.steps + 1 + min(args.steps, 100))
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     xd = torch.from_numpy(x).to("cuda")
     pd = torch.from_numpy(p).to("cuda") if pol else None
     torch.cuda.synchronize()
     sim.set_state_device(xd.data_ptr(), pd.data_ptr() if pol else None, n)
-    sim.set_profiling(True)
     dt = w["dt"]
 
     for _ in range(args.warmup):
@@ -304,11 +313,9 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    step_ms, kern = [], {}
-    cell_steps = 0
-    with Clocks(local) as clocks:
-        clocks.start()
-        for _ in range(args.steps):
+    def timed_steps(k, profile):
+        ms, cs = [], 0
+        for _ in range(k):
             nb = sim.get_agent_count()
             with torch.cuda.stream(stream):
                 flush.zero_()
@@ -319,11 +326,25 @@ def run_gb300(args):
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-            for name, ms in sim.last_step_profile():
-                kern.setdefault(name, []).append(ms)
-            cell_steps += nb
+            ms.append(e0.elapsed_time(e1))
+            if profile:
+                for name, v in sim.last_step_profile():
+                    kern.setdefault(name, []).append(v)
+            cs += nb
+        return ms, cs
+
+    kern = {}
+    with Clocks(local) as clocks:
+        clocks.start()
+        step_ms, cell_steps = timed_steps(args.steps, False)
         clocks.stop()
+    torch.cuda.synchronize()
+    # per-kernel CUDA events (event nodes inside the step graph) on a second,
+    # shorter run: the kernel table, the shares and the roofline's launch times
+    sim.set_profiling(True)
+    sim.take_step(dt)
+    prof_ms, prof_cells = timed_steps(min(args.steps, 100), True)
+    sim.set_profiling(False)
     torch.cuda.synchronize()
     total_s = sum(step_ms) / 1e3
     if world > 1:
@@ -365,23 +386,29 @@ def run_gb300(args):
         nn = ctypes.c_uint(n)
         h2d = d2h = 0
         cs = 0
+        t_up = t_rest = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             m = nn.value
+            ta = time.perf_counter()
             tg._check(L.tecs_sim_upload(sim._h, ctypes.c_void_p(hx.data_ptr()),
                                         ctypes.c_void_p(hp.data_ptr()) if pol else None, m))
+            tb = time.perf_counter()
             h2d += m * (20 if pol else 12)
             tg._check(L.tecs_sim_step(sim._h, dt, 1))
             tg._check(L.tecs_sim_download(sim._h, ctypes.c_void_p(hx.data_ptr()),
                                           ctypes.c_void_p(hp.data_ptr()) if pol else None, ctypes.byref(nn)))
+            t_up += tb - ta
+            t_rest += time.perf_counter() - tb
             d2h += nn.value * (20 if pol else 12)
             cs += m
         t1 = time.perf_counter()
         e2e = {"value": cs / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                "d2h_bytes_per_step": int(d2h / args.steps),
-               "note": "each step: pinned host state -> device (tecs_sim_upload), tecs_sim_step, "
-                       "device -> pinned host state (tecs_sim_download)"}
+               "ms_upload": 1e3 * t_up / args.steps, "ms_step_and_download": 1e3 * t_rest / args.steps,
+               "note": "each step: pinned host state -> device (tecs_sim_upload, synchronous), tecs_sim_step, "
+                       "device -> pinned host state (tecs_sim_download, synchronous)"}
 
     if rank != 0:
         if world > 1:
@@ -390,22 +417,23 @@ def run_gb300(args):
 
     hbm, peak_kind = peaks()
     n_avg = cell_steps / max(args.steps, 1)
+    n_prof = prof_cells / max(len(prof_ms), 1)
     pass_bytes, pass_s, pass_launches = 0.0, 0.0, 0
     for name, v in kern.items():
         if name in PASS_BYTES:
             b = PASS_BYTES[name][0] + (PASS_BYTES[name][1] if pol else 0)
-            pass_bytes += b * n_avg * len(v)
+            pass_bytes += b * n_prof * len(v)
             pass_s += sum(v) / 1e3
             pass_launches += len(v)
     achieved = pass_bytes / pass_s / 1e9 if pass_s else float("nan")
     tpc = traffic_per_pass(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": (tpc * n_avg if tpc else None),
+                "traffic": (tpc * n_prof if tpc else None),
                 "kernel": "force pass (k_pass_*: pair finding + force + fused integrator epilogue)",
                 "bytes_per_launch": pass_bytes / max(pass_launches, 1),
                 "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_s / max(pass_launches, 1)}
     step_achieved = w["step_bytes"] * n_avg / (statistics.mean(step_ms) / 1e3) / 1e9
-    kernel_table = {k: {"launches": len(v), "mean_ms": statistics.mean(v), "share": sum(v) / max(sum(step_ms), 1e-9)}
+    kernel_table = {k: {"launches": len(v), "mean_ms": statistics.mean(v), "share": sum(v) / max(sum(prof_ms), 1e-9)}
                     for k, v in kern.items()}
     cpu = None
     if not args.no_cpu_baseline and world == 1:

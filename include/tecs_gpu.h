@@ -87,8 +87,10 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out);
 /* Frees every device buffer of the simulation. */
 int tecs_sim_destroy(tecs_sim* sim);
 
-/* Initial state from host memory (n <= capacity); resets the step counters
- * as Simulation::set_agent_count does (include/simulation.hpp:295-302). */
+/* Initial state from host memory (n <= capacity); resets the finder's
+ * rebuild counter as Simulation::set_agent_count does
+ * (include/simulation.hpp:295-302).  The division stream stays keyed by the
+ * steps taken since creation. */
 int tecs_sim_upload(tecs_sim* sim, const float* positions, const float* polarity, unsigned n);
 
 /* Same from device memory on the simulation's device (no host copy). */

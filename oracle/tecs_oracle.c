@@ -109,7 +109,7 @@ int tecs_oracle_set_state(tecs_oracle* o, const float* pos, const float* pol, un
   memset(o->vold, 0, cap * D * 4);
   o->n = n;
   o->step_count = 0;  /* Simulation::set_agent_count -> finder.set_agent_count (binned_gabriel.hpp:61-64) */
-  o->step_index = 0;
+  /* step_index (the division stream) counts the steps since creation: a new state does not restart it */
   return 0;
 }
 

@@ -155,8 +155,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   __shared__ float4 cand[NB * kPassThreads];
   __shared__ float4 home[kPassThreads];
   __shared__ unsigned short pinfo[NB * kPassThreads];
-  __shared__ int pofs[kPassThreads + 1];
-  __shared__ int wsum[kPassThreads / 32];
+  __shared__ unsigned wpk[kPassThreads / 32];
+  __shared__ unsigned amask[kPassThreads];
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
   __shared__ unsigned hsim[kPassThreads];
@@ -192,7 +192,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   if (run && !fb) {
     const GridP& g = sl.g;
     const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
-    unsigned rlo[9], rhi[9], rb0[9], rmask[9];
+    unsigned rlo[9], rhi[9], rb0[9];
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
       const int cy = bc[1] + r % 3 - 1, cz = bc[2] + r / 3 - 1;
@@ -205,36 +205,47 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     }
     const int rxo = x0 - bc[0] + 1;
     const float rc2 = sl.fp.rc2;
-    int total = 0;
+    // as k_pass_gabriel: the three rows of each z-plane scanned together, two
+    // candidates at a time, in-cutoff ones appended in candidate order
 #pragma unroll
-    for (int r = 0; r < 9; ++r) {
-      unsigned m = 0u;
-      if (rhi[r] - rlo[r] > 32u) { fb = true; rmask[r] = 0u; continue; }
-      for (unsigned j0 = rlo[r]; j0 < rhi[r]; j0 += 4u) {
-        float4 v[4];
+    for (int g0 = 0; g0 < 9; g0 += 3) {
+      unsigned len[3];
+      unsigned lmax = 0u;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) v[k] = __ldg(&e.X[min(j0 + k, rhi[r] - 1u)]);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const unsigned j = j0 + k;
-          const float e0 = xi[0] - v[k].x, e1 = xi[1] - v[k].y, e2 = xi[2] - v[k].z;
-          float d2 = e0 * e0 + e1 * e1;
-          d2 = d2 + e2 * e2;
-          if (j < rhi[r] && j != i && d2 < rc2) m |= 1u << (j - rlo[r]);
-        }
+      for (int q = 0; q < 3; ++q) {
+        len[q] = rhi[g0 + q] - rlo[g0 + q];
+        lmax = max(lmax, len[q]);
       }
-      rmask[r] = m;
-      total += __popc(m);
-    }
-    if (total > NB) fb = true;
-    if (!fb) {
+      if (lmax > 32u) fb = true;
+      if (fb) continue;
+      unsigned m[3] = {0u, 0u, 0u};
+      for (unsigned o = 0; o < lmax; o += 2u) {
+        float4 v[3][2];
 #pragma unroll
-      for (int r = 0; r < 9; ++r) {
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+            v[q][k] = __ldg(&e.X[len[q] ? rlo[g0 + q] + min(o + k, len[q] - 1u) : i]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const unsigned j = rlo[g0 + q] + o + k;
+            const float e0 = xi[0] - v[q][k].x, e1 = xi[1] - v[q][k].y, e2 = xi[2] - v[q][k].z;
+            float d2 = e0 * e0 + e1 * e1;
+            d2 = d2 + e2 * e2;
+            if (o + k < len[q] && j != i && d2 < rc2) m[q] |= 1u << (o + k);
+          }
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int r = g0 + q;
         const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(r / 3);
-        unsigned m = rmask[r];
-        while (m) {
-          const unsigned j = rlo[r] + (unsigned)(__ffs(m) - 1);
-          m &= m - 1u;
+        unsigned mm = m[q];
+        if (cnt + __popc(mm) > NB) { fb = true; break; }
+        while (mm) {
+          const unsigned j = rlo[r] + (unsigned)(__ffs(mm) - 1);
+          mm &= mm - 1u;
           const float4 v = __ldg(&e.X[j]);
           const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
           cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
@@ -253,30 +264,42 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     hpol[t] = pi;
     if (cnt && polar) htrig[t] = pol_trig(pi);
   }
+  // pair offsets, pairs grouped by their cell's neighbour count (as k_pass_gabriel)
+  int P = 0;
   {
     const int lane = t & 31, warp = t >> 5;
-    int incl = cnt;
+    const int cls = cnt <= 4 ? 0 : (cnt <= 8 ? 1 : 2);
+    unsigned incl = (unsigned)cnt << (10 * cls);
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    if (lane == 31) wsum[warp] = incl;
+    if (lane == 31) wpk[warp] = incl;
+    amask[t] = 0u;
     __syncthreads();
-    int base = 0;
-    for (int w = 0; w < warp; ++w) base += wsum[w];
-    pofs[t] = base + incl - cnt;
-    if (t == kPassThreads - 1) pofs[kPassThreads] = base + incl;
+    int tot[3] = {0, 0, 0}, before = 0;
+#pragma unroll
+    for (int w = 0; w < kPassThreads / 32; ++w) {
+      const unsigned v = wpk[w];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) tot[f] += (int)((v >> (10 * f)) & 1023u);
+      if (w < warp) before += (int)((v >> (10 * cls)) & 1023u);
+    }
+    int base = before + (int)((incl >> (10 * cls)) & 1023u) - cnt;
+    if (cls >= 1) base += tot[0];
+    if (cls >= 2) base += tot[1];
+    P = tot[0] + tot[1] + tot[2];
+    for (int q = 0; q < cnt; ++q) pinfo[base + q] = (unsigned short)((t << 4) | q);
   }
-  for (int q = 0; q < cnt; ++q) pinfo[pofs[t] + q] = (unsigned short)((t << 4) | q);
   __syncthreads();
-  const int P = pofs[kPassThreads];
+
   // Gabriel test (all-pairs slots accept every in-cutoff pair)
   for (int p = t; p < P; p += kPassThreads) {
     const unsigned info = pinfo[p];
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const SimSlot& cs = e.table[hsim[c]];
     if (cs.finder != TECS_FINDER_BINNED_GABRIEL) {
-      pinfo[p] = (unsigned short)(info | 0x8000u);
+      atomicOr(&amask[c], 1u << q);
       continue;
     }
     const float4 h = home[c];
@@ -312,14 +335,14 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       }
       if (inside) { blocked = true; break; }
     }
-    if (!blocked) pinfo[p] = (unsigned short)(info | 0x8000u);
+    if (!blocked) atomicOr(&amask[c], 1u << q);
   }
   __syncthreads();
   // pair forces (spring2r), written over the candidate slot
   for (int p = t; p < P; p += kPassThreads) {
     const unsigned info = pinfo[p];
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
-    if (!(info & 0x8000u)) continue;
+    if (!((amask[c] >> q) & 1u)) continue;
     const SimSlot& cs = e.table[hsim[c]];
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
@@ -352,9 +375,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   // ordered sums of the cooperative pairs
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
   if (run && !fallback[t]) {
-    const int base = pofs[t];
     for (int q = 0; q < cnt; ++q) {
-      if (!(pinfo[base + q] & 0x8000u)) continue;
+      if (!((amask[t] >> q) & 1u)) continue;
       const float4 f = cand[cix(q, t)];
       acc.x[0] = acc.x[0] + f.x;
       acc.x[1] = acc.x[1] + f.y;

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -531,9 +532,13 @@ static int upload_common(tecs_sim* s, unsigned n) {
     CK(cudaMemsetAsync(s->dp1, 0, cap * 8, s->stream));
     CK(cudaMemsetAsync(s->dp2, 0, cap * 8, s->stream));
   }
+  // reset every counter but the step index: the division stream is keyed by
+  // the steps taken since creation, and a new state does not restart it
   Counters c{};
   c.n = n;
-  CK(cudaMemcpyAsync(s->ctr, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+  static_assert(offsetof(Counters, step) + sizeof(c.step) == offsetof(Counters, pair_count), "Counters layout");
+  CK(cudaMemcpyAsync(s->ctr, &c, offsetof(Counters, step), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemsetAsync(&s->ctr->pair_count, 0, sizeof(c.pair_count), s->stream));
   if (s->fuse_count) {
     // the first rebuild expects the bin counts of A to be made already
     CK(cudaMemsetAsync(s->cnt, 0, ((size_t)s->g.nbins + 1) * 4, s->stream));
