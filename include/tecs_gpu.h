@@ -123,6 +123,15 @@ int tecs_sim_evaluate(tecs_sim* sim, float* dpos, float* dpol, uint32_t* pairs, 
 /* The simulation's CUDA stream (a cudaStream_t). */
 void* tecs_sim_stream(tecs_sim* sim);
 
+/* Links (include/types/link.hpp): n_links (a, b) cell-id pairs with the
+ * constant-pull link law of examples/intercalation.cpp:65-71 -- at every
+ * force evaluation cell a gets strength*(x_b - x_a)/|x_b - x_a| and cell b
+ * its negative, after the pairwise forces and in link order
+ * (integrators/base.hpp:197-234); links with a == b are skipped.  Replaces
+ * Settings::link_capacity + get_links() + a LINK_FORCE of that law.  Non-symmetric
+ * finders; n_links == 0 removes the links. */
+int tecs_sim_set_links(tecs_sim* sim, const uint32_t* links, unsigned n_links, float strength);
+
 /* Change the pairwise force law between steps: take_step(dt, force) with a
  * different force functor (include/simulation.hpp:548-556).  No-op when the
  * law and its constants are unchanged; otherwise waits for queued steps. */

@@ -80,6 +80,7 @@ def lib():
         L.tecs_oracle_evaluate.restype = ctypes.c_long
         L.tecs_oracle_evaluate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_long, ctypes.c_int]
+        L.tecs_oracle_set_links.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_float]
         L.tecs_oracle_hash.restype = ctypes.c_uint64
         L.tecs_oracle_hash.argtypes = [ctypes.c_uint64] * 4
         L.tecs_oracle_last_error.restype = ctypes.c_char_p
@@ -128,6 +129,12 @@ class Oracle:
         x = np.ascontiguousarray(positions, dtype=np.float32)
         p = None if polarity is None else np.ascontiguousarray(polarity, dtype=np.float32)
         if lib().tecs_oracle_set_state(self._h, _ptr(x), _ptr(p), x.shape[0]) != 0:
+            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+
+    def set_links(self, links, strength):
+        """(a, b) pairs with the constant-pull link law of strength `strength`."""
+        lk = np.ascontiguousarray(links, dtype=np.uint32).reshape(-1, 2)
+        if lib().tecs_oracle_set_links(self._h, _ptr(lk), lk.shape[0], strength) != 0:
             raise RuntimeError(lib().tecs_oracle_last_error().decode())
 
     @property

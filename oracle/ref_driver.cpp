@@ -12,6 +12,10 @@
 // outputs: <out>.pairs (uint32 pairs, evaluation order), <out>.dpos, <out>.dpol
 //          (one full-step pass from a fresh finder), <out>.pos / <out>.pol
 //          (state after <steps> take_step calls).
+// Link scenarios (names starting "lk_") read, after the polarity block,
+// uint32 n_links and uint32 links[2*n_links] (a, b), take the link strength
+// from params[15], step with take_step(dt, link_force, pairwise_force) and
+// write <out>.pos only.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -48,9 +52,10 @@ struct Input {
   unsigned n = 0, dims = 0, has_pol = 0;
   float prm[16] = {};
   std::vector<float> x, p;
+  std::vector<unsigned> links;
 };
 
-static Input read_input(const char* path) {
+static Input read_input(const char* path, bool with_links) {
   Input in;
   FILE* f = std::fopen(path, "rb");
   if (!f) { std::perror(path); std::exit(2); }
@@ -63,6 +68,12 @@ static Input read_input(const char* path) {
   if (in.has_pol) {
     in.p.resize((size_t)in.n * 2);
     if (in.n && std::fread(in.p.data(), 4, in.p.size(), f) != in.p.size()) std::exit(2);
+  }
+  if (with_links) {
+    unsigned nl = 0;
+    if (std::fread(&nl, 4, 1, f) != 1) std::exit(2);
+    in.links.resize((size_t)nl * 2);
+    if (nl && std::fread(in.links.data(), 4, in.links.size(), f) != in.links.size()) std::exit(2);
   }
   std::fclose(f);
   return in;
@@ -214,6 +225,58 @@ static int tecs_driver_run(const Input& in, const std::string& out, int steps, d
   return 0;
 }
 
+// Link scenarios: the protrusion law of examples/intercalation.cpp:65-71
+// (constant pull of strength k along the link) with the spring pairwise law.
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields, class LinkForceFields>
+static int tecs_driver_run_links(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const Scalar k_link = in.prm[15];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() { return PAIRWISE_FORCE(TECS_DRIVER_SPRING)(); };
+  auto make_link_force = LINK_FORCE(
+    Vector displacement = ctx.position.b - ctx.position.a;
+    Scalar distance = displacement.length();
+    ctx.position.delta_a += k_link * displacement / distance;
+    ctx.position.delta_b += -k_link * displacement / distance;
+  );
+  typename Simulation<Config>::Settings st(n, "unused");
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  const unsigned nl = (unsigned)(in.links.size() / 2);
+  st.link_capacity = nl ? nl : 1;
+  st.link_active_count = nl;
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+  auto& links = sim.get_links();
+  for (unsigned l = 0; l < nl; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+  auto force = make_force();
+  auto link_force = make_link_force();
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, link_force, force);
+  std::vector<float> flat((size_t)n * in.dims);
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) flat[(size_t)i * in.dims + d] = pos(i)[d];
+  write_raw(out + ".pos", flat.data(), flat.size() * 4);
+  return 0;
+}
+
+#define TECS_LINK_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                           \
+  namespace NAME {                                                                                      \
+  CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
+                                       CONFIG_COM_FIXER(COMFIXER) CONFIG_WRITER(tecs::io::Dummy)         \
+                                           TECS_FIELDS_0)                                                \
+  EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)                                                            \
+  static int run(const Input& in, const std::string& out, int steps, double dt) {                       \
+    return tecs_driver_run_links<Config, Scalar, Vector, Random, PairwiseForceFields, LinkForceFields>(  \
+        in, out, steps, dt);                                                                            \
+  }                                                                                                     \
+  }
+
 using namespace tecs;
 TECS_SCENARIO(ba_euler_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::NoComFixer, 3, 0)
 TECS_SCENARIO(ba_heun_com_3, pair_finders::BinnedAllPairs, integrators::Heun, com_fixers::GlobalComFixer, 3, 0)
@@ -231,6 +294,8 @@ TECS_SCENARIO(ng_euler_2, pair_finders::NaiveGabriel, integrators::Euler, com_fi
 TECS_SCENARIO(bg_heun_2, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 2, 0)
 TECS_SCENARIO(nd_euler_2, pair_finders::NaiveDelaunay, integrators::Euler, com_fixers::NoComFixer, 2, 0)
 TECS_SCENARIO(nd_heun_3, pair_finders::NaiveDelaunay, integrators::Heun, com_fixers::NoComFixer, 3, 0)
+TECS_LINK_SCENARIO(lk_bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer)
+TECS_LINK_SCENARIO(lk_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::GlobalComFixer)
 
 int main(int argc, char** argv) {
   if (argc < 6) {
@@ -239,7 +304,7 @@ int main(int argc, char** argv) {
   }
   Kokkos::initialize();
   const std::string sc = argv[1];
-  const Input in = read_input(argv[2]);
+  const Input in = read_input(argv[2], sc.rfind("lk_", 0) == 0);
   const std::string out = argv[3];
   const int steps = std::atoi(argv[4]);
   const double dt = std::atof(argv[5]);
@@ -249,6 +314,7 @@ int main(int argc, char** argv) {
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2) DISPATCH(nd_euler_2) DISPATCH(nd_heun_3)
+  DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3)
 #undef DISPATCH
   if (rc == 3) std::fprintf(stderr, "unknown scenario %s\n", sc.c_str());
   return rc;

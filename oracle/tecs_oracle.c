@@ -43,6 +43,9 @@ struct tecs_oracle {
   unsigned perm_cap;
   int step_count;      /* pair finder rebuild counter (binned_gabriel.hpp:58-59) */
   uint64_t step_index; /* integrator steps taken, keys the division RNG */
+  uint32_t* links;     /* (a, b) pairs */
+  unsigned n_links;
+  float link_strength;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -93,7 +96,7 @@ tecs_oracle* tecs_oracle_create(const tecs_oracle_desc* desc) {
 void tecs_oracle_destroy(tecs_oracle* o) {
   if (!o) return;
   free(o->x); free(o->p); free(o->d1x); free(o->d1p); free(o->x2); free(o->p2);
-  free(o->d3x); free(o->d3p); free(o->vold);
+  free(o->d3x); free(o->d3p); free(o->vold); free(o->links);
   free(o->perm); free(o->offsets); free(o->bins_scratch);
   free(o);
 }
@@ -424,6 +427,38 @@ static int visit_pair(const tecs_oracle* o, const float* xin, const float* pin, 
   return reps;
 }
 
+/* The link forces of one evaluation, after the pairwise ones: Serial order of
+ * integrators/base.hpp:205-233, each endpoint's accumulator starting at zero. */
+static void apply_links(const tecs_oracle* o, const float* xin, float* ox) {
+  const int D = o->d.dims;
+  const float k = o->link_strength;
+  for (unsigned l = 0; l < o->n_links; ++l) {
+    const unsigned a = o->links[2 * l], b = o->links[2 * l + 1];
+    if (a == b) continue;
+    float disp[3] = {0, 0, 0}, d2 = 0.0f;
+    for (int d = 0; d < D; ++d) disp[d] = xin[(size_t)b * D + d] - xin[(size_t)a * D + d];
+    for (int d = 0; d < D; ++d) d2 = d2 + disp[d] * disp[d];
+    const float dist = sqrtf(d2);
+    for (int d = 0; d < D; ++d) ox[(size_t)a * D + d] = ox[(size_t)a * D + d] + (0.0f + (k * disp[d]) / dist);
+    for (int d = 0; d < D; ++d) ox[(size_t)b * D + d] = ox[(size_t)b * D + d] + (0.0f + (-k * disp[d]) / dist);
+  }
+}
+
+int tecs_oracle_set_links(tecs_oracle* o, const uint32_t* links, unsigned n_links, float strength) {
+  for (unsigned l = 0; l < 2 * n_links; ++l)
+    if (links[l] >= o->d.capacity) { set_err("link endpoint beyond capacity"); return -1; }
+  free(o->links);
+  o->links = NULL;
+  o->n_links = 0;
+  if (n_links) {
+    o->links = (uint32_t*)malloc((size_t)n_links * 8);
+    memcpy(o->links, links, (size_t)n_links * 8);
+  }
+  o->n_links = n_links;
+  o->link_strength = strength;
+  return 0;
+}
+
 /* One pass of finder.evaluate_force: in = (xin, pin), out = (ox, op).
  * Non-symmetric finders: each cell i owns its accumulator (…/binned_gabriel.hpp:95-361,
  * binned_all_pairs.hpp:97-182, naive_*.hpp).  Symmetric finders: j < i only, +delta
@@ -482,6 +517,7 @@ static void eval_pass(tecs_oracle* o, const float* xin, const float* pin, float*
     for (unsigned i = 0; i < n; ++i)
       for (int d = 0; d < D; ++d) ox[(size_t)i * D + d] += tvel[(size_t)i * D + d] / fmaxf(tdrag[i], eps);
     free(tdrag); free(tvel);
+    apply_links(o, xin, ox);
     return;
   }
 
@@ -533,6 +569,7 @@ static void eval_pass(tecs_oracle* o, const float* xin, const float* pin, float*
     if (op) { op[(size_t)i * 2] = op[(size_t)i * 2] + a.dp[0]; op[(size_t)i * 2 + 1] = op[(size_t)i * 2 + 1] + a.dp[1]; }
     for (int d = 0; d < D; ++d) ox[(size_t)i * D + d] = ox[(size_t)i * D + d] + tvel[d] / fmaxf(tdrag, eps);
   }
+  apply_links(o, xin, ox);
 }
 
 /* com_fixers.hpp:24-45: sum over extent(0) == capacity, divided by it */

@@ -72,6 +72,13 @@ int tecs_oracle_set_state(tecs_oracle* o, const float* positions, const float* p
 unsigned tecs_oracle_count(const tecs_oracle* o);
 int tecs_oracle_get_state(const tecs_oracle* o, float* positions, float* polarity);
 
+/* Links (include/types/link.hpp) with the constant-pull link law of
+ * examples/intercalation.cpp:65-71: every force evaluation adds, after the
+ * pairwise forces and in link order, k*(x_b - x_a)/|x_b - x_a| to cell a and
+ * its negative to cell b; links with a == b are skipped
+ * (integrators/base.hpp:197-234).  links: n_links (a, b) pairs; 0 clears. */
+int tecs_oracle_set_links(tecs_oracle* o, const uint32_t* links, unsigned n_links, float strength);
+
 /* n_steps integrator steps (plus division when enabled) */
 int tecs_oracle_step(tecs_oracle* o, double dt, int n_steps, int threads);
 

@@ -70,7 +70,8 @@ _EXPORTS = (
     "tecs_sim_desc_default", "tecs_sim_create", "tecs_sim_destroy", "tecs_sim_upload", "tecs_sim_upload_device",
     "tecs_sim_step", "tecs_sim_synchronize", "tecs_sim_count", "tecs_sim_download", "tecs_sim_evaluate",
     "tecs_sim_stream", "tecs_sim_set_graph", "tecs_sim_kernels_per_step", "tecs_last_error",
-    "tecs_sim_set_profiling", "tecs_sim_last_step_profile", "tecs_sim_profile_name",
+    "tecs_sim_set_profiling", "tecs_sim_last_step_profile", "tecs_sim_profile_name", "tecs_sim_set_links",
+    "tecs_sim_set_force",
 )
 
 
@@ -103,6 +104,8 @@ def load(build_if_missing: bool = True):
     L.tecs_sim_stream.restype = vp
     L.tecs_sim_stream.argtypes = [vp]
     L.tecs_sim_set_graph.argtypes = [vp, ctypes.c_int]
+    L.tecs_sim_set_links.argtypes = [vp, vp, ctypes.c_uint, ctypes.c_float]
+    L.tecs_sim_set_force.argtypes = [vp, ctypes.c_int] + [ctypes.c_float] * 5
     L.tecs_sim_kernels_per_step.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.tecs_sim_set_profiling.argtypes = [vp, ctypes.c_int]
     L.tecs_sim_last_step_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
@@ -245,6 +248,12 @@ class Simulation:
         x = np.ascontiguousarray(positions, dtype=np.float32)
         p = None if polarity is None else np.ascontiguousarray(polarity, dtype=np.float32)
         _check(load().tecs_sim_upload(self._h, _ptr(x), _ptr(p), x.shape[0]))
+
+    def set_links(self, links, strength: float):
+        """Links as (a, b) cell-id pairs with the constant-pull link law of strength
+        `strength` (examples/intercalation.cpp:65-71); an empty array removes them."""
+        lk = np.ascontiguousarray(links, dtype=np.uint32).reshape(-1, 2)
+        _check(load().tecs_sim_set_links(self._h, _ptr(lk) if len(lk) else None, lk.shape[0], float(strength)))
 
     def set_state_device(self, positions_ptr: int, polarity_ptr: Optional[int], n: int):
         _check(load().tecs_sim_upload_device(self._h, ctypes.c_void_p(positions_ptr),

@@ -81,6 +81,13 @@ struct PassArgs {
   unsigned* cnt;
   // naive Delaunay: how many times each directed pair is applied, row i at i * capacity
   const unsigned short* dmult;
+  // links of each cell id, in link order: link_ent[link_off[id] .. link_off[id + 1])
+  // = (other cell id, 1 when this cell is the link's b end); slot_of maps an
+  // id to its slot in X (null when X is in id order)
+  const unsigned* link_off;
+  const uint2* link_ent;
+  const unsigned* slot_of;
+  float link_k;
 };
 
 // ---------------------------------------------------------------------------
@@ -195,7 +202,8 @@ __device__ __forceinline__ unsigned id_at(const float4* X, const unsigned* Bid, 
 static __global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
                                       const unsigned* __restrict__ off, const unsigned* __restrict__ src,
                                       const float4* __restrict__ A, const float2* __restrict__ PA,
-                                      float4* __restrict__ B, float2* __restrict__ PB, unsigned* __restrict__ Bid) {
+                                      float4* __restrict__ B, float2* __restrict__ PB, unsigned* __restrict__ Bid,
+                                      unsigned* __restrict__ slot_of) {
   const unsigned n = ctr->n;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const unsigned s = src[t];
@@ -213,6 +221,7 @@ static __global__ void k_order_gather(const Counters* __restrict__ ctr, const un
     // position); the id moves to Bid
     B[dst] = make_float4(v.x, v.y, v.z, __uint_as_float(b));
     Bid[dst] = id_of(v);
+    if (slot_of) slot_of[id_of(v)] = dst;  // links find their other end by id
     if (PB) PB[dst] = PA[s];
   }
 }
@@ -556,12 +565,42 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
 // Commit of one cell: out(i) = 0 + sum (views(i) += values on cleared stage
 // buffers); the drag term adds exactly zero for the built-in laws
 // (pairwise_drag = 0).  Then the fused integrator epilogue of the mode.
+// One link's force on this cell, added after the pairwise sum: the
+// constant-pull law of examples/intercalation.cpp:65-71 -- cell a gets
+// k*(x_b - x_a)/|x_b - x_a|, cell b its negative -- in the Serial order of
+// integrators/base.hpp:205-233 (link order, each term from a zero accumulator).
+// A link to an id beyond the active cells sees the zero position of an unused
+// view slot.
+template <int D>
+__device__ __forceinline__ void add_link(const PassArgs& a, unsigned n, const float* xs, unsigned e, float* s) {
+  const uint2 le = a.link_ent[e];
+  float xo[3] = {0.f, 0.f, 0.f};
+  if (le.x < n) {
+    const float4 v = a.X[a.slot_of ? a.slot_of[le.x] : le.x];
+    xo[0] = v.x; xo[1] = v.y; xo[2] = v.z;
+  }
+  float disp[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = 0; d < D; ++d) disp[d] = le.y ? xs[d] - xo[d] : xo[d] - xs[d];
+  float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+  if (D >= 3) d2 = d2 + disp[2] * disp[2];
+  const float dist = sqrtf(d2);
+  const float k = le.y ? -a.link_k : a.link_k;
+#pragma unroll
+  for (int d = 0; d < D; ++d) s[d] = s[d] + (0.0f + (k * disp[d]) / dist);
+}
+
 template <int D>
 __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
                                               const float* xi, const float4& vi, const float2& pi, const Acc& acc) {
   float s[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
+  if (a.link_off && active) {
+    const unsigned id = a.Bid ? a.Bid[i] : id_of(vi);
+    const unsigned e1 = a.link_off[id + 1];
+    for (unsigned e = a.link_off[id]; e < e1; ++e) add_link<D>(a, n, xi, e, s);
+  }
   const float sp0 = 0.0f + acc.p[0], sp1 = 0.0f + acc.p[1];
   if (a.mode == kStore) {
     if (active) {

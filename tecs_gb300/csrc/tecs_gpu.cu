@@ -63,6 +63,16 @@ __global__ void k_pack(const float* __restrict__ in, unsigned n, int dims, float
     A[s] = v;
   }
 }
+// id -> slot map of the sorted copy, from its slot -> id array
+__global__ void k_slot_map(const Counters* __restrict__ ctr, const unsigned* __restrict__ Bid, unsigned capacity,
+                           unsigned* __restrict__ slot_of) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const unsigned id = Bid[s];
+    if (id < capacity) slot_of[id] = s;
+  }
+}
+
 // scatter slot-ordered float4 values into cell-id order AoS float[n][dims]
 __global__ void k_unpack(const float4* __restrict__ idw, const unsigned* __restrict__ ids,
                          const float4* __restrict__ val, unsigned n, int dims, float* __restrict__ out) {
@@ -93,6 +103,15 @@ struct tecs_sim {
   unsigned *div_parent = nullptr, *div_slot = nullptr;
   unsigned* Bid = nullptr;  // cell ids of B's slots (B.w holds the bin key)
   unsigned short* dmult = nullptr;  // naive Delaunay: applications per directed pair, capacity x capacity
+  // links: per-cell entries in link order, and the id -> slot map of the sorted copy
+  unsigned* link_off = nullptr;
+  uint2* link_ent = nullptr;
+  unsigned* slot_of = nullptr;
+  unsigned n_links = 0;
+  float link_k = 0.f;
+  // B and Bid hold a sort of the current cells (false from an upload until the
+  // next rebuild, which the first step after an upload always does)
+  bool sorted = false;
   Counters* ctr = nullptr;
   double* com_part = nullptr;
   float* com = nullptr;  // [0..2] pass 1, [4..6] pass 2
@@ -205,6 +224,10 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.rank = s->rank;
   a.cnt = s->cnt;
   a.dmult = s->dmult;
+  a.link_off = s->n_links ? s->link_off : nullptr;
+  a.link_ent = s->n_links ? s->link_ent : nullptr;
+  a.slot_of = (s->n_links && s->binned) ? s->slot_of : nullptr;
+  a.link_k = s->link_k;
   return a;
 }
 
@@ -234,7 +257,8 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
-    k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid);
+    k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid,
+                                              s->n_links ? s->slot_of : nullptr);
     PROF_END(s, "k_order_gather");
     K += 4;
   } else {
@@ -516,7 +540,7 @@ int tecs_sim_destroy(tecs_sim* s) {
     if (e) cudaEventDestroy(e);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
-                  s->Bid, s->dmult};
+                  s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -551,6 +575,7 @@ static int upload_common(tecs_sim* s, unsigned n) {
   const unsigned old_launch = launch_count(s);
   s->n_host = n;
   s->step_count = 0;
+  s->sorted = false;
   if (launch_count(s) != old_launch) drop_graphs(s);
   return 0;
 }
@@ -605,6 +630,7 @@ int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
       if (enqueue_step(s, fdt, rebuild, K)) return -1;
       s->last_kernels = K;
       s->prof_last = s->prof_n;
+      if (rebuild) s->sorted = true;
       continue;
     }
     if (!s->gexec[gk] || s->gdt[gk] != fdt) {
@@ -628,6 +654,7 @@ int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
     }
     CK(cudaGraphLaunch(s->gexec[gk], s->stream));
     s->last_kernels = s->kernels[gk];
+    if (rebuild) s->sorted = true;
   }
   return 0;
 }
@@ -694,6 +721,7 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   a.pair_cap = dpairs ? pair_cap : 0;
   a.count_next = 0;
   int rc = enqueue_pass(s, a, K);
+  if (rc == 0 && s->binned) s->sorted = true;  // the rebuild above sorted the current cells
   if (rc == 0 && s->fuse_count && n) {
     // A is unchanged: count it again for the next step's rebuild
     k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
@@ -747,6 +775,58 @@ int tecs_sim_set_force(tecs_sim* s, int force, float k_rep, float r_rep, float k
   s->d.k_rep = k_rep; s->d.r_rep = r_rep; s->d.k_adh = k_adh; s->d.r_adh = r_adh; s->d.k_pol = k_pol;
   f.force = force;
   f.k_rep = k_rep; f.r_rep = r_rep; f.k_adh = k_adh; f.r_adh = r_adh; f.k_pol = k_pol;
+  drop_graphs(s);
+  return 0;
+}
+
+int tecs_sim_set_links(tecs_sim* s, const uint32_t* links, unsigned n_links, float strength) {
+  if (!s || (n_links && !links)) return fail("null argument");
+  if (n_links && s->d.symmetric) return fail("links are served with the non-symmetric finders");
+  const unsigned cap = s->d.capacity;
+  for (size_t l = 0; l < 2 * (size_t)n_links; ++l)
+    if (links[l] >= cap) return fail("link endpoint beyond capacity");
+  CK(cudaSetDevice(s->d.device));
+  CK(cudaStreamSynchronize(s->stream));
+  // per-cell entries, each cell's in link order (a counting sort by endpoint)
+  std::vector<unsigned> off((size_t)cap + 1, 0u);
+  for (unsigned l = 0; l < n_links; ++l) {
+    const unsigned a = links[2 * l], b = links[2 * l + 1];
+    if (a == b) continue;  // skipped by the reference (integrators/base.hpp:211-212)
+    ++off[a + 1];
+    ++off[b + 1];
+  }
+  for (unsigned c = 0; c < cap; ++c) off[c + 1] += off[c];
+  const unsigned entries = off[cap];
+  std::vector<uint2> ent(entries ? entries : 1);
+  std::vector<unsigned> fill(off.begin(), off.end() - 1);
+  for (unsigned l = 0; l < n_links; ++l) {
+    const unsigned a = links[2 * l], b = links[2 * l + 1];
+    if (a == b) continue;
+    ent[fill[a]++] = make_uint2(b, 0u);
+    ent[fill[b]++] = make_uint2(a, 1u);
+  }
+  for (void* p : {(void*)s->link_off, (void*)s->link_ent, (void*)s->slot_of})
+    if (p) CK(cudaFree(p));
+  s->link_off = nullptr;
+  s->link_ent = nullptr;
+  s->slot_of = nullptr;
+  s->n_links = 0;
+  if (entries) {
+    CK(cudaMalloc((void**)&s->link_off, ((size_t)cap + 1) * 4));
+    CK(cudaMalloc((void**)&s->link_ent, (size_t)entries * sizeof(uint2)));
+    CK(cudaMalloc((void**)&s->slot_of, (size_t)cap * 4));
+    CK(cudaMemcpy(s->link_off, off.data(), ((size_t)cap + 1) * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->link_ent, ent.data(), (size_t)entries * sizeof(uint2), cudaMemcpyHostToDevice));
+    s->n_links = n_links;
+  }
+  s->link_k = strength;
+  // the id -> slot map of the current sorted order (every rebuild rewrites it);
+  // the rebuild schedule itself is not touched, as in the reference
+  if (s->n_links && s->binned && s->sorted) {
+    k_slot_map<<<ceil_div(s->d.capacity, 256), 256, 0, s->stream>>>(s->ctr, s->Bid, s->d.capacity, s->slot_of);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+  }
   drop_graphs(s);
   return 0;
 }

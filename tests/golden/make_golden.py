@@ -54,7 +54,26 @@ SCENARIOS = {
     "nd_euler_2d": ("nd_euler_2", 4, 0, 0, 0, 2, 0),
     "nd_euler_2d_points11": ("nd_euler_2", 4, 0, 0, 0, 2, 0),
     "nd_heun_3d": ("nd_heun_3", 4, 0, 1, 0, 3, 0),
+    "lk_bg_heun": ("lk_bg_heun_3", 3, 0, 1, 0, 3, 0),
+    "lk_ba_euler_com": ("lk_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
 }
+
+
+def make_links(x, seed, n_links):
+    """Protrusion-like links: cells joined to a random cell within 1.6, plus
+    duplicates and self links (a == b, skipped by the reference)."""
+    rng = np.random.default_rng(seed)
+    from scipy.spatial import cKDTree
+
+    t = cKDTree(x)
+    out = []
+    while len(out) < n_links:
+        a = int(rng.integers(len(x)))
+        near = [b for b in t.query_ball_point(x[a], 1.6) if b != a]
+        if near:
+            out.append((a, int(rng.choice(near))))
+    out += [out[0], out[1], (5, 5), (len(x) - 1, len(x) - 1)]
+    return np.array(out, np.uint32)
 
 
 def main_cpp_points():
@@ -116,6 +135,13 @@ def inputs(name):
     elif name == "nd_euler_2d":
         x = np.ascontiguousarray(wl.ball(120, 14)[:, :2])
         mn, mx, steps, dt = (-20, -20, 0), (20, 20, 0), 4, 0.02
+    elif name in ("lk_bg_heun", "lk_ba_euler_com"):
+        x = wl.ball(2000, 16)
+        mn, mx = wl.bounds_for(x)
+        prm[15] = 0.2  # link strength
+        steps, dt = (10, 0.05) if name == "lk_bg_heun" else (20, 0.05)
+        if name == "lk_ba_euler_com":
+            prm[13] = 2100
     elif name == "nd_heun_3d":
         x = wl.ball(48, 15)
         mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
@@ -129,6 +155,7 @@ def inputs(name):
 def run(name):
     scen, *_rest, dims, pol = SCENARIOS[name]
     x, p0, prm, steps, dt = inputs(name)
+    links = make_links(x, 17, 400) if scen.startswith("lk_") else None
     with tempfile.TemporaryDirectory() as td:
         inp = Path(td) / "in.bin"
         with open(inp, "wb") as f:
@@ -137,14 +164,18 @@ def run(name):
             x.tofile(f)
             if p0 is not None:
                 p0.astype(np.float32).tofile(f)
+            if links is not None:
+                np.array([len(links)], np.uint32).tofile(f)
+                links.tofile(f)
         out = Path(td) / "out"
         subprocess.run([str(DRIVER), scen, str(inp), str(out), str(steps), repr(dt)], check=True)
-        res = {
-            "x0": x, "prm": prm, "steps": np.int64(steps), "dt": np.float64(dt),
-            "pairs": np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2),
-            "dpos": np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims),
-            "pos": np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims),
-        }
+        res = {"x0": x, "prm": prm, "steps": np.int64(steps), "dt": np.float64(dt),
+               "pos": np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims)}
+        if links is not None:
+            res["links"] = links
+        else:
+            res["pairs"] = np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2)
+            res["dpos"] = np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims)
         if p0 is not None:
             res["p0"] = p0
             res["dpol"] = np.fromfile(f"{out}.dpol", np.float32).reshape(-1, 2)
@@ -161,7 +192,9 @@ def main():
     manifest = {}
     for name in names:
         r = run(name)
-        manifest[name] = {"scenario": SCENARIOS[name][0], "cells": int(len(r["x0"])), "pairs": int(len(r["pairs"])),
+        manifest[name] = {"scenario": SCENARIOS[name][0], "cells": int(len(r["x0"])),
+                          "pairs": int(len(r["pairs"])) if "pairs" in r else None,
+                          "links": int(len(r["links"])) if "links" in r else None,
                           "steps": int(r["steps"]), "dt": float(r["dt"])}
         print(name, manifest[name])
     old = {}

@@ -36,7 +36,11 @@ KIND = {
     "nd_euler_2d": (4, 0, 0, 0, 2, 0),
     "nd_euler_2d_points11": (4, 0, 0, 0, 2, 0),
     "nd_heun_3d": (4, 0, 1, 0, 3, 0),
+    "lk_bg_heun": (3, 0, 1, 0, 3, 0),
+    "lk_ba_euler_com": (1, 0, 0, 1, 3, 0),
 }
+# fixtures of the link-force scenarios hold the final state only
+LINKED = sorted(k for k in KIND if k.startswith("lk_"))
 
 
 def load(name):
@@ -55,6 +59,8 @@ def make_oracle(name, g):
                       r_rep=float(prm[9]), k_adh=float(prm[10]), r_adh=float(prm[11]), k_pol=float(prm[12]),
                       has_polarity=bool(pol), capacity=cap)
     o.set_state(g["x0"], g.get("p0"))
+    if "links" in g:
+        o.set_links(g["links"], float(prm[15]))
     return o
 
 
@@ -64,7 +70,7 @@ def test_manifest_covers_every_fixture():
         assert (GOLDEN / f"{name}.npz").exists()
 
 
-@pytest.mark.parametrize("name", sorted(KIND))
+@pytest.mark.parametrize("name", sorted(set(KIND) - set(LINKED)))
 def test_pairs_and_deltas_match_reference(name):
     g = load(name)
     o = make_oracle(name, g)
@@ -114,3 +120,11 @@ def test_delaunay_applies_a_pair_once_per_empty_simplex():
     # in 2-D an edge borders at most two triangles of points in general position
     u, c = np.unique(load("nd_euler_2d")["pairs"], axis=0, return_counts=True)
     assert c.max() <= 2
+
+
+def test_link_fixtures_include_skipped_and_repeated_links():
+    # the reference skips links with a == b and applies repeated links each time
+    for name in LINKED:
+        lk = load(name)["links"]
+        assert (lk[:, 0] == lk[:, 1]).any()
+        assert len(np.unique(lk, axis=0)) < len(lk)
