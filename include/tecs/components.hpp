@@ -115,6 +115,7 @@ namespace forces {
 // (include/forces/predefined.hpp:60-144).
 struct Spring2R {
   float k_rep = 2.0f, r_rep = 0.7f, k_adh = 0.5f, r_adh = 0.8f;
+  static constexpr bool is_link = false;
   static constexpr int force_id = TECS_FORCE_SPRING2R;
   static constexpr bool needs_polarity = false;
   float k_pol_value() const { return 0.0f; }
@@ -125,6 +126,7 @@ struct Spring2R {
 // (include/types/polarity.hpp:131-198).
 struct PolaritySpring {
   float k_rep = 2.0f, r_rep = 0.7f, k_adh = 0.5f, r_adh = 0.8f, k_pol = 0.2f;
+  static constexpr bool is_link = false;
   static constexpr int force_id = TECS_FORCE_POLARITY;
   static constexpr bool needs_polarity = true;
   float k_pol_value() const { return k_pol; }
@@ -133,11 +135,28 @@ struct PolaritySpring {
 // Pairs found, no deltas: the neighbour-counting use of main.cpp.
 struct NoForce {
   float k_rep = 0.0f, r_rep = 0.0f, k_adh = 0.0f, r_adh = 0.0f;
+  static constexpr bool is_link = false;
   static constexpr int force_id = TECS_FORCE_NONE;
   static constexpr bool needs_polarity = false;
   float k_pol_value() const { return 0.0f; }
 };
+// The link law of the reference's protrusion examples
+// (examples/intercalation.cpp:65-71): along every link (a, b), cell a gets
+// strength * (x_b - x_a) / |x_b - x_a| and cell b its negative, after the
+// pairwise forces and in link order.
+struct LinkPull {
+  float strength = 0.0f;
+  static constexpr bool is_link = true;
+};
 }  // namespace forces
+
+// A connection between two agents (include/types/link.hpp).
+struct Link {
+  static constexpr unsigned int dimensions = 2;
+  unsigned int a = 0;
+  unsigned int b = 0;
+};
+static_assert(sizeof(Link) == 8, "links upload as (a, b) pairs");
 
 namespace io {
 // The reference's no-op writer (include/io/dummy.hpp).

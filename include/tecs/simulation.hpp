@@ -123,6 +123,9 @@ class Simulation {
     // extension: device-side cell division after every step
     DivisionSettings division = {};
     int device = 0;
+    /// Allocate space for links between agents (0 = no links), and how many are active.
+    unsigned int link_capacity = 0;
+    unsigned int link_active_count = 0;
   };
 
   // legacy positional constructor (include/simulation.hpp:110-126)
@@ -157,6 +160,8 @@ class Simulation {
     }
     host_valid_ = true;  // zero-initialised, as Kokkos views are
     host_dirty_ = true;
+    links_ = View<Link>("links", s.link_capacity);
+    links_.set_active_count(s.link_active_count);
   }
 
   Simulation(const Simulation&) = delete;
@@ -180,6 +185,16 @@ class Simulation {
   }
   View<Vector>& get_positions_view() { return get_view<FIELD(Vector, position)>(); }
 
+  // The links (include/simulation.hpp:317-332): a host view of link_capacity
+  // entries, the first get_active_count() in use; written links reach the
+  // device with the next step that passes a link law.
+  View<Link>& get_links() {
+    links_dirty_ = true;
+    return links_;
+  }
+  const View<Link>& get_links() const { return links_; }
+  unsigned get_link_count() const { return links_.get_active_count(); }
+
   unsigned get_capacity() const { return capacity; }
   unsigned get_agent_count() const {
     if (!host_valid_) {
@@ -201,23 +216,20 @@ class Simulation {
   }
 
   // -- stepping ---------------------------------------------------------------
-  // take_step(dt, force): one integrator step with the given built-in law
-  template <typename Force>
-  void take_step(double dt, const Force& force) {
-    static_assert(!Force::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
-    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
-                             force.k_pol_value()));
-    upload_if_dirty();
-    check(tecs_sim_step(handle_, dt, 1));
-    host_valid_ = false;
-    ++current_step;
-    last_dt = dt;
+  // take_step(dt, forces...): one integrator step with at most one built-in
+  // pairwise law and at most one link law, in any order (the reference fuses
+  // forces by kind and evaluates pairwise before link forces)
+  template <typename... Forces>
+  void take_step(double dt, const Forces&... forces) {
+    take_steps(dt, 1, forces...);
   }
   // n steps queued at once (one graph replay each)
-  template <typename Force>
-  void take_steps(double dt, int n, const Force& force) {
-    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
-                             force.k_pol_value()));
+  template <typename... Forces>
+  void take_steps(double dt, int n, const Forces&... forces) {
+    static_assert((0 + ... + (Forces::is_link ? 0 : 1)) <= 1, "one pairwise law per step");
+    static_assert((0 + ... + (Forces::is_link ? 1 : 0)) <= 1, "one link law per step");
+    apply_pair_law(forces...);
+    apply_link_law(forces...);
     upload_if_dirty();
     check(tecs_sim_step(handle_, dt, n));
     host_valid_ = false;
@@ -229,8 +241,8 @@ class Simulation {
   // per-cell deltas and the directed (self, other) pairs found.
   template <typename Force>
   std::vector<std::pair<unsigned, unsigned>> evaluate(const Force& force, std::vector<Vector>* deltas = nullptr) {
-    check(tecs_sim_set_force(handle_, Force::force_id, force.k_rep, force.r_rep, force.k_adh, force.r_adh,
-                             force.k_pol_value()));
+    apply_pair_law(force);
+    apply_link_law(force);
     upload_if_dirty();
     const unsigned n = get_agent_count();
     std::vector<Vector> dx(n ? n : 1);
@@ -302,6 +314,46 @@ class Simulation {
     return s;
   }
 
+  // the pairwise law of this step (none: pairs only, no deltas)
+  template <typename... Forces>
+  void apply_pair_law(const Forces&... forces) {
+    int id = TECS_FORCE_NONE;
+    float k[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    auto one = [&](const auto& f) {
+      using F = std::decay_t<decltype(f)>;
+      if constexpr (!F::is_link) {
+        static_assert(!F::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
+        id = F::force_id;
+        k[0] = f.k_rep; k[1] = f.r_rep; k[2] = f.k_adh; k[3] = f.r_adh; k[4] = f.k_pol_value();
+      }
+    };
+    (one(forces), ...);
+    check(tecs_sim_set_force(handle_, id, k[0], k[1], k[2], k[3], k[4]));
+  }
+
+  // the link law of this step: links act only in steps that pass one
+  template <typename... Forces>
+  void apply_link_law(const Forces&... forces) {
+    bool has = false;
+    float strength = 0.f;
+    auto one = [&](const auto& f) {
+      using F = std::decay_t<decltype(f)>;
+      if constexpr (F::is_link) {
+        has = true;
+        strength = f.strength;
+      }
+    };
+    (one(forces), ...);
+    const unsigned want = has ? links_.get_active_count() : 0u;
+    if (!links_dirty_ && want == links_on_device_ && (!has || strength == link_strength_)) return;
+    if (want > links_.extent(0)) throw Error("link active count exceeds link_capacity");
+    check(tecs_sim_set_links(handle_, want ? reinterpret_cast<const uint32_t*>(links_.data()) : nullptr, want,
+                             strength));
+    links_on_device_ = want;
+    link_strength_ = strength;
+    links_dirty_ = false;
+  }
+
   template <typename PFS>
   static void apply_finder_settings(tecs_sim_desc& d, const PFS& p) {
     if constexpr (requires { p.gabriel_coefficient; }) d.gabriel_coefficient = p.gabriel_coefficient;
@@ -348,6 +400,10 @@ class Simulation {
   tecs_sim* handle_ = nullptr;
   View<Vector> positions_;
   View<Polarity> polarity_;
+  View<Link> links_;
+  bool links_dirty_ = false;        // the host links may differ from the device's
+  unsigned links_on_device_ = 0;    // links active in the library
+  float link_strength_ = 0.f;
   bool host_valid_ = false;  // the host mirror holds the device state
   bool host_dirty_ = false;  // the host mirror may differ from the device state
 };

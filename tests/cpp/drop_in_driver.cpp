@@ -12,6 +12,9 @@
 //         k_rep, r_rep, k_adh, r_adh, k_pol, capacity, bin_size_scale, spare
 // outputs: <out>.pairs (uint32 directed pairs), <out>.dpos (deltas of one
 //          full-step pass), <out>.pos / <out>.pol (state after the steps).
+// Link scenarios ("lk_*") read, after the polarity block, uint32 n_links and
+// uint32 links[2*n_links], take the link strength from params[15], step with
+// take_step(dt, link_law, pairwise_law) and write <out>.pos only.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -39,6 +42,11 @@ CREATE_SIMULATION_CONFIG(EpithelialSheet,
                          CONFIG_INTEGRATOR(integrators::Heun)
                          CONFIG_FIELDS((Vector, position), (Polarity, polarity)))
 
+CREATE_SIMULATION_CONFIG(BinnedAllPairsEulerCom,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
+                         CONFIG_INTEGRATOR(integrators::Euler)
+                         CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
+
 struct PlainDelaunay2D : public DefaultSimulationConfig {
   CONFIG_PAIR_FINDER(pair_finders::NaiveDelaunay)
   CONFIG_INTEGRATOR(integrators::Euler)
@@ -50,9 +58,10 @@ struct Input {
   unsigned n = 0, dims = 0, has_pol = 0;
   float prm[16] = {};
   std::vector<float> x, p;
+  std::vector<unsigned> links;
 };
 
-static Input read_input(const char* path) {
+static Input read_input(const char* path, bool with_links) {
   Input in;
   FILE* f = std::fopen(path, "rb");
   if (!f) { std::perror(path); std::exit(2); }
@@ -65,6 +74,12 @@ static Input read_input(const char* path) {
   if (in.has_pol) {
     in.p.resize(std::size_t(in.n) * 2);
     if (in.n && std::fread(in.p.data(), 4, in.p.size(), f) != in.p.size()) std::exit(2);
+  }
+  if (with_links) {
+    unsigned nl = 0;
+    if (std::fread(&nl, 4, 1, f) != 1) std::exit(2);
+    in.links.resize(std::size_t(nl) * 2);
+    if (nl && std::fread(in.links.data(), 4, in.links.size(), f) != in.links.size()) std::exit(2);
   }
   std::fclose(f);
   return in;
@@ -123,13 +138,43 @@ static int run(const Input& in, const std::string& out, int steps, double dt, co
   return 0;
 }
 
+// the reference's protrusion programs: links written through get_links(),
+// stepped with a link law and a pairwise law
+template <typename Config>
+static int run_links(const Input& in, const std::string& out, int steps, double dt) {
+  using Sim = Simulation<Config>;
+  constexpr int D = Sim::dimensions;
+  typename Sim::Settings settings(in.n, "unused");
+  settings.cutoff_distance = in.prm[0];
+  settings.capacity = unsigned(in.prm[13]) > in.n ? unsigned(in.prm[13]) : in.n;
+  const unsigned nl = unsigned(in.links.size() / 2);
+  settings.link_capacity = nl;
+  settings.link_active_count = nl;
+  for (int d = 0; d < D; ++d) {
+    settings.pair_finder_settings.min_bounds[d] = in.prm[2 + d];
+    settings.pair_finder_settings.max_bounds[d] = in.prm[5 + d];
+  }
+  Sim sim(settings);
+  auto& positions = sim.get_positions_view();
+  for (unsigned i = 0; i < in.n; ++i)
+    for (int d = 0; d < D; ++d) positions(i)[d] = in.x[std::size_t(i) * D + d];
+  auto& links = sim.get_links();
+  for (unsigned l = 0; l < nl; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+  const forces::Spring2R spring{in.prm[8], in.prm[9], in.prm[10], in.prm[11]};
+  const forces::LinkPull protrusions{in.prm[15]};
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, protrusions, spring);
+  const auto& final_positions = sim.get_positions_view();
+  write_raw(out + ".pos", final_positions.data(), std::size_t(sim.get_agent_count()) * sizeof(typename Sim::Vector));
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
     return 2;
   }
   const std::string sc = argv[1];
-  const Input in = read_input(argv[2]);
+  const Input in = read_input(argv[2], sc.rfind("lk_", 0) == 0);
   const std::string out = argv[3];
   const int steps = std::atoi(argv[4]);
   const double dt = std::atof(argv[5]);
@@ -141,6 +186,8 @@ int main(int argc, char** argv) {
     if (sc == "bg_heun_com") return run<BinnedGabrielHeunCom>(in, out, steps, dt, spring);
     if (sc == "bg_heun_pol") return run<EpithelialSheet>(in, out, steps, dt, polar);
     if (sc == "nd_euler_2d") return run<PlainDelaunay2D>(in, out, steps, dt, spring);
+    if (sc == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
+    if (sc == "lk_ba_euler_com") return run_links<BinnedAllPairsEulerCom>(in, out, steps, dt);
   } catch (const tecs::Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());
     return 1;

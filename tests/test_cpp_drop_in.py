@@ -71,6 +71,9 @@ def write_input(path, g):
         x0.astype(np.float32).tofile(f)
         if p0 is not None:
             p0.astype(np.float32).tofile(f)
+        if "links" in g:
+            np.array([len(g["links"])], np.uint32).tofile(f)
+            g["links"].astype(np.uint32).tofile(f)
 
 
 def run_driver(driver, scenario, name, tmp_path):
@@ -132,3 +135,16 @@ def test_drop_in_program_reproduces_reference(driver, tmp_path, scenario, name, 
     if "pol" in g:
         pol = np.fromfile(f"{out}.pol", np.float32).reshape(-1, 2)
         assert close(pol, g["pol"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,exact", [("lk_bg_heun", True), ("lk_ba_euler_com", False)])
+def test_drop_in_links_reproduce_reference(driver, tmp_path, name, exact):
+    """get_links() + take_step(dt, forces::LinkPull, forces::Spring2R) against the reference's link runs."""
+    g, out, r = run_driver(driver, name, name, tmp_path)
+    assert r.returncode == 0, r.stderr
+    pos = np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3)
+    if exact:
+        np.testing.assert_array_equal(pos, g["pos"])
+    else:
+        assert close(pos, g["pos"])
