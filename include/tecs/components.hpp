@@ -15,6 +15,8 @@
 #ifndef TECS_CXX_COMPONENTS_HPP
 #define TECS_CXX_COMPONENTS_HPP
 
+#include <string>
+
 #include "../tecs_gpu.h"
 #include "vector.hpp"
 
@@ -163,6 +165,12 @@ namespace io {
 template <typename... Ts>
 struct Dummy {
   static constexpr bool writes = false;
+  struct Settings {};
+  Dummy(const std::string&, const Settings& = {}) {}
+  template <typename... A>
+  void write(A&&...) {}
+  template <typename... A>
+  void write_static(A&&...) {}
 };
 }  // namespace io
 

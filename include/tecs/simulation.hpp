@@ -25,6 +25,7 @@
 #include "../tecs_gpu.h"
 #include "components.hpp"
 #include "config.hpp"
+#include "hdf5_writer.hpp"
 #include "vector.hpp"
 
 namespace tecs {
@@ -120,6 +121,7 @@ class Simulation {
     Scalar cutoff_distance = Scalar(1'000'000);
     std::uint64_t seed = 2807;
     typename PairFinder::Settings pair_finder_settings = {};
+    typename Writer::Settings writer_settings = {};
     // extension: device-side cell division after every step
     DivisionSettings division = {};
     int device = 0;
@@ -133,7 +135,8 @@ class Simulation {
              const typename PairFinder::Settings& pair_finder_settings = {}, std::uint64_t seed = 2807)
       : Simulation(make_settings(agent_count, output_path, cutoff_distance, pair_finder_settings, seed)) {}
 
-  explicit Simulation(const Settings& s) : agent_count(s.agent_count), capacity(s.capacity), settings_(s) {
+  explicit Simulation(const Settings& s)
+      : agent_count(s.agent_count), capacity(s.capacity), settings_(s), writer_(s.output_path, s.writer_settings) {
     if (s.capacity < s.agent_count) throw Error("capacity must be >= agent_count");
     tecs_sim_desc d{};
     check(tecs_sim_desc_default(&d));
@@ -233,7 +236,6 @@ class Simulation {
     upload_if_dirty();
     check(tecs_sim_step(handle_, dt, n));
     host_valid_ = false;
-    current_step += static_cast<unsigned>(n);
     last_dt = dt;
   }
 
@@ -293,9 +295,25 @@ class Simulation {
     host_dirty_ = true;
   }
 
-  // The writer of the config: io::Dummy writes nothing.
-  template <typename... Extra>
-  void write(double /*time*/, Extra&&...) {}
+  // -- output (include/simulation.hpp:600-667) --------------------------------
+  // One snapshot of every field, the given extra views and the links, in
+  // group "t<current_step>"; current_step counts the writes.  The config's
+  // writer decides the format (io::HDF5_Writer: "<output_path>.h5";
+  // io::Dummy: nothing).
+  void write(double time) { write_all(time); }
+  template <typename T0, typename... Ts>
+  void write(double time, const View<T0>& extra0, const View<Ts>&... extra) {
+    write_all(time, extra0, extra...);
+  }
+  void write() { write(last_dt * current_step); }
+  template <typename T0, typename... Ts>
+  void write(const View<T0>& extra0, const View<Ts>&... extra) {
+    write(last_dt * current_step, extra0, extra...);
+  }
+  template <typename... Ts>
+  void write_static(const View<Ts>&... views) {
+    writer_.write_static(views...);
+  }
 
   tecs_sim* handle() const { return handle_; }
 
@@ -377,6 +395,14 @@ class Simulation {
     }
   }
 
+  template <typename... Ts>
+  void write_all(double time, const View<Ts>&... extra) {
+    refresh_host();
+    const unsigned step = current_step++;
+    if constexpr (has_polarity) writer_.write(time, step, positions_, polarity_, extra..., links_);
+    else writer_.write(time, step, positions_, extra..., links_);
+  }
+
   void refresh_host() {
     if (host_valid_) return;
     unsigned n = 0;
@@ -397,6 +423,7 @@ class Simulation {
   }
 
   Settings settings_;
+  Writer writer_;
   tecs_sim* handle_ = nullptr;
   View<Vector> positions_;
   View<Polarity> polarity_;

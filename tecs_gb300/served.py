@@ -254,6 +254,29 @@ def summarize(results: List[Result], makespan: float, cell_steps: int):
     }
 
 
+def plain_sample(requests: List[wl.Request], every: int = 10, dt: float = 0.05):
+    """The plain drop-in (one tecs_gb300.Simulation per request, one request
+    after another, state set up outside the timing) on every `every`-th
+    request of the stream; returns cell-steps/s and the sample's size."""
+    import torch
+
+    sample = requests[::every]
+    cs, t = 0, 0.0
+    for r in sample:
+        x, p, d, settings, force = request_sim(r)
+        s = tg.Simulation(settings, pair_finder="binned_gabriel", integrator=r.integrator, force=force,
+                          polarity=p is not None)
+        s.set_state(x, p)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.take_step(dt, r.steps)
+        s.synchronize()
+        t += time.perf_counter() - t0
+        cs += len(x) * r.steps
+        s.close()
+    return cs / t, len(sample), cs
+
+
 def bench_main(args):
     """bench.py --workload served: the served stream on one GPU."""
     import torch
@@ -275,6 +298,7 @@ def bench_main(args):
     written = srv.writer.written
     srv.close()
     sink.close()
+    plain_v, plain_n, plain_cs = plain_sample(reqs)
     line = {
         "metric": "cell-steps/s, served stream (continuous batching)", "value": summ["cell_steps_per_s"],
         "unit": "cell-steps/s", "n_gpus": 1, "steps": srv.steps, "warmup": 0,
@@ -284,6 +308,9 @@ def bench_main(args):
                                "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
                                "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins},
         "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"]},
+        "plain_sequential": {"value": plain_v, "requests": plain_n, "cell_steps": plain_cs,
+                             "note": "every 10th request run alone through the plain path, one after another"},
+        "speedup_vs_plain": summ["cell_steps_per_s"] / plain_v,
         "snapshots_written": written, "makespan_s": srv.makespan,
     }
     print(json.dumps(line), flush=True)

@@ -42,6 +42,11 @@ CREATE_SIMULATION_CONFIG(EpithelialSheet,
                          CONFIG_INTEGRATOR(integrators::Heun)
                          CONFIG_FIELDS((Vector, position), (Polarity, polarity)))
 
+CREATE_SIMULATION_CONFIG(BinnedGabrielHeunH5,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun)
+                         CONFIG_WRITER(io::HDF5_Writer))
+
 CREATE_SIMULATION_CONFIG(BinnedAllPairsEulerCom,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
                          CONFIG_INTEGRATOR(integrators::Euler)
@@ -168,6 +173,29 @@ static int run_links(const Input& in, const std::string& out, int steps, double 
   return 0;
 }
 
+// the reference's example loop: write(0), then take_step + write each step,
+// into "<out>.h5"
+static int run_written(const Input& in, const std::string& out, int steps, double dt) {
+  using Sim = Simulation<BinnedGabrielHeunH5>;
+  Sim::Settings settings(in.n, out);
+  settings.cutoff_distance = in.prm[0];
+  for (int d = 0; d < 3; ++d) {
+    settings.pair_finder_settings.min_bounds[d] = in.prm[2 + d];
+    settings.pair_finder_settings.max_bounds[d] = in.prm[5 + d];
+  }
+  Sim sim(settings);
+  auto& positions = sim.get_positions_view();
+  for (unsigned i = 0; i < in.n; ++i)
+    for (int d = 0; d < 3; ++d) positions(i)[d] = in.x[std::size_t(i) * 3 + d];
+  sim.write(0.0);
+  const forces::Spring2R spring{in.prm[8], in.prm[9], in.prm[10], in.prm[11]};
+  for (int s = 1; s <= steps; ++s) {
+    sim.take_step(dt, spring);
+    sim.write(s * dt);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
@@ -187,6 +215,7 @@ int main(int argc, char** argv) {
     if (sc == "bg_heun_pol") return run<EpithelialSheet>(in, out, steps, dt, polar);
     if (sc == "nd_euler_2d") return run<PlainDelaunay2D>(in, out, steps, dt, spring);
     if (sc == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
+    if (sc == "bg_heun_h5") return run_written(in, out, steps, dt);
     if (sc == "lk_ba_euler_com") return run_links<BinnedAllPairsEulerCom>(in, out, steps, dt);
   } catch (const tecs::Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());

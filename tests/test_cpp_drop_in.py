@@ -62,6 +62,37 @@ def test_value_types_known_answers(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_hdf5_writer_matches_python_writer(tmp_path):
+    """io::HDF5_Writer writes the same bytes as tecs_gb300.h5.H5Writer, and the reader reads them."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    import numpy as np
+    from tecs_gb300 import h5
+
+    src = Path(__file__).resolve().parent / "cpp" / "h5_writer.cpp"
+    exe = tmp_path / "h5_writer"
+    r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe), str(tmp_path / "cxx")]).returncode == 0
+    pos0 = np.array([[0.5 * i, -1.0 * i, 2.0 + i] for i in range(5)], np.float32)
+    links = np.array([[l, 4 - l] for l in range(3)], np.uint32)
+    pos1 = np.array([[1.0 + i, 0.25 * i, -0.5 * i] for i in range(7)], np.float32)
+    pol1 = np.array([[np.float32(0.1) * np.float32(i), np.float32(-0.2) * np.float32(i)] for i in range(7)],
+                    np.float32)
+    w = h5.H5Writer(tmp_path / "py.h5")
+    w.write_group("t0", {"position": pos0, "links": links})
+    w.write_group("t1", {"position": pos1, "polarity": pol1})
+    w.write_group("static", {"cell_type": np.array([[0], [1], [0], [1]], np.float32)})
+    w.close()
+    assert (tmp_path / "cxx.h5").read_bytes() == (tmp_path / "py.h5").read_bytes()
+    f = h5.H5File(tmp_path / "cxx.h5")
+    assert sorted(f.keys()) == ["static", "t0", "t1"]
+    np.testing.assert_array_equal(f.read("t0/position"), pos0)
+    np.testing.assert_array_equal(f.read("t0/links"), links)
+    np.testing.assert_array_equal(f.read("t1/polarity"), pol1)
+
+
 def write_input(path, g):
     x0 = g["x0"]
     p0 = g.get("p0")
@@ -148,3 +179,17 @@ def test_drop_in_links_reproduce_reference(driver, tmp_path, name, exact):
         np.testing.assert_array_equal(pos, g["pos"])
     else:
         assert close(pos, g["pos"])
+
+
+@pytest.mark.gpu
+def test_drop_in_program_writes_hdf5_snapshots(driver, tmp_path):
+    """CONFIG_WRITER(io::HDF5_Writer): write(0), then take_step + write per step; the groups hold the trajectory."""
+    from tecs_gb300 import h5
+
+    g, out, r = run_driver(driver, "bg_heun_h5", "bg_heun", tmp_path)
+    assert r.returncode == 0, r.stderr
+    f = h5.H5File(f"{out}.h5")
+    steps = int(g["steps"])
+    assert sorted(f.keys(), key=lambda k: int(k[1:])) == [f"t{k}" for k in range(steps + 1)]
+    np.testing.assert_array_equal(f.read("t0/position"), g["x0"])
+    np.testing.assert_array_equal(f.read(f"t{steps}/position"), g["pos"])

@@ -334,3 +334,22 @@ def test_delaunay_rejects_symmetric_and_large_capacity():
         make_pair(x, finder="naive_delaunay", symmetric=True)
     with pytest.raises(tg.TecsError, match="4096"):
         make_pair(x, finder="naive_delaunay", capacity=5000)
+
+
+def test_delaunay_edge_cases():
+    # two cells: no third point, no simplex, no pair; collinear 2-D points:
+    # every circumcircle is degenerate (|den| <= eps), so no pair either
+    for x in (np.array([[0, 0, 0], [0.5, 0, 0]], np.float32),
+              np.array([[0, 0], [0.3, 0], [0.6, 0], [0.9, 0]], np.float32)):
+        dims = x.shape[1]
+        g, c = make_pair(x, finder="naive_delaunay", dims=dims, integrator="euler", bounds=((-5,) * 3, (5,) * 3))
+        dg, _, pg = g.evaluate()
+        dc, _, pc = c.evaluate()
+        assert len(pg) == len(pc) == 0
+        np.testing.assert_array_equal(dg, dc)
+    # a square's four cocircular corners: whether the fourth corner counts as
+    # inside a circumcircle (<= r^2) is decided by rounding, and the directed
+    # pair list comes out asymmetric; the CUDA path must round as the oracle does
+    x = np.array([[0, 0], [0.7, 0], [0.7, 0.7], [0, 0.7]], np.float32)
+    g, c = make_pair(x, finder="naive_delaunay", dims=2, integrator="euler", bounds=((-5,) * 3, (5,) * 3))
+    np.testing.assert_array_equal(tg.canonical_pairs(g.evaluate()[2]), tg.canonical_pairs(c.evaluate()[2]))
