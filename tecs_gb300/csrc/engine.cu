@@ -561,6 +561,7 @@ int enqueue_engine_step(tecs_engine* e, float dt) {
   const unsigned len = e->gNB + 1;
   const unsigned chunks = cdiv(len, kScanChunk);
   k_ecount<<<gb, 256, 0, e->stream>>>(e->A, e->Asim, e->ctr, e->table, e->key, e->rank, e->cnt);
+  ECK(cudaMemsetAsync(e->part + chunks, 0, (scan_part_words(len) - chunks) * 4, e->stream));
   k_scan_reduce<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part);
   k_scan_apply<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part, e->off);
   k_escatter<<<gb, 256, 0, e->stream>>>(e->ctr, e->key, e->rank, e->off, e->src);
@@ -637,7 +638,7 @@ int tecs_engine_create(const tecs_engine_desc* desc, tecs_engine** out) {
        al((void**)&e->Bsim, C * 4) && al((void**)&e->Bid, C * 4) && al((void**)&e->key, C * 4) &&
        al((void**)&e->rank, C * 4) && al((void**)&e->src, C * 4) &&
        al((void**)&e->cnt, ((size_t)e->NB + 1) * 4) && al((void**)&e->off, ((size_t)e->NB + 1) * 4) &&
-       al((void**)&e->part, (size_t)cdiv((size_t)e->NB + 1, kScanChunk) * 4) && al((void**)&e->range, 64) &&
+       al((void**)&e->part, scan_part_words((size_t)e->NB + 1) * 4) && al((void**)&e->range, 64) &&
        al((void**)&e->ctr, sizeof(Counters)) && al((void**)&e->table, sizeof(SimSlot) * e->S) &&
        al((void**)&e->stage, C * 12) && al((void**)&e->stagep, C * 8);
   ok = ok && cudaMallocHost((void**)&e->htable, sizeof(SimSlot) * e->S) == cudaSuccess &&

@@ -111,6 +111,15 @@ static __global__ void k_count(const float4* __restrict__ A, const Counters* __r
 constexpr int kScanThreads = 256;
 constexpr int kScanPer = 16;
 constexpr int kScanChunk = kScanThreads * kScanPer;
+// The bin scan keeps one partial sum per chunk of kScanChunk bins and, after
+// those, one sum per kScanSuper chunks, so a chunk's prefix adds up at most
+// len / (kScanChunk * kScanSuper) super sums and kScanSuper - 1 chunk sums:
+// linear in the bin count (a server's bin space reaches billions of bins).
+constexpr unsigned kScanSuper = 4096;
+constexpr size_t scan_part_words(size_t len) {
+  const size_t chunks = (len + kScanChunk - 1) / kScanChunk;
+  return chunks + (chunks + kScanSuper - 1) / kScanSuper;
+}
 
 __device__ __forceinline__ unsigned block_sum(unsigned v, unsigned* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -139,7 +148,11 @@ static __global__ void k_scan_reduce(const unsigned* __restrict__ cnt, unsigned 
     if (idx < len) v += cnt[idx];
   }
   unsigned t = block_sum(v, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = t;
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = t;
+    // the super sums follow the chunk partials and are zeroed before this kernel
+    atomicAdd(&part[gridDim.x + blockIdx.x / kScanSuper], t);
+  }
 }
 
 // Exclusive scan of cnt into off, zeroing cnt for the next step.  Each warp
@@ -151,7 +164,9 @@ static __global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, co
   __shared__ unsigned sh[32];
   __shared__ unsigned wtot[kScanThreads / 32];
   unsigned pre = 0;
-  for (unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += part[b];
+  const unsigned s0 = blockIdx.x / kScanSuper;
+  for (unsigned j = threadIdx.x; j < s0; j += blockDim.x) pre += part[gridDim.x + j];
+  for (unsigned b = s0 * kScanSuper + threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += part[b];
   pre = block_sum(pre, sh);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kPerWarp = kScanChunk / (kScanThreads / 32);

@@ -248,6 +248,7 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
       K += 1;
     }
     PROF_BEGIN(s);
+    CK(cudaMemsetAsync(s->part + chunks, 0, (scan_part_words(len) - chunks) * 4, s->stream));
     k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
     PROF_END(s, "k_scan_reduce");
     PROF_BEGIN(s);
@@ -513,7 +514,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   if (s->binned) {
     const size_t len = (size_t)g.nbins + 1;
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
-         alloc((void**)&s->part, (size_t)ceil_div(len, kScanChunk) * 4);
+         alloc((void**)&s->part, scan_part_words(len) * 4);
   }
   // COM accumulators: 3 per reduction slot, two slots (Heun's two passes)
   const size_t pass_blocks = std::max<size_t>(ceil_div(cap, 128), 2);
@@ -895,7 +896,7 @@ constexpr size_t kOffCnt = align_up(kOffBid + (size_t)kNoallocMaxCells * 4);
 constexpr size_t kOffOff = align_up(kOffCnt + ((size_t)kNoallocMaxBins + 1) * 4);
 constexpr size_t kOffPart = align_up(kOffOff + ((size_t)kNoallocMaxBins + 1) * 4);
 constexpr size_t kNoallocScratchBytes =
-    align_up(kOffPart + ((size_t)kNoallocMaxBins + 1 + kScanChunk - 1) / kScanChunk * 4);
+    align_up(kOffPart + scan_part_words((size_t)kNoallocMaxBins + 1) * 4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 

@@ -257,12 +257,12 @@ def summarize(results: List[Result], makespan: float, cell_steps: int):
 def plain_sample(requests: List[wl.Request], every: int = 10, dt: float = 0.05):
     """The plain drop-in (one tecs_gb300.Simulation per request, one request
     after another, state set up outside the timing) on every `every`-th
-    request of the stream; returns cell-steps/s and the sample's size."""
+    request of the stream.  Returns cell-steps/s, the sample's (cells, steps,
+    seconds) rows."""
     import torch
 
-    sample = requests[::every]
-    cs, t = 0, 0.0
-    for r in sample:
+    rows = []
+    for r in requests[::every]:
         x, p, d, settings, force = request_sim(r)
         s = tg.Simulation(settings, pair_finder="binned_gabriel", integrator=r.integrator, force=force,
                           polarity=p is not None)
@@ -271,10 +271,31 @@ def plain_sample(requests: List[wl.Request], every: int = 10, dt: float = 0.05):
         t0 = time.perf_counter()
         s.take_step(dt, r.steps)
         s.synchronize()
-        t += time.perf_counter() - t0
-        cs += len(x) * r.steps
+        rows.append((len(x), r.steps, time.perf_counter() - t0))
         s.close()
-    return cs / t, len(sample), cs
+    cs = sum(n * k for n, k, _ in rows)
+    return cs / sum(t for _, _, t in rows), rows
+
+
+def plain_fcfs_latency(requests: List[wl.Request], rows, time_scale: float = 1.0):
+    """Time to completion of the same arrivals served by the plain path one
+    request at a time, first come first served.  A request's run time is
+    steps * (a + b * cells) (+ c per request), least-squares fitted to the
+    measured sample rows."""
+    A = np.array([[k, k * n, 1.0] for n, k, _ in rows])
+    y = np.array([t for _, _, t in rows])
+    coef, *_ = np.linalg.lstsq(A, y, rcond=None)
+    coef = np.maximum(coef, 0.0)
+    free_at, lat = 0.0, []
+    for r in sorted(requests, key=lambda r: r.arrival_s):
+        n = r.n
+        t = coef[0] * r.steps + coef[1] * r.steps * n + coef[2]
+        start = max(free_at, r.arrival_s / time_scale)
+        free_at = start + t
+        lat.append(free_at - r.arrival_s / time_scale)
+    lat = np.array(lat)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "makespan_s": float(free_at), "model_s_per_step": [float(c) for c in coef]}
 
 
 def bench_main(args):
@@ -298,7 +319,13 @@ def bench_main(args):
     written = srv.writer.written
     srv.close()
     sink.close()
-    plain_v, plain_n, plain_cs = plain_sample(reqs)
+    plain_v, rows = plain_sample(reqs)
+    plain_lat = plain_fcfs_latency(reqs, rows, args.time_scale)
+    # capacity: the same stream with arrivals compressed 100 times (compute-bound)
+    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, sink=None)
+    cap_res = cap_srv.run(reqs, time_scale=100.0)
+    cap = summarize(cap_res, cap_srv.makespan, cap_srv.cell_steps)
+    cap_srv.close()
     line = {
         "metric": "cell-steps/s, served stream (continuous batching)", "value": summ["cell_steps_per_s"],
         "unit": "cell-steps/s", "n_gpus": 1, "steps": srv.steps, "warmup": 0,
@@ -308,9 +335,14 @@ def bench_main(args):
                                "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
                                "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins},
         "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"]},
-        "plain_sequential": {"value": plain_v, "requests": plain_n, "cell_steps": plain_cs,
-                             "note": "every 10th request run alone through the plain path, one after another"},
-        "speedup_vs_plain": summ["cell_steps_per_s"] / plain_v,
+        "capacity": {"value": cap["cell_steps_per_s"], "makespan_s": cap["makespan_s"],
+                     "note": "the same requests with arrivals compressed x100 (no snapshots): compute-bound"},
+        "plain_sequential": {"value": plain_v, "requests": len(rows),
+                             "fcfs_latency_model": plain_lat,
+                             "note": "every 10th request run alone through the plain path, one after another; "
+                                     "fcfs_latency_model = the same arrivals served one at a time by the plain "
+                                     "path, run times fitted to the sample"},
+        "capacity_vs_plain": cap["cell_steps_per_s"] / plain_v,
         "snapshots_written": written, "makespan_s": srv.makespan,
     }
     print(json.dumps(line), flush=True)

@@ -353,3 +353,18 @@ def test_delaunay_edge_cases():
     x = np.array([[0, 0], [0.7, 0], [0.7, 0.7], [0, 0.7]], np.float32)
     g, c = make_pair(x, finder="naive_delaunay", dims=2, integrator="euler", bounds=((-5,) * 3, (5,) * 3))
     np.testing.assert_array_equal(tg.canonical_pairs(g.evaluate()[2]), tg.canonical_pairs(c.evaluate()[2]))
+
+
+def test_huge_sparse_grid_scan():
+    # a +-300 grid (216M bins, ~53k scan chunks in 13 super-chunk sums) around a
+    # small ball: the bin scan must stay exact where the chunk partials are
+    # summed in two levels
+    x = ball(3000, seed=31)
+    g, c = make_pair(x, finder="binned_gabriel", bounds=((-300,) * 3, (300,) * 3))
+    dg, _, pg = g.evaluate()
+    dc, _, pc = c.evaluate()
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
+    np.testing.assert_array_equal(dg, dc)
+    g.take_step(0.05, 2)
+    c.step(0.05, 2)
+    np.testing.assert_array_equal(g.get_state()[0], c.get_state()[0])
