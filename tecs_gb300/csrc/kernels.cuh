@@ -846,19 +846,21 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 }
 
 // ---------------------------------------------------------------------------
-// Block-cooperative Gabriel pass (spring laws).
+// Block-cooperative Gabriel pass (spring laws and the 3-D polarity law).
 //
 // Same pair semantics as gabriel_cell_fast, reorganised so that the lanes stay
 // busy: (1) each thread collects its cell's in-cutoff neighbours into shared
-// memory; (2) the block lists every (cell, neighbour) pair and the threads
-// take pairs round-robin for the Gabriel test; (3) the same for the pair
-// forces, each written over its candidate slot; (4) each thread adds its
-// cell's accepted contributions in candidate order -- the reference's
-// summation order, so the sums stay bit-identical.  Cells with more than
-// kMaxNb neighbours, or whose witness ball leaves the 3x3x3 bin block, take
-// the general path in phase 4.
-// candidate slot (q, cell c) in shared memory, XOR-swizzled so that threads
-// reading different q of the same cell hit different banks
+// memory, in candidate order; (2) the block lists every (cell, neighbour)
+// pair -- pairs of cells with similar neighbour counts together, so a warp's
+// Gabriel loops run similar lengths -- and the threads take pairs
+// round-robin for the Gabriel test, setting accept bits per cell; (3) the same
+// for the pair forces, each written over its candidate slot; (4) each thread
+// adds its cell's accepted contributions in candidate order -- the
+// reference's summation order, so the sums stay bit-identical.  Cells with
+// more neighbours than the slots, or whose witness ball leaves the 3x3x3 bin
+// block, take the general path in phase 4.
+// Candidate slot (q, cell c) in shared memory, XOR-swizzled so that threads
+// reading different q of the same cell hit different banks.
 __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c ^ q); }
 
 template <int D, int FORCE>
