@@ -561,8 +561,11 @@ int enqueue_engine_step(tecs_engine* e, float dt) {
   const unsigned len = e->gNB + 1;
   const unsigned chunks = cdiv(len, kScanChunk);
   k_ecount<<<gb, 256, 0, e->stream>>>(e->A, e->Asim, e->ctr, e->table, e->key, e->rank, e->cnt);
-  ECK(cudaMemsetAsync(e->part + chunks, 0, (scan_part_words(len) - chunks) * 4, e->stream));
-  k_scan_reduce<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part);
+  if (chunks > 1) {  // one chunk: its prefix needs no partial sums
+    ECK(cudaMemsetAsync(e->part + chunks, 0, (scan_part_words(len) - chunks) * 4, e->stream));
+    k_scan_reduce<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part);
+  }
+  e->kernels = chunks > 1 ? 7 : 6;
   k_scan_apply<<<chunks, kScanThreads, 0, e->stream>>>(e->cnt, len, e->part, e->off);
   k_escatter<<<gb, 256, 0, e->stream>>>(e->ctr, e->key, e->rank, e->off, e->src);
   k_eorder_gather<<<gb, 256, 0, e->stream>>>(e->off, e->gNB, e->key, e->src, e->A, e->PA, e->Asim, e->B, e->PB,

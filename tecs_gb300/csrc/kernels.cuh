@@ -863,9 +863,13 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 // reading different q of the same cell hit different banks.
 __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c ^ q); }
 
-template <int D, int FORCE>
+// FINDER 3: binned Gabriel; FINDER 1: binned all-pairs (i's bin by
+// multiplication, binned_all_pairs.hpp:103-109, and every in-cutoff pair
+// accepted: no phase 2).
+template <int D, int FORCE, int FINDER = 3>
 static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
   static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
+  static_assert(FINDER == 1 || FINDER == 3, "the binned finders");
   constexpr bool POL = FORCE == 2;
   // neighbour slots per cell; the polarity law's extra per-pair float only
   // fits in the static shared memory with 12 (cells with more in-cutoff
@@ -903,7 +907,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     vi = __ldg(&a.X[i]);
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
-    bin_coords_div<D>(g, xi, bc);
+    if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
+    else bin_coords_div<D>(g, xi, bc);
     constexpr int kRows = D >= 3 ? 9 : 3;
     unsigned rlo[kRows], rhi[kRows], rb0[kRows];
     const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
@@ -992,7 +997,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       if (lane >= o) incl += y;
     }
     if (lane == 31) wpk[warp] = incl;
-    amask[t] = 0u;
+    amask[t] = FINDER == 1 ? (1u << cnt) - 1u : 0u;  // cnt <= 16
     __syncthreads();
     int tot[3] = {0, 0, 0}, before = 0;
 #pragma unroll
@@ -1014,7 +1019,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   // blocks (i, j) when it is inside the ball (|x_k - m|^2 < r^2) and its bin
   // lies in the ball's bin range; the range (sqrt + floors) is only worked out
   // for the rare k that pass the distance test.
-  for (int p = t; p < P; p += kPassThreads) {
+  for (int p = t; p < (FINDER == 3 ? P : 0); p += kPassThreads) {
     const unsigned info = pinfo[p];
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const float4 h = home[c];
@@ -1102,7 +1107,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
   if (active) {
     if (fallback[t]) {
-      cell_general<D, 3, FORCE>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc);
+      cell_general<D, FINDER, FORCE>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc);
     } else {
       for (int q = 0; q < cnt; ++q) {
         if (!((amask[t] >> q) & 1u)) continue;

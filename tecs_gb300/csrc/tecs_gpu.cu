@@ -169,9 +169,9 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
   // the block-cooperative Gabriel pass needs the fast-path geometry and packs
   // bin coordinates in 10 bits and slots in 27 bits
-  const bool coop = s->d.gabriel_coefficient <= 0.9f && s->g.R == 1 && s->g.bin_size >= s->d.cutoff &&
-                    s->g.ext[0] <= 1024 && s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 &&
-                    s->d.capacity < (1u << 27) && s->use_coop;
+  const bool coop_geom = s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
+                         s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27) && s->use_coop;
+  const bool coop = coop_geom && s->d.gabriel_coefficient <= 0.9f;
 #define PICK(DD, FF)                                                            \
   if (D == DD && F == FF) {                                                     \
     if (sym) {                                                                  \
@@ -182,6 +182,9 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
       if (FF == 3 && coop && FO == 0) return k_pass_gabriel<DD, 0>;             \
       if (FF == 3 && coop && FO == 1) return k_pass_gabriel<DD, 1>;             \
       if (FF == 3 && coop && FO == 2 && DD == 3) return k_pass_gabriel<3, 2>;   \
+      if (FF == 1 && coop_geom && FO == 0) return k_pass_gabriel<DD, 0, 1>;     \
+      if (FF == 1 && coop_geom && FO == 1) return k_pass_gabriel<DD, 1, 1>;     \
+      if (FF == 1 && coop_geom && FO == 2 && DD == 3) return k_pass_gabriel<3, 2, 1>; \
       if (FO == 0) return k_pass<DD, FF, 0>;                                    \
       if (FO == 1) return k_pass<DD, FF, 1>;                                    \
       if (DD == 3) return k_pass<DD, FF, 2>;                                    \
@@ -247,10 +250,14 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
       PROF_END(s, "k_count");
       K += 1;
     }
-    PROF_BEGIN(s);
-    CK(cudaMemsetAsync(s->part + chunks, 0, (scan_part_words(len) - chunks) * 4, s->stream));
-    k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
-    PROF_END(s, "k_scan_reduce");
+    // one chunk: its prefix needs no partial sums
+    if (chunks > 1) {
+      PROF_BEGIN(s);
+      CK(cudaMemsetAsync(s->part + chunks, 0, (scan_part_words(len) - chunks) * 4, s->stream));
+      k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
+      PROF_END(s, "k_scan_reduce");
+      K += 1;
+    }
     PROF_BEGIN(s);
     k_scan_apply<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part, s->off);
     PROF_END(s, "k_scan_apply");
@@ -261,7 +268,7 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid,
                                               s->n_links ? s->slot_of : nullptr);
     PROF_END(s, "k_order_gather");
-    K += 4;
+    K += 3;
   } else {
     PROF_BEGIN(s);
     k_id_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, PA, s->B, PB);
