@@ -229,6 +229,21 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def aggregate_over_ranks(total_s: float, cell_steps: float, device):
+    """Job totals over the replicas: the slowest rank's time and the summed
+    cell-steps (one process per GPU, no data-path collective)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return total_s, float(cell_steps)
+    t = torch.tensor([total_s], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(cell_steps)], device=device, dtype=torch.float64)
+    dist.all_reduce(c)
+    return float(t.item()), float(c.item())
+
+
 def traffic_per_pass(workload: str):
     """DRAM bytes per cell of one force-pass launch, from the committed ncu capture of this workload."""
     p = ROOT / "profiles" / "traffic.json"
@@ -339,6 +354,8 @@ def run_gb300(args):
         step_ms, cell_steps = timed_steps(args.steps, False)
         clocks.stop()
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     # per-kernel CUDA events (event nodes inside the step graph) on a second,
     # shorter run: the kernel table, the shares and the roofline's launch times
     sim.set_profiling(True)
@@ -346,16 +363,7 @@ def run_gb300(args):
     prof_ms, prof_cells = timed_steps(min(args.steps, 100), True)
     sim.set_profiling(False)
     torch.cuda.synchronize()
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-        c = torch.tensor([cell_steps], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(c)
-        cell_steps_all = float(c.item())
-    else:
-        cell_steps_all = float(cell_steps)
+    total_s, cell_steps_all = aggregate_over_ranks(sum(step_ms) / 1e3, cell_steps, "cuda")
     torch.cuda.synchronize()
     value = cell_steps_all / total_s
     kpl = sim.kernels_per_step()
