@@ -10,7 +10,11 @@
 // object headers, symbol-table groups (version 1 B-tree, symbol table nodes,
 // local heaps), contiguous datasets with dataspace v1, datatype v1, fill
 // value v2 and layout v3 messages -- with the same byte layout as
-// tecs_gb300/h5.py's writer.  No XDMF sidecar is written.
+// tecs_gb300/h5.py's writer.  With Settings::write_xmf (the default) it also
+// writes the reference's XDMF sidecar "<path>.xmf" (hdf5_writer.hpp:134-287)
+// for visualisation tools: one temporal collection, a uniform grid per write
+// with the first view as geometry, the other views as node attributes (links
+// as polyline topology) and the static group in every grid.
 #ifndef TECS_CXX_HDF5_WRITER_HPP
 #define TECS_CXX_HDF5_WRITER_HPP
 
@@ -19,6 +23,7 @@
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -372,31 +377,106 @@ template <typename SimulationConfig>
 class HDF5_Writer {
  public:
   static constexpr bool writes = true;
+  // field names as the reference's (the second keeps its spelling)
   struct Settings {
-    bool write_xmf = false;  // no XDMF sidecar is written
+    bool write_xmf = true;
+    std::size_t buffer_treshold = 65536;  // XDMF text kept before writing it out
   };
 
-  HDF5_Writer(const std::string& path, const Settings& = {}) {
+  HDF5_Writer(const std::string& path, const Settings& settings = {})
+      : xmf_threshold_(settings.buffer_treshold), filename_(std::filesystem::path(path).filename().string()) {
     const std::filesystem::path p(path + ".h5");
     if (p.has_parent_path()) std::filesystem::create_directories(p.parent_path());
     file_ = std::make_unique<h5detail::File>(p.string());
+    if (settings.write_xmf) {
+      xmf_.open(path + ".xmf", std::ios::out | std::ios::trunc);
+      xmf_buf_ = "<?xml version=\"1.0\"?>\n<Xdmf Version=\"3.0\">\n\t<Domain>\n"
+                 "\t\t<Grid Name=\"Agents\" GridType=\"Collection\" CollectionType=\"Temporal\">\n";
+    }
+  }
+  HDF5_Writer(const HDF5_Writer&) = delete;
+  HDF5_Writer& operator=(const HDF5_Writer&) = delete;
+  ~HDF5_Writer() {
+    if (!xmf_.is_open()) return;
+    xmf_buf_ += "\t\t</Grid>\n\t</Domain>\n</Xdmf>\n";
+    xmf_.write(xmf_buf_.data(), static_cast<std::streamsize>(xmf_buf_.size()));
+    xmf_.close();
   }
 
   // one group "t<step>" with one dataset per non-empty view (hdf5_writer.hpp:306-321)
   template <typename T0, typename... Ts>
-  void write(double /*time*/, unsigned step, const View<T0>& first, const View<Ts>&... rest) {
-    write_group("t" + std::to_string(step), first, rest...);
+  void write(double time, unsigned step, const View<T0>& first, const View<Ts>&... rest) {
+    const std::string group = "t" + std::to_string(step);
+    write_group(group, first, rest...);
+    if (!xmf_.is_open()) return;
+    // with active links the grid's topology is the links' polylines, else the cells as vertices
+    bool links = false;
+    auto is_link = [&](const auto& v) {
+      using T = typename std::decay_t<decltype(v)>::value_type;
+      if constexpr (std::is_same_v<T, Link>) links = links || v.get_active_count() != 0;
+    };
+    (is_link(rest), ...);
+    xmf_grid_open(time, group, first, links);
+    (xmf_item(xmf_buf_, group, rest), ...);
+    xmf_buf_ += xmf_static_;
+    xmf_buf_ += "\t\t\t</Grid>\n";
+    if (xmf_buf_.size() > xmf_threshold_) {
+      xmf_.write(xmf_buf_.data(), static_cast<std::streamsize>(xmf_buf_.size()));
+      xmf_buf_.clear();
+    }
   }
 
-  // the "static" group, once (hdf5_writer.hpp:335-347)
+  // the "static" group, once (hdf5_writer.hpp:335-347); in every later XDMF grid
   template <typename... Ts>
   void write_static(const View<Ts>&... views) {
     if (static_written_) throw std::runtime_error("Static data has already been written. You can only write to static data once.");
     static_written_ = true;
     write_group("static", views...);
+    if (xmf_.is_open()) (xmf_item(xmf_static_, "static", views), ...);
   }
 
  private:
+  template <typename T>
+  static std::string active_rows(const View<T>& v) {
+    return std::to_string(v.get_active_count());
+  }
+
+  template <typename T>
+  void xmf_grid_open(double time, const std::string& group, const View<T>& geometry, bool links) {
+    constexpr int D = SimulationConfig::dimensions;
+    std::string& b = xmf_buf_;
+    b += "\t\t\t<Grid Name=\"" + group + "\" GridType=\"Uniform\">\n\t\t\t\t<Time Value=\"";
+    b += std::to_string(time);
+    if (!links) b += "\"/>\n\t\t\t\t<Topology TopologyType=\"Polyvertex\" NumberOfElements=\"" + active_rows(geometry);
+    b += "\"/>\n\t\t\t\t<Geometry GeometryType=\"";
+    b += D == 1 ? "X" : (D == 2 ? "XY" : "XYZ");
+    b += "\">\n\t\t\t\t\t<DataItem Format=\"HDF\" Dimensions=\"" + active_rows(geometry) + " " + std::to_string(D);
+    b += "\">\n\t\t\t\t\t\t" + filename_ + ".h5:" + group + "/" + geometry.label();
+    b += "\n\t\t\t\t\t</DataItem>\n\t\t\t\t</Geometry>\n";
+  }
+
+  // a node attribute, or the links' polyline topology (hdf5_writer.hpp:210-262)
+  template <typename T>
+  void xmf_item(std::string& b, const std::string& group, const View<T>& v) const {
+    if (v.extent(0) == 0) return;
+    std::string dims = active_rows(v) + " ";
+    int cols = 0;
+    if constexpr (requires { T::dimensions; }) cols = int(T::dimensions);
+    else if constexpr (requires { T::components; }) cols = int(T::components);
+    if (cols) dims += std::to_string(cols) + " ";
+    const char* type = !cols ? "Scalar" : (cols == 2 || cols == 3) ? "Vector" : cols == 9 ? "Tensor" : "Matrix";
+    if constexpr (std::is_same_v<T, Link>) {
+      b += "\t\t\t\t<Topology TopologyType=\"Polyline\" NumberOfElements=\"" + active_rows(v) + "\">\n";
+      b += "\t\t\t\t\t<DataItem Format=\"HDF\" DataType=\"UInt32\"";
+    } else {
+      b += "\t\t\t\t<Attribute Name=\"" + v.label() + "\" AttributeType=\"" + type + "\" Center=\"Node\">\n";
+      b += "\t\t\t\t\t<DataItem Format=\"HDF\"";
+    }
+    b += " Dimensions=\"" + dims + "\">\n\t\t\t\t\t\t" + filename_ + ".h5:" + group + "/" + v.label();
+    b += "\n\t\t\t\t\t</DataItem>\n";
+    b += std::is_same_v<T, Link> ? "\t\t\t\t</Topology>\n" : "\t\t\t\t</Attribute>\n";
+  }
+
   template <typename... Ts>
   void write_group(const std::string& group, const View<Ts>&... views) {
     std::vector<h5detail::Dataset> ds;
@@ -410,7 +490,11 @@ class HDF5_Writer {
     file_->write_group(group, ds);
   }
 
+  std::size_t xmf_threshold_;
+  std::string filename_;
   std::unique_ptr<h5detail::File> file_;
+  std::ofstream xmf_;
+  std::string xmf_buf_, xmf_static_;
   bool static_written_ = false;
 };
 

@@ -19,6 +19,7 @@ template <typename Scalar, int dimensions>
 struct VectorN {
   static_assert(dimensions >= 1 && dimensions <= 4, "VectorN holds 1 to 4 components");
   using value_type = Scalar;
+  static constexpr int components = dimensions;
 
   Scalar data_[dimensions] = {};
 

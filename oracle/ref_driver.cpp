@@ -47,6 +47,7 @@
 #include <integrators/heun.hpp>
 #include <com_fixers/com_fixers.hpp>
 #include <io/dummy.hpp>
+#include <io/hdf5_writer.hpp>
 
 struct Input {
   unsigned n = 0, dims = 0, has_pol = 0;
@@ -265,6 +266,44 @@ static int tecs_driver_run_links(const Input& in, const std::string& out, int st
   return 0;
 }
 
+// The reference's writer on a stepped simulation: write_static, write(0), then
+// take_step + write(); its XDMF sidecar <out>.xmf is the output (the HDF5
+// calls go to the HighFive stand-in and write nothing).
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields>
+static int tecs_driver_run_writer(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() { return PAIRWISE_FORCE(TECS_DRIVER_SPRING)(); };
+  typename Simulation<Config>::Settings st(n, out);
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  const unsigned nl = (unsigned)(in.links.size() / 2);
+  st.link_capacity = nl;
+  st.link_active_count = nl;
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+  auto& pol = sim.template get_view<FIELD(Polarity_<Scalar>, polarity)>();
+  for (unsigned i = 0; i < n; ++i) { pol(i)[0] = in.p[2 * i]; pol(i)[1] = in.p[2 * i + 1]; }
+  auto& links = sim.get_links();
+  for (unsigned l = 0; l < nl; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+  View<float> cell_type("cell_type", n);
+  for (unsigned i = 0; i < n; ++i) cell_type(i) = (float)(i % 3);
+  sim.write_static(cell_type);
+  sim.write(0.0);
+  auto force = make_force();
+  for (int s = 0; s < steps; ++s) {
+    sim.take_step(dt, force);
+    sim.write();
+  }
+  return 0;
+}
+
 #define TECS_LINK_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                           \
   namespace NAME {                                                                                      \
   CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
@@ -295,6 +334,14 @@ TECS_SCENARIO(bg_heun_2, pair_finders::BinnedGabriel, integrators::Heun, com_fix
 TECS_SCENARIO(nd_euler_2, pair_finders::NaiveDelaunay, integrators::Euler, com_fixers::NoComFixer, 2, 0)
 TECS_SCENARIO(nd_heun_3, pair_finders::NaiveDelaunay, integrators::Heun, com_fixers::NoComFixer, 3, 0)
 TECS_LINK_SCENARIO(lk_bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer)
+namespace lk_writer_3 {
+CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel) CONFIG_INTEGRATOR(integrators::Heun)
+                                     CONFIG_WRITER(tecs::io::HDF5_Writer) TECS_FIELDS_1)
+EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)
+static int run(const Input& in, const std::string& out, int steps, double dt) {
+  return tecs_driver_run_writer<Config, Scalar, Vector, Random, PairwiseForceFields>(in, out, steps, dt);
+}
+}  // namespace lk_writer_3
 TECS_LINK_SCENARIO(lk_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::GlobalComFixer)
 
 int main(int argc, char** argv) {
@@ -314,7 +361,7 @@ int main(int argc, char** argv) {
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2) DISPATCH(nd_euler_2) DISPATCH(nd_heun_3)
-  DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3)
+  DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3) DISPATCH(lk_writer_3)
 #undef DISPATCH
   if (rc == 3) std::fprintf(stderr, "unknown scenario %s\n", sc.c_str());
   return rc;

@@ -14,7 +14,8 @@
 //          full-step pass), <out>.pos / <out>.pol (state after the steps).
 // Link scenarios ("lk_*") read, after the polarity block, uint32 n_links and
 // uint32 links[2*n_links], take the link strength from params[15], step with
-// take_step(dt, link_law, pairwise_law) and write <out>.pos only.
+// take_step(dt, link_law, pairwise_law) and write <out>.pos only; "lk_writer"
+// writes <out>.h5 and <out>.xmf through CONFIG_WRITER(io::HDF5_Writer).
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -51,6 +52,12 @@ CREATE_SIMULATION_CONFIG(BinnedAllPairsEulerCom,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
                          CONFIG_INTEGRATOR(integrators::Euler)
                          CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
+
+CREATE_SIMULATION_CONFIG(EpithelialSheetH5,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun)
+                         CONFIG_WRITER(io::HDF5_Writer)
+                         CONFIG_FIELDS((Vector, position), (Polarity, polarity)))
 
 struct PlainDelaunay2D : public DefaultSimulationConfig {
   CONFIG_PAIR_FINDER(pair_finders::NaiveDelaunay)
@@ -196,6 +203,40 @@ static int run_written(const Input& in, const std::string& out, int steps, doubl
   return 0;
 }
 
+// positions, polarity and links written with a static cell-type view:
+// write_static, write(0), then take_step + write() each step, into
+// "<out>.h5" and its XDMF sidecar "<out>.xmf"
+static int run_written_links(const Input& in, const std::string& out, int steps, double dt) {
+  using Sim = Simulation<EpithelialSheetH5>;
+  Sim::Settings settings(in.n, out);
+  settings.cutoff_distance = in.prm[0];
+  const unsigned nl = unsigned(in.links.size() / 2);
+  settings.link_capacity = nl;
+  settings.link_active_count = nl;
+  for (int d = 0; d < 3; ++d) {
+    settings.pair_finder_settings.min_bounds[d] = in.prm[2 + d];
+    settings.pair_finder_settings.max_bounds[d] = in.prm[5 + d];
+  }
+  Sim sim(settings);
+  auto& positions = sim.get_positions_view();
+  for (unsigned i = 0; i < in.n; ++i)
+    for (int d = 0; d < 3; ++d) positions(i)[d] = in.x[std::size_t(i) * 3 + d];
+  auto& polarity = sim.get_view<FIELD(Polarity_<float>, polarity)>();
+  for (unsigned i = 0; i < in.n; ++i) polarity(i) = Polarity_<float>(in.p[2 * i], in.p[2 * i + 1]);
+  auto& links = sim.get_links();
+  for (unsigned l = 0; l < nl; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+  View<float> cell_type("cell_type", in.n);
+  for (unsigned i = 0; i < in.n; ++i) cell_type(i) = float(i % 3);
+  sim.write_static(cell_type);
+  sim.write(0.0);
+  const forces::Spring2R spring{in.prm[8], in.prm[9], in.prm[10], in.prm[11]};
+  for (int s = 0; s < steps; ++s) {
+    sim.take_step(dt, spring);
+    sim.write();
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
@@ -217,6 +258,7 @@ int main(int argc, char** argv) {
     if (sc == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
     if (sc == "bg_heun_h5") return run_written(in, out, steps, dt);
     if (sc == "lk_ba_euler_com") return run_links<BinnedAllPairsEulerCom>(in, out, steps, dt);
+    if (sc == "lk_writer") return run_written_links(in, out, steps, dt);
   } catch (const tecs::Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());
     return 1;

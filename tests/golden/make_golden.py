@@ -56,6 +56,10 @@ SCENARIOS = {
     "nd_heun_3d": ("nd_heun_3", 4, 0, 1, 0, 3, 0),
     "lk_bg_heun": ("lk_bg_heun_3", 3, 0, 1, 0, 3, 0),
     "lk_ba_euler_com": ("lk_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
+    # the reference's HDF5_Writer on a stepped run: its XDMF sidecar (lk_writer.xmf)
+    "lk_writer": ("lk_writer_3", 3, 0, 1, 0, 3, 1),
+    # the same without links: the grids' topology is then the cells as vertices
+    "lk_writer_nolinks": ("lk_writer_3", 3, 0, 1, 0, 3, 1),
 }
 
 
@@ -142,6 +146,11 @@ def inputs(name):
         steps, dt = (10, 0.05) if name == "lk_bg_heun" else (20, 0.05)
         if name == "lk_ba_euler_com":
             prm[13] = 2100
+    elif name in ("lk_writer", "lk_writer_nolinks"):
+        x = wl.sheet(60 if name == "lk_writer" else 45, 18)
+        p0 = wl.outward_polarity(x, 18)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 2, 0.05
     elif name == "nd_heun_3d":
         x = wl.ball(48, 15)
         mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
@@ -155,7 +164,12 @@ def inputs(name):
 def run(name):
     scen, *_rest, dims, pol = SCENARIOS[name]
     x, p0, prm, steps, dt = inputs(name)
-    links = make_links(x, 17, 400) if scen.startswith("lk_") else None
+    if name == "lk_writer_nolinks":
+        links = np.zeros((0, 2), np.uint32)
+    elif scen.startswith("lk_"):
+        links = make_links(x, 17, 30 if name == "lk_writer" else 400)
+    else:
+        links = None
     with tempfile.TemporaryDirectory() as td:
         inp = Path(td) / "in.bin"
         with open(inp, "wb") as f:
@@ -169,6 +183,11 @@ def run(name):
                 links.tofile(f)
         out = Path(td) / "out"
         subprocess.run([str(DRIVER), scen, str(inp), str(out), str(steps), repr(dt)], check=True)
+        if scen == "lk_writer_3":
+            (HERE / f"{name}.xmf").write_bytes(Path(f"{out}.xmf").read_bytes())
+            res = {"x0": x, "p0": p0, "prm": prm, "steps": np.int64(steps), "dt": np.float64(dt), "links": links}
+            np.savez_compressed(HERE / f"{name}.npz", **res)
+            return res
         res = {"x0": x, "prm": prm, "steps": np.int64(steps), "dt": np.float64(dt),
                "pos": np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims)}
         if links is not None:

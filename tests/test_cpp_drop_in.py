@@ -93,6 +93,24 @@ def test_hdf5_writer_matches_python_writer(tmp_path):
     np.testing.assert_array_equal(f.read("t1/polarity"), pol1)
 
 
+@pytest.mark.parametrize("name", ["lk_writer", "lk_writer_nolinks"])
+def test_xdmf_sidecar_matches_reference(tmp_path, name):
+    """io::HDF5_Writer's "<path>.xmf" equals, byte for byte, the reference writer's sidecar for the
+    same write sequence: write_static(cell_type), then (position, polarity, links) at t = 0, dt, 2 dt;
+    with links the grids' topology is the links' polylines, without them the cells as vertices."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    g = dict(np.load(GOLDEN / f"{name}.npz"))
+    src = Path(__file__).resolve().parent / "cpp" / "xdmf_writer.cpp"
+    exe = tmp_path / "xdmf_writer"
+    r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    args = [str(len(g["x0"])), str(len(g["links"])), str(int(g["steps"]) + 1), repr(float(g["dt"]))]
+    assert subprocess.run([str(exe), str(tmp_path / "out"), *args]).returncode == 0
+    assert (tmp_path / "out.xmf").read_bytes() == (GOLDEN / f"{name}.xmf").read_bytes()
+
+
 def write_input(path, g):
     x0 = g["x0"]
     p0 = g.get("p0")
@@ -193,3 +211,22 @@ def test_drop_in_program_writes_hdf5_snapshots(driver, tmp_path):
     assert sorted(f.keys(), key=lambda k: int(k[1:])) == [f"t{k}" for k in range(steps + 1)]
     np.testing.assert_array_equal(f.read("t0/position"), g["x0"])
     np.testing.assert_array_equal(f.read(f"t{steps}/position"), g["pos"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["lk_writer", "lk_writer_nolinks"])
+def test_drop_in_program_writes_the_reference_xdmf(driver, tmp_path, name):
+    """A stepped program with polarity, links and a static view: its "<out>.xmf" equals the
+    reference's byte for byte, and every group it names is in "<out>.h5"."""
+    from tecs_gb300 import h5
+
+    g, out, r = run_driver(driver, "lk_writer", name, tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert Path(f"{out}.xmf").read_bytes() == (GOLDEN / f"{name}.xmf").read_bytes()
+    f = h5.H5File(f"{out}.h5")
+    steps = int(g["steps"])
+    assert sorted(f.keys()) == sorted(["static"] + [f"t{k}" for k in range(steps + 1)])
+    np.testing.assert_array_equal(f.read("t0/position"), g["x0"])
+    np.testing.assert_array_equal(f.read("static/cell_type").reshape(-1), np.arange(len(g["x0"])) % 3)
+    if len(g["links"]):
+        np.testing.assert_array_equal(f.read(f"t{steps}/links"), g["links"])

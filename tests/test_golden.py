@@ -41,6 +41,9 @@ KIND = {
 }
 # fixtures of the link-force scenarios hold the final state only
 LINKED = sorted(k for k in KIND if k.startswith("lk_"))
+# fixtures of the reference's HDF5_Writer: the inputs and the XDMF sidecar
+# (tests/test_cpp_drop_in.py compares the drop-in writer's with it)
+WRITER = ["lk_writer", "lk_writer_nolinks"]
 
 
 def load(name):
@@ -65,9 +68,11 @@ def make_oracle(name, g):
 
 
 def test_manifest_covers_every_fixture():
-    assert set(MANIFEST) == set(KIND)
-    for name in KIND:
+    assert set(MANIFEST) == set(KIND) | set(WRITER)
+    for name in list(KIND) + WRITER:
         assert (GOLDEN / f"{name}.npz").exists()
+    for name in WRITER:
+        assert (GOLDEN / f"{name}.xmf").read_bytes().startswith(b'<?xml version="1.0"?>\n<Xdmf Version="3.0">')
 
 
 @pytest.mark.parametrize("name", sorted(set(KIND) - set(LINKED)))
