@@ -677,6 +677,10 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
 // a ball's bin range leaves i's 3x3x3 block, the cell takes the general path.
 constexpr int kMaxNb = 16;
 constexpr int kPassThreads = 128;
+// Position arrays that the cooperative pass scans hold this many float4 past
+// their capacity: the candidate scan reads whole rounds past a row's end (at
+// most 31 slots) and masks the extra slots off.
+constexpr unsigned kRowPad = 64;
 
 // nb: room for MAXN neighbours at a stride of kPassThreads
 template <int D, int FORCE, int MAXN = kMaxNb>
@@ -846,15 +850,15 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 }
 
 // ---------------------------------------------------------------------------
-// Block-cooperative Gabriel pass (spring laws and the 3-D polarity law).
+// Warp-cooperative Gabriel pass (spring laws and the 3-D polarity law).
 //
 // Same pair semantics as gabriel_cell_fast, reorganised so that the lanes stay
 // busy: (1) each thread collects its cell's in-cutoff neighbours into shared
-// memory, in candidate order; (2) the block lists every (cell, neighbour)
-// pair -- pairs of cells with similar neighbour counts together, so a warp's
-// Gabriel loops run similar lengths -- and the threads take pairs
-// round-robin for the Gabriel test, setting accept bits per cell; (3) the same
-// for the pair forces, each written over its candidate slot; (4) each thread
+// memory, in candidate order; (2) each warp lists every (cell, neighbour)
+// pair of its 32 cells -- sorted by the cell's neighbour count, so the
+// Gabriel loops of a round of pairs run the same length -- and its lanes take
+// pairs round-robin for the Gabriel test, setting accept bits per cell; (3)
+// the same for the pair forces, each written over its candidate slot; (4) each thread
 // adds its cell's accepted contributions in candidate order -- the
 // reference's summation order, so the sums stay bit-identical.  Cells with
 // more neighbours than the slots, or whose witness ball leaves the 3x3x3 bin
@@ -877,8 +881,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   constexpr int NB = POL ? 12 : kMaxNb;
   __shared__ float4 cand[NB * kPassThreads];           // [q][t]: position, w = (slot << 5) | bin code
   __shared__ float4 home[kPassThreads];                // position, w = packed bin coords
-  __shared__ unsigned short pinfo[NB * kPassThreads];  // the block's pairs: (t << 4) | q
-  __shared__ unsigned wpk[kPassThreads / 32];          // per-warp pair counts, three classes packed
+  __shared__ unsigned short pinfo[NB * kPassThreads];  // each warp's pairs: (t << 4) | q
+  __shared__ unsigned short wcls[kPassThreads / 32][NB + 1];  // pairs per (warp, neighbour count)
   __shared__ unsigned amask[kPassThreads];             // accepted pairs of each cell, bit q
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
@@ -939,23 +943,31 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       if (lmax > 32u) fb = true;
       if (fb) continue;
       unsigned m[3] = {0u, 0u, 0u};
+      // whole rounds of two slots per row; a slot past its row's end reads
+      // the cells that follow (padded arrays) and is masked off below
       for (unsigned o = 0; o < lmax; o += 2u) {
         float4 v[3][2];
 #pragma unroll
         for (int q = 0; q < 3; ++q)
 #pragma unroll
-          for (int k = 0; k < 2; ++k)
-            v[q][k] = __ldg(&a.X[len[q] ? rlo[g0 + q] + min(o + k, len[q] - 1u) : i]);
+          for (int k = 0; k < 2; ++k) v[q][k] = __ldg(&a.X[rlo[g0 + q] + o + k]);
+        const unsigned bit[2] = {1u << o, 2u << o};  // o <= 30
 #pragma unroll
         for (int q = 0; q < 3; ++q)
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const unsigned j = rlo[g0 + q] + o + k;
             const float e0 = xi[0] - v[q][k].x, e1 = xi[1] - v[q][k].y;
             float d2 = e0 * e0 + e1 * e1;
             if (D >= 3) { const float e2 = xi[2] - v[q][k].z; d2 = d2 + e2 * e2; }
-            if (o + k < len[q] && j != i && d2 < fp.rc2) m[q] |= 1u << (o + k);
+            if (d2 < fp.rc2) m[q] |= bit[k];
           }
+      }
+      // the row's own slots only, and never the cell itself
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        m[q] &= len[q] >= 32u ? 0xffffffffu : (1u << len[q]) - 1u;
+        const unsigned self = i - rlo[g0 + q];
+        if (self < len[q]) m[q] &= ~(1u << self);
       }
       // append this plane's rows in order
 #pragma unroll
@@ -984,43 +996,42 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     hpol[t] = pi;
     if (cnt) htrig[t] = pol_trig(pi);
   }
-  // pair offsets: pairs grouped by their cell's neighbour count (<= 4, <= 8,
-  // more), so that the Gabriel loops of a warp's pairs run similar lengths;
-  // three 10-bit per-class sums packed in one word per scan
-  int P = 0;
+  // Phases 2-4 run per warp over the warp's own 32 cells (no block
+  // barrier).  Pair offsets: the warp's pairs sorted by their cell's
+  // neighbour count, so that the Gabriel loops of a round of pairs run the
+  // same length.  The cells of one count are ranked (match_any), the first
+  // records the class's pairs, and lane v forms class v's base.
+  const int lane = t & 31, warp = t >> 5;
+  unsigned short* const wp = pinfo + warp * 32 * NB;
+  int P = 0, P1 = 0;
   {
-    const int lane = t & 31, warp = t >> 5;
-    const int cls = cnt <= 4 ? 0 : (cnt <= 8 ? 1 : 2);
-    unsigned incl = (unsigned)cnt << (10 * cls);
+    if (lane <= NB) wcls[warp][lane] = 0;
+    __syncwarp();
+    const unsigned same = __match_any_sync(0xffffffffu, cnt);
+    const int rank = __popc(same & ((1u << lane) - 1u));
+    if (rank == 0) wcls[warp][cnt] = (unsigned short)(__popc(same) * (unsigned)cnt);
+    // a single neighbour has no witness: accepted (cnt <= 16)
+    amask[t] = FINDER == 1 ? (1u << cnt) - 1u : (cnt == 1 ? 1u : 0u);
+    __syncwarp();
+    const unsigned tot = lane <= NB ? (unsigned)wcls[warp][lane] : 0u;
+    unsigned incl = tot;
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    if (lane == 31) wpk[warp] = incl;
-    amask[t] = FINDER == 1 ? (1u << cnt) - 1u : 0u;  // cnt <= 16
-    __syncthreads();
-    int tot[3] = {0, 0, 0}, before = 0;
-#pragma unroll
-    for (int w = 0; w < kPassThreads / 32; ++w) {
-      const unsigned v = wpk[w];
-#pragma unroll
-      for (int f = 0; f < 3; ++f) tot[f] += (int)((v >> (10 * f)) & 1023u);
-      if (w < warp) before += (int)((v >> (10 * cls)) & 1023u);
-    }
-    int base = before + (int)((incl >> (10 * cls)) & 1023u) - cnt;
-    if (cls >= 1) base += tot[0];
-    if (cls >= 2) base += tot[1];
-    P = tot[0] + tot[1] + tot[2];
-    for (int q = 0; q < cnt; ++q) pinfo[base + q] = (unsigned short)((t << 4) | q);
+    P = (int)__shfl_sync(0xffffffffu, incl, NB);
+    P1 = (int)__shfl_sync(0xffffffffu, incl, 1);  // the pairs of single-neighbour cells come first
+    const int base = (int)__shfl_sync(0xffffffffu, incl - tot, cnt) + rank * cnt;
+    for (int q = 0; q < cnt; ++q) wp[base + q] = (unsigned short)((t << 4) | q);
   }
-  __syncthreads();
+  __syncwarp();
 
   // ---- phase 2: Gabriel test, one pair per thread at a time.  A witness k
   // blocks (i, j) when it is inside the ball (|x_k - m|^2 < r^2) and its bin
   // lies in the ball's bin range; the range (sqrt + floors) is only worked out
   // for the rare k that pass the distance test.
-  for (int p = t; p < (FINDER == 3 ? P : 0); p += kPassThreads) {
-    const unsigned info = pinfo[p];
+  for (int p = P1 + lane; p < (FINDER == 3 ? P : 0); p += 32) {
+    const unsigned info = wp[p];
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
@@ -1036,15 +1047,9 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     for (int d = 0; d < D; ++d) m[d] = hx[d] - disp[d] * 0.5f;
     const float rsq = d2 * fp.gab_factor;
     const int cc = ncnt[c];
-    bool blocked = false;
-    for (int w = 0; w < cc; ++w) {
-      if (w == q) continue;
-      const float4 vk = cand[cix(w, c)];
-      const float f0 = vk.x - m[0], f1 = vk.y - m[1];
-      float sd = f0 * f0 + f1 * f1;
-      if (D >= 3) { const float f2 = vk.z - m[2]; sd = sd + f2 * f2; }
-      if (!(sd < rsq)) continue;
-      // binned_gabriel.hpp:142-153: the bins overlapping the ball
+    // binned_gabriel.hpp:142-153: a witness in the ball blocks only from a
+    // bin overlapping the ball
+    auto in_ball_bins = [&](const float4& vk) {
       const unsigned hb = __float_as_uint(h.w);
       const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
       const unsigned code = __float_as_uint(vk.w) & 31u;
@@ -1057,14 +1062,30 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
         const int hi = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
         inside = inside && rel[d] >= lo && rel[d] <= hi;
       }
-      if (inside) { blocked = true; break; }
+      return inside;
+    };
+    bool blocked = false;
+    // two witnesses per round (the last round of an odd count tests one twice)
+    for (int w = 0; w < cc && !blocked; w += 2) {
+      const int w1 = min(w + 1, cc - 1);
+      const float4 vk0 = cand[cix(w, c)], vk1 = cand[cix(w1, c)];
+      const float f0 = vk0.x - m[0], f1 = vk0.y - m[1];
+      const float g0 = vk1.x - m[0], g1 = vk1.y - m[1];
+      float sd0 = f0 * f0 + f1 * f1, sd1 = g0 * g0 + g1 * g1;
+      if (D >= 3) {
+        const float f2 = vk0.z - m[2], g2 = vk1.z - m[2];
+        sd0 = sd0 + f2 * f2;
+        sd1 = sd1 + g2 * g2;
+      }
+      const bool h0 = sd0 < rsq && w != q, h1 = sd1 < rsq && w1 != q;
+      if (h0 || h1) blocked = (h0 && in_ball_bins(vk0)) || (h1 && in_ball_bins(vk1));
     }
     if (!blocked) atomicOr(&amask[c], 1u << q);
   }
-  __syncthreads();
+  __syncwarp();
   // ---- phase 3: pair forces, written over the candidate slot
-  for (int p = t; p < P; p += kPassThreads) {
-    const unsigned info = pinfo[p];
+  for (int p = lane; p < P; p += 32) {
+    const unsigned info = wp[p];
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
     if (!((amask[c] >> q) & 1u) || fallback[c]) continue;
     const float4 h = home[c];
@@ -1102,7 +1123,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     }
     cand[cix(q, c)] = f;
   }
-  __syncthreads();
+  __syncwarp();
   // ---- phase 4: ordered per-cell sums
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
   if (active) {

@@ -509,8 +509,12 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   const size_t cap = desc->capacity;
   auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
   bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
-  ok = ok && alloc((void**)&s->A, cap * 16) && alloc((void**)&s->B, cap * 16) && alloc((void**)&s->Xt, cap * 16) &&
+  // the sorted position arrays carry kRowPad zeroed float4 past the capacity
+  const size_t xcap = cap + kRowPad;
+  ok = ok && alloc((void**)&s->A, xcap * 16) && alloc((void**)&s->B, xcap * 16) && alloc((void**)&s->Xt, xcap * 16) &&
        alloc((void**)&s->d1, cap * 16) && alloc((void**)&s->d2, cap * 16);
+  ok = ok && cudaMemset(s->A, 0, xcap * 16) == cudaSuccess && cudaMemset(s->B, 0, xcap * 16) == cudaSuccess &&
+       cudaMemset(s->Xt, 0, xcap * 16) == cudaSuccess;
   if (desc->has_polarity)
     ok = ok && alloc((void**)&s->PA, cap * 8) && alloc((void**)&s->PB, cap * 8) && alloc((void**)&s->Pt, cap * 8) &&
          alloc((void**)&s->dp1, cap * 8) && alloc((void**)&s->dp2, cap * 8);
@@ -894,7 +898,7 @@ constexpr size_t align_up(size_t v) { return (v + kNoallocAlign - 1) / kNoallocA
 constexpr size_t kOffCtr = 0;
 constexpr size_t kOffA = align_up(kOffCtr + sizeof(Counters));
 constexpr size_t kOffB = align_up(kOffA + (size_t)kNoallocMaxCells * sizeof(float4));
-constexpr size_t kOffD = align_up(kOffB + (size_t)kNoallocMaxCells * sizeof(float4));
+constexpr size_t kOffD = align_up(kOffB + ((size_t)kNoallocMaxCells + kRowPad) * sizeof(float4));
 constexpr size_t kOffKey = align_up(kOffD + (size_t)kNoallocMaxCells * sizeof(float4));
 constexpr size_t kOffRank = align_up(kOffKey + (size_t)kNoallocMaxCells * 4);
 constexpr size_t kOffSrc = align_up(kOffRank + (size_t)kNoallocMaxCells * 4);
