@@ -1047,26 +1047,10 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     for (int d = 0; d < D; ++d) m[d] = hx[d] - disp[d] * 0.5f;
     const float rsq = d2 * fp.gab_factor;
     const int cc = ncnt[c];
-    // binned_gabriel.hpp:142-153: a witness in the ball blocks only from a
-    // bin overlapping the ball
-    auto in_ball_bins = [&](const float4& vk) {
-      const unsigned hb = __float_as_uint(h.w);
-      const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
-      const unsigned code = __float_as_uint(vk.w) & 31u;
-      const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
-      const float r = sqrtf(rsq);
-      bool inside = true;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const int lo = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-        const int hi = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-        inside = inside && rel[d] >= lo && rel[d] <= hi;
-      }
-      return inside;
-    };
-    bool blocked = false;
-    // two witnesses per round (the last round of an odd count tests one twice)
-    for (int w = 0; w < cc && !blocked; w += 2) {
+    // every witness, two per round and without branches: bit w of hits is a
+    // witness inside the ball (an odd count's last round tests one twice)
+    unsigned hits = 0u, bit = 1u;
+    for (int w = 0; w < cc; w += 2) {
       const int w1 = min(w + 1, cc - 1);
       const float4 vk0 = cand[cix(w, c)], vk1 = cand[cix(w1, c)];
       const float f0 = vk0.x - m[0], f1 = vk0.y - m[1];
@@ -1077,17 +1061,59 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
         sd0 = sd0 + f2 * f2;
         sd1 = sd1 + g2 * g2;
       }
-      const bool h0 = sd0 < rsq && w != q, h1 = sd1 < rsq && w1 != q;
-      if (h0 || h1) blocked = (h0 && in_ball_bins(vk0)) || (h1 && in_ball_bins(vk1));
+      if (sd0 < rsq) hits |= bit;
+      if (sd1 < rsq) hits |= bit << 1;
+      bit <<= 2;
+    }
+    hits &= ((1u << cc) - 1u) & ~(1u << q);
+    bool blocked = false;
+    if (hits) {
+      // binned_gabriel.hpp:142-153: a witness in the ball blocks only from a
+      // bin overlapping the ball, [lo, hi] per axis relative to the cell's bin
+      const unsigned hb = __float_as_uint(h.w);
+      const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
+      const float r = sqrtf(rsq);
+      int lo[3] = {-1, -1, -1}, hi[3] = {1, 1, 1};
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        lo[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+        hi[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
+      }
+      while (hits && !blocked) {
+        const int w = __ffs(hits) - 1;
+        hits &= hits - 1u;
+        const unsigned code = __float_as_uint(cand[cix(w, c)].w) & 31u;
+        const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
+        bool inside = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d) inside = inside && rel[d] >= lo[d] && rel[d] <= hi[d];
+        blocked = inside;
+      }
     }
     if (!blocked) atomicOr(&amask[c], 1u << q);
   }
   __syncwarp();
-  // ---- phase 3: pair forces, written over the candidate slot
-  for (int p = lane; p < P; p += 32) {
+  // the warp's accepted pairs, cell by cell, written over the pair list
+  // (phase 2 has finished reading it)
+  int PA = 0;
+  {
+    const unsigned acc_bits = fallback[t] ? 0u : amask[t];
+    const int na = __popc(acc_bits);
+    int incl = na;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    PA = __shfl_sync(0xffffffffu, incl, 31);
+    int base = incl - na;
+    __syncwarp();
+    for (unsigned b = acc_bits; b; b &= b - 1u) wp[base++] = (unsigned short)((t << 4) | (__ffs(b) - 1));
+  }
+  __syncwarp();
+  // ---- phase 3: forces of the accepted pairs, written over the candidate slot
+  for (int p = lane; p < PA; p += 32) {
     const unsigned info = wp[p];
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
-    if (!((amask[c] >> q) & 1u) || fallback[c]) continue;
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
     float disp[3];

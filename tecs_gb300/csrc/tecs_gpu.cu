@@ -89,6 +89,89 @@ __global__ void k_unpack2(const float4* __restrict__ idw, const unsigned* __rest
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     out[ids ? ids[s] : id_of(idw[s])] = val[s];
 }
+
+// The upload of a state in one pass: positions packed as (x, y, z, id) and
+// polarities copied -- read straight from the caller's page-locked host
+// buffers when they are mapped (on GB300 a kernel reaches host memory over
+// NVLink-C2C at the link's rate, so no staging copy is needed) -- the
+// counters reset (all but the step index, which keys the division stream),
+// and, when the first rebuild expects them, the cells counted per bin.
+__global__ void k_upload(const float* __restrict__ pos, const float2* __restrict__ pol, unsigned n, int dims,
+                         float4* __restrict__ A, float2* __restrict__ PA, Counters* __restrict__ ctr, GridP g,
+                         unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctr->n = n;
+    ctr->div_count = 0u;
+    ctr->done[0] = ctr->done[1] = 0u;
+    ctr->error = 0u;
+    ctr->done_div = 0u;
+    ctr->pair_count = 0ull;
+  }
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = make_float4(0.f, 0.f, 0.f, __uint_as_float(s));
+    v.x = pos[(size_t)s * dims];
+    if (dims >= 2) v.y = pos[(size_t)s * dims + 1];
+    if (dims >= 3) v.z = pos[(size_t)s * dims + 2];
+    A[s] = v;
+    if (pol) PA[s] = pol[s];
+    if (cnt) {
+      float p[3] = {v.x, v.y, v.z};
+      int c[3] = {0, 0, 0};
+      unsigned b;
+      if (dims == 3) { bin_coords_div<3>(g, p, c); b = flatten<3>(g, c); }
+      else { bin_coords_div<2>(g, p, c); b = flatten<2>(g, c); }
+      key[s] = b;
+      rank[s] = atomicAdd(&cnt[b], 1u);
+    }
+  }
+}
+
+// download helpers that take the agent count from the device counters, so
+// that a download needs no host round trip before its copies
+__global__ void k_unpack_dev(const float4* __restrict__ A, const Counters* __restrict__ ctr, int dims,
+                             float* __restrict__ out) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const float4 v = A[s];
+    const size_t o = (size_t)id_of(v) * dims;
+    out[o] = v.x;
+    if (dims >= 2) out[o + 1] = v.y;
+    if (dims >= 3) out[o + 2] = v.z;
+  }
+}
+__global__ void k_unpack2_dev(const float4* __restrict__ A, const Counters* __restrict__ ctr,
+                              const float2* __restrict__ val, float2* __restrict__ out) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    out[id_of(A[s])] = val[s];
+}
+// copy the first n * per floats of src to dst (a mapped host buffer), four at
+// a time when dst is 16-byte aligned
+__global__ void k_copy_out(const float* __restrict__ src, const Counters* __restrict__ ctr, unsigned per,
+                           float* __restrict__ dst) {
+  const size_t total = (size_t)ctr->n * per;
+  const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+    const size_t q = total / 4;
+    for (size_t k = t0; k < q; k += stride)
+      reinterpret_cast<float4*>(dst)[k] = reinterpret_cast<const float4*>(src)[k];
+    done = q * 4;
+  }
+  for (size_t k = done + t0; k < total; k += stride) dst[k] = src[k];
+}
+
+// The device address of a page-locked host buffer mapped into the device's
+// address space, or null for any other pointer.
+const void* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
 }  // namespace
 
 struct tecs_sim {
@@ -125,6 +208,7 @@ struct tecs_sim {
   int last_kernels = 0;
   // the next rebuild's bin count is done by the state-writing kernel
   bool fuse_count = false;
+  Counters* hctr = nullptr;  // page-locked mirror of the device counters
   // block-cooperative Gabriel pass enabled (off only for comparison runs)
   bool use_coop = true;
   // per-kernel CUDA events (external event-record nodes when captured in a graph)
@@ -529,6 +613,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   }
   // COM accumulators: 3 per reduction slot, two slots (Heun's two passes)
   const size_t pass_blocks = std::max<size_t>(ceil_div(cap, 128), 2);
+  ok = ok && cudaMallocHost((void**)&s->hctr, sizeof(Counters)) == cudaSuccess;
   ok = ok && alloc((void**)&s->ctr, sizeof(Counters)) && alloc((void**)&s->com_part, pass_blocks * 3 * 8) &&
        alloc((void**)&s->com, 8 * 4) && alloc((void**)&s->stage, cap * 4 * 4);
   if (ok && s->cnt) ok = cudaMemset(s->cnt, 0, ((size_t)g.nbins + 1) * 4) == cudaSuccess;
@@ -550,6 +635,7 @@ int tecs_sim_destroy(tecs_sim* s) {
   drop_graphs(s);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
+  if (s->hctr) cudaFreeHost(s->hctr);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
                   s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of};
@@ -560,27 +646,16 @@ int tecs_sim_destroy(tecs_sim* s) {
   return 0;
 }
 
-static int upload_common(tecs_sim* s, unsigned n) {
-  const size_t cap = s->d.capacity;
-  CK(cudaMemsetAsync(s->d1, 0, cap * 16, s->stream));
-  CK(cudaMemsetAsync(s->d2, 0, cap * 16, s->stream));
-  if (s->d.has_polarity) {
-    CK(cudaMemsetAsync(s->dp1, 0, cap * 8, s->stream));
-    CK(cudaMemsetAsync(s->dp2, 0, cap * 8, s->stream));
-  }
-  // reset every counter but the step index: the division stream is keyed by
-  // the steps taken since creation, and a new state does not restart it
-  Counters c{};
-  c.n = n;
-  static_assert(offsetof(Counters, step) + sizeof(c.step) == offsetof(Counters, pair_count), "Counters layout");
-  CK(cudaMemcpyAsync(s->ctr, &c, offsetof(Counters, step), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemsetAsync(&s->ctr->pair_count, 0, sizeof(c.pair_count), s->stream));
-  if (s->fuse_count) {
-    // the first rebuild expects the bin counts of A to be made already
-    CK(cudaMemsetAsync(s->cnt, 0, ((size_t)s->g.nbins + 1) * 4, s->stream));
-    if (n) k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
-    CK(cudaGetLastError());
-  }
+// A new state from positions (and polarities) the device can read: one
+// k_upload pass.  The delta buffers need no reset: every pass writes the
+// deltas of all active cells before they are read.
+static int upload_common(tecs_sim* s, const float* pos, const float2* pol, unsigned n) {
+  // the first rebuild expects the bin counts of A to be made already
+  if (s->fuse_count) CK(cudaMemsetAsync(s->cnt, 0, ((size_t)s->g.nbins + 1) * 4, s->stream));
+  k_upload<<<std::max(1u, ceil_div(n, 256)), 256, 0, s->stream>>>(
+      pos, s->d.has_polarity ? pol : nullptr, n, s->d.dims, s->A, s->PA, s->ctr, s->g, s->key, s->rank,
+      s->fuse_count ? s->cnt : nullptr);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s->stream));
   // the captured step graphs depend on the state only through their grid
   // size: keep them unless that changes
@@ -597,15 +672,20 @@ int tecs_sim_upload(tecs_sim* s, const float* pos, const float* pol, unsigned n)
   if (n > s->d.capacity) return fail("agent count exceeds capacity");
   if (s->d.has_polarity && n && !pol) return fail("simulation has a polarity field: polarity required");
   CK(cudaSetDevice(s->d.device));
-  CK(cudaStreamSynchronize(s->stream));
   const int D = s->d.dims;
-  if (n) {
+  // page-locked host buffers are read by k_upload itself; other host memory
+  // is copied to the device first
+  const float* src = static_cast<const float*>(mapped_host(pos));
+  const float2* psrc = static_cast<const float2*>(mapped_host(pol));
+  if (n && !src) {
     CK(cudaMemcpyAsync(s->stage, pos, (size_t)n * D * 4, cudaMemcpyHostToDevice, s->stream));
-    k_pack<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->stage, n, D, s->A);
-    CK(cudaGetLastError());
-    if (s->d.has_polarity) CK(cudaMemcpyAsync(s->PA, pol, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
+    src = s->stage;
   }
-  return upload_common(s, n);
+  if (n && s->d.has_polarity && !psrc) {
+    CK(cudaMemcpyAsync(s->Pt, pol, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
+    psrc = s->Pt;
+  }
+  return upload_common(s, src, psrc, n);
 }
 
 int tecs_sim_upload_device(tecs_sim* s, const float* dpos, const float* dpol, unsigned n) {
@@ -613,14 +693,7 @@ int tecs_sim_upload_device(tecs_sim* s, const float* dpos, const float* dpol, un
   if (n > s->d.capacity) return fail("agent count exceeds capacity");
   if (s->d.has_polarity && n && !dpol) return fail("simulation has a polarity field: polarity required");
   CK(cudaSetDevice(s->d.device));
-  CK(cudaStreamSynchronize(s->stream));
-  const int D = s->d.dims;
-  if (n) {
-    k_pack<<<ceil_div(n, 256), 256, 0, s->stream>>>(dpos, n, D, s->A);
-    CK(cudaGetLastError());
-    if (s->d.has_polarity) CK(cudaMemcpyAsync(s->PA, dpol, (size_t)n * 8, cudaMemcpyDeviceToDevice, s->stream));
-  }
-  return upload_common(s, n);
+  return upload_common(s, dpos, reinterpret_cast<const float2*>(dpol), n);
 }
 
 int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
@@ -679,16 +752,35 @@ int tecs_sim_synchronize(tecs_sim* s) {
 
 int tecs_sim_count(tecs_sim* s, unsigned* n) {
   if (!s || !n) return fail("null argument");
-  Counters c;
-  CK(cudaMemcpyAsync(&c, s->ctr, sizeof c, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(s->hctr, s->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
-  if (c.error & 1u) return fail("capacity exceeded by cell division");
-  *n = c.n;
+  if (s->hctr->error & 1u) return fail("capacity exceeded by cell division");
+  *n = s->hctr->n;
   return 0;
 }
 
 int tecs_sim_download(tecs_sim* s, float* pos, float* pol, unsigned* n_out) {
   if (!s || !pos) return fail("null argument");
+  float* dst = static_cast<float*>(const_cast<void*>(mapped_host(pos)));
+  float* pdst = (pol && s->d.has_polarity) ? static_cast<float*>(const_cast<void*>(mapped_host(pol))) : nullptr;
+  if (dst && (pdst || !(pol && s->d.has_polarity))) {
+    // page-locked host buffers: unpack in id order on the device and write
+    // them from kernels, the count taken on the device; one synchronisation
+    CK(cudaSetDevice(s->d.device));
+    const unsigned gb = std::max(1u, ceil_div((unsigned)s->d.capacity, 256));
+    const int D = s->d.dims;
+    k_unpack_dev<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, D, (float*)s->Xt);
+    k_copy_out<<<gb, 256, 0, s->stream>>>((const float*)s->Xt, s->ctr, (unsigned)D, dst);
+    if (pdst) {
+      k_unpack2_dev<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->PA, s->Pt);
+      k_copy_out<<<gb, 256, 0, s->stream>>>((const float*)s->Pt, s->ctr, 2u, pdst);
+    }
+    CK(cudaGetLastError());
+    unsigned n = 0;
+    if (tecs_sim_count(s, &n)) return -1;
+    if (n_out) *n_out = n;
+    return 0;
+  }
   unsigned n = 0;
   if (tecs_sim_count(s, &n)) return -1;
   const int D = s->d.dims;
