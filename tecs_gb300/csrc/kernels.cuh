@@ -676,7 +676,10 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
 // (binned_gabriel.hpp:142-207).  If a cell has more than kMaxNb neighbours, or
 // a ball's bin range leaves i's 3x3x3 block, the cell takes the general path.
 constexpr int kMaxNb = 16;
-constexpr int kPassThreads = 128;
+// Threads (cells) per block of the cooperative passes: three warps.  The
+// block's shared memory (about 30 KB) then lets seven blocks share an SM, 672
+// cells, so that a 100k-cell pass runs in a single wave on 152 SMs.
+constexpr int kPassThreads = 96;
 // Position arrays that the cooperative pass scans hold this many float4 past
 // their capacity: the candidate scan reads whole rounds past a row's end (at
 // most 31 slots) and masks the extra slots off.

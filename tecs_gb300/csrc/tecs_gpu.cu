@@ -368,7 +368,7 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   PassFn fn = pass_fn(s, sym);
   if (!fn) return fail("unsupported finder/force/dims combination");
   const unsigned L = launch_count(s);
-  const unsigned blocks = ceil_div(L ? L : 1, 128);
+  const unsigned blocks = ceil_div(L ? L : 1, kPassThreads);
   if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY) {
     // applications per pair on this pass's positions, then the pass
     PROF_BEGIN(s);
@@ -380,7 +380,7 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
     K += 1;
   }
   PROF_BEGIN(s);
-  fn<<<blocks, 128, 0, s->stream>>>(s->g, s->fp, a);
+  fn<<<blocks, kPassThreads, 0, s->stream>>>(s->g, s->fp, a);
   PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
               : a.mode == kHeun1Fused ? "k_pass_heun1" : "k_pass_heun2");
   K += 1;
