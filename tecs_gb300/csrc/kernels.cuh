@@ -79,6 +79,7 @@ struct PassArgs {
   unsigned* key;
   unsigned* rank;
   unsigned* cnt;
+  unsigned* part;       // scan chunk totals formed while counting (count_bin), or null
   // naive Delaunay: how many times each directed pair is applied, row i at i * capacity
   const unsigned short* dmult;
   // links of each cell id, in link order: link_ent[link_off[id] .. link_off[id + 1])
@@ -93,21 +94,6 @@ struct PassArgs {
 // ---------------------------------------------------------------------------
 // binning: key + count, exclusive scan, scatter, per-bin id sort + gather
 
-static __global__ void k_count(const float4* __restrict__ A, const Counters* __restrict__ ctr, GridP g, int dims,
-                        unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt) {
-  const unsigned n = ctr->n;
-  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    float4 v = A[s];
-    float p[3] = {v.x, v.y, v.z};
-    int c[3] = {0, 0, 0};
-    unsigned b;
-    if (dims == 3) { bin_coords_div<3>(g, p, c); b = flatten<3>(g, c); }
-    else { bin_coords_div<2>(g, p, c); b = flatten<2>(g, c); }
-    key[s] = b;
-    rank[s] = atomicAdd(&cnt[b], 1u);
-  }
-}
-
 constexpr int kScanThreads = 256;
 constexpr int kScanPer = 16;
 constexpr int kScanChunk = kScanThreads * kScanPer;
@@ -119,6 +105,56 @@ constexpr unsigned kScanSuper = 4096;
 constexpr size_t scan_part_words(size_t len) {
   const size_t chunks = (len + kScanChunk - 1) / kScanChunk;
   return chunks + (chunks + kScanSuper - 1) / kScanSuper;
+}
+
+// Count a cell into bin b and return its tentative rank.  With part set, the
+// cell is also added to its scan chunk's total -- what k_scan_reduce would
+// form from the finished counts -- with one atomic per group of lanes that
+// share the chunk (consecutive cells mostly do: they are in bin order).  The
+// super-chunk totals, needed past kScanSuper chunks only, come from
+// k_scan_super.
+static __device__ __noinline__ void add_chunk_total(unsigned* part, unsigned b) {
+  const unsigned c = b / (unsigned)kScanChunk;
+  const unsigned grp = __match_any_sync(__activemask(), c);
+  if ((threadIdx.x & 31u) == (unsigned)(__ffs(grp) - 1)) atomicAdd(&part[c], (unsigned)__popc(grp));
+}
+__device__ __forceinline__ unsigned count_bin(unsigned* cnt, unsigned* part, unsigned b) {
+  const unsigned r = atomicAdd(&cnt[b], 1u);
+  if (part) add_chunk_total(part, b);
+  return r;
+}
+
+// Super-chunk totals part[chunks + j] = sum of chunk totals j*kScanSuper ..,
+// one block per super-chunk.
+static __global__ void k_scan_super(unsigned* __restrict__ part, unsigned chunks) {
+  __shared__ unsigned sh[32];
+  const unsigned lo = blockIdx.x * kScanSuper, hi = min(chunks, lo + kScanSuper);
+  unsigned v = 0u;
+  for (unsigned c = lo + threadIdx.x; c < hi; c += blockDim.x) v += part[c];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31u) == 0u) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = 0u;
+    for (unsigned w = 0; w < blockDim.x / 32u; ++w) t += sh[w];
+    part[chunks + blockIdx.x] = t;
+  }
+}
+
+static __global__ void k_count(const float4* __restrict__ A, const Counters* __restrict__ ctr, GridP g, int dims,
+                               unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt,
+                               unsigned* __restrict__ part) {
+  const unsigned n = ctr->n;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float4 v = A[s];
+    float p[3] = {v.x, v.y, v.z};
+    int c[3] = {0, 0, 0};
+    unsigned b;
+    if (dims == 3) { bin_coords_div<3>(g, p, c); b = flatten<3>(g, c); }
+    else { bin_coords_div<2>(g, p, c); b = flatten<2>(g, c); }
+    key[s] = b;
+    rank[s] = count_bin(cnt, part, b);
+  }
 }
 
 __device__ __forceinline__ unsigned block_sum(unsigned v, unsigned* sh) {
@@ -197,10 +233,14 @@ static __global__ void k_scan_apply(unsigned* __restrict__ cnt, unsigned len, co
   }
 }
 
+// (part_words > 0: the scan has read the chunk totals that the counting
+// formed; they start again from zero for the next step's count)
 static __global__ void k_scatter(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
                           const unsigned* __restrict__ rank, const unsigned* __restrict__ off,
-                          unsigned* __restrict__ src) {
+                          unsigned* __restrict__ src, unsigned* __restrict__ part, unsigned part_words) {
   const unsigned n = ctr->n;
+  if (blockIdx.x == 0)
+    for (unsigned w = threadIdx.x; w < part_words; w += blockDim.x) part[w] = 0u;
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     src[off[key[s]] + rank[s]] = s;
 }
@@ -317,7 +357,7 @@ __device__ __forceinline__ void count_cell(const GridP& g, const PassArgs& a, un
   bin_coords_div<D>(g, x, c);
   const unsigned b = flatten<D>(g, c);
   a.key[slot] = b;
-  a.rank[slot] = atomicAdd(&a.cnt[b], 1u);
+  a.rank[slot] = count_bin(a.cnt, a.part, b);
 }
 
 // ---------------------------------------------------------------------------

@@ -98,7 +98,8 @@ __global__ void k_unpack2(const float4* __restrict__ idw, const unsigned* __rest
 // and, when the first rebuild expects them, the cells counted per bin.
 __global__ void k_upload(const float* __restrict__ pos, const float2* __restrict__ pol, unsigned n, int dims,
                          float4* __restrict__ A, float2* __restrict__ PA, Counters* __restrict__ ctr, GridP g,
-                         unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt) {
+                         unsigned* __restrict__ key, unsigned* __restrict__ rank, unsigned* __restrict__ cnt,
+                         unsigned* __restrict__ part) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctr->n = n;
     ctr->div_count = 0u;
@@ -121,7 +122,7 @@ __global__ void k_upload(const float* __restrict__ pos, const float2* __restrict
       if (dims == 3) { bin_coords_div<3>(g, p, c); b = flatten<3>(g, c); }
       else { bin_coords_div<2>(g, p, c); b = flatten<2>(g, c); }
       key[s] = b;
-      rank[s] = atomicAdd(&cnt[b], 1u);
+      rank[s] = count_bin(cnt, part, b);
     }
   }
 }
@@ -208,6 +209,9 @@ struct tecs_sim {
   int last_kernels = 0;
   // the next rebuild's bin count is done by the state-writing kernel
   bool fuse_count = false;
+  // sparse grids (bins > 4 x capacity): the counting also forms the scan's
+  // chunk totals, and the rebuild needs no reduction pass over the bins
+  bool fuse_part = false;
   Counters* hctr = nullptr;  // page-locked mirror of the device counters
   // block-cooperative Gabriel pass enabled (off only for comparison runs)
   bool use_coop = true;
@@ -310,6 +314,7 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.key = s->key;
   a.rank = s->rank;
   a.cnt = s->cnt;
+  a.part = s->fuse_part ? s->part : nullptr;
   a.dmult = s->dmult;
   a.link_off = s->n_links ? s->link_off : nullptr;
   a.link_ent = s->n_links ? s->link_ent : nullptr;
@@ -328,16 +333,28 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
   if (s->binned) {
     const unsigned len = s->g.nbins + 1;
     const unsigned chunks = ceil_div(len, kScanChunk);
+    const unsigned pw = (unsigned)scan_part_words(len);
+    unsigned* part = s->fuse_part ? s->part : nullptr;
     if (run_count) {
       PROF_BEGIN(s);
-      k_count<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+      if (part) CK(cudaMemsetAsync(part, 0, (size_t)pw * 4, s->stream));
+      k_count<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt, part);
       PROF_END(s, "k_count");
       K += 1;
     }
-    // one chunk: its prefix needs no partial sums
-    if (chunks > 1) {
+    if (part) {
+      // sparse grid: the counting formed the chunk totals (count_bin); the
+      // super-chunk totals are needed past kScanSuper chunks only
+      if (chunks > kScanSuper) {
+        PROF_BEGIN(s);
+        k_scan_super<<<ceil_div(chunks, kScanSuper), kScanThreads, 0, s->stream>>>(part, chunks);
+        PROF_END(s, "k_scan_super");
+        K += 1;
+      }
+    } else if (chunks > 1) {
+      // one chunk: its prefix needs no partial sums
       PROF_BEGIN(s);
-      CK(cudaMemsetAsync(s->part + chunks, 0, (scan_part_words(len) - chunks) * 4, s->stream));
+      CK(cudaMemsetAsync(s->part + chunks, 0, (pw - chunks) * 4, s->stream));
       k_scan_reduce<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part);
       PROF_END(s, "k_scan_reduce");
       K += 1;
@@ -346,7 +363,7 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     k_scan_apply<<<chunks, kScanThreads, 0, s->stream>>>(s->cnt, len, s->part, s->off);
     PROF_END(s, "k_scan_apply");
     PROF_BEGIN(s);
-    k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src);
+    k_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->rank, s->off, s->src, s->part, part ? pw : 0u);
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
     k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid,
@@ -589,6 +606,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   f.gab_csq = desc->gabriel_coefficient * desc->gabriel_coefficient;
   s->binned = desc->finder == TECS_FINDER_BINNED_ALL_PAIRS || desc->finder == TECS_FINDER_BINNED_GABRIEL;
   s->fuse_count = s->binned && (desc->division_probability > 0.0 || desc->rebuild_every_n <= 1);
+  s->fuse_part = s->binned && (double)g.nbins > 4.0 * (double)desc->capacity;
 
   const size_t cap = desc->capacity;
   auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
@@ -650,11 +668,16 @@ int tecs_sim_destroy(tecs_sim* s) {
 // k_upload pass.  The delta buffers need no reset: every pass writes the
 // deltas of all active cells before they are read.
 static int upload_common(tecs_sim* s, const float* pos, const float2* pol, unsigned n) {
-  // the first rebuild expects the bin counts of A to be made already
-  if (s->fuse_count) CK(cudaMemsetAsync(s->cnt, 0, ((size_t)s->g.nbins + 1) * 4, s->stream));
+  // the first rebuild expects the bin counts of A, and their chunk totals,
+  // to be made already
+  const unsigned len = s->g.nbins + 1;
+  if (s->fuse_count) {
+    CK(cudaMemsetAsync(s->cnt, 0, (size_t)len * 4, s->stream));
+    if (s->fuse_part) CK(cudaMemsetAsync(s->part, 0, scan_part_words(len) * 4, s->stream));
+  }
   k_upload<<<std::max(1u, ceil_div(n, 256)), 256, 0, s->stream>>>(
       pos, s->d.has_polarity ? pol : nullptr, n, s->d.dims, s->A, s->PA, s->ctr, s->g, s->key, s->rank,
-      s->fuse_count ? s->cnt : nullptr);
+      s->fuse_count ? s->cnt : nullptr, (s->fuse_count && s->fuse_part) ? s->part : nullptr);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s->stream));
   // the captured step graphs depend on the state only through their grid
@@ -828,7 +851,8 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   if (rc == 0 && s->binned) s->sorted = true;  // the rebuild above sorted the current cells
   if (rc == 0 && s->fuse_count && n) {
     // A is unchanged: count it again for the next step's rebuild
-    k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt);
+    k_count<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, s->ctr, s->g, s->d.dims, s->key, s->rank, s->cnt,
+                                                     s->fuse_part ? s->part : nullptr);
   }
   if (rc == 0 && n) {
     if (dpos) {
