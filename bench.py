@@ -161,6 +161,7 @@ class Clocks:
         self.index = index
         self.proc = None
         self.path = None
+        self._summary = None
 
     def __enter__(self):
         try:
@@ -205,6 +206,12 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        """Median SM clock, maximum and throttle reasons inside the timed region (read once, then kept)."""
+        if self._summary is None:
+            self._summary = self._read()
+        return self._summary
+
+    def _read(self):
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm, smax, reasons = [], [], set()
@@ -244,15 +251,20 @@ def aggregate_over_ranks(total_s: float, cell_steps: float, device):
     return float(t.item()), float(c.item())
 
 
-def traffic_per_pass(workload: str):
-    """DRAM bytes per cell of one force-pass launch, from the committed ncu capture of this workload."""
+def pass_profile(workload: str, key: str):
+    """A per-cell figure of one force-pass launch (DRAM bytes, warp instructions) from the committed ncu
+    capture of this workload."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
-        return json.loads(p.read_text()).get(workload, {}).get("pass_dram_bytes_per_cell")
+        return json.loads(p.read_text()).get(workload, {}).get(key)
     except Exception:
         return None
+
+
+def traffic_per_pass(workload: str):
+    return pass_profile(workload, "pass_dram_bytes_per_cell")
 
 
 def cpu_steps(w, n, mn, mx, x, p, steps, threads, budget_s):
@@ -440,6 +452,19 @@ def run_gb300(args):
                 "kernel": "force pass (k_pass_*: pair finding + force + fused integrator epilogue)",
                 "bytes_per_launch": pass_bytes / max(pass_launches, 1),
                 "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_s / max(pass_launches, 1)}
+    # The pass is bound by instruction issue, not HBM: warp instructions per launch (ncu count per cell x
+    # cells) over the live launch time, against SMs x 4 schedulers x the sampled SM clock.
+    ipc = pass_profile(args.workload, "pass_warp_inst_per_cell")
+    issue_roofline = None
+    if ipc and pass_s:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = (clocks.summary() or {}).get("sm_mhz") or 2070.0
+        ipeak = sms * 4 * mhz * 1e6
+        iach = ipc * n_prof * pass_launches / pass_s
+        issue_roofline = {"bound": "issue", "achieved": iach, "peak": ipeak, "unit": "warp instructions/s",
+                          "frac": iach / ipeak, "inst_per_cell": ipc,
+                          "peak_basis": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)",
+                          "source": "profiles/traffic.json (ncu smsp__inst_executed.sum of one launch)"}
     step_achieved = w["step_bytes"] * n_avg / (statistics.mean(step_ms) / 1e3) / 1e9
     kernel_table = {k: {"launches": len(v), "mean_ms": statistics.mean(v), "share": sum(v) / max(sum(prof_ms), 1e-9)}
                     for k, v in kern.items()}
@@ -458,6 +483,7 @@ def run_gb300(args):
         "roofline": roofline,
         "step_roofline": {"bytes_per_cell": w["step_bytes"], "achieved": step_achieved,
                           "frac": step_achieved / hbm},
+        "issue_roofline": issue_roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": kpl * args.steps,
