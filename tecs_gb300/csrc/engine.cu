@@ -141,7 +141,8 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 }
 
 // ---------------------------------------------------------------------------
-// the force pass over all slots (block-cooperative, as k_pass_gabriel)
+// the force pass over all slots: block-cooperative, the design k_pass_gabriel
+// had before its phases became per-warp (the engine keeps this one)
 
 // POL: some resident simulation carries polarity; their cells then take the
 // cooperative path with the polarity law (as k_pass_gabriel<3, 2>), which

@@ -213,7 +213,7 @@ struct tecs_sim {
   // chunk totals, and the rebuild needs no reduction pass over the bins
   bool fuse_part = false;
   Counters* hctr = nullptr;  // page-locked mirror of the device counters
-  // block-cooperative Gabriel pass enabled (off only for comparison runs)
+  // cooperative Gabriel pass enabled (off only for comparison runs)
   bool use_coop = true;
   // per-kernel CUDA events (external event-record nodes when captured in a graph)
   bool profiling = false;
@@ -255,7 +255,7 @@ int prof_mark(tecs_sim* s, int which, const char* name) {
 
 PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
-  // the block-cooperative Gabriel pass needs the fast-path geometry and packs
+  // the cooperative Gabriel pass needs the fast-path geometry and packs
   // bin coordinates in 10 bits and slots in 27 bits
   const bool coop_geom = s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
                          s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27) && s->use_coop;
