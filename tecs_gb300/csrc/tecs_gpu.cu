@@ -213,8 +213,6 @@ struct tecs_sim {
   // chunk totals, and the rebuild needs no reduction pass over the bins
   bool fuse_part = false;
   Counters* hctr = nullptr;  // page-locked mirror of the device counters
-  // cooperative Gabriel pass enabled (off only for comparison runs)
-  bool use_coop = true;
   // per-kernel CUDA events (external event-record nodes when captured in a graph)
   bool profiling = false;
   static constexpr int kMaxProf = 32;
@@ -258,7 +256,7 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
   // the cooperative Gabriel pass needs the fast-path geometry and packs
   // bin coordinates in 10 bits and slots in 27 bits
   const bool coop_geom = s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
-                         s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27) && s->use_coop;
+                         s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27);
   const bool coop = coop_geom && s->d.gabriel_coefficient <= 0.9f;
 #define PICK(DD, FF)                                                            \
   if (D == DD && F == FF) {                                                     \
