@@ -90,7 +90,9 @@ int tecs_sim_destroy(tecs_sim* sim);
 /* Initial state from host memory (n <= capacity); resets the finder's
  * rebuild counter as Simulation::set_agent_count does
  * (include/simulation.hpp:295-302).  The division stream stays keyed by the
- * steps taken since creation. */
+ * steps taken since creation.  Page-locked buffers are read by the upload
+ * kernel directly; other host memory is staged with one copy.  Returns once
+ * the buffers may be reused. */
 int tecs_sim_upload(tecs_sim* sim, const float* positions, const float* polarity, unsigned n);
 
 /* Same from device memory on the simulation's device (no host copy). */
@@ -109,7 +111,9 @@ int tecs_sim_count(tecs_sim* sim, unsigned* n);
 
 /* Copy the state back in cell-id order (synchronises).  The host side of
  * View::sync_host + HDF5_Writer::write (include/io/hdf5_writer.hpp:306-321).
- * positions: capacity*dims floats; polarity: capacity*2 floats or NULL. */
+ * positions: capacity*dims floats; polarity: capacity*2 floats or NULL.
+ * Page-locked buffers are written by kernels directly (one synchronisation);
+ * other host memory receives one staged copy. */
 int tecs_sim_download(tecs_sim* sim, float* positions, float* polarity, unsigned* n);
 
 /* Test hook: one full-step force evaluation of the current state with a
