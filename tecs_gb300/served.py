@@ -10,6 +10,13 @@ unpacked on the device and copied to pinned host memory on a side stream, and
 a writer thread stores it (HDF5 via tecs_gb300.h5) without stalling the steps.
 A simulation that reaches its step count is downloaded, retired, and its
 time-to-completion (arrival -> result on the host) recorded.
+
+An engine advances all its resident simulations in lockstep, so a small
+request sharing an engine with a large one pays the large one's step time for
+each of its steps.  With size classes the server keeps one engine (a lane) per
+class -- e.g. requests up to 50k cells in one, the rest in another -- each on
+its own stream and paced by its own step events, so small requests progress
+at their own rate while the large ones run alongside on the same GPU.
 """
 from __future__ import annotations
 
@@ -30,6 +37,9 @@ import tecs_gb300 as tg
 from tecs_gb300 import workloads as wl
 from tecs_gb300.engine import Engine, bins_needed
 
+IN_FLIGHT = 2  # steps a lane may have queued on the GPU
+# the served bench's lanes: requests up to 50k cells in an engine with a tenth of the capacity
+BENCH_SIZE_CLASSES = [(50_000, 0.1), (None, 0.9)]
 BYTES_PER_CELL = 140  # device bytes the engine keeps per cell (positions, deltas, polarity, sort scratch)
 BYTES_PER_BIN = 8
 
@@ -62,6 +72,22 @@ class Live:
     steps_done: int = 0
     admitted_at: float = 0.0
     req_index: int = -1
+
+
+@dataclass
+class Lane:
+    """One engine of the server and the requests it serves."""
+    engine: Engine
+    max_req_cells: Optional[int]  # requests up to this many cells (None: any)
+    cell_capacity: int
+    bin_capacity: int
+    live: Dict[int, Live] = field(default_factory=dict)
+    waiting: collections.deque = field(default_factory=collections.deque)
+    stage_next: int = 0
+    pending: collections.deque = field(default_factory=collections.deque)  # events of queued steps
+
+    def takes(self, n: int) -> bool:
+        return self.max_req_cells is None or n <= self.max_req_cells
 
 
 @dataclass
@@ -131,9 +157,25 @@ class PinnedPool:
 
 
 class Server:
+    """size_classes: [(largest request in cells, or None for any; share of the capacity)], one engine
+    (lane) per class, in order; None keeps a single engine for every request."""
+
     def __init__(self, cell_capacity: int, bin_capacity: int, max_sims: int = 1024, snapshot_every: int = 100,
-                 dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0):
-        self.engine = Engine(cell_capacity, bin_capacity, max_sims, device)
+                 dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0,
+                 size_classes=None):
+        import torch
+
+        self.torch = torch
+        classes = size_classes or [(None, 1.0)]
+        if classes[-1][0] is not None:
+            raise ValueError("the last size class must take any request (None)")
+        self.lanes: List[Lane] = []
+        for max_cells, share in classes:
+            c, b = max(int(cell_capacity * share), 1), max(int(bin_capacity * share), 1)
+            self.lanes.append(Lane(Engine(c, b, max_sims, device), max_cells, c, b))
+        self.engine = self.lanes[0].engine
+        self.streams = [torch.cuda.ExternalStream(l.engine.stream, device=torch.device("cuda", device))
+                        for l in self.lanes]
         self.cell_capacity = cell_capacity
         self.bin_capacity = bin_capacity
         self.dt = dt
@@ -142,9 +184,11 @@ class Server:
         self.writer.start()
         self.pool = PinnedPool()
         self.keep_results = keep_results
-        self.stage_next = 0
         self.cell_steps = 0
         self.steps = 0
+
+    def lane_for(self, n: int) -> Lane:
+        return next(l for l in self.lanes if l.takes(n))
 
     @staticmethod
     def capacity_from_free_hbm(fraction: float = 0.5, bins_per_cell: float = 3.0):
@@ -155,15 +199,15 @@ class Server:
         cells = int(budget / (BYTES_PER_CELL + bins_per_cell * BYTES_PER_BIN))
         return max(cells, 1 << 16), int(max(cells, 1 << 16) * bins_per_cell)
 
-    def _snapshot(self, live: Live, step: int):
+    def _snapshot(self, lane: Lane, live: Live, step: int):
         pos = self.pool.get(live.n, 3)
         pol = self.pool.get(live.n, 2) if live.has_pol else None
-        if self.stage_next + live.n > self.cell_capacity:
-            self.stage_next = 0
-            self.engine.synchronize()  # staging reused: let queued copies finish
-        ev = self.engine.snapshot_async(live.slot, pos.data_ptr(), None if pol is None else pol.data_ptr(),
-                                        self.stage_next)
-        self.stage_next += live.n
+        if lane.stage_next + live.n > lane.cell_capacity:
+            lane.stage_next = 0
+            lane.engine.synchronize()  # staging reused: let queued copies finish
+        ev = lane.engine.snapshot_async(live.slot, pos.data_ptr(), None if pol is None else pol.data_ptr(),
+                                        lane.stage_next)
+        lane.stage_next += live.n
 
         def release(pos=pos, pol=pol):
             self.pool.put(pos)
@@ -179,67 +223,85 @@ class Server:
         built = {}
         for idx, r in reqs:
             sim = request_sim(r, max_cells)
-            if len(sim[0]) > self.cell_capacity or bins_needed(sim[2]) > self.bin_capacity:
+            lane = self.lane_for(len(sim[0]))
+            if len(sim[0]) > lane.cell_capacity or bins_needed(sim[2]) > lane.bin_capacity:
                 raise ValueError(f"request {idx} ({len(sim[0])} cells, {bins_needed(sim[2])} bins) "
-                                 f"exceeds the engine ({self.cell_capacity} cells, {self.bin_capacity} bins)")
+                                 f"exceeds its engine ({lane.cell_capacity} cells, {lane.bin_capacity} bins)")
             if prebuild:
                 built[idx] = sim
-        waiting = collections.deque()
-        live: Dict[int, Live] = {}
         results: List[Result] = []
         arrival = {idx: r.arrival_s / time_scale for idx, r in reqs}
         k = 0
         t0 = time.perf_counter()
-        while k < len(reqs) or waiting or live:
+        while k < len(reqs) or any(l.waiting or l.live for l in self.lanes):
             now = time.perf_counter() - t0
             while k < len(reqs) and arrival[reqs[k][0]] <= now:
-                waiting.append(reqs[k][0])
+                idx = reqs[k][0]
+                n = len(built[idx][0]) if idx in built else len(request_sim(requests[idx], max_cells)[0])
+                self.lane_for(n).waiting.append(idx)
                 k += 1
-            # admission: first come, first served, while cells and bins are free
-            while waiting:
-                idx = waiting[0]
-                x, p, d, _, _ = built[idx] if idx in built else request_sim(requests[idx], max_cells)
-                free_cells, free_bins = self.engine.free()
-                if len(x) > free_cells or bins_needed(d) > free_bins:
-                    break
-                waiting.popleft()
-                slot = self.engine.add(d, x, p)
-                live[slot] = Live(requests[idx], slot, len(x), p is not None, 0, time.perf_counter() - t0, idx)
-            if not live:
-                if waiting:  # an idle engine holds nothing: the head request must fit
-                    raise RuntimeError(f"request {waiting[0]} cannot be admitted into an idle engine")
+            # admission, per lane: first come, first served, while cells and bins are free
+            for lane in self.lanes:
+                while lane.waiting:
+                    idx = lane.waiting[0]
+                    x, p, d, _, _ = built[idx] if idx in built else request_sim(requests[idx], max_cells)
+                    free_cells, free_bins = lane.engine.free()
+                    if len(x) > free_cells or bins_needed(d) > free_bins:
+                        break
+                    lane.waiting.popleft()
+                    slot = lane.engine.add(d, x, p)
+                    lane.live[slot] = Live(requests[idx], slot, len(x), p is not None, 0,
+                                           time.perf_counter() - t0, idx)
+                if lane.waiting and not lane.live:  # an idle engine holds nothing: the head must fit
+                    raise RuntimeError(f"request {lane.waiting[0]} cannot be admitted into an idle engine")
+            if not any(l.live for l in self.lanes):
                 if k < len(reqs):
                     time.sleep(max(0.0, min(0.01, arrival[reqs[k][0]] - (time.perf_counter() - t0))))
                 continue
-            # one step of every resident simulation
-            self.engine.step(self.dt, 1)
-            self.steps += 1
-            for lv in live.values():
-                lv.steps_done += 1
-                self.cell_steps += lv.n
-            done = []
-            for slot, lv in live.items():
-                if lv.steps_done % self.snapshot_every == 0 and lv.steps_done < lv.req.steps:
-                    self._snapshot(lv, lv.steps_done)
-                if lv.steps_done >= lv.req.steps:
-                    done.append(slot)
-            for slot in done:
-                lv = live.pop(slot)
-                xf, pf = self.engine.download(slot)
-                self.engine.remove(slot)
-                res = Result(lv.req_index, lv.n, lv.req.steps, arrival[lv.req_index], lv.admitted_at,
-                             time.perf_counter() - t0)
-                if self.keep_results:
-                    res.positions, res.polarity = xf, pf
-                results.append(res)
-        self.engine.synchronize()
+            # one step of every resident simulation of each lane with fewer than IN_FLIGHT steps queued
+            # (each lane keeps its GPU queue fed at its own pace)
+            issued = False
+            for lane, stream in zip(self.lanes, self.streams):
+                while lane.pending and lane.pending[0].query():
+                    lane.pending.popleft()
+                if not lane.live or len(lane.pending) >= IN_FLIGHT:
+                    continue
+                lane.engine.step(self.dt, 1)
+                ev = self.torch.cuda.Event()
+                ev.record(stream)
+                lane.pending.append(ev)
+                issued = True
+                self.steps += 1
+                for lv in lane.live.values():
+                    lv.steps_done += 1
+                    self.cell_steps += lv.n
+                done = []
+                for slot, lv in lane.live.items():
+                    if lv.steps_done % self.snapshot_every == 0 and lv.steps_done < lv.req.steps:
+                        self._snapshot(lane, lv, lv.steps_done)
+                    if lv.steps_done >= lv.req.steps:
+                        done.append(slot)
+                for slot in done:
+                    lv = lane.live.pop(slot)
+                    xf, pf = lane.engine.download(slot)
+                    lane.engine.remove(slot)
+                    res = Result(lv.req_index, lv.n, lv.req.steps, arrival[lv.req_index], lv.admitted_at,
+                                 time.perf_counter() - t0)
+                    if self.keep_results:
+                        res.positions, res.polarity = xf, pf
+                    results.append(res)
+            if not issued:
+                time.sleep(0.00005)
+        for lane in self.lanes:
+            lane.engine.synchronize()
         self.makespan = time.perf_counter() - t0
         return results
 
     def close(self):
         self.writer.q.put(None)
         self.writer.join(timeout=60)
-        self.engine.close()
+        for lane in self.lanes:
+            lane.engine.close()
 
 
 def summarize(results: List[Result], makespan: float, cell_steps: int):
@@ -313,16 +375,22 @@ def bench_main(args):
     out_dir = Path(os.environ.get("TECS_SNAPSHOT_DIR", "/tmp/tecs_snapshots"))
     out_dir.mkdir(parents=True, exist_ok=True)
     sink = h5.SnapshotSink(out_dir)
-    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink)
+    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink, size_classes=BENCH_SIZE_CLASSES)
     res = srv.run(reqs, time_scale=args.time_scale)
     summ = summarize(res, srv.makespan, srv.cell_steps)
+    small = [r for r in res if r.n <= BENCH_SIZE_CLASSES[0][0]]
+    large = [r for r in res if r.n > BENCH_SIZE_CLASSES[0][0]]
+    by_class = {name: {"requests": len(rs), "p50_s": float(np.percentile([r.latency for r in rs], 50)),
+                       "p99_s": float(np.percentile([r.latency for r in rs], 99))}
+                for name, rs in (("small", small), ("large", large)) if rs}
     written = srv.writer.written
     srv.close()
     sink.close()
     plain_v, rows = plain_sample(reqs)
     plain_lat = plain_fcfs_latency(reqs, rows, args.time_scale)
     # capacity: the same stream with arrivals compressed 100 times (compute-bound)
-    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, sink=None)
+    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, sink=None,
+                     size_classes=BENCH_SIZE_CLASSES)
     cap_res = cap_srv.run(reqs, time_scale=100.0)
     cap = summarize(cap_res, cap_srv.makespan, cap_srv.cell_steps)
     cap_srv.close()
@@ -333,8 +401,10 @@ def bench_main(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{n_req} requests, Poisson 20/s (seed 3) with arrivals compressed x{args.time_scale}, "
                                "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
-                               "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins},
-        "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"]},
+                               "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins,
+                   "size_classes": [{"max_request_cells": m, "capacity_share": f} for m, f in BENCH_SIZE_CLASSES]},
+        "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"],
+                    "by_size_class": by_class},
         "capacity": {"value": cap["cell_steps_per_s"], "makespan_s": cap["makespan_s"],
                      "note": "the same requests with arrivals compressed x100 (no snapshots): compute-bound"},
         "plain_sequential": {"value": plain_v, "requests": len(rows),

@@ -67,3 +67,25 @@ def test_failing_snapshot_sink_fails_only_that_snapshot(tmp_path):
     srv.close()
     assert len(res) == 4
     assert srv.writer.errors and all("request 1" in e for e in srv.writer.errors)
+
+
+def test_size_classes_keep_results_and_let_small_requests_pass_large_ones(tmp_path):
+    # two lanes: requests up to 3000 cells in one engine, the rest in another, each on its own stream
+    reqs = wl.served_stream(12, seed=7, rate_hz=400.0, lo=800, hi=12000, steps_lo=30, steps_hi=150)
+    srv = Server(cell_capacity=60000, bin_capacity=400000, max_sims=16, snapshot_every=40,
+                 sink=h5.SnapshotSink(tmp_path), keep_results=True, size_classes=[(3000, 0.3), (None, 0.7)])
+    res = srv.run(reqs, time_scale=1.0)
+    srv.close()
+    assert len(res) == len(reqs)
+    assert {r.n <= 3000 for r in res} == {True, False}  # both lanes served requests
+    for r in res:
+        x_alone, p_alone = alone(reqs[r.index], None)
+        np.testing.assert_array_equal(r.positions, x_alone)
+        if p_alone is not None:
+            np.testing.assert_array_equal(r.polarity, p_alone)
+    assert not srv.writer.errors
+
+
+def test_size_classes_need_a_lane_for_any_request():
+    with pytest.raises(ValueError):
+        Server(cell_capacity=1000, bin_capacity=1000, size_classes=[(500, 1.0)])
