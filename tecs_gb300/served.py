@@ -162,7 +162,7 @@ class Server:
 
     def __init__(self, cell_capacity: int, bin_capacity: int, max_sims: int = 1024, snapshot_every: int = 100,
                  dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0,
-                 size_classes=None):
+                 size_classes=None, steps_per_issue: int = 1):
         import torch
 
         self.torch = torch
@@ -186,6 +186,8 @@ class Server:
         self.keep_results = keep_results
         self.cell_steps = 0
         self.steps = 0
+        # up to this many steps per engine call, never past a resident request's next snapshot or end
+        self.steps_per_issue = max(1, int(steps_per_issue))
 
     def lane_for(self, n: int) -> Lane:
         return next(l for l in self.lanes if l.takes(n))
@@ -266,15 +268,20 @@ class Server:
                     lane.pending.popleft()
                 if not lane.live or len(lane.pending) >= IN_FLIGHT:
                     continue
-                lane.engine.step(self.dt, 1)
+                kk = self.steps_per_issue
+                for lv in lane.live.values():
+                    to_snap = self.snapshot_every - lv.steps_done % self.snapshot_every
+                    kk = min(kk, lv.req.steps - lv.steps_done, to_snap)
+                kk = max(kk, 1)
+                lane.engine.step(self.dt, kk)
                 ev = self.torch.cuda.Event()
                 ev.record(stream)
                 lane.pending.append(ev)
                 issued = True
-                self.steps += 1
+                self.steps += kk
                 for lv in lane.live.values():
-                    lv.steps_done += 1
-                    self.cell_steps += lv.n
+                    lv.steps_done += kk
+                    self.cell_steps += lv.n * kk
                 done = []
                 for slot, lv in lane.live.items():
                     if lv.steps_done % self.snapshot_every == 0 and lv.steps_done < lv.req.steps:
@@ -375,7 +382,8 @@ def bench_main(args):
     out_dir = Path(os.environ.get("TECS_SNAPSHOT_DIR", "/tmp/tecs_snapshots"))
     out_dir.mkdir(parents=True, exist_ok=True)
     sink = h5.SnapshotSink(out_dir)
-    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink, size_classes=BENCH_SIZE_CLASSES)
+    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink, size_classes=BENCH_SIZE_CLASSES,
+                 steps_per_issue=8)
     res = srv.run(reqs, time_scale=args.time_scale)
     summ = summarize(res, srv.makespan, srv.cell_steps)
     small = [r for r in res if r.n <= BENCH_SIZE_CLASSES[0][0]]
@@ -390,7 +398,7 @@ def bench_main(args):
     plain_lat = plain_fcfs_latency(reqs, rows, args.time_scale)
     # capacity: the same stream with arrivals compressed 100 times (compute-bound)
     cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, sink=None,
-                     size_classes=BENCH_SIZE_CLASSES)
+                     size_classes=BENCH_SIZE_CLASSES, steps_per_issue=8)
     cap_res = cap_srv.run(reqs, time_scale=100.0)
     cap = summarize(cap_res, cap_srv.makespan, cap_srv.cell_steps)
     cap_srv.close()
@@ -402,7 +410,8 @@ def bench_main(args):
         "config": {"workload": f"{n_req} requests, Poisson 20/s (seed 3) with arrivals compressed x{args.time_scale}, "
                                "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
                                "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins,
-                   "size_classes": [{"max_request_cells": m, "capacity_share": f} for m, f in BENCH_SIZE_CLASSES]},
+                   "size_classes": [{"max_request_cells": m, "capacity_share": f} for m, f in BENCH_SIZE_CLASSES],
+                   "steps_per_issue": 8},
         "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"],
                     "by_size_class": by_class},
         "capacity": {"value": cap["cell_steps_per_s"], "makespan_s": cap["makespan_s"],

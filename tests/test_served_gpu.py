@@ -69,13 +69,16 @@ def test_failing_snapshot_sink_fails_only_that_snapshot(tmp_path):
     assert srv.writer.errors and all("request 1" in e for e in srv.writer.errors)
 
 
-def test_size_classes_keep_results_and_let_small_requests_pass_large_ones(tmp_path):
+def test_size_classes_and_batched_issue_keep_results_and_snapshots(tmp_path):
     # two lanes: requests up to 3000 cells in one engine, the rest in another, each on its own stream
     reqs = wl.served_stream(12, seed=7, rate_hz=400.0, lo=800, hi=12000, steps_lo=30, steps_hi=150)
-    srv = Server(cell_capacity=60000, bin_capacity=400000, max_sims=16, snapshot_every=40,
-                 sink=h5.SnapshotSink(tmp_path), keep_results=True, size_classes=[(3000, 0.3), (None, 0.7)])
+    # and up to 8 steps per engine call, never past a request's next snapshot or end
+    sink = h5.SnapshotSink(tmp_path)
+    srv = Server(cell_capacity=60000, bin_capacity=400000, max_sims=16, snapshot_every=40, sink=sink,
+                 keep_results=True, size_classes=[(3000, 0.3), (None, 0.7)], steps_per_issue=8)
     res = srv.run(reqs, time_scale=1.0)
     srv.close()
+    sink.close()
     assert len(res) == len(reqs)
     assert {r.n <= 3000 for r in res} == {True, False}  # both lanes served requests
     for r in res:
@@ -84,6 +87,10 @@ def test_size_classes_keep_results_and_let_small_requests_pass_large_ones(tmp_pa
         if p_alone is not None:
             np.testing.assert_array_equal(r.polarity, p_alone)
     assert not srv.writer.errors
+    for r in res:
+        want = [f"t{k}" for k in range(40, reqs[r.index].steps, 40)]
+        if want:
+            assert sorted(h5.H5File(tmp_path / f"request_{r.index:05d}.h5").keys()) == sorted(want)
 
 
 def test_size_classes_need_a_lane_for_any_request():
