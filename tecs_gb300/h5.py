@@ -394,3 +394,27 @@ class SnapshotSink:
             for w in self.files.values():
                 w.close()
             self.files.clear()
+
+
+def last_snapshot(directory: str | os.PathLike, request: int):
+    """(step, positions, polarity or None) of the newest snapshot SnapshotSink wrote for a request, or None.
+
+    A file the writer never closed (a server that stopped mid-run) has no
+    superblock yet and is not a snapshot: None."""
+    path = Path(directory) / f"request_{request:05d}.h5"
+    if not path.exists():
+        return None
+    try:
+        f = H5File(path)
+        steps = sorted(int(k[1:]) for k in f.keys() if k.startswith("t") and k[1:].isdigit())
+    except Exception:
+        return None
+    if not steps:
+        return None
+    g = f"t{steps[-1]}"
+    pos = f.read(f"{g}/position")
+    try:
+        pol = f.read(f"{g}/polarity")
+    except Exception:
+        pol = None
+    return steps[-1], pos, pol

@@ -219,12 +219,24 @@ class Server:
         self.writer.q.put((ev, live.req_index, step, pos.numpy(), None if pol is None else pol.numpy(), release))
 
     def run(self, requests: List[wl.Request], time_scale: float = 1.0, max_cells: Optional[int] = None,
-            prebuild: bool = True):
-        """Serve the requests; arrival times are divided by time_scale.  Returns the results."""
+            prebuild: bool = True, resume: Optional[Dict[int, tuple]] = None):
+        """Serve the requests; arrival times are divided by time_scale.  Returns the results.
+
+        resume: {request index: (step, positions, polarity or None)} -- such a request starts from that
+        state (a snapshot, h5.last_snapshot) and runs only its remaining steps; its snapshots and its end
+        fall on the same steps as in an uninterrupted run, and so does its result (the state is the
+        positions and polarities, in cell-id order)."""
+        resume = resume or {}
         reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival_s)
         built = {}
         for idx, r in reqs:
             sim = request_sim(r, max_cells)
+            if idx in resume:
+                step, pos, pol = resume[idx]
+                if len(pos) != len(sim[0]) or (pol is None) != (sim[1] is None) or not 0 <= step <= r.steps:
+                    raise ValueError(f"resume state of request {idx} does not match the request")
+                sim = (np.ascontiguousarray(pos, np.float32),
+                       None if pol is None else np.ascontiguousarray(pol, np.float32)) + tuple(sim[2:])
             lane = self.lane_for(len(sim[0]))
             if len(sim[0]) > lane.cell_capacity or bins_needed(sim[2]) > lane.bin_capacity:
                 raise ValueError(f"request {idx} ({len(sim[0])} cells, {bins_needed(sim[2])} bins) "
@@ -252,10 +264,21 @@ class Server:
                         break
                     lane.waiting.popleft()
                     slot = lane.engine.add(d, x, p)
-                    lane.live[slot] = Live(requests[idx], slot, len(x), p is not None, 0,
-                                           time.perf_counter() - t0, idx)
+                    lane.live[slot] = Live(requests[idx], slot, len(x), p is not None,
+                                           resume[idx][0] if idx in resume else 0, time.perf_counter() - t0, idx)
                 if lane.waiting and not lane.live:  # an idle engine holds nothing: the head must fit
                     raise RuntimeError(f"request {lane.waiting[0]} cannot be admitted into an idle engine")
+            # resumed requests that were already complete
+            for lane in self.lanes:
+                for slot in [s_ for s_, lv in lane.live.items() if lv.steps_done >= lv.req.steps]:
+                    lv = lane.live.pop(slot)
+                    xf, pf = lane.engine.download(slot)
+                    lane.engine.remove(slot)
+                    res = Result(lv.req_index, lv.n, lv.req.steps, arrival[lv.req_index], lv.admitted_at,
+                                 time.perf_counter() - t0)
+                    if self.keep_results:
+                        res.positions, res.polarity = xf, pf
+                    results.append(res)
             if not any(l.live for l in self.lanes):
                 if k < len(reqs):
                     time.sleep(max(0.0, min(0.01, arrival[reqs[k][0]] - (time.perf_counter() - t0))))
@@ -309,6 +332,19 @@ class Server:
         self.writer.join(timeout=60)
         for lane in self.lanes:
             lane.engine.close()
+
+
+def resume_points(directory, indices) -> Dict[int, tuple]:
+    """{request index: (step, positions, polarity)} from the newest snapshots in `directory`, for the
+    requests that have one."""
+    from tecs_gb300 import h5
+
+    out = {}
+    for idx in indices:
+        snap = h5.last_snapshot(directory, idx)
+        if snap is not None:
+            out[idx] = snap
+    return out
 
 
 def summarize(results: List[Result], makespan: float, cell_steps: int):

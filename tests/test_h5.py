@@ -64,3 +64,26 @@ def test_empty_dataset_and_int_types(tmp_path):
     f = h5.H5File(tmp_path / "e.h5")
     np.testing.assert_array_equal(f.read("static/cell_type"), np.arange(7))
     assert f.read("static/empty").shape == (0, 3)
+
+
+def test_last_snapshot_is_the_newest_group(tmp_path):
+    from tecs_gb300 import h5
+
+    sink = h5.SnapshotSink(tmp_path)
+    rng = np.random.default_rng(3)
+    pos = {k: rng.standard_normal((7, 3)).astype(np.float32) for k in (50, 100, 150)}
+    pol = {k: rng.standard_normal((7, 2)).astype(np.float32) for k in (50, 100, 150)}
+    for k in (50, 100, 150):
+        sink(4, k, pos[k], pol[k])
+    sink(5, 50, pos[50], None)
+    sink.close()
+    step, p, q = h5.last_snapshot(tmp_path, 4)
+    assert step == 150
+    np.testing.assert_array_equal(p, pos[150])
+    np.testing.assert_array_equal(q, pol[150])
+    step, p, q = h5.last_snapshot(tmp_path, 5)
+    assert step == 50 and q is None
+    np.testing.assert_array_equal(p, pos[50])
+    assert h5.last_snapshot(tmp_path, 6) is None  # no file
+    (tmp_path / "request_00007.h5").write_bytes(b"\0" * 64)  # a file never closed: no superblock
+    assert h5.last_snapshot(tmp_path, 7) is None

@@ -96,3 +96,29 @@ def test_size_classes_and_batched_issue_keep_results_and_snapshots(tmp_path):
 def test_size_classes_need_a_lane_for_any_request():
     with pytest.raises(ValueError):
         Server(cell_capacity=1000, bin_capacity=1000, size_classes=[(500, 1.0)])
+
+
+def test_resume_from_snapshots_gives_the_uninterrupted_results(tmp_path):
+    from tecs_gb300 import h5
+    from tecs_gb300.served import resume_points
+
+    reqs = wl.served_stream(6, seed=8, rate_hz=500.0, lo=800, hi=6000, steps_lo=90, steps_hi=140)
+    sink = h5.SnapshotSink(tmp_path)
+    srv = Server(cell_capacity=40000, bin_capacity=300000, max_sims=8, snapshot_every=40, sink=sink,
+                 keep_results=True)
+    full = {r.index: r for r in srv.run(reqs)}
+    srv.close()
+    sink.close()
+    # resume every request from its newest snapshot (step 40 or 80) in a fresh server
+    points = resume_points(tmp_path, range(len(reqs)))
+    assert set(points) == set(range(len(reqs))) and {s for s, _, _ in points.values()} <= {40, 80, 120}
+    srv2 = Server(cell_capacity=40000, bin_capacity=300000, max_sims=8, snapshot_every=40, sink=None,
+                  keep_results=True, size_classes=[(3000, 0.4), (None, 0.6)], steps_per_issue=8)
+    resumed = srv2.run(reqs, resume=points)
+    srv2.close()
+    assert len(resumed) == len(reqs)
+    assert srv2.cell_steps == sum(r.n * (r.steps - points[r.index][0]) for r in resumed)
+    for r in resumed:
+        np.testing.assert_array_equal(r.positions, full[r.index].positions)
+        if full[r.index].polarity is not None:
+            np.testing.assert_array_equal(r.polarity, full[r.index].polarity)
