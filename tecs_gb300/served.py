@@ -109,10 +109,12 @@ class Result:
 class SnapshotWriter(threading.Thread):
     """Waits for each snapshot's copy event, then hands the pinned buffer to the sink."""
 
-    def __init__(self, sink: Optional[Callable] = None):
+    def __init__(self, sink: Optional[Callable] = None, ready: Callable = Engine.event_ready,
+                 destroy: Callable = Engine.event_destroy):
         super().__init__(daemon=True)
         self.q = queue.Queue()
         self.sink = sink
+        self.ready, self.destroy = ready, destroy
         self.written = 0
         self.errors: List[str] = []
 
@@ -122,9 +124,9 @@ class SnapshotWriter(threading.Thread):
             if item is None:
                 return
             ev, req_index, step, pos, pol, release = item
-            while not Engine.event_ready(ev):
+            while not self.ready(ev):
                 time.sleep(0.0002)
-            Engine.event_destroy(ev)
+            self.destroy(ev)
             try:
                 if self.sink:
                     self.sink(req_index, step, pos, pol)
@@ -163,26 +165,23 @@ class Server:
     def __init__(self, cell_capacity: int, bin_capacity: int, max_sims: int = 1024, snapshot_every: int = 100,
                  dt: float = 0.05, sink: Optional[Callable] = None, keep_results: bool = False, device: int = 0,
                  size_classes=None, steps_per_issue: int = 1):
-        import torch
-
-        self.torch = torch
+        self.device = device
         classes = size_classes or [(None, 1.0)]
         if classes[-1][0] is not None:
             raise ValueError("the last size class must take any request (None)")
         self.lanes: List[Lane] = []
         for max_cells, share in classes:
             c, b = max(int(cell_capacity * share), 1), max(int(bin_capacity * share), 1)
-            self.lanes.append(Lane(Engine(c, b, max_sims, device), max_cells, c, b))
+            self.lanes.append(Lane(self._engine(c, b, max_sims), max_cells, c, b))
         self.engine = self.lanes[0].engine
-        self.streams = [torch.cuda.ExternalStream(l.engine.stream, device=torch.device("cuda", device))
-                        for l in self.lanes]
+        self.streams = [self._stream(l) for l in self.lanes]
         self.cell_capacity = cell_capacity
         self.bin_capacity = bin_capacity
         self.dt = dt
         self.snapshot_every = snapshot_every
-        self.writer = SnapshotWriter(sink)
+        self.writer = SnapshotWriter(sink, *self._event_ops())
         self.writer.start()
-        self.pool = PinnedPool()
+        self.pool = self._pool()
         self.keep_results = keep_results
         self.cell_steps = 0
         self.steps = 0
@@ -191,6 +190,29 @@ class Server:
 
     def lane_for(self, n: int) -> Lane:
         return next(l for l in self.lanes if l.takes(n))
+
+    # the device-facing pieces: a lane's engine and stream, an event recorded after its queued steps, the
+    # readiness test of a snapshot copy's event, pinned buffers
+    def _engine(self, cells: int, bins: int, max_sims: int):
+        return Engine(cells, bins, max_sims, self.device)
+
+    def _stream(self, lane: Lane):
+        import torch
+
+        return torch.cuda.ExternalStream(lane.engine.stream, device=torch.device("cuda", self.device))
+
+    def _record(self, stream):
+        import torch
+
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        return ev
+
+    def _event_ops(self):
+        return Engine.event_ready, Engine.event_destroy
+
+    def _pool(self):
+        return PinnedPool()
 
     @staticmethod
     def capacity_from_free_hbm(fraction: float = 0.5, bins_per_cell: float = 3.0):
@@ -297,9 +319,7 @@ class Server:
                     kk = min(kk, lv.req.steps - lv.steps_done, to_snap)
                 kk = max(kk, 1)
                 lane.engine.step(self.dt, kk)
-                ev = self.torch.cuda.Event()
-                ev.record(stream)
-                lane.pending.append(ev)
+                lane.pending.append(self._record(stream))
                 issued = True
                 self.steps += kk
                 for lv in lane.live.values():
