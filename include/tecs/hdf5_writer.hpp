@@ -10,7 +10,10 @@
 // object headers, symbol-table groups (version 1 B-tree, symbol table nodes,
 // local heaps), contiguous datasets with dataspace v1, datatype v1, fill
 // value v2 and layout v3 messages -- with the same byte layout as
-// tecs_gb300/h5.py's writer.  With Settings::write_xmf (the default) it also
+// tecs_gb300/h5.py's writer.  The file takes any number of writes: the root
+// group's B-tree gains levels (32 children per node) as its symbol table nodes
+// (8 groups each) grow, and its name heap moves to a segment twice the size
+// when it fills.  With Settings::write_xmf (the default) it also
 // writes the reference's XDMF sidecar "<path>.xmf" (hdf5_writer.hpp:134-287)
 // for visualisation tools: one temporal collection, a uniform grid per write
 // with the first view as geometry, the other views as node attributes (links
@@ -166,10 +169,11 @@ inline Bytes snod(const std::vector<Bytes>& entries) {
   return b;
 }
 
-inline Bytes btree(const std::vector<std::uint64_t>& keys, const std::vector<std::uint64_t>& children) {
-  Bytes b = {'T', 'R', 'E', 'E', 0, 0};
+inline Bytes btree(const std::vector<std::uint64_t>& keys, const std::vector<std::uint64_t>& children,
+                   unsigned level = 0, std::uint64_t left = kUndef, std::uint64_t right = kUndef) {
+  Bytes b = {'T', 'R', 'E', 'E', 0, static_cast<unsigned char>(level)};
   put<std::uint16_t>(b, static_cast<std::uint16_t>(children.size()));
-  put(b, kUndef); put(b, kUndef);
+  put(b, left); put(b, right);
   for (std::size_t k = 0; k < children.size(); ++k) { put(b, keys[k]); put(b, children[k]); }
   put(b, keys[children.size()]);
   zeros(b, kBtreeSize - b.size());
@@ -187,6 +191,7 @@ struct Heap {
   std::size_t size;
   Bytes data = Bytes(8, 0);  // offset 0: the empty name
   explicit Heap(std::size_t s) : size(s) {}
+  bool fits(const std::string& name) const { return data.size() + pad8(name.size() + 1) + 16 <= size; }
   std::uint64_t add(const std::string& name) {
     const std::uint64_t off = data.size();
     data.insert(data.end(), name.begin(), name.end());
@@ -195,14 +200,15 @@ struct Heap {
     if (data.size() + 16 > size) throw std::runtime_error("group name heap full");
     return off;
   }
-  // the full segment and its free-list head
-  std::pair<Bytes, std::uint64_t> segment() const {
-    Bytes out = data;
+  // the segment from `start` and the free-list head; full = false stops after the free block's header
+  // (what changes when a name is added to a segment whose rest is zero)
+  std::pair<Bytes, std::uint64_t> segment(std::size_t start = 0, bool full = true) const {
+    Bytes out(data.begin() + static_cast<std::ptrdiff_t>(start), data.end());
     const std::size_t free = size - data.size();
     if (free >= 16) {
       put<std::uint64_t>(out, 1);  // one free block, the last in the list
       put<std::uint64_t>(out, free);
-      zeros(out, free - 16);
+      if (full) zeros(out, free - 16);
       return {out, data.size()};
     }
     zeros(out, free);
@@ -274,8 +280,17 @@ class File {
     const Bytes goh = object_header({symbol_table_msg(bt, heap)}, 24);
     const std::uint64_t gaddr = alloc(goh.size());
     write_at(gaddr, goh);
-    groups_[group] = {heap_.add(group), gaddr, bt, heap};
-    write_root();
+    const bool moved = !heap_.fits(group);
+    if (moved) {  // a name segment twice the size at the end of the file
+      while (!heap_.fits(group)) heap_.size *= 2;
+      root_heap_data_ = alloc(heap_.size);
+    }
+    const std::uint64_t group_name = heap_.add(group);
+    groups_[group] = {group_name, gaddr, bt, heap};
+    const auto at = std::lower_bound(order_.begin(), order_.end(), group);
+    const std::size_t first = static_cast<std::size_t>(at - order_.begin());
+    order_.insert(at, group);
+    write_root(first, moved ? 0 : group_name);
     std::fflush(f_);
   }
 
@@ -307,29 +322,52 @@ class File {
     return b;
   }
 
-  void write_root() {
-    // groups in name order, in symbol table nodes of 8
-    std::vector<std::pair<std::string, Group>> ordered(groups_.begin(), groups_.end());
-    std::vector<std::vector<Bytes>> chunks;
-    for (std::size_t k = 0; k < ordered.size(); ++k) {
-      if (k % kSnodEntries == 0) chunks.emplace_back();
-      const Group& g = ordered[k].second;
-      chunks.back().push_back(entry(g.name_off, g.ohdr, g.btree, g.heap));
+  // The root group's metadata: its entries in name order in symbol table nodes of 8 (those before the
+  // node holding entry `first` are unchanged and not rewritten), a B-tree of 32 children per node that
+  // gains levels as the nodes grow (the root node stays at its fixed address), the name heap (from offset
+  // `heap_from`; 0: all of it).
+  void write_root(std::size_t first = 0, std::uint64_t heap_from = 0) {
+    const std::size_t n = order_.size();
+    const std::size_t nchunks = std::max<std::size_t>(1, (n + kSnodEntries - 1) / kSnodEntries);
+    while (snods_.size() < nchunks) snods_.push_back(alloc(kSnodSize));
+    for (std::size_t k = first / kSnodEntries; k < nchunks; ++k) {
+      std::vector<Bytes> chunk;
+      for (std::size_t i = k * kSnodEntries; i < std::min(n, (k + 1) * kSnodEntries); ++i) {
+        const Group& g = groups_.at(order_[i]);
+        chunk.push_back(entry(g.name_off, g.ohdr, g.btree, g.heap));
+      }
+      write_at(snods_[k], snod(chunk));
     }
-    if (chunks.empty()) chunks.emplace_back();
-    while (snods_.size() < chunks.size()) snods_.push_back(alloc(kSnodSize));
-    if (chunks.size() > 2 * kInternalK) throw std::runtime_error("too many groups for a one-level group B-tree");
+    // each child's largest name (heap offset); a node's keys: the bound left of its first child, then these
+    std::vector<std::uint64_t> children(snods_.begin(), snods_.begin() + nchunks), maxkey;
+    for (std::size_t k = 0; k < nchunks; ++k)
+      maxkey.push_back(n ? groups_.at(order_[std::min(n, (k + 1) * kSnodEntries) - 1]).name_off : 0);
+    unsigned level = 0;
+    constexpr std::size_t width = 2 * kInternalK;
+    while (children.size() > width) {
+      const std::size_t count = (children.size() + width - 1) / width;
+      if (nodes_.size() <= level) nodes_.emplace_back();
+      auto& addrs = nodes_[level];
+      while (addrs.size() < count) addrs.push_back(alloc(kBtreeSize));
+      std::vector<std::uint64_t> up;
+      for (std::size_t j = 0; j < count; ++j) {
+        const std::size_t lo = j * width, hi = std::min(children.size(), lo + width);
+        std::vector<std::uint64_t> keys = {j ? maxkey[lo - 1] : 0};
+        keys.insert(keys.end(), maxkey.begin() + lo, maxkey.begin() + hi);
+        write_at(addrs[j], btree(keys, std::vector<std::uint64_t>(children.begin() + lo, children.begin() + hi), level,
+                                 j ? addrs[j - 1] : kUndef, j + 1 < count ? addrs[j + 1] : kUndef));
+        up.push_back(maxkey[hi - 1]);
+      }
+      children.assign(addrs.begin(), addrs.begin() + count);
+      maxkey = up;
+      ++level;
+    }
     std::vector<std::uint64_t> keys = {0};
-    for (std::size_t k = 0; k < chunks.size(); ++k) {
-      write_at(snods_[k], snod(chunks[k]));
-      std::uint64_t last = 0;
-      if (!ordered.empty()) last = ordered[std::min(ordered.size() - 1, (k + 1) * kSnodEntries - 1)].second.name_off;
-      keys.push_back(last);
-    }
-    write_at(root_btree_, btree(keys, std::vector<std::uint64_t>(snods_.begin(), snods_.begin() + chunks.size())));
-    const auto [seg, free] = heap_.segment();
-    write_at(root_heap_, heap_header(kRootHeapData, free, root_heap_data_));
-    write_at(root_heap_data_, seg);
+    keys.insert(keys.end(), maxkey.begin(), maxkey.end());
+    write_at(root_btree_, btree(keys, children, level));
+    const auto [seg, free] = heap_.segment(heap_from, heap_from == 0);
+    write_at(root_heap_, heap_header(heap_.size, free, root_heap_data_));
+    write_at(root_heap_data_ + heap_from, seg);
     write_at(root_ohdr_, object_header({symbol_table_msg(root_btree_, root_heap_)}));
     write_at(0, superblock());
   }
@@ -338,7 +376,9 @@ class File {
   std::filesystem::path path_;
   Heap heap_;
   std::map<std::string, Group> groups_;
+  std::vector<std::string> order_;  // group names in name order
   std::vector<std::uint64_t> snods_;
+  std::vector<std::vector<std::uint64_t>> nodes_;  // B-tree nodes below the root, per level (leaf level first)
   std::uint64_t root_ohdr_ = 0, root_btree_ = 0, root_heap_ = 0, root_heap_data_ = 0, eof_ = 0;
 };
 
@@ -411,7 +451,7 @@ class HDF5_Writer {
     if (!xmf_.is_open()) return;
     // with active links the grid's topology is the links' polylines, else the cells as vertices
     bool links = false;
-    auto is_link = [&](const auto& v) {
+    [[maybe_unused]] auto is_link = [&](const auto& v) {  // unused when only the geometry is written
       using T = typename std::decay_t<decltype(v)>::value_type;
       if constexpr (std::is_same_v<T, Link>) links = links || v.get_active_count() != 0;
     };

@@ -14,11 +14,15 @@ reference's own fixture files (examples/data/sphere_ic.h5).
 
 Writer: snapshots are appended as they arrive (data and the new group's
 metadata at the end of the file; the root group's heap, symbol table nodes and
-B-tree live in fixed, pre-sized places and are rewritten in place), so a
-running simulation streams into one file.
+B-tree nodes are rewritten in place), so a running simulation streams into one
+file.  The root group takes any number of groups: its B-tree gains levels
+(32 children per node) as the symbol table nodes (8 entries each) grow, and
+its name heap moves to a segment twice the size when it fills, as the HDF5
+library does; the root node and the heap header stay where they are.
 """
 from __future__ import annotations
 
+import bisect
 import os
 import struct
 import threading
@@ -113,8 +117,8 @@ def _snod(entries: List[bytes]) -> bytes:
     return out + b"\0" * (SNOD_SIZE - len(out))
 
 
-def _btree(keys: List[int], children: List[int]) -> bytes:
-    out = b"TREE" + struct.pack("<BBHQQ", 0, 0, len(children), UNDEF, UNDEF)
+def _btree(keys: List[int], children: List[int], level: int = 0, left: int = UNDEF, right: int = UNDEF) -> bytes:
+    out = b"TREE" + struct.pack("<BBHQQ", 0, level, len(children), left, right)
     for k in range(len(children)):
         out += struct.pack("<QQ", keys[k], children[k])
     out += struct.pack("<Q", keys[len(children)])
@@ -132,6 +136,9 @@ class _Heap:
         self.size = size
         self.data = bytearray(8)  # offset 0: the empty name
 
+    def fits(self, name: str) -> bool:
+        return len(self.data) + _pad8(len(name.encode()) + 1) + 16 <= self.size
+
     def add(self, name: str) -> int:
         off = len(self.data)
         raw = name.encode() + b"\0"
@@ -140,13 +147,14 @@ class _Heap:
             raise ValueError("group name heap full")
         return off
 
-    def segment(self) -> Tuple[bytes, int]:
-        """(data bytes of the full segment, free-list head offset)"""
+    def segment(self, start: int = 0, full: bool = True) -> Tuple[bytes, int]:
+        """(data bytes of the segment from `start`, free-list head offset); full=False stops after the free
+        block's header (what changes when a name is added to a segment whose rest is zero)"""
         used = len(self.data)
         free = self.size - used
-        out = bytes(self.data)
+        out = bytes(self.data[start:])
         if free >= 16:
-            out += struct.pack("<QQ", 1, free) + b"\0" * (free - 16)  # one free block, last in list
+            out += struct.pack("<QQ", 1, free) + (b"\0" * (free - 16) if full else b"")  # one free block, last
             return out, used
         return out + b"\0" * free, UNDEF
 
@@ -161,6 +169,7 @@ class H5Writer:
         self.path = Path(path)
         self.f = open(self.path, "wb+")
         self.names: Dict[str, Tuple[int, int, int, int]] = {}  # group name -> (name_off, ohdr, btree, heap)
+        self.order: List[str] = []  # group names in name order
         self.heap = _Heap(ROOT_HEAP_DATA)
         # fixed metadata region: superblock, root object header, B-tree, heap header + data, first SNODs
         self.root_ohdr = 96                     # after the 96-byte superblock
@@ -168,6 +177,7 @@ class H5Writer:
         self.root_heap = self.root_btree + BTREE_SIZE
         self.root_heap_data = self.root_heap + 32
         self.snods: List[int] = []
+        self.nodes: List[List[int]] = []  # B-tree nodes below the root, per level (leaf level first)
         self.eof = self.root_heap_data + ROOT_HEAP_DATA
         self._write_root()
 
@@ -187,23 +197,42 @@ class H5Writer:
         sb += _entry(0, self.root_ohdr, self.root_btree, self.root_heap)
         return sb
 
-    def _write_root(self):
-        ordered = sorted(self.names.items())
-        entries = [_entry(v[0], v[1], v[2], v[3]) for _, v in ordered]
-        chunks = [entries[k:k + SNOD_ENTRIES] for k in range(0, len(entries), SNOD_ENTRIES)] or [[]]
-        while len(self.snods) < len(chunks):
+    def _write_root(self, first: int = 0, heap_from: int = 0):
+        """Rewrite the root group's metadata; symbol table nodes before the one holding name-order entry
+        `first`, and the name heap before offset `heap_from` (0: all of it), are unchanged and not
+        rewritten."""
+        n = len(self.order)
+        nchunks = max(1, -(-n // SNOD_ENTRIES))
+        while len(self.snods) < nchunks:
             self.snods.append(self._alloc(SNOD_SIZE))
-        if len(chunks) > 2 * INTERNAL_K:
-            raise ValueError("too many groups for a one-level group B-tree")
-        keys = [0]
-        for k, chunk in enumerate(chunks):
+        for k in range(first // SNOD_ENTRIES, nchunks):
+            chunk = [_entry(*self.names[g]) for g in self.order[k * SNOD_ENTRIES:(k + 1) * SNOD_ENTRIES]]
             self._write_at(self.snods[k], _snod(chunk))
-            last = ordered[min(len(ordered) - 1, (k + 1) * SNOD_ENTRIES - 1)][1][0] if ordered else 0
-            keys.append(last)
-        self._write_at(self.root_btree, _btree(keys, self.snods[: len(chunks)]))
-        seg, free = self.heap.segment()
-        self._write_at(self.root_heap, _heap_header(ROOT_HEAP_DATA, free, self.root_heap_data))
-        self._write_at(self.root_heap_data, seg)
+        # each child's largest name (heap offset); a node's keys: the bound left of its first child, then these
+        children = self.snods[:nchunks]
+        maxkey = [self.names[self.order[min(n, (k + 1) * SNOD_ENTRIES) - 1]][0] if n else 0 for k in range(nchunks)]
+        level = 0
+        while len(children) > 2 * INTERNAL_K:
+            width = 2 * INTERNAL_K
+            count = -(-len(children) // width)
+            if len(self.nodes) <= level:
+                self.nodes.append([])
+            addrs = self.nodes[level]
+            while len(addrs) < count:
+                addrs.append(self._alloc(BTREE_SIZE))
+            up = []
+            for j in range(count):
+                kids, keys = children[j * width:(j + 1) * width], maxkey[j * width:(j + 1) * width]
+                left_key = maxkey[j * width - 1] if j else 0
+                self._write_at(addrs[j], _btree([left_key] + keys, kids, level, addrs[j - 1] if j else UNDEF,
+                                                addrs[j + 1] if j + 1 < count else UNDEF))
+                up.append(keys[-1])
+            children, maxkey = addrs[:count], up
+            level += 1
+        self._write_at(self.root_btree, _btree([0] + maxkey, children, level))
+        seg, free = self.heap.segment(heap_from, full=heap_from == 0)
+        self._write_at(self.root_heap, _heap_header(self.heap.size, free, self.root_heap_data))
+        self._write_at(self.root_heap_data + heap_from, seg)
         self._write_at(self.root_ohdr, _object_header([_symbol_table_msg(self.root_btree, self.root_heap)]))
         self._write_at(0, self._superblock())
 
@@ -242,8 +271,16 @@ class H5Writer:
         gohdr = _object_header([_symbol_table_msg(btree, heap)], min_size=24)
         gaddr = self._alloc(len(gohdr))
         self._write_at(gaddr, gohdr)
-        self.names[group] = (self.heap.add(group), gaddr, btree, heap)
-        self._write_root()
+        moved = not self.heap.fits(group)
+        if moved:  # a segment twice the size at the end of the file
+            while not self.heap.fits(group):
+                self.heap.size *= 2
+            self.root_heap_data = self._alloc(self.heap.size)
+        name_off = self.heap.add(group)
+        self.names[group] = (name_off, gaddr, btree, heap)
+        at = bisect.bisect_left(self.order, group)
+        self.order.insert(at, group)
+        self._write_root(at, 0 if moved else name_off)
         self.f.flush()
 
     def close(self):

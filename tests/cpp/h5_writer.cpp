@@ -3,7 +3,10 @@
 // it back and compares it byte for byte with tecs_gb300.h5's writer.
 //
 //   h5_writer <path without extension>
+//   h5_writer <path without extension> <steps>   one write per step, t0 .. t<steps-1>, of a 2-cell position
+//                                                view (a long run, as the reference's examples write)
 #include <cstdio>
+#include <string>
 
 #include "tecs/tecs.hpp"
 
@@ -12,6 +15,16 @@ using namespace tecs;
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   io::HDF5_Writer<DefaultSimulationConfig> w(argv[1]);
+  if (argc >= 3) {
+    const unsigned steps = static_cast<unsigned>(std::stoul(argv[2]));
+    View<VectorN<float, 3>> pos("position", 2);
+    for (unsigned s = 0; s < steps; ++s) {
+      pos(0) = VectorN<float, 3>(float(s), -float(s), 0.5f * float(s));
+      pos(1) = VectorN<float, 3>(1.0f, float(s % 7), -2.0f);
+      w.write(0.05 * s, s, pos);
+    }
+    return 0;
+  }
   View<VectorN<float, 3>> pos0("position", 5);
   for (unsigned i = 0; i < 5; ++i) pos0(i) = VectorN<float, 3>(0.5f * i, -1.0f * i, 2.0f + i);
   View<Link> links("links", 3);

@@ -93,6 +93,36 @@ def test_hdf5_writer_matches_python_writer(tmp_path):
     np.testing.assert_array_equal(f.read("t1/polarity"), pol1)
 
 
+def test_hdf5_writer_long_run_matches_python_writer(tmp_path):
+    """A write per step for 2,001 steps (t0 .. t2000, as the reference's bending example writes): the root
+    group outgrows one B-tree node and its first name heap; both writers give the same bytes and every
+    group reads back.  The writes hold the geometry alone, as sim.write(t) does."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from tecs_gb300 import h5
+
+    src = Path(__file__).resolve().parent / "cpp" / "h5_writer.cpp"
+    exe = tmp_path / "h5_writer"
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    steps = 2001
+    assert subprocess.run([str(exe), str(tmp_path / "cxx"), str(steps)]).returncode == 0
+
+    def pos(s):
+        return np.array([[s, -np.float32(s), np.float32(0.5) * np.float32(s)], [1.0, s % 7, -2.0]], np.float32)
+
+    w = h5.H5Writer(tmp_path / "py.h5")
+    for s in range(steps):
+        w.write_group(f"t{s}", {"position": pos(s)})
+    w.close()
+    assert (tmp_path / "cxx.h5").read_bytes() == (tmp_path / "py.h5").read_bytes()
+    f = h5.H5File(tmp_path / "cxx.h5")
+    assert f.keys() == sorted(f"t{s}" for s in range(steps))
+    for s in (0, 9, 10, 99, 100, 256, 257, 999, 1000, 1999, 2000):
+        np.testing.assert_array_equal(f.read(f"t{s}/position"), pos(s))
+
+
 @pytest.mark.parametrize("name", ["lk_writer", "lk_writer_nolinks"])
 def test_xdmf_sidecar_matches_reference(tmp_path, name):
     """io::HDF5_Writer's "<path>.xmf" equals, byte for byte, the reference writer's sidecar for the

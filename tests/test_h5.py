@@ -87,3 +87,66 @@ def test_last_snapshot_is_the_newest_group(tmp_path):
     assert h5.last_snapshot(tmp_path, 6) is None  # no file
     (tmp_path / "request_00007.h5").write_bytes(b"\0" * 64)  # a file never closed: no superblock
     assert h5.last_snapshot(tmp_path, 7) is None
+
+
+def _root_tree(path):
+    """The root group's B-tree as [(level, left sibling, right sibling, keys as names, children)] per node,
+    top down, and the heap's name at each key."""
+    import struct
+
+    b = Path(path).read_bytes()
+    btree, heap = struct.unpack_from("<QQ", b, 56 + 24)  # the scratch pad of the superblock's root entry
+    assert b[heap:heap + 4] == b"HEAP"
+    size, _, data = struct.unpack_from("<QQQ", b, heap + 8)
+
+    def name(off):
+        assert off < size
+        return b[data + off:b.index(b"\0", data + off)].decode()
+
+    levels = {}
+
+    def walk(node):
+        assert b[node:node + 4] == b"TREE"
+        _, level, used, left, right = struct.unpack_from("<BBHQQ", b, node + 4)
+        keys = [name(struct.unpack_from("<Q", b, node + 24 + 16 * k)[0]) for k in range(used + 1)]
+        kids = [struct.unpack_from("<Q", b, node + 32 + 16 * k)[0] for k in range(used)]
+        levels.setdefault(level, []).append((node, left, right))
+        names = []
+        for k, c in enumerate(kids):
+            if level:
+                sub = walk(c)
+            else:
+                assert b[c:c + 4] == b"SNOD"
+                nsym = struct.unpack_from("<H", b, c + 6)[0]
+                sub = [name(struct.unpack_from("<Q", b, c + 8 + 40 * e)[0]) for e in range(nsym)]
+            # the library's lookup rule: a child holds the names above its left key and up to its right key
+            assert all(keys[k].encode() < s.encode() <= keys[k + 1].encode() for s in sub)
+            assert sub[-1] == keys[k + 1]
+            names += sub
+        return names
+
+    names = walk(btree)
+    return b[btree + 5], levels, names
+
+
+@pytest.mark.parametrize("count, fmt", [(300, "t{}"), (2001, "t{}"), (9000, "t{:05d}")])
+def test_root_group_takes_any_number_of_groups(tmp_path, count, fmt):
+    """Past 256 groups (32 symbol table nodes) the root B-tree gains a level, past 8,192 a second, and
+    past 1,024 short names the name heap moves to a larger segment; every node keeps the library's key
+    rule and sibling links, and every group reads back."""
+    w = h5.H5Writer(tmp_path / "long.h5")
+    for s in range(count):
+        w.write_group(fmt.format(s), {"position": np.full((1, 3), s, np.float32)})
+    w.close()
+    top, levels, names = _root_tree(tmp_path / "long.h5")
+    want = sorted((fmt.format(s) for s in range(count)), key=str.encode)
+    assert names == want
+    assert top == (0 if count <= 256 else 1 if count <= 8192 else 2)
+    for level, nodes in levels.items():
+        for j, (node, left, right) in enumerate(nodes):
+            assert left == (nodes[j - 1][0] if j else h5.UNDEF)
+            assert right == (nodes[j + 1][0] if j + 1 < len(nodes) else h5.UNDEF)
+    f = h5.H5File(tmp_path / "long.h5")
+    assert f.keys() == sorted(want)
+    for s in (0, count // 3, count - 1):
+        np.testing.assert_array_equal(f.read(fmt.format(s) + "/position"), np.full((1, 3), s, np.float32))
