@@ -405,32 +405,108 @@ class H5File:
 
 
 # ---------------------------------------------------------------------------
+# XDMF sidecar
+
+class XdmfSidecar:
+    """The XDMF sidecar "<path>.xmf" of the snapshot file "<path>.h5", for visualisation tools, in the
+    reference writer's text (include/io/hdf5_writer.hpp:134-287): one temporal collection; per write a
+    uniform grid whose geometry is the first field, the others node attributes ("Scalar" for one column,
+    "Vector" for 2 or 3, "Tensor" for 9, else "Matrix"), a links field the grid's polyline topology in
+    place of the cells as vertices; the static fields in every later grid.  Text is kept until it passes
+    `threshold` characters, then appended to the file; close() ends the document."""
+
+    def __init__(self, path: str | os.PathLike, threshold: int = 65536):
+        path = Path(path)
+        self.file = path.name + ".h5"
+        self.f = open(str(path) + ".xmf", "w", newline="\n")
+        self.threshold = threshold
+        self.buf = ('<?xml version="1.0"?>\n<Xdmf Version="3.0">\n\t<Domain>\n'
+                    '\t\t<Grid Name="Agents" GridType="Collection" CollectionType="Temporal">\n')
+        self.static = ""
+
+    def _item(self, group: str, label: str, arr: np.ndarray, link: bool = False) -> str:
+        if len(arr) == 0:
+            return ""
+        cols = arr.shape[1] if arr.ndim > 1 else 0
+        dims = f"{len(arr)} " + (f"{cols} " if cols else "")
+        kind = "Scalar" if not cols else "Vector" if cols in (2, 3) else "Tensor" if cols == 9 else "Matrix"
+        if link:
+            out = (f'\t\t\t\t<Topology TopologyType="Polyline" NumberOfElements="{len(arr)}">\n'
+                   '\t\t\t\t\t<DataItem Format="HDF" DataType="UInt32"')
+        else:
+            out = (f'\t\t\t\t<Attribute Name="{label}" AttributeType="{kind}" Center="Node">\n'
+                   '\t\t\t\t\t<DataItem Format="HDF"')
+        out += f' Dimensions="{dims}">\n\t\t\t\t\t\t{self.file}:{group}/{label}\n\t\t\t\t\t</DataItem>\n'
+        return out + ("\t\t\t\t</Topology>\n" if link else "\t\t\t\t</Attribute>\n")
+
+    def write(self, time: float, group: str, fields: List[Tuple[str, np.ndarray]], links: Tuple[str, ...] = ()):
+        """One grid: `fields` in write order, the first the geometry; names in `links` are link fields."""
+        (glabel, geom), rest = fields[0], fields[1:]
+        n, d = len(geom), geom.shape[1]
+        has_links = any(label in links and len(a) for label, a in rest)
+        b = f'\t\t\t<Grid Name="{group}" GridType="Uniform">\n\t\t\t\t<Time Value="{time:f}'
+        if not has_links:
+            b += f'"/>\n\t\t\t\t<Topology TopologyType="Polyvertex" NumberOfElements="{n}'
+        b += f'"/>\n\t\t\t\t<Geometry GeometryType="{"X" if d == 1 else "XY" if d == 2 else "XYZ"}">\n'
+        b += f'\t\t\t\t\t<DataItem Format="HDF" Dimensions="{n} {d}">\n\t\t\t\t\t\t{self.file}:{group}/{glabel}\n'
+        b += "\t\t\t\t\t</DataItem>\n\t\t\t\t</Geometry>\n"
+        for label, a in rest:
+            b += self._item(group, label, a, label in links)
+        self.buf += b + self.static + "\t\t\t</Grid>\n"
+        if len(self.buf) > self.threshold:
+            self.f.write(self.buf)
+            self.f.flush()
+            self.buf = ""
+
+    def write_static(self, fields: List[Tuple[str, np.ndarray]]):
+        for label, a in fields:
+            self.static += self._item("static", label, a)
+
+    def close(self):
+        if self.f:
+            self.f.write(self.buf + "\t\t</Grid>\n\t</Domain>\n</Xdmf>\n")
+            self.f.close()
+            self.f = None
+
+
+# ---------------------------------------------------------------------------
 # snapshot sink used by the served loop
 
 class SnapshotSink:
-    """One HDF5 file per request, one t<step> group per snapshot (position, polarity)."""
+    """One HDF5 file per request, request_<index>.h5, one t<step> group per snapshot (position, polarity).
+    With dt (the step's time) it also writes each file's XDMF sidecar, request_<index>.xmf, with time
+    step * dt per grid."""
 
-    def __init__(self, directory: str | os.PathLike):
+    def __init__(self, directory: str | os.PathLike, dt: Optional[float] = None):
         self.dir = Path(directory)
         self.dir.mkdir(parents=True, exist_ok=True)
+        self.dt = dt
         self.files: Dict[int, H5Writer] = {}
+        self.sidecars: Dict[int, XdmfSidecar] = {}
         self.lock = threading.Lock()
 
     def __call__(self, request: int, step: int, positions: np.ndarray, polarity: Optional[np.ndarray]):
         with self.lock:
             w = self.files.get(request)
             if w is None:
-                w = self.files[request] = H5Writer(self.dir / f"request_{request:05d}.h5")
-        ds = {"position": positions}
-        if polarity is not None:
-            ds["polarity"] = polarity
-        w.write_group(f"t{step}", ds)
+                base = self.dir / f"request_{request:05d}"
+                w = self.files[request] = H5Writer(str(base) + ".h5")
+                if self.dt is not None:
+                    self.sidecars[request] = XdmfSidecar(base)
+            x = self.sidecars.get(request)
+        fields = [("position", positions)] + ([("polarity", polarity)] if polarity is not None else [])
+        w.write_group(f"t{step}", dict(fields))
+        if x is not None:
+            x.write(step * self.dt, f"t{step}", fields)
 
     def close(self):
         with self.lock:
             for w in self.files.values():
                 w.close()
+            for x in self.sidecars.values():
+                x.close()
             self.files.clear()
+            self.sidecars.clear()
 
 
 def last_snapshot(directory: str | os.PathLike, request: int):

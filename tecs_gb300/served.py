@@ -7,7 +7,8 @@ the GPU's free HBM), so requests that arrive while others are on the GPU join
 the very next step and share every step's kernel launches with them.  Each
 simulation's state stays on the device; every `snapshot_every` steps it is
 unpacked on the device and copied to pinned host memory on a side stream, and
-a writer thread stores it (HDF5 via tecs_gb300.h5) without stalling the steps.
+a writer thread stores it (HDF5 via tecs_gb300.h5, with the XDMF sidecar when
+the sink is given the step's time) without stalling the steps.
 A simulation that reaches its step count is downloaded, retired, and its
 time-to-completion (arrival -> result on the host) recorded.
 
@@ -437,8 +438,9 @@ def bench_main(args):
     cells, bins = Server.capacity_from_free_hbm(0.4)
     out_dir = Path(os.environ.get("TECS_SNAPSHOT_DIR", "/tmp/tecs_snapshots"))
     out_dir.mkdir(parents=True, exist_ok=True)
-    sink = h5.SnapshotSink(out_dir)
-    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, sink=sink, size_classes=BENCH_SIZE_CLASSES,
+    dt = 0.05
+    sink = h5.SnapshotSink(out_dir, dt=dt)  # HDF5 files and their XDMF sidecars
+    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, dt=dt, sink=sink, size_classes=BENCH_SIZE_CLASSES,
                  steps_per_issue=8)
     res = srv.run(reqs, time_scale=args.time_scale)
     summ = summarize(res, srv.makespan, srv.cell_steps)
@@ -453,7 +455,7 @@ def bench_main(args):
     plain_v, rows = plain_sample(reqs)
     plain_lat = plain_fcfs_latency(reqs, rows, args.time_scale)
     # capacity: the same stream with arrivals compressed 100 times (compute-bound)
-    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, sink=None,
+    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, dt=dt, sink=None,
                      size_classes=BENCH_SIZE_CLASSES, steps_per_issue=8)
     cap_res = cap_srv.run(reqs, time_scale=100.0)
     cap = summarize(cap_res, cap_srv.makespan, cap_srv.cell_steps)

@@ -150,3 +150,56 @@ def test_root_group_takes_any_number_of_groups(tmp_path, count, fmt):
     assert f.keys() == sorted(want)
     for s in (0, count // 3, count - 1):
         np.testing.assert_array_equal(f.read(fmt.format(s) + "/position"), np.full((1, 3), s, np.float32))
+
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("name", ["lk_writer", "lk_writer_nolinks"])
+def test_xdmf_sidecar_matches_reference(tmp_path, name):
+    """XdmfSidecar gives, byte for byte, the reference writer's sidecar for its write sequence:
+    write_static(cell_type), then (position, polarity, links) at t = 0, dt, 2 dt; with links each grid's
+    topology is the links' polylines, without them the cells as vertices."""
+    g = dict(np.load(GOLDEN / f"{name}.npz"))
+    n, dt = len(g["x0"]), float(g["dt"])
+    x = h5.XdmfSidecar(tmp_path / "out", threshold=1000)  # several partial writes before the end
+    x.write_static([("cell_type", np.zeros(n, np.float32))])
+    for k in range(int(g["steps"]) + 1):
+        x.write(k * dt, f"t{k}", [("position", g["x0"]), ("polarity", g["p0"]), ("links", g["links"])],
+                links=("links",))
+    x.close()
+    assert (tmp_path / "out.xmf").read_bytes() == (GOLDEN / f"{name}.xmf").read_bytes()
+
+
+def test_snapshot_sink_sidecar_points_at_its_datasets(tmp_path):
+    import xml.etree.ElementTree as ET
+
+    sink = h5.SnapshotSink(tmp_path, dt=0.05)
+    rng = np.random.default_rng(5)
+    data = {}
+    for req, pol in ((2, True), (7, False)):
+        for step in (100, 200, 300):
+            x = rng.standard_normal((11 + req, 3)).astype(np.float32)
+            p = rng.standard_normal((11 + req, 2)).astype(np.float32) if pol else None
+            sink(req, step, x, p)
+            data[(req, step)] = (x, p)
+    sink.close()
+    for req in (2, 7):
+        root = ET.parse(tmp_path / f"request_{req:05d}.xmf").getroot()
+        grids = root.find("Domain").find("Grid").findall("Grid")
+        assert [gr.get("Name") for gr in grids] == ["t100", "t200", "t300"]
+        f = h5.H5File(tmp_path / f"request_{req:05d}.h5")
+        for gr in grids:
+            step = int(gr.get("Name")[1:])
+            assert gr.find("Time").get("Value") == f"{step * 0.05:f}"
+            assert gr.find("Topology").get("TopologyType") == "Polyvertex"
+            items = gr.iter("DataItem")
+            for item in items:
+                fname, path = item.text.strip().split(":")
+                assert fname == f"request_{req:05d}.h5"
+                arr = f.read(path)
+                assert [int(v) for v in item.get("Dimensions").split()] == list(arr.shape)
+            x, p = data[(req, step)]
+            np.testing.assert_array_equal(f.read(f"t{step}/position"), x)
+            names = [a.get("Name") for a in gr.findall("Attribute")]
+            assert names == (["polarity"] if p is not None else [])
