@@ -512,8 +512,10 @@ class SnapshotSink:
 def last_snapshot(directory: str | os.PathLike, request: int):
     """(step, positions, polarity or None) of the newest snapshot SnapshotSink wrote for a request, or None.
 
-    A file the writer never closed (a server that stopped mid-run) has no
-    superblock yet and is not a snapshot: None."""
+    A file whose writer stopped mid-run (a server that never closed it) holds
+    every group written before the stop: each write rewrites and flushes the
+    root metadata after the group's data.  A file with no group, or that does
+    not parse, gives None."""
     path = Path(directory) / f"request_{request:05d}.h5"
     if not path.exists():
         return None

@@ -85,13 +85,27 @@ def test_last_snapshot_is_the_newest_group(tmp_path):
     assert step == 50 and q is None
     np.testing.assert_array_equal(p, pos[50])
     assert h5.last_snapshot(tmp_path, 6) is None  # no file
-    (tmp_path / "request_00007.h5").write_bytes(b"\0" * 64)  # a file never closed: no superblock
+    (tmp_path / "request_00007.h5").write_bytes(b"\0" * 64)  # not an HDF5 file
     assert h5.last_snapshot(tmp_path, 7) is None
 
 
+def test_last_snapshot_of_a_file_whose_writer_stopped(tmp_path):
+    """A server that stops mid-run leaves its files unclosed; every group written before the stop is
+    complete on disk (each write rewrites and flushes the root metadata), so the newest one resumes."""
+    w = h5.H5Writer(tmp_path / "request_00003.h5")
+    assert h5.last_snapshot(tmp_path, 3) is None  # no group yet
+    pos = {k: np.full((5, 3), k, np.float32) for k in (100, 200, 300)}
+    for k in (100, 200, 300):
+        w.write_group(f"t{k}", {"position": pos[k]})
+        step, p, q = h5.last_snapshot(tmp_path, 3)
+        assert step == k and q is None
+        np.testing.assert_array_equal(p, pos[k])
+    w.f.close()  # the process ends without close(): no final truncation
+
+
 def _root_tree(path):
-    """The root group's B-tree as [(level, left sibling, right sibling, keys as names, children)] per node,
-    top down, and the heap's name at each key."""
+    """(the root node's level, {level: [(node, left sibling, right sibling)] left to right}, the group
+    names in tree order); asserts each node's keys bound its children's names."""
     import struct
 
     b = Path(path).read_bytes()
