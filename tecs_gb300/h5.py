@@ -163,11 +163,16 @@ class _Heap:
 # writer
 
 class H5Writer:
-    """Append-only HDF5 file of groups of float32 datasets (t<step>/<field>)."""
+    """Append-only HDF5 file of groups of float32 datasets (t<step>/<field>).
 
-    def __init__(self, path: str | os.PathLike):
+    append=True continues a file this writer made (closed, or left by a writer that stopped mid-run) with
+    the state it had after its last complete group, so the file ends as if one writer had written every
+    group; a missing or empty file is created."""
+
+    def __init__(self, path: str | os.PathLike, append: bool = False):
         self.path = Path(path)
-        self.f = open(self.path, "wb+")
+        resume = append and self.path.exists() and self.path.stat().st_size > 0
+        self.f = open(self.path, "rb+" if resume else "wb+")
         self.names: Dict[str, Tuple[int, int, int, int]] = {}  # group name -> (name_off, ohdr, btree, heap)
         self.order: List[str] = []  # group names in name order
         self.heap = _Heap(ROOT_HEAP_DATA)
@@ -179,7 +184,44 @@ class H5Writer:
         self.snods: List[int] = []
         self.nodes: List[List[int]] = []  # B-tree nodes below the root, per level (leaf level first)
         self.eof = self.root_heap_data + ROOT_HEAP_DATA
-        self._write_root()
+        if resume:
+            self._load()
+        else:
+            self._write_root()
+
+    def _load(self):
+        """The writer's state from the root metadata of a file it wrote (the superblock, written last by
+        every group write, holds the end of the last complete group)."""
+        self.f.seek(0)
+        b = self.f.read()
+        if b[:8] != SIG or struct.unpack_from("<QII", b, 64) != (self.root_ohdr, 1, 0) or \
+                struct.unpack_from("<QQ", b, 80) != (self.root_btree, self.root_heap):
+            raise ValueError(f"{self.path} was not written by this writer")
+        self.eof = struct.unpack_from("<Q", b, 40)[0]
+        size, free, data = struct.unpack_from("<QQQ", b, self.root_heap + 8)
+        self.heap = _Heap(size)
+        self.heap.data = bytearray(b[data:data + (size if free == UNDEF else free)])
+        self.root_heap_data = data
+
+        def walk(node):
+            _, level, used = struct.unpack_from("<BBH", b, node + 4)
+            for k in range(used):
+                child = struct.unpack_from("<Q", b, node + 32 + 16 * k)[0]
+                if level:
+                    while len(self.nodes) < level:
+                        self.nodes.append([])
+                    self.nodes[level - 1].append(child)
+                    walk(child)
+                else:
+                    self.snods.append(child)
+
+        walk(self.root_btree)
+        for sn in self.snods:
+            for e in range(struct.unpack_from("<H", b, sn + 6)[0]):
+                name_off, ohdr, _, _, btree, heap = struct.unpack_from("<QQIIQQ", b, sn + 8 + ENTRY_SIZE * e)
+                name = b[data + name_off:b.index(b"\0", data + name_off)].decode()
+                self.names[name] = (name_off, ohdr, btree, heap)
+                self.order.append(name)
 
     def _write_at(self, addr: int, data: bytes):
         self.f.seek(addr)
@@ -370,12 +412,19 @@ class H5File:
     def keys(self, path: str = "/") -> List[str]:
         return sorted(self._group_entries(self._resolve(path)))
 
-    def read(self, path: str) -> np.ndarray:
-        msgs = dict(self._messages(self._resolve(path)))
+    @staticmethod
+    def _shape(msgs) -> Tuple[int, ...]:
         ds = msgs[0x0001]
         ver, rank = ds[0], ds[1]
         off = 8 if ver == 1 else 4
-        shape = tuple(struct.unpack_from("<Q", ds, off + 8 * k)[0] for k in range(rank))
+        return tuple(struct.unpack_from("<Q", ds, off + 8 * k)[0] for k in range(rank))
+
+    def shape(self, path: str) -> Tuple[int, ...]:
+        return self._shape(dict(self._messages(self._resolve(path))))
+
+    def read(self, path: str) -> np.ndarray:
+        msgs = dict(self._messages(self._resolve(path)))
+        shape = self._shape(msgs)
         dt = msgs[0x0003]
         cls = dt[0] & 0x0F
         size = struct.unpack_from("<I", dt, 4)[0]
@@ -475,12 +524,14 @@ class XdmfSidecar:
 class SnapshotSink:
     """One HDF5 file per request, request_<index>.h5, one t<step> group per snapshot (position, polarity).
     With dt (the step's time) it also writes each file's XDMF sidecar, request_<index>.xmf, with time
-    step * dt per grid."""
+    step * dt per grid.  append=True (a server resuming requests from their snapshots) continues existing
+    files instead of starting them afresh, and their sidecars list the earlier snapshots too."""
 
-    def __init__(self, directory: str | os.PathLike, dt: Optional[float] = None):
+    def __init__(self, directory: str | os.PathLike, dt: Optional[float] = None, append: bool = False):
         self.dir = Path(directory)
         self.dir.mkdir(parents=True, exist_ok=True)
         self.dt = dt
+        self.append = append
         self.files: Dict[int, H5Writer] = {}
         self.sidecars: Dict[int, XdmfSidecar] = {}
         self.lock = threading.Lock()
@@ -490,9 +541,15 @@ class SnapshotSink:
             w = self.files.get(request)
             if w is None:
                 base = self.dir / f"request_{request:05d}"
-                w = self.files[request] = H5Writer(str(base) + ".h5")
+                w = self.files[request] = H5Writer(str(base) + ".h5", append=self.append)
                 if self.dt is not None:
-                    self.sidecars[request] = XdmfSidecar(base)
+                    x = self.sidecars[request] = XdmfSidecar(base)
+                    if w.order:  # a continued file: its earlier snapshots' grids first, in step order
+                        f = H5File(str(base) + ".h5")
+                        for g in sorted(w.order, key=lambda g: int(g[1:])):
+                            names = [nm for nm in ("position", "polarity") if nm in f.keys(g)]
+                            x.write(int(g[1:]) * self.dt, g, [(nm, np.empty(f.shape(f"{g}/{nm}"), np.float32))
+                                                             for nm in names])
             x = self.sidecars.get(request)
         fields = [("position", positions)] + ([("polarity", polarity)] if polarity is not None else [])
         w.write_group(f"t{step}", dict(fields))

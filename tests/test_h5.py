@@ -217,3 +217,59 @@ def test_snapshot_sink_sidecar_points_at_its_datasets(tmp_path):
             np.testing.assert_array_equal(f.read(f"t{step}/position"), x)
             names = [a.get("Name") for a in gr.findall("Attribute")]
             assert names == (["polarity"] if p is not None else [])
+
+
+@pytest.mark.parametrize("first, closed", [(5, True), (300, True), (300, False), (0, True)])
+def test_append_continues_as_one_writer(tmp_path, first, closed):
+    """A file continued with append=True -- after a clean close, or after a writer that stopped mid-run --
+    ends byte for byte as one writer's file of all the groups (here past one B-tree node and the first
+    name heap)."""
+    total = first + 80 if first < 300 else 2100
+
+    def group(s):
+        return {"position": np.full((1 + s % 3, 3), s, np.float32)}
+
+    one = h5.H5Writer(tmp_path / "one.h5")
+    for s in range(total):
+        one.write_group(f"t{s}", group(s))
+    one.close()
+    w = h5.H5Writer(tmp_path / "two.h5")
+    for s in range(first):
+        w.write_group(f"t{s}", group(s))
+    if closed:
+        w.close()
+    else:
+        w.f.close()
+    w = h5.H5Writer(tmp_path / "two.h5", append=True)
+    assert w.order == sorted(f"t{s}" for s in range(first))
+    for s in range(first, total):
+        w.write_group(f"t{s}", group(s))
+    w.close()
+    assert (tmp_path / "two.h5").read_bytes() == (tmp_path / "one.h5").read_bytes()
+
+
+def test_append_refuses_a_foreign_file(tmp_path):
+    p = tmp_path / "x.h5"
+    p.write_bytes(b"not hdf5" * 20)
+    with pytest.raises(ValueError, match="not written by this writer"):
+        h5.H5Writer(p, append=True)
+
+
+def test_sink_append_keeps_earlier_snapshots_and_sidecar(tmp_path):
+    """A resumed server's sink continues each request's file; file and sidecar end as one run's."""
+    pos = {k: np.full((4, 3), k, np.float32) for k in (100, 200, 300, 400)}
+    pol = {k: np.full((4, 2), -k, np.float32) for k in (100, 200, 300, 400)}
+    one = h5.SnapshotSink(tmp_path / "one", dt=0.05)
+    for k in (100, 200, 300, 400):
+        one(9, k, pos[k], pol[k])
+    one.close()
+    two = h5.SnapshotSink(tmp_path / "two", dt=0.05)
+    for k in (100, 200):
+        two(9, k, pos[k], pol[k])
+    two.files[9].f.close()  # the server stops: the file is left unclosed, the sidecar unwritten
+    two = h5.SnapshotSink(tmp_path / "two", dt=0.05, append=True)
+    for k in (300, 400):
+        two(9, k, pos[k], pol[k])
+    two.close()
+    for name in ("request_00009.h5", "request_00009.xmf"):
+        assert (tmp_path / "two" / name).read_bytes() == (tmp_path / "one" / name).read_bytes()

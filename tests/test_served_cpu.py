@@ -11,7 +11,8 @@ bookkeeping around the engine calls:
 - admission waits, first come first served, for free cells and bins;
 - no lane queues more than IN_FLIGHT steps;
 - a resumed request runs only its remaining steps and ends where the
-  uninterrupted run does.
+  uninterrupted run does, and an appending sink leaves its snapshot files as
+  one run's.
 The same loop over the CUDA engine is covered by the GPU tests.
 """
 import ctypes
@@ -298,3 +299,31 @@ def test_a_failing_sink_loses_only_that_snapshot():
     check_results(reqs, res)
     assert (1, 20) not in sink.got and (1, 30) in sink.got
     assert srv.writer.errors == ["request 1 step 20: disk full"]
+
+
+def test_resumed_server_continues_its_snapshot_files(tmp_path):
+    """A server stops after step 25 of each request; a new one resumes them from their newest snapshots
+    with an appending sink.  Each request's HDF5 file and XDMF sidecar end byte for byte as those of one
+    uninterrupted run."""
+    import dataclasses
+
+    from tecs_gb300 import h5
+
+    reqs = stream([(300, 47), (1200, 40), (150, 33)])
+    one = h5.SnapshotSink(tmp_path / "one", dt=DT)
+    serve(reqs, sink=one)
+    one.close()
+    first = h5.SnapshotSink(tmp_path / "two", dt=DT)
+    serve([dataclasses.replace(r, steps=25) for r in reqs], sink=first)  # stops after step 25
+    for w in first.files.values():
+        w.f.close()  # left unclosed, as by a server that stopped
+    resume = served.resume_points(tmp_path / "two", range(len(reqs)))
+    assert {i: r[0] for i, r in resume.items()} == {0: 20, 1: 20, 2: 20}
+    again = h5.SnapshotSink(tmp_path / "two", dt=DT, append=True)
+    _, res = serve(reqs, sink=again, resume=resume, steps_per_issue=8)
+    again.close()
+    check_results(reqs, res)
+    for i in range(len(reqs)):
+        for ext in ("h5", "xmf"):
+            name = f"request_{i:05d}.{ext}"
+            assert (tmp_path / "two" / name).read_bytes() == (tmp_path / "one" / name).read_bytes(), name
