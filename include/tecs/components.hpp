@@ -12,6 +12,7 @@
 //   integrators::Euler, Heun                      include/integrators/{euler,heun}.hpp
 //   com_fixers::NoComFixer, GlobalComFixer        include/com_fixers/com_fixers.hpp:11-45
 //   forces::Spring2R, PolaritySpring              the built-in pairwise laws
+//   forces::Spring, PiecewiseLinear (+Potential)  the force functions of user laws
 #ifndef TECS_CXX_COMPONENTS_HPP
 #define TECS_CXX_COMPONENTS_HPP
 
@@ -109,6 +110,35 @@ struct GlobalComFixer {
 }  // namespace com_fixers
 
 namespace forces {
+// The reference's predefined force functions for pairwise laws written as
+// PAIRWISE_FORCE lambdas (include/forces/predefined.hpp:60-144), with its
+// operation order: a vector displacement * F / distance, zero at distance 0.
+template <typename Scalar>
+TECS_HD Scalar SpringPotential(const Scalar distance, const Scalar homeostatic_radius, const Scalar scale = Scalar(1)) {
+  return scale * (homeostatic_radius - distance);
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector Spring(const Vector& displacement, const Scalar distance, const Scalar homeostatic_radius,
+                      const Scalar scale = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = SpringPotential(distance, homeostatic_radius, scale);
+  return displacement * F / distance;
+}
+template <typename Scalar>
+TECS_HD Scalar PiecewiseLinearPotential(const Scalar distance, const Scalar homeostatic_radius,
+                                        const Scalar repulsion_scale = Scalar(1),
+                                        const Scalar adhesion_scale = Scalar(1)) {
+  return repulsion_scale * tecs::detail::fmax_(homeostatic_radius - distance, Scalar(0)) -
+         adhesion_scale * tecs::detail::fmax_(distance - homeostatic_radius, Scalar(0));
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector PiecewiseLinear(const Vector& displacement, const Scalar distance, const Scalar homeostatic_radius,
+                               const Scalar repulsion_scale = Scalar(1), const Scalar adhesion_scale = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = PiecewiseLinearPotential(distance, homeostatic_radius, repulsion_scale, adhesion_scale);
+  return displacement * F / distance;
+}
+
 // Built-in pairwise force laws.  A pair at distance d < cutoff gets
 // displacement * F(d) / d (zero at d == 0) with
 //   F(d) = k_rep * max(r_rep - d, 0) - k_adh * max(d - r_adh, 0),

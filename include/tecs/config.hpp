@@ -16,6 +16,7 @@
 #include <string_view>
 
 #include "components.hpp"
+#include "random.hpp"
 #include "vector.hpp"
 
 namespace tecs {
@@ -44,6 +45,20 @@ struct Field {
 template <typename... Fs>
 struct FieldList {
   static constexpr std::size_t size = sizeof...(Fs);
+};
+
+// What a force law sees of one field (include/forces/detail.hpp:185-206): a
+// config's ForceFields<Ref> has one such member per field, named as the field.
+template <typename T>
+struct GenericFieldRef {
+  const T& self;  // the agent's value
+  T& delta;       // its delta, written by the law
+};
+template <typename T>
+struct PairwiseFieldRef {
+  const T& self;   // agent i's value
+  const T& other;  // agent j's value
+  T& delta;        // i's delta, written by the law
 };
 
 // bind a finder template to the config's position view, scalar and dimensions
@@ -87,18 +102,31 @@ using pair_finder_t =
 #define TECS_CXX_LIST_2(a, b) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b)
 #define TECS_CXX_LIST_3(a, b, c) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b), TECS_CXX_APPLY(c)
 #define TECS_CXX_LIST_4(a, b, c, d) TECS_CXX_APPLY(a), TECS_CXX_APPLY(b), TECS_CXX_APPLY(c), TECS_CXX_APPLY(d)
+// one member per field of a ForceFields<Ref> struct
+#define TECS_CXX_REF_OF(T, N) TecsRef_<TECS_CXX_TYPE_##T(TecsScalar_, TecsDims_)> N;
+#define TECS_CXX_REF_APPLY(P) TECS_CXX_REF_OF P
+#define TECS_CXX_REFS_1(a) TECS_CXX_REF_APPLY(a)
+#define TECS_CXX_REFS_2(a, b) TECS_CXX_REF_APPLY(a) TECS_CXX_REF_APPLY(b)
+#define TECS_CXX_REFS_3(a, b, c) TECS_CXX_REF_APPLY(a) TECS_CXX_REF_APPLY(b) TECS_CXX_REF_APPLY(c)
+#define TECS_CXX_REFS_4(a, b, c, d) TECS_CXX_REF_APPLY(a) TECS_CXX_REF_APPLY(b) TECS_CXX_REF_APPLY(c) TECS_CXX_REF_APPLY(d)
 
 #define CONFIG_FIELDS(...)                                                                            \
   template <typename TecsScalar_, int TecsDims_>                                                      \
   struct TecsFieldsOf_ {                                                                              \
     using type = tecs::detail::FieldList<TECS_CXX_CAT(TECS_CXX_LIST_, TECS_CXX_NARG(__VA_ARGS__))(__VA_ARGS__)>; \
+    template <template <typename> class TecsRef_>                                                     \
+    struct ForceFields {                                                                              \
+      TECS_CXX_CAT(TECS_CXX_REFS_, TECS_CXX_NARG(__VA_ARGS__))(__VA_ARGS__)                            \
+    };                                                                                                \
   };
 
-#define RESOLVE_TECS_CONFIG()                                   \
-  using Vector = tecs::VectorN<Scalar, dimensions>;             \
-  using Polarity = tecs::Polarity_<Scalar>;                     \
-  using VectorView = tecs::View<Vector>;                        \
-  using Fields = typename TecsFieldsOf_<Scalar, dimensions>::type;
+#define RESOLVE_TECS_CONFIG()                                                                \
+  using Vector = tecs::VectorN<Scalar, dimensions>;                                          \
+  using Polarity = tecs::Polarity_<Scalar>;                                                  \
+  using VectorView = tecs::View<Vector>;                                                     \
+  using Fields = typename TecsFieldsOf_<Scalar, dimensions>::type;                           \
+  template <template <typename> class TecsRef_>                                              \
+  using ForceFields = typename TecsFieldsOf_<Scalar, dimensions>::template ForceFields<TecsRef_>;
 
 namespace tecs {
 
@@ -121,13 +149,16 @@ struct DefaultSimulationConfig {
     RESOLVE_TECS_CONFIG()                                  \
   };
 
-#define EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                          \
-  using Scalar = typename C::Scalar;                                     \
-  static constexpr int dimensions = C::dimensions;                       \
-  using Vector = tecs::VectorN<Scalar, dimensions>;                      \
-  using VectorI = tecs::VectorN<int, dimensions>;                        \
-  using VectorView = tecs::View<Vector>;                                 \
-  using Polarity = tecs::Polarity_<Scalar>;
+#define EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                                 \
+  using Scalar = typename C::Scalar;                                                            \
+  static constexpr int dimensions = C::dimensions;                                              \
+  using Vector = tecs::VectorN<Scalar, dimensions>;                                             \
+  using VectorI = tecs::VectorN<int, dimensions>;                                               \
+  using VectorView = tecs::View<Vector>;                                                        \
+  using Polarity = tecs::Polarity_<Scalar>;                                                     \
+  using Random = tecs::CounterRandom;                                                           \
+  using GenericForceFields = typename C::template ForceFields<tecs::detail::GenericFieldRef>;   \
+  using PairwiseForceFields = typename C::template ForceFields<tecs::detail::PairwiseFieldRef>;
 
 #define EXTRACT_ALL_FROM_SIMULATION_CONFIG(C)                            \
   EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                \

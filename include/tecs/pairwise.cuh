@@ -1,0 +1,151 @@
+// tecs/pairwise.cuh -- user pairwise force laws for the C++20 drop-in layer.
+//
+// The reference's programs write their pairwise laws as lambdas or functors
+// (include/utils/utils.hpp:181-276):
+//
+//   auto spring = PAIRWISE_FORCE(
+//     ctx.position.delta += forces::Spring(displacement, distance, L_0);
+//   );
+//   sim.take_step(dt, spring());
+//
+// Included in a program compiled by nvcc (-std=c++20 --extended-lambda,
+// sm_103a), this header makes such a law run on the GPU: the library's force
+// pass (tecs_gb300/csrc/kernels.cuh, k_pass_law) is instantiated here with the
+// law in place of a built-in one, and Simulation::take_step hands the library
+// a launcher for it (tecs_sim_set_pair_law).  The pass finds the same pairs in
+// the same order and adds each law call to the same per-cell sums as the
+// built-in laws, so a law written with a built-in law's operations gives that
+// law's bits (compile with -fmad=false, as the library is, for the reference's).
+//
+// What a law sees, per pair (i, j) the finder accepts (PAIRWISE_FORCE_PARAMETERS):
+//   is_full_step   Euler and Heun's first evaluation: true; Heun's second: false
+//   i, j           the two cells' ids
+//   displacement   x_i - x_j, distance its length
+//   rng            a tecs::CounterRandom keyed by (seed, step, evaluation, i, j)
+//   drag           must stay 0: the drag term is not supported, and a law that
+//                  sets it makes the next count or download fail
+//   ctx            ctx.<field>.self / .other / .delta for the config's fields
+// Finders: the non-symmetric all-pairs and Gabriel finders (naive and binned).
+#ifndef TECS_CXX_PAIRWISE_CUH
+#define TECS_CXX_PAIRWISE_CUH
+
+#if !defined(__CUDACC__)
+#error "tecs/pairwise.cuh needs nvcc (user force laws are compiled into the program's kernels)"
+#endif
+#if !defined(__CUDACC_EXTENDED_LAMBDA__)
+#error "tecs/pairwise.cuh needs nvcc --extended-lambda (PAIRWISE_FORCE makes __host__ __device__ lambdas)"
+#endif
+
+#include <cstring>
+#include <memory>
+
+#include "../../tecs_gb300/csrc/kernels.cuh"
+#include "tecs.hpp"
+
+namespace tecs {
+namespace detail {
+
+// PAIRWISE_FORCE's value: the law lambda with the pairwise tag
+template <typename L>
+struct PairwiseForce {
+  using tag = PairwiseForceTag;
+  L f;
+  template <typename... A>
+  __host__ __device__ void operator()(A&&... a) const {
+    f(static_cast<A&&>(a)...);
+  }
+};
+struct PairwiseForceMaker {
+  template <typename L>
+  PairwiseForce<L> operator|(L f) const {
+    return PairwiseForce<L>{f};
+  }
+};
+inline constexpr PairwiseForceMaker pairwise_force{};
+
+// The law in the form k_pass_law calls: the pair's values as the config's
+// types, the cell's running sums as the deltas, the law, the sums back.
+template <typename Config, typename F>
+struct PairLaw {
+  F law;
+  __device__ void operator()(const PassArgs& a, unsigned idi, unsigned idj, const float* xi, const float4& vj,
+                             const float* disp, float dist, float2 pi, float2 pj, Acc& acc) const {
+    constexpr int D = Config::dimensions;
+    using Vector = VectorN<float, D>;
+    using Fields = typename Config::template ForceFields<PairwiseFieldRef>;
+    Vector self, other, displacement, delta;
+    const float xj[3] = {vj.x, vj.y, vj.z};
+    for (int d = 0; d < D; ++d) {
+      self[d] = xi[d];
+      other[d] = xj[d];
+      displacement[d] = disp[d];
+      delta[d] = acc.x[d];
+    }
+    float drag = 0.f;
+    CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
+    if constexpr (Simulation<Config>::has_polarity) {
+      const Polarity_<float> ps(pi.x, pi.y), po(pj.x, pj.y);
+      Polarity_<float> pd(acc.p[0], acc.p[1]);
+      const Fields ctx{{self, other, delta}, {ps, po, pd}};
+      law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
+      acc.p[0] = pd[0];
+      acc.p[1] = pd[1];
+    } else {
+      const Fields ctx{{self, other, delta}};
+      law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
+    }
+    for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
+    if (drag != 0.f) atomicOr(&a.ctr->error, 2u);
+  }
+};
+
+template <typename Config>
+using FinderOf = typename Config::template PairFinderT<Config>;
+
+// the launcher the library calls for every force evaluation
+template <typename Config, typename F>
+int pair_law_launcher(void* user, const void* call, void* stream) {
+  static_assert(!FinderOf<Config>::symmetric && FinderOf<Config>::finder_id <= TECS_FINDER_BINNED_GABRIEL,
+                "user pairwise laws run with the non-symmetric all-pairs and Gabriel finders");
+  return launch_user_pass<Config::dimensions, FinderOf<Config>::finder_id>(
+      static_cast<const UserPassCall*>(call), static_cast<cudaStream_t>(stream),
+      *static_cast<const PairLaw<Config, F>*>(user));
+}
+
+template <typename Config, typename F>
+struct PairLawBinding {
+  // Binds the law unless the same law with the same captured values is bound
+  // already; a new binding makes the library re-capture its step graph.
+  static void bind(tecs_sim* handle, int device, const F& f, std::shared_ptr<void>& holder,
+                   tecs_pair_law_fn& bound) {
+    const tecs_pair_law_fn fn = &pair_law_launcher<Config, F>;
+    auto next = std::make_shared<PairLaw<Config, F>>(PairLaw<Config, F>{f});
+    if (holder && bound == fn && std::memcmp(holder.get(), next.get(), sizeof(PairLaw<Config, F>)) == 0) return;
+    if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, PairLaw<Config, F>>(device))
+      throw Error("cannot load the user pairwise law's pass on the device");
+    check(tecs_sim_set_pair_law(handle, fn, next.get()));
+    holder = next;
+    bound = fn;
+  }
+};
+
+}  // namespace detail
+}  // namespace tecs
+
+#define PAIRWISE_FORCE_PARAMETERS                                                                          \
+  const bool is_full_step, const unsigned int i, const unsigned int j, const Vector &displacement,          \
+      const Scalar distance, Random &rng, Scalar &drag, const PairwiseForceFields &ctx
+#define PAIRWISE_REF(TYPE, NAME) tecs::detail::PairwiseFieldRef<TYPE> NAME
+
+// a lambda factory, as the reference's: PAIRWISE_FORCE(body)() is the law
+#define PAIRWISE_FORCE(...)                                                                                \
+  [&]() {                                                                                                  \
+    return tecs::detail::pairwise_force | [=] __host__ __device__(PAIRWISE_FORCE_PARAMETERS) { __VA_ARGS__ }; \
+  }
+
+// a functor's call operator: struct Law { PAIRWISE_FORCE_OP { body } };
+#define PAIRWISE_FORCE_OP                  \
+  using tag = tecs::detail::PairwiseForceTag; \
+  __host__ __device__ void operator()(PAIRWISE_FORCE_PARAMETERS) const
+
+#endif  // TECS_CXX_PAIRWISE_CUH

@@ -15,6 +15,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -64,6 +65,22 @@ class View {
   std::vector<T> data_;
   unsigned active_ = 0;
 };
+
+namespace detail {
+// the tag of a user pairwise law: a PAIRWISE_FORCE lambda or a PAIRWISE_FORCE_OP functor
+// (include/utils/utils.hpp:181-276), defined with tecs/pairwise.cuh
+struct PairwiseForceTag {};
+template <typename F>
+concept UserPairLaw = requires { typename F::tag; } && std::is_same_v<typename F::tag, PairwiseForceTag>;
+template <typename F>
+constexpr bool is_link_law() {
+  if constexpr (requires { F::is_link; }) return F::is_link;
+  else return false;
+}
+// Hands a user law to a simulation's library handle; defined by tecs/pairwise.cuh.
+template <typename Config, typename F>
+struct PairLawBinding;
+}  // namespace detail
 
 // Cell division after each step (the pattern of examples/growth_w_wall.cpp:119-136,
 // done on the device): each active cell divides with this probability per step;
@@ -219,9 +236,10 @@ class Simulation {
   }
 
   // -- stepping ---------------------------------------------------------------
-  // take_step(dt, forces...): one integrator step with at most one built-in
-  // pairwise law and at most one link law, in any order (the reference fuses
-  // forces by kind and evaluates pairwise before link forces)
+  // take_step(dt, forces...): one integrator step with at most one pairwise
+  // law (built-in, or a user law of tecs/pairwise.cuh) and at most one link
+  // law, in any order (the reference fuses forces by kind and evaluates
+  // pairwise before link forces)
   template <typename... Forces>
   void take_step(double dt, const Forces&... forces) {
     take_steps(dt, 1, forces...);
@@ -229,8 +247,8 @@ class Simulation {
   // n steps queued at once (one graph replay each)
   template <typename... Forces>
   void take_steps(double dt, int n, const Forces&... forces) {
-    static_assert((0 + ... + (Forces::is_link ? 0 : 1)) <= 1, "one pairwise law per step");
-    static_assert((0 + ... + (Forces::is_link ? 1 : 0)) <= 1, "one link law per step");
+    static_assert((0 + ... + (detail::is_link_law<Forces>() ? 0 : 1)) <= 1, "one pairwise law per step");
+    static_assert((0 + ... + (detail::is_link_law<Forces>() ? 1 : 0)) <= 1, "one link law per step");
     apply_pair_law(forces...);
     apply_link_law(forces...);
     upload_if_dirty();
@@ -332,20 +350,30 @@ class Simulation {
     return s;
   }
 
-  // the pairwise law of this step (none: pairs only, no deltas)
+  // the pairwise law of this step (none: pairs only, no deltas); a user law
+  // replaces the built-in one until a step passes a built-in law again
   template <typename... Forces>
   void apply_pair_law(const Forces&... forces) {
     int id = TECS_FORCE_NONE;
     float k[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    bool user = false;
     auto one = [&](const auto& f) {
       using F = std::decay_t<decltype(f)>;
-      if constexpr (!F::is_link) {
+      if constexpr (detail::UserPairLaw<F>) {
+        user = true;
+        detail::PairLawBinding<Config, F>::bind(handle_, settings_.device, f, law_holder_, law_fn_);
+      } else if constexpr (!detail::is_link_law<F>()) {
         static_assert(!F::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
         id = F::force_id;
         k[0] = f.k_rep; k[1] = f.r_rep; k[2] = f.k_adh; k[3] = f.r_adh; k[4] = f.k_pol_value();
       }
     };
     (one(forces), ...);
+    if (!user && law_fn_) {
+      check(tecs_sim_set_pair_law(handle_, nullptr, nullptr));
+      law_holder_.reset();
+      law_fn_ = nullptr;
+    }
     check(tecs_sim_set_force(handle_, id, k[0], k[1], k[2], k[3], k[4]));
   }
 
@@ -356,7 +384,7 @@ class Simulation {
     float strength = 0.f;
     auto one = [&](const auto& f) {
       using F = std::decay_t<decltype(f)>;
-      if constexpr (F::is_link) {
+      if constexpr (detail::is_link_law<F>()) {
         has = true;
         strength = f.strength;
       }
@@ -424,6 +452,9 @@ class Simulation {
 
   Settings settings_;
   Writer writer_;
+  // the bound user pairwise law (its launcher and the law object it launches with); destroyed after handle_
+  std::shared_ptr<void> law_holder_;
+  tecs_pair_law_fn law_fn_ = nullptr;
   tecs_sim* handle_ = nullptr;
   View<Vector> positions_;
   View<Polarity> polarity_;

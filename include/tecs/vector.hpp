@@ -4,8 +4,8 @@
 // operators and memory layout (D, respectively 2, contiguous scalars;
 // include/types/vector.hpp:34-436, include/types/polarity.hpp:28-124), so a
 // View<VectorN<float, 3>> is exactly the AoS float[n][3] array the C ABI
-// (tecs_gpu.h) uploads and downloads.  They are host types: the arithmetic of
-// a step runs in the CUDA library.
+// (tecs_gpu.h) uploads and downloads.  Compiled by nvcc their members are
+// also device functions, for the user pairwise laws of tecs/pairwise.cuh.
 #ifndef TECS_CXX_VECTOR_HPP
 #define TECS_CXX_VECTOR_HPP
 
@@ -13,7 +13,21 @@
 #include <cstddef>
 #include <type_traits>
 
+#if defined(__CUDACC__)
+#define TECS_HD __host__ __device__
+#else
+#define TECS_HD
+#endif
+
 namespace tecs {
+
+namespace detail {
+// the square root of float or double, on the host and the device
+TECS_HD inline float sqrt_(float v) { return sqrtf(v); }
+TECS_HD inline double sqrt_(double v) { return sqrt(v); }
+TECS_HD inline float fmax_(float a, float b) { return fmaxf(a, b); }
+TECS_HD inline double fmax_(double a, double b) { return fmax(a, b); }
+}  // namespace detail
 
 template <typename Scalar, int dimensions>
 struct VectorN {
@@ -25,40 +39,40 @@ struct VectorN {
 
   constexpr VectorN() = default;
   // every component set to v (the reference's Vector(-20) bounds idiom)
-  constexpr explicit VectorN(Scalar v) {
+  TECS_HD constexpr explicit VectorN(Scalar v) {
     for (int d = 0; d < dimensions; ++d) data_[d] = v;
   }
   template <typename... Ts>
     requires(sizeof...(Ts) == dimensions && dimensions > 1 && (std::is_arithmetic_v<Ts> && ...))
-  constexpr VectorN(Ts... v) : data_{static_cast<Scalar>(v)...} {}
+  TECS_HD constexpr VectorN(Ts... v) : data_{static_cast<Scalar>(v)...} {}
 
-  static constexpr int size() { return dimensions; }
-  constexpr Scalar& operator[](int d) { return data_[d]; }
-  constexpr const Scalar& operator[](int d) const { return data_[d]; }
-  constexpr Scalar& x() { return data_[0]; }
-  constexpr const Scalar& x() const { return data_[0]; }
-  constexpr Scalar& y() requires(dimensions >= 2) { return data_[1]; }
-  constexpr const Scalar& y() const requires(dimensions >= 2) { return data_[1]; }
-  constexpr Scalar& z() requires(dimensions >= 3) { return data_[2]; }
-  constexpr const Scalar& z() const requires(dimensions >= 3) { return data_[2]; }
-  constexpr Scalar& w() requires(dimensions >= 4) { return data_[3]; }
-  constexpr const Scalar& w() const requires(dimensions >= 4) { return data_[3]; }
+  TECS_HD static constexpr int size() { return dimensions; }
+  TECS_HD constexpr Scalar& operator[](int d) { return data_[d]; }
+  TECS_HD constexpr const Scalar& operator[](int d) const { return data_[d]; }
+  TECS_HD constexpr Scalar& x() { return data_[0]; }
+  TECS_HD constexpr const Scalar& x() const { return data_[0]; }
+  TECS_HD constexpr Scalar& y() requires(dimensions >= 2) { return data_[1]; }
+  TECS_HD constexpr const Scalar& y() const requires(dimensions >= 2) { return data_[1]; }
+  TECS_HD constexpr Scalar& z() requires(dimensions >= 3) { return data_[2]; }
+  TECS_HD constexpr const Scalar& z() const requires(dimensions >= 3) { return data_[2]; }
+  TECS_HD constexpr Scalar& w() requires(dimensions >= 4) { return data_[3]; }
+  TECS_HD constexpr const Scalar& w() const requires(dimensions >= 4) { return data_[3]; }
 
   // component-wise with a vector or a scalar
-#define TECS_CXX_VEC_OP(OP)                                          \
-  constexpr VectorN& operator OP##=(const VectorN& o) {              \
-    for (int d = 0; d < dimensions; ++d) data_[d] OP## = o.data_[d]; \
-    return *this;                                                    \
-  }                                                                  \
-  constexpr VectorN& operator OP##=(Scalar s) {                      \
-    for (int d = 0; d < dimensions; ++d) data_[d] OP## = s;          \
-    return *this;                                                    \
-  }                                                                  \
-  friend constexpr VectorN operator OP(VectorN a, const VectorN& b) { return a OP## = b; } \
-  friend constexpr VectorN operator OP(VectorN a, Scalar s) { return a OP## = s; }        \
-  friend constexpr VectorN operator OP(Scalar s, VectorN a) {        \
-    for (int d = 0; d < dimensions; ++d) a.data_[d] = s OP a.data_[d]; \
-    return a;                                                        \
+#define TECS_CXX_VEC_OP(OP)                                                                        \
+  TECS_HD constexpr VectorN& operator OP##=(const VectorN& o) {                                    \
+    for (int d = 0; d < dimensions; ++d) data_[d] OP## = o.data_[d];                               \
+    return *this;                                                                                  \
+  }                                                                                                \
+  TECS_HD constexpr VectorN& operator OP##=(Scalar s) {                                            \
+    for (int d = 0; d < dimensions; ++d) data_[d] OP## = s;                                        \
+    return *this;                                                                                  \
+  }                                                                                                \
+  friend TECS_HD constexpr VectorN operator OP(VectorN a, const VectorN& b) { return a OP## = b; } \
+  friend TECS_HD constexpr VectorN operator OP(VectorN a, Scalar s) { return a OP## = s; }         \
+  friend TECS_HD constexpr VectorN operator OP(Scalar s, VectorN a) {                              \
+    for (int d = 0; d < dimensions; ++d) a.data_[d] = s OP a.data_[d];                             \
+    return a;                                                                                      \
   }
   TECS_CXX_VEC_OP(+)
   TECS_CXX_VEC_OP(-)
@@ -66,26 +80,26 @@ struct VectorN {
   TECS_CXX_VEC_OP(/)
 #undef TECS_CXX_VEC_OP
 
-  friend constexpr VectorN operator-(VectorN a) {
+  friend TECS_HD constexpr VectorN operator-(VectorN a) {
     for (int d = 0; d < dimensions; ++d) a.data_[d] = -a.data_[d];
     return a;
   }
-  friend constexpr VectorN operator+(const VectorN& a) { return a; }
-  friend constexpr bool operator==(const VectorN& a, const VectorN& b) {
+  friend TECS_HD constexpr VectorN operator+(const VectorN& a) { return a; }
+  friend TECS_HD constexpr bool operator==(const VectorN& a, const VectorN& b) {
     for (int d = 0; d < dimensions; ++d)
       if (a.data_[d] != b.data_[d]) return false;
     return true;
   }
 
   // index-order sums, as the reference's dot / length_squared / distance_to_squared
-  constexpr Scalar dot(const VectorN& o) const {
+  TECS_HD constexpr Scalar dot(const VectorN& o) const {
     Scalar r{};
     for (int d = 0; d < dimensions; ++d) r += data_[d] * o.data_[d];
     return r;
   }
-  constexpr Scalar length_squared() const { return dot(*this); }
-  Scalar length() const { return std::sqrt(length_squared()); }
-  constexpr Scalar distance_to_squared(const VectorN& o) const {
+  TECS_HD constexpr Scalar length_squared() const { return dot(*this); }
+  TECS_HD Scalar length() const { return detail::sqrt_(length_squared()); }
+  TECS_HD constexpr Scalar distance_to_squared(const VectorN& o) const {
     Scalar r{};
     for (int d = 0; d < dimensions; ++d) {
       const Scalar e = data_[d] - o.data_[d];
@@ -93,9 +107,9 @@ struct VectorN {
     }
     return r;
   }
-  Scalar distance_to(const VectorN& o) const { return std::sqrt(distance_to_squared(o)); }
-  VectorN normalized() const { return *this / length(); }
-  constexpr VectorN cross(const VectorN& o) const requires(dimensions == 3) {
+  TECS_HD Scalar distance_to(const VectorN& o) const { return detail::sqrt_(distance_to_squared(o)); }
+  TECS_HD VectorN normalized() const { return *this / length(); }
+  TECS_HD constexpr VectorN cross(const VectorN& o) const requires(dimensions == 3) {
     return VectorN(data_[1] * o.data_[2] - data_[2] * o.data_[1], data_[2] * o.data_[0] - data_[0] * o.data_[2],
                    data_[0] * o.data_[1] - data_[1] * o.data_[0]);
   }
@@ -110,28 +124,28 @@ struct Polarity_ : VectorN<Scalar, 2> {
   using Base = VectorN<Scalar, 2>;
 
   constexpr Polarity_() = default;
-  constexpr explicit Polarity_(Scalar v) : Base(v) {}
-  constexpr Polarity_(Scalar theta, Scalar phi) : Base(theta, phi) {}
+  TECS_HD constexpr explicit Polarity_(Scalar v) : Base(v) {}
+  TECS_HD constexpr Polarity_(Scalar theta, Scalar phi) : Base(theta, phi) {}
   // the direction of v (polarity.hpp:74-77)
-  explicit Polarity_(const Vector3<Scalar>& v) : Polarity_(from_vector3(v)) {}
+  TECS_HD explicit Polarity_(const Vector3<Scalar>& v) : Polarity_(from_vector3(v)) {}
 
-  constexpr Scalar& theta() { return this->data_[0]; }
-  constexpr const Scalar& theta() const { return this->data_[0]; }
-  constexpr Scalar& phi() { return this->data_[1]; }
-  constexpr const Scalar& phi() const { return this->data_[1]; }
+  TECS_HD constexpr Scalar& theta() { return this->data_[0]; }
+  TECS_HD constexpr const Scalar& theta() const { return this->data_[0]; }
+  TECS_HD constexpr Scalar& phi() { return this->data_[1]; }
+  TECS_HD constexpr const Scalar& phi() const { return this->data_[1]; }
 
   // theta = acos(clamp(z / |v|, -1, 1)), phi = atan2(y, x) (polarity.hpp:62-76)
-  static Polarity_ from_vector3(const Vector3<Scalar>& v, Scalar length) {
+  TECS_HD static Polarity_ from_vector3(const Vector3<Scalar>& v, Scalar length) {
     return Polarity_(std::acos(std::fmin(Scalar(1), std::fmax(Scalar(-1), v[2] / length))), std::atan2(v[1], v[0]));
   }
-  static Polarity_ from_vector3(const Vector3<Scalar>& v) { return from_vector3(v, v.length()); }
-  static Vector3<Scalar> to_vector3(const Polarity_& p) {
+  TECS_HD static Polarity_ from_vector3(const Vector3<Scalar>& v) { return from_vector3(v, v.length()); }
+  TECS_HD static Vector3<Scalar> to_vector3(const Polarity_& p) {
     return Vector3<Scalar>(std::sin(p.theta()) * std::cos(p.phi()), std::sin(p.theta()) * std::sin(p.phi()),
                            std::cos(p.theta()));
   }
-  Vector3<Scalar> to_vector3() const { return to_vector3(*this); }
+  TECS_HD Vector3<Scalar> to_vector3() const { return to_vector3(*this); }
   // cosine of the angle between the two directions (polarity.hpp:132-136)
-  Scalar dot(const Polarity_& o) const {
+  TECS_HD Scalar dot(const Polarity_& o) const {
     return std::sin(theta()) * std::sin(o.theta()) * std::cos(phi() - o.phi()) +
            std::cos(theta()) * std::cos(o.theta());
   }

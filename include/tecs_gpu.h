@@ -141,6 +141,20 @@ int tecs_sim_set_links(tecs_sim* sim, const uint32_t* links, unsigned n_links, f
  * law and its constants are unchanged; otherwise waits for queued steps. */
 int tecs_sim_set_force(tecs_sim* sim, int force, float k_rep, float r_rep, float k_adh, float r_adh, float k_pol);
 
+/* A user pairwise law (a PAIRWISE_FORCE lambda or functor of the calling
+ * program, include/utils/utils.hpp:181-276) in place of the built-in one:
+ * for every force evaluation the library calls fn(user, call, stream), and
+ * fn launches the pass compiled with the law into the program -- the header
+ * include/tecs/pairwise.cuh makes fn for a lambda.  call points to the
+ * library's description of the evaluation (its first field is its size in
+ * bytes), stream is the simulation's cudaStream_t; fn returns 0 on success.
+ * Launches made while a step is captured into a graph replay with it.
+ * Non-symmetric all-pairs and Gabriel finders; fn == NULL returns to the
+ * built-in law.  Replaces the force argument of take_step
+ * (include/simulation.hpp:548-556) for such laws. */
+typedef int (*tecs_pair_law_fn)(void* user, const void* call, void* stream);
+int tecs_sim_set_pair_law(tecs_sim* sim, tecs_pair_law_fn fn, void* user);
+
 /* Capture each step as a CUDA graph and replay it (default on). */
 int tecs_sim_set_graph(tecs_sim* sim, int enable);
 

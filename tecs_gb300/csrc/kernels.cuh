@@ -89,6 +89,8 @@ struct PassArgs {
   const uint2* link_ent;
   const unsigned* slot_of;
   float link_k;
+  // the integrator's is_full_step of this evaluation (Euler, Heun pass 1: 1; Heun pass 2: 0), for user laws
+  int full_step;
 };
 
 // ---------------------------------------------------------------------------
@@ -890,6 +892,126 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
         visit<D, FINDER, FORCE>(g, fp, a, n, i, j, xi, pi, acc, idi);
       }
     }
+}
+
+// ---------------------------------------------------------------------------
+// User pairwise laws: a PAIRWISE_FORCE lambda or functor compiled into the
+// calling program (include/tecs/pairwise.cuh) takes pair_force's place in the
+// general pass.  Candidate order, pair predicates, per-cell sums and the
+// epilogues (COM, links, fused integrator modes, division) are those of
+// k_pass, so a law written like a built-in one gives the built-in's bits.
+// Law is a device callable adding the pair (self = i, other = j) to acc:
+//   law(a, id_i, id_j, x_i, x_j (w = key or id), displacement x_i - x_j, distance, p_i, p_j, acc)
+// with displacement[2] = 0 in 2-D and p = 0 without polarity.
+
+template <int D, int FINDER, class Law>
+__device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+                                          unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi,
+                                          const Law& law) {
+  const float4 vj = a.X[j];
+  float disp[3] = {xi[0] - vj.x, xi[1] - vj.y, D >= 3 ? xi[2] - vj.z : 0.f};
+  float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+  if (D >= 3) d2 = d2 + disp[2] * disp[2];
+  if (d2 >= fp.rc2) return;
+  if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
+  if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
+  const unsigned idj = id_at(a.X, a.Bid, j);
+  if (a.pairs) {
+    const unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, idj);
+  }
+  const float dist = sqrtf(d2);
+  const float2 pj = a.P ? a.P[j] : make_float2(0.f, 0.f);
+  law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc);
+}
+
+// cell_general's loops with a user law
+template <int D, int FINDER, class Law>
+__device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
+                                         const float* xi, float2 pi, unsigned idi, Acc& acc, const Law& law) {
+  if (FINDER == 1 || FINDER == 3) {
+    int bc[3] = {0, 0, 0};
+    if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
+    else bin_coords_div<D>(g, xi, bc);
+    const int R = g.R;
+    const int z0 = D >= 3 ? -R : 0, z1 = D >= 3 ? R : 0;
+    for (int dz = z0; dz <= z1; ++dz) {
+      const int cz = D >= 3 ? bc[2] + dz : 0;
+      if (D >= 3 && (cz < 0 || cz >= g.ext[2])) continue;
+      for (int dy = -R; dy <= R; ++dy) {
+        const int cy = bc[1] + dy;
+        if (cy < 0 || cy >= g.ext[1]) continue;
+        const int x0 = max(bc[0] - R, 0), x1 = min(bc[0] + R, g.ext[0] - 1);
+        int c0[3] = {x0, cy, cz}, c1[3] = {x1, cy, cz};
+        const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
+        for (unsigned j = lo; j < hi; ++j) {
+          if (j == i) continue;
+          visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, idi, law);
+        }
+      }
+    }
+  } else {
+    for (unsigned j = 0; j < n; ++j) {
+      if (j == i) continue;
+      visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, idi, law);
+    }
+  }
+}
+
+template <int D, int FINDER, class Law>
+static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, ForceP fp, PassArgs a, Law law) {
+  const unsigned n = a.ctr->n;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  float xi[3] = {0.f, 0.f, 0.f};
+  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 pi = make_float2(0.f, 0.f);
+  if (active) {
+    vi = a.X[i];
+    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
+    if (a.P) pi = a.P[i];
+    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc, law);
+  }
+  pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+}
+
+// One force evaluation handed to a user law's launcher (tecs_sim_set_pair_law).
+// size is sizeof(UserPassCall) of the library that filled it: a program built
+// against other headers is refused.
+struct UserPassCall {
+  unsigned size;
+  int device;           // the simulation's GPU
+  int dims;
+  int finder;           // TECS_FINDER_NAIVE_ALL_PAIRS .. TECS_FINDER_BINNED_GABRIEL
+  unsigned blocks;      // of kPassThreads threads
+  GridP g;
+  ForceP fp;
+  PassArgs a;
+};
+
+// Launches the pass of one evaluation with the law, on the library's stream,
+// for the finder and dimension count the program was compiled for.  0 on
+// success; 1 the call's layout differs; 2 a launch error; 3 the simulation's
+// finder or dimension count is not the program's.
+template <int D, int FINDER, class Law>
+int launch_user_pass(const UserPassCall* c, cudaStream_t stream, const Law& law) {
+  static_assert(FINDER >= 0 && FINDER <= 3, "user laws run with the all-pairs and Gabriel finders");
+  if (!c || c->size != sizeof(UserPassCall)) return 1;
+  if (c->dims != D || c->finder != FINDER) return 3;
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess || (cur != c->device && cudaSetDevice(c->device) != cudaSuccess)) return 2;
+  k_pass_law<D, FINDER, Law><<<c->blocks, kPassThreads, 0, stream>>>(c->g, c->fp, c->a, law);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Loads the law's pass on the device before the library first launches it,
+// which may be while it captures a step graph: 0 on success.
+template <int D, int FINDER, class Law>
+int prepare_user_pass(int device) {
+  cudaFuncAttributes fa;
+  if (cudaSetDevice(device) != cudaSuccess) return 2;
+  return cudaFuncGetAttributes(&fa, k_pass_law<D, FINDER, Law>) == cudaSuccess ? 0 : 2;
 }
 
 // ---------------------------------------------------------------------------

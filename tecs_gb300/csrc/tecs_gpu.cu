@@ -213,6 +213,9 @@ struct tecs_sim {
   // chunk totals, and the rebuild needs no reduction pass over the bins
   bool fuse_part = false;
   Counters* hctr = nullptr;  // page-locked mirror of the device counters
+  // a user pairwise law compiled into the calling program: launches each force pass in place of pass_fn's
+  tecs_pair_law_fn law_fn = nullptr;
+  void* law_user = nullptr;
   // per-kernel CUDA events (external event-record nodes when captured in a graph)
   bool profiling = false;
   static constexpr int kMaxProf = 32;
@@ -318,6 +321,7 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.link_ent = s->n_links ? s->link_ent : nullptr;
   a.slot_of = (s->n_links && s->binned) ? s->slot_of : nullptr;
   a.link_k = s->link_k;
+  a.full_step = 1;
   return a;
 }
 
@@ -380,10 +384,28 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
 
 int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   const bool sym = s->d.symmetric != 0;
-  PassFn fn = pass_fn(s, sym);
-  if (!fn) return fail("unsupported finder/force/dims combination");
   const unsigned L = launch_count(s);
   const unsigned blocks = ceil_div(L ? L : 1, kPassThreads);
+  if (s->law_fn) {
+    UserPassCall c{};
+    c.size = sizeof(UserPassCall);
+    c.device = s->d.device;
+    c.dims = s->d.dims;
+    c.finder = s->d.finder;
+    c.blocks = blocks;
+    c.g = s->g;
+    c.fp = s->fp;
+    c.a = a;
+    PROF_BEGIN(s);
+    const int r = s->law_fn(s->law_user, &c, s->stream);
+    PROF_END(s, "k_pass_law");
+    K += 1;
+    if (r) return fail("the user pairwise law's launcher failed (code " + std::to_string(r) + ")");
+    CK(cudaGetLastError());
+    return 0;
+  }
+  PassFn fn = pass_fn(s, sym);
+  if (!fn) return fail("unsupported finder/force/dims combination");
   if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY) {
     // applications per pair on this pass's positions, then the pass
     PROF_BEGIN(s);
@@ -497,6 +519,7 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     PassArgs p2 = a;
     p2.X = s->Xt;
     p2.P = pol ? s->Pt : nullptr;
+    p2.full_step = 0;  // heun.hpp:117
     if (fused) {
       p2.mode = kHeun2Fused;
       p2.Bx = s->B;
@@ -776,6 +799,7 @@ int tecs_sim_count(tecs_sim* s, unsigned* n) {
   CK(cudaMemcpyAsync(s->hctr, s->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   if (s->hctr->error & 1u) return fail("capacity exceeded by cell division");
+  if (s->hctr->error & 2u) return fail("a user pairwise law set drag, which this library does not support");
   *n = s->hctr->n;
   return 0;
 }
@@ -901,6 +925,20 @@ int tecs_sim_set_force(tecs_sim* s, int force, float k_rep, float r_rep, float k
   s->d.k_rep = k_rep; s->d.r_rep = r_rep; s->d.k_adh = k_adh; s->d.r_adh = r_adh; s->d.k_pol = k_pol;
   f.force = force;
   f.k_rep = k_rep; f.r_rep = r_rep; f.k_adh = k_adh; f.r_adh = r_adh; f.k_pol = k_pol;
+  drop_graphs(s);
+  return 0;
+}
+
+int tecs_sim_set_pair_law(tecs_sim* s, tecs_pair_law_fn fn, void* user) {
+  if (!s) return fail("null simulation");
+  if (fn && (s->d.symmetric || s->d.finder > TECS_FINDER_BINNED_GABRIEL))
+    return fail("user pairwise laws run with the non-symmetric all-pairs and Gabriel finders");
+  if (fn == s->law_fn && user == s->law_user) return 0;
+  CK(cudaSetDevice(s->d.device));
+  // queued steps launched the old law from their graphs
+  CK(cudaStreamSynchronize(s->stream));
+  s->law_fn = fn;
+  s->law_user = fn ? user : nullptr;
   drop_graphs(s);
   return 0;
 }

@@ -1,0 +1,242 @@
+// user_law_driver.cu -- a program whose pairwise laws are PAIRWISE_FORCE
+// lambdas and PAIRWISE_FORCE_OP functors, as the reference's programs write
+// them, compiled by nvcc against include/tecs/pairwise.cuh.  The law is the
+// two-radius spring the reference's fixtures were made with, written with the
+// same operations, so its outputs must equal the reference's bit for bit.
+//
+//   user_law_driver <scenario> <in.bin> <out_prefix> <steps> <dt>
+//
+// in.bin and the outputs are those of drop_in_driver.cpp (.pairs, .dpos,
+// .pos; link scenarios read the links and write .pos only).  Scenario
+// "rng_twice" steps two copies of the input with a law that draws from rng and
+// writes <out>.a.pos and <out>.b.pos; "drag" steps with a law that sets drag
+// and must fail with tecs::Error.
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "tecs/pairwise.cuh"
+
+using namespace tecs;
+
+CREATE_SIMULATION_CONFIG(NaiveAllPairsHeun,
+                         CONFIG_PAIR_FINDER(pair_finders::NaiveAllPairs)
+                         CONFIG_INTEGRATOR(integrators::Heun))
+CREATE_SIMULATION_CONFIG(NaiveGabrielHeun,
+                         CONFIG_PAIR_FINDER(pair_finders::NaiveGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun))
+CREATE_SIMULATION_CONFIG(BinnedAllPairsEuler,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
+                         CONFIG_INTEGRATOR(integrators::Euler))
+CREATE_SIMULATION_CONFIG(BinnedGabrielHeun,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun))
+CREATE_SIMULATION_CONFIG(BinnedGabrielHeunCom,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun)
+                         CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
+struct BinnedGabrielHeun2D : public DefaultSimulationConfig {
+  CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+  CONFIG_INTEGRATOR(integrators::Heun)
+  CONFIG_DIMENSIONS(2)
+  RESOLVE_TECS_CONFIG()
+};
+
+struct Input {
+  unsigned n = 0, dims = 0, has_pol = 0;
+  float prm[16] = {};
+  std::vector<float> x, p;
+  std::vector<unsigned> links;
+};
+
+static Input read_input(const char* path, bool with_links) {
+  Input in;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) { std::perror(path); std::exit(2); }
+  unsigned hdr[3];
+  if (std::fread(hdr, 4, 3, f) != 3) std::exit(2);
+  in.n = hdr[0]; in.dims = hdr[1]; in.has_pol = hdr[2];
+  if (std::fread(in.prm, 4, 16, f) != 16) std::exit(2);
+  in.x.resize(std::size_t(in.n) * in.dims);
+  if (in.n && std::fread(in.x.data(), 4, in.x.size(), f) != in.x.size()) std::exit(2);
+  if (in.has_pol) {
+    in.p.resize(std::size_t(in.n) * 2);
+    if (in.n && std::fread(in.p.data(), 4, in.p.size(), f) != in.p.size()) std::exit(2);
+  }
+  if (with_links) {
+    unsigned nl = 0;
+    if (std::fread(&nl, 4, 1, f) != 1) std::exit(2);
+    in.links.resize(std::size_t(nl) * 2);
+    if (nl && std::fread(in.links.data(), 4, in.links.size(), f) != in.links.size()) std::exit(2);
+  }
+  std::fclose(f);
+  return in;
+}
+
+static void write_raw(const std::string& path, const void* data, std::size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { std::perror(path.c_str()); std::exit(2); }
+  if (bytes) std::fwrite(data, 1, bytes, f);
+  std::fclose(f);
+}
+
+// the fixtures' law, F(d) = k_rep*max(r_rep-d,0) - k_adh*max(d-r_adh,0), as a functor
+template <typename Config>
+struct SpringFunctor {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(Config)
+  float k_rep, r_rep, k_adh, r_adh;
+  PAIRWISE_FORCE_OP {
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+  }
+};
+
+template <typename Config>
+static typename Simulation<Config>::Settings settings_of(const Input& in) {
+  using Sim = Simulation<Config>;
+  constexpr int D = Sim::dimensions;
+  typename Sim::Settings settings(in.n, "unused");
+  settings.cutoff_distance = in.prm[0];
+  settings.capacity = unsigned(in.prm[13]) > in.n ? unsigned(in.prm[13]) : in.n;
+  auto& pfs = settings.pair_finder_settings;
+  if constexpr (requires { pfs.gabriel_coefficient; }) pfs.gabriel_coefficient = in.prm[1];
+  if constexpr (requires { pfs.min_bounds; }) {
+    for (int d = 0; d < D; ++d) {
+      pfs.min_bounds[d] = in.prm[2 + d];
+      pfs.max_bounds[d] = in.prm[5 + d];
+    }
+    pfs.bin_size_scale = in.prm[14];
+  }
+  settings.link_capacity = unsigned(in.links.size() / 2);
+  settings.link_active_count = settings.link_capacity;
+  return settings;
+}
+
+template <typename Config>
+static void fill(Simulation<Config>& sim, const Input& in) {
+  constexpr int D = Config::dimensions;
+  auto& positions = sim.get_positions_view();
+  for (unsigned i = 0; i < in.n; ++i)
+    for (int d = 0; d < D; ++d) positions(i)[d] = in.x[std::size_t(i) * D + d];
+  auto& links = sim.get_links();
+  for (unsigned l = 0; l < in.links.size() / 2; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+}
+
+template <typename Config>
+static int run(const Input& in, const std::string& out, int steps, double dt, bool functor) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(Config)
+  if (int(in.dims) != dimensions) { std::fprintf(stderr, "input has %u dims\n", in.dims); return 2; }
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  auto spring = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+  );
+  Simulation<Config> sim(settings_of<Config>(in));
+  fill(sim, in);
+  auto go = [&](const auto& law) {
+    std::vector<Vector> deltas;
+    const auto pairs = sim.evaluate(law, &deltas);
+    std::vector<unsigned> flat;
+    for (const auto& pr : pairs) { flat.push_back(pr.first); flat.push_back(pr.second); }
+    write_raw(out + ".pairs", flat.data(), flat.size() * 4);
+    write_raw(out + ".dpos", deltas.data(), deltas.size() * sizeof(Vector));
+    for (int s = 0; s < steps; ++s) sim.take_step(dt, law);
+  };
+  if (functor) go(SpringFunctor<Config>{k_rep, r_rep, k_adh, r_adh});
+  else go(spring());
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  return 0;
+}
+
+// links and a user law in one step, as the reference's protrusion programs
+template <typename Config>
+static int run_links(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(Config)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  auto spring = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+  );
+  Simulation<Config> sim(settings_of<Config>(in));
+  fill(sim, in);
+  const forces::LinkPull protrusions{in.prm[15]};
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, protrusions, spring());
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  return 0;
+}
+
+// a law that draws from rng: two simulations of the same input give the same run
+static int run_rng_twice(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
+  auto noisy = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = Scalar(2) * fmaxf(Scalar(0.7) - distance, Scalar(0)) + Scalar(0.1) * rng.frand(-1.f, 1.f);
+      ctx.position.delta += displacement * F / distance;
+      if (is_full_step) ctx.position.delta += Vector(Scalar(0.01) * Scalar(rng.normal()));
+    }
+  );
+  for (const char* tag : {".a.pos", ".b.pos"}) {
+    Simulation<BinnedGabrielHeun> sim(settings_of<BinnedGabrielHeun>(in));
+    fill(sim, in);
+    for (int s = 0; s < steps; ++s) sim.take_step(dt, noisy());
+    const auto& x = sim.get_positions_view();
+    write_raw(out + tag, x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  }
+  return 0;
+}
+
+// a law that sets drag, which the library does not support: the next download fails
+static int run_drag(const Input& in, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
+  auto dragging = PAIRWISE_FORCE(
+    drag = Scalar(0.5);
+    ctx.position.delta += displacement * Scalar(0.1);
+  );
+  Simulation<BinnedGabrielHeun> sim(settings_of<BinnedGabrielHeun>(in));
+  fill(sim, in);
+  sim.take_step(dt, dragging());
+  try {
+    (void)sim.get_positions_view();
+    sim.get_agent_count();
+  } catch (const Error& e) {
+    std::printf("refused: %s\n", e.what());
+    return 0;
+  }
+  return 3;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 6) return 2;
+  const std::string scenario = argv[1];
+  const bool links = scenario.rfind("lk_", 0) == 0;
+  const Input in = read_input(argv[2], links);
+  const std::string out = argv[3];
+  const int steps = std::atoi(argv[4]);
+  const double dt = std::atof(argv[5]);
+  try {
+    if (scenario == "na_heun") return run<NaiveAllPairsHeun>(in, out, steps, dt, false);
+    if (scenario == "ng_heun") return run<NaiveGabrielHeun>(in, out, steps, dt, false);
+    if (scenario == "ba_euler") return run<BinnedAllPairsEuler>(in, out, steps, dt, false);
+    if (scenario == "bg_heun") return run<BinnedGabrielHeun>(in, out, steps, dt, false);
+    if (scenario == "bg_heun_functor") return run<BinnedGabrielHeun>(in, out, steps, dt, true);
+    if (scenario == "bg_heun_com") return run<BinnedGabrielHeunCom>(in, out, steps, dt, false);
+    if (scenario == "bg_heun_2d") return run<BinnedGabrielHeun2D>(in, out, steps, dt, false);
+    if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
+    if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
+    if (scenario == "drag") return run_drag(in, dt);
+  } catch (const Error& e) {
+    std::fprintf(stderr, "tecs error: %s\n", e.what());
+    return 1;
+  }
+  std::fprintf(stderr, "unknown scenario %s\n", scenario.c_str());
+  return 2;
+}
