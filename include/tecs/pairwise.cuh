@@ -132,9 +132,12 @@ struct PairLawBinding {
 }  // namespace detail
 }  // namespace tecs
 
-#define PAIRWISE_FORCE_PARAMETERS                                                                          \
-  const bool is_full_step, const unsigned int i, const unsigned int j, const Vector &displacement,          \
-      const Scalar distance, Random &rng, Scalar &drag, const PairwiseForceFields &ctx
+// the reference's parameter list (utils.hpp:206-209); a law need not use them all
+#define PAIRWISE_FORCE_PARAMETERS                                                                              \
+  [[maybe_unused]] const bool is_full_step, [[maybe_unused]] const unsigned int i,                             \
+      [[maybe_unused]] const unsigned int j, [[maybe_unused]] const Vector &displacement,                      \
+      [[maybe_unused]] const Scalar distance, [[maybe_unused]] Random &rng, [[maybe_unused]] Scalar &drag,     \
+      [[maybe_unused]] const PairwiseForceFields &ctx
 #define PAIRWISE_REF(TYPE, NAME) tecs::detail::PairwiseFieldRef<TYPE> NAME
 
 // a lambda factory, as the reference's: PAIRWISE_FORCE(body)() is the law

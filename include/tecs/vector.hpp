@@ -9,6 +9,7 @@
 #ifndef TECS_CXX_VECTOR_HPP
 #define TECS_CXX_VECTOR_HPP
 
+#include <cfloat>
 #include <cmath>
 #include <cstddef>
 #include <type_traits>
@@ -27,6 +28,11 @@ TECS_HD inline float sqrt_(float v) { return sqrtf(v); }
 TECS_HD inline double sqrt_(double v) { return sqrt(v); }
 TECS_HD inline float fmax_(float a, float b) { return fmaxf(a, b); }
 TECS_HD inline double fmax_(double a, double b) { return fmax(a, b); }
+// the machine epsilon (Kokkos::Experimental::epsilon_v)
+template <typename Scalar>
+TECS_HD constexpr Scalar epsilon_() {
+  return sizeof(Scalar) == sizeof(float) ? Scalar(FLT_EPSILON) : Scalar(DBL_EPSILON);
+}
 }  // namespace detail
 
 template <typename Scalar, int dimensions>
@@ -126,8 +132,10 @@ struct Polarity_ : VectorN<Scalar, 2> {
   constexpr Polarity_() = default;
   TECS_HD constexpr explicit Polarity_(Scalar v) : Base(v) {}
   TECS_HD constexpr Polarity_(Scalar theta, Scalar phi) : Base(theta, phi) {}
-  // the direction of v (polarity.hpp:74-77)
+  // the direction of v (polarity.hpp:62-77), its length given or computed
   TECS_HD explicit Polarity_(const Vector3<Scalar>& v) : Polarity_(from_vector3(v)) {}
+  TECS_HD Polarity_(const Vector3<Scalar>& v, Scalar length) : Polarity_(from_vector3(v, length)) {}
+  TECS_HD constexpr Polarity_(const Base& b) : Base(b) {}
 
   TECS_HD constexpr Scalar& theta() { return this->data_[0]; }
   TECS_HD constexpr const Scalar& theta() const { return this->data_[0]; }
@@ -148,6 +156,44 @@ struct Polarity_ : VectorN<Scalar, 2> {
   TECS_HD Scalar dot(const Polarity_& o) const {
     return std::sin(theta()) * std::sin(o.theta()) * std::cos(phi() - o.phi()) +
            std::cos(theta()) * std::cos(o.theta());
+  }
+
+  // The force laws of the reference's polarity programs, with its operations
+  // (polarity.hpp:138-198).  The angular gradient of dot(other) that turns
+  // this polarity towards other; no phi term where sin(theta) is within
+  // epsilon of 0.
+  TECS_HD Polarity_ unidirectional_polarization_force(const Polarity_& other) const {
+    Polarity_ r(std::cos(theta()) * std::sin(other.theta()) * std::cos(phi() - other.phi()) -
+                    std::sin(theta()) * std::cos(other.theta()),
+                Scalar(0));
+    const Scalar st = std::sin(theta());
+    if (std::abs(st) > detail::epsilon_<Scalar>())
+      r[1] = -std::sin(other.theta()) * std::sin(phi() - other.phi()) / st;
+    return r;
+  }
+  // the same, scaled by the alignment dot(other)
+  TECS_HD Polarity_ bidirectional_polarization_force(const Polarity_& other) const {
+    return Polarity_(dot(other) * unidirectional_polarization_force(other));
+  }
+  struct BendingForceResult {
+    Vector3<Scalar> vector;  // force on the cell
+    Polarity_ polarity;      // change of its polarity
+  };
+  // Bending between this cell and a neighbour at displacement (this - other).
+  // The squares prod^2 / distance^2 are formed in double, as the reference's
+  // pow(Scalar, int) promotes them; a float's square is exact in double.
+  TECS_HD BendingForceResult bending_force(const Vector3<Scalar>& displacement, const Polarity_& other_polarity,
+                                           const Scalar distance) const {
+    const Vector3<Scalar> this_vector = to_vector3();
+    const Scalar prod_i = this_vector.dot(displacement) / distance;
+    const Vector3<Scalar> other_vector = to_vector3(other_polarity);
+    const Scalar prod_j = other_vector.dot(displacement) / distance;
+    const double d2 = double(distance) * double(distance);
+    const Scalar ci = Scalar(double(prod_i) * double(prod_i) / d2);
+    const Scalar cj = Scalar(double(prod_j) * double(prod_j) / d2);
+    return BendingForceResult{-prod_i / distance * this_vector + ci * displacement + -prod_j / distance * other_vector +
+                                  cj * displacement,
+                              Polarity_(-prod_i * unidirectional_polarization_force(Polarity_(displacement, distance)))};
   }
 };
 

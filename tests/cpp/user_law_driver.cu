@@ -7,7 +7,8 @@
 //   user_law_driver <scenario> <in.bin> <out_prefix> <steps> <dt>
 //
 // in.bin and the outputs are those of drop_in_driver.cpp (.pairs, .dpos,
-// .pos; link scenarios read the links and write .pos only).  Scenario
+// .pos, and .pol for "bg_heun_pol"; link scenarios read the links and write
+// .pos only).  Scenario
 // "rng_twice" steps two copies of the input with a law that draws from rng and
 // writes <out>.a.pos and <out>.b.pos; "drag" steps with a law that sets drag
 // and must fail with tecs::Error.
@@ -36,6 +37,10 @@ CREATE_SIMULATION_CONFIG(BinnedGabrielHeunCom,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
                          CONFIG_INTEGRATOR(integrators::Heun)
                          CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
+CREATE_SIMULATION_CONFIG(EpithelialSheet,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun)
+                         CONFIG_FIELDS((Vector, position), (Polarity, polarity)))
 struct BinnedGabrielHeun2D : public DefaultSimulationConfig {
   CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
   CONFIG_INTEGRATOR(integrators::Heun)
@@ -123,6 +128,10 @@ static void fill(Simulation<Config>& sim, const Input& in) {
     for (int d = 0; d < D; ++d) positions(i)[d] = in.x[std::size_t(i) * D + d];
   auto& links = sim.get_links();
   for (unsigned l = 0; l < in.links.size() / 2; ++l) links(l) = Link{in.links[2 * l], in.links[2 * l + 1]};
+  if constexpr (Simulation<Config>::has_polarity) {
+    auto& polarity = sim.template get_view<FIELD(Polarity_<float>, polarity)>();
+    for (unsigned i = 0; i < in.n; ++i) polarity(i) = Polarity_<float>(in.p[2 * i], in.p[2 * i + 1]);
+  }
 }
 
 template <typename Config>
@@ -151,6 +160,37 @@ static int run(const Input& in, const std::string& out, int steps, double dt, bo
   else go(spring());
   const auto& x = sim.get_positions_view();
   write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  return 0;
+}
+
+// the epithelium law: the spring plus k_pol * (bending + bidirectional alignment), written with the
+// reference's Polarity_ force functions as its polarity programs write it
+static int run_polarity(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(EpithelialSheet)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11], k_pol = in.prm[12];
+  auto epithelium = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+    auto bend = ctx.polarity.self.bending_force(displacement, ctx.polarity.other, distance);
+    ctx.position.delta += bend.vector * k_pol;
+    ctx.polarity.delta += bend.polarity * k_pol;
+    ctx.polarity.delta += ctx.polarity.self.bidirectional_polarization_force(ctx.polarity.other) * k_pol;
+  );
+  Simulation<EpithelialSheet> sim(settings_of<EpithelialSheet>(in));
+  fill(sim, in);
+  std::vector<Vector> deltas;
+  const auto pairs = sim.evaluate(epithelium(), &deltas);
+  std::vector<unsigned> flat;
+  for (const auto& pr : pairs) { flat.push_back(pr.first); flat.push_back(pr.second); }
+  write_raw(out + ".pairs", flat.data(), flat.size() * 4);
+  write_raw(out + ".dpos", deltas.data(), deltas.size() * sizeof(Vector));
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, epithelium());
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  const auto& p = sim.template get_view<FIELD(Polarity_<float>, polarity)>();
+  write_raw(out + ".pol", p.data(), std::size_t(sim.get_agent_count()) * 8);
   return 0;
 }
 
@@ -230,6 +270,7 @@ int main(int argc, char** argv) {
     if (scenario == "bg_heun_functor") return run<BinnedGabrielHeun>(in, out, steps, dt, true);
     if (scenario == "bg_heun_com") return run<BinnedGabrielHeunCom>(in, out, steps, dt, false);
     if (scenario == "bg_heun_2d") return run<BinnedGabrielHeun2D>(in, out, steps, dt, false);
+    if (scenario == "bg_heun_pol") return run_polarity(in, out, steps, dt);
     if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
     if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
     if (scenario == "drag") return run_drag(in, dt);

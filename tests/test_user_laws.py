@@ -44,10 +44,13 @@ def driver(tmp_path_factory):
 
 def write_input(path, g):
     x0 = g["x0"]
+    p0 = g.get("p0")
     with open(path, "wb") as f:
-        np.array([len(x0), x0.shape[1], 0], np.uint32).tofile(f)
+        np.array([len(x0), x0.shape[1], 0 if p0 is None else 1], np.uint32).tofile(f)
         g["prm"].astype(np.float32).tofile(f)
         x0.astype(np.float32).tofile(f)
+        if p0 is not None:
+            p0.astype(np.float32).tofile(f)
         if "links" in g:
             np.array([len(g["links"])], np.uint32).tofile(f)
             g["links"].astype(np.uint32).tofile(f)
@@ -90,6 +93,7 @@ CASES = [
     ("bg_heun_functor", "bg_heun", True),
     ("bg_heun_2d", "bg_heun_2d", True),
     ("bg_heun_com", "bg_heun_com", False),
+    ("bg_heun_pol", "bg_heun_polarity", False),
 ]
 
 
@@ -108,6 +112,8 @@ def test_user_law_reproduces_reference(driver, tmp_path, scenario, name, exact):
         np.testing.assert_array_equal(pos, g["pos"])
     else:
         assert close(dpos, g["dpos"]) and close(pos, g["pos"])
+    if "pol" in g:
+        assert close(np.fromfile(f"{out}.pol", np.float32).reshape(-1, 2), g["pol"])
 
 
 @pytest.mark.gpu
