@@ -25,6 +25,9 @@
 //   drag           must stay 0: the drag term is not supported, and a law that
 //                  sets it makes the next count or download fail
 //   ctx            ctx.<field>.self / .other / .delta for the config's fields
+// A GENERIC_FORCE law (per cell: is_full_step, i, rng, ctx.<field>.self /
+// .delta) runs in the same pass, added before the pair sums as the reference
+// orders it; it combines with a PAIRWISE_FORCE law or runs alone.
 // Finders: the non-symmetric all-pairs and Gabriel finders (naive and binned).
 #ifndef TECS_CXX_PAIRWISE_CUH
 #define TECS_CXX_PAIRWISE_CUH
@@ -45,57 +48,91 @@
 namespace tecs {
 namespace detail {
 
-// PAIRWISE_FORCE's value: the law lambda with the pairwise tag
-template <typename L>
-struct PairwiseForce {
-  using tag = PairwiseForceTag;
+// PAIRWISE_FORCE's and GENERIC_FORCE's values: the law lambda with its tag
+template <typename L, typename Tag>
+struct TaggedForce {
+  using tag = Tag;
   L f;
   template <typename... A>
   __host__ __device__ void operator()(A&&... a) const {
     f(static_cast<A&&>(a)...);
   }
 };
-struct PairwiseForceMaker {
+template <typename Tag>
+struct TaggedForceMaker {
   template <typename L>
-  PairwiseForce<L> operator|(L f) const {
-    return PairwiseForce<L>{f};
+  TaggedForce<L, Tag> operator|(L f) const {
+    return TaggedForce<L, Tag>{f};
   }
 };
-inline constexpr PairwiseForceMaker pairwise_force{};
+inline constexpr TaggedForceMaker<PairwiseForceTag> pairwise_force{};
+inline constexpr TaggedForceMaker<GenericForceTag> generic_force{};
 
-// The law in the form k_pass_law calls: the pair's values as the config's
-// types, the cell's running sums as the deltas, the law, the sums back.
-template <typename Config, typename F>
+// The laws in the form k_pass_law calls them: the values as the config's
+// types, the running sums as the deltas, the law, the sums back.  G: the
+// GENERIC_FORCE law or NoLaw; P: the PAIRWISE_FORCE law or NoLaw.
+template <typename Config, typename G, typename P>
 struct PairLaw {
-  F law;
+  static constexpr bool kGeneric = !std::is_same_v<G, NoLaw>;
+  G gen;
+  P law;
+
+  __device__ void generic(const PassArgs& a, unsigned idi, const float* xi, float2 pi, Acc& acc) const {
+    if constexpr (kGeneric) {
+      constexpr int D = Config::dimensions;
+      using Vector = VectorN<float, D>;
+      using Fields = typename Config::template ForceFields<GenericFieldRef>;
+      Vector self, delta;
+      for (int d = 0; d < D; ++d) {
+        self[d] = xi[d];
+        delta[d] = acc.x[d];
+      }
+      CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 3u : 4u, idi, idi);
+      if constexpr (Simulation<Config>::has_polarity) {
+        const Polarity_<float> ps(pi.x, pi.y);
+        Polarity_<float> pd(acc.p[0], acc.p[1]);
+        const Fields ctx{{self, delta}, {ps, pd}};
+        gen(a.full_step != 0, idi, rng, ctx);
+        acc.p[0] = pd[0];
+        acc.p[1] = pd[1];
+      } else {
+        const Fields ctx{{self, delta}};
+        gen(a.full_step != 0, idi, rng, ctx);
+      }
+      for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
+    }
+  }
+
   __device__ void operator()(const PassArgs& a, unsigned idi, unsigned idj, const float* xi, const float4& vj,
                              const float* disp, float dist, float2 pi, float2 pj, Acc& acc) const {
-    constexpr int D = Config::dimensions;
-    using Vector = VectorN<float, D>;
-    using Fields = typename Config::template ForceFields<PairwiseFieldRef>;
-    Vector self, other, displacement, delta;
-    const float xj[3] = {vj.x, vj.y, vj.z};
-    for (int d = 0; d < D; ++d) {
-      self[d] = xi[d];
-      other[d] = xj[d];
-      displacement[d] = disp[d];
-      delta[d] = acc.x[d];
+    if constexpr (!std::is_same_v<P, NoLaw>) {
+      constexpr int D = Config::dimensions;
+      using Vector = VectorN<float, D>;
+      using Fields = typename Config::template ForceFields<PairwiseFieldRef>;
+      Vector self, other, displacement, delta;
+      const float xj[3] = {vj.x, vj.y, vj.z};
+      for (int d = 0; d < D; ++d) {
+        self[d] = xi[d];
+        other[d] = xj[d];
+        displacement[d] = disp[d];
+        delta[d] = acc.x[d];
+      }
+      float drag = 0.f;
+      CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
+      if constexpr (Simulation<Config>::has_polarity) {
+        const Polarity_<float> ps(pi.x, pi.y), po(pj.x, pj.y);
+        Polarity_<float> pd(acc.p[0], acc.p[1]);
+        const Fields ctx{{self, other, delta}, {ps, po, pd}};
+        law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
+        acc.p[0] = pd[0];
+        acc.p[1] = pd[1];
+      } else {
+        const Fields ctx{{self, other, delta}};
+        law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
+      }
+      for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
+      if (drag != 0.f) atomicOr(&a.ctr->error, 2u);
     }
-    float drag = 0.f;
-    CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
-    if constexpr (Simulation<Config>::has_polarity) {
-      const Polarity_<float> ps(pi.x, pi.y), po(pj.x, pj.y);
-      Polarity_<float> pd(acc.p[0], acc.p[1]);
-      const Fields ctx{{self, other, delta}, {ps, po, pd}};
-      law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
-      acc.p[0] = pd[0];
-      acc.p[1] = pd[1];
-    } else {
-      const Fields ctx{{self, other, delta}};
-      law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
-    }
-    for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
-    if (drag != 0.f) atomicOr(&a.ctr->error, 2u);
   }
 };
 
@@ -103,26 +140,26 @@ template <typename Config>
 using FinderOf = typename Config::template PairFinderT<Config>;
 
 // the launcher the library calls for every force evaluation
-template <typename Config, typename F>
+template <typename Config, typename Law>
 int pair_law_launcher(void* user, const void* call, void* stream) {
   static_assert(!FinderOf<Config>::symmetric && FinderOf<Config>::finder_id <= TECS_FINDER_BINNED_GABRIEL,
-                "user pairwise laws run with the non-symmetric all-pairs and Gabriel finders");
+                "user laws run with the non-symmetric all-pairs and Gabriel finders");
   return launch_user_pass<Config::dimensions, FinderOf<Config>::finder_id>(
-      static_cast<const UserPassCall*>(call), static_cast<cudaStream_t>(stream),
-      *static_cast<const PairLaw<Config, F>*>(user));
+      static_cast<const UserPassCall*>(call), static_cast<cudaStream_t>(stream), *static_cast<const Law*>(user));
 }
 
-template <typename Config, typename F>
+template <typename Config, typename G, typename P>
 struct PairLawBinding {
-  // Binds the law unless the same law with the same captured values is bound
-  // already; a new binding makes the library re-capture its step graph.
-  static void bind(tecs_sim* handle, int device, const F& f, std::shared_ptr<void>& holder,
+  using Law = PairLaw<Config, G, P>;
+  // Binds the laws unless the same laws with the same captured values are
+  // bound already; a new binding makes the library re-capture its step graph.
+  static void bind(tecs_sim* handle, int device, const G& g, const P& p, std::shared_ptr<void>& holder,
                    tecs_pair_law_fn& bound) {
-    const tecs_pair_law_fn fn = &pair_law_launcher<Config, F>;
-    auto next = std::make_shared<PairLaw<Config, F>>(PairLaw<Config, F>{f});
-    if (holder && bound == fn && std::memcmp(holder.get(), next.get(), sizeof(PairLaw<Config, F>)) == 0) return;
-    if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, PairLaw<Config, F>>(device))
-      throw Error("cannot load the user pairwise law's pass on the device");
+    const tecs_pair_law_fn fn = &pair_law_launcher<Config, Law>;
+    auto next = std::make_shared<Law>(Law{g, p});
+    if (holder && bound == fn && std::memcmp(holder.get(), next.get(), sizeof(Law)) == 0) return;
+    if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
+      throw Error("cannot load the user laws' pass on the device");
     check(tecs_sim_set_pair_law(handle, fn, next.get()));
     holder = next;
     bound = fn;
@@ -147,8 +184,21 @@ struct PairLawBinding {
   }
 
 // a functor's call operator: struct Law { PAIRWISE_FORCE_OP { body } };
-#define PAIRWISE_FORCE_OP                  \
+#define PAIRWISE_FORCE_OP                     \
   using tag = tecs::detail::PairwiseForceTag; \
   __host__ __device__ void operator()(PAIRWISE_FORCE_PARAMETERS) const
+
+// per-cell laws (integrators/base.hpp:116-142): ctx.<field>.self / .delta
+#define GENERIC_FORCE_PARAMETERS                                                                   \
+  [[maybe_unused]] const bool is_full_step, [[maybe_unused]] const unsigned int i,                 \
+      [[maybe_unused]] Random &rng, [[maybe_unused]] const GenericForceFields &ctx
+#define GENERIC_REF(TYPE, NAME) tecs::detail::GenericFieldRef<TYPE> NAME
+#define GENERIC_FORCE(...)                                                                                \
+  [&]() {                                                                                                 \
+    return tecs::detail::generic_force | [=] __host__ __device__(GENERIC_FORCE_PARAMETERS) { __VA_ARGS__ }; \
+  }
+#define GENERIC_FORCE_OP                     \
+  using tag = tecs::detail::GenericForceTag; \
+  __host__ __device__ void operator()(GENERIC_FORCE_PARAMETERS) const
 
 #endif  // TECS_CXX_PAIRWISE_CUH

@@ -67,18 +67,26 @@ class View {
 };
 
 namespace detail {
-// the tag of a user pairwise law: a PAIRWISE_FORCE lambda or a PAIRWISE_FORCE_OP functor
+// the tags of user laws: PAIRWISE_FORCE / GENERIC_FORCE lambdas and their _OP functors
 // (include/utils/utils.hpp:181-276), defined with tecs/pairwise.cuh
 struct PairwiseForceTag {};
+struct GenericForceTag {};
+template <typename F, typename Tag>
+concept TaggedLaw = requires { typename F::tag; } && std::is_same_v<typename F::tag, Tag>;
 template <typename F>
-concept UserPairLaw = requires { typename F::tag; } && std::is_same_v<typename F::tag, PairwiseForceTag>;
+concept UserPairLaw = TaggedLaw<F, PairwiseForceTag>;
+template <typename F>
+concept UserGenericLaw = TaggedLaw<F, GenericForceTag>;
 template <typename F>
 constexpr bool is_link_law() {
   if constexpr (requires { F::is_link; }) return F::is_link;
   else return false;
 }
-// Hands a user law to a simulation's library handle; defined by tecs/pairwise.cuh.
-template <typename Config, typename F>
+// no law of that kind in the step
+struct NoLaw {};
+// Hands a step's user laws (generic G, pairwise P; NoLaw where absent) to a
+// simulation's library handle; defined by tecs/pairwise.cuh.
+template <typename Config, typename G, typename P>
 struct PairLawBinding;
 }  // namespace detail
 
@@ -247,8 +255,10 @@ class Simulation {
   // n steps queued at once (one graph replay each)
   template <typename... Forces>
   void take_steps(double dt, int n, const Forces&... forces) {
-    static_assert((0 + ... + (detail::is_link_law<Forces>() ? 0 : 1)) <= 1, "one pairwise law per step");
+    static_assert((0 + ... + (detail::is_link_law<Forces>() || detail::UserGenericLaw<Forces> ? 0 : 1)) <= 1,
+                  "one pairwise law per step");
     static_assert((0 + ... + (detail::is_link_law<Forces>() ? 1 : 0)) <= 1, "one link law per step");
+    static_assert((0 + ... + (detail::UserGenericLaw<Forces> ? 1 : 0)) <= 1, "one generic law per step");
     apply_pair_law(forces...);
     apply_link_law(forces...);
     upload_if_dirty();
@@ -350,25 +360,49 @@ class Simulation {
     return s;
   }
 
-  // the pairwise law of this step (none: pairs only, no deltas); a user law
-  // replaces the built-in one until a step passes a built-in law again
+  // the first force of type kind in the pack, or NoLaw{}
+  template <template <typename> class Is, typename F0, typename... Fs>
+  static const auto& first_of(const F0& f0, const Fs&... fs) {
+    if constexpr (Is<F0>::value) return f0;
+    else return first_of<Is>(fs...);
+  }
+  template <template <typename> class Is>
+  static const detail::NoLaw& first_of() {
+    static const detail::NoLaw none{};
+    return none;
+  }
+  template <typename F>
+  struct IsGeneric : std::bool_constant<detail::UserGenericLaw<F>> {};
+  template <typename F>
+  struct IsUserPair : std::bool_constant<detail::UserPairLaw<F>> {};
+
+  // the pairwise law of this step (none: pairs only, no deltas); user laws
+  // (a PAIRWISE_FORCE law, a GENERIC_FORCE law, or both) replace the built-in
+  // one until a step passes a built-in law again
   template <typename... Forces>
   void apply_pair_law(const Forces&... forces) {
     int id = TECS_FORCE_NONE;
     float k[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    bool user = false;
+    constexpr bool generic = (false || ... || detail::UserGenericLaw<Forces>);
+    constexpr bool user_pair = (false || ... || detail::UserPairLaw<Forces>);
+    constexpr bool user = generic || user_pair;
     auto one = [&](const auto& f) {
       using F = std::decay_t<decltype(f)>;
-      if constexpr (detail::UserPairLaw<F>) {
-        user = true;
-        detail::PairLawBinding<Config, F>::bind(handle_, settings_.device, f, law_holder_, law_fn_);
-      } else if constexpr (!detail::is_link_law<F>()) {
+      if constexpr (!detail::UserPairLaw<F> && !detail::UserGenericLaw<F> && !detail::is_link_law<F>()) {
+        static_assert(!user || sizeof(F) == 0,
+                      "a GENERIC_FORCE law combines with a PAIRWISE_FORCE law, not a built-in one");
         static_assert(!F::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
         id = F::force_id;
         k[0] = f.k_rep; k[1] = f.r_rep; k[2] = f.k_adh; k[3] = f.r_adh; k[4] = f.k_pol_value();
       }
     };
     (one(forces), ...);
+    if constexpr (user) {
+      const auto& g = first_of<IsGeneric>(forces...);
+      const auto& p = first_of<IsUserPair>(forces...);
+      detail::PairLawBinding<Config, std::decay_t<decltype(g)>, std::decay_t<decltype(p)>>::bind(
+          handle_, settings_.device, g, p, law_holder_, law_fn_);
+    }
     if (!user && law_fn_) {
       check(tecs_sim_set_pair_law(handle_, nullptr, nullptr));
       law_holder_.reset();

@@ -266,6 +266,40 @@ static int tecs_driver_run_links(const Input& in, const std::string& out, int st
   return 0;
 }
 
+// Generic-force scenarios: a GENERIC_FORCE law (a pull towards the origin on
+// full steps, a constant push on Heun's second evaluation) with the spring
+// pairwise law, passed pairwise first: the reference evaluates the generic
+// force first (kernel_fuser.hpp:148-156).  Writes <out>.pos only.
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields, class GenericForceFields>
+static int tecs_driver_run_generic(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() { return PAIRWISE_FORCE(TECS_DRIVER_SPRING)(); };
+  auto make_generic = GENERIC_FORCE(
+    if (is_full_step) ctx.position.delta += ctx.position.self * Scalar(-0.02);
+    else ctx.position.delta += Vector(Scalar(0.001));
+  );
+  typename Simulation<Config>::Settings st(n, "unused");
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+  auto force = make_force();
+  auto generic = make_generic();
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, force, generic);
+  std::vector<float> flat((size_t)n * in.dims);
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) flat[(size_t)i * in.dims + d] = pos(i)[d];
+  write_raw(out + ".pos", flat.data(), flat.size() * 4);
+  return 0;
+}
+
 // The reference's writer on a stepped simulation: write_static, write(0), then
 // take_step + write(); its XDMF sidecar <out>.xmf is the output (the HDF5
 // calls go to the HighFive stand-in and write nothing).
@@ -343,6 +377,15 @@ static int run(const Input& in, const std::string& out, int steps, double dt) {
 }
 }  // namespace lk_writer_3
 TECS_LINK_SCENARIO(lk_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::GlobalComFixer)
+namespace gen_bg_heun_3 {
+CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel) CONFIG_INTEGRATOR(integrators::Heun)
+                                     CONFIG_WRITER(tecs::io::Dummy) TECS_FIELDS_0)
+EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)
+static int run(const Input& in, const std::string& out, int steps, double dt) {
+  return tecs_driver_run_generic<Config, Scalar, Vector, Random, PairwiseForceFields, GenericForceFields>(in, out,
+                                                                                                        steps, dt);
+}
+}  // namespace gen_bg_heun_3
 
 int main(int argc, char** argv) {
   if (argc < 6) {
@@ -361,7 +404,7 @@ int main(int argc, char** argv) {
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2) DISPATCH(nd_euler_2) DISPATCH(nd_heun_3)
-  DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3) DISPATCH(lk_writer_3)
+  DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3) DISPATCH(lk_writer_3) DISPATCH(gen_bg_heun_3)
 #undef DISPATCH
   if (rc == 3) std::fprintf(stderr, "unknown scenario %s\n", sc.c_str());
   return rc;

@@ -902,7 +902,13 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 // k_pass, so a law written like a built-in one gives the built-in's bits.
 // Law is a device callable adding the pair (self = i, other = j) to acc:
 //   law(a, id_i, id_j, x_i, x_j (w = key or id), displacement x_i - x_j, distance, p_i, p_j, acc)
-// with displacement[2] = 0 in 2-D and p = 0 without polarity.
+// with displacement[2] = 0 in 2-D and p = 0 without polarity.  With
+// Law::kGeneric it also carries a per-cell (GENERIC_FORCE) law,
+//   law.generic(a, id_i, x_i, p_i, g)
+// adding to a zero g; the reference evaluates it before the pairwise forces
+// (integrators/base.hpp:116-142, kernel_fuser.hpp:148-156), into the cleared
+// stage buffer that the pair sums are then added to, so the cell's delta is
+// 0 + (g + pair sum) -- the reference's ((0 + g) + pair sum) + 0 bit for bit.
 
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
@@ -971,7 +977,16 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, Force
     vi = a.X[i];
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
-    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc, law);
+    const unsigned idi = id_at(a.X, a.Bid, i);
+    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, idi, acc, law);
+    if constexpr (Law::kGeneric) {
+      Acc gen = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+      law.generic(a, idi, xi, pi, gen);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) acc.x[d] = gen.x[d] + acc.x[d];
+      acc.p[0] = gen.p[0] + acc.p[0];
+      acc.p[1] = gen.p[1] + acc.p[1];
+    }
   }
   pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
 }

@@ -194,6 +194,29 @@ static int run_polarity(const Input& in, const std::string& out, int steps, doub
   return 0;
 }
 
+// a GENERIC_FORCE law with the spring, passed pairwise first; the generic
+// force is evaluated first, as the reference fuses them.  Writes .pos only.
+static int run_generic(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  auto spring = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+  );
+  auto pull = GENERIC_FORCE(
+    if (is_full_step) ctx.position.delta += ctx.position.self * Scalar(-0.02);
+    else ctx.position.delta += Vector(Scalar(0.001));
+  );
+  Simulation<BinnedGabrielHeun> sim(settings_of<BinnedGabrielHeun>(in));
+  fill(sim, in);
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, spring(), pull());
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  return 0;
+}
+
 // links and a user law in one step, as the reference's protrusion programs
 template <typename Config>
 static int run_links(const Input& in, const std::string& out, int steps, double dt) {
@@ -271,6 +294,7 @@ int main(int argc, char** argv) {
     if (scenario == "bg_heun_com") return run<BinnedGabrielHeunCom>(in, out, steps, dt, false);
     if (scenario == "bg_heun_2d") return run<BinnedGabrielHeun2D>(in, out, steps, dt, false);
     if (scenario == "bg_heun_pol") return run_polarity(in, out, steps, dt);
+    if (scenario == "gen_bg_heun") return run_generic(in, out, steps, dt);
     if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
     if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
     if (scenario == "drag") return run_drag(in, dt);

@@ -60,6 +60,8 @@ SCENARIOS = {
     "lk_writer": ("lk_writer_3", 3, 0, 1, 0, 3, 1),
     # the same without links: the grids' topology is then the cells as vertices
     "lk_writer_nolinks": ("lk_writer_3", 3, 0, 1, 0, 3, 1),
+    # a GENERIC_FORCE law with the spring: final positions only
+    "gen_bg_heun": ("gen_bg_heun_3", 3, 0, 1, 0, 3, 0),
 }
 
 
@@ -154,6 +156,10 @@ def inputs(name):
     elif name == "nd_heun_3d":
         x = wl.ball(48, 15)
         mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
+    elif name == "gen_bg_heun":
+        x = wl.ball(2000, 19)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 10, 0.05
     else:
         raise KeyError(name)
     prm[2:5] = mn
@@ -192,6 +198,8 @@ def run(name):
                "pos": np.fromfile(f"{out}.pos", np.float32).reshape(-1, dims)}
         if links is not None:
             res["links"] = links
+        elif scen.startswith("gen_"):
+            pass
         else:
             res["pairs"] = np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2)
             res["dpos"] = np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims)

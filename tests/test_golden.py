@@ -44,14 +44,18 @@ LINKED = sorted(k for k in KIND if k.startswith("lk_"))
 # fixtures of the reference's HDF5_Writer: the inputs and the XDMF sidecar
 # (tests/test_cpp_drop_in.py compares the drop-in writer's with it)
 WRITER = ["lk_writer", "lk_writer_nolinks"]
+# fixtures of a GENERIC_FORCE law with the spring: the reference's final state,
+# which the user-law program reproduces on a GPU (tests/test_user_laws.py);
+# the C restatement has built-in laws only
+USER_LAW = ["gen_bg_heun"]
 
 
 def load(name):
     return dict(np.load(GOLDEN / f"{name}.npz"))
 
 
-def make_oracle(name, g):
-    finder, sym, integ, com, dims, pol = KIND[name]
+def make_oracle(name, g, kind=None):
+    finder, sym, integ, com, dims, pol = kind or KIND[name]
     prm = g["prm"]
     n = len(g["x0"])
     cap = max(int(prm[13]), n)
@@ -68,7 +72,9 @@ def make_oracle(name, g):
 
 
 def test_manifest_covers_every_fixture():
-    assert set(MANIFEST) == set(KIND) | set(WRITER)
+    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW)
+    for name in USER_LAW:
+        assert (GOLDEN / f"{name}.npz").exists()
     for name in list(KIND) + WRITER:
         assert (GOLDEN / f"{name}.npz").exists()
     for name in WRITER:
@@ -133,3 +139,14 @@ def test_link_fixtures_include_skipped_and_repeated_links():
         lk = load(name)["links"]
         assert (lk[:, 0] == lk[:, 1]).any()
         assert len(np.unique(lk, axis=0)) < len(lk)
+
+
+def test_generic_force_fixture_is_the_spring_plus_the_generic_pull():
+    # the same input under the spring alone ends elsewhere; the generic law pulls cells towards the
+    # origin on full steps, so the reference's run ends more contracted
+    g = load("gen_bg_heun")
+    o = make_oracle("gen_bg_heun", g, kind=KIND["bg_heun"])
+    o.step(float(g["dt"]), int(g["steps"]))
+    spring_only, _ = o.get_state()
+    assert np.isfinite(g["pos"]).all() and not np.array_equal(g["pos"], spring_only)
+    assert np.sqrt((g["pos"] ** 2).sum(1)).mean() < np.sqrt((spring_only ** 2).sum(1)).mean()

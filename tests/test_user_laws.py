@@ -125,6 +125,15 @@ def test_user_law_with_links_reproduces_reference(driver, tmp_path):
 
 
 @pytest.mark.gpu
+def test_generic_law_with_pairwise_law_reproduces_reference(driver, tmp_path):
+    """take_step(dt, PAIRWISE_FORCE(...)(), GENERIC_FORCE(...)()): the generic law (is_full_step-dependent,
+    reading ctx.position.self) is added before the pair sums, as the reference fuses them; bit for bit."""
+    g, out, r = run(driver, "gen_bg_heun", "gen_bg_heun", tmp_path)
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3), g["pos"])
+
+
+@pytest.mark.gpu
 def test_user_law_random_draws_are_reproducible(driver, tmp_path):
     """A law drawing from rng gives the same run twice, and a run that differs from the plain spring's."""
     g, out, r = run(driver, "rng_twice", "bg_heun", tmp_path, steps=5)
