@@ -83,6 +83,18 @@ def test_user_law_program_builds_and_fails_cleanly_without_a_device(tmp_path):
     assert r.returncode == 1 and "tecs error" in r.stderr
 
 
+def test_counter_random_is_reproducible_and_well_distributed(tmp_path):
+    """tests/cpp/random_checks.cpp: the generator user laws draw from (host build of the same code)."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "random_checks"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
+                        str(SOURCE.parent / "random_checks.cpp"), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+
+
 CASES = [
     # (scenario, fixture, exact)
     ("na_heun", "na_heun", True),
