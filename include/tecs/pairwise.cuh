@@ -156,10 +156,11 @@ struct PairLawBinding {
   static void bind(tecs_sim* handle, int device, const G& g, const P& p, std::shared_ptr<void>& holder,
                    tecs_pair_law_fn& bound) {
     const tecs_pair_law_fn fn = &pair_law_launcher<Config, Law>;
-    auto next = std::make_shared<Law>(Law{g, p});
-    if (holder && bound == fn && std::memcmp(holder.get(), next.get(), sizeof(Law)) == 0) return;
+    const Law law{g, p};
+    if (holder && bound == fn && std::memcmp(holder.get(), &law, sizeof(Law)) == 0) return;
     if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
       throw Error("cannot load the user laws' pass on the device");
+    auto next = std::make_shared<Law>(law);
     check(tecs_sim_set_pair_law(handle, fn, next.get()));
     holder = next;
     bound = fn;
