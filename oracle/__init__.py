@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
-The oracle is the checker the CUDA path is compared against.  Only the test
+The oracle is the CPU result the CUDA path is compared against.  Only the test
 suite, ``__graft_entry__.smoke()`` and the benchmark's CPU-baseline leg import
 this module; the product package never does.
 """

@@ -1,8 +1,9 @@
 /*
  * tecs_oracle.c -- CPU restatement of the TECS per-timestep hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, used by tests/,
- * the smoke check and the benchmark's CPU-baseline leg.  Never part of the
+ * TEST INFRASTRUCTURE ONLY: the CPU result the CUDA path is compared
+ * against, used by tests/, the smoke check and the benchmark's CPU-baseline
+ * leg.  Never part of the
  * product library.
  *
  * Every function cites the reference file:line it restates (paths relative

@@ -1,9 +1,9 @@
 /*
  * tecs_oracle.h -- CPU restatement of the TECS per-timestep hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This oracle is the checker that the CUDA path is
- * compared against; it is never linked into, loaded by, or called from the
- * product library.  Only the test suite, the smoke check and the benchmark's
+ * TEST INFRASTRUCTURE ONLY.  This oracle is the CPU result that the CUDA
+ * path is compared against; it is never linked into, loaded by, or called
+ * from the product library.  Only the test suite, the smoke check and the benchmark's
  * CPU-baseline leg use it.
  *
  * Parity pin: the restatement is checked against golden vectors produced by
