@@ -46,3 +46,16 @@ def test_create_without_gpu_fails_loudly():
         assert "device" in str(e).lower()
     else:
         raise AssertionError("Simulation() succeeded without a GPU")
+
+
+def test_null_handles_are_refused_without_touching_a_device():
+    # argument checks come before any CUDA call, so they work on a machine without a GPU
+    lib = tg.load()
+    lib.tecs_last_error.restype = ctypes.c_char_p
+    fn = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)(lambda u, c, s: 0)
+    lib.tecs_sim_set_pair_law.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    assert lib.tecs_sim_set_pair_law(None, ctypes.cast(fn, ctypes.c_void_p), None) != 0
+    assert b"null" in lib.tecs_last_error()
+    lib.tecs_sim_set_links.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_float]
+    assert lib.tecs_sim_set_links(None, None, 0, 0.0) != 0
+    assert b"null" in lib.tecs_last_error()
