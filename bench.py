@@ -138,7 +138,7 @@ def make_sim(w, n, mn, mx, device=0, steps=0):
                          division=tg.Division(probability=w["division"], offset=0.25), device=device)
 
 
-def make_oracle(w, n, mn, mx, steps=0):
+def make_oracle(w, n, mn, mx, steps=0, timing=False):
     import oracle
 
     cap = capacity_for(w, n, steps)
@@ -147,7 +147,7 @@ def make_oracle(w, n, mn, mx, steps=0):
                          com_fix=w["com"], min_bounds=mn, max_bounds=mx, capacity=cap,
                          force=oracle.FORCE_POLARITY if w["polarity"] else oracle.FORCE_SPRING2R,
                          k_pol=0.2 if w["polarity"] else 0.0, has_polarity=w["polarity"],
-                         division_probability=w["division"], division_offset=0.25, seed=1)
+                         division_probability=w["division"], division_offset=0.25, seed=1, timing=timing)
 
 
 class Clocks:
@@ -269,7 +269,7 @@ def traffic_per_pass(workload: str):
 
 def cpu_steps(w, n, mn, mx, x, p, steps, threads, budget_s):
     """Time up to `steps` oracle steps (about budget_s seconds) after one warm-up step."""
-    o = make_oracle(w, n, mn, mx, steps + 2)
+    o = make_oracle(w, n, mn, mx, steps + 2, timing=True)
     o.set_state(x, p)
     t0 = time.perf_counter()
     o.step(w["dt"], 1, threads)

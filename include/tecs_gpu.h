@@ -234,10 +234,13 @@ void* tecs_engine_stream(tecs_engine* engine);
  * force, queued on `stream` (a cudaStream_t, 0 = legacy default).  Allocates
  * nothing: its scratch is a static device array of about 6 MB that every GPU
  * loading the library keeps until exit.  Rejects more than
- * TECS_NOALLOC_MAX_CELLS cells or TECS_NOALLOC_MAX_BINS bins.  The first call
- * on a device looks up the array's device address (once per device), so make
- * that first call before any stream capture.  All calls on a device share the
- * array: calls whose GPU work overlaps race and must be serialised. */
+ * TECS_NOALLOC_MAX_CELLS cells or TECS_NOALLOC_MAX_BINS bins.  Runs on
+ * desc->device, which it makes current like the other entry points; the
+ * buffers and the stream must belong to that device.  The first call on a
+ * device looks up the array's device address (once per device, kept for the
+ * life of the process: resetting the device in between is not supported), so
+ * make that first call before any stream capture.  All calls on a device share
+ * the array: calls whose GPU work overlaps race and must be serialised. */
 int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d_positions, unsigned n, float* d_deltas,
                             void* stream);
 

@@ -16,6 +16,13 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libtecs_oracle.so"
+# The timed CPU baseline: the same restatement built the way the reference's
+# release build compiles (CMakeLists.txt:195-196: -O3, multiply-add
+# contraction left on).  -march=native is left out: host builds here must give
+# the same code on the x86 development container and the Arm GPU machine, and
+# aarch64's default target already has Advanced SIMD.  Its results are not
+# compared bit for bit; only its time is reported.
+LIB_TIMING = BUILD / "libtecs_oracle_rel.so"
 
 NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL, NAIVE_DELAUNAY = 0, 1, 2, 3, 4
 FORCE_NONE, FORCE_SPRING2R, FORCE_POLARITY = 0, 1, 2
@@ -49,26 +56,41 @@ class Desc(ctypes.Structure):
     ]
 
 
-def build(force: bool = False) -> Path:
-    """Compile the C restatement into oracle/_build/libtecs_oracle.so."""
+def reference_root():
+    """The TECS reference checkout, or None: $TECS_REFERENCE, else a directory
+    named ``reference`` beside this repository.  Only fixture generation and
+    the reference-header build read it; nothing on the GPU path does."""
+    env = os.environ.get("TECS_REFERENCE")
+    cand = Path(env) if env else HERE.parent.parent / "reference"
+    return cand if (cand / "include" / "tecs.hpp").exists() else None
+
+
+def build(force: bool = False, timing: bool = False) -> Path:
+    """Compile the C restatement: oracle/_build/libtecs_oracle.so (parity:
+    -O2, no multiply-add contraction) or, with timing, the -O3 build of the
+    timed CPU baseline."""
     src = HERE / "tecs_oracle.c"
-    if LIB.exists() and not force and LIB.stat().st_mtime >= src.stat().st_mtime:
-        return LIB
+    out = LIB_TIMING if timing else LIB
+    if out.exists() and not force and out.stat().st_mtime >= src.stat().st_mtime:
+        return out
     BUILD.mkdir(exist_ok=True)
-    cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-fopenmp", str(src), "-o", str(LIB), "-lm"]
-    subprocess.run(cmd, check=True)
-    return LIB
+    if timing:
+        flags = ["-O3", "-std=gnu11", "-fPIC", "-shared", "-fno-fast-math", "-fopenmp"]
+    else:
+        flags = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp"]
+    tmp = out.with_suffix(".so.tmp")
+    subprocess.run(["gcc", *flags, str(src), "-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, out)
+    return out
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build()
-        L = ctypes.CDLL(str(LIB))
+def lib(timing: bool = False):
+    if timing not in _libs:
+        path = build(timing=timing)
+        L = ctypes.CDLL(str(path))
         L.tecs_oracle_create.restype = ctypes.c_void_p
         L.tecs_oracle_create.argtypes = [ctypes.POINTER(Desc)]
         L.tecs_oracle_destroy.argtypes = [ctypes.c_void_p]
@@ -84,8 +106,8 @@ def lib():
         L.tecs_oracle_hash.restype = ctypes.c_uint64
         L.tecs_oracle_hash.argtypes = [ctypes.c_uint64] * 4
         L.tecs_oracle_last_error.restype = ctypes.c_char_p
-        _lib = L
-    return _lib
+        _libs[timing] = L
+    return _libs[timing]
 
 
 def _ptr(a):
@@ -100,7 +122,10 @@ class Oracle:
                  bin_size_scale=1.0, rebuild_every_n=0, integrator=HEUN, com_fix=False,
                  force=FORCE_SPRING2R, k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8, k_pol=0.0,
                  has_polarity=False, capacity=0, division_probability=0.0, division_offset=0.25,
-                 seed=2807):
+                 seed=2807, timing=False):
+        """timing: hold the simulation in the -O3 build of the timed CPU
+        baseline instead of the parity build."""
+        self._L = lib(timing)
         d = Desc()
         d.dims, d.finder, d.symmetric = dims, finder, int(symmetric)
         d.cutoff, d.gabriel_coefficient = cutoff, gabriel_coefficient
@@ -115,41 +140,41 @@ class Oracle:
         self.desc = d
         self.dims = dims
         self.has_polarity = has_polarity
-        self._h = lib().tecs_oracle_create(ctypes.byref(d))
+        self._h = self._L.tecs_oracle_create(ctypes.byref(d))
         if not self._h:
-            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+            raise RuntimeError(self._L.tecs_oracle_last_error().decode())
 
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
-            lib().tecs_oracle_destroy(h)
+            self._L.tecs_oracle_destroy(h)
             self._h = None
 
     def set_state(self, positions, polarity=None):
         x = np.ascontiguousarray(positions, dtype=np.float32)
         p = None if polarity is None else np.ascontiguousarray(polarity, dtype=np.float32)
-        if lib().tecs_oracle_set_state(self._h, _ptr(x), _ptr(p), x.shape[0]) != 0:
-            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+        if self._L.tecs_oracle_set_state(self._h, _ptr(x), _ptr(p), x.shape[0]) != 0:
+            raise RuntimeError(self._L.tecs_oracle_last_error().decode())
 
     def set_links(self, links, strength):
         """(a, b) pairs with the constant-pull link law of strength `strength`."""
         lk = np.ascontiguousarray(links, dtype=np.uint32).reshape(-1, 2)
-        if lib().tecs_oracle_set_links(self._h, _ptr(lk), lk.shape[0], strength) != 0:
-            raise RuntimeError(lib().tecs_oracle_last_error().decode())
+        if self._L.tecs_oracle_set_links(self._h, _ptr(lk), lk.shape[0], strength) != 0:
+            raise RuntimeError(self._L.tecs_oracle_last_error().decode())
 
     @property
     def count(self):
-        return lib().tecs_oracle_count(self._h)
+        return self._L.tecs_oracle_count(self._h)
 
     def get_state(self):
         n = self.count
         x = np.empty((n, self.dims), np.float32)
         p = np.empty((n, 2), np.float32) if self.has_polarity else None
-        lib().tecs_oracle_get_state(self._h, _ptr(x), _ptr(p))
+        self._L.tecs_oracle_get_state(self._h, _ptr(x), _ptr(p))
         return x, p
 
     def step(self, dt, n_steps=1, threads=1):
-        lib().tecs_oracle_step(self._h, dt, n_steps, threads)
+        self._L.tecs_oracle_step(self._h, dt, n_steps, threads)
 
     def evaluate(self, want_pairs=True, threads=1):
         """Deltas of one full-step force pass and the directed pairs in evaluation order."""
@@ -157,12 +182,12 @@ class Oracle:
         dx = np.zeros((n, self.dims), np.float32)
         dp = np.zeros((n, 2), np.float32) if self.has_polarity else None
         if not want_pairs:
-            lib().tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), None, 0, threads)
+            self._L.tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), None, 0, threads)
             return dx, dp, None
         cap = max(1024, 64 * n)
         while True:
             pairs = np.zeros((cap, 2), np.uint32)
-            cnt = lib().tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), _ptr(pairs), cap, threads)
+            cnt = self._L.tecs_oracle_evaluate(self._h, _ptr(dx), _ptr(dp), _ptr(pairs), cap, threads)
             if cnt <= cap:
                 return dx, dp, pairs[:cnt]
             cap = cnt

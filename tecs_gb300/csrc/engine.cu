@@ -650,11 +650,17 @@ int tecs_engine_create(const tecs_engine_desc* desc, tecs_engine** out) {
   if (ok) {
     std::memset(e->htable, 0, sizeof(SimSlot) * e->S);
     std::memset(e->hctr, 0, sizeof(Counters));
-    ok = cudaMemset(e->cnt, 0, ((size_t)e->NB + 1) * 4) == cudaSuccess &&
-         cudaMemset(e->off, 0, ((size_t)e->NB + 1) * 4) == cudaSuccess &&
-         cudaMemset(e->ctr, 0, sizeof(Counters)) == cudaSuccess &&
-         cudaMemset(e->table, 0, sizeof(SimSlot) * e->S) == cudaSuccess &&
-         cudaMemset(e->PA, 0, C * 8) == cudaSuccess && cudaMemset(e->PB, 0, C * 8) == cudaSuccess;
+    // cleared on the engine's own stream: it is non-blocking, so its kernels
+    // are not ordered after work on the legacy default stream, which a plain
+    // cudaMemset would use (and a buffer reused from a freed engine would
+    // then be read before it is cleared)
+    cudaStream_t st = e->stream;
+    ok = cudaMemsetAsync(e->cnt, 0, ((size_t)e->NB + 1) * 4, st) == cudaSuccess &&
+         cudaMemsetAsync(e->off, 0, ((size_t)e->NB + 1) * 4, st) == cudaSuccess &&
+         cudaMemsetAsync(e->ctr, 0, sizeof(Counters), st) == cudaSuccess &&
+         cudaMemsetAsync(e->table, 0, sizeof(SimSlot) * e->S, st) == cudaSuccess &&
+         cudaMemsetAsync(e->PA, 0, C * 8, st) == cudaSuccess && cudaMemsetAsync(e->PB, 0, C * 8, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
   }
   if (!ok) {
     std::string m = std::string("engine allocation failed: ") + cudaGetErrorString(cudaGetLastError());

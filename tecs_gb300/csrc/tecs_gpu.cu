@@ -636,8 +636,12 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   const size_t xcap = cap + kRowPad;
   ok = ok && alloc((void**)&s->A, xcap * 16) && alloc((void**)&s->B, xcap * 16) && alloc((void**)&s->Xt, xcap * 16) &&
        alloc((void**)&s->d1, cap * 16) && alloc((void**)&s->d2, cap * 16);
-  ok = ok && cudaMemset(s->A, 0, xcap * 16) == cudaSuccess && cudaMemset(s->B, 0, xcap * 16) == cudaSuccess &&
-       cudaMemset(s->Xt, 0, xcap * 16) == cudaSuccess;
+  // every clear is queued on the simulation's own stream: the stream is
+  // non-blocking, so work on it is not ordered after the legacy default
+  // stream, which a plain cudaMemset would use
+  ok = ok && cudaMemsetAsync(s->A, 0, xcap * 16, s->stream) == cudaSuccess &&
+       cudaMemsetAsync(s->B, 0, xcap * 16, s->stream) == cudaSuccess &&
+       cudaMemsetAsync(s->Xt, 0, xcap * 16, s->stream) == cudaSuccess;
   if (desc->has_polarity)
     ok = ok && alloc((void**)&s->PA, cap * 8) && alloc((void**)&s->PB, cap * 8) && alloc((void**)&s->Pt, cap * 8) &&
          alloc((void**)&s->dp1, cap * 8) && alloc((void**)&s->dp2, cap * 8);
@@ -655,9 +659,12 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   ok = ok && cudaMallocHost((void**)&s->hctr, sizeof(Counters)) == cudaSuccess;
   ok = ok && alloc((void**)&s->ctr, sizeof(Counters)) && alloc((void**)&s->com_part, pass_blocks * 3 * 8) &&
        alloc((void**)&s->com, 8 * 4) && alloc((void**)&s->stage, cap * 4 * 4);
-  if (ok && s->cnt) ok = cudaMemset(s->cnt, 0, ((size_t)g.nbins + 1) * 4) == cudaSuccess;
-  if (ok) ok = cudaMemset(s->ctr, 0, sizeof(Counters)) == cudaSuccess && cudaMemset(s->com, 0, 32) == cudaSuccess &&
-               cudaMemset(s->com_part, 0, pass_blocks * 3 * 8) == cudaSuccess;
+  if (ok && s->cnt) ok = cudaMemsetAsync(s->cnt, 0, ((size_t)g.nbins + 1) * 4, s->stream) == cudaSuccess;
+  if (ok)
+    ok = cudaMemsetAsync(s->ctr, 0, sizeof(Counters), s->stream) == cudaSuccess &&
+         cudaMemsetAsync(s->com, 0, 32, s->stream) == cudaSuccess &&
+         cudaMemsetAsync(s->com_part, 0, pass_blocks * 3 * 8, s->stream) == cudaSuccess &&
+         cudaStreamSynchronize(s->stream) == cudaSuccess;
   if (!ok) {
     std::string m = std::string("device allocation failed: ") + cudaGetErrorString(cudaGetLastError());
     tecs_sim_destroy(s);
@@ -892,7 +899,8 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
   cudaError_t e = cudaStreamSynchronize(s->stream);
   if (rc == 0 && e == cudaSuccess && dpairs) {
     size_t m = cnt < pair_cap ? (size_t)cnt : pair_cap;
-    e = cudaMemcpy(pairs, dpairs, m * sizeof(uint2), cudaMemcpyDeviceToHost);
+    e = cudaMemcpyAsync(pairs, dpairs, m * sizeof(uint2), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   }
   if (dpairs) cudaFree(dpairs);
   if (rc) return rc;
@@ -979,8 +987,11 @@ int tecs_sim_set_links(tecs_sim* s, const uint32_t* links, unsigned n_links, flo
     CK(cudaMalloc((void**)&s->link_off, ((size_t)cap + 1) * 4));
     CK(cudaMalloc((void**)&s->link_ent, (size_t)entries * sizeof(uint2)));
     CK(cudaMalloc((void**)&s->slot_of, (size_t)cap * 4));
-    CK(cudaMemcpy(s->link_off, off.data(), ((size_t)cap + 1) * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->link_ent, ent.data(), (size_t)entries * sizeof(uint2), cudaMemcpyHostToDevice));
+    // on the simulation's stream, which the legacy default stream does not order
+    CK(cudaMemcpyAsync(s->link_off, off.data(), ((size_t)cap + 1) * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->link_ent, ent.data(), (size_t)entries * sizeof(uint2), cudaMemcpyHostToDevice,
+                       s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     s->n_links = n_links;
   }
   s->link_k = strength;
@@ -1073,7 +1084,8 @@ __global__ void k_noalloc_reset(Counters* ctr, unsigned n) {
 
 // Device address of g_noalloc_scratch, looked up once per device with that
 // device current.  The host-side name of the array is only a stand-in; kernels
-// must be given this address.
+// must be given this address.  The address is kept for the life of the
+// process, so a device reset (cudaDeviceReset) between calls is not supported.
 int noalloc_scratch(int device, unsigned char** out) {
   static std::mutex mu;
   static unsigned char* addr[64] = {};
@@ -1131,10 +1143,11 @@ extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d
   f.gab_csq = desc->gabriel_coefficient * desc->gabriel_coefficient;
   s.binned = true;
   s.fuse_count = false;
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
+  // the device named by the description, as for every other entry point; its
+  // scratch array is the one this call uses
+  CK(cudaSetDevice(desc->device));
   unsigned char* base = nullptr;
-  if (noalloc_scratch(dev, &base)) return -1;
+  if (noalloc_scratch(desc->device, &base)) return -1;
   s.stream = (cudaStream_t)stream;
   s.d.capacity = n ? n : 1;
   s.d.division_probability = 0.0;
@@ -1159,7 +1172,6 @@ extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d
   }
   k_pack<<<ceil_div(n, 256), 256, 0, s.stream>>>(d_positions, n, desc->dims, s.A);
   int K = 0;
-  s.stream = (cudaStream_t)stream;
   if (enqueue_rebuild(&s, K, true)) return -1;
   PassArgs a = base_args(&s, 0.f);
   a.X = s.B;

@@ -32,7 +32,7 @@ sys.path.insert(0, str(ROOT))
 
 from tecs_gb300 import workloads as wl  # noqa: E402
 
-REF = Path(os.environ.get("TECS_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("TECS_REFERENCE", "/root/reference"))  # this script reads the reference where it lies
 DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
 
 # name: (driver scenario, oracle finder, symmetric, integrator, com, dims, polarity)

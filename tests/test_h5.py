@@ -1,7 +1,6 @@
 """The minimal HDF5 codec: reads files written by the HDF5 library (the
 reference's own fixtures, when its sources are present) and round-trips the
 snapshot layout of include/io/hdf5_writer.hpp (t<step>/<field>, float32)."""
-import os
 from pathlib import Path
 
 import numpy as np
@@ -9,7 +8,11 @@ import pytest
 
 from tecs_gb300 import h5
 
-REF = Path(os.environ.get("TECS_REFERENCE", "/root/reference"))
+import oracle
+
+# the reference checkout ($TECS_REFERENCE or a "reference" directory beside
+# the repository); the fixtures below are skipped without it
+REF = oracle.reference_root() or Path("/nonexistent")
 FIXTURES = [REF / "examples" / "data" / "sphere_ic.h5", REF / "examples" / "tribolium" / "initial_data" / "serosa.h5",
             REF / "examples" / "tribolium" / "initial_data" / "surface.h5"]
 
