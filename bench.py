@@ -19,8 +19,11 @@ Workloads (--workload):
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload W] [--cells N]
 
 Prints one JSON line (rank 0).  value = cell-steps/s with the state resident
-in HBM, each step timed with CUDA events on the simulation's stream and the L2
-flushed (256 MiB memset) between steps; e2e = the same metric through the C
+in HBM: each timed step is --chunk simulation steps (default 10, so the
+default 20 timed steps run the spheroid's 200), timed with CUDA events on the
+simulation's stream, the L2 flushed (256 MiB memset) before each; the default
+spheroid line also carries the 256-simulation ensemble, batched against the
+plain path one simulation after another.  e2e = the same metric through the C
 ABI with host buffers (every step: pinned upload of the state, the step, and
 the download of the new state).  --impl reference times the reference's
 algorithm (the oracle's C restatement, OpenMP) on the host cores.  Under
@@ -324,7 +327,9 @@ def run_gb300(args):
     x, p, mn, mx = w["make"](n)
     # steps before the end-to-end leg re-uploads the initial state: warm-up,
     # timed, and the profiled run
-    sim = make_sim(w, n, mn, mx, device=local, steps=args.warmup + args.steps + 1 + min(args.steps, 100))
+    chunk = max(1, args.chunk)
+    sim = make_sim(w, n, mn, mx, device=local,
+                   steps=(args.warmup + args.steps) * chunk + 1 + min(args.steps * chunk, 100))
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     xd = torch.from_numpy(x).to("cuda")
@@ -340,42 +345,47 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    def timed_steps(k, profile):
-        ms, cs = [], 0
+    def timed_steps(k, per, profile):
+        """k timed iterations of `per` simulation steps each, the L2 flushed
+        before each; per-step milliseconds and cell-steps (the agent count
+        before and after an iteration averaged over its steps)."""
+        ms, cs = [], 0.0
+        nb = sim.get_agent_count()
         for _ in range(k):
-            nb = sim.get_agent_count()
             with torch.cuda.stream(stream):
                 flush.zero_()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            sim.take_step(dt)
+            sim.take_step(dt, per)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
+            ms.append(e0.elapsed_time(e1) / per)
             if profile:
                 for name, v in sim.last_step_profile():
                     kern.setdefault(name, []).append(v)
-            cs += nb
+            na = sim.get_agent_count()
+            cs += 0.5 * (nb + na) * per
+            nb = na
         return ms, cs
 
     kern = {}
     with Clocks(local) as clocks:
         clocks.start()
-        step_ms, cell_steps = timed_steps(args.steps, False)
+        step_ms, cell_steps = timed_steps(args.steps, chunk, False)
         clocks.stop()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     # per-kernel CUDA events (event nodes inside the step graph) on a second,
-    # shorter run: the kernel table, the shares and the roofline's launch times
+    # shorter run of single steps: the kernel table and the shares
     sim.set_profiling(True)
     sim.take_step(dt)
-    prof_ms, prof_cells = timed_steps(min(args.steps, 100), True)
+    prof_ms, prof_cells = timed_steps(min(args.steps * chunk, 100), 1, True)
     sim.set_profiling(False)
     torch.cuda.synchronize()
-    total_s, cell_steps_all = aggregate_over_ranks(sum(step_ms) / 1e3, cell_steps, "cuda")
+    total_s, cell_steps_all = aggregate_over_ranks(sum(step_ms) * chunk / 1e3, cell_steps, "cuda")
     torch.cuda.synchronize()
     value = cell_steps_all / total_s
     kpl = sim.kernels_per_step()
@@ -436,22 +446,38 @@ def run_gb300(args):
         return 0
 
     hbm, peak_kind = peaks()
-    n_avg = cell_steps / max(args.steps, 1)
+    n_avg = cell_steps / max(args.steps * chunk, 1)
     n_prof = prof_cells / max(len(prof_ms), 1)
-    pass_bytes, pass_s, pass_launches = 0.0, 0.0, 0
+    pass_bytes, pass_s_prof, pass_launches = 0.0, 0.0, 0
     for name, v in kern.items():
         if name in PASS_BYTES:
             b = PASS_BYTES[name][0] + (PASS_BYTES[name][1] if pol else 0)
             pass_bytes += b * n_prof * len(v)
-            pass_s += sum(v) / 1e3
+            pass_s_prof += sum(v) / 1e3
             pass_launches += len(v)
-    achieved = pass_bytes / pass_s / 1e9 if pass_s else float("nan")
+    # The pass's launch time in the TIMED run: its share of the profiled
+    # step (per-kernel events) times the timed step; the event nodes of the
+    # profiled run add their own overhead, stated beside it.
+    prof_kernel_s = sum(sum(v) for v in kern.values()) / 1e3
+    share = pass_s_prof / prof_kernel_s if prof_kernel_s else float("nan")
+    steps_prof = max(len(prof_ms), 1)
+    launches_per_step = pass_launches / steps_prof
+    timed_step_s = statistics.mean(step_ms) / 1e3
+    pass_launch_s = share * timed_step_s / max(launches_per_step, 1e-9)
+    bytes_per_launch = pass_bytes / max(pass_launches, 1)
+    achieved = bytes_per_launch * (n_avg / n_prof) / pass_launch_s / 1e9 if pass_launch_s else float("nan")
     tpc = traffic_per_pass(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": (tpc * n_prof if tpc else None),
+                "traffic": (tpc * n_avg if tpc else None),
                 "kernel": "force pass (k_pass_*: pair finding + force + fused integrator epilogue)",
-                "bytes_per_launch": pass_bytes / max(pass_launches, 1),
-                "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_s / max(pass_launches, 1)}
+                "bytes_per_launch": bytes_per_launch * n_avg / n_prof,
+                "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_launch_s,
+                "avg_launch_ms_basis": "the pass's share of the profiled step (per-kernel CUDA events) times "
+                                       "the timed step",
+                "profiled_launch_ms": 1e3 * pass_s_prof / max(pass_launches, 1),
+                "profiled_step_over_timed_step": (prof_kernel_s / steps_prof) / timed_step_s}
+    pass_s = pass_launch_s * launches_per_step * len(step_ms) * chunk
+    pass_launches_timed = launches_per_step * len(step_ms) * chunk
     # The pass is bound by instruction issue, not HBM: warp instructions per launch (ncu count per cell x
     # cells) over the live launch time, against SMs x 4 schedulers x the sampled SM clock.
     ipc = pass_profile(args.workload, "pass_warp_inst_per_cell")
@@ -460,7 +486,7 @@ def run_gb300(args):
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         mhz = (clocks.summary() or {}).get("sm_mhz") or 2070.0
         ipeak = sms * 4 * mhz * 1e6
-        iach = ipc * n_prof * pass_launches / pass_s
+        iach = ipc * n_avg * pass_launches_timed / pass_s
         issue_roofline = {"bound": "issue", "achieved": iach, "peak": ipeak, "unit": "warp instructions/s",
                           "frac": iach / ipeak, "inst_per_cell": ipc,
                           "peak_basis": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)",
@@ -474,26 +500,54 @@ def run_gb300(args):
         v, k, sec = cpu_steps(w, n, mn, mx, x, p, 1000, threads, 15.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{k} steps of the {n}-cell workload after 1 warm-up step ({sec:.1f} s, OpenMP)"}
+    ensemble = None
+    if world == 1 and args.workload == "spheroid" and not args.no_ensemble:
+        ensemble = ensemble_comparison(args, local)
     line = {
         "metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["desc"].format(n=n), "cells": n, "capacity": sim.desc.capacity,
-                   "l2": "flushed between timed steps (256 MiB memset)", "parallelism": f"replicas x{world}"},
+                   "sim_steps_per_timed_step": chunk, "sim_steps_timed": args.steps * chunk,
+                   "l2": f"flushed (256 MiB memset) before each timed step of {chunk} simulation steps",
+                   "parallelism": f"replicas x{world}"},
         "roofline": roofline,
         "step_roofline": {"bytes_per_cell": w["step_bytes"], "achieved": step_achieved,
                           "frac": step_achieved / hbm},
         "issue_roofline": issue_roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": kpl * args.steps,
+        "gpu_launches": kpl * args.steps * chunk,
         "kernels": kernel_table,
         "clocks": clocks.summary(),
+        "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def ensemble_comparison(args, device, steps: int = 300):
+    """The 256-simulation ensemble (cells log-uniform in [500, 200000], seed 2;
+    half Gabriel, half binned all-pairs; Heun dt 0.05) for its 300 steps:
+    the batched engine against the plain drop-in run one simulation after
+    another, both timed with the state resident on the device."""
+    from tecs_gb300 import batched
+
+    members = batched.ensemble(256, 2)
+    cells = sum(len(m.x) for m in members)
+    scales, _ = batched.autotune(members)
+    eng, _ = batched.build_engine(members, scales, device=device)
+    t_b = batched.time_engine_steps(eng, steps, warmup=3)
+    kpl = eng.kernels_per_step()
+    eng.close()
+    t_p = batched.run_plain_steps_only(members, steps)
+    v_b, v_p = cells * steps / t_b, cells * steps / t_p
+    return {"metric": "cell-steps/s, 256-simulation ensemble", "unit": UNIT, "steps": steps, "cells": cells,
+            "batched": {"value": v_b, "ms_per_step": 1e3 * t_b / steps, "gpu_launches": kpl * steps},
+            "plain_sequential": {"value": v_p, "ms_per_step_all_sims": 1e3 * t_p / steps},
+            "speedup_batched_vs_plain": v_b / v_p, "bin_size_scale": scales}
 
 
 def run_ensemble(args):
@@ -541,6 +595,9 @@ def main():
     ap.add_argument("--cells", type=int, default=0, help="cell count (default: the workload's)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble comparison of the default run")
+    ap.add_argument("--chunk", type=int, default=10,
+                    help="simulation steps per timed step (the L2 is flushed between timed steps)")
     ap.add_argument("--workload", default="spheroid", choices=["spheroid", "sheet", "small", "ensemble", "served"])
     ap.add_argument("--sims", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true")

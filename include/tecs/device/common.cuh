@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace tecs {
 
 constexpr float kFltEpsilon = 1.19209290e-7f;  // Kokkos::Experimental::epsilon_v<float>
@@ -22,7 +24,17 @@ struct GridP {
   int ext[3];       // ceil((max - min) / bin_size), 1 for unused dimensions
   int R;            // search radius in bins, ceil(cutoff * inv_bin)
   unsigned nbins;   // product of extents
+  int pow2;         // bin_size is a power of two: (p - min) / bin_size == (p - min) * inv_bin exactly
 };
+
+// Sets g.pow2 from g.bin_size (host side, after bin_size and inv_bin are set).
+// Dividing by 2^k and multiplying by 2^-k round the same real number, so the
+// two forms of the bin coordinate agree bit for bit.
+inline void grid_set_pow2(GridP& g) {
+  int e = 0;
+  const float m = std::frexp(g.bin_size, &e);
+  g.pow2 = (m == 0.5f && g.inv_bin * g.bin_size == 1.0f) ? 1 : 0;
+}
 
 // Built-in force descriptor plus the pair predicates' constants.
 struct ForceP {
@@ -35,11 +47,17 @@ struct ForceP {
 
 __device__ __forceinline__ int clampi(int v, int hi) { return v < hi ? (v < 0 ? 0 : v) : hi; }
 
-// grid.hpp:222-230: clamp(int((p - min) / bin_size), 0, ext - 1)
+// grid.hpp:222-230: clamp(int((p - min) / bin_size), 0, ext - 1); with a
+// power-of-two bin size the division is the (identical) multiplication
 template <int D>
 __device__ __forceinline__ void bin_coords_div(const GridP& g, const float* p, int* c) {
+  if (g.pow2) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) c[d] = clampi((int)((p[d] - g.mn[d]) / g.bin_size), g.ext[d] - 1);
+    for (int d = 0; d < D; ++d) c[d] = clampi((int)((p[d] - g.mn[d]) * g.inv_bin), g.ext[d] - 1);
+  } else {
+#pragma unroll
+    for (int d = 0; d < D; ++d) c[d] = clampi((int)((p[d] - g.mn[d]) / g.bin_size), g.ext[d] - 1);
+  }
 }
 // binned_all_pairs.hpp:103-109: the same with the inverse bin size
 template <int D>

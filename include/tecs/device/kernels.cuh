@@ -32,6 +32,8 @@ struct Counters {
   unsigned done_div;    // last-block counter of the division fixup
   unsigned long long step;        // integrator steps taken (keys the division RNG)
   unsigned long long pair_count;  // pairs recorded by the capture hook
+  unsigned tile_next;             // staged-rows pass: next tile to hand out (zero between launches)
+  unsigned tile_exhausted;        // warps that found no tile left (zero between launches)
 };
 
 struct PassArgs {
@@ -647,28 +649,26 @@ __device__ __forceinline__ void add_link(const PassArgs& a, unsigned n, const fl
   for (int d = 0; d < D; ++d) s[d] = s[d] + (0.0f + (k * disp[d]) / dist);
 }
 
+// The write of one active cell: links, then the mode's store or fused
+// integrator update, the next rebuild's bin count and division.  s receives
+// the cell's position delta (for the COM partials).
 template <int D>
-__device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
-                                              const float* xi, const float4& vi, const float2& pi, const Acc& acc) {
-  float s[3];
+__device__ __forceinline__ void cell_commit(const GridP& g, const PassArgs& a, unsigned n, unsigned i,
+                                            const float* xi, const float4& vi, const float2& pi, const Acc& acc,
+                                            float* s) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
-  if (a.link_off && active) {
+  if (a.link_off) {
     const unsigned id = a.Bid ? a.Bid[i] : id_of(vi);
     const unsigned e1 = a.link_off[id + 1];
     for (unsigned e = a.link_off[id]; e < e1; ++e) add_link<D>(a, n, xi, e, s);
   }
   const float sp0 = 0.0f + acc.p[0], sp1 = 0.0f + acc.p[1];
   if (a.mode == kStore) {
-    if (active) {
-      a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
-      if (a.dp_out) a.dp_out[i] = make_float2(sp0, sp1);
-    }
-    if (a.com_part) com_reduce_block(a, active ? com_fixed(s[0]) : 0ll, active ? com_fixed(s[1]) : 0ll,
-                                     active ? com_fixed(s[2]) : 0ll);
+    a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
+    if (a.dp_out) a.dp_out[i] = make_float2(sp0, sp1);
     return;
   }
-  if (!active) return;
   const float dt = a.dt;
   if (a.mode == kHeun1Fused) {
     a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
@@ -702,6 +702,18 @@ __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a,
   if (a.PA) a.PA[i] = pn;
   if (a.count_next) count_cell<D>(g, a, i, xn);
   maybe_divide<D>(g, a, n, idb, xn, pn, a.ctr->step);
+}
+
+// cell_commit for an active cell, then (every thread of the block) the COM
+// partials of kStore.
+template <int D>
+__device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
+                                              const float* xi, const float4& vi, const float2& pi, const Acc& acc) {
+  float s[3] = {0.f, 0.f, 0.f};
+  if (active) cell_commit<D>(g, a, n, i, xi, vi, pi, acc, s);
+  if (a.mode == kStore && a.com_part)
+    com_reduce_block(a, active ? com_fixed(s[0]) : 0ll, active ? com_fixed(s[1]) : 0ll,
+                     active ? com_fixed(s[2]) : 0ll);
 }
 
 

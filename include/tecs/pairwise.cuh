@@ -10,7 +10,7 @@
 //
 // Included in a program compiled by nvcc (-std=c++20 --extended-lambda,
 // sm_103a), this header makes such a law run on the GPU: the library's force
-// pass (tecs_gb300/csrc/kernels.cuh, k_pass_law) is instantiated here with the
+// pass (tecs/device/kernels.cuh, k_pass_law) is instantiated here with the
 // law in place of a built-in one, and Simulation::take_step hands the library
 // a launcher for it (tecs_sim_set_pair_law).  The pass finds the same pairs in
 // the same order and adds each law call to the same per-cell sums as the
@@ -42,7 +42,7 @@
 #include <cstring>
 #include <memory>
 
-#include "../../tecs_gb300/csrc/kernels.cuh"
+#include "device/kernels.cuh"
 #include "tecs.hpp"
 
 namespace tecs {

@@ -221,6 +221,48 @@ int tecs_engine_event_destroy(void* event);
 int tecs_engine_kernels_per_step(tecs_engine* engine, int* kernels);
 void* tecs_engine_stream(tecs_engine* engine);
 
+/* ------------------------------------------------------------------------
+ * Standalone bin grid: acceleration::Grid (include/utils/grid.hpp:29-638),
+ * the grid user forces query for the nearest point or a random neighbour
+ * (examples/tribolium/main.cpp:84-95, intercalation_w_gradient.cpp:73-91).
+ * Bins of bin_size over [min_bounds, max_bounds) (ceil((max-min)/bin_size)
+ * per axis, grid.hpp:201-206); a point's bin is clamp(int((p-min)/bin_size))
+ * (grid.hpp:222-230).  Points are sorted by (bin, index) on every rebuild.
+ * ------------------------------------------------------------------------ */
+typedef struct tecs_grid tecs_grid;
+
+enum tecs_grid_query_kind {
+  TECS_GRID_NEAREST = 0,          /* get_nearest_point_index(point, radius_bins), grid.hpp:413-441            */
+  TECS_GRID_RANDOM_IN_BINS = 1,   /* get_random_point_index_in_neighbourhood_bins(point, radius_bins, rng),
+                                     grid.hpp:453-492                                                        */
+  TECS_GRID_RANDOM_IN_RADIUS = 2  /* get_random_point_index_in_neighbourhood(point, radius, rng[, filter]),
+                                     grid.hpp:505-637                                                        */
+};
+
+/* A grid for up to `capacity` points of `dims` (2 or 3) coordinates. */
+int tecs_grid_create(int dims, const float* min_bounds, const float* max_bounds, float bin_size, unsigned capacity,
+                     int device, tecs_grid** out);
+int tecs_grid_destroy(tecs_grid* grid);
+/* Grid::rebuild (grid.hpp:389-401) over n points float[n][dims] in host
+ * memory; synchronises. */
+int tecs_grid_rebuild(tecs_grid* grid, const float* points, unsigned n);
+/* The same from device memory on the grid's device. */
+int tecs_grid_rebuild_device(tecs_grid* grid, const float* d_points, unsigned n);
+/* m queries (host arrays): out[q] = the point index the reference's query
+ * returns at queries[q], or -1.  The random kinds take draws[q] for the
+ * reference's rng.rand(0, total) / rng.urand(total): the target is
+ * draws[q] mod total.  eligible (host, one byte per point, or NULL) is the
+ * filter of the radius query: points with eligible[index] == 0 are skipped.
+ * Synchronises. */
+int tecs_grid_query(tecs_grid* grid, int kind, const float* queries, unsigned m, int radius_bins, float radius,
+                    const uint32_t* draws, const uint8_t* eligible, int32_t* out);
+/* Device arrays of the last rebuild, for device code that queries the grid
+ * itself (tecs/device/grid_query.cuh): positions sorted by (bin, index)
+ * (float4, w = bin key), the index of each sorted slot, and the nbins + 1
+ * bin offsets. */
+int tecs_grid_device_view(const tecs_grid* grid, const void** sorted_positions, const unsigned** sorted_index,
+                          const unsigned** bin_offsets);
+
 /* Limits of tecs_force_pass_noalloc (its scratch is a fixed static device array). */
 #define TECS_NOALLOC_MAX_CELLS 65536u
 #define TECS_NOALLOC_MAX_BINS 262144u

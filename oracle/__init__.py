@@ -106,6 +106,10 @@ def lib(timing: bool = False):
         L.tecs_oracle_hash.restype = ctypes.c_uint64
         L.tecs_oracle_hash.argtypes = [ctypes.c_uint64] * 4
         L.tecs_oracle_last_error.restype = ctypes.c_char_p
+        L.tecs_oracle_grid_query.restype = ctypes.c_int
+        L.tecs_oracle_grid_query.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_uint,
+                                             ctypes.c_void_p, ctypes.c_float] + [ctypes.c_void_p] * 5
         _libs[timing] = L
     return _libs[timing]
 
@@ -195,3 +199,21 @@ class Oracle:
 
 def hash64(seed, step, cell, stream):
     return lib().tecs_oracle_hash(seed, step, cell, stream)
+
+
+def grid_query(points, min_bounds, max_bounds, bin_size, queries, draws, radius):
+    """The reference's acceleration::Grid queries (restated): dict of int32
+    arrays near1, near2, rbins, rrad, rfilt (see tecs_oracle_grid_query)."""
+    x = np.ascontiguousarray(points, dtype=np.float32)
+    q = np.ascontiguousarray(queries, dtype=np.float32)
+    dr = np.ascontiguousarray(draws, dtype=np.uint32)
+    dims = x.shape[1]
+    mn = np.ascontiguousarray(np.asarray(min_bounds, np.float32)[:dims])
+    mx = np.ascontiguousarray(np.asarray(max_bounds, np.float32)[:dims])
+    out = {k: np.zeros(len(q), np.int32) for k in ("near1", "near2", "rbins", "rrad", "rfilt")}
+    rc = lib().tecs_oracle_grid_query(dims, _ptr(x), len(x), _ptr(mn), _ptr(mx), float(bin_size), _ptr(q), len(q),
+                                      _ptr(dr), float(radius), *[_ptr(out[k]) for k in
+                                                                 ("near1", "near2", "rbins", "rrad", "rfilt")])
+    if rc != 0:
+        raise RuntimeError(lib().tecs_oracle_last_error().decode())
+    return out

@@ -362,6 +362,7 @@ TECS_SCENARIO(bgs_euler_com_3, pair_finders::BinnedGabrielSymmetric, integrators
               3, 0)
 TECS_SCENARIO(bas_heun_3, pair_finders::BinnedAllPairsSymmetric, integrators::Heun, com_fixers::NoComFixer, 3, 0)
 TECS_SCENARIO(ngs_euler_3, pair_finders::NaiveGabrielSymmetric, integrators::Euler, com_fixers::NoComFixer, 3, 0)
+TECS_SCENARIO(nas_heun_3, pair_finders::NaiveAllPairsSymmetric, integrators::Heun, com_fixers::NoComFixer, 3, 0)
 TECS_SCENARIO(bg_heun_pol_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 3, 1)
 TECS_SCENARIO(ng_euler_2, pair_finders::NaiveGabriel, integrators::Euler, com_fixers::NoComFixer, 2, 0)
 TECS_SCENARIO(bg_heun_2, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer, 2, 0)
@@ -387,6 +388,65 @@ static int run(const Input& in, const std::string& out, int steps, double dt) {
 }
 }  // namespace gen_bg_heun_3
 
+// Grid-query scenarios (names starting "grid_"): the reference's standalone
+// acceleration::Grid (utils/grid.hpp:29-638) over the input points, with bins
+// of params[0] over [params[2..4], params[5..7]), rebuilt once, then queried
+// at m points read after the positions (uint32 m, float32 q[m*dims], uint32
+// draws[m]).  The random pickers draw from a stub generator whose rand(a, b)
+// and urand(r) return a + draw % (b - a) and draw % r, so the draw decides the
+// target exactly.  Outputs (int32[m] each): <out>.near1 / .near2 (nearest
+// point, search radius 1 / 2 bins), .rbins (random point in the 3^d bins),
+// .rrad (random point within params[1]), .rfilt (the same among indices not
+// divisible by 3).
+struct DrawRng {
+  unsigned draw = 0;
+  int rand(int a, int b) const { return b > a ? a + (int)(draw % (unsigned)(b - a)) : a; }
+  unsigned urand(unsigned r) const { return r ? draw % r : 0u; }
+};
+
+template <int DIMS>
+static int run_grid(const char* path, const std::string& out) {
+  using Vector = tecs::VectorN<float, DIMS>;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return 2;
+  unsigned hdr[3];
+  float prm[16];
+  if (std::fread(hdr, 4, 3, f) != 3 || std::fread(prm, 4, 16, f) != 16) return 2;
+  const unsigned n = hdr[0];
+  std::vector<float> x((size_t)n * DIMS);
+  if (n && std::fread(x.data(), 4, x.size(), f) != x.size()) return 2;
+  unsigned m = 0;
+  if (std::fread(&m, 4, 1, f) != 1) return 2;
+  std::vector<float> q((size_t)m * DIMS);
+  std::vector<unsigned> draws(m);
+  if (m && (std::fread(q.data(), 4, q.size(), f) != q.size() || std::fread(draws.data(), 4, m, f) != m)) return 2;
+  std::fclose(f);
+  tecs::View<Vector> pts("points", n);
+  for (unsigned i = 0; i < n; ++i)
+    for (int d = 0; d < DIMS; ++d) pts(i)[d] = x[(size_t)i * DIMS + d];
+  Vector mn, mx;
+  for (int d = 0; d < DIMS; ++d) { mn[d] = prm[2 + d]; mx[d] = prm[5 + d]; }
+  tecs::acceleration::Grid<Vector> grid(pts, n, mn, mx, prm[0]);
+  grid.rebuild();
+  std::vector<int> near1(m), near2(m), rbins(m), rrad(m), rfilt(m);
+  for (unsigned k = 0; k < m; ++k) {
+    Vector p;
+    for (int d = 0; d < DIMS; ++d) p[d] = q[(size_t)k * DIMS + d];
+    DrawRng rng{draws[k]};
+    near1[k] = grid.get_nearest_point_index(p, 1);
+    near2[k] = grid.get_nearest_point_index(p, 2);
+    rbins[k] = grid.get_random_point_index_in_neighbourhood_bins(p, 1, rng);
+    rrad[k] = grid.get_random_point_index_in_neighbourhood(p, prm[1], rng);
+    rfilt[k] = grid.get_random_point_index_in_neighbourhood(p, prm[1], rng, [](int j) { return j % 3 != 0; });
+  }
+  write_raw(out + ".near1", near1.data(), (size_t)m * 4);
+  write_raw(out + ".near2", near2.data(), (size_t)m * 4);
+  write_raw(out + ".rbins", rbins.data(), (size_t)m * 4);
+  write_raw(out + ".rrad", rrad.data(), (size_t)m * 4);
+  write_raw(out + ".rfilt", rfilt.data(), (size_t)m * 4);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
@@ -394,6 +454,11 @@ int main(int argc, char** argv) {
   }
   Kokkos::initialize();
   const std::string sc = argv[1];
+  if (sc == "grid_3" || sc == "grid_2") {
+    const int rc = sc == "grid_3" ? run_grid<3>(argv[2], argv[3]) : run_grid<2>(argv[2], argv[3]);
+    Kokkos::finalize();
+    return rc;
+  }
   const Input in = read_input(argv[2], sc.rfind("lk_", 0) == 0);
   const std::string out = argv[3];
   const int steps = std::atoi(argv[4]);
@@ -403,6 +468,7 @@ int main(int argc, char** argv) {
   if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
+  DISPATCH(nas_heun_3)
   DISPATCH(bg_heun_pol_3) DISPATCH(ng_euler_2) DISPATCH(bg_heun_2) DISPATCH(nd_euler_2) DISPATCH(nd_heun_3)
   DISPATCH(lk_bg_heun_3) DISPATCH(lk_ba_euler_com_3) DISPATCH(lk_writer_3) DISPATCH(gen_bg_heun_3)
 #undef DISPATCH

@@ -691,3 +691,171 @@ long tecs_oracle_evaluate(tecs_oracle* o, float* dpos, float* dpol, uint32_t* pa
   free(ox); free(op);
   return pairs ? sink.count : 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* standalone grid queries: acceleration::Grid (utils/grid.hpp:29-638)       */
+
+typedef struct {
+  int dims;
+  float mn[3];
+  float bin_size;
+  int ext[3];
+  long nbins;
+  const float* x;
+  unsigned* offsets; /* nbins + 1 */
+  unsigned* perm;
+} grid_q;
+
+/* grid.hpp:222-230 (division, truncation, clamp) and :235-259 (x fastest) */
+static void gq_coords(const grid_q* g, const float* p, int* c) {
+  for (int d = 0; d < g->dims; ++d) {
+    int v = (int)((p[d] - g->mn[d]) / g->bin_size);
+    int hi = g->ext[d] - 1;
+    v = v < hi ? v : hi;
+    c[d] = v < 0 ? 0 : v;
+  }
+}
+static long gq_flat(const grid_q* g, const int* c) {
+  long b = c[0];
+  if (g->dims >= 2) b += (long)c[1] * g->ext[0];
+  if (g->dims >= 3) b += (long)c[2] * ((long)g->ext[0] * g->ext[1]);
+  return b;
+}
+/* grid.hpp:307-340 linear_index_to_offset + :346-373 is_bin_outside_extents:
+ * the bin of task t around c, or -1 outside the grid */
+static long gq_task_bin(const grid_q* g, const int* c, int t, int side, int r) {
+  int nb[3] = {0, 0, 0};
+  int off[3] = {t % side - r, 0, 0};
+  if (g->dims == 2) off[1] = t / side - r;
+  if (g->dims == 3) { int tmp = t / side; off[1] = tmp % side - r; off[2] = tmp / side - r; }
+  for (int d = 0; d < g->dims; ++d) {
+    nb[d] = c[d] + off[d];
+    if (nb[d] < 0 || nb[d] >= g->ext[d]) return -1;
+  }
+  return gq_flat(g, nb);
+}
+static int gq_tasks(const grid_q* g, int side) { return g->dims == 2 ? side * side : side * side * side; }
+
+/* grid.hpp:413-441: nearest point within the (2r+1)^d bins, strict < keeps the first */
+static int gq_nearest(const grid_q* g, const float* p, int r) {
+  int c[3];
+  gq_coords(g, p, c);
+  const int side = 2 * r + 1;
+  int best = -1;
+  float bd = FLT_MAX;
+  for (int t = 0; t < gq_tasks(g, side); ++t) {
+    long b = gq_task_bin(g, c, t, side, r);
+    if (b < 0) continue;
+    for (unsigned k = g->offsets[b]; k < g->offsets[b + 1]; ++k) {
+      const unsigned j = g->perm[k];
+      const float s = dist2(p, g->x + (size_t)j * g->dims, g->dims);
+      if (s < bd) { best = (int)j; bd = s; }
+    }
+  }
+  return best;
+}
+
+/* grid.hpp:453-492: the target-th point of the (2r+1)^d bins in task order,
+ * target = rand(0, total) = draw mod total */
+static int gq_random_bins(const grid_q* g, const float* p, int r, uint32_t draw) {
+  int c[3];
+  gq_coords(g, p, c);
+  const int side = 2 * r + 1;
+  int total = 0;
+  for (int t = 0; t < gq_tasks(g, side); ++t) {
+    long b = gq_task_bin(g, c, t, side, r);
+    if (b >= 0) total += (int)(g->offsets[b + 1] - g->offsets[b]);
+  }
+  const int target = total > 0 ? (int)(draw % (uint32_t)total) : 0;
+  int seen = 0;
+  for (int t = 0; t < gq_tasks(g, side); ++t) {
+    long b = gq_task_bin(g, c, t, side, r);
+    if (b < 0) continue;
+    const int count = (int)(g->offsets[b + 1] - g->offsets[b]);
+    if (count == 0) continue;
+    if (target < seen + count) return (int)g->perm[g->offsets[b] + (unsigned)(target - seen)];
+    seen += count;
+  }
+  return -1;
+}
+
+/* grid.hpp:505-637: among the points within the physical radius (<= r^2),
+ * optionally those whose index is not a multiple of 3 (the filtered form),
+ * the target-th in task order, target = urand(total) = draw mod total */
+static int gq_random_radius(const grid_q* g, const float* p, float radius, uint32_t draw, int filtered) {
+  int rb = (int)ceilf(radius / g->bin_size);
+  if (rb < 1) rb = 1;
+  int c[3];
+  gq_coords(g, p, c);
+  const int side = 2 * rb + 1;
+  const float r2 = radius * radius;
+  int total = 0;
+  for (int t = 0; t < gq_tasks(g, side); ++t) {
+    long b = gq_task_bin(g, c, t, side, rb);
+    if (b < 0) continue;
+    for (unsigned k = g->offsets[b]; k < g->offsets[b + 1]; ++k) {
+      const unsigned j = g->perm[k];
+      if (dist2(p, g->x + (size_t)j * g->dims, g->dims) <= r2 && (!filtered || j % 3 != 0)) ++total;
+    }
+  }
+  if (total == 0) return -1;
+  const int target = (int)(draw % (uint32_t)total);
+  int seen = 0;
+  for (int t = 0; t < gq_tasks(g, side); ++t) {
+    long b = gq_task_bin(g, c, t, side, rb);
+    if (b < 0) continue;
+    for (unsigned k = g->offsets[b]; k < g->offsets[b + 1]; ++k) {
+      const unsigned j = g->perm[k];
+      if (dist2(p, g->x + (size_t)j * g->dims, g->dims) <= r2 && (!filtered || j % 3 != 0)) {
+        if (seen == target) return (int)j;
+        ++seen;
+      }
+    }
+  }
+  return -1;
+}
+
+int tecs_oracle_grid_query(int dims, const float* points, unsigned n, const float* min_bounds,
+                           const float* max_bounds, float bin_size, const float* queries, unsigned m,
+                           const uint32_t* draws, float radius, int32_t* near1, int32_t* near2, int32_t* rbins,
+                           int32_t* rrad, int32_t* rfilt) {
+  if (dims != 2 && dims != 3) { set_err("dims must be 2 or 3"); return -1; }
+  if (!(bin_size > 0.0f)) { set_err("bin size must be > 0"); return -1; }
+  grid_q g;
+  memset(&g, 0, sizeof g);
+  g.dims = dims;
+  g.bin_size = bin_size;
+  g.nbins = 1;
+  for (int d = 0; d < 3; ++d) g.ext[d] = 1;
+  for (int d = 0; d < dims; ++d) {
+    g.mn[d] = min_bounds[d];
+    g.ext[d] = (int)ceilf((max_bounds[d] - min_bounds[d]) / bin_size); /* grid.hpp:201-206 */
+    if (g.ext[d] < 1) { set_err("max_bounds must exceed min_bounds"); return -1; }
+    g.nbins *= g.ext[d];
+  }
+  g.x = points;
+  g.offsets = (unsigned*)calloc((size_t)g.nbins + 1, 4);
+  g.perm = (unsigned*)malloc((size_t)(n ? n : 1) * 4);
+  unsigned* key = (unsigned*)malloc((size_t)(n ? n : 1) * 4);
+  unsigned* cnt = (unsigned*)calloc((size_t)g.nbins + 1, 4);
+  /* rebuild (grid.hpp:389-401): bin keys, BinSort in ascending index order */
+  for (unsigned i = 0; i < n; ++i) {
+    int c[3];
+    gq_coords(&g, points + (size_t)i * dims, c);
+    key[i] = (unsigned)gq_flat(&g, c);
+    cnt[key[i]]++;
+  }
+  unsigned acc = 0;
+  for (long b = 0; b <= g.nbins; ++b) { g.offsets[b] = acc; acc += cnt[b]; cnt[b] = 0; }
+  for (unsigned i = 0; i < n; ++i) g.perm[g.offsets[key[i]] + cnt[key[i]]++] = i;
+  for (unsigned q = 0; q < m; ++q) {
+    const float* p = queries + (size_t)q * dims;
+    if (near1) near1[q] = gq_nearest(&g, p, 1);
+    if (near2) near2[q] = gq_nearest(&g, p, 2);
+    if (rbins) rbins[q] = gq_random_bins(&g, p, 1, draws[q]);
+    if (rrad) rrad[q] = gq_random_radius(&g, p, radius, draws[q], 0);
+    if (rfilt) rfilt[q] = gq_random_radius(&g, p, radius, draws[q], 1);
+  }
+  free(g.offsets); free(g.perm); free(key); free(cnt);
+  return 0;
+}

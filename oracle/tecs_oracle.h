@@ -93,6 +93,17 @@ long tecs_oracle_evaluate(tecs_oracle* o, float* delta_positions, float* delta_p
 /* Counter-based RNG shared with the CUDA path (division decisions). */
 uint64_t tecs_oracle_hash(uint64_t seed, uint64_t step, uint64_t cell, uint64_t stream);
 
+/* The reference's standalone acceleration::Grid (utils/grid.hpp:29-638) over
+ * n points (float[n][dims]), bins of bin_size over [min, max), queried at m
+ * points: nearest point in 3^d (near1) and 5^d (near2) bins, a random point of
+ * the 3^d bins (rbins), a random point within `radius` (rrad) and the same
+ * among indices not divisible by 3 (rfilt), the random targets being
+ * draws[q] mod (number of eligible points).  Any output may be NULL. */
+int tecs_oracle_grid_query(int dims, const float* points, unsigned n, const float* min_bounds,
+                           const float* max_bounds, float bin_size, const float* queries, unsigned m,
+                           const uint32_t* draws, float radius, int32_t* near1, int32_t* near2, int32_t* rbins,
+                           int32_t* rrad, int32_t* rfilt);
+
 const char* tecs_oracle_last_error(void);
 
 #ifdef __cplusplus

@@ -71,8 +71,11 @@ _EXPORTS = (
     "tecs_sim_step", "tecs_sim_synchronize", "tecs_sim_count", "tecs_sim_download", "tecs_sim_evaluate",
     "tecs_sim_stream", "tecs_sim_set_graph", "tecs_sim_kernels_per_step", "tecs_last_error",
     "tecs_sim_set_profiling", "tecs_sim_last_step_profile", "tecs_sim_profile_name", "tecs_sim_set_links",
-    "tecs_sim_set_force",
+    "tecs_sim_set_force", "tecs_grid_create", "tecs_grid_destroy", "tecs_grid_rebuild", "tecs_grid_rebuild_device",
+    "tecs_grid_query", "tecs_grid_device_view",
 )
+
+GRID_NEAREST, GRID_RANDOM_IN_BINS, GRID_RANDOM_IN_RADIUS = 0, 1, 2
 
 
 def library_path() -> Path:
@@ -112,6 +115,15 @@ def load(build_if_missing: bool = True):
                                              ctypes.POINTER(ctypes.c_int)]
     L.tecs_sim_profile_name.restype = ctypes.c_char_p
     L.tecs_sim_profile_name.argtypes = [vp, ctypes.c_int]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.tecs_grid_create.argtypes = [ctypes.c_int, vp, vp, ctypes.c_float, ctypes.c_uint, ctypes.c_int,
+                                   ctypes.POINTER(vp)]
+    L.tecs_grid_destroy.argtypes = [vp]
+    L.tecs_grid_rebuild.argtypes = [vp, vp, ctypes.c_uint]
+    L.tecs_grid_rebuild_device.argtypes = [vp, vp, ctypes.c_uint]
+    L.tecs_grid_query.argtypes = [vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_int, ctypes.c_float, vp, vp, vp]
+    L.tecs_grid_device_view.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    del fp
     for name in _EXPORTS:
         if name not in ("tecs_last_error", "tecs_sim_stream", "tecs_sim_profile_name"):
             getattr(L, name).restype = ctypes.c_int
@@ -320,6 +332,56 @@ class Simulation:
             if cnt.value <= cap:
                 return dx[:n], (dp[:n] if dp is not None else None), pairs[: cnt.value]
             cap = cnt.value
+
+
+class Grid:
+    """A standalone bin grid on the GPU: the reference's acceleration::Grid
+    (include/utils/grid.hpp:29-638) -- rebuild over a point set, then nearest
+    and random-neighbour queries (tecs_grid_* of the C ABI)."""
+
+    def __init__(self, dims: int, min_bounds, max_bounds, bin_size: float, capacity: int, device: int = 0):
+        L = load()
+        mn = np.ascontiguousarray(np.asarray(min_bounds, np.float32)[:dims])
+        mx = np.ascontiguousarray(np.asarray(max_bounds, np.float32)[:dims])
+        h = ctypes.c_void_p()
+        _check(L.tecs_grid_create(dims, _ptr(mn), _ptr(mx), float(bin_size), int(capacity), device, ctypes.byref(h)))
+        self._h = h
+        self.dims = dims
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().tecs_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rebuild(self, points):
+        x = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, self.dims)
+        _check(load().tecs_grid_rebuild(self._h, _ptr(x), len(x)))
+        self.n = len(x)
+
+    def _query(self, kind, queries, radius_bins=1, radius=0.0, draws=None, eligible=None):
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.dims)
+        out = np.zeros(len(q), np.int32)
+        dr = None if draws is None else np.ascontiguousarray(draws, dtype=np.uint32)
+        el = None if eligible is None else np.ascontiguousarray(eligible, dtype=np.uint8)
+        _check(load().tecs_grid_query(self._h, kind, _ptr(q), len(q), int(radius_bins), float(radius), _ptr(dr),
+                                      _ptr(el), _ptr(out)))
+        return out
+
+    def nearest(self, queries, radius_bins: int = 1):
+        return self._query(GRID_NEAREST, queries, radius_bins=radius_bins)
+
+    def random_in_bins(self, queries, radius_bins: int, draws):
+        return self._query(GRID_RANDOM_IN_BINS, queries, radius_bins=radius_bins, draws=draws)
+
+    def random_in_radius(self, queries, radius: float, draws, eligible=None):
+        return self._query(GRID_RANDOM_IN_RADIUS, queries, radius=radius, draws=draws, eligible=eligible)
 
 
 def canonical_pairs(pairs: np.ndarray) -> np.ndarray:

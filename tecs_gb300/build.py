@@ -29,8 +29,12 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+DEVICE_HEADERS = PKG.parent / "include" / "tecs" / "device"
+
+
 def sources():
-    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "tecs_gpu.h"]
+    return (sorted(CSRC.glob("*.cu")) + sorted(DEVICE_HEADERS.glob("*.cuh")) +
+            [PKG.parent / "include" / "tecs_gpu.h"])
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:

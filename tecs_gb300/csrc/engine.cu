@@ -26,7 +26,7 @@
 #include <vector>
 
 #include "../../include/tecs_gpu.h"
-#include "kernels.cuh"
+#include "../../include/tecs/device/kernels.cuh"
 
 namespace tecs {
 int set_last_error(const std::string& m);
@@ -745,6 +745,7 @@ int tecs_engine_add(tecs_engine* e, const tecs_sim_desc* d, const float* positio
   }
   if (g.R != 1 || g.bin_size < d->cutoff) return fail("the engine needs bin_size_scale >= 1");
   g.nbins = (unsigned)nb;
+  grid_set_pow2(g);
   unsigned base = 0;
   if (bins_alloc(e, g.nbins, &base)) return fail("engine bin capacity exhausted");
   ForceP& f = sl.fp;

@@ -26,7 +26,8 @@
 #include <vector>
 
 #include "../../include/tecs_gpu.h"
-#include "kernels.cuh"
+#include "../../include/tecs/device/kernels.cuh"
+#include "../../include/tecs/device/pass_rows.cuh"
 
 using namespace tecs;
 
@@ -107,6 +108,8 @@ __global__ void k_upload(const float* __restrict__ pos, const float2* __restrict
     ctr->error = 0u;
     ctr->done_div = 0u;
     ctr->pair_count = 0ull;
+    ctr->tile_next = 0u;
+    ctr->tile_exhausted = 0u;
   }
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     float4 v = make_float4(0.f, 0.f, 0.f, __uint_as_float(s));
@@ -254,6 +257,33 @@ int prof_mark(tecs_sim* s, int which, const char* name) {
 #define PROF_END(s, name) \
   if (prof_mark((s), 1, (name))) return -1
 
+// A pass kernel and its launch shape: the staged-rows pass runs a persistent
+// grid of 128-thread blocks (at most what is resident at once), the others
+// one 96-thread block per 96 cells.
+struct PassKernel {
+  PassFn fn = nullptr;
+  int threads = kPassThreads;
+  bool persistent = false;
+};
+
+// Blocks of fn resident on the whole device at once (cached per kernel).
+unsigned resident_blocks(PassFn fn, int threads) {
+  static std::mutex mu;
+  static std::vector<std::pair<PassFn, unsigned>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& c : cache)
+    if (c.first == fn) return c.second;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
+  const unsigned r = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per);
+  cache.emplace_back(fn, r);
+  return r;
+}
+
+PassKernel pass_kernel(const tecs_sim* s, bool sym);
+
 PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
   // the cooperative Gabriel pass needs the fast-path geometry and packs
@@ -289,6 +319,32 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
     if (D == 2 && FO == 1) return k_pass<2, 4, 1>;
   }
   return nullptr;
+}
+
+// The staged-rows pass where its geometry holds (every witness inside the
+// 3x3x3 bin block, bin coordinates in 10 bits), else pass_fn's kernel.
+PassKernel pass_kernel(const tecs_sim* s, bool sym) {
+  PassKernel k;
+  const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
+  const bool geom = !sym && s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
+                    s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27);
+  const bool gab = F == TECS_FINDER_BINNED_GABRIEL && s->d.gabriel_coefficient <= 0.9f;
+  const bool all = F == TECS_FINDER_BINNED_ALL_PAIRS;
+  const char* env = std::getenv("TECS_PASS");
+  const bool rows = !(env && std::strcmp(env, "coop") == 0);
+  if (rows && geom && (gab || all)) {
+#define ROWS(DD, FF)                                                     \
+    if (D == DD && FO == FF) k.fn = gab ? k_pass_rows<DD, FF, 3> : k_pass_rows<DD, FF, 1>;
+    ROWS(3, 0) ROWS(3, 1) ROWS(3, 2) ROWS(2, 0) ROWS(2, 1)
+#undef ROWS
+    if (k.fn) {
+      k.threads = kRowsThreads;
+      k.persistent = true;
+      return k;
+    }
+  }
+  k.fn = pass_fn(s, sym);
+  return k;
 }
 
 PassArgs base_args(const tecs_sim* s, float dt) {
@@ -404,8 +460,8 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
     CK(cudaGetLastError());
     return 0;
   }
-  PassFn fn = pass_fn(s, sym);
-  if (!fn) return fail("unsupported finder/force/dims combination");
+  const PassKernel pk = pass_kernel(s, sym);
+  if (!pk.fn) return fail("unsupported finder/force/dims combination");
   if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY) {
     // applications per pair on this pass's positions, then the pass
     PROF_BEGIN(s);
@@ -416,8 +472,10 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
     PROF_END(s, "k_delaunay_mult");
     K += 1;
   }
+  unsigned pblocks = ceil_div(L ? L : 1, (unsigned)pk.threads);
+  if (pk.persistent) pblocks = std::max(1u, std::min(pblocks, resident_blocks(pk.fn, pk.threads)));
   PROF_BEGIN(s);
-  fn<<<blocks, kPassThreads, 0, s->stream>>>(s->g, s->fp, a);
+  pk.fn<<<pblocks, pk.threads, 0, s->stream>>>(s->g, s->fp, a);
   PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
               : a.mode == kHeun1Fused ? "k_pass_heun1" : "k_pass_heun2");
   K += 1;
@@ -619,6 +677,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   }
   if (nb > (1ull << 31)) { delete s; return fail("bin grid too large"); }
   g.nbins = (unsigned)nb;
+  grid_set_pow2(g);
   ForceP& f = s->fp;
   f.force = desc->force;
   f.k_rep = desc->k_rep; f.r_rep = desc->r_rep; f.k_adh = desc->k_adh; f.r_adh = desc->r_adh; f.k_pol = desc->k_pol;
@@ -807,6 +866,7 @@ int tecs_sim_count(tecs_sim* s, unsigned* n) {
   CK(cudaStreamSynchronize(s->stream));
   if (s->hctr->error & 1u) return fail("capacity exceeded by cell division");
   if (s->hctr->error & 2u) return fail("a user pairwise law set drag, which this library does not support");
+  if (s->hctr->error & kErrStageTimeout) return fail("a force pass timed out waiting for its staged rows");
   *n = s->hctr->n;
   return 0;
 }
@@ -1135,6 +1195,7 @@ extern "C" int tecs_force_pass_noalloc(const tecs_sim_desc* desc, const float* d
     return fail("tecs_force_pass_noalloc: " + std::to_string(nb) + " bins exceed the allocation-free limit of " +
                 std::to_string(kNoallocMaxBins));
   g.nbins = (unsigned)nb;
+  grid_set_pow2(g);
   ForceP& f = s.fp;
   f.force = desc->force;
   f.k_rep = desc->k_rep; f.r_rep = desc->r_rep; f.k_adh = desc->k_adh; f.r_adh = desc->r_adh; f.k_pol = 0.f;

@@ -48,6 +48,7 @@ SCENARIOS = {
     "bgs_euler_com": ("bgs_euler_com_3", 3, 1, 0, 1, 3, 0),
     "bas_heun": ("bas_heun_3", 1, 1, 1, 0, 3, 0),
     "ngs_euler": ("ngs_euler_3", 2, 1, 0, 0, 3, 0),
+    "nas_heun": ("nas_heun_3", 0, 1, 1, 0, 3, 0),
     "bg_heun_polarity": ("bg_heun_pol_3", 3, 0, 1, 0, 3, 1),
     "ng_euler_2d_points11": ("ng_euler_2", 2, 0, 0, 0, 2, 0),
     "bg_heun_2d": ("bg_heun_2", 3, 0, 1, 0, 2, 0),
@@ -121,6 +122,9 @@ def inputs(name):
     elif name == "na_heun":
         x = wl.ball(600, 5)
         mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 5, 0.05
+    elif name == "nas_heun":
+        x = wl.ball(500, 20)
+        mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 4, 0.05
     elif name in ("ng_heun", "ngs_euler"):
         x = wl.ball(400 if name == "ng_heun" else 300, 6 if name == "ng_heun" else 9)
         mn, mx, steps, dt = (-20,) * 3, (20,) * 3, 3, 0.05
@@ -167,7 +171,54 @@ def inputs(name):
     return np.ascontiguousarray(x, np.float32), p0, prm, steps, dt
 
 
+# grid-query fixtures: the reference's acceleration::Grid queried at seeded
+# points; name: (driver scenario, dims, points, queries, bin size, search radius, half-width of the bounds)
+GRID = {
+    "grid_q_3d": ("grid_3", 3, 3000, 600, 0.75, 1.3, 7.0),
+    "grid_q_2d": ("grid_2", 2, 1500, 400, 1.0, 1.6, 12.0),
+}
+
+
+def grid_inputs(name):
+    scen, dims, n, m, bin_size, radius, half = GRID[name]
+    rng = np.random.default_rng(40 + dims)
+    # points in a ball slightly larger than the bounds (the outside ones are
+    # clamped into edge bins), queries over a wider box (some far from every point)
+    x = (wl.ball(n, 41 + dims)[:, :dims] * (half * 1.15 / wl.ball_radius(n))).astype(np.float32)
+    q = rng.uniform(-half * 1.3, half * 1.3, (m, dims)).astype(np.float32)
+    q[: m // 4] = x[rng.integers(0, n, m // 4)]  # some queries exactly at points
+    draws = rng.integers(0, 2 ** 32, m, dtype=np.uint64).astype(np.uint32)
+    prm = np.zeros(16, np.float32)
+    prm[0], prm[1] = bin_size, radius
+    prm[2:2 + dims] = -half
+    prm[5:5 + dims] = half
+    return np.ascontiguousarray(x), np.ascontiguousarray(q), draws, prm
+
+
+def run_grid(name):
+    scen, dims = GRID[name][0], GRID[name][1]
+    x, q, draws, prm = grid_inputs(name)
+    with tempfile.TemporaryDirectory() as td:
+        inp = Path(td) / "in.bin"
+        with open(inp, "wb") as f:
+            np.array([len(x), dims, 0], np.uint32).tofile(f)
+            prm.tofile(f)
+            x.tofile(f)
+            np.array([len(q)], np.uint32).tofile(f)
+            q.tofile(f)
+            draws.tofile(f)
+        out = Path(td) / "out"
+        subprocess.run([str(DRIVER), scen, str(inp), str(out), "0", "0"], check=True)
+        res = {"x": x, "q": q, "draws": draws, "prm": prm}
+        for k in ("near1", "near2", "rbins", "rrad", "rfilt"):
+            res[k] = np.fromfile(f"{out}.{k}", np.int32)
+    np.savez_compressed(HERE / f"{name}.npz", **res)
+    return res
+
+
 def run(name):
+    if name in GRID:
+        return run_grid(name)
     scen, *_rest, dims, pol = SCENARIOS[name]
     x, p0, prm, steps, dt = inputs(name)
     if name == "lk_writer_nolinks":
@@ -215,10 +266,14 @@ def main():
     if not REF.exists():
         sys.exit(f"reference sources not found at {REF}")
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    names = sys.argv[1:] or list(SCENARIOS)
+    names = sys.argv[1:] or list(SCENARIOS) + list(GRID)
     manifest = {}
     for name in names:
         r = run(name)
+        if name in GRID:
+            manifest[name] = {"scenario": GRID[name][0], "points": int(len(r["x"])), "queries": int(len(r["q"]))}
+            print(name, manifest[name])
+            continue
         manifest[name] = {"scenario": SCENARIOS[name][0], "cells": int(len(r["x0"])),
                           "pairs": int(len(r["pairs"])) if "pairs" in r else None,
                           "links": int(len(r["links"])) if "links" in r else None,

@@ -131,3 +131,26 @@ def test_idle_engine_returns_everything_at_remove():
     eng.step(0.05, 3)
     xc, _ = eng.download(sc)
     np.testing.assert_array_equal(xc, plain_run(a[0], None, a[3], "binned_gabriel", "heun", a[4], False, 3)[0])
+
+
+def test_engine_after_other_engines_closed_matches_plain_runs():
+    # Engines created and closed first (as the bin-scale autotuner does) leave
+    # freed device memory that a new engine may reuse: its clears must be
+    # ordered before its first kernels, or stale contents leak into the step.
+    from tecs_gb300 import batched
+
+    members = batched.ensemble(24, 7, lo=500, hi=20_000)
+    for scale in (1.0, 1.25, 1.5):
+        eng, _ = batched.build_engine(members, {"small": scale, "medium": scale, "large": scale})
+        eng.step(0.05, 2)
+        eng.close()
+    eng, slots = batched.build_engine(members, {})
+    eng.step(0.05, 5)
+    for m, slot in zip(members, slots):
+        xe, _ = eng.download(slot)
+        s = tg.Simulation(m.settings, pair_finder=m.finder, integrator=m.integrator, force=m.force)
+        s.set_state(m.x)
+        s.take_step(0.05, 5)
+        np.testing.assert_array_equal(xe, s.get_state()[0])
+        s.close()
+    eng.close()

@@ -30,6 +30,7 @@ KIND = {
     "bgs_euler_com": (3, 1, 0, 1, 3, 0),
     "bas_heun": (1, 1, 1, 0, 3, 0),
     "ngs_euler": (2, 1, 0, 0, 3, 0),
+    "nas_heun": (0, 1, 1, 0, 3, 0),
     "bg_heun_polarity": (3, 0, 1, 0, 3, 1),
     "ng_euler_2d_points11": (2, 0, 0, 0, 2, 0),
     "bg_heun_2d": (3, 0, 1, 0, 2, 0),
@@ -48,6 +49,8 @@ WRITER = ["lk_writer", "lk_writer_nolinks"]
 # which the user-law program reproduces on a GPU (tests/test_user_laws.py);
 # the C restatement has built-in laws only
 USER_LAW = ["gen_bg_heun"]
+# fixtures of the reference's standalone acceleration::Grid queries
+GRID = ["grid_q_3d", "grid_q_2d"]
 
 
 def load(name):
@@ -72,7 +75,7 @@ def make_oracle(name, g, kind=None):
 
 
 def test_manifest_covers_every_fixture():
-    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW)
+    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW) | set(GRID)
     for name in USER_LAW:
         assert (GOLDEN / f"{name}.npz").exists()
     for name in list(KIND) + WRITER:
@@ -150,3 +153,15 @@ def test_generic_force_fixture_is_the_spring_plus_the_generic_pull():
     spring_only, _ = o.get_state()
     assert np.isfinite(g["pos"]).all() and not np.array_equal(g["pos"], spring_only)
     assert np.sqrt((g["pos"] ** 2).sum(1)).mean() < np.sqrt((spring_only ** 2).sum(1)).mean()
+
+
+@pytest.mark.parametrize("name", ["grid_q_3d", "grid_q_2d"])
+def test_oracle_grid_queries_match_reference(name):
+    # acceleration::Grid queried by the reference's own code (make_golden.py, GRID)
+    g = load(name)
+    prm = g["prm"]
+    dims = g["x"].shape[1]
+    out = oracle.grid_query(g["x"], prm[2:2 + dims], prm[5:5 + dims], float(prm[0]), g["q"], g["draws"],
+                            float(prm[1]))
+    for k in ("near1", "near2", "rbins", "rrad", "rfilt"):
+        np.testing.assert_array_equal(out[k], g[k], err_msg=k)

@@ -98,7 +98,7 @@ def test_binned_equals_naive_pair_set():
     np.testing.assert_array_equal(tg.canonical_pairs(g1.evaluate()[2]), tg.canonical_pairs(g2.evaluate()[2]))
 
 
-@pytest.mark.parametrize("finder", ["binned_all_pairs", "binned_gabriel", "naive_gabriel"])
+@pytest.mark.parametrize("finder", ["binned_all_pairs", "binned_gabriel", "naive_gabriel", "naive_all_pairs"])
 def test_symmetric_pairs_exact_deltas_close(finder):
     n = 1200 if finder.startswith("naive") else 3000
     x = ball(n, seed=3)
@@ -107,6 +107,28 @@ def test_symmetric_pairs_exact_deltas_close(finder):
     dc, _, pc = c.evaluate()
     np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(pc))
     ok, err, nbad = close(dg, dc)
+    assert ok, (err, nbad)
+
+
+def test_naive_all_pairs_symmetric_matches_reference_fixture():
+    # naive_all_pairs_symmetric.hpp:82-155 run by the reference's own code
+    # (tests/golden/make_golden.py, scenario nas_heun): j < i pairs, +delta to
+    # i and -delta to j; float atomics here, so deltas and steps within tolerance
+    from pathlib import Path
+    gold = dict(np.load(Path(__file__).resolve().parent / "golden" / "nas_heun.npz"))
+    prm = gold["prm"]
+    x = gold["x0"]
+    pf = tg.PairFinderSettings(min_bounds=tuple(prm[2:5]), max_bounds=tuple(prm[5:8]))
+    s = tg.Simulation(tg.Settings(agent_count=len(x), capacity=len(x), cutoff_distance=float(prm[0]),
+                                  pair_finder_settings=pf), pair_finder="naive_all_pairs", symmetric=True,
+                      integrator="heun", force=tg.Spring2R())
+    s.set_state(x)
+    dg, _, pg = s.evaluate()
+    np.testing.assert_array_equal(tg.canonical_pairs(pg), tg.canonical_pairs(gold["pairs"]))
+    ok, err, nbad = close(dg, gold["dpos"])
+    assert ok, (err, nbad)
+    s.take_step(float(gold["dt"]), int(gold["steps"]))
+    ok, err, nbad = close(s.get_state()[0], gold["pos"])
     assert ok, (err, nbad)
 
 
