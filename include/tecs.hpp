@@ -1,0 +1,15 @@
+// tecs.hpp -- the drop-in layer's umbrella header at the path the reference's
+// programs include (include/tecs.hpp, as "../include/tecs.hpp" from
+// examples/).  A program compiled by g++ gets the simulation API with the
+// built-in force laws; compiled by nvcc (-std=c++20 --extended-lambda) it
+// also gets its own PAIRWISE_FORCE / GENERIC_FORCE laws and INIT_FUNC /
+// UPDATE_FUNC functions (tecs/pairwise.cuh).  Link with -ltecs_gb300.
+#ifndef TECS_DROP_IN_TECS_HPP
+#define TECS_DROP_IN_TECS_HPP
+
+#include "tecs/tecs.hpp"
+#if defined(__CUDACC__)
+#include "tecs/pairwise.cuh"
+#endif
+
+#endif  // TECS_DROP_IN_TECS_HPP

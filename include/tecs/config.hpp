@@ -16,6 +16,8 @@
 #include <string_view>
 
 #include "components.hpp"
+#include "hdf5_writer.hpp"
+#include "plane.hpp"
 #include "random.hpp"
 #include "vector.hpp"
 
@@ -60,6 +62,14 @@ struct PairwiseFieldRef {
   const T& other;  // agent j's value
   T& delta;        // i's delta, written by the law
 };
+// a link's two ends (forces/detail.hpp: LinkFieldRef)
+template <typename T>
+struct LinkFieldRef {
+  const T& a;
+  const T& b;
+  T& delta_a;
+  T& delta_b;
+};
 
 // bind a finder template to the config's position view, scalar and dimensions
 template <template <typename, typename, int> class Finder, typename Config>
@@ -73,7 +83,7 @@ using pair_finder_t =
 
 #define CONFIG_SCALAR(S) using Scalar = S;
 #define CONFIG_DIMENSIONS(D) static constexpr int dimensions = D;
-// one random stream per simulation is part of the CUDA library (counter-based)
+// the drop-in layer's generator (tecs::XorShiftPool) serves every config
 #define CONFIG_RANDOM_POOL(POOL)
 #define CONFIG_INTEGRATOR(I) \
   template <typename SimulationConfig_> \
@@ -136,7 +146,7 @@ struct DefaultSimulationConfig {
   CONFIG_PAIR_FINDER(tecs::pair_finders::NaiveAllPairs)
   CONFIG_COM_FIXER(tecs::com_fixers::NoComFixer)
   CONFIG_INTEGRATOR(tecs::integrators::Heun)
-  CONFIG_WRITER(tecs::io::Dummy)
+  CONFIG_WRITER(tecs::io::HDF5_Writer)
   CONFIG_FIELDS((Vector, position))
   RESOLVE_TECS_CONFIG()
 };
@@ -156,9 +166,12 @@ struct DefaultSimulationConfig {
   using VectorI = tecs::VectorN<int, dimensions>;                                               \
   using VectorView = tecs::View<Vector>;                                                        \
   using Polarity = tecs::Polarity_<Scalar>;                                                     \
-  using Random = tecs::CounterRandom;                                                           \
+  using Plane = tecs::PlaneN<Scalar, dimensions>;                                               \
+  using RandomPool = tecs::XorShiftPool;                                                        \
+  using Random = tecs::XorShiftRandom;                                                          \
   using GenericForceFields = typename C::template ForceFields<tecs::detail::GenericFieldRef>;   \
-  using PairwiseForceFields = typename C::template ForceFields<tecs::detail::PairwiseFieldRef>;
+  using PairwiseForceFields = typename C::template ForceFields<tecs::detail::PairwiseFieldRef>; \
+  using LinkForceFields = typename C::template ForceFields<tecs::detail::LinkFieldRef>;
 
 #define EXTRACT_ALL_FROM_SIMULATION_CONFIG(C)                            \
   EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                \

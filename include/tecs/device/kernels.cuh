@@ -933,14 +933,18 @@ __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, cons
   if (d2 >= fp.rc2) return;
   if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
   if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
+  // naive Delaunay: the law is called once per accepted simplex, in j order
+  unsigned reps = 1;
+  if (FINDER == 4 && (reps = a.dmult[(size_t)i * a.capacity + j]) == 0u) return;
   const unsigned idj = id_at(a.X, a.Bid, j);
   if (a.pairs) {
-    const unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-    if (s < a.pair_cap) a.pairs[s] = make_uint2(idi, idj);
+    const unsigned long long s = atomicAdd(&a.ctr->pair_count, (unsigned long long)reps);
+    for (unsigned r = 0; r < reps; ++r)
+      if (s + r < a.pair_cap) a.pairs[s + r] = make_uint2(idi, idj);
   }
   const float dist = sqrtf(d2);
   const float2 pj = a.P ? a.P[j] : make_float2(0.f, 0.f);
-  law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc);
+  for (unsigned r = 0; r < reps; ++r) law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc);
 }
 
 // cell_general's loops with a user law
@@ -977,7 +981,9 @@ __device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const
 }
 
 template <int D, int FINDER, class Law>
-static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, ForceP fp, PassArgs a, Law law) {
+static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, ForceP fp, PassArgs a,
+                                                                  const Law* __restrict__ lawp) {
+  const Law& law = *lawp;
   const unsigned n = a.ctr->n;
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n;
@@ -1022,8 +1028,8 @@ struct UserPassCall {
 // success; 1 the call's layout differs; 2 a launch error; 3 the simulation's
 // finder or dimension count is not the program's.
 template <int D, int FINDER, class Law>
-int launch_user_pass(const UserPassCall* c, cudaStream_t stream, const Law& law) {
-  static_assert(FINDER >= 0 && FINDER <= 3, "user laws run with the all-pairs and Gabriel finders");
+int launch_user_pass(const UserPassCall* c, cudaStream_t stream, const Law* law) {
+  static_assert(FINDER >= 0 && FINDER <= 4, "user laws run with the all-pairs, Gabriel and Delaunay finders");
   if (!c || c->size != sizeof(UserPassCall)) return 1;
   if (c->dims != D || c->finder != FINDER) return 3;
   int cur = -1;
@@ -1323,11 +1329,15 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
     const float dist = sqrtf(d2);
     if (FORCE == 1 && dist != 0.0f) {
-      // (displacement * F) / distance, forces/predefined.hpp:134-143
+      // (displacement * F) / distance, forces/predefined.hpp:134-143; a zero
+      // F gives +-0 terms, which leave the cell's sum (never -0) unchanged,
+      // so the +0 left in f adds the same
       const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
-      f.x = (disp[0] * F) / dist;
-      f.y = (disp[1] * F) / dist;
-      if (D >= 3) f.z = (disp[2] * F) / dist;
+      if (F != 0.0f) {
+        f.x = (disp[0] * F) / dist;
+        f.y = (disp[1] * F) / dist;
+        if (D >= 3) f.z = (disp[2] * F) / dist;
+      }
     }
     if (POL) {
       // the spring and bending vector terms of the pair, and its two polarity

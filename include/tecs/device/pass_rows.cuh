@@ -32,8 +32,13 @@ namespace tecs {
 constexpr int kRowsWarps = 4;
 constexpr int kRowsThreads = 32 * kRowsWarps;
 // staged positions per warp: nine runs of about 34 cells at density 1 per bin;
-// a warp whose runs hold more takes the general per-cell path
-constexpr unsigned kStageCap = 384;
+// a warp whose runs hold more takes them in two halves
+constexpr unsigned kStageCap = 368;
+// In Heun's second pass a cell may have left its rebuild bin; its rows then
+// lie apart from the other lanes' (a row or a plane away in slot order).  The
+// warp copies such a cell's nine rows into this many extra stage slots
+// instead (a cell whose rows do not fit takes the general path).
+constexpr unsigned kStageExtra = 32;
 // bounded wait on the bulk copies (each try_wait returns after at most a
 // hardware-defined suspension); past it the kernel flags an error and the warp
 // stops staging
@@ -78,20 +83,91 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 template <int NB>
 struct __align__(16) RowsWarp {
-  float4 stage[kStageCap];          // the staged runs: x, y, z, bin key
-  float4 home[32];                  // the tile's cells; w = packed bin coordinates
+  float4 stage[kStageCap + kStageExtra];  // the staged runs (x, y, z, bin key), then the extra slots
+  unsigned hbc[32];                 // the tile's cells' packed bin coordinates
+  unsigned short self[32];          // each cell's own stage entry
   unsigned short list[NB][32];      // per lane: (staged index << 5) | bin code, candidate order
   unsigned short pinfo[NB * 32];    // (lane << 4) | q of the warp's pairs, by neighbour count
   unsigned short wcls[NB + 2];      // pairs per neighbour count
   unsigned amask[32];               // accepted neighbours of each cell, bit q
   unsigned seg0[9];                 // first slot of each row's run
   unsigned segb[9];                 // its first staged index
+  unsigned extra_j[kStageExtra];    // slot of each extra stage entry
   unsigned char ncnt[32];
   unsigned long long bar;
 };
 
+// Slot of staged entry idx of row rr.
+template <int NB>
+__device__ __forceinline__ unsigned staged_slot(const RowsWarp<NB>& W, unsigned idx, unsigned rr) {
+  return idx >= kStageCap ? W.extra_j[idx - kStageCap] : W.seg0[rr] + (idx - W.segb[rr]);
+}
+
 // Row index of a bin code (rx' + 3 ry' + 9 rz', each in 0..2): ry' + 3 rz'.
 __device__ __forceinline__ unsigned code_row(unsigned code) { return code / 3u; }
+
+// One accepted pair's terms, and their addition to the cell's sums in the
+// reference's order (the spring, then for the polarity law the bending
+// vector, the bending and the alignment polarity terms; pair_force's order).
+template <int FORCE>
+struct RowsPair {
+  float sx[3];
+  bool spring;  // a non-zero spring term (a zero one adds +-0 to a sum that
+                // starts at +0 and so is never -0: the sum is unchanged)
+  float bv[FORCE == 2 ? 3 : 1];
+  float bp[FORCE == 2 ? 2 : 1];
+  float al[FORCE == 2 ? 2 : 1];
+};
+
+template <int D, int FORCE, int NB>
+__device__ __forceinline__ void rows_pair_terms(const RowsWarp<NB>& W, const PassArgs& a, const ForceP& fp,
+                                                unsigned ent, unsigned i, const float* xi, float2 pi,
+                                                const PolTrig& ti, RowsPair<FORCE>& t) {
+  const float4 vj = W.stage[ent >> 5];
+  float disp[3];
+  disp[0] = xi[0] - vj.x;
+  disp[1] = xi[1] - vj.y;
+  disp[2] = D >= 3 ? xi[2] - vj.z : 0.f;
+  float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+  if (D >= 3) d2 = d2 + disp[2] * disp[2];
+  unsigned j = 0u;
+  if (a.pairs || FORCE == 2) j = staged_slot(W, ent >> 5, code_row(ent & 31u));
+  if (a.pairs) {
+    const unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
+    if (s < a.pair_cap) a.pairs[s] = make_uint2(id_at(a.X, a.Bid, i), id_at(a.X, a.Bid, j));
+  }
+  t.spring = false;
+  if (FORCE == 0) return;
+  const float dist = sqrtf(d2);
+  if (dist != 0.0f) {
+    const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
+    if (F != 0.0f) {
+      t.spring = true;
+#pragma unroll
+      for (int d = 0; d < D; ++d) t.sx[d] = (disp[d] * F) / dist;
+    }
+  }
+  if constexpr (FORCE == 2) {
+    const float2 pj = __ldg(&a.P[j]);
+    polarity_terms(fp, disp, dist, pi, ti, pj, pol_trig(pj), t.bv, t.bp, t.al);
+  }
+}
+
+template <int FORCE>
+__device__ __forceinline__ void rows_pair_add(const RowsPair<FORCE>& t, Acc& acc) {
+  if (t.spring) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc.x[d] = acc.x[d] + t.sx[d];
+  }
+  if constexpr (FORCE == 2) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc.x[d] = acc.x[d] + t.bv[d];
+    acc.p[0] = acc.p[0] + t.bp[0];
+    acc.p[1] = acc.p[1] + t.bp[1];
+    acc.p[0] = acc.p[0] + t.al[0];
+    acc.p[1] = acc.p[1] + t.al[1];
+  }
+}
 
 template <int D, int FORCE, int FINDER>
 static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, ForceP fp, PassArgs a) {
@@ -145,8 +221,13 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
         hi[r] = __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]);
       }
     }
-    W.home[lane] = make_float4(xi[0], xi[1], xi[2],
-                               __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
+    W.hbc[lane] = (unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20);
+    // a cell outside its rebuild bin (w holds that bin's key) has its rows staged apart
+    bool mover = false;
+    if (active) {
+      int cc[3] = {bc[0], bc[1], bc[2]};
+      mover = flatten<D>(g, cc) != __float_as_uint(vi.w);
+    }
     // The warp stages the union runs of its 32 cells; when they hold more
     // than the stage, the low and the high half-warp take turns, each with
     // its own runs (a half that still does not fit takes the general path).
@@ -158,7 +239,7 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
       unsigned total = 0u;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
-        const bool ne = member && hi[r] > lo[r];
+        const bool ne = member && !mover && hi[r] > lo[r];
         const unsigned s = __reduce_min_sync(0xffffffffu, ne ? lo[r] : 0xffffffffu);
         const unsigned e = __reduce_max_sync(0xffffffffu, ne ? hi[r] : 0u);
         const unsigned len = e > s ? e - s : 0u;
@@ -174,8 +255,8 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
         gm = 0x0000ffffu;
         continue;
       }
-      const bool staged = can_stage && total <= kStageCap && total > 0u;
-      if (staged) {
+      const bool fits = can_stage && total <= kStageCap;
+      if (fits && total > 0u) {
         // the warp's earlier reads of the stage are complete (__syncwarp
         // above); lane 0 sets the bytes to expect, then one lane per row
         // issues that row's bulk copy
@@ -199,20 +280,62 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
           can_stage = false;
         }
       }
-      const bool use_stage = staged && can_stage;
+      // Movers: the warp copies each one's nine rows, one after the other, into
+      // the extra slots, one element per lane; mbase0 is where a mover's first
+      // row starts there.
+      unsigned mbase0 = 0u;
+      bool mover_fb = false;
+      {
+        unsigned mov = __ballot_sync(0xffffffffu, mine && mover);
+        unsigned ext = 0u;
+        while (mov) {
+          const int m = __ffs(mov) - 1;
+          mov &= mov - 1u;
+          unsigned tot = 0u;
+#pragma unroll
+          for (int r = 0; r < kRows; ++r) tot += __shfl_sync(0xffffffffu, hi[r] - lo[r], m);
+          if (ext + tot > kStageExtra) {
+            if (lane == m) mover_fb = true;
+            continue;
+          }
+          if (lane == m) mbase0 = kStageCap + ext;
+          for (unsigned t0 = 0u; t0 < tot; t0 += 32u) {
+            // the row holding element t: the last row starting at or before it
+            const unsigned t = t0 + (unsigned)lane;
+            unsigned j = 0u, start = 0u;
+#pragma unroll
+            for (int r = 0; r < kRows; ++r) {
+              const unsigned rlo = __shfl_sync(0xffffffffu, lo[r], m);
+              const unsigned rlen = __shfl_sync(0xffffffffu, hi[r] - lo[r], m);
+              if (t >= start) j = rlo + (t - start);
+              start += rlen;
+            }
+            if (t < tot) {
+              W.stage[kStageCap + ext + t] = __ldg(&a.X[j]);
+              W.extra_j[ext + t] = j;
+            }
+          }
+          ext += tot;
+        }
+        __syncwarp();
+      }
+      const bool use_stage = fits && can_stage;
       // ---- phase 1: in-cutoff neighbours, from the stage
       int cnt = 0;
-      bool fb = !use_stage;
-      if (mine && use_stage) {
+      bool fb = mover ? mover_fb : !use_stage;
+      if (mine && !fb) {
+        unsigned run = mbase0;  // a mover's rows follow each other in the extra slots
 #pragma unroll
         for (int r = 0; r < kRows; ++r) {
           const int ridx = D >= 3 ? r : r + 3;
-          const unsigned s0 = lo[r] - W.seg0[ridx] + W.segb[ridx];
-          const unsigned s1 = hi[r] - W.seg0[ridx] + W.segb[ridx];
+          const unsigned s0 = mover ? run : lo[r] - W.seg0[ridx] + W.segb[ridx];
+          run += hi[r] - lo[r];
+          const unsigned s1 = s0 + (hi[r] - lo[r]);
           // the cell itself, wherever its slot lies: in Heun's second pass a
           // cell may have left its rebuild bin, so its slot need not be in the
           // centre row
           const unsigned self = (i >= lo[r] && i < hi[r]) ? s0 + (i - lo[r]) : 0xffffffffu;
+          if (self != 0xffffffffu) W.self[lane] = (unsigned short)self;
           const int cy = bc[1] + (r % 3 - 1), cz = D >= 3 ? bc[2] + (r / 3 - 1) : 0;
           int c0[3] = {x0, cy, cz};
           // bin code base: rx' = key - (key of the row's first bin) + (x0 - bx + 1)
@@ -267,7 +390,7 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
         for (int p = P1 + lane; p < P; p += 32) {
           const unsigned info = W.pinfo[p];
           const int c = (int)(info >> 4), q = (int)(info & 15u);
-          const float4 h = W.home[c];
+          const float4 h = W.stage[W.self[c]];
           const float4 vj = W.stage[W.list[q][c] >> 5];
           float disp[3];
           disp[0] = h.x - vj.x;
@@ -300,7 +423,7 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
           if (hits) {
             // binned_gabriel.hpp:142-153: a witness in the ball blocks only from a
             // bin that overlaps the ball, [lo, hi] per axis relative to the cell's bin
-            const unsigned hb = __float_as_uint(h.w);
+            const unsigned hb = W.hbc[c];
             const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
             const float rr = sqrtf(rsq);
             int blo[3] = {-1, -1, -1}, bhi[3] = {1, 1, 1};
@@ -333,47 +456,22 @@ static __global__ void __launch_bounds__(kRowsThreads) k_pass_rows(GridP g, Forc
         } else {
           PolTrig ti{};
           if (FORCE == 2 && acc_bits) ti = pol_trig(pi);
-          for (unsigned b = acc_bits; b; b &= b - 1u) {
-            const int q = __ffs(b) - 1;
-            const unsigned ent = W.list[q][lane];
-            const float4 vj = W.stage[ent >> 5];
-            float disp[3];
-            disp[0] = xi[0] - vj.x;
-            disp[1] = xi[1] - vj.y;
-            disp[2] = D >= 3 ? xi[2] - vj.z : 0.f;
-            float d2 = disp[0] * disp[0] + disp[1] * disp[1];
-            if (D >= 3) d2 = d2 + disp[2] * disp[2];
-            unsigned j = 0u;
-            if (a.pairs || FORCE == 2) {
-              const unsigned rr = code_row(ent & 31u);
-              j = W.seg0[rr] + ((ent >> 5) - W.segb[rr]);
-            }
-            if (a.pairs) {
-              const unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-              if (s < a.pair_cap) a.pairs[s] = make_uint2(id_at(a.X, a.Bid, i), id_at(a.X, a.Bid, j));
-            }
-            if (FORCE == 0) continue;
-            const float dist = sqrtf(d2);
-            if (dist != 0.0f) {
-              const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
-              // a zero F adds +-0 to a sum that starts at +0 and so is never -0:
-              // the sum is unchanged, and the three divisions are skipped
-              if (F != 0.0f) {
+          // two pairs at a time: their terms are independent (the square
+          // roots and divisions overlap), their sums go in candidate order
+          for (unsigned b = acc_bits; b;) {
+            RowsPair<FORCE> t[2];
+            int m = 0;
 #pragma unroll
-                for (int d = 0; d < D; ++d) acc.x[d] = acc.x[d] + (disp[d] * F) / dist;
-              }
+            for (int u = 0; u < 2; ++u) {
+              if (!b) break;
+              const int q = __ffs(b) - 1;
+              b &= b - 1u;
+              rows_pair_terms<D, FORCE>(W, a, fp, W.list[q][lane], i, xi, pi, ti, t[u]);
+              ++m;
             }
-            if (FORCE == 2) {
-              const float2 pj = __ldg(&a.P[j]);
-              float bv[3], bp[2], al[2];
-              polarity_terms(fp, disp, dist, pi, ti, pj, pol_trig(pj), bv, bp, al);
 #pragma unroll
-              for (int d = 0; d < 3; ++d) acc.x[d] = acc.x[d] + bv[d];
-              acc.p[0] = acc.p[0] + bp[0];
-              acc.p[1] = acc.p[1] + bp[1];
-              acc.p[0] = acc.p[0] + al[0];
-              acc.p[1] = acc.p[1] + al[1];
-            }
+            for (int u = 0; u < 2; ++u)
+              if (u < m) rows_pair_add<FORCE>(t[u], acc);
           }
         }
         float s[3];

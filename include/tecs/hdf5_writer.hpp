@@ -523,6 +523,9 @@ class HDF5_Writer {
     auto one = [&](const auto& v) {
       using T = typename std::decay_t<decltype(v)>::value_type;
       if (v.get_active_count() == 0) return;
+      // the host copy, with what device code wrote (hdf5_writer.hpp:120-129)
+      std::decay_t<decltype(v)> h = v;
+      h.sync_host();
       ds.push_back({v.label(), static_cast<const void*>(v.data()), v.get_active_count(), h5detail::ViewShape<T>::cols,
                     h5detail::ViewShape<T>::is_float});
     };

@@ -48,26 +48,6 @@
 namespace tecs {
 namespace detail {
 
-// PAIRWISE_FORCE's and GENERIC_FORCE's values: the law lambda with its tag
-template <typename L, typename Tag>
-struct TaggedForce {
-  using tag = Tag;
-  L f;
-  template <typename... A>
-  __host__ __device__ void operator()(A&&... a) const {
-    f(static_cast<A&&>(a)...);
-  }
-};
-template <typename Tag>
-struct TaggedForceMaker {
-  template <typename L>
-  TaggedForce<L, Tag> operator|(L f) const {
-    return TaggedForce<L, Tag>{f};
-  }
-};
-inline constexpr TaggedForceMaker<PairwiseForceTag> pairwise_force{};
-inline constexpr TaggedForceMaker<GenericForceTag> generic_force{};
-
 // The laws in the form k_pass_law calls them: the values as the config's
 // types, the running sums as the deltas, the law, the sums back.  G: the
 // GENERIC_FORCE law or NoLaw; P: the PAIRWISE_FORCE law or NoLaw.
@@ -87,7 +67,7 @@ struct PairLaw {
         self[d] = xi[d];
         delta[d] = acc.x[d];
       }
-      CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 3u : 4u, idi, idi);
+      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 3u : 4u, idi, idi);
       if constexpr (Simulation<Config>::has_polarity) {
         const Polarity_<float> ps(pi.x, pi.y);
         Polarity_<float> pd(acc.p[0], acc.p[1]);
@@ -118,7 +98,7 @@ struct PairLaw {
         delta[d] = acc.x[d];
       }
       float drag = 0.f;
-      CounterRandom rng = CounterRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
+      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
       if constexpr (Simulation<Config>::has_polarity) {
         const Polarity_<float> ps(pi.x, pi.y), po(pj.x, pj.y);
         Polarity_<float> pd(acc.p[0], acc.p[1]);
@@ -139,31 +119,57 @@ struct PairLaw {
 template <typename Config>
 using FinderOf = typename Config::template PairFinderT<Config>;
 
-// the launcher the library calls for every force evaluation
+// the launcher the library calls for every force evaluation; user is the
+// binding, which holds the laws in device memory
+template <typename Config, typename Law>
+struct LawOnDevice {
+  Law* dev = nullptr;
+  alignas(Law) unsigned char host[sizeof(Law)] = {};
+  bool valid = false;
+  ~LawOnDevice() {
+    if (dev) cudaFree(dev);
+  }
+};
 template <typename Config, typename Law>
 int pair_law_launcher(void* user, const void* call, void* stream) {
-  static_assert(!FinderOf<Config>::symmetric && FinderOf<Config>::finder_id <= TECS_FINDER_BINNED_GABRIEL,
-                "user laws run with the non-symmetric all-pairs and Gabriel finders");
+  static_assert(!FinderOf<Config>::symmetric && FinderOf<Config>::finder_id <= TECS_FINDER_NAIVE_DELAUNAY,
+                "user laws run with the non-symmetric all-pairs, Gabriel and Delaunay finders");
   return launch_user_pass<Config::dimensions, FinderOf<Config>::finder_id>(
-      static_cast<const UserPassCall*>(call), static_cast<cudaStream_t>(stream), *static_cast<const Law*>(user));
+      static_cast<const UserPassCall*>(call), static_cast<cudaStream_t>(stream),
+      static_cast<const LawOnDevice<Config, Law>*>(user)->dev);
 }
 
 template <typename Config, typename G, typename P>
 struct PairLawBinding {
   using Law = PairLaw<Config, G, P>;
-  // Binds the laws unless the same laws with the same captured values are
-  // bound already; a new binding makes the library re-capture its step graph.
+  using Bound = LawOnDevice<Config, Law>;
+  // The step's graph launches the pass with a pointer to the laws in device
+  // memory, so laws of the same types rebind by copying their values there
+  // on the simulation's stream (ordered before its next step) -- no new
+  // graph.  Values that compare equal byte for byte are not copied again.
   static void bind(tecs_sim* handle, int device, const G& g, const P& p, std::shared_ptr<void>& holder,
                    tecs_pair_law_fn& bound) {
     const tecs_pair_law_fn fn = &pair_law_launcher<Config, Law>;
     const Law law{g, p};
-    if (holder && bound == fn && std::memcmp(holder.get(), &law, sizeof(Law)) == 0) return;
-    if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
-      throw Error("cannot load the user laws' pass on the device");
-    auto next = std::make_shared<Law>(law);
-    check(tecs_sim_set_pair_law(handle, fn, next.get()));
-    holder = next;
-    bound = fn;
+    Bound* b = (holder && bound == fn) ? static_cast<Bound*>(holder.get()) : nullptr;
+    if (!b) {
+      if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
+        throw Error("cannot load the user laws' pass on the device");
+      auto next = std::make_shared<Bound>();
+      if (cudaMalloc(reinterpret_cast<void**>(&next->dev), sizeof(Law)) != cudaSuccess)
+        throw Error("cannot allocate the user laws on the device");
+      check(tecs_sim_set_pair_law(handle, fn, next.get()));
+      holder = next;
+      bound = fn;
+      b = next.get();
+    }
+    if (!b->valid || std::memcmp(b->host, &law, sizeof(Law)) != 0) {
+      std::memcpy(b->host, &law, sizeof(Law));
+      b->valid = true;
+      if (cudaMemcpyAsync(b->dev, b->host, sizeof(Law), cudaMemcpyHostToDevice,
+                          static_cast<cudaStream_t>(tecs_sim_stream(handle))) != cudaSuccess)
+        throw Error("cannot copy the user laws to the device");
+    }
   }
 };
 

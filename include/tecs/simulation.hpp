@@ -1,13 +1,21 @@
 // tecs/simulation.hpp -- Simulation<Config> of the C++20 drop-in layer.
 //
 // Keeps the reference's Simulation interface for the per-timestep path
-// (include/simulation.hpp:76-153 constructors and Settings, :231-302 views and
-// counts, :548-556 take_step) and runs every step in the CUDA library through
-// the C ABI of include/tecs_gpu.h.  The device holds the state; a field's
-// View is a host mirror that is refreshed from the device when the program
-// asks for it after steps and uploaded again before the next step if the
-// program may have written it -- the DualView modified-flag protocol of
-// include/types/view.hpp:47-266, with the host side explicit.
+// (include/simulation.hpp:76-153 constructors and Settings, :231-332 views,
+// counts and links, :338-546 initialisers and init, :548-556 take_step,
+// :600-667 write) and runs every step in the CUDA library through the C ABI
+// of include/tecs_gpu.h.  The library holds the state between steps; a
+// field's View (tecs/view.hpp) mirrors it on the host and on the device.
+// The views are refreshed from the library when they are read or synchronised
+// after steps, and their changes -- written on the host, or by device code --
+// go back to the library before the next step: the DualView protocol of
+// include/types/view.hpp:47-266, with the library as the view's source.
+//
+// Initialisers and init functions (INIT_FUNC, UPDATE_FUNC through init) run
+// on the host in cell order from one generator state, seeded from
+// Settings::seed -- the order in which the reference's Serial backend hands
+// its pool state from cell to cell -- so a program's initial state is
+// reproducible; the steps run on the GPU.
 //
 // Errors: every C-ABI failure throws tecs::Error with tecs_last_error().
 #ifndef TECS_CXX_SIMULATION_HPP
@@ -16,7 +24,6 @@
 #include <cmath>
 #include <cstdint>
 #include <memory>
-#include <random>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -27,7 +34,10 @@
 #include "components.hpp"
 #include "config.hpp"
 #include "hdf5_writer.hpp"
+#include "kokkos_compat.hpp"
+#include "random.hpp"
 #include "vector.hpp"
+#include "view.hpp"
 
 namespace tecs {
 
@@ -39,38 +49,34 @@ inline void check(int rc) {
   if (rc != 0) throw Error(tecs_last_error());
 }
 
-// A field's values for the active agents, on the host.
-template <typename T>
-class View {
- public:
-  using value_type = T;
-  using non_const_value_type = std::remove_const_t<T>;
-
-  View() = default;
-  View(const std::string& label, std::size_t n) : label_(label), data_(n), active_(static_cast<unsigned>(n)) {}
-
-  T& operator()(std::size_t i) { return data_[i]; }
-  const T& operator()(std::size_t i) const { return data_[i]; }
-  std::size_t extent(int) const { return data_.size(); }
-  T* data() { return data_.data(); }
-  const T* data() const { return data_.data(); }
-  unsigned get_active_count() const { return active_; }
-  void set_active_count(unsigned n) { active_ = n; }
-  const std::string& label() const { return label_; }
-
-  void resize(std::size_t n) { data_.resize(n); }
-
- private:
-  std::string label_;
-  std::vector<T> data_;
-  unsigned active_ = 0;
-};
-
 namespace detail {
 // the tags of user laws: PAIRWISE_FORCE / GENERIC_FORCE lambdas and their _OP functors
 // (include/utils/utils.hpp:181-276), defined with tecs/pairwise.cuh
 struct PairwiseForceTag {};
 struct GenericForceTag {};
+struct UpdateFuncTag {};
+
+// PAIRWISE_FORCE's, GENERIC_FORCE's and UPDATE_FUNC's values: the lambda with
+// its tag (utils.hpp:181-184)
+template <typename L, typename Tag>
+struct TaggedForce {
+  using tag = Tag;
+  L f;
+  template <typename... A>
+  TECS_HD void operator()(A&&... a) const {
+    f(static_cast<A&&>(a)...);
+  }
+};
+template <typename Tag>
+struct TaggedForceMaker {
+  template <typename L>
+  TaggedForce<L, Tag> operator|(L f) const {
+    return TaggedForce<L, Tag>{f};
+  }
+};
+inline constexpr TaggedForceMaker<PairwiseForceTag> pairwise_force{};
+inline constexpr TaggedForceMaker<GenericForceTag> generic_force{};
+inline constexpr TaggedForceMaker<UpdateFuncTag> update_func{};
 template <typename F, typename Tag>
 concept TaggedLaw = requires { typename F::tag; } && std::is_same_v<typename F::tag, Tag>;
 template <typename F>
@@ -78,12 +84,27 @@ concept UserPairLaw = TaggedLaw<F, PairwiseForceTag>;
 template <typename F>
 concept UserGenericLaw = TaggedLaw<F, GenericForceTag>;
 template <typename F>
+concept UserUpdateFunc = TaggedLaw<F, UpdateFuncTag>;
+template <typename F>
 constexpr bool is_link_law() {
   if constexpr (requires { F::is_link; }) return F::is_link;
   else return false;
 }
 // no law of that kind in the step
 struct NoLaw {};
+// A force argument as a step uses it.  PAIRWISE_FORCE(...) and its kin are
+// factories (utils.hpp:237-255); the reference's take_step takes a factory
+// or its result, so a factory is called here.
+template <typename F>
+decltype(auto) resolve_force(const F& f) {
+  if constexpr (requires { typename F::tag; } || requires { F::force_id; } || is_link_law<F>()) {
+    return (f);
+  } else if constexpr (std::is_invocable_v<const F&>) {
+    return f();
+  } else {
+    return (f);
+  }
+}
 // Hands a step's user laws (generic G, pairwise P; NoLaw where absent) to a
 // simulation's library handle; defined by tecs/pairwise.cuh.
 template <typename Config, typename G, typename P>
@@ -161,7 +182,8 @@ class Simulation {
       : Simulation(make_settings(agent_count, output_path, cutoff_distance, pair_finder_settings, seed)) {}
 
   explicit Simulation(const Settings& s)
-      : agent_count(s.agent_count), capacity(s.capacity), settings_(s), writer_(s.output_path, s.writer_settings) {
+      : agent_count(s.agent_count), capacity(s.capacity), settings_(s), writer_(s.output_path, s.writer_settings),
+        pool_(s.seed) {
     if (s.capacity < s.agent_count) throw Error("capacity must be >= agent_count");
     tecs_sim_desc d{};
     check(tecs_sim_desc_default(&d));
@@ -180,42 +202,40 @@ class Simulation {
     d.seed = s.seed;
     d.device = s.device;
     check(tecs_sim_create(&d, &handle_));
-    positions_ = View<Vector>("position", s.capacity);
-    positions_.set_active_count(s.agent_count);
-    if constexpr (has_polarity) {
-      polarity_ = View<Polarity>("polarity", s.capacity);
-      polarity_.set_active_count(s.agent_count);
-    }
-    host_valid_ = true;  // zero-initialised, as Kokkos views are
-    host_dirty_ = true;
-    links_ = View<Link>("links", s.link_capacity);
-    links_.set_active_count(s.link_active_count);
+    positions_ = View<Vector>("position", s.agent_count, s.capacity);
+    if constexpr (has_polarity) polarity_ = View<Polarity>("polarity", s.agent_count, s.capacity);
+    links_ = View<Link>("links", s.link_active_count, s.link_capacity);
+    // zero-initialised views are the first state, as Kokkos views are
+    positions_.set_host_modified(true);
+    auto refresh = [this]() { refresh_host(); };
+    positions_.set_refresh(refresh);
+    if constexpr (has_polarity) polarity_.set_refresh(refresh);
   }
 
   Simulation(const Simulation&) = delete;
   Simulation& operator=(const Simulation&) = delete;
   ~Simulation() {
+    positions_.set_refresh(nullptr);
+    if constexpr (has_polarity) polarity_.set_refresh(nullptr);
     if (handle_) tecs_sim_destroy(handle_);
   }
 
   // -- views ----------------------------------------------------------------
-  // The returned view may be written: it is uploaded before the next step.
+  // A field's view (simulation.hpp:231-256): current on the host when read
+  // there, and sent to the library before the next step if written.
   template <typename Field>
   View<typename Field::value_type>& get_view() {
-    refresh_host();
-    host_dirty_ = true;
     return view_of<Field>();
   }
   template <typename Field>
   const View<typename Field::value_type>& get_view() const {
-    const_cast<Simulation*>(this)->refresh_host();
     return const_cast<Simulation*>(this)->template view_of<Field>();
   }
-  View<Vector>& get_positions_view() { return get_view<FIELD(Vector, position)>(); }
+  View<Vector>& get_positions_view() { return positions_; }
 
-  // The links (include/simulation.hpp:317-332): a host view of link_capacity
-  // entries, the first get_active_count() in use; written links reach the
-  // device with the next step that passes a link law.
+  // The links (include/simulation.hpp:317-332): link_capacity entries, the
+  // first get_active_count() in use, written on the host or by device code;
+  // they reach the library with the next step that passes a link law.
   View<Link>& get_links() {
     links_dirty_ = true;
     return links_;
@@ -225,7 +245,7 @@ class Simulation {
 
   unsigned get_capacity() const { return capacity; }
   unsigned get_agent_count() const {
-    if (!host_valid_) {
+    if (lib_newer_host_ || lib_newer_dev_) {
       unsigned n = 0;
       check(tecs_sim_count(handle_, &n));
       const_cast<Simulation*>(this)->agent_count = n;
@@ -233,21 +253,22 @@ class Simulation {
     return agent_count;
   }
   // Simulation::set_agent_count (include/simulation.hpp:295-302): the next
-  // step starts from the first n host values and resets the finder's counter
+  // step starts from the first n cells and resets the finder's counter
   void set_agent_count(unsigned n) {
     if (n > capacity) throw Error("agent count exceeds capacity");
     refresh_host();
     agent_count = n;
     positions_.set_active_count(n);
     if constexpr (has_polarity) polarity_.set_active_count(n);
-    host_dirty_ = true;
+    positions_.set_host_modified(true);
   }
 
   // -- stepping ---------------------------------------------------------------
   // take_step(dt, forces...): one integrator step with at most one pairwise
-  // law (built-in, or a user law of tecs/pairwise.cuh) and at most one link
-  // law, in any order (the reference fuses forces by kind and evaluates
-  // pairwise before link forces)
+  // law (built-in, or a user law of tecs/pairwise.cuh), at most one generic
+  // law and at most one link law, in any order (the reference fuses forces by
+  // kind, kernel_fuser.hpp:148-156).  A PAIRWISE_FORCE(...) factory may be
+  // passed itself or called, as the reference accepts both.
   template <typename... Forces>
   void take_step(double dt, const Forces&... forces) {
     take_steps(dt, 1, forces...);
@@ -255,25 +276,17 @@ class Simulation {
   // n steps queued at once (one graph replay each)
   template <typename... Forces>
   void take_steps(double dt, int n, const Forces&... forces) {
-    static_assert((0 + ... + (detail::is_link_law<Forces>() || detail::UserGenericLaw<Forces> ? 0 : 1)) <= 1,
-                  "one pairwise law per step");
-    static_assert((0 + ... + (detail::is_link_law<Forces>() ? 1 : 0)) <= 1, "one link law per step");
-    static_assert((0 + ... + (detail::UserGenericLaw<Forces> ? 1 : 0)) <= 1, "one generic law per step");
-    apply_pair_law(forces...);
-    apply_link_law(forces...);
-    upload_if_dirty();
-    check(tecs_sim_step(handle_, dt, n));
-    host_valid_ = false;
-    last_dt = dt;
+    take_steps_impl(dt, n, detail::resolve_force(forces)...);
   }
 
   // One full-step force evaluation of the current state without moving it:
   // per-cell deltas and the directed (self, other) pairs found.
   template <typename Force>
   std::vector<std::pair<unsigned, unsigned>> evaluate(const Force& force, std::vector<Vector>* deltas = nullptr) {
-    apply_pair_law(force);
-    apply_link_law(force);
-    upload_if_dirty();
+    const auto& f = detail::resolve_force(force);
+    apply_pair_law(f);
+    apply_link_law(f);
+    sync_to_library();
     const unsigned n = get_agent_count();
     std::vector<Vector> dx(n ? n : 1);
     std::vector<std::uint32_t> raw(2 * std::size_t(64) * (n ? n : 1));
@@ -292,35 +305,69 @@ class Simulation {
 
   void synchronize() { check(tecs_sim_synchronize(handle_)); }
 
-  // -- initialisers (subset of include/initializers) -------------------------
-  // Uniform in a ball of the given radius (initializers/spheres.hpp's
-  // random filled sphere; the stream is this library's own).
-  void init_random_filled_sphere(Scalar radius) {
-    std::mt19937_64 rng(settings_.seed);
-    std::uniform_real_distribution<double> u(-1.0, 1.0);
-    refresh_host();
-    for (unsigned i = 0; i < agent_count; ++i) {
-      double p[3] = {0, 0, 0}, r2;
-      do {
-        r2 = 0;
-        for (int d = 0; d < dimensions; ++d) { p[d] = u(rng); r2 += p[d] * p[d]; }
-      } while (r2 > 1.0);
-      for (int d = 0; d < dimensions; ++d) positions_(i)[d] = static_cast<Scalar>(p[d] * radius);
-    }
-    host_dirty_ = true;
+  // -- initialisers (include/initializers, simulation.hpp:348-546) -----------
+  // Each places the agents, then applies the given init functions, all on the
+  // host in cell order from the simulation's generator (see the file comment).
+  template <typename... InitFuncs>
+  void init_random_filled_sphere(Scalar radius, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 3, "a random filled sphere needs 3 dimensions");
+    init(
+        [&](unsigned i, Random& g) {
+          // initializers/spheres.hpp:56-75
+          const Scalar r = radius * Kokkos::cbrt(static_cast<Scalar>(g.drand()));
+          const Scalar z = static_cast<Scalar>(g.drand(0.0, 2.0)) - Scalar(1.0);
+          const Scalar theta = static_cast<Scalar>(g.drand(0.0, 2.0 * Kokkos::numbers::pi_v<double>));
+          const Scalar rxy = Kokkos::sqrt(Scalar(1.0) - z * z) * r;
+          positions_(i)[0] = rxy * Kokkos::cos(theta);
+          positions_(i)[1] = rxy * Kokkos::sin(theta);
+          positions_(i)[2] = z * r;
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
   }
-  // Uniform on a sphere surface of the given radius (random hollow sphere).
-  void init_random_hollow_sphere(Scalar radius) {
-    std::mt19937_64 rng(settings_.seed);
-    std::normal_distribution<double> g(0.0, 1.0);
-    refresh_host();
-    for (unsigned i = 0; i < agent_count; ++i) {
-      double p[3] = {0, 0, 0}, r2 = 0;
-      for (int d = 0; d < dimensions; ++d) { p[d] = g(rng); r2 += p[d] * p[d]; }
-      const double s = radius / std::sqrt(r2);
-      for (int d = 0; d < dimensions; ++d) positions_(i)[d] = static_cast<Scalar>(p[d] * s);
+  template <typename... InitFuncs>
+  void init_random_hollow_sphere(Scalar radius, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 3, "a random hollow sphere needs 3 dimensions");
+    init(
+        [&](unsigned i, Random& g) {
+          // initializers/spheres.hpp:24-41
+          const Scalar u = static_cast<Scalar>(g.drand());
+          const Scalar v = static_cast<Scalar>(g.drand());
+          const Scalar z = Scalar(2.0) * u - Scalar(1.0);
+          const Scalar theta = Scalar(2.0) * Scalar(Kokkos::numbers::pi_v<Scalar>) * v;
+          const Scalar rxy = Kokkos::sqrt(Scalar(1.0) - z * z) * radius;
+          positions_(i)[0] = rxy * Kokkos::cos(theta);
+          positions_(i)[1] = rxy * Kokkos::sin(theta);
+          positions_(i)[2] = z * radius;
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // A random filled sphere relaxed by `steps` steps (default 2000) of dt 0.1
+  // with the piecewise-linear law at distance 0.8 (repulsion 2, adhesion 1;
+  // initializers/spheres.hpp:86-106, relax_force.hpp:17-30), then the init
+  // functions.  The relax law is the built-in spring of the same arithmetic.
+  template <typename... Args>
+  void init_relaxed_sphere(Scalar radius, Args&&... args) {
+    if constexpr (sizeof...(Args) > 0 && (std::is_integral_v<std::decay_t<Args>> || ...)) {
+      init_relaxed_sphere_n(radius, static_cast<Args&&>(args)...);
+    } else {
+      init_relaxed_sphere_n(radius, 2000u, static_cast<Args&&>(args)...);
     }
-    host_dirty_ = true;
+  }
+
+  // init(f, fs...) (simulation.hpp:519-537): f(i, rng) for every agent in
+  // cell order, then the next function
+  template <typename Initializer, typename... InitFuncs>
+  void init(Initializer&& initializer, InitFuncs&&... init_functions) {
+    refresh_host();
+    const unsigned n = agent_count;
+    for (unsigned i = 0; i < n; ++i) {
+      Random g = pool_.get_state();
+      initializer(i, g);
+      pool_.free_state(g);
+    }
+    positions_.set_host_modified(true);
+    if constexpr (has_polarity) polarity_.set_host_modified(true);
+    if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
   }
 
   // -- output (include/simulation.hpp:600-667) --------------------------------
@@ -351,6 +398,8 @@ class Simulation {
   double last_dt = 0.0;
 
  private:
+  using Random = XorShiftRandom;
+
   static Settings make_settings(unsigned n, const std::string& path, Scalar cutoff,
                                 const typename PairFinder::Settings& pfs, std::uint64_t seed) {
     Settings s(n, path);
@@ -358,6 +407,40 @@ class Simulation {
     s.pair_finder_settings = pfs;
     s.seed = seed;
     return s;
+  }
+
+  template <typename... InitFuncs>
+  void init_relaxed_sphere_n(Scalar radius, unsigned steps, InitFuncs&&... init_functions) {
+    init_random_filled_sphere(radius);
+    for (unsigned k = 0; k < steps; ++k)
+      take_step(0.1, forces::Spring2R{2.0f, 0.8f, 1.0f, 0.8f});
+    if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
+  }
+
+  template <typename... Forces>
+  void take_steps_impl(double dt, int n, const Forces&... forces) {
+    static_assert((0 + ... + (detail::is_link_law<Forces>() || detail::UserGenericLaw<Forces> ? 0 : 1)) <= 1,
+                  "one pairwise law per step");
+    static_assert((0 + ... + (detail::is_link_law<Forces>() ? 1 : 0)) <= 1, "one link law per step");
+    static_assert((0 + ... + (detail::UserGenericLaw<Forces> ? 1 : 0)) <= 1, "one generic law per step");
+    static_assert(!(false || ... || detail::UserUpdateFunc<Forces>),
+                  "UPDATE_FUNC functions run through Simulation::init, not take_step");
+    constexpr bool user = (false || ... || (detail::UserGenericLaw<Forces> || detail::UserPairLaw<Forces>));
+    apply_pair_law(forces...);
+    apply_link_law(forces...);
+    sync_to_library();
+    if constexpr (user) {
+      // user code may read and write views and device values on the device
+      refresh_device();
+      detail::push_device_vars();
+    }
+    check(tecs_sim_step(handle_, dt, n));
+    mark_library_newer();
+    if constexpr (user) {
+      detail::device_ran_user_code();
+      user_code_ran_ = true;
+    }
+    last_dt = dt;
   }
 
   // the first force of type kind in the pack, or NoLaw{}
@@ -427,6 +510,7 @@ class Simulation {
     const unsigned want = has ? links_.get_active_count() : 0u;
     if (!links_dirty_ && want == links_on_device_ && (!has || strength == link_strength_)) return;
     if (want > links_.extent(0)) throw Error("link active count exceeds link_capacity");
+    if (want) links_.sync_host();  // links written by device code
     check(tecs_sim_set_links(handle_, want ? reinterpret_cast<const uint32_t*>(links_.data()) : nullptr, want,
                              strength));
     links_on_device_ = want;
@@ -465,27 +549,73 @@ class Simulation {
     else writer_.write(time, step, positions_, extra..., links_);
   }
 
-  void refresh_host() {
-    if (host_valid_) return;
+  // The library's state after steps is newer than both arrays of the field views.
+  void mark_library_newer() {
+    lib_newer_dev_ = lib_newer_host_ = true;
+    positions_.set_stale(true);
+    if constexpr (has_polarity) polarity_.set_stale(true);
+  }
+  // library -> the field views' device arrays (cell-id order, on the device)
+  void refresh_device() {
+    if (!lib_newer_dev_) return;
     unsigned n = 0;
-    check(tecs_sim_download(handle_, reinterpret_cast<float*>(positions_.data()),
-                            has_polarity ? reinterpret_cast<float*>(polarity_.data()) : nullptr, &n));
+    check(tecs_sim_download_device(handle_, reinterpret_cast<float*>(positions_.device_data()),
+                                   has_polarity ? reinterpret_cast<float*>(polarity_.device_data()) : nullptr, &n));
+    set_count(n);
+    lib_newer_dev_ = false;
+    positions_.clear_device_flag();
+    if constexpr (has_polarity) polarity_.clear_device_flag();
+  }
+  // library -> the field views' host arrays (through their device arrays)
+  void refresh_host() {
+    if (!lib_newer_host_) return;
+    refresh_device();
+    positions_.copy_to_host();
+    if constexpr (has_polarity) polarity_.copy_to_host();
+    positions_.set_stale(false);
+    if constexpr (has_polarity) polarity_.set_stale(false);
+    positions_.set_host_modified(false);
+    if constexpr (has_polarity) polarity_.set_host_modified(false);
+    lib_newer_host_ = false;
+  }
+  void set_count(unsigned n) {
     agent_count = n;
     positions_.set_active_count(n);
     if constexpr (has_polarity) polarity_.set_active_count(n);
-    host_valid_ = true;
-    host_dirty_ = false;
   }
-
-  void upload_if_dirty() {
-    if (!host_dirty_) return;
-    check(tecs_sim_upload(handle_, reinterpret_cast<const float*>(positions_.data()),
-                          has_polarity ? reinterpret_cast<const float*>(polarity_.data()) : nullptr, agent_count));
-    host_dirty_ = false;
+  // field views written since the library last read them -> the library: the
+  // host arrays when host code wrote them, else the device arrays when
+  // device code did
+  void sync_to_library() {
+    const bool host = positions_.host_modified() || (has_polarity && polarity_.host_modified());
+    if (host) {
+      check(tecs_sim_upload(handle_, reinterpret_cast<const float*>(positions_.host_array()),
+                            has_polarity ? reinterpret_cast<const float*>(polarity_.host_array()) : nullptr,
+                            agent_count));
+      positions_.set_host_modified(false);
+      if constexpr (has_polarity) polarity_.set_host_modified(false);
+      // the device arrays did not see these writes
+      lib_newer_dev_ = true;
+      return;
+    }
+    if (!user_code_ran_) return;
+    user_code_ran_ = false;
+    const bool dev = positions_.device_flag() || (has_polarity && polarity_.device_flag());
+    if (dev && !lib_newer_dev_) {
+      check(tecs_sim_upload_device(handle_, reinterpret_cast<const float*>(positions_.device_data()),
+                                   has_polarity ? reinterpret_cast<const float*>(polarity_.device_data()) : nullptr,
+                                   agent_count));
+      positions_.clear_device_flag();
+      if constexpr (has_polarity) polarity_.clear_device_flag();
+      lib_newer_host_ = true;
+      positions_.set_stale(true);
+      if constexpr (has_polarity) polarity_.set_stale(true);
+    }
   }
 
   Settings settings_;
   Writer writer_;
+  XorShiftPool pool_;
   // the bound user pairwise law (its launcher and the law object it launches with); destroyed after handle_
   std::shared_ptr<void> law_holder_;
   tecs_pair_law_fn law_fn_ = nullptr;
@@ -496,10 +626,28 @@ class Simulation {
   bool links_dirty_ = false;        // the host links may differ from the device's
   unsigned links_on_device_ = 0;    // links active in the library
   float link_strength_ = 0.f;
-  bool host_valid_ = false;  // the host mirror holds the device state
-  bool host_dirty_ = false;  // the host mirror may differ from the device state
+  bool lib_newer_dev_ = false;      // the library's state is newer than the views' device arrays
+  bool lib_newer_host_ = false;     // ... than their host arrays
+  bool user_code_ran_ = false;      // user code ran on the device since the views were last checked
 };
 
 }  // namespace tecs
+
+// Init and update functions (utils.hpp:217, 249, 279-306): f(i, rng) per
+// agent, run by Simulation::init and the initialisers.
+#if defined(__CUDACC__)
+#define TECS_CXX_LAMBDA [=] __host__ __device__
+#else
+#define TECS_CXX_LAMBDA [=]
+#endif
+#define INIT_FUNC(...) \
+  [&]() { return TECS_CXX_LAMBDA([[maybe_unused]] const unsigned int i, [[maybe_unused]] Random& rng) { __VA_ARGS__ }; }
+#define INIT_OP TECS_HD void operator()([[maybe_unused]] const unsigned int i, [[maybe_unused]] Random& generator) const
+#define UPDATE_FUNC_PARAMETERS [[maybe_unused]] const unsigned int i, [[maybe_unused]] Random &rng
+#define UPDATE_FUNC(...) \
+  [&]() { return tecs::detail::update_func | TECS_CXX_LAMBDA(UPDATE_FUNC_PARAMETERS) { __VA_ARGS__ }; }
+#define UPDATE_FUNC_OP                    \
+  using tag = tecs::detail::UpdateFuncTag; \
+  TECS_HD void operator()(UPDATE_FUNC_PARAMETERS) const
 
 #endif  // TECS_CXX_SIMULATION_HPP

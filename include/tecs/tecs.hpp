@@ -6,7 +6,11 @@
 
 #include "components.hpp"
 #include "config.hpp"
+#include "kokkos_compat.hpp"
+#include "plane.hpp"
+#include "random.hpp"
 #include "simulation.hpp"
 #include "vector.hpp"
+#include "view.hpp"
 
 #endif  // TECS_CXX_TECS_HPP

@@ -131,7 +131,10 @@ struct Polarity_ : VectorN<Scalar, 2> {
 
   constexpr Polarity_() = default;
   TECS_HD constexpr explicit Polarity_(Scalar v) : Base(v) {}
-  TECS_HD constexpr Polarity_(Scalar theta, Scalar phi) : Base(theta, phi) {}
+  // any arithmetic angles, converted (Polarity{acos(...), 2.0 * pi * u} as the reference's programs write it)
+  template <typename A, typename B>
+    requires(std::is_arithmetic_v<A> && std::is_arithmetic_v<B>)
+  TECS_HD constexpr Polarity_(A theta, B phi) : Base(static_cast<Scalar>(theta), static_cast<Scalar>(phi)) {}
   // the direction of v (polarity.hpp:62-77), its length given or computed
   TECS_HD explicit Polarity_(const Vector3<Scalar>& v) : Polarity_(from_vector3(v)) {}
   TECS_HD Polarity_(const Vector3<Scalar>& v, Scalar length) : Polarity_(from_vector3(v, length)) {}

@@ -127,6 +127,22 @@ int tecs_sim_evaluate(tecs_sim* sim, float* dpos, float* dpol, uint32_t* pairs, 
 /* The simulation's CUDA stream (a cudaStream_t). */
 void* tecs_sim_stream(tecs_sim* sim);
 
+/* The state in cell-id order into device memory on the simulation's device
+ * (positions: capacity*dims floats, polarity: capacity*2 floats or NULL);
+ * synchronises.  Replaces View::sync_host's counterpart for device-side
+ * user code (include/types/view.hpp:139-148): the drop-in layer's field
+ * views read the state from here. */
+int tecs_sim_download_device(tecs_sim* sim, float* d_positions, float* d_polarity, unsigned* n);
+
+/* Device memory for the drop-in layer's views and device variables
+ * (include/types/view.hpp:47-266, device_var.hpp:38-134 hold theirs in
+ * Kokkos::View device allocations).  tecs_device_copy copies between any two
+ * of host and device memory (the direction taken from the addresses) and
+ * synchronises. */
+int tecs_device_alloc(int device, size_t bytes, void** out);
+int tecs_device_free(void* ptr);
+int tecs_device_copy(void* dst, const void* src, size_t bytes);
+
 /* Links (include/types/link.hpp): n_links (a, b) cell-id pairs with the
  * constant-pull link law of examples/intercalation.cpp:65-71 -- at every
  * force evaluation cell a gets strength*(x_b - x_a)/|x_b - x_a| and cell b
@@ -149,8 +165,9 @@ int tecs_sim_set_force(tecs_sim* sim, int force, float k_rep, float r_rep, float
  * library's description of the evaluation (its first field is its size in
  * bytes), stream is the simulation's cudaStream_t; fn returns 0 on success.
  * Launches made while a step is captured into a graph replay with it.
- * Non-symmetric all-pairs and Gabriel finders; fn == NULL returns to the
- * built-in law.  Replaces the force argument of take_step
+ * Non-symmetric all-pairs, Gabriel and Delaunay finders (with the Delaunay
+ * finder the library counts each pair's simplices first, and the pass calls
+ * the law once per simplex); fn == NULL returns to the built-in law.  Replaces the force argument of take_step
  * (include/simulation.hpp:548-556) for such laws. */
 typedef int (*tecs_pair_law_fn)(void* user, const void* call, void* stream);
 int tecs_sim_set_pair_law(tecs_sim* sim, tecs_pair_law_fn fn, void* user);

@@ -145,14 +145,11 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 // had before its phases became per-warp (the engine keeps this one)
 
 // POL: some resident simulation carries polarity; their cells then take the
-// cooperative path with the polarity law (as k_pass_gabriel<3, 2>), which
-// needs more shared memory -- spring-only engines use the leaner instance.
+// cooperative path with the polarity law, its pair terms added in the ordered
+// sums -- spring-only engines use the instance without that branch.
 template <int PASS, bool POL>
 static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
-  // neighbour slots per cell; the polarity law's extra per-pair float only
-  // fits in the static shared memory with 12 (cells with more in-cutoff
-  // neighbours take the per-thread path)
-  constexpr int NB = POL ? 12 : kMaxNb;
+  constexpr int NB = kMaxNb;  // neighbour slots per cell (more: the per-thread path)
   __shared__ float4 cand[NB * kPassThreads];
   __shared__ float4 home[kPassThreads];
   __shared__ unsigned short pinfo[NB * kPassThreads];
@@ -161,10 +158,6 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
   __shared__ unsigned hsim[kPassThreads];
-  __shared__ float2 hpol[POL ? kPassThreads : 1];
-  __shared__ PolTrig htrig[POL ? kPassThreads : 1];
-  __shared__ float pext[POL ? NB * kPassThreads : 1];
-
   const unsigned n = e.off[e.nb_total];
   const int t = threadIdx.x;
   const unsigned i = blockIdx.x * kPassThreads + t;
@@ -261,10 +254,6 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   hsim[t] = sim;
   ncnt[t] = (unsigned char)cnt;
   fallback[t] = fb ? 1 : 0;
-  if (POL) {
-    hpol[t] = pi;
-    if (cnt && polar) htrig[t] = pol_trig(pi);
-  }
   // pair offsets, pairs grouped by their cell's neighbour count (as k_pass_gabriel)
   int P = 0;
   {
@@ -359,33 +348,32 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       f.y = (disp[1] * F) / dist;
       f.z = (disp[2] * F) / dist;
     }
-    if (POL && cs.fp.force == TECS_FORCE_POLARITY) {
-      // as k_pass_gabriel<3, 2>: spring + bending vector, and the polarity terms, pre-added per pair
-      float bv[3], bp[2], al[2];
-      const float2 pj = __ldg(&e.P[__float_as_uint(vj.w) >> 5]);
-      polarity_terms(cs.fp, disp, dist, hpol[c], htrig[c], pj, pol_trig(pj), bv, bp, al);
-      f.x = f.x + bv[0];
-      f.y = f.y + bv[1];
-      f.z = f.z + bv[2];
-      f.w = bp[0] + al[0];
-      pext[cix(q, c)] = bp[1] + al[1];
-    }
+    // the polarity law's pairs are summed term by term in the ordered sums
+    // below (the reference's order, as the single-simulation pass adds them)
+    if (POL && cs.fp.force == TECS_FORCE_POLARITY) continue;
     cand[cix(q, c)] = f;
   }
   __syncthreads();
   // ordered sums of the cooperative pairs
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
   if (run && !fallback[t]) {
+    const bool pol_law = POL && polar && sl.fp.force == TECS_FORCE_POLARITY;
     for (int q = 0; q < cnt; ++q) {
       if (!((amask[t] >> q) & 1u)) continue;
       const float4 f = cand[cix(q, t)];
+      if (pol_law) {
+        // this pair's spring, bending vector, bending and alignment terms, each
+        // added to the sums in turn (polarity.hpp:131-198 as pair_force adds them)
+        const float disp[3] = {xi[0] - f.x, xi[1] - f.y, xi[2] - f.z};
+        float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+        d2 = d2 + disp[2] * disp[2];
+        const float2 pj = __ldg(&e.P[__float_as_uint(f.w) >> 5]);
+        pair_force<3, 2>(sl.fp, disp, sqrtf(d2), pi, pj, acc);
+        continue;
+      }
       acc.x[0] = acc.x[0] + f.x;
       acc.x[1] = acc.x[1] + f.y;
       acc.x[2] = acc.x[2] + f.z;
-      if (POL && polar && sl.fp.force == TECS_FORCE_POLARITY) {
-        acc.p[0] = acc.p[0] + f.w;
-        acc.p[1] = acc.p[1] + pext[cix(q, t)];
-      }
     }
   }
   // every thread has read its sums: the candidate array is free again and

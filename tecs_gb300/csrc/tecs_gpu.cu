@@ -438,11 +438,25 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
   return 0;
 }
 
+int enqueue_delaunay_mult(tecs_sim* s, const PassArgs& a, int& K) {
+  const unsigned L = launch_count(s);
+  // applications per pair on this pass's positions, before the pass
+  PROF_BEGIN(s);
+  if (s->d.dims == 3) k_delaunay_mult<3><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2,
+                                                                                       s->d.capacity, s->dmult);
+  else k_delaunay_mult<2><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2, s->d.capacity,
+                                                                           s->dmult);
+  PROF_END(s, "k_delaunay_mult");
+  K += 1;
+  return 0;
+}
+
 int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   const bool sym = s->d.symmetric != 0;
   const unsigned L = launch_count(s);
   const unsigned blocks = ceil_div(L ? L : 1, kPassThreads);
   if (s->law_fn) {
+    if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
     UserPassCall c{};
     c.size = sizeof(UserPassCall);
     c.device = s->d.device;
@@ -462,16 +476,7 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   }
   const PassKernel pk = pass_kernel(s, sym);
   if (!pk.fn) return fail("unsupported finder/force/dims combination");
-  if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY) {
-    // applications per pair on this pass's positions, then the pass
-    PROF_BEGIN(s);
-    if (s->d.dims == 3) k_delaunay_mult<3><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2,
-                                                                                         s->d.capacity, s->dmult);
-    else k_delaunay_mult<2><<<L ? L : 1, kDelaunayThreads, 0, s->stream>>>(a.X, s->ctr, s->fp.rc2, s->d.capacity,
-                                                                             s->dmult);
-    PROF_END(s, "k_delaunay_mult");
-    K += 1;
-  }
+  if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
   unsigned pblocks = ceil_div(L ? L : 1, (unsigned)pk.threads);
   if (pk.persistent) pblocks = std::max(1u, std::min(pblocks, resident_blocks(pk.fn, pk.threads)));
   PROF_BEGIN(s);
@@ -971,6 +976,49 @@ int tecs_sim_evaluate(tecs_sim* s, float* dpos, float* dpol, uint32_t* pairs, si
 
 void* tecs_sim_stream(tecs_sim* s) { return s ? (void*)s->stream : nullptr; }
 
+int tecs_sim_download_device(tecs_sim* s, float* d_positions, float* d_polarity, unsigned* n_out) {
+  if (!s || !d_positions) return fail("null argument");
+  CK(cudaSetDevice(s->d.device));
+  const unsigned gb = std::max(1u, ceil_div((unsigned)s->d.capacity, 256));
+  // the unpack takes the agent count from the device counters
+  k_unpack_dev<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->d.dims, d_positions);
+  if (d_polarity && s->d.has_polarity)
+    k_unpack2_dev<<<gb, 256, 0, s->stream>>>(s->A, s->ctr, s->PA, reinterpret_cast<float2*>(d_polarity));
+  CK(cudaGetLastError());
+  unsigned n = 0;
+  if (tecs_sim_count(s, &n)) return -1;
+  if (n_out) *n_out = n;
+  return 0;
+}
+
+int tecs_device_alloc(int device, size_t bytes, void** out) {
+  if (!out) return fail("null argument");
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail("no CUDA device");
+  }
+  CK(cudaSetDevice(device));
+  CK(cudaMalloc(out, bytes ? bytes : 16));
+  return 0;
+}
+
+int tecs_device_free(void* p) {
+  if (p) CK(cudaFree(p));
+  return 0;
+}
+
+int tecs_device_copy(void* dst, const void* src, size_t bytes) {
+  if (!bytes) return 0;
+  if (!dst || !src) return fail("null argument");
+  // after the device's queued work (a step on a simulation's own stream may
+  // be writing what is read here)
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
+  return 0;
+}
+
 int tecs_sim_set_graph(tecs_sim* s, int enable) {
   if (!s) return fail("null simulation");
   s->use_graph = enable != 0;
@@ -999,8 +1047,8 @@ int tecs_sim_set_force(tecs_sim* s, int force, float k_rep, float r_rep, float k
 
 int tecs_sim_set_pair_law(tecs_sim* s, tecs_pair_law_fn fn, void* user) {
   if (!s) return fail("null simulation");
-  if (fn && (s->d.symmetric || s->d.finder > TECS_FINDER_BINNED_GABRIEL))
-    return fail("user pairwise laws run with the non-symmetric all-pairs and Gabriel finders");
+  if (fn && s->d.symmetric)
+    return fail("user pairwise laws run with the non-symmetric all-pairs, Gabriel and Delaunay finders");
   if (fn == s->law_fn && user == s->law_user) return 0;
   CK(cudaSetDevice(s->d.device));
   // queued steps launched the old law from their graphs

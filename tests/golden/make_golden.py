@@ -216,9 +216,46 @@ def run_grid(name):
     return res
 
 
+# whole reference programs (examples/<program>.cpp, unmodified) run on the
+# shim with their datasets dumped: name -> (program, snapshots kept, stop after K groups or None)
+EXAMPLES = {
+    "ex_springs": ("springs", "first_last", None),
+    "ex_epithelium": ("epithelium", "first_last", None),
+    "ex_polarization": ("polarization", "first_last", None),
+    "ex_growth_w_wall": ("growth_w_wall", "first_last", None),
+    "ex_delaunay_spheroid": ("delaunay_spheroid", "first", 1),
+}
+
+
+def run_example(name):
+    prog, keep, stop = EXAMPLES[name]
+    exe = ROOT / "oracle" / "_ref" / "examples" / prog
+    with tempfile.TemporaryDirectory() as td:
+        (Path(td) / "output").mkdir()
+        dump = Path(td) / "dump"
+        dump.mkdir()
+        env = dict(os.environ, TECS_SHIM_DUMP=str(dump))
+        if stop:
+            env["TECS_SHIM_STOP_AFTER"] = str(stop)
+        subprocess.run([str(exe)], cwd=td, env=env, check=True, stdout=subprocess.DEVNULL)
+        groups = sorted({f.name.split(".")[0] for f in dump.iterdir()}, key=lambda g: int(g[1:]))
+        res = {"counts": np.array([(dump / f"{g}.position.bin").stat().st_size // 12 for g in groups], np.int64)}
+        for g in ([groups[0], groups[-1]] if keep == "first_last" else [groups[0]]):
+            for field, dtype, cols in (("position", np.float32, 3), ("polarity", np.float32, 2),
+                                       ("links", np.uint32, 2)):
+                f = dump / f"{g}.{field}.bin"
+                if f.exists():
+                    res[f"{g}_{field}"] = np.fromfile(f, dtype).reshape(-1, cols)
+        res["groups"] = np.array([int(g[1:]) for g in groups], np.int64)
+    np.savez_compressed(HERE / f"{name}.npz", **res)
+    return res
+
+
 def run(name):
     if name in GRID:
         return run_grid(name)
+    if name in EXAMPLES:
+        return run_example(name)
     scen, *_rest, dims, pol = SCENARIOS[name]
     x, p0, prm, steps, dt = inputs(name)
     if name == "lk_writer_nolinks":
@@ -265,13 +302,18 @@ def run(name):
 def main():
     if not REF.exists():
         sys.exit(f"reference sources not found at {REF}")
-    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    names = sys.argv[1:] or list(SCENARIOS) + list(GRID)
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"REF={REF}", "all", "examples"], check=True)
+    names = sys.argv[1:] or list(SCENARIOS) + list(GRID) + list(EXAMPLES)
     manifest = {}
     for name in names:
         r = run(name)
         if name in GRID:
             manifest[name] = {"scenario": GRID[name][0], "points": int(len(r["x"])), "queries": int(len(r["q"]))}
+            print(name, manifest[name])
+            continue
+        if name in EXAMPLES:
+            manifest[name] = {"program": EXAMPLES[name][0], "snapshots": int(len(r["groups"])),
+                              "agents_last": int(r["counts"][-1])}
             print(name, manifest[name])
             continue
         manifest[name] = {"scenario": SCENARIOS[name][0], "cells": int(len(r["x0"])),

@@ -22,6 +22,12 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 SOURCE = Path(__file__).resolve().parent / "cpp" / "drop_in_driver.cpp"
 
 
+def link_flags():
+    """The library the drop-in headers call (views hold device memory through it)."""
+    lib = Path(tg.library_path())
+    return [f"-L{lib.parent}", "-l" + lib.stem[3:], f"-Wl,-rpath,{lib.parent}"]
+
+
 @pytest.fixture(scope="module")
 def driver(tmp_path_factory):
     if shutil.which("g++") is None:
@@ -46,7 +52,7 @@ def test_config_machinery_and_defaults(tmp_path):
                         f"-L{lib.parent}", "-l" + lib.stem[3:], f"-Wl,-rpath,{lib.parent}", "-o", str(out)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    assert subprocess.run([str(out)]).returncode == 0
+    assert subprocess.run([str(out)], cwd=tmp_path).returncode == 0
 
 
 def test_value_types_known_answers(tmp_path):
@@ -56,9 +62,9 @@ def test_value_types_known_answers(tmp_path):
     src = Path(__file__).resolve().parent / "cpp" / "value_types.cpp"
     out = tmp_path / "value_types"
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
-                        "-o", str(out)], capture_output=True, text=True)
+                        *link_flags(), "-o", str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    r = subprocess.run([str(out)], capture_output=True, text=True)
+    r = subprocess.run([str(out)], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0, r.stderr
 
 
@@ -72,9 +78,9 @@ def test_hdf5_writer_matches_python_writer(tmp_path):
     src = Path(__file__).resolve().parent / "cpp" / "h5_writer.cpp"
     exe = tmp_path / "h5_writer"
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
-                        "-o", str(exe)], capture_output=True, text=True)
+                        *link_flags(), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    assert subprocess.run([str(exe), str(tmp_path / "cxx")]).returncode == 0
+    assert subprocess.run([str(exe), str(tmp_path / "cxx")], cwd=tmp_path).returncode == 0
     pos0 = np.array([[0.5 * i, -1.0 * i, 2.0 + i] for i in range(5)], np.float32)
     links = np.array([[l, 4 - l] for l in range(3)], np.uint32)
     pos1 = np.array([[1.0 + i, 0.25 * i, -0.5 * i] for i in range(7)], np.float32)
@@ -104,10 +110,10 @@ def test_hdf5_writer_long_run_matches_python_writer(tmp_path):
     src = Path(__file__).resolve().parent / "cpp" / "h5_writer.cpp"
     exe = tmp_path / "h5_writer"
     r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
-                        str(src), "-o", str(exe)], capture_output=True, text=True)
+                        str(src), *link_flags(), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     steps = 2001
-    assert subprocess.run([str(exe), str(tmp_path / "cxx"), str(steps)]).returncode == 0
+    assert subprocess.run([str(exe), str(tmp_path / "cxx"), str(steps)], cwd=tmp_path).returncode == 0
 
     def pos(s):
         return np.array([[s, -np.float32(s), np.float32(0.5) * np.float32(s)], [1.0, s % 7, -2.0]], np.float32)
@@ -134,10 +140,10 @@ def test_xdmf_sidecar_matches_reference(tmp_path, name):
     src = Path(__file__).resolve().parent / "cpp" / "xdmf_writer.cpp"
     exe = tmp_path / "xdmf_writer"
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
-                        "-o", str(exe)], capture_output=True, text=True)
+                        *link_flags(), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     args = [str(len(g["x0"])), str(len(g["links"])), str(int(g["steps"]) + 1), repr(float(g["dt"]))]
-    assert subprocess.run([str(exe), str(tmp_path / "out"), *args]).returncode == 0
+    assert subprocess.run([str(exe), str(tmp_path / "out"), *args], cwd=tmp_path).returncode == 0
     assert (tmp_path / "out.xmf").read_bytes() == (GOLDEN / f"{name}.xmf").read_bytes()
 
 
@@ -161,7 +167,7 @@ def run_driver(driver, scenario, name, tmp_path):
     write_input(inp, g)
     out = tmp_path / "out"
     r = subprocess.run([str(driver), scenario, str(inp), str(out), str(int(g["steps"])), repr(float(g["dt"]))],
-                       capture_output=True, text=True, timeout=600)
+                       capture_output=True, text=True, timeout=600, cwd=tmp_path)
     return g, out, r
 
 

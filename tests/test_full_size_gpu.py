@@ -55,6 +55,11 @@ def spring_f64(x, pairs, k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8):
     return out
 
 
+def unit(p):
+    th, ph = p[:, 0].astype(np.float64), p[:, 1].astype(np.float64)
+    return np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+
+
 def rel_error(got, ref):
     """max over components of |got - ref| / (|ref| + 1e-6 rms(ref)) and the fraction above RTOL."""
     got = np.asarray(got, np.float64)
@@ -81,7 +86,9 @@ def test_sheet_100k_pass_and_heun_steps():
     xc, qc = c.get_state()
     ok, err, nbad = close(xg, xc, atol=1e-5)
     assert ok, ("positions", err, nbad)
-    ok, err, nbad = close(qg, qc, atol=1e-5)
+    # polarities as unit vectors: the angle phi of a polarity near a pole
+    # (theta ~ 0) is ill-conditioned, its direction is not
+    ok, err, nbad = close(unit(qg), unit(qc), atol=1e-5)
     assert ok, ("polarities", err, nbad)
 
 

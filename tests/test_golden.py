@@ -51,6 +51,9 @@ WRITER = ["lk_writer", "lk_writer_nolinks"]
 USER_LAW = ["gen_bg_heun"]
 # fixtures of the reference's standalone acceleration::Grid queries
 GRID = ["grid_q_3d", "grid_q_2d"]
+# output of five of the reference's example programs run on its headers
+# (tests/test_reference_examples.py compares the drop-in layer's runs with it)
+EXAMPLES = ["ex_springs", "ex_epithelium", "ex_polarization", "ex_growth_w_wall", "ex_delaunay_spheroid"]
 
 
 def load(name):
@@ -75,8 +78,8 @@ def make_oracle(name, g, kind=None):
 
 
 def test_manifest_covers_every_fixture():
-    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW) | set(GRID)
-    for name in USER_LAW:
+    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW) | set(GRID) | set(EXAMPLES)
+    for name in USER_LAW + GRID + EXAMPLES:
         assert (GOLDEN / f"{name}.npz").exists()
     for name in list(KIND) + WRITER:
         assert (GOLDEN / f"{name}.npz").exists()

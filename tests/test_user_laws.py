@@ -63,7 +63,7 @@ def run(driver, scenario, name, tmp_path, steps=None):
     out = tmp_path / "out"
     k = int(g["steps"]) if steps is None else steps
     r = subprocess.run([str(driver), scenario, str(inp), str(out), str(k), repr(float(g["dt"]))],
-                       capture_output=True, text=True, timeout=600)
+                       capture_output=True, text=True, timeout=600, cwd=tmp_path)
     return g, out, r
 
 
@@ -91,7 +91,7 @@ def test_counter_random_is_reproducible_and_well_distributed(tmp_path):
     r = subprocess.run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
                         str(SOURCE.parent / "random_checks.cpp"), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0, r.stdout
 
 
