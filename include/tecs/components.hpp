@@ -12,7 +12,8 @@
 //   integrators::Euler, Heun                      include/integrators/{euler,heun}.hpp
 //   com_fixers::NoComFixer, GlobalComFixer        include/com_fixers/com_fixers.hpp:11-45
 //   forces::Spring2R, PolaritySpring              the built-in pairwise laws
-//   forces::Spring, PiecewiseLinear (+Potential)  the force functions of user laws
+//   forces::Spring, PiecewiseLinear, PiecewiseQuadratic, Cubic, Morse,
+//   LennardJones, HertzContact (+Potential)       the force functions of user laws
 #ifndef TECS_CXX_COMPONENTS_HPP
 #define TECS_CXX_COMPONENTS_HPP
 
@@ -136,6 +137,108 @@ TECS_HD Vector PiecewiseLinear(const Vector& displacement, const Scalar distance
                                const Scalar repulsion_scale = Scalar(1), const Scalar adhesion_scale = Scalar(1)) {
   if (distance == Scalar(0)) return Vector{Scalar(0)};
   const Scalar F = PiecewiseLinearPotential(distance, homeostatic_radius, repulsion_scale, adhesion_scale);
+  return displacement * F / distance;
+}
+
+// The other predefined laws (include/forces/predefined.hpp:167-491), each a
+// magnitude F(d) and the vector displacement * F / distance (zero at d == 0):
+//   PiecewiseQuadratic  k_rep (d - d_c)(d - d_rep) below d_c, k_adh (d - d_c)(d - d_sigma) below d_sigma, else 0
+//   Cubic               mu (d_sigma - d)^2 (d_c - d) below d_sigma, else 0
+//   Morse               2 F0 (exp(-2a(d - d_c)) - exp(-a(d - d_c)))
+//   LennardJones        24 eps / d * (2 (sigma/d)^12 - (d_c/d)^6), 0 at d == 0
+//   HertzContact        4/3 E* sqrt(R*) (R_i + R_j - d)^(3/2) below R_i + R_j, else 0,
+//                       1/E* = (1 - v_i^2)/E_i + (1 - v_j^2)/E_j, R* = R_i R_j / (R_i + R_j)
+// evaluated in the operation order written there.
+template <typename Scalar>
+TECS_HD Scalar PiecewiseQuadraticPotential(const Scalar distance, const Scalar homeostatic_radius,
+                                           const Scalar repulsion_radius, const Scalar cutoff_distance,
+                                           const Scalar repulsion_scale = Scalar(1),
+                                           const Scalar adhesion_scale = Scalar(1)) {
+  if (distance < homeostatic_radius)
+    return repulsion_scale * (distance - homeostatic_radius) * (distance - repulsion_radius);
+  if (distance < cutoff_distance) return adhesion_scale * (distance - homeostatic_radius) * (distance - cutoff_distance);
+  return Scalar(0);
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector PiecewiseQuadratic(const Vector& displacement, const Scalar distance, const Scalar homeostatic_radius,
+                                  const Scalar repulsion_radius, const Scalar cutoff_distance,
+                                  const Scalar repulsion_scale = Scalar(1), const Scalar adhesion_scale = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = PiecewiseQuadraticPotential(distance, homeostatic_radius, repulsion_radius, cutoff_distance,
+                                               repulsion_scale, adhesion_scale);
+  return displacement * F / distance;
+}
+template <typename Scalar>
+TECS_HD Scalar CubicPotential(const Scalar distance, const Scalar homeostatic_radius, const Scalar cutoff_distance,
+                              const Scalar scale = Scalar(1)) {
+  if (distance >= cutoff_distance) return Scalar(0);
+  const Scalar overlap = cutoff_distance - distance;
+  const Scalar diff = homeostatic_radius - distance;
+  return scale * overlap * overlap * diff;
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector Cubic(const Vector& displacement, const Scalar distance, const Scalar homeostatic_radius,
+                     const Scalar cutoff_distance, const Scalar scale = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = CubicPotential(distance, homeostatic_radius, cutoff_distance, scale);
+  return displacement * F / distance;
+}
+template <typename Scalar>
+TECS_HD Scalar MorsePotential(const Scalar distance, const Scalar equilibrium_distance, const Scalar slope = Scalar(1),
+                              const Scalar scaling_factor = Scalar(1)) {
+  const Scalar dx = distance - equilibrium_distance;
+  const Scalar repulsion = tecs::detail::exp_(-Scalar(2) * slope * dx);
+  const Scalar adhesion = tecs::detail::exp_(-slope * dx);
+  return Scalar(2) * scaling_factor * (repulsion - adhesion);
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector Morse(const Vector& displacement, const Scalar distance, const Scalar equilibrium_distance,
+                     const Scalar slope = Scalar(1), const Scalar scaling_factor = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = MorsePotential(distance, equilibrium_distance, slope, scaling_factor);
+  return displacement * F / distance;
+}
+template <typename Scalar>
+TECS_HD Scalar LennardJonesPotential(const Scalar distance, const Scalar sigma, const Scalar equilibrium_distance,
+                                     const Scalar epsilon = Scalar(1)) {
+  if (distance == Scalar(0)) return Scalar(0);
+  const Scalar s6 = tecs::detail::pow_(sigma / distance, Scalar(6));
+  const Scalar s12 = s6 * s6;
+  const Scalar e6 = tecs::detail::pow_(equilibrium_distance / distance, Scalar(6));
+  return (Scalar(24) * epsilon / distance) * (Scalar(2) * s12 - e6);
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector LennardJones(const Vector& displacement, const Scalar distance, const Scalar sigma,
+                            const Scalar equilibrium_distance, const Scalar epsilon = Scalar(1)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = LennardJonesPotential(distance, sigma, equilibrium_distance, epsilon);
+  return displacement * F / distance;
+}
+template <typename Scalar>
+TECS_HD Scalar HertzContactPotential(const Scalar distance, const Scalar radius_i, const Scalar radius_j,
+                                     const Scalar young_modulus_i = Scalar(1), const Scalar young_modulus_j = Scalar(1),
+                                     const Scalar poisson_ratio_i = Scalar(0),
+                                     const Scalar poisson_ratio_j = Scalar(0)) {
+  const Scalar contact = radius_i + radius_j;
+  if (distance >= contact) return Scalar(0);
+  // v^2 as an exact square, which a correctly rounded pow(v, 2) also gives
+  const Scalar vi2 = poisson_ratio_i * poisson_ratio_i;
+  const Scalar vj2 = poisson_ratio_j * poisson_ratio_j;
+  const Scalar e_star = young_modulus_i * young_modulus_j /
+                        ((Scalar(1) - vi2) * young_modulus_j + (Scalar(1) - vj2) * young_modulus_i);
+  const Scalar r_star = (radius_i * radius_j) / contact;
+  const Scalar overlap = contact - distance;
+  return (Scalar(4) / Scalar(3)) * e_star * tecs::detail::sqrt_(r_star) *
+         tecs::detail::pow_(overlap, Scalar(3) / Scalar(2));
+}
+template <typename Scalar, typename Vector>
+TECS_HD Vector HertzContact(const Vector& displacement, const Scalar distance, const Scalar radius_i,
+                            const Scalar radius_j, const Scalar young_modulus_i = Scalar(1),
+                            const Scalar young_modulus_j = Scalar(1), const Scalar poisson_ratio_i = Scalar(0),
+                            const Scalar poisson_ratio_j = Scalar(0)) {
+  if (distance == Scalar(0)) return Vector{Scalar(0)};
+  const Scalar F = HertzContactPotential(distance, radius_i, radius_j, young_modulus_i, young_modulus_j,
+                                         poisson_ratio_i, poisson_ratio_j);
   return displacement * F / distance;
 }
 

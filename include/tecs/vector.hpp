@@ -28,6 +28,10 @@ TECS_HD inline float sqrt_(float v) { return sqrtf(v); }
 TECS_HD inline double sqrt_(double v) { return sqrt(v); }
 TECS_HD inline float fmax_(float a, float b) { return fmaxf(a, b); }
 TECS_HD inline double fmax_(double a, double b) { return fmax(a, b); }
+TECS_HD inline float exp_(float v) { return expf(v); }
+TECS_HD inline double exp_(double v) { return exp(v); }
+TECS_HD inline float pow_(float a, float b) { return powf(a, b); }
+TECS_HD inline double pow_(double a, double b) { return pow(a, b); }
 // the machine epsilon (Kokkos::Experimental::epsilon_v)
 template <typename Scalar>
 TECS_HD constexpr Scalar epsilon_() {

@@ -48,6 +48,7 @@
 #include <com_fixers/com_fixers.hpp>
 #include <io/dummy.hpp>
 #include <io/hdf5_writer.hpp>
+#include <forces/predefined.hpp>
 
 struct Input {
   unsigned n = 0, dims = 0, has_pol = 0;
@@ -447,6 +448,50 @@ static int run_grid(const char* path, const std::string& out) {
   return 0;
 }
 
+// Scenario "laws": the reference's predefined force functions
+// (forces/predefined.hpp:60-491) in float at m distances and displacements
+// read from the input (uint32 m, float32 d[m], float32 disp[m*3]).  Output
+// <out>.laws: per
+// distance 7 magnitudes then 7 vectors (x, y, z), in the order Spring,
+// PiecewiseLinear, PiecewiseQuadratic, Cubic, Morse, LennardJones,
+// HertzContact, with the parameters written beside each call.
+static int run_laws(const char* path, const std::string& out) {
+  using Vector = tecs::VectorN<float, 3>;
+  namespace F = tecs::forces;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return 2;
+  unsigned m = 0;
+  if (std::fread(&m, 4, 1, f) != 1) return 2;
+  std::vector<float> d(m), disp((size_t)m * 3);
+  if (m && (std::fread(d.data(), 4, m, f) != m || std::fread(disp.data(), 4, disp.size(), f) != disp.size()))
+    return 2;
+  std::fclose(f);
+  std::vector<float> res((size_t)m * 28);
+  for (unsigned k = 0; k < m; ++k) {
+    const float r = d[k];
+    const Vector v{disp[3 * k], disp[3 * k + 1], disp[3 * k + 2]};
+    float* o = &res[(size_t)k * 28];
+    o[0] = F::SpringPotential(r, 1.0f, 0.5f);
+    o[1] = F::PiecewiseLinearPotential(r, 0.8f, 1.5f, 0.3f);
+    o[2] = F::PiecewiseQuadraticPotential(r, 1.0f, 1.4f, 1.8f, 2.0f, 0.7f);
+    o[3] = F::CubicPotential(r, 1.0f, 1.6f, 3.0f);
+    o[4] = F::MorsePotential(r, 1.0f, 2.0f, 0.25f);
+    o[5] = F::LennardJonesPotential(r, 0.9f, 1.1f, 0.5f);
+    o[6] = F::HertzContactPotential(r, 0.6f, 0.7f, 2.0f, 3.0f, 0.3f, 0.4f);
+    const Vector w[7] = {F::Spring(v, r, 1.0f, 0.5f),
+                         F::PiecewiseLinear(v, r, 0.8f, 1.5f, 0.3f),
+                         F::PiecewiseQuadratic(v, r, 1.0f, 1.4f, 1.8f, 2.0f, 0.7f),
+                         F::Cubic(v, r, 1.0f, 1.6f, 3.0f),
+                         F::Morse(v, r, 1.0f, 2.0f, 0.25f),
+                         F::LennardJones(v, r, 0.9f, 1.1f, 0.5f),
+                         F::HertzContact(v, r, 0.6f, 0.7f, 2.0f, 3.0f, 0.3f, 0.4f)};
+    for (int l = 0; l < 7; ++l)
+      for (int c = 0; c < 3; ++c) o[7 + 3 * l + c] = w[l][c];
+  }
+  write_raw(out + ".laws", res.data(), res.size() * 4);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
@@ -456,6 +501,11 @@ int main(int argc, char** argv) {
   const std::string sc = argv[1];
   if (sc == "grid_3" || sc == "grid_2") {
     const int rc = sc == "grid_3" ? run_grid<3>(argv[2], argv[3]) : run_grid<2>(argv[2], argv[3]);
+    Kokkos::finalize();
+    return rc;
+  }
+  if (sc == "laws") {
+    const int rc = run_laws(argv[2], argv[3]);
     Kokkos::finalize();
     return rc;
   }

@@ -251,7 +251,39 @@ def run_example(name):
     return res
 
 
+# the reference's predefined force functions (forces/predefined.hpp) at a
+# table of distances: name -> driver scenario
+LAWS = {"laws_predefined": "laws"}
+
+
+def run_laws(name):
+    """Distances 0..2.5 (every branch point of the seven laws, the points
+    beside them, and a random spread) with displacements of those lengths."""
+    rng = np.random.default_rng(11)
+    marks = np.array([0.0, 0.6, 0.8, 0.9, 1.0, 1.1, 1.3, 1.4, 1.6, 1.8, 2.0], np.float32)
+    d = np.concatenate([marks, np.nextafter(marks, np.float32(-1)), np.nextafter(marks, np.float32(3)),
+                        rng.uniform(0.0, 2.5, 200).astype(np.float32)]).astype(np.float32)
+    d = np.abs(d)
+    u = rng.normal(size=(len(d), 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    disp = (u * d[:, None]).astype(np.float32)
+    with tempfile.TemporaryDirectory() as td:
+        inp = Path(td) / "in.bin"
+        with open(inp, "wb") as f:
+            np.array([len(d)], np.uint32).tofile(f)
+            d.tofile(f)
+            disp.tofile(f)
+        out = Path(td) / "out"
+        subprocess.run([str(DRIVER), LAWS[name], str(inp), str(out), "0", "0"], check=True)
+        res = np.fromfile(f"{out}.laws", np.float32).reshape(len(d), 28)
+    r = {"d": d, "disp": disp, "magnitude": res[:, :7], "vector": res[:, 7:].reshape(len(d), 7, 3)}
+    np.savez_compressed(HERE / f"{name}.npz", **r)
+    return r
+
+
 def run(name):
+    if name in LAWS:
+        return run_laws(name)
     if name in GRID:
         return run_grid(name)
     if name in EXAMPLES:
@@ -303,10 +335,14 @@ def main():
     if not REF.exists():
         sys.exit(f"reference sources not found at {REF}")
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"REF={REF}", "all", "examples"], check=True)
-    names = sys.argv[1:] or list(SCENARIOS) + list(GRID) + list(EXAMPLES)
+    names = sys.argv[1:] or list(SCENARIOS) + list(GRID) + list(EXAMPLES) + list(LAWS)
     manifest = {}
     for name in names:
         r = run(name)
+        if name in LAWS:
+            manifest[name] = {"scenario": LAWS[name], "distances": int(len(r["d"]))}
+            print(name, manifest[name])
+            continue
         if name in GRID:
             manifest[name] = {"scenario": GRID[name][0], "points": int(len(r["x"])), "queries": int(len(r["q"]))}
             print(name, manifest[name])

@@ -54,6 +54,9 @@ GRID = ["grid_q_3d", "grid_q_2d"]
 # output of five of the reference's example programs run on its headers
 # (tests/test_reference_examples.py compares the drop-in layer's runs with it)
 EXAMPLES = ["ex_springs", "ex_epithelium", "ex_polarization", "ex_growth_w_wall", "ex_delaunay_spheroid"]
+# the reference's predefined force functions at a table of distances
+# (tests/test_force_laws.py)
+LAWS = ["laws_predefined"]
 
 
 def load(name):
@@ -78,8 +81,8 @@ def make_oracle(name, g, kind=None):
 
 
 def test_manifest_covers_every_fixture():
-    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW) | set(GRID) | set(EXAMPLES)
-    for name in USER_LAW + GRID + EXAMPLES:
+    assert set(MANIFEST) == set(KIND) | set(WRITER) | set(USER_LAW) | set(GRID) | set(EXAMPLES) | set(LAWS)
+    for name in USER_LAW + GRID + EXAMPLES + LAWS:
         assert (GOLDEN / f"{name}.npz").exists()
     for name in list(KIND) + WRITER:
         assert (GOLDEN / f"{name}.npz").exists()
