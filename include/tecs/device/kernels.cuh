@@ -28,12 +28,10 @@ struct Counters {
   unsigned n;           // active cells
   unsigned div_count;   // daughters requested this step
   unsigned done[2];     // last-block counters of the two COM reductions
-  unsigned error;       // bit 0: capacity overflow on division
+  unsigned error;       // bit 0: capacity overflow on division; bit 1: a user law set drag, no old velocities kept
   unsigned done_div;    // last-block counter of the division fixup
   unsigned long long step;        // integrator steps taken (keys the division RNG)
   unsigned long long pair_count;  // pairs recorded by the capture hook
-  unsigned tile_next;             // staged-rows pass: next tile to hand out (zero between launches)
-  unsigned tile_exhausted;        // warps that found no tile left (zero between launches)
 };
 
 struct PassArgs {
@@ -93,6 +91,18 @@ struct PassArgs {
   float link_k;
   // the integrator's is_full_step of this evaluation (Euler, Heun pass 1: 1; Heun pass 2: 0), for user laws
   int full_step;
+  // the integrator's old velocities by cell id (integrators/base.hpp:74), or
+  // null when the simulation does not keep them: user laws that set drag
+  // read them (binned_gabriel.hpp:225-226, 356-357), and k_finish writes the
+  // step's velocity there (euler.hpp:59, heun.hpp:87)
+  float4* old_vel;
+};
+
+// The drag sums of one cell: sum of the pairs' drag and of drag * the other
+// cell's old velocity, in pair order (binned_gabriel.hpp:105-106, 225-226)
+struct DragAcc {
+  float drag;
+  float v[3];
 };
 
 // ---------------------------------------------------------------------------
@@ -924,8 +934,8 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
-                                          unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi,
-                                          const Law& law) {
+                                          unsigned j, const float* xi, float2 pi, Acc& acc, DragAcc& dacc,
+                                          unsigned idi, const Law& law) {
   const float4 vj = a.X[j];
   float disp[3] = {xi[0] - vj.x, xi[1] - vj.y, D >= 3 ? xi[2] - vj.z : 0.f};
   float d2 = disp[0] * disp[0] + disp[1] * disp[1];
@@ -944,13 +954,14 @@ __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, cons
   }
   const float dist = sqrtf(d2);
   const float2 pj = a.P ? a.P[j] : make_float2(0.f, 0.f);
-  for (unsigned r = 0; r < reps; ++r) law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc);
+  for (unsigned r = 0; r < reps; ++r) law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc, dacc);
 }
 
 // cell_general's loops with a user law
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
-                                         const float* xi, float2 pi, unsigned idi, Acc& acc, const Law& law) {
+                                         const float* xi, float2 pi, unsigned idi, Acc& acc, DragAcc& dacc,
+                                         const Law& law) {
   if (FINDER == 1 || FINDER == 3) {
     int bc[3] = {0, 0, 0};
     if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
@@ -968,14 +979,14 @@ __device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const
         const unsigned lo = a.off[flatten<D>(g, c0)], hi = a.off[flatten<D>(g, c1) + 1];
         for (unsigned j = lo; j < hi; ++j) {
           if (j == i) continue;
-          visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, idi, law);
+          visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, dacc, idi, law);
         }
       }
     }
   } else {
     for (unsigned j = 0; j < n; ++j) {
       if (j == i) continue;
-      visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, idi, law);
+      visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, dacc, idi, law);
     }
   }
 }
@@ -996,7 +1007,8 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, Force
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
     const unsigned idi = id_at(a.X, a.Bid, i);
-    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, idi, acc, law);
+    DragAcc dacc = {0.f, {0.f, 0.f, 0.f}};
+    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, idi, acc, dacc, law);
     if constexpr (Law::kGeneric) {
       Acc gen = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
       law.generic(a, idi, xi, pi, gen);
@@ -1004,6 +1016,13 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, Force
       for (int d = 0; d < 3; ++d) acc.x[d] = gen.x[d] + acc.x[d];
       acc.p[0] = gen.p[0] + acc.p[0];
       acc.p[1] = gen.p[1] + acc.p[1];
+    }
+    // out(i) += total_velocity / fmax(total_drag, epsilon), after the pair
+    // sums (binned_gabriel.hpp:356-357); with no drag this adds +0
+    if constexpr (Law::kPairwise) {
+      const float den = fmaxf(dacc.drag, FLT_EPSILON);
+#pragma unroll
+      for (int d = 0; d < D; ++d) acc.x[d] = acc.x[d] + dacc.v[d] / den;
     }
   }
   pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
@@ -1475,7 +1494,7 @@ static __global__ void k_predict(const Counters* __restrict__ ctr, const float* 
 }
 
 // heun.hpp:78-98 (corrector) and euler.hpp:49-69 with the COM subtraction,
-// plus division.  Heun: s = d1 + (d2 - c); x += (s * 0.5) * dt.
+// the old velocities when the simulation keeps them, plus division.  Heun: s = d1 + (d2 - c); x += (s * 0.5) * dt.
 // Euler:  s = d1 - c; x += s * dt.
 template <int D>
 static __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __restrict__ com, const float4* __restrict__ d2,
@@ -1497,6 +1516,8 @@ static __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __re
       const float e0 = v2.x - c0, e1 = v2.y - c1, e2 = v2.z - c2;  // d2 - c2 (corrector)
       const float h0 = f0 + e0, h1 = f1 + e1, h2 = f2 + e2;
       xn[0] = xb.x + (h0 * 0.5f) * dt; xn[1] = xb.y + (h1 * 0.5f) * dt; xn[2] = xb.z + (h2 * 0.5f) * dt;
+      // old_velocities(i) = (d1' + d2') * 0.5 (heun.hpp:87)
+      if (a.old_vel) a.old_vel[a.Bid ? a.Bid[i] : id_of(xb)] = make_float4(h0 * 0.5f, h1 * 0.5f, h2 * 0.5f, 0.f);
       if (a.PA) {
         const float2 pb = a.Bp[i], q1 = a.dp1[i], q2 = dp2[i];
         const float g0 = q1.x + q2.x, g1 = q1.y + q2.y;
@@ -1505,6 +1526,8 @@ static __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __re
     } else {
       const float e0 = v1.x - c0, e1 = v1.y - c1, e2 = v1.z - c2;
       xn[0] = xb.x + e0 * dt; xn[1] = xb.y + e1 * dt; xn[2] = xb.z + e2 * dt;
+      // old_velocities(i) = d1' (euler.hpp:59)
+      if (a.old_vel) a.old_vel[a.Bid ? a.Bid[i] : id_of(xb)] = make_float4(e0, e1, e2, 0.f);
       if (a.PA) {
         const float2 pb = a.Bp[i], q1 = a.dp1[i];
         pn = make_float2(pb.x + q1.x * dt, pb.y + q1.y * dt);

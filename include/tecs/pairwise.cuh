@@ -22,8 +22,12 @@
 //   i, j           the two cells' ids
 //   displacement   x_i - x_j, distance its length
 //   rng            a tecs::CounterRandom keyed by (seed, step, evaluation, i, j)
-//   drag           must stay 0: the drag term is not supported, and a law that
-//                  sets it makes the next count or download fail
+//   drag           the pair's drag coefficient (0 unless the law sets it): the
+//                  cell's position delta gains sum(drag * old velocity of j) /
+//                  max(sum(drag), FLT_EPSILON) after its pair sums.  The
+//                  simulation must keep old velocities (Settings::old_velocities,
+//                  tecs_sim_keep_old_velocities); without them a law that sets
+//                  drag makes the next count or download fail
 //   ctx            ctx.<field>.self / .other / .delta for the config's fields
 // A GENERIC_FORCE law (per cell: is_full_step, i, rng, ctx.<field>.self /
 // .delta) runs in the same pass, added before the pair sums as the reference
@@ -54,6 +58,7 @@ namespace detail {
 template <typename Config, typename G, typename P>
 struct PairLaw {
   static constexpr bool kGeneric = !std::is_same_v<G, NoLaw>;
+  static constexpr bool kPairwise = !std::is_same_v<P, NoLaw>;
   G gen;
   P law;
 
@@ -84,7 +89,7 @@ struct PairLaw {
   }
 
   __device__ void operator()(const PassArgs& a, unsigned idi, unsigned idj, const float* xi, const float4& vj,
-                             const float* disp, float dist, float2 pi, float2 pj, Acc& acc) const {
+                             const float* disp, float dist, float2 pi, float2 pj, Acc& acc, DragAcc& dacc) const {
     if constexpr (!std::is_same_v<P, NoLaw>) {
       constexpr int D = Config::dimensions;
       using Vector = VectorN<float, D>;
@@ -111,7 +116,17 @@ struct PairLaw {
         law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
       }
       for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
-      if (drag != 0.f) atomicOr(&a.ctr->error, 2u);
+      // total_drag += drag; total_velocity += drag * old_velocities(j)
+      // (binned_gabriel.hpp:225-226); a simulation that keeps no old
+      // velocities fails its next count or download when a law sets drag
+      if (a.old_vel) {
+        const float4 ov = a.old_vel[idj];
+        const float o[3] = {ov.x, ov.y, ov.z};
+        dacc.drag = dacc.drag + drag;
+        for (int d = 0; d < D; ++d) dacc.v[d] = dacc.v[d] + drag * o[d];
+      } else if (drag != 0.f) {
+        atomicOr(&a.ctr->error, 2u);
+      }
     }
   }
 };

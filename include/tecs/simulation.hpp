@@ -243,6 +243,23 @@ class Simulation {
   const View<Link>& get_links() const { return links_; }
   unsigned get_link_count() const { return links_.get_active_count(); }
 
+  // The integrator's old velocities (include/simulation.hpp:312-314,
+  // integrators/base.hpp:74): each step's velocity per cell, which user
+  // pairwise laws that set drag read.  The library keeps them once a step
+  // has run a user pairwise law or this was called (zero until the next
+  // step); the view returned is a copy of them as they are now.
+  View<Vector> get_old_velocities_view_from_integrator() {
+    keep_old_velocities();
+    View<Vector> v("integrator_base_old_velocities", capacity);
+    std::vector<float> buf(std::size_t(capacity) * dimensions);
+    unsigned n = 0;
+    check(tecs_sim_old_velocities(handle_, buf.data(), &n));
+    for (unsigned c = 0; c < n; ++c)
+      for (int d = 0; d < dimensions; ++d) v.host_array()[c][d] = buf[std::size_t(c) * dimensions + d];
+    v.copy_to_device();
+    return v;
+  }
+
   unsigned get_capacity() const { return capacity; }
   unsigned get_agent_count() const {
     if (lib_newer_host_ || lib_newer_dev_) {
@@ -480,6 +497,8 @@ class Simulation {
       }
     };
     (one(forces), ...);
+    // a pairwise law may set drag, which reads the old velocities
+    if constexpr (user_pair) keep_old_velocities();
     if constexpr (user) {
       const auto& g = first_of<IsGeneric>(forces...);
       const auto& p = first_of<IsUserPair>(forces...);
@@ -629,6 +648,13 @@ class Simulation {
   bool lib_newer_dev_ = false;      // the library's state is newer than the views' device arrays
   bool lib_newer_host_ = false;     // ... than their host arrays
   bool user_code_ran_ = false;      // user code ran on the device since the views were last checked
+  bool old_velocities_kept_ = false;
+
+  void keep_old_velocities() {
+    if (old_velocities_kept_) return;
+    check(tecs_sim_keep_old_velocities(handle_, 1));
+    old_velocities_kept_ = true;
+  }
 };
 
 }  // namespace tecs

@@ -134,6 +134,20 @@ void* tecs_sim_stream(tecs_sim* sim);
  * views read the state from here. */
 int tecs_sim_download_device(tecs_sim* sim, float* d_positions, float* d_polarity, unsigned* n);
 
+/* The integrator's old velocities (integrators/base.hpp:59,74), which user
+ * pairwise laws that set drag read (binned_gabriel.hpp:225-226, 356-357).
+ * keep != 0 allocates them (capacity x 16 bytes, zeroed) and makes every
+ * step write them: the step's velocity, d1 - c for Euler (euler.hpp:59),
+ * (d1' + d2') * 0.5 for Heun (heun.hpp:87), by cell id.  Keeping them moves
+ * the integrator update out of the last force pass into its own kernel;
+ * keep == 0 frees them.  Non-symmetric finders only.  Synchronises. */
+int tecs_sim_keep_old_velocities(tecs_sim* sim, int keep);
+/* The old velocities of the n active cells in cell-id order (out: n*dims
+ * floats), *n receiving the count; fails when they are not kept. */
+int tecs_sim_old_velocities(tecs_sim* sim, float* out, unsigned* n);
+/* Sets the old velocities of cells 0 .. n-1 (v: n*dims floats). */
+int tecs_sim_set_old_velocities(tecs_sim* sim, const float* v, unsigned n);
+
 /* Device memory for the drop-in layer's views and device variables
  * (include/types/view.hpp:47-266, device_var.hpp:38-134 hold theirs in
  * Kokkos::View device allocations).  tecs_device_copy copies between any two

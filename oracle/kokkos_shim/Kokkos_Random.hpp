@@ -6,6 +6,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <memory>
 
 #include "Kokkos_Core.hpp"
 
@@ -43,17 +44,22 @@ class Random_XorShift64 {
   uint64_t state_;
 };
 
+// Copies of a pool share its state, as Kokkos's pools (which hold their
+// generator states in a View) do: the reference's kernels capture the pool by
+// value (KOKKOS_LAMBDA), and a state freed inside one must be the state the
+// next kernel gets.
 template <class Device = Serial>
 class Random_XorShift64_Pool {
  public:
   using generator_type = Random_XorShift64<Device>;
   using device_type = Device;
-  Random_XorShift64_Pool() = default;
-  explicit Random_XorShift64_Pool(uint64_t seed) : gen_(seed * 0x9E3779B97F4A7C15ull + 1ull) {}
-  generator_type get_state() const { return gen_; }
-  void free_state(const generator_type& g) const { gen_ = g; }
+  Random_XorShift64_Pool() : gen_(std::make_shared<generator_type>(1)) {}
+  explicit Random_XorShift64_Pool(uint64_t seed)
+      : gen_(std::make_shared<generator_type>(seed * 0x9E3779B97F4A7C15ull + 1ull)) {}
+  generator_type get_state() const { return *gen_; }
+  void free_state(const generator_type& g) const { *gen_ = g; }
 
  private:
-  mutable generator_type gen_{1};
+  std::shared_ptr<generator_type> gen_;
 };
 }  // namespace Kokkos

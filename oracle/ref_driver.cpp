@@ -301,6 +301,55 @@ static int tecs_driver_run_generic(const Input& in, const std::string& out, int 
   return 0;
 }
 
+// A pairwise law that sets drag (the spring plus drag = 0.5 * max(1.2 - d, 0)
+// + 0.1): the reference's finders add sum(drag * old velocity of j) /
+// max(sum(drag), eps) to each cell's position delta, and its integrators
+// write the old velocities every step.  Outputs <out>.pos and <out>.ov (the
+// old velocities after the last step).
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields>
+static int tecs_driver_run_drag(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() {
+    return PAIRWISE_FORCE(TECS_DRIVER_SPRING drag = Scalar(0.5) * Kokkos::fmax(Scalar(1.2) - distance, Scalar(0)) +
+                                                    Scalar(0.1);)();
+  };
+  typename Simulation<Config>::Settings st(n, "unused");
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+  auto force = make_force();
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, force);
+  std::vector<float> flat((size_t)n * in.dims), ov((size_t)n * in.dims);
+  auto old = sim.get_old_velocities_view_from_integrator();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) {
+      flat[(size_t)i * in.dims + d] = pos(i)[d];
+      ov[(size_t)i * in.dims + d] = old(i)[d];
+    }
+  write_raw(out + ".pos", flat.data(), flat.size() * 4);
+  write_raw(out + ".ov", ov.data(), ov.size() * 4);
+  return 0;
+}
+
+#define TECS_DRAG_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                          \
+  namespace NAME {                                                                                      \
+  CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
+                                       CONFIG_COM_FIXER(COMFIXER) CONFIG_WRITER(tecs::io::Dummy)        \
+                                           TECS_FIELDS_0)                                                \
+  EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)                                                            \
+  static int run(const Input& in, const std::string& out, int steps, double dt) {                       \
+    return tecs_driver_run_drag<Config, Scalar, Vector, Random, PairwiseForceFields>(in, out, steps, dt); \
+  }                                                                                                     \
+  }
+
 // The reference's writer on a stepped simulation: write_static, write(0), then
 // take_step + write(); its XDMF sidecar <out>.xmf is the output (the HDF5
 // calls go to the HighFive stand-in and write nothing).
@@ -388,6 +437,9 @@ static int run(const Input& in, const std::string& out, int steps, double dt) {
                                                                                                         steps, dt);
 }
 }  // namespace gen_bg_heun_3
+
+TECS_DRAG_SCENARIO(drag_bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer)
+TECS_DRAG_SCENARIO(drag_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::GlobalComFixer)
 
 // Grid-query scenarios (names starting "grid_"): the reference's standalone
 // acceleration::Grid (utils/grid.hpp:29-638) over the input points, with bins
@@ -516,6 +568,7 @@ int main(int argc, char** argv) {
   int rc = 3;
 #define DISPATCH(NAME) \
   if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
+  DISPATCH(drag_bg_heun_3) DISPATCH(drag_ba_euler_com_3)
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(nas_heun_3)

@@ -72,7 +72,8 @@ _EXPORTS = (
     "tecs_sim_stream", "tecs_sim_set_graph", "tecs_sim_kernels_per_step", "tecs_last_error",
     "tecs_sim_set_profiling", "tecs_sim_last_step_profile", "tecs_sim_profile_name", "tecs_sim_set_links",
     "tecs_sim_set_force", "tecs_grid_create", "tecs_grid_destroy", "tecs_grid_rebuild", "tecs_grid_rebuild_device",
-    "tecs_grid_query", "tecs_grid_device_view",
+    "tecs_grid_query", "tecs_grid_device_view", "tecs_sim_keep_old_velocities", "tecs_sim_old_velocities",
+    "tecs_sim_set_old_velocities",
 )
 
 GRID_NEAREST, GRID_RANDOM_IN_BINS, GRID_RANDOM_IN_RADIUS = 0, 1, 2
@@ -123,6 +124,9 @@ def load(build_if_missing: bool = True):
     L.tecs_grid_rebuild_device.argtypes = [vp, vp, ctypes.c_uint]
     L.tecs_grid_query.argtypes = [vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_int, ctypes.c_float, vp, vp, vp]
     L.tecs_grid_device_view.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.tecs_sim_keep_old_velocities.argtypes = [vp, ctypes.c_int]
+    L.tecs_sim_old_velocities.argtypes = [vp, vp, u32p]
+    L.tecs_sim_set_old_velocities.argtypes = [vp, vp, ctypes.c_uint]
     del fp
     for name in _EXPORTS:
         if name not in ("tecs_last_error", "tecs_sim_stream", "tecs_sim_profile_name"):
@@ -266,6 +270,22 @@ class Simulation:
         `strength` (examples/intercalation.cpp:65-71); an empty array removes them."""
         lk = np.ascontiguousarray(links, dtype=np.uint32).reshape(-1, 2)
         _check(load().tecs_sim_set_links(self._h, _ptr(lk) if len(lk) else None, lk.shape[0], float(strength)))
+
+    def keep_old_velocities(self, keep: bool = True):
+        """Keep the integrator's old velocities (integrators/base.hpp:74): each
+        step writes its velocity per cell, and user laws that set drag read
+        them."""
+        _check(load().tecs_sim_keep_old_velocities(self._h, 1 if keep else 0))
+
+    def get_old_velocities(self):
+        v = np.empty((self.desc.capacity, self.dims), np.float32)
+        n = ctypes.c_uint()
+        _check(load().tecs_sim_old_velocities(self._h, _ptr(v), ctypes.byref(n)))
+        return v[: n.value]
+
+    def set_old_velocities(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, self.dims)
+        _check(load().tecs_sim_set_old_velocities(self._h, _ptr(v) if len(v) else None, v.shape[0]))
 
     def set_state_device(self, positions_ptr: int, polarity_ptr: Optional[int], n: int):
         _check(load().tecs_sim_upload_device(self._h, ctypes.c_void_p(positions_ptr),

@@ -27,7 +27,6 @@
 
 #include "../../include/tecs_gpu.h"
 #include "../../include/tecs/device/kernels.cuh"
-#include "../../include/tecs/device/pass_rows.cuh"
 
 using namespace tecs;
 
@@ -108,8 +107,6 @@ __global__ void k_upload(const float* __restrict__ pos, const float2* __restrict
     ctr->error = 0u;
     ctr->done_div = 0u;
     ctr->pair_count = 0ull;
-    ctr->tile_next = 0u;
-    ctr->tile_exhausted = 0u;
   }
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     float4 v = make_float4(0.f, 0.f, 0.f, __uint_as_float(s));
@@ -194,6 +191,8 @@ struct tecs_sim {
   unsigned* link_off = nullptr;
   uint2* link_ent = nullptr;
   unsigned* slot_of = nullptr;
+  // the integrator's old velocities by cell id (float4, capacity), when kept
+  float4* ov = nullptr;
   unsigned n_links = 0;
   float link_k = 0.f;
   // B and Bid hold a sort of the current cells (false from an upload until the
@@ -257,32 +256,6 @@ int prof_mark(tecs_sim* s, int which, const char* name) {
 #define PROF_END(s, name) \
   if (prof_mark((s), 1, (name))) return -1
 
-// A pass kernel and its launch shape: the staged-rows pass runs a persistent
-// grid of 128-thread blocks (at most what is resident at once), the others
-// one 96-thread block per 96 cells.
-struct PassKernel {
-  PassFn fn = nullptr;
-  int threads = kPassThreads;
-  bool persistent = false;
-};
-
-// Blocks of fn resident on the whole device at once (cached per kernel).
-unsigned resident_blocks(PassFn fn, int threads) {
-  static std::mutex mu;
-  static std::vector<std::pair<PassFn, unsigned>> cache;
-  std::lock_guard<std::mutex> lock(mu);
-  for (auto& c : cache)
-    if (c.first == fn) return c.second;
-  int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
-  const unsigned r = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per);
-  cache.emplace_back(fn, r);
-  return r;
-}
-
-PassKernel pass_kernel(const tecs_sim* s, bool sym);
 
 PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
@@ -321,31 +294,6 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
   return nullptr;
 }
 
-// The staged-rows pass where its geometry holds (every witness inside the
-// 3x3x3 bin block, bin coordinates in 10 bits), else pass_fn's kernel.
-PassKernel pass_kernel(const tecs_sim* s, bool sym) {
-  PassKernel k;
-  const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
-  const bool geom = !sym && s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
-                    s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27);
-  const bool gab = F == TECS_FINDER_BINNED_GABRIEL && s->d.gabriel_coefficient <= 0.9f;
-  const bool all = F == TECS_FINDER_BINNED_ALL_PAIRS;
-  const char* env = std::getenv("TECS_PASS");
-  const bool rows = !(env && std::strcmp(env, "coop") == 0);
-  if (rows && geom && (gab || all)) {
-#define ROWS(DD, FF)                                                     \
-    if (D == DD && FO == FF) k.fn = gab ? k_pass_rows<DD, FF, 3> : k_pass_rows<DD, FF, 1>;
-    ROWS(3, 0) ROWS(3, 1) ROWS(3, 2) ROWS(2, 0) ROWS(2, 1)
-#undef ROWS
-    if (k.fn) {
-      k.threads = kRowsThreads;
-      k.persistent = true;
-      return k;
-    }
-  }
-  k.fn = pass_fn(s, sym);
-  return k;
-}
 
 PassArgs base_args(const tecs_sim* s, float dt) {
   PassArgs a{};
@@ -378,6 +326,7 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.slot_of = (s->n_links && s->binned) ? s->slot_of : nullptr;
   a.link_k = s->link_k;
   a.full_step = 1;
+  a.old_vel = s->ov;
   return a;
 }
 
@@ -474,13 +423,11 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
     CK(cudaGetLastError());
     return 0;
   }
-  const PassKernel pk = pass_kernel(s, sym);
-  if (!pk.fn) return fail("unsupported finder/force/dims combination");
+  const PassFn fn = pass_fn(s, sym);
+  if (!fn) return fail("unsupported finder/force/dims combination");
   if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
-  unsigned pblocks = ceil_div(L ? L : 1, (unsigned)pk.threads);
-  if (pk.persistent) pblocks = std::max(1u, std::min(pblocks, resident_blocks(pk.fn, pk.threads)));
   PROF_BEGIN(s);
-  pk.fn<<<pblocks, pk.threads, 0, s->stream>>>(s->g, s->fp, a);
+  fn<<<ceil_div(L ? L : 1, kPassThreads), kPassThreads, 0, s->stream>>>(s->g, s->fp, a);
   PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
               : a.mode == kHeun1Fused ? "k_pass_heun1" : "k_pass_heun2");
   K += 1;
@@ -493,7 +440,8 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
   const bool pol = s->d.has_polarity != 0;
   const bool sym = s->d.symmetric != 0;
   const bool com = s->d.com_fix != 0;
-  const bool fused = !com && !sym;
+  // the old velocities are written by k_finish, after every pass that reads them
+  const bool fused = !com && !sym && !s->ov;
   const unsigned L = launch_count(s);
   const unsigned gb = ceil_div(L ? L : 1, 256);
   const int D = s->d.dims;
@@ -748,7 +696,7 @@ int tecs_sim_destroy(tecs_sim* s) {
   if (s->hctr) cudaFreeHost(s->hctr);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
-                  s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of};
+                  s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of, s->ov};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -870,8 +818,7 @@ int tecs_sim_count(tecs_sim* s, unsigned* n) {
   CK(cudaMemcpyAsync(s->hctr, s->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   if (s->hctr->error & 1u) return fail("capacity exceeded by cell division");
-  if (s->hctr->error & 2u) return fail("a user pairwise law set drag, which this library does not support");
-  if (s->hctr->error & kErrStageTimeout) return fail("a force pass timed out waiting for its staged rows");
+  if (s->hctr->error & 2u) return fail("a user pairwise law set drag in a simulation that keeps no old velocities");
   *n = s->hctr->n;
   return 0;
 }
@@ -988,6 +935,73 @@ int tecs_sim_download_device(tecs_sim* s, float* d_positions, float* d_polarity,
   unsigned n = 0;
   if (tecs_sim_count(s, &n)) return -1;
   if (n_out) *n_out = n;
+  return 0;
+}
+
+namespace {
+// old velocities (float4 by id) <-> D floats per cell
+__global__ void k_vel_out(const float4* __restrict__ ov, unsigned n, int D, float* __restrict__ out) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = ov[i];
+    const float c[3] = {v.x, v.y, v.z};
+    for (int d = 0; d < D; ++d) out[(size_t)i * D + d] = c[d];
+  }
+}
+__global__ void k_vel_in(const float* __restrict__ in, unsigned n, int D, float4* __restrict__ ov) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float c[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < D; ++d) c[d] = in[(size_t)i * D + d];
+    ov[i] = make_float4(c[0], c[1], c[2], 0.f);
+  }
+}
+}  // namespace
+
+int tecs_sim_keep_old_velocities(tecs_sim* s, int keep) {
+  if (!s) return fail("null simulation");
+  if (keep && s->d.symmetric) return fail("old velocities are kept with the non-symmetric finders");
+  if ((keep != 0) == (s->ov != nullptr)) return 0;
+  CK(cudaSetDevice(s->d.device));
+  CK(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  if (!keep) {
+    CK(cudaFree(s->ov));
+    s->ov = nullptr;
+    return 0;
+  }
+  CK(cudaMalloc(&s->ov, sizeof(float4) * s->d.capacity));
+  CK(cudaMemsetAsync(s->ov, 0, sizeof(float4) * s->d.capacity, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+int tecs_sim_old_velocities(tecs_sim* s, float* out, unsigned* n_out) {
+  if (!s || !out) return fail("null argument");
+  if (!s->ov) return fail("the simulation keeps no old velocities");
+  CK(cudaSetDevice(s->d.device));
+  unsigned n = 0;
+  if (tecs_sim_count(s, &n)) return -1;
+  if (n_out) *n_out = n;
+  if (!n) return 0;
+  const int D = s->d.dims;
+  // Xt is free between steps
+  k_vel_out<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->ov, n, D, reinterpret_cast<float*>(s->Xt));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, s->Xt, (size_t)n * D * 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+int tecs_sim_set_old_velocities(tecs_sim* s, const float* v, unsigned n) {
+  if (!s || (!v && n)) return fail("null argument");
+  if (!s->ov) return fail("the simulation keeps no old velocities");
+  if (n > s->d.capacity) return fail("agent count exceeds capacity");
+  if (!n) return 0;
+  CK(cudaSetDevice(s->d.device));
+  const int D = s->d.dims;
+  CK(cudaMemcpyAsync(s->Xt, v, (size_t)n * D * 4, cudaMemcpyHostToDevice, s->stream));
+  k_vel_in<<<ceil_div(n, 256), 256, 0, s->stream>>>(reinterpret_cast<const float*>(s->Xt), n, D, s->ov);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s->stream));
   return 0;
 }
 

