@@ -505,7 +505,8 @@ def run_gb300(args):
         ensemble = ensemble_comparison(args, local)
     line = {
         "metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms),
+        "ms_per_timed_step": statistics.mean(step_ms) * chunk, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["desc"].format(n=n), "cells": n, "capacity": sim.desc.capacity,
                    "sim_steps_per_timed_step": chunk, "sim_steps_timed": args.steps * chunk,
@@ -589,7 +590,9 @@ def run_ensemble(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20,
+                    help="timed steps, each of --chunk simulation steps (default 20 x 10: the spheroid "
+                         "configuration's 200 steps)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=0, help="cell count (default: the workload's)")

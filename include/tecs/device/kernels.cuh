@@ -1092,10 +1092,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
   static_assert(FINDER == 1 || FINDER == 3, "the binned finders");
   constexpr bool POL = FORCE == 2;
-  // neighbour slots per cell; the polarity law's extra per-pair float only
-  // fits in the static shared memory with 12 (cells with more in-cutoff
-  // neighbours take the per-thread path)
-  constexpr int NB = POL ? 12 : kMaxNb;
+  constexpr int NB = kMaxNb;  // neighbour slots per cell (more: the per-thread path)
   __shared__ float4 cand[NB * kPassThreads];           // [q][t]: position, w = (slot << 5) | bin code
   __shared__ float4 home[kPassThreads];                // position, w = packed bin coords
   __shared__ unsigned short pinfo[NB * kPassThreads];  // each warp's pairs: (t << 4) | q
@@ -1103,11 +1100,6 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
   __shared__ unsigned amask[kPassThreads];             // accepted pairs of each cell, bit q
   __shared__ unsigned char ncnt[kPassThreads];
   __shared__ unsigned char fallback[kPassThreads];
-  // polarity law: the home cells' angles and their sin/cos, and the second
-  // polarity component of each pair's force (the first rides in cand.w)
-  __shared__ float2 hpol[POL ? kPassThreads : 1];
-  __shared__ PolTrig htrig[POL ? kPassThreads : 1];
-  __shared__ float pext[POL ? NB * kPassThreads : 1];
 
   const unsigned n = a.ctr->n;
   const int t = threadIdx.x;
@@ -1209,10 +1201,6 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
                         __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
   ncnt[t] = (unsigned char)cnt;
   fallback[t] = fb ? 1 : 0;
-  if (POL) {
-    hpol[t] = pi;
-    if (cnt) htrig[t] = pol_trig(pi);
-  }
   // Phases 2-4 run per warp over the warp's own 32 cells (no block
   // barrier).  Pair offsets: the warp's pairs sorted by their cell's
   // neighbour count, so that the Gabriel loops of a round of pairs run the
@@ -1358,17 +1346,9 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
         if (D >= 3) f.z = (disp[2] * F) / dist;
       }
     }
-    if (POL) {
-      // the spring and bending vector terms of the pair, and its two polarity
-      // terms, each pre-added (phase 4 adds one sum per pair)
-      float sv[3], bv[3], bp[2], al[2];
-      spring_term<3>(fp, disp, dist, sv);
-      const float2 pj = __ldg(&a.P[__float_as_uint(vj.w) >> 5]);
-      polarity_terms(fp, disp, dist, hpol[c], htrig[c], pj, pol_trig(pj), bv, bp, al);
-      f = make_float4(sv[0] + bv[0], sv[1] + bv[1], sv[2] + bv[2], bp[0] + al[0]);
-      pext[cix(q, c)] = bp[1] + al[1];
-    }
-    cand[cix(q, c)] = f;
+    // the polarity law's pairs are summed term by term in phase 4: the
+    // candidate keeps its position
+    if (!POL) cand[cix(q, c)] = f;
   }
   __syncwarp();
   // ---- phase 4: ordered per-cell sums
@@ -1380,13 +1360,19 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
       for (int q = 0; q < cnt; ++q) {
         if (!((amask[t] >> q) & 1u)) continue;
         const float4 f = cand[cix(q, t)];
+        if (POL) {
+          // the pair's spring, bending vector, bending and alignment terms,
+          // each added to the sums in turn (polarity.hpp:131-198)
+          const float disp[3] = {xi[0] - f.x, xi[1] - f.y, xi[2] - f.z};
+          float d2 = disp[0] * disp[0] + disp[1] * disp[1];
+          d2 = d2 + disp[2] * disp[2];
+          const float2 pj = __ldg(&a.P[__float_as_uint(f.w) >> 5]);
+          pair_force<3, 2>(fp, disp, sqrtf(d2), pi, pj, acc);
+          continue;
+        }
         acc.x[0] = acc.x[0] + f.x;
         acc.x[1] = acc.x[1] + f.y;
         if (D >= 3) acc.x[2] = acc.x[2] + f.z;
-        if (POL) {
-          acc.p[0] = acc.p[0] + f.w;
-          acc.p[1] = acc.p[1] + pext[cix(q, t)];
-        }
       }
     }
   }

@@ -141,8 +141,8 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 }
 
 // ---------------------------------------------------------------------------
-// the force pass over all slots: block-cooperative, the design k_pass_gabriel
-// had before its phases became per-warp (the engine keeps this one)
+// the force pass over all slots: k_pass_gabriel's per-warp phases with each
+// cell's simulation parameters taken from the table
 
 // POL: some resident simulation carries polarity; their cells then take the
 // cooperative path with the polarity law, its pair terms added in the ordered
@@ -153,10 +153,9 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
   __shared__ float4 cand[NB * kPassThreads];
   __shared__ float4 home[kPassThreads];
   __shared__ unsigned short pinfo[NB * kPassThreads];
-  __shared__ unsigned wpk[kPassThreads / 32];
+  __shared__ unsigned short wcls[kPassThreads / 32][NB + 1];  // pairs per (warp, neighbour count)
   __shared__ unsigned amask[kPassThreads];
   __shared__ unsigned char ncnt[kPassThreads];
-  __shared__ unsigned char fallback[kPassThreads];
   __shared__ unsigned hsim[kPassThreads];
   const unsigned n = e.off[e.nb_total];
   const int t = threadIdx.x;
@@ -253,49 +252,46 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
                         __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
   hsim[t] = sim;
   ncnt[t] = (unsigned char)cnt;
-  fallback[t] = fb ? 1 : 0;
-  // pair offsets, pairs grouped by their cell's neighbour count (as k_pass_gabriel)
+  // Phases 2-4 run per warp over the warp's own 32 cells, as in
+  // k_pass_gabriel.  Only cells of Gabriel slots with two or more neighbours
+  // need the Gabriel test (a single neighbour has no witness; all-pairs
+  // slots accept every in-cutoff pair); their pairs are listed sorted by the
+  // cell's neighbour count, so that the witness loops of a round run the
+  // same length.
+  const int lane = t & 31, warp = t >> 5;
+  unsigned short* const wp = pinfo + warp * 32 * NB;
+  const bool tested = run && !fb && gab && cnt >= 2;
+  const int tcnt = tested ? cnt : 0;
   int P = 0;
   {
-    const int lane = t & 31, warp = t >> 5;
-    const int cls = cnt <= 4 ? 0 : (cnt <= 8 ? 1 : 2);
-    unsigned incl = (unsigned)cnt << (10 * cls);
+    if (lane <= NB) wcls[warp][lane] = 0;
+    __syncwarp();
+    const unsigned same = __match_any_sync(0xffffffffu, tcnt);
+    const int rank = __popc(same & ((1u << lane) - 1u));
+    if (rank == 0) wcls[warp][tcnt] = (unsigned short)(__popc(same) * (unsigned)tcnt);
+    amask[t] = tested ? 0u : (1u << cnt) - 1u;  // cnt <= 16; 0 for fallback and idle cells
+    __syncwarp();
+    const unsigned tot = lane <= NB ? (unsigned)wcls[warp][lane] : 0u;
+    unsigned incl = tot;
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    if (lane == 31) wpk[warp] = incl;
-    amask[t] = 0u;
-    __syncthreads();
-    int tot[3] = {0, 0, 0}, before = 0;
-#pragma unroll
-    for (int w = 0; w < kPassThreads / 32; ++w) {
-      const unsigned v = wpk[w];
-#pragma unroll
-      for (int f = 0; f < 3; ++f) tot[f] += (int)((v >> (10 * f)) & 1023u);
-      if (w < warp) before += (int)((v >> (10 * cls)) & 1023u);
-    }
-    int base = before + (int)((incl >> (10 * cls)) & 1023u) - cnt;
-    if (cls >= 1) base += tot[0];
-    if (cls >= 2) base += tot[1];
-    P = tot[0] + tot[1] + tot[2];
-    for (int q = 0; q < cnt; ++q) pinfo[base + q] = (unsigned short)((t << 4) | q);
+    P = (int)__shfl_sync(0xffffffffu, incl, NB);
+    const int base = (int)__shfl_sync(0xffffffffu, incl - tot, tcnt) + rank * tcnt;
+    for (int q = 0; q < tcnt; ++q) wp[base + q] = (unsigned short)((t << 4) | q);
   }
-  __syncthreads();
+  __syncwarp();
 
-  // Gabriel test (all-pairs slots accept every in-cutoff pair)
-  for (int p = t; p < P; p += kPassThreads) {
-    const unsigned info = pinfo[p];
+  // ---- Gabriel test, one pair per lane at a time, two witnesses per round
+  for (int p = lane; p < P; p += 32) {
+    const unsigned info = wp[p];
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const SimSlot& cs = e.table[hsim[c]];
-    if (cs.finder != TECS_FINDER_BINNED_GABRIEL) {
-      atomicOr(&amask[c], 1u << q);
-      continue;
-    }
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
     const float hx[3] = {h.x, h.y, h.z};
-    float disp[3] = {hx[0] - vj.x, hx[1] - vj.y, hx[2] - vj.z};
+    const float disp[3] = {hx[0] - vj.x, hx[1] - vj.y, hx[2] - vj.z};
     float d2 = disp[0] * disp[0] + disp[1] * disp[1];
     d2 = d2 + disp[2] * disp[2];
     float m[3];
@@ -303,36 +299,69 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     for (int d = 0; d < 3; ++d) m[d] = hx[d] - disp[d] * 0.5f;
     const float rsq = d2 * cs.fp.gab_factor;
     const int cc = ncnt[c];
+    unsigned hits = 0u, bit = 1u;
+    for (int w = 0; w < cc; w += 2) {
+      const int w1 = min(w + 1, cc - 1);
+      const float4 vk0 = cand[cix(w, c)], vk1 = cand[cix(w1, c)];
+      const float f0 = vk0.x - m[0], f1 = vk0.y - m[1], f2 = vk0.z - m[2];
+      const float g0 = vk1.x - m[0], g1 = vk1.y - m[1], g2 = vk1.z - m[2];
+      float sd0 = f0 * f0 + f1 * f1, sd1 = g0 * g0 + g1 * g1;
+      sd0 = sd0 + f2 * f2;
+      sd1 = sd1 + g2 * g2;
+      if (sd0 < rsq) hits |= bit;
+      if (sd1 < rsq) hits |= bit << 1;
+      bit <<= 2;
+    }
+    hits &= ((1u << cc) - 1u) & ~(1u << q);
     bool blocked = false;
-    for (int w = 0; w < cc; ++w) {
-      if (w == q) continue;
-      const float4 vk = cand[cix(w, c)];
-      const float f0 = vk.x - m[0], f1 = vk.y - m[1], f2 = vk.z - m[2];
-      float sd = f0 * f0 + f1 * f1;
-      sd = sd + f2 * f2;
-      if (!(sd < rsq)) continue;
+    if (hits) {
+      // a witness in the ball blocks only from a bin overlapping the ball
+      // (binned_gabriel.hpp:142-153), relative to the cell's bin
       const unsigned hb = __float_as_uint(h.w);
       const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
-      const unsigned code = __float_as_uint(vk.w) & 31u;
-      const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
       const float r = sqrtf(rsq);
-      bool inside = true;
+      int lo[3], hi[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const int lo = clampi((int)floorf((m[d] - r - cs.g.mn[d]) * cs.g.inv_bin), cs.g.ext[d] - 1) - hbc[d];
-        const int hi = clampi((int)floorf((m[d] + r - cs.g.mn[d]) * cs.g.inv_bin), cs.g.ext[d] - 1) - hbc[d];
-        inside = inside && rel[d] >= lo && rel[d] <= hi;
+        lo[d] = clampi((int)floorf((m[d] - r - cs.g.mn[d]) * cs.g.inv_bin), cs.g.ext[d] - 1) - hbc[d];
+        hi[d] = clampi((int)floorf((m[d] + r - cs.g.mn[d]) * cs.g.inv_bin), cs.g.ext[d] - 1) - hbc[d];
       }
-      if (inside) { blocked = true; break; }
+      while (hits && !blocked) {
+        const int w = __ffs(hits) - 1;
+        hits &= hits - 1u;
+        const unsigned code = __float_as_uint(cand[cix(w, c)].w) & 31u;
+        const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
+        bool inside = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) inside = inside && rel[d] >= lo[d] && rel[d] <= hi[d];
+        blocked = inside;
+      }
     }
     if (!blocked) atomicOr(&amask[c], 1u << q);
   }
-  __syncthreads();
-  // pair forces (spring2r), written over the candidate slot
-  for (int p = t; p < P; p += kPassThreads) {
-    const unsigned info = pinfo[p];
+  __syncwarp();
+  // the warp's accepted spring pairs, cell by cell, over the pair list (the
+  // polarity law's pairs are summed term by term in the ordered sums)
+  int PA = 0;
+  {
+    const bool pol_cell = POL && polar && sl.fp.force == TECS_FORCE_POLARITY;
+    const unsigned acc_bits = (fb || pol_cell || !run) ? 0u : amask[t];
+    const int na = __popc(acc_bits);
+    int incl = na;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    PA = __shfl_sync(0xffffffffu, incl, 31);
+    int base = incl - na;
+    __syncwarp();
+    for (unsigned b = acc_bits; b; b &= b - 1u) wp[base++] = (unsigned short)((t << 4) | (__ffs(b) - 1));
+  }
+  __syncwarp();
+  // ---- spring2r forces of the accepted pairs, written over the candidate slot
+  for (int p = lane; p < PA; p += 32) {
+    const unsigned info = wp[p];
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
-    if (!((amask[c] >> q) & 1u)) continue;
     const SimSlot& cs = e.table[hsim[c]];
     const float4 h = home[c];
     const float4 vj = cand[cix(q, c)];
@@ -342,21 +371,21 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
     const float dist = sqrtf(d2);
     if (cs.fp.force != TECS_FORCE_NONE && dist != 0.0f) {
+      // (displacement * F) / distance; a zero F leaves the sum unchanged
       const ForceP& fp = cs.fp;
       const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
-      f.x = (disp[0] * F) / dist;
-      f.y = (disp[1] * F) / dist;
-      f.z = (disp[2] * F) / dist;
+      if (F != 0.0f) {
+        f.x = (disp[0] * F) / dist;
+        f.y = (disp[1] * F) / dist;
+        f.z = (disp[2] * F) / dist;
+      }
     }
-    // the polarity law's pairs are summed term by term in the ordered sums
-    // below (the reference's order, as the single-simulation pass adds them)
-    if (POL && cs.fp.force == TECS_FORCE_POLARITY) continue;
     cand[cix(q, c)] = f;
   }
-  __syncthreads();
-  // ordered sums of the cooperative pairs
+  __syncwarp();
+  // ---- ordered per-cell sums
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
-  if (run && !fallback[t]) {
+  if (run && !fb) {
     const bool pol_law = POL && polar && sl.fp.force == TECS_FORCE_POLARITY;
     for (int q = 0; q < cnt; ++q) {
       if (!((amask[t] >> q) & 1u)) continue;
@@ -376,11 +405,11 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       acc.x[2] = acc.x[2] + f.z;
     }
   }
-  // every thread has read its sums: the candidate array is free again and
-  // serves the per-thread neighbour lists of the polarity / overflow paths
-  __syncthreads();
+  // the warp's sums are read: its candidate columns serve the per-thread
+  // neighbour lists of the overflow path
+  __syncwarp();
   if (!run) return;
-  if (fallback[t]) {
+  if (fb) {
     PassArgs pa{};
     pa.X = e.X;
     pa.P = sl.has_pol ? e.P : nullptr;

@@ -172,4 +172,8 @@ def test_user_law_setting_drag_reproduces_reference(driver, tmp_path, name, exac
         np.testing.assert_array_equal(pos, g["pos"])
         np.testing.assert_array_equal(ov, g["ov"])
     else:
-        assert close(pos, g["pos"]) and close(ov, g["ov"])
+        # the COM sum's last bits move the positions by ~1e-6; the old
+        # velocities are forces at those positions (spring stiffness 2, drag
+        # weights up to 0.6), so they agree to ~1e-5 absolute
+        assert close(pos, g["pos"])
+        assert close(ov, g["ov"], rtol=1e-4, atol=1e-4)
