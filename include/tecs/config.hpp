@@ -159,26 +159,26 @@ struct DefaultSimulationConfig {
     RESOLVE_TECS_CONFIG()                                  \
   };
 
-#define EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                                 \
-  using Scalar = typename C::Scalar;                                                            \
-  static constexpr int dimensions = C::dimensions;                                              \
-  using Vector = tecs::VectorN<Scalar, dimensions>;                                             \
-  using VectorI = tecs::VectorN<int, dimensions>;                                               \
-  using VectorView = tecs::View<Vector>;                                                        \
-  using Polarity = tecs::Polarity_<Scalar>;                                                     \
-  using Plane = tecs::PlaneN<Scalar, dimensions>;                                               \
-  using RandomPool = tecs::XorShiftPool;                                                        \
-  using Random = tecs::XorShiftRandom;                                                          \
-  using GenericForceFields = typename C::template ForceFields<tecs::detail::GenericFieldRef>;   \
-  using PairwiseForceFields = typename C::template ForceFields<tecs::detail::PairwiseFieldRef>; \
-  using LinkForceFields = typename C::template ForceFields<tecs::detail::LinkFieldRef>;
+#define EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                                                  \
+  using Scalar [[maybe_unused]] = typename C::Scalar;                                                            \
+  [[maybe_unused]] static constexpr int dimensions = C::dimensions;                                              \
+  using Vector [[maybe_unused]] = tecs::VectorN<Scalar, dimensions>;                                             \
+  using VectorI [[maybe_unused]] = tecs::VectorN<int, dimensions>;                                               \
+  using VectorView [[maybe_unused]] = tecs::View<Vector>;                                                        \
+  using Polarity [[maybe_unused]] = tecs::Polarity_<Scalar>;                                                     \
+  using Plane [[maybe_unused]] = tecs::PlaneN<Scalar, dimensions>;                                               \
+  using RandomPool [[maybe_unused]] = tecs::XorShiftPool;                                                        \
+  using Random [[maybe_unused]] = tecs::XorShiftRandom;                                                          \
+  using GenericForceFields [[maybe_unused]] = typename C::template ForceFields<tecs::detail::GenericFieldRef>;   \
+  using PairwiseForceFields [[maybe_unused]] = typename C::template ForceFields<tecs::detail::PairwiseFieldRef>; \
+  using LinkForceFields [[maybe_unused]] = typename C::template ForceFields<tecs::detail::LinkFieldRef>;
 
-#define EXTRACT_ALL_FROM_SIMULATION_CONFIG(C)                            \
-  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                \
-  using Fields = typename C::Fields;                                     \
-  using Integrator = typename C::template IntegratorT<C>;                \
-  using PairFinder = typename C::template PairFinderT<C>;                \
-  using ComFixer = typename C::template ComFixerT<C>;                    \
-  using Writer = typename C::template WriterT<C>;
+#define EXTRACT_ALL_FROM_SIMULATION_CONFIG(C)                                                                    \
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(C)                                                                        \
+  using Fields [[maybe_unused]] = typename C::Fields;                                                            \
+  using Integrator [[maybe_unused]] = typename C::template IntegratorT<C>;                                       \
+  using PairFinder [[maybe_unused]] = typename C::template PairFinderT<C>;                                       \
+  using ComFixer [[maybe_unused]] = typename C::template ComFixerT<C>;                                           \
+  using Writer [[maybe_unused]] = typename C::template WriterT<C>;
 
 #endif  // TECS_CXX_CONFIG_HPP

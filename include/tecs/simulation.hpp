@@ -387,6 +387,35 @@ class Simulation {
     if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
   }
 
+  // run_custom(count, f...) (include/simulation.hpp:566-598): f(i, rng) for
+  // i in [0, count).  Several functions are fused per index as the
+  // reference's kernel fuser does (kernel_fuser.hpp:42-48): for each i every
+  // function in turn, with the same generator.  Like init, on the host in
+  // index order from the reference's generator stream; the views and the
+  // links the functions may write are sent to the library before the next
+  // step.
+  template <typename... Funcs>
+  void run_custom(unsigned count, Funcs&&... functions) {
+    refresh_host();
+    for (unsigned i = 0; i < count; ++i) {
+      Random g = pool_.get_state();
+      (functions(i, g), ...);
+      pool_.free_state(g);
+    }
+    positions_.set_host_modified(true);
+    if constexpr (has_polarity) polarity_.set_host_modified(true);
+    links_dirty_ = true;
+  }
+  // over the agents, and over the active links
+  template <typename... Funcs>
+  void run(Funcs&&... functions) {
+    run_custom(agent_count, static_cast<Funcs&&>(functions)...);
+  }
+  template <typename... Funcs>
+  void run_links(Funcs&&... functions) {
+    run_custom(links_.get_active_count(), static_cast<Funcs&&>(functions)...);
+  }
+
   // -- output (include/simulation.hpp:600-667) --------------------------------
   // One snapshot of every field, the given extra views and the links, in
   // group "t<current_step>"; current_step counts the writes.  The config's

@@ -339,6 +339,67 @@ static int tecs_driver_run_drag(const Input& in, const std::string& out, int ste
   return 0;
 }
 
+// Update functions between steps, as the reference's growth and protrusion
+// programs run them: Simulation::run with two UPDATE_FUNC functions (fused per
+// cell, one generator), run_links with one that rewires every link, and an
+// INIT_FUNC through init; then the steps.  Outputs <out>.pos, <out>.links
+// (uint32 pairs) and <out>.hits (int32: a DeviceVar counter the functions add to).
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields>
+static int tecs_driver_run_update(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() { return PAIRWISE_FORCE(TECS_DRIVER_SPRING)(); };
+  typename Simulation<Config>::Settings st(n, "unused");
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  st.link_capacity = n;
+  st.link_active_count = n;
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+  auto& links = sim.get_links();
+  DeviceVar<int> hits = 0;
+  auto nudge_x = UPDATE_FUNC(pos(i)[0] += Scalar(0.01) * Scalar(rng.drand(-1.0, 1.0)););
+  auto nudge_y = UPDATE_FUNC(
+    pos(i)[1] += Scalar(0.01) * Scalar(rng.drand(-1.0, 1.0));
+    if (rng.drand(0.0, 1.0) < 0.1) Kokkos::atomic_fetch_add(hits.data(), 1););
+  auto rewire = UPDATE_FUNC(links(i) = Link{i, (unsigned)rng.urand(n)};);
+  auto lift = INIT_FUNC(pos(i)[2] += Scalar(0.001) * Scalar(rng.frand(0.0f, 1.0f)););
+  sim.run(nudge_x(), nudge_y());
+  sim.run_links(rewire());
+  sim.init(lift());
+  auto force = make_force();
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, force);
+  std::vector<float> flat((size_t)n * in.dims);
+  for (unsigned i = 0; i < n; ++i)
+    for (unsigned d = 0; d < in.dims; ++d) flat[(size_t)i * in.dims + d] = pos(i)[d];
+  std::vector<unsigned> lk(2 * (size_t)n);
+  for (unsigned l = 0; l < n; ++l) {
+    lk[2 * l] = links(l).a;
+    lk[2 * l + 1] = links(l).b;
+  }
+  const int h = hits;
+  write_raw(out + ".pos", flat.data(), flat.size() * 4);
+  write_raw(out + ".links", lk.data(), lk.size() * 4);
+  write_raw(out + ".hits", &h, 4);
+  return 0;
+}
+
+namespace upd_bg_heun_3 {
+using namespace tecs;
+CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel) CONFIG_INTEGRATOR(integrators::Heun)
+                                     CONFIG_WRITER(tecs::io::Dummy) TECS_FIELDS_0)
+EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)
+static int run(const Input& in, const std::string& out, int steps, double dt) {
+  return tecs_driver_run_update<Config, Scalar, Vector, Random, PairwiseForceFields>(in, out, steps, dt);
+}
+}  // namespace upd_bg_heun_3
+
 #define TECS_DRAG_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                          \
   namespace NAME {                                                                                      \
   CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
@@ -568,7 +629,7 @@ int main(int argc, char** argv) {
   int rc = 3;
 #define DISPATCH(NAME) \
   if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
-  DISPATCH(drag_bg_heun_3) DISPATCH(drag_ba_euler_com_3)
+  DISPATCH(drag_bg_heun_3) DISPATCH(drag_ba_euler_com_3) DISPATCH(upd_bg_heun_3)
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(nas_heun_3)

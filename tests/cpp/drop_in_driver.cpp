@@ -237,6 +237,54 @@ static int run_written_links(const Input& in, const std::string& out, int steps,
   return 0;
 }
 
+// update functions between steps, as the reference's growth and protrusion
+// programs run them: run with two UPDATE_FUNC functions (fused per cell),
+// run_links with one that rewires every link, an INIT_FUNC through init,
+// then the steps; writes <out>.pos, <out>.links and <out>.hits
+static int run_update(const Input& in, const std::string& out, int steps, double dt) {
+  using Sim = Simulation<BinnedGabrielHeun>;
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
+  const unsigned n = in.n;
+  Sim::Settings settings(n, "unused");
+  settings.cutoff_distance = in.prm[0];
+  settings.pair_finder_settings.gabriel_coefficient = in.prm[1];
+  for (int d = 0; d < 3; ++d) {
+    settings.pair_finder_settings.min_bounds[d] = in.prm[2 + d];
+    settings.pair_finder_settings.max_bounds[d] = in.prm[5 + d];
+  }
+  settings.pair_finder_settings.bin_size_scale = in.prm[14];
+  settings.link_capacity = n;
+  settings.link_active_count = n;
+  Sim sim(settings);
+  auto& pos = sim.get_view<FIELD(Vector, position)>();
+  for (unsigned i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) pos(i)[d] = in.x[std::size_t(i) * 3 + d];
+  auto& links = sim.get_links();
+  DeviceVar<int> hits = 0;
+  auto nudge_x = UPDATE_FUNC(pos(i)[0] += Scalar(0.01) * Scalar(rng.drand(-1.0, 1.0)););
+  auto nudge_y = UPDATE_FUNC(
+    pos(i)[1] += Scalar(0.01) * Scalar(rng.drand(-1.0, 1.0));
+    if (rng.drand(0.0, 1.0) < 0.1) Kokkos::atomic_fetch_add(hits.data(), 1););
+  auto rewire = UPDATE_FUNC(links(i) = Link{i, (unsigned)rng.urand(n)};);
+  auto lift = INIT_FUNC(pos(i)[2] += Scalar(0.001) * Scalar(rng.frand(0.0f, 1.0f)););
+  sim.run(nudge_x(), nudge_y());
+  sim.run_links(rewire());
+  sim.init(lift());
+  const forces::Spring2R spring{in.prm[8], in.prm[9], in.prm[10], in.prm[11]};
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, spring);
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(n) * sizeof(Vector));
+  std::vector<unsigned> lk(2 * std::size_t(n));
+  for (unsigned l = 0; l < n; ++l) {
+    lk[2 * l] = links(l).a;
+    lk[2 * l + 1] = links(l).b;
+  }
+  write_raw(out + ".links", lk.data(), lk.size() * 4);
+  const int h = hits;
+  write_raw(out + ".hits", &h, 4);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 6) {
     std::fprintf(stderr, "usage: %s <scenario> <in.bin> <out_prefix> <steps> <dt>\n", argv[0]);
@@ -259,6 +307,7 @@ int main(int argc, char** argv) {
     if (sc == "bg_heun_h5") return run_written(in, out, steps, dt);
     if (sc == "lk_ba_euler_com") return run_links<BinnedAllPairsEulerCom>(in, out, steps, dt);
     if (sc == "lk_writer") return run_written_links(in, out, steps, dt);
+    if (sc == "upd_bg_heun") return run_update(in, out, steps, dt);
   } catch (const tecs::Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());
     return 1;

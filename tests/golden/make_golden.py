@@ -66,6 +66,8 @@ SCENARIOS = {
     # a pairwise law that sets drag: final positions and old velocities
     "drag_bg_heun": ("drag_bg_heun_3", 3, 0, 1, 0, 3, 0),
     "drag_ba_euler_com": ("drag_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
+    # update functions between steps (run, run_links, init): positions, links, a DeviceVar count
+    "upd_bg_heun": ("upd_bg_heun_3", 3, 0, 1, 0, 3, 0),
 }
 
 
@@ -167,6 +169,10 @@ def inputs(name):
         x = wl.ball(2000, 19)
         mn, mx = wl.bounds_for(x)
         steps, dt = 10, 0.05
+    elif name == "upd_bg_heun":
+        x = wl.ball(800, 23)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 3, 0.05
     elif name in ("drag_bg_heun", "drag_ba_euler_com"):
         x = wl.ball(1500, 21 if name == "drag_bg_heun" else 22)
         mn, mx = wl.bounds_for(x)
@@ -331,6 +337,9 @@ def run(name):
             pass
         elif scen.startswith("drag_"):
             res["ov"] = np.fromfile(f"{out}.ov", np.float32).reshape(-1, dims)
+        elif scen.startswith("upd_"):
+            res["links"] = np.fromfile(f"{out}.links", np.uint32).reshape(-1, 2)
+            res["hits"] = np.fromfile(f"{out}.hits", np.int32)
         else:
             res["pairs"] = np.fromfile(f"{out}.pairs", np.uint32).reshape(-1, 2)
             res["dpos"] = np.fromfile(f"{out}.dpos", np.float32).reshape(-1, dims)

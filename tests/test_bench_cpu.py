@@ -62,10 +62,10 @@ def test_clock_summary_without_samples():
 
 def test_pass_figures_come_from_the_committed_captures():
     assert bench.pass_profile("spheroid", "pass_dram_bytes_per_cell") == pytest.approx(21.78)
-    assert bench.pass_profile("spheroid", "pass_warp_inst_per_cell") == pytest.approx(156.46)
-    assert bench.pass_profile("sheet", "pass_warp_inst_per_cell") == pytest.approx(220.4)
+    assert bench.pass_profile("spheroid", "pass_warp_inst_per_cell") == pytest.approx(140.96)
+    assert bench.pass_profile("sheet", "pass_warp_inst_per_cell") == pytest.approx(289.0)
     assert bench.pass_profile("small", "pass_warp_inst_per_cell") is None
-    assert bench.traffic_per_pass("sheet") == pytest.approx(71.7)
+    assert bench.traffic_per_pass("sheet") == pytest.approx(71.6)
 
 
 def test_fcfs_latency_model_fits_and_queues():

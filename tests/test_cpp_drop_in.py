@@ -266,3 +266,15 @@ def test_drop_in_program_writes_the_reference_xdmf(driver, tmp_path, name):
     np.testing.assert_array_equal(f.read("static/cell_type").reshape(-1), np.arange(len(g["x0"])) % 3)
     if len(g["links"]):
         np.testing.assert_array_equal(f.read(f"t{steps}/links"), g["links"])
+
+
+@pytest.mark.gpu
+def test_update_functions_between_steps_reproduce_reference(driver, tmp_path):
+    """Simulation::run with two UPDATE_FUNC functions (fused per cell on one generator), run_links
+    rewiring every link, an INIT_FUNC through init, then three Heun steps: positions, links and the
+    DeviceVar counter the functions add to, bit for bit against the reference's run."""
+    g, out, r = run_driver(driver, "upd_bg_heun", "upd_bg_heun", tmp_path)
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(np.fromfile(f"{out}.links", np.uint32).reshape(-1, 2), g["links"])
+    np.testing.assert_array_equal(np.fromfile(f"{out}.hits", np.int32), g["hits"])
+    np.testing.assert_array_equal(np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3), g["pos"])
