@@ -290,6 +290,8 @@ struct Link {
   static constexpr unsigned int dimensions = 2;
   unsigned int a = 0;
   unsigned int b = 0;
+  constexpr Link() = default;
+  TECS_HD constexpr Link(unsigned int a_, unsigned int b_) : a(a_), b(b_) {}
 };
 static_assert(sizeof(Link) == 8, "links upload as (a, b) pairs");
 

@@ -83,8 +83,8 @@ struct PassArgs {
   // naive Delaunay: how many times each directed pair is applied, row i at i * capacity
   const unsigned short* dmult;
   // links of each cell id, in link order: link_ent[link_off[id] .. link_off[id + 1])
-  // = (other cell id, 1 when this cell is the link's b end); slot_of maps an
-  // id to its slot in X (null when X is in id order)
+  // = (other cell id, (link index << 1) | 1 when this cell is the link's b
+  // end); slot_of maps an id to its slot in X (null when X is in id order)
   const unsigned* link_off;
   const uint2* link_ent;
   const unsigned* slot_of;
@@ -643,6 +643,7 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
 template <int D>
 __device__ __forceinline__ void add_link(const PassArgs& a, unsigned n, const float* xs, unsigned e, float* s) {
   const uint2 le = a.link_ent[e];
+  const bool b_end = (le.y & 1u) != 0u;
   float xo[3] = {0.f, 0.f, 0.f};
   if (le.x < n) {
     const float4 v = a.X[a.slot_of ? a.slot_of[le.x] : le.x];
@@ -650,30 +651,41 @@ __device__ __forceinline__ void add_link(const PassArgs& a, unsigned n, const fl
   }
   float disp[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-  for (int d = 0; d < D; ++d) disp[d] = le.y ? xs[d] - xo[d] : xo[d] - xs[d];
+  for (int d = 0; d < D; ++d) disp[d] = b_end ? xs[d] - xo[d] : xo[d] - xs[d];
   float d2 = disp[0] * disp[0] + disp[1] * disp[1];
   if (D >= 3) d2 = d2 + disp[2] * disp[2];
   const float dist = sqrtf(d2);
-  const float k = le.y ? -a.link_k : a.link_k;
+  const float k = b_end ? -a.link_k : a.link_k;
 #pragma unroll
   for (int d = 0; d < D; ++d) s[d] = s[d] + (0.0f + (k * disp[d]) / dist);
 }
 
+// The library's link law: the constant pull (add_link).  A user LINK_FORCE
+// law takes its place in the user-law pass (tecs/pairwise.cuh).
+struct BuiltinLinks {
+  template <int D>
+  __device__ __forceinline__ void add(const PassArgs& a, unsigned n, unsigned id, const float* xs, float2 ps,
+                                      unsigned e, float* s, float* sp) const {
+    add_link<D>(a, n, xs, e, s);
+  }
+};
+
 // The write of one active cell: links, then the mode's store or fused
 // integrator update, the next rebuild's bin count and division.  s receives
 // the cell's position delta (for the COM partials).
-template <int D>
+template <int D, class Links = BuiltinLinks>
 __device__ __forceinline__ void cell_commit(const GridP& g, const PassArgs& a, unsigned n, unsigned i,
                                             const float* xi, const float4& vi, const float2& pi, const Acc& acc,
-                                            float* s) {
+                                            float* s, const Links& links = Links{}) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
+  float sp[2] = {0.0f + acc.p[0], 0.0f + acc.p[1]};
   if (a.link_off) {
     const unsigned id = a.Bid ? a.Bid[i] : id_of(vi);
     const unsigned e1 = a.link_off[id + 1];
-    for (unsigned e = a.link_off[id]; e < e1; ++e) add_link<D>(a, n, xi, e, s);
+    for (unsigned e = a.link_off[id]; e < e1; ++e) links.template add<D>(a, n, id, xi, pi, e, s, sp);
   }
-  const float sp0 = 0.0f + acc.p[0], sp1 = 0.0f + acc.p[1];
+  const float sp0 = sp[0], sp1 = sp[1];
   if (a.mode == kStore) {
     a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
     if (a.dp_out) a.dp_out[i] = make_float2(sp0, sp1);
@@ -716,11 +728,12 @@ __device__ __forceinline__ void cell_commit(const GridP& g, const PassArgs& a, u
 
 // cell_commit for an active cell, then (every thread of the block) the COM
 // partials of kStore.
-template <int D>
+template <int D, class Links = BuiltinLinks>
 __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
-                                              const float* xi, const float4& vi, const float2& pi, const Acc& acc) {
+                                              const float* xi, const float4& vi, const float2& pi, const Acc& acc,
+                                              const Links& links = Links{}) {
   float s[3] = {0.f, 0.f, 0.f};
-  if (active) cell_commit<D>(g, a, n, i, xi, vi, pi, acc, s);
+  if (active) cell_commit<D>(g, a, n, i, xi, vi, pi, acc, s, links);
   if (a.mode == kStore && a.com_part)
     com_reduce_block(a, active ? com_fixed(s[0]) : 0ll, active ? com_fixed(s[1]) : 0ll,
                      active ? com_fixed(s[2]) : 0ll);
@@ -1025,7 +1038,9 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, Force
       for (int d = 0; d < D; ++d) acc.x[d] = acc.x[d] + dacc.v[d] / den;
     }
   }
-  pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+  // a LINK_FORCE law evaluates the cell's links in place of the built-in pull
+  if constexpr (Law::kLink) pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc, law);
+  else pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
 }
 
 // One force evaluation handed to a user law's launcher (tecs_sim_set_pair_law).

@@ -87,17 +87,18 @@ inline Bytes dataspace(std::uint64_t rows, std::uint64_t cols) {
   return msg(0x0001, b);
 }
 
-// float32 (IEEE little endian) or unsigned 32-bit integer
-inline Bytes datatype(bool is_float) {
+// float32 (IEEE little endian), or a 32-bit integer (signed or not)
+enum class Kind { u32, f32, i32 };
+inline Bytes datatype(Kind kind) {
   Bytes b;
-  if (is_float) {
+  if (kind == Kind::f32) {
     b = {0x11, 0x20, 0x1F, 0x00};
     put<std::uint32_t>(b, 4);
     put<std::uint16_t>(b, 0); put<std::uint16_t>(b, 32);
     put<std::uint8_t>(b, 23); put<std::uint8_t>(b, 8); put<std::uint8_t>(b, 0); put<std::uint8_t>(b, 23);
     put<std::uint32_t>(b, 127);
   } else {
-    b = {0x10, 0x00, 0x00, 0x00};
+    b = {0x10, static_cast<unsigned char>(kind == Kind::i32 ? 0x08 : 0x00), 0x00, 0x00};
     put<std::uint32_t>(b, 4);
     put<std::uint16_t>(b, 0); put<std::uint16_t>(b, 32);
   }
@@ -220,7 +221,7 @@ struct Dataset {
   std::string name;
   const void* data;
   std::uint64_t rows, cols;
-  bool is_float;
+  Kind kind;
 };
 
 // An append-only HDF5 file of groups of 2-D datasets.
@@ -261,7 +262,7 @@ class File {
       const std::uint64_t bytes = d.rows * d.cols * 4;
       const std::uint64_t data_addr = alloc(std::max<std::uint64_t>(bytes, 1));
       write_raw(data_addr, d.data, bytes);
-      const Bytes oh = object_header({dataspace(d.rows, d.cols), datatype(d.is_float), fill_value(),
+      const Bytes oh = object_header({dataspace(d.rows, d.cols), datatype(d.kind), fill_value(),
                                       layout_contiguous(bytes ? data_addr : kUndef, bytes)},
                                      216);
       const std::uint64_t oaddr = alloc(oh.size());
@@ -386,29 +387,35 @@ template <typename T>
 struct ViewShape;
 template <typename S, int D>
 struct ViewShape<VectorN<S, D>> {
-  static_assert(std::is_same_v<S, float> || std::is_same_v<S, unsigned>, "float32 or uint32 views");
+  static_assert(std::is_same_v<S, float> || std::is_same_v<S, unsigned> || std::is_same_v<S, int>,
+                "float32, uint32 or int32 views");
   static constexpr std::uint64_t cols = D;
-  static constexpr bool is_float = std::is_same_v<S, float>;
+  static constexpr Kind kind = std::is_same_v<S, float> ? Kind::f32 : std::is_same_v<S, int> ? Kind::i32 : Kind::u32;
 };
 template <typename S>
 struct ViewShape<Polarity_<S>> {
   static constexpr std::uint64_t cols = 2;
-  static constexpr bool is_float = true;
+  static constexpr Kind kind = Kind::f32;
 };
 template <>
 struct ViewShape<Link> {
   static constexpr std::uint64_t cols = 2;
-  static constexpr bool is_float = false;
+  static constexpr Kind kind = Kind::u32;
 };
 template <>
 struct ViewShape<float> {
   static constexpr std::uint64_t cols = 1;
-  static constexpr bool is_float = true;
+  static constexpr Kind kind = Kind::f32;
 };
 template <>
 struct ViewShape<unsigned> {
   static constexpr std::uint64_t cols = 1;
-  static constexpr bool is_float = false;
+  static constexpr Kind kind = Kind::u32;
+};
+template <>
+struct ViewShape<int> {
+  static constexpr std::uint64_t cols = 1;
+  static constexpr Kind kind = Kind::i32;
 };
 
 }  // namespace h5detail
@@ -527,7 +534,7 @@ class HDF5_Writer {
       std::decay_t<decltype(v)> h = v;
       h.sync_host();
       ds.push_back({v.label(), static_cast<const void*>(v.data()), v.get_active_count(), h5detail::ViewShape<T>::cols,
-                    h5detail::ViewShape<T>::is_float});
+                    h5detail::ViewShape<T>::kind});
     };
     (one(views), ...);
     file_->write_group(group, ds);

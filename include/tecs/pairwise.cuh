@@ -31,7 +31,10 @@
 //   ctx            ctx.<field>.self / .other / .delta for the config's fields
 // A GENERIC_FORCE law (per cell: is_full_step, i, rng, ctx.<field>.self /
 // .delta) runs in the same pass, added before the pair sums as the reference
-// orders it; it combines with a PAIRWISE_FORCE law or runs alone.
+// orders it; it combines with a PAIRWISE_FORCE law or runs alone.  A
+// LINK_FORCE law (per link: is_full_step, link, rng, ctx.<field>.a / .b /
+// .delta_a / .delta_b) takes the place of the built-in link pull: each cell
+// adds its ends' accumulators after its pair sums, in link order.
 // Finders: the non-symmetric all-pairs and Gabriel finders (naive and binned).
 #ifndef TECS_CXX_PAIRWISE_CUH
 #define TECS_CXX_PAIRWISE_CUH
@@ -55,12 +58,66 @@ namespace detail {
 // The laws in the form k_pass_law calls them: the values as the config's
 // types, the running sums as the deltas, the law, the sums back.  G: the
 // GENERIC_FORCE law or NoLaw; P: the PAIRWISE_FORCE law or NoLaw.
-template <typename Config, typename G, typename P>
+template <typename Config, typename G, typename P, typename L = NoLaw>
 struct PairLaw {
   static constexpr bool kGeneric = !std::is_same_v<G, NoLaw>;
   static constexpr bool kPairwise = !std::is_same_v<P, NoLaw>;
+  static constexpr bool kLink = !std::is_same_v<L, NoLaw>;
   G gen;
   P law;
+  L link;
+
+  // One of the cell's links (entry e of its link list) through the LINK_FORCE
+  // law: the reference calls the law once per link with zeroed accumulators
+  // for both ends and adds each end's accumulator to that end's delta, in
+  // link order (integrators/base.hpp:196-233).  Here each end evaluates the
+  // link and adds its own accumulator, so the law runs twice per link with
+  // the same inputs and the same generator draws (keyed by the link's index).
+  template <int D>
+  __device__ void add(const PassArgs& a, unsigned n, unsigned id, const float* xs, float2 ps, unsigned e, float* s,
+                      float* sp) const {
+    if constexpr (kLink) {
+      using Vector = VectorN<float, D>;
+      using Fields = typename Config::template ForceFields<LinkFieldRef>;
+      const uint2 le = a.link_ent[e];
+      const bool b_end = (le.y & 1u) != 0u;
+      // the other end's value: an id beyond the active cells reads an unused
+      // view slot's zero
+      float xo[3] = {0.f, 0.f, 0.f};
+      float2 po = make_float2(0.f, 0.f);
+      if (le.x < n) {
+        const unsigned so = a.slot_of ? a.slot_of[le.x] : le.x;
+        const float4 v = a.X[so];
+        xo[0] = v.x; xo[1] = v.y; xo[2] = v.z;
+        if (a.P) po = a.P[so];
+      }
+      Vector self, other, da, db;
+      for (int d = 0; d < D; ++d) {
+        self[d] = xs[d];
+        other[d] = xo[d];
+        da[d] = 0.f;
+        db[d] = 0.f;
+      }
+      const Link lk{b_end ? le.x : id, b_end ? id : le.x};
+      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 5u : 6u, le.y >> 1, 0u);
+      const Vector& va = b_end ? other : self;
+      const Vector& vb = b_end ? self : other;
+      if constexpr (Simulation<Config>::has_polarity) {
+        const Polarity_<float> pself(ps.x, ps.y), pother(po.x, po.y);
+        Polarity_<float> qa(0.f, 0.f), qb(0.f, 0.f);
+        const Fields ctx{{va, vb, da, db}, {b_end ? pother : pself, b_end ? pself : pother, qa, qb}};
+        link(a.full_step != 0, lk, rng, ctx);
+        const Polarity_<float>& q = b_end ? qb : qa;
+        sp[0] = sp[0] + q[0];
+        sp[1] = sp[1] + q[1];
+      } else {
+        const Fields ctx{{va, vb, da, db}};
+        link(a.full_step != 0, lk, rng, ctx);
+      }
+      const Vector& mine = b_end ? db : da;
+      for (int d = 0; d < D; ++d) s[d] = s[d] + mine[d];
+    }
+  }
 
   __device__ void generic(const PassArgs& a, unsigned idi, const float* xi, float2 pi, Acc& acc) const {
     if constexpr (kGeneric) {
@@ -154,18 +211,18 @@ int pair_law_launcher(void* user, const void* call, void* stream) {
       static_cast<const LawOnDevice<Config, Law>*>(user)->dev);
 }
 
-template <typename Config, typename G, typename P>
+template <typename Config, typename G, typename P, typename L>
 struct PairLawBinding {
-  using Law = PairLaw<Config, G, P>;
+  using Law = PairLaw<Config, G, P, L>;
   using Bound = LawOnDevice<Config, Law>;
   // The step's graph launches the pass with a pointer to the laws in device
   // memory, so laws of the same types rebind by copying their values there
   // on the simulation's stream (ordered before its next step) -- no new
   // graph.  Values that compare equal byte for byte are not copied again.
-  static void bind(tecs_sim* handle, int device, const G& g, const P& p, std::shared_ptr<void>& holder,
+  static void bind(tecs_sim* handle, int device, const G& g, const P& p, const L& l, std::shared_ptr<void>& holder,
                    tecs_pair_law_fn& bound) {
     const tecs_pair_law_fn fn = &pair_law_launcher<Config, Law>;
-    const Law law{g, p};
+    const Law law{g, p, l};
     Bound* b = (holder && bound == fn) ? static_cast<Bound*>(holder.get()) : nullptr;
     if (!b) {
       if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
@@ -222,5 +279,18 @@ struct PairLawBinding {
 #define GENERIC_FORCE_OP                     \
   using tag = tecs::detail::GenericForceTag; \
   __host__ __device__ void operator()(GENERIC_FORCE_PARAMETERS) const
+
+// per-link laws (utils.hpp:219-226): the link (a, b) and ctx.<field>.a / .b /
+// .delta_a / .delta_b
+#define LINK_FORCE_PARAMETERS                                                                        \
+  [[maybe_unused]] const bool is_full_step, [[maybe_unused]] const tecs::Link &link,                 \
+      [[maybe_unused]] Random &rng, [[maybe_unused]] const LinkForceFields &ctx
+#define LINK_FORCE(...)                                                                                \
+  [&]() {                                                                                              \
+    return tecs::detail::link_force | [=] __host__ __device__(LINK_FORCE_PARAMETERS) { __VA_ARGS__ }; \
+  }
+#define LINK_FORCE_OP                     \
+  using tag = tecs::detail::LinkForceTag; \
+  __host__ __device__ void operator()(LINK_FORCE_PARAMETERS) const
 
 #endif  // TECS_CXX_PAIRWISE_CUH

@@ -55,6 +55,7 @@ namespace detail {
 struct PairwiseForceTag {};
 struct GenericForceTag {};
 struct UpdateFuncTag {};
+struct LinkForceTag {};
 
 // PAIRWISE_FORCE's, GENERIC_FORCE's and UPDATE_FUNC's values: the lambda with
 // its tag (utils.hpp:181-184)
@@ -77,6 +78,7 @@ struct TaggedForceMaker {
 inline constexpr TaggedForceMaker<PairwiseForceTag> pairwise_force{};
 inline constexpr TaggedForceMaker<GenericForceTag> generic_force{};
 inline constexpr TaggedForceMaker<UpdateFuncTag> update_func{};
+inline constexpr TaggedForceMaker<LinkForceTag> link_force{};
 template <typename F, typename Tag>
 concept TaggedLaw = requires { typename F::tag; } && std::is_same_v<typename F::tag, Tag>;
 template <typename F>
@@ -86,9 +88,11 @@ concept UserGenericLaw = TaggedLaw<F, GenericForceTag>;
 template <typename F>
 concept UserUpdateFunc = TaggedLaw<F, UpdateFuncTag>;
 template <typename F>
+concept UserLinkLaw = TaggedLaw<F, LinkForceTag>;
+template <typename F>
 constexpr bool is_link_law() {
   if constexpr (requires { F::is_link; }) return F::is_link;
-  else return false;
+  else return UserLinkLaw<F>;
 }
 // no law of that kind in the step
 struct NoLaw {};
@@ -107,7 +111,7 @@ decltype(auto) resolve_force(const F& f) {
 }
 // Hands a step's user laws (generic G, pairwise P; NoLaw where absent) to a
 // simulation's library handle; defined by tecs/pairwise.cuh.
-template <typename Config, typename G, typename P>
+template <typename Config, typename G, typename P, typename L>
 struct PairLawBinding;
 }  // namespace detail
 
@@ -202,6 +206,7 @@ class Simulation {
     d.seed = s.seed;
     d.device = s.device;
     check(tecs_sim_create(&d, &handle_));
+    desc_ = d;
     positions_ = View<Vector>("position", s.agent_count, s.capacity);
     if constexpr (has_polarity) polarity_ = View<Polarity>("polarity", s.agent_count, s.capacity);
     links_ = View<Link>("links", s.link_active_count, s.link_capacity);
@@ -241,7 +246,8 @@ class Simulation {
     return links_;
   }
   const View<Link>& get_links() const { return links_; }
-  unsigned get_link_count() const { return links_.get_active_count(); }
+  // the links view's capacity, as the reference's (simulation.hpp:330-333)
+  unsigned get_link_count() const { return static_cast<unsigned>(links_.extent(0)); }
 
   // The integrator's old velocities (include/simulation.hpp:312-314,
   // integrators/base.hpp:74): each step's velocity per cell, which user
@@ -271,6 +277,52 @@ class Simulation {
   }
   // Simulation::set_agent_count (include/simulation.hpp:295-302): the next
   // step starts from the first n cells and resets the finder's counter
+  // A new capacity (include/simulation.hpp:266-281): the field views, the
+  // library's state and the integrator's old velocities keep their first
+  // values; extra views passed along are resized too.  The library's
+  // simulation is made anew at the new size and the state sent to it, so user
+  // laws bind again at the next step.
+  void set_capacity(unsigned value) {
+    if (value < agent_count) throw Error("capacity below the agent count");
+    sync_to_library();
+    refresh_host();
+    std::vector<float> ov;
+    if (old_velocities_kept_ && agent_count) {
+      ov.resize(std::size_t(agent_count) * dimensions);
+      unsigned n = 0;
+      check(tecs_sim_old_velocities(handle_, ov.data(), &n));
+    }
+    tecs_sim_desc d = desc_;
+    d.capacity = value;
+    tecs_sim* next = nullptr;
+    check(tecs_sim_create(&d, &next));
+    check(tecs_sim_set_pair_law(handle_, nullptr, nullptr));
+    tecs_sim_destroy(handle_);
+    handle_ = next;
+    desc_ = d;
+    law_holder_.reset();
+    law_fn_ = nullptr;
+    links_on_device_ = 0;
+    links_dirty_ = true;
+    capacity = value;
+    positions_.resize(value);
+    if constexpr (has_polarity) polarity_.resize(value);
+    set_count(agent_count);
+    positions_.set_host_modified(true);
+    lib_newer_dev_ = lib_newer_host_ = false;
+    if (old_velocities_kept_) {
+      old_velocities_kept_ = false;
+      keep_old_velocities();
+      if (!ov.empty()) check(tecs_sim_set_old_velocities(handle_, ov.data(), agent_count));
+    }
+  }
+  template <typename V0, typename... Vs>
+  void set_capacity(unsigned value, V0& view0, Vs&... views) {
+    set_capacity(value);
+    view0.resize(value);
+    (views.resize(value), ...);
+  }
+
   void set_agent_count(unsigned n) {
     if (n > capacity) throw Error("agent count exceeds capacity");
     refresh_host();
@@ -278,6 +330,13 @@ class Simulation {
     positions_.set_active_count(n);
     if constexpr (has_polarity) polarity_.set_active_count(n);
     positions_.set_host_modified(true);
+  }
+  // the same, and the active count of extra views (simulation.hpp:305-309)
+  template <typename V0, typename... Vs>
+  void set_agent_count(unsigned n, V0& view0, Vs&... views) {
+    set_agent_count(n);
+    view0.set_active_count(n);
+    (views.set_active_count(n), ...);
   }
 
   // -- stepping ---------------------------------------------------------------
@@ -371,6 +430,114 @@ class Simulation {
     }
   }
 
+  // agents on a line: every component of cell i at i * distance (initializers/line.hpp)
+  template <typename... InitFuncs>
+  void init_line(Scalar distance, InitFuncs&&... init_functions) {
+    init([&](unsigned i, Random&) { positions_(i) = Vector(Scalar(i) * distance); },
+         static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // uniform in [min, max) per component (initializers/cuboid.hpp:19-44)
+  template <typename... InitFuncs>
+  void init_random_cuboid(const Vector& min, const Vector& max, InitFuncs&&... init_functions) {
+    const Vector extent = max - min;
+    init(
+        [&](unsigned i, Random& g) {
+          for (int d = 0; d < dimensions; ++d) positions_(i)[d] = min[d] + g.drand(0.0, extent[d]);
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // a random cuboid relaxed by `steps` steps (default 2000), then the init
+  // functions (initializers/cuboid.hpp:50-85, simulation.hpp:452-506)
+  template <typename... Args>
+  void init_relaxed_cuboid(const Vector& min, const Vector& max, Args&&... args) {
+    if constexpr (sizeof...(Args) > 0 && (std::is_integral_v<std::decay_t<Args>> || ...)) {
+      init_relaxed_cuboid_n(min, max, static_cast<Args&&>(args)...);
+    } else {
+      init_relaxed_cuboid_n(min, max, 2000u, static_cast<Args&&>(args)...);
+    }
+  }
+  // rings of a hexagonal lattice around cell 0 (initializers/hexagon.hpp:21-64):
+  // cell i > 0 on ring k, side s, step t, linearly between the ring's corners
+  template <typename... InitFuncs>
+  void init_regular_hexagon(Scalar distance_to_neighbour, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 2, "a hexagon needs 2 dimensions");
+    init(
+        [&](unsigned i, Random&) {
+          if (i == 0) return;
+          unsigned remaining = i - 1, ring = 1;
+          while (remaining >= 6 * ring) {
+            remaining -= 6 * ring;
+            ++ring;
+          }
+          const Scalar beta = Scalar(Kokkos::numbers::pi_v<Scalar>) / Scalar(3);
+          const unsigned side = remaining / ring, step = remaining % ring;
+          const Scalar radius = distance_to_neighbour * Scalar(ring);
+          const Scalar t = Scalar(step) / Scalar(ring);
+          const Scalar s0 = -radius * Kokkos::sin(beta * Scalar(side));
+          const Scalar c0 = radius * Kokkos::cos(beta * Scalar(side));
+          const Scalar s1 = -radius * Kokkos::sin(beta * Scalar(side + 1));
+          const Scalar c1 = radius * Kokkos::cos(beta * Scalar(side + 1));
+          Vector p{Scalar(0)};
+          p[0] = s0 + (s1 - s0) * t;
+          p[1] = c0 + (c1 - c0) * t;
+          positions_(i) = p;
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // rows of nx cells, every other row shifted by half a spacing
+  // (initializers/rectangle.hpp:21-50)
+  template <typename... InitFuncs>
+  void init_regular_rectangle(Scalar distance_to_neighbour, unsigned nx, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 2, "a rectangle needs 2 dimensions");
+    init(
+        [&](unsigned i, Random&) {
+          const unsigned row = i / nx, col = i % nx;
+          const Scalar row_height = distance_to_neighbour * Scalar(0.5) * Kokkos::sqrt(Scalar(3.0));
+          const Scalar row_offset = (row % 2 != 0) ? (distance_to_neighbour * Scalar(0.5)) : Scalar(0.0);
+          positions_(i)[0] = row_offset + Scalar(col) * distance_to_neighbour;
+          positions_(i)[1] = Scalar(row) * row_height;
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // uniform in a disk of radius sqrt(capacity) * spacing / 2
+  // (initializers/disk.hpp:20-41: the view's extent is its capacity)
+  template <typename... InitFuncs>
+  void init_random_disk(Scalar distance_to_neighbour, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 2, "a disk needs 2 dimensions");
+    const Scalar r_max = Kokkos::sqrt(static_cast<Scalar>(positions_.extent(0))) * distance_to_neighbour / Scalar(2.0);
+    init(
+        [&](unsigned i, Random& g) {
+          const Scalar r = r_max * Kokkos::sqrt(static_cast<Scalar>(g.drand()));
+          const Scalar phi = static_cast<Scalar>(g.drand()) * Scalar(2.0) * Kokkos::numbers::pi_v<Scalar>;
+          positions_(i)[0] = r * Kokkos::sin(phi);
+          positions_(i)[1] = r * Kokkos::cos(phi);
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // rejection sampling of the heart surface's inside in [-2, 2)^3, scaled
+  // (initializers/heart.hpp:22-55)
+  template <typename... InitFuncs>
+  void init_random_heart(Scalar scale, InitFuncs&&... init_functions) {
+    static_assert(dimensions >= 3, "a heart needs 3 dimensions");
+    auto outside = [](Scalar x, Scalar y, Scalar z) {
+      return Kokkos::pow(x * x + 9.0 / 4.0 * y * y + z * z - 1.0, 3) - x * x * z * z * z -
+             9.0 / 80.0 * y * y * z * z * z;
+    };
+    init(
+        [&](unsigned i, Random& g) {
+          Scalar x, y, z;
+          do {
+            x = static_cast<Scalar>(g.drand(-2.0, 2.0));
+            y = static_cast<Scalar>(g.drand(-2.0, 2.0));
+            z = static_cast<Scalar>(g.drand(-2.0, 2.0));
+          } while (outside(x, y, z) > Scalar(0.0));
+          positions_(i)[0] = x * scale;
+          positions_(i)[1] = y * scale;
+          positions_(i)[2] = z * scale;
+        },
+        static_cast<InitFuncs&&>(init_functions)...);
+  }
+
   // init(f, fs...) (simulation.hpp:519-537): f(i, rng) for every agent in
   // cell order, then the next function
   template <typename Initializer, typename... InitFuncs>
@@ -458,9 +625,20 @@ class Simulation {
   template <typename... InitFuncs>
   void init_relaxed_sphere_n(Scalar radius, unsigned steps, InitFuncs&&... init_functions) {
     init_random_filled_sphere(radius);
-    for (unsigned k = 0; k < steps; ++k)
-      take_step(0.1, forces::Spring2R{2.0f, 0.8f, 1.0f, 0.8f});
+    relax(steps);
     if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
+  }
+  template <typename... InitFuncs>
+  void init_relaxed_cuboid_n(const Vector& min, const Vector& max, unsigned steps, InitFuncs&&... init_functions) {
+    init_random_cuboid(min, max);
+    relax(steps);
+    if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
+  }
+  // `steps` steps of dt 0.1 with the piecewise-linear law at distance 0.8,
+  // repulsion 2, adhesion 1 (initializers/relax_force.hpp:17-30: the
+  // built-in two-radius spring of the same arithmetic)
+  void relax(unsigned steps) {
+    for (unsigned k = 0; k < steps; ++k) take_step(0.1, forces::Spring2R{2.0f, 0.8f, 1.0f, 0.8f});
   }
 
   template <typename... Forces>
@@ -471,7 +649,8 @@ class Simulation {
     static_assert((0 + ... + (detail::UserGenericLaw<Forces> ? 1 : 0)) <= 1, "one generic law per step");
     static_assert(!(false || ... || detail::UserUpdateFunc<Forces>),
                   "UPDATE_FUNC functions run through Simulation::init, not take_step");
-    constexpr bool user = (false || ... || (detail::UserGenericLaw<Forces> || detail::UserPairLaw<Forces>));
+    constexpr bool user = (false || ... ||
+                           (detail::UserGenericLaw<Forces> || detail::UserPairLaw<Forces> || detail::UserLinkLaw<Forces>));
     apply_pair_law(forces...);
     apply_link_law(forces...);
     sync_to_library();
@@ -504,22 +683,25 @@ class Simulation {
   struct IsGeneric : std::bool_constant<detail::UserGenericLaw<F>> {};
   template <typename F>
   struct IsUserPair : std::bool_constant<detail::UserPairLaw<F>> {};
+  template <typename F>
+  struct IsUserLink : std::bool_constant<detail::UserLinkLaw<F>> {};
 
   // the pairwise law of this step (none: pairs only, no deltas); user laws
-  // (a PAIRWISE_FORCE law, a GENERIC_FORCE law, or both) replace the built-in
-  // one until a step passes a built-in law again
+  // (a PAIRWISE_FORCE, a GENERIC_FORCE and a LINK_FORCE law, any of them)
+  // replace the built-in one until a step passes a built-in law again
   template <typename... Forces>
   void apply_pair_law(const Forces&... forces) {
     int id = TECS_FORCE_NONE;
     float k[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     constexpr bool generic = (false || ... || detail::UserGenericLaw<Forces>);
     constexpr bool user_pair = (false || ... || detail::UserPairLaw<Forces>);
-    constexpr bool user = generic || user_pair;
+    constexpr bool user_link = (false || ... || detail::UserLinkLaw<Forces>);
+    constexpr bool user = generic || user_pair || user_link;
     auto one = [&](const auto& f) {
       using F = std::decay_t<decltype(f)>;
       if constexpr (!detail::UserPairLaw<F> && !detail::UserGenericLaw<F> && !detail::is_link_law<F>()) {
         static_assert(!user || sizeof(F) == 0,
-                      "a GENERIC_FORCE law combines with a PAIRWISE_FORCE law, not a built-in one");
+                      "GENERIC_FORCE and LINK_FORCE laws combine with a PAIRWISE_FORCE law, not a built-in one");
         static_assert(!F::needs_polarity || has_polarity, "this force needs a (Polarity, polarity) field");
         id = F::force_id;
         k[0] = f.k_rep; k[1] = f.r_rep; k[2] = f.k_adh; k[3] = f.r_adh; k[4] = f.k_pol_value();
@@ -531,8 +713,10 @@ class Simulation {
     if constexpr (user) {
       const auto& g = first_of<IsGeneric>(forces...);
       const auto& p = first_of<IsUserPair>(forces...);
-      detail::PairLawBinding<Config, std::decay_t<decltype(g)>, std::decay_t<decltype(p)>>::bind(
-          handle_, settings_.device, g, p, law_holder_, law_fn_);
+      const auto& l = first_of<IsUserLink>(forces...);
+      detail::PairLawBinding<Config, std::decay_t<decltype(g)>, std::decay_t<decltype(p)>,
+                             std::decay_t<decltype(l)>>::bind(handle_, settings_.device, g, p, l, law_holder_,
+                                                              law_fn_);
     }
     if (!user && law_fn_) {
       check(tecs_sim_set_pair_law(handle_, nullptr, nullptr));
@@ -542,22 +726,26 @@ class Simulation {
     check(tecs_sim_set_force(handle_, id, k[0], k[1], k[2], k[3], k[4]));
   }
 
-  // the link law of this step: links act only in steps that pass one
+  // the link law of this step: links act only in steps that pass one.  The
+  // reference evaluates every link of the view's capacity
+  // (integrators/base.hpp:196-233, links.extent(0)); unused slots hold
+  // (0, 0), which it skips as a self link.
   template <typename... Forces>
   void apply_link_law(const Forces&... forces) {
     bool has = false;
     float strength = 0.f;
     auto one = [&](const auto& f) {
       using F = std::decay_t<decltype(f)>;
-      if constexpr (detail::is_link_law<F>()) {
+      if constexpr (detail::UserLinkLaw<F>) {
+        has = true;
+      } else if constexpr (detail::is_link_law<F>()) {
         has = true;
         strength = f.strength;
       }
     };
     (one(forces), ...);
-    const unsigned want = has ? links_.get_active_count() : 0u;
+    const unsigned want = has ? static_cast<unsigned>(links_.extent(0)) : 0u;
     if (!links_dirty_ && want == links_on_device_ && (!has || strength == link_strength_)) return;
-    if (want > links_.extent(0)) throw Error("link active count exceeds link_capacity");
     if (want) links_.sync_host();  // links written by device code
     check(tecs_sim_set_links(handle_, want ? reinterpret_cast<const uint32_t*>(links_.data()) : nullptr, want,
                              strength));
@@ -678,6 +866,7 @@ class Simulation {
   bool lib_newer_host_ = false;     // ... than their host arrays
   bool user_code_ran_ = false;      // user code ran on the device since the views were last checked
   bool old_velocities_kept_ = false;
+  tecs_sim_desc desc_{};
 
   void keep_old_velocities() {
     if (old_velocities_kept_) return;

@@ -119,6 +119,12 @@ struct VectorN {
   }
   TECS_HD Scalar distance_to(const VectorN& o) const { return detail::sqrt_(distance_to_squared(o)); }
   TECS_HD VectorN normalized() const { return *this / length(); }
+  // Gram-Schmidt against a unit vector u: (v - (v.u) u) / |v - (v.u) u|
+  // (vector.hpp:385-400)
+  TECS_HD VectorN orthonormal(const VectorN& u) const {
+    const VectorN normal = *this - dot(u) * u;
+    return normal / detail::sqrt_(normal.dot(normal));
+  }
   TECS_HD constexpr VectorN cross(const VectorN& o) const requires(dimensions == 3) {
     return VectorN(data_[1] * o.data_[2] - data_[2] * o.data_[1], data_[2] * o.data_[0] - data_[0] * o.data_[2],
                    data_[0] * o.data_[1] - data_[1] * o.data_[0]);
@@ -201,6 +207,47 @@ struct Polarity_ : VectorN<Scalar, 2> {
     return BendingForceResult{-prod_i / distance * this_vector + ci * displacement + -prod_j / distance * other_vector +
                                   cj * displacement,
                               Polarity_(-prod_i * unidirectional_polarization_force(Polarity_(displacement, distance)))};
+  }
+  // Bending towards a preferred angle between the polarity and the
+  // displacement (polarity.hpp:212-229): bending_force with cos(angle) added
+  // to this cell's projection and taken from the neighbour's.
+  TECS_HD BendingForceResult apical_constriction_force(const Vector3<Scalar>& displacement, const Scalar distance,
+                                                       const Polarity_& other_polarity,
+                                                       const Scalar preferred_angle) const {
+    const Vector3<Scalar> this_vector = to_vector3();
+    const Scalar prod_i = this_vector.dot(displacement) / distance + std::cos(preferred_angle);
+    const Vector3<Scalar> other_vector = to_vector3(other_polarity);
+    const Scalar prod_j = other_vector.dot(displacement) / distance - std::cos(preferred_angle);
+    const double d2 = double(distance) * double(distance);
+    const Scalar ci = Scalar(double(prod_i) * double(prod_i) / d2);
+    const Scalar cj = Scalar(double(prod_j) * double(prod_j) / d2);
+    return BendingForceResult{-prod_i / distance * this_vector + ci * displacement + -prod_j / distance * other_vector +
+                                  cj * displacement,
+                              Polarity_(-prod_i * unidirectional_polarization_force(Polarity_(displacement, distance)))};
+  }
+  // Migration along polarities (polarity.hpp:244-274): pulled around a
+  // neighbour that lies behind this polarity (alignment with the
+  // displacement <= -0.15), pushed by a neighbour whose polarity points at
+  // this cell (>= 0.15); each term 0.6 along the polarity plus 0.8 across it.
+  TECS_HD Vector3<Scalar> migration_force(const Vector3<Scalar>& displacement, const Polarity_& other_polarity,
+                                          const Scalar distance) const {
+    Vector3<Scalar> result{};
+    const Polarity_ displacement_polarity = from_vector3(displacement, distance);
+    if (this->data_[0] != 0 || this->data_[1] != 0) {
+      if (double(dot(displacement_polarity)) <= -0.15) {
+        const Vector3<Scalar> this_vector = to_vector3();
+        const Vector3<Scalar> this_vector_t = displacement.orthonormal(this_vector);
+        result = Scalar(0.6) * this_vector + Scalar(0.8) * this_vector_t;
+      }
+    }
+    if (other_polarity[0] > detail::epsilon_<Scalar>() || other_polarity[1] > detail::epsilon_<Scalar>()) {
+      if (double(other_polarity.dot(displacement_polarity)) >= 0.15) {
+        const Vector3<Scalar> other_vector = to_vector3(other_polarity);
+        const Vector3<Scalar> other_vector_t = (-displacement).orthonormal(other_vector);
+        result -= Scalar(0.6) * other_vector + Scalar(0.8) * other_vector_t;
+      }
+    }
+    return result;
   }
 };
 

@@ -1076,6 +1076,7 @@ int tecs_sim_set_pair_law(tecs_sim* s, tecs_pair_law_fn fn, void* user) {
 int tecs_sim_set_links(tecs_sim* s, const uint32_t* links, unsigned n_links, float strength) {
   if (!s || (n_links && !links)) return fail("null argument");
   if (n_links && s->d.symmetric) return fail("links are served with the non-symmetric finders");
+  if (n_links >= (1u << 31)) return fail("too many links");
   const unsigned cap = s->d.capacity;
   for (size_t l = 0; l < 2 * (size_t)n_links; ++l)
     if (links[l] >= cap) return fail("link endpoint beyond capacity");
@@ -1096,8 +1097,8 @@ int tecs_sim_set_links(tecs_sim* s, const uint32_t* links, unsigned n_links, flo
   for (unsigned l = 0; l < n_links; ++l) {
     const unsigned a = links[2 * l], b = links[2 * l + 1];
     if (a == b) continue;
-    ent[fill[a]++] = make_uint2(b, 0u);
-    ent[fill[b]++] = make_uint2(a, 1u);
+    ent[fill[a]++] = make_uint2(b, l << 1);
+    ent[fill[b]++] = make_uint2(a, (l << 1) | 1u);
   }
   for (void* p : {(void*)s->link_off, (void*)s->link_ent, (void*)s->slot_of})
     if (p) CK(cudaFree(p));

@@ -241,6 +241,33 @@ static int run_links(const Input& in, const std::string& out, int steps, double 
   return 0;
 }
 
+// the same run with the link law written as a LINK_FORCE lambda, as the
+// reference's protrusion programs write it (examples/intercalation.cpp:65-71)
+template <typename Config>
+static int run_link_lambda(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(Config)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const Scalar k_link = in.prm[15];
+  auto spring = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+  );
+  auto protrusions = LINK_FORCE(
+    Vector displacement = ctx.position.b - ctx.position.a;
+    Scalar distance = displacement.length();
+    ctx.position.delta_a += k_link * displacement / distance;
+    ctx.position.delta_b += -k_link * displacement / distance;
+  );
+  Simulation<Config> sim(settings_of<Config>(in));
+  fill(sim, in);
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, protrusions(), spring());
+  const auto& x = sim.get_positions_view();
+  write_raw(out + ".pos", x.data(), std::size_t(sim.get_agent_count()) * sizeof(Vector));
+  return 0;
+}
+
 // a law that draws from rng: two simulations of the same input give the same run
 static int run_rng_twice(const Input& in, const std::string& out, int steps, double dt) {
   EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
@@ -288,7 +315,7 @@ static int run_drag(const Input& in, const std::string& out, int steps, double d
 int main(int argc, char** argv) {
   if (argc < 6) return 2;
   const std::string scenario = argv[1];
-  const bool links = scenario.rfind("lk_", 0) == 0;
+  const bool links = scenario.rfind("lk_", 0) == 0;  // lk_* scenarios read links
   const Input in = read_input(argv[2], links);
   const std::string out = argv[3];
   const int steps = std::atoi(argv[4]);
@@ -304,6 +331,8 @@ int main(int argc, char** argv) {
     if (scenario == "bg_heun_pol") return run_polarity(in, out, steps, dt);
     if (scenario == "gen_bg_heun") return run_generic(in, out, steps, dt);
     if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);
+    if (scenario == "lk_lambda_bg_heun") return run_link_lambda<BinnedGabrielHeun>(in, out, steps, dt);
+    if (scenario == "lk_lambda_ba_euler_com") return run_link_lambda<BinnedAllPairsEulerCom>(in, out, steps, dt);
     if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
     if (scenario == "drag_bg_heun") return run_drag<BinnedGabrielHeun>(in, out, steps, dt);
     if (scenario == "drag_ba_euler_com") return run_drag<BinnedAllPairsEulerCom>(in, out, steps, dt);

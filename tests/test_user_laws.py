@@ -137,6 +137,22 @@ def test_user_law_with_links_reproduces_reference(driver, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scenario,name,exact", [("lk_lambda_bg_heun", "lk_bg_heun", True),
+                                                 ("lk_lambda_ba_euler_com", "lk_ba_euler_com", False)])
+def test_link_force_lambda_reproduces_reference(driver, tmp_path, scenario, name, exact):
+    """take_step(dt, LINK_FORCE(...)(), PAIRWISE_FORCE(...)()): the protrusion law written as the reference's
+    programs write it, evaluated per link end after the pair sums in link order; bit for bit against the
+    reference's link runs (within the COM tolerance with the COM fix)."""
+    g, out, r = run(driver, scenario, name, tmp_path)
+    assert r.returncode == 0, r.stderr
+    pos = np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3)
+    if exact:
+        np.testing.assert_array_equal(pos, g["pos"])
+    else:
+        assert close(pos, g["pos"])
+
+
+@pytest.mark.gpu
 def test_generic_law_with_pairwise_law_reproduces_reference(driver, tmp_path):
     """take_step(dt, PAIRWISE_FORCE(...)(), GENERIC_FORCE(...)()): the generic law (is_full_step-dependent,
     reading ctx.position.self) is added before the pair sums, as the reference fuses them; bit for bit."""
