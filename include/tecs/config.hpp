@@ -14,6 +14,8 @@
 
 #include <cstddef>
 #include <string_view>
+#include <tuple>
+#include <type_traits>
 
 #include "components.hpp"
 #include "hdf5_writer.hpp"
@@ -69,6 +71,68 @@ struct LinkFieldRef {
   const T& b;
   T& delta_a;
   T& delta_b;
+};
+
+// How the library holds a config's fields: the first field is the position
+// (a Vector); a (Polarity, polarity) field is the library's polarity (the
+// built-in polarity law reads it); every other field is an extra field, its
+// float components packed one after another (Scalar 1, Polarity 2, Vector D)
+// into the cell's extra block.  role: 0 position, 1 polarity, 2 extra.
+template <typename T>
+struct FieldWidth;
+template <typename S, int D>
+struct FieldWidth<VectorN<S, D>> {
+  static constexpr unsigned value = D;
+  static constexpr bool scalar = false;
+};
+template <typename S>
+struct FieldWidth<Polarity_<S>> {
+  static constexpr unsigned value = 2;
+  static constexpr bool scalar = false;
+};
+template <>
+struct FieldWidth<float> {
+  static constexpr unsigned value = 1;
+  static constexpr bool scalar = true;  // updated in double by the reference's integrators
+};
+
+template <typename List>
+struct FieldLayout;
+template <typename... Fs>
+struct FieldLayout<FieldList<Fs...>> {
+  static constexpr std::size_t n = sizeof...(Fs);
+  template <std::size_t I>
+  using type = typename std::tuple_element_t<I, std::tuple<Fs...>>::value_type;
+
+ private:
+  static constexpr bool is_pol[n] = {(std::is_same_v<typename Fs::value_type, Polarity_<float>> &&
+                                      Fs::name == "polarity")...};
+  static constexpr unsigned width[n] = {FieldWidth<typename Fs::value_type>::value...};
+  static constexpr bool scalar[n] = {FieldWidth<typename Fs::value_type>::scalar...};
+  TECS_HD static constexpr std::size_t first_polarity() {
+    for (std::size_t k = 1; k < n; ++k)
+      if (is_pol[k]) return k;
+    return n;
+  }
+
+ public:
+  static constexpr std::size_t polarity_index = first_polarity();  // n: none
+  static constexpr bool has_polarity = polarity_index < n;
+  TECS_HD static constexpr int role(std::size_t k) { return k == 0 ? 0 : k == polarity_index ? 1 : 2; }
+  // the field's first component in the extra block (extra fields only)
+  TECS_HD static constexpr unsigned offset(std::size_t k) {
+    unsigned o = 0;
+    for (std::size_t q = 0; q < k; ++q)
+      if (role(q) == 2) o += width[q];
+    return o;
+  }
+  static constexpr unsigned extra = offset(n);
+  TECS_HD static constexpr unsigned double_mask() {
+    unsigned m = 0;
+    for (std::size_t q = 0; q < n; ++q)
+      if (role(q) == 2 && scalar[q]) m |= 1u << offset(q);
+    return m;
+  }
 };
 
 // bind a finder template to the config's position view, scalar and dimensions

@@ -96,13 +96,37 @@ struct PassArgs {
   // read them (binned_gabriel.hpp:225-226, 356-357), and k_finish writes the
   // step's velocity there (euler.hpp:59, heun.hpp:87)
   float4* old_vel;
+  // extra fields: E float components per cell beyond position and polarity
+  // (the config's other fields), stored component-major (component k of
+  // slot s at k * capacity + s).  Bit k of ex_dbl: component k belongs to a
+  // Scalar field, which the reference's integrators update in double
+  // (float += delta * double dt); Vector and Polarity components update in
+  // float (VectorN * Scalar).
+  unsigned E;
+  unsigned ex_dbl;
+  const float* EX;   // extras read by the pass (EB or Et)
+  const float* EBx;  // x_n extras (sorted) for the fused updates
+  float* ed_out;     // extra deltas written (kStore, kHeun1Fused)
+  const float* ed1;  // pass-1 extra deltas (Heun pass 2, k_finish)
+  const float* ed2;  // pass-2 extra deltas (k_finish)
+  float* EA;         // extras of the next state
+  float* Et;         // extras of the predictor
+  double dt64;       // the step's dt as the caller gave it
 };
 
-// The drag sums of one cell: sum of the pairs' drag and of drag * the other
-// cell's old velocity, in pair order (binned_gabriel.hpp:105-106, 225-226)
-struct DragAcc {
+// at most this many extra components per cell
+constexpr unsigned kMaxExtra = 8;
+
+// What the user-law pass keeps per cell besides the position and polarity
+// sums: the drag sums (the pairs' drag and drag * the other cell's old
+// velocity, in pair order, binned_gabriel.hpp:105-106, 225-226) and the NE
+// extra components' values and delta sums.
+template <unsigned NE>
+struct LawCell {
   float drag;
   float v[3];
+  float ex_self[NE > 0 ? NE : 1];
+  float ex_delta[NE > 0 ? NE : 1];
 };
 
 // ---------------------------------------------------------------------------
@@ -268,11 +292,19 @@ __device__ __forceinline__ unsigned id_at(const float4* X, const unsigned* Bid, 
 // lo + (number of cells of its bin with a smaller id), so every bin lists its
 // cells in ascending id -- the order of Kokkos BinSort's binning loop on the
 // Serial backend.  Single-cell bins (most of them) copy straight through.
+// the extra fields moved along with a state copy
+struct ExtraMove {
+  unsigned E;
+  size_t C;  // capacity (component stride)
+  const float* EA;
+  float* EB;
+};
+
 static __global__ void k_order_gather(const Counters* __restrict__ ctr, const unsigned* __restrict__ key,
                                       const unsigned* __restrict__ off, const unsigned* __restrict__ src,
                                       const float4* __restrict__ A, const float2* __restrict__ PA,
                                       float4* __restrict__ B, float2* __restrict__ PB, unsigned* __restrict__ Bid,
-                                      unsigned* __restrict__ slot_of) {
+                                      unsigned* __restrict__ slot_of, ExtraMove ex) {
   const unsigned n = ctr->n;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const unsigned s = src[t];
@@ -292,30 +324,35 @@ static __global__ void k_order_gather(const Counters* __restrict__ ctr, const un
     Bid[dst] = id_of(v);
     if (slot_of) slot_of[id_of(v)] = dst;  // links find their other end by id
     if (PB) PB[dst] = PA[s];
+    for (unsigned k = 0; k < ex.E; ++k) ex.EB[k * ex.C + dst] = ex.EA[k * ex.C + s];
   }
 }
 
 // A step without a rebuild (rebuild_every_n > 1): the working copy takes the
 // new positions in the same slot order and keeps each slot's bin key in w.
 static __global__ void k_refresh(const Counters* __restrict__ ctr, const float4* __restrict__ A,
-                                 const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB) {
+                                 const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB,
+                                 ExtraMove ex) {
   const unsigned n = ctr->n;
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const float4 v = A[s];
     B[s] = make_float4(v.x, v.y, v.z, B[s].w);
     if (PB) PB[s] = PA[s];
+    for (unsigned k = 0; k < ex.E; ++k) ex.EB[k * ex.C + s] = ex.EA[k * ex.C + s];
   }
 }
 
 // Naive finders keep the working copy in cell-id order.
 static __global__ void k_id_scatter(const Counters* __restrict__ ctr, const float4* __restrict__ A,
-                             const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB) {
+                             const float2* __restrict__ PA, float4* __restrict__ B, float2* __restrict__ PB,
+                             ExtraMove ex) {
   const unsigned n = ctr->n;
   for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     float4 v = A[s];
     unsigned id = id_of(v);
     B[id] = v;
     if (PB) PB[id] = PA[s];
+    for (unsigned k = 0; k < ex.E; ++k) ex.EB[k * ex.C + id] = ex.EA[k * ex.C + s];
   }
 }
 
@@ -379,7 +416,8 @@ __device__ __forceinline__ void count_cell(const GridP& g, const PassArgs& a, un
 
 template <int D>
 __device__ __forceinline__ void maybe_divide(const GridP& g, const PassArgs& a, unsigned n, unsigned id,
-                                             const float* xnew, float2 pnew, unsigned long long step) {
+                                             const float* xnew, float2 pnew, unsigned long long step,
+                                             unsigned parent_slot) {
   if (!a.div_enabled) return;
   if ((hash64(a.seed, step, id, 0) >> 11) > a.div_thresh) return;
   unsigned k = atomicAdd(&a.ctr->div_count, 1u);
@@ -395,6 +433,8 @@ __device__ __forceinline__ void maybe_divide(const GridP& g, const PassArgs& a, 
   if (D >= 3) o.z = xnew[2] + a.div_offset * v[2];
   a.A[slot] = o;
   if (a.PA) a.PA[slot] = pnew;
+  // the daughter takes the parent's new extra fields (written before this)
+  for (unsigned c = 0; c < a.E; ++c) a.EA[c * (size_t)a.capacity + slot] = a.EA[c * (size_t)a.capacity + parent_slot];
   a.div_parent[k] = id;
   a.div_slot[k] = slot;
   if (a.count_next) {
@@ -660,12 +700,43 @@ __device__ __forceinline__ void add_link(const PassArgs& a, unsigned n, const fl
   for (int d = 0; d < D; ++d) s[d] = s[d] + (0.0f + (k * disp[d]) / dist);
 }
 
+// One extra component's update, in double for Scalar fields (the reference's
+// float += float * double) and in float otherwise.
+__device__ __forceinline__ float ex_update(float x, float d, float dt, double dt64, bool dbl) {
+  return dbl ? (float)((double)x + (double)d * dt64) : x + d * dt;
+}
+
+// The extra fields of one active cell (slot i): the mode's delta store and
+// state update, as cell_commit does for the position.  exd: the cell's extra
+// deltas, 0 + its sums (null: zero).
+__device__ __forceinline__ void commit_extras(const PassArgs& a, unsigned i, const float* exd) {
+  const size_t C = a.capacity;
+  for (unsigned k = 0; k < a.E; ++k) {
+    const float d = exd ? exd[k] : 0.0f;
+    const bool dbl = (a.ex_dbl >> k) & 1u;
+    const size_t at = k * C + i;
+    if (a.mode == kStore) {
+      a.ed_out[at] = d;
+    } else if (a.mode == kHeun1Fused) {
+      a.ed_out[at] = d;
+      a.Et[at] = ex_update(a.EX[at], d, a.dt, a.dt64, dbl);
+    } else if (a.mode == kEulerFused) {
+      a.EA[at] = ex_update(a.EBx[at], d, a.dt, a.dt64, dbl);
+    } else {
+      // Heun: x += (d1 + d2) * 0.5 * dt (heun.hpp:89-90)
+      const float h = a.ed1[at] + d;
+      const float xb = a.EBx[at];
+      a.EA[at] = dbl ? (float)((double)xb + ((double)h * 0.5) * a.dt64) : xb + (h * 0.5f) * a.dt;
+    }
+  }
+}
+
 // The library's link law: the constant pull (add_link).  A user LINK_FORCE
 // law takes its place in the user-law pass (tecs/pairwise.cuh).
 struct BuiltinLinks {
   template <int D>
   __device__ __forceinline__ void add(const PassArgs& a, unsigned n, unsigned id, const float* xs, float2 ps,
-                                      unsigned e, float* s, float* sp) const {
+                                      unsigned e, float* s, float* sp, float* se) const {
     add_link<D>(a, n, xs, e, s);
   }
 };
@@ -673,18 +744,27 @@ struct BuiltinLinks {
 // The write of one active cell: links, then the mode's store or fused
 // integrator update, the next rebuild's bin count and division.  s receives
 // the cell's position delta (for the COM partials).
-template <int D, class Links = BuiltinLinks>
+// NE: the extra components the pass carries (the user-law pass of a config
+// with extra fields; the built-in passes carry none and leave the extra
+// fields to k_predict / k_finish, see enqueue_step).
+template <int D, class Links = BuiltinLinks, unsigned NE = 0>
 __device__ __forceinline__ void cell_commit(const GridP& g, const PassArgs& a, unsigned n, unsigned i,
                                             const float* xi, const float4& vi, const float2& pi, const Acc& acc,
-                                            float* s, const Links& links = Links{}) {
+                                            float* s, const Links& links = Links{}, const float* exd = nullptr) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) s[d] = 0.0f + acc.x[d];
   float sp[2] = {0.0f + acc.p[0], 0.0f + acc.p[1]};
+  float se[NE > 0 ? NE : 1];
+  if constexpr (NE > 0) {
+#pragma unroll
+    for (unsigned k = 0; k < NE; ++k) se[k] = 0.0f + exd[k];
+  }
   if (a.link_off) {
     const unsigned id = a.Bid ? a.Bid[i] : id_of(vi);
     const unsigned e1 = a.link_off[id + 1];
-    for (unsigned e = a.link_off[id]; e < e1; ++e) links.template add<D>(a, n, id, xi, pi, e, s, sp);
+    for (unsigned e = a.link_off[id]; e < e1; ++e) links.template add<D>(a, n, id, xi, pi, e, s, sp, se);
   }
+  if constexpr (NE > 0) commit_extras(a, i, se);
   const float sp0 = sp[0], sp1 = sp[1];
   if (a.mode == kStore) {
     a.d_out[i] = make_float4(s[0], s[1], s[2], 0.f);
@@ -723,17 +803,17 @@ __device__ __forceinline__ void cell_commit(const GridP& g, const PassArgs& a, u
   a.A[i] = make_float4(xn[0], xn[1], xn[2], __uint_as_float(idb));
   if (a.PA) a.PA[i] = pn;
   if (a.count_next) count_cell<D>(g, a, i, xn);
-  maybe_divide<D>(g, a, n, idb, xn, pn, a.ctr->step);
+  maybe_divide<D>(g, a, n, idb, xn, pn, a.ctr->step, i);
 }
 
 // cell_commit for an active cell, then (every thread of the block) the COM
 // partials of kStore.
-template <int D, class Links = BuiltinLinks>
+template <int D, class Links = BuiltinLinks, unsigned NE = 0>
 __device__ __forceinline__ void pass_epilogue(const GridP& g, const PassArgs& a, bool active, unsigned n, unsigned i,
                                               const float* xi, const float4& vi, const float2& pi, const Acc& acc,
-                                              const Links& links = Links{}) {
+                                              const Links& links = Links{}, const float* exd = nullptr) {
   float s[3] = {0.f, 0.f, 0.f};
-  if (active) cell_commit<D>(g, a, n, i, xi, vi, pi, acc, s, links);
+  if (active) cell_commit<D, Links, NE>(g, a, n, i, xi, vi, pi, acc, s, links, exd);
   if (a.mode == kStore && a.com_part)
     com_reduce_block(a, active ? com_fixed(s[0]) : 0ll, active ? com_fixed(s[1]) : 0ll,
                      active ? com_fixed(s[2]) : 0ll);
@@ -947,8 +1027,8 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
-                                          unsigned j, const float* xi, float2 pi, Acc& acc, DragAcc& dacc,
-                                          unsigned idi, const Law& law) {
+                                          unsigned j, const float* xi, float2 pi, Acc& acc,
+                                          typename Law::Cell& dacc, unsigned idi, const Law& law) {
   const float4 vj = a.X[j];
   float disp[3] = {xi[0] - vj.x, xi[1] - vj.y, D >= 3 ? xi[2] - vj.z : 0.f};
   float d2 = disp[0] * disp[0] + disp[1] * disp[1];
@@ -967,14 +1047,14 @@ __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, cons
   }
   const float dist = sqrtf(d2);
   const float2 pj = a.P ? a.P[j] : make_float2(0.f, 0.f);
-  for (unsigned r = 0; r < reps; ++r) law(a, idi, idj, xi, vj, disp, dist, pi, pj, acc, dacc);
+  for (unsigned r = 0; r < reps; ++r) law(a, idi, idj, j, xi, vj, disp, dist, pi, pj, acc, dacc);
 }
 
 // cell_general's loops with a user law
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
-                                         const float* xi, float2 pi, unsigned idi, Acc& acc, DragAcc& dacc,
-                                         const Law& law) {
+                                         const float* xi, float2 pi, unsigned idi, Acc& acc,
+                                         typename Law::Cell& dacc, const Law& law) {
   if (FINDER == 1 || FINDER == 3) {
     int bc[3] = {0, 0, 0};
     if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
@@ -1008,10 +1088,12 @@ template <int D, int FINDER, class Law>
 static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, ForceP fp, PassArgs a,
                                                                   const Law* __restrict__ lawp) {
   const Law& law = *lawp;
+  constexpr unsigned NE = Law::kExtra;
   const unsigned n = a.ctr->n;
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n;
   Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
+  typename Law::Cell cell;
   float xi[3] = {0.f, 0.f, 0.f};
   float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
   float2 pi = make_float2(0.f, 0.f);
@@ -1020,27 +1102,46 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_law(GridP g, Force
     xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
     if (a.P) pi = a.P[i];
     const unsigned idi = id_at(a.X, a.Bid, i);
-    DragAcc dacc = {0.f, {0.f, 0.f, 0.f}};
-    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, idi, acc, dacc, law);
+    cell.drag = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) cell.v[d] = 0.f;
+    if constexpr (NE > 0) {
+#pragma unroll
+      for (unsigned k = 0; k < NE; ++k) {
+        cell.ex_self[k] = a.EX[k * (size_t)a.capacity + i];
+        cell.ex_delta[k] = 0.f;
+      }
+    }
+    cell_law<D, FINDER>(g, fp, a, n, i, xi, pi, idi, acc, cell, law);
     if constexpr (Law::kGeneric) {
       Acc gen = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
-      law.generic(a, idi, xi, pi, gen);
+      float gex[NE > 0 ? NE : 1] = {};
+      law.generic(a, idi, xi, pi, gen, cell.ex_self, gex);
 #pragma unroll
       for (int d = 0; d < 3; ++d) acc.x[d] = gen.x[d] + acc.x[d];
       acc.p[0] = gen.p[0] + acc.p[0];
       acc.p[1] = gen.p[1] + acc.p[1];
+      if constexpr (NE > 0) {
+#pragma unroll
+        for (unsigned k = 0; k < NE; ++k) cell.ex_delta[k] = gex[k] + cell.ex_delta[k];
+      }
     }
     // out(i) += total_velocity / fmax(total_drag, epsilon), after the pair
     // sums (binned_gabriel.hpp:356-357); with no drag this adds +0
     if constexpr (Law::kPairwise) {
-      const float den = fmaxf(dacc.drag, FLT_EPSILON);
+      const float den = fmaxf(cell.drag, FLT_EPSILON);
 #pragma unroll
-      for (int d = 0; d < D; ++d) acc.x[d] = acc.x[d] + dacc.v[d] / den;
+      for (int d = 0; d < D; ++d) acc.x[d] = acc.x[d] + cell.v[d] / den;
     }
   }
   // a LINK_FORCE law evaluates the cell's links in place of the built-in pull
-  if constexpr (Law::kLink) pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc, law);
-  else pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+  if constexpr (NE > 0) {
+    if constexpr (Law::kLink) pass_epilogue<D, Law, NE>(g, a, active, n, i, xi, vi, pi, acc, law, cell.ex_delta);
+    else pass_epilogue<D, BuiltinLinks, NE>(g, a, active, n, i, xi, vi, pi, acc, BuiltinLinks{}, cell.ex_delta);
+  } else {
+    if constexpr (Law::kLink) pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc, law);
+    else pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+  }
 }
 
 // One force evaluation handed to a user law's launcher (tecs_sim_set_pair_law).
@@ -1065,7 +1166,7 @@ template <int D, int FINDER, class Law>
 int launch_user_pass(const UserPassCall* c, cudaStream_t stream, const Law* law) {
   static_assert(FINDER >= 0 && FINDER <= 4, "user laws run with the all-pairs, Gabriel and Delaunay finders");
   if (!c || c->size != sizeof(UserPassCall)) return 1;
-  if (c->dims != D || c->finder != FINDER) return 3;
+  if (c->dims != D || c->finder != FINDER || c->a.E != Law::kExtra) return 3;
   int cur = -1;
   if (cudaGetDevice(&cur) != cudaSuccess || (cur != c->device && cudaSetDevice(c->device) != cudaSuccess)) return 2;
   k_pass_law<D, FINDER, Law><<<c->blocks, kPassThreads, 0, stream>>>(c->g, c->fp, c->a, law);
@@ -1479,10 +1580,17 @@ static __global__ void k_com(const float4* __restrict__ d, PassArgs a) {
 // stored: the corrector forms it again with the same operations.
 static __global__ void k_predict(const Counters* __restrict__ ctr, const float* __restrict__ com, float dt,
                           const float4* __restrict__ B, const float2* __restrict__ PB, const float4* __restrict__ d1,
-                          const float2* __restrict__ dp1, float4* __restrict__ Xt, float2* __restrict__ Pt) {
+                          const float2* __restrict__ dp1, float4* __restrict__ Xt, float2* __restrict__ Pt,
+                          PassArgs ex) {
   const unsigned n = ctr->n;
   const float c0 = com[0], c1 = com[1], c2 = com[2];
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // the extra fields' predictor: x~ = x + d1 * dt (no COM fix: it acts on
+    // the first field only)
+    for (unsigned k = 0; k < ex.E; ++k) {
+      const size_t at = k * (size_t)ex.capacity + i;
+      ex.Et[at] = ex_update(ex.EBx[at], ex.ed1[at], dt, ex.dt64, (ex.ex_dbl >> k) & 1u);
+    }
     float4 v = d1[i];
     v.x = v.x - c0; v.y = v.y - c1; v.z = v.z - c2;  // d1 - c1 (re-formed by k_finish)
     const float4 x = B[i];
@@ -1538,8 +1646,20 @@ static __global__ void k_finish(int heun, GridP g, PassArgs a, const float* __re
     const unsigned idb = a.Bid ? a.Bid[i] : id_of(xb);
     a.A[i] = make_float4(xn[0], xn[1], xn[2], __uint_as_float(idb));
     if (a.PA) a.PA[i] = pn;
+    // the extra fields: Euler x + d1 dt, Heun x + (d1 + d2) * 0.5 * dt
+    for (unsigned k = 0; k < a.E; ++k) {
+      const size_t at = k * (size_t)a.capacity + i;
+      const bool dbl = (a.ex_dbl >> k) & 1u;
+      const float xe = a.EBx[at];
+      if (heun) {
+        const float h = a.ed1[at] + a.ed2[at];
+        a.EA[at] = dbl ? (float)((double)xe + ((double)h * 0.5) * a.dt64) : xe + (h * 0.5f) * dt;
+      } else {
+        a.EA[at] = ex_update(xe, a.ed1[at], dt, a.dt64, dbl);
+      }
+    }
     if (a.count_next) count_cell<D>(g, a, i, xn);
-    maybe_divide<D>(g, a, n, idb, xn, pn, step);
+    maybe_divide<D>(g, a, n, idb, xn, pn, step, i);
   }
 }
 

@@ -48,6 +48,7 @@
 
 #include <cstring>
 #include <memory>
+#include <utility>
 
 #include "device/kernels.cuh"
 #include "tecs.hpp"
@@ -55,17 +56,149 @@
 namespace tecs {
 namespace detail {
 
+// A tuple usable in device code: one value per field.
+template <std::size_t I, typename T>
+struct TupLeaf {
+  T v;
+};
+template <typename Seq, typename... T>
+struct TupImpl;
+template <std::size_t... I, typename... T>
+struct TupImpl<std::index_sequence<I...>, T...> : TupLeaf<I, T>... {};
+template <std::size_t I, typename T>
+__host__ __device__ T& tget(TupLeaf<I, T>& leaf) {
+  return leaf.v;
+}
+template <typename Layout, typename Seq>
+struct ValuesOf;
+template <typename Layout, std::size_t... I>
+struct ValuesOf<Layout, std::index_sequence<I...>> {
+  using type = TupImpl<std::index_sequence<I...>, typename Layout::template type<I>...>;
+};
+
 // The laws in the form k_pass_law calls them: the values as the config's
 // types, the running sums as the deltas, the law, the sums back.  G: the
-// GENERIC_FORCE law or NoLaw; P: the PAIRWISE_FORCE law or NoLaw.
+// GENERIC_FORCE law, P: the PAIRWISE_FORCE law, L: the LINK_FORCE law (NoLaw
+// where absent).  Every field of the config is built from where the library
+// holds it (FieldLayout: the position, the polarity, or the cell's extra
+// block) into a value of the field's type, the law gets references to those,
+// and the deltas go back.
 template <typename Config, typename G, typename P, typename L = NoLaw>
 struct PairLaw {
   static constexpr bool kGeneric = !std::is_same_v<G, NoLaw>;
   static constexpr bool kPairwise = !std::is_same_v<P, NoLaw>;
   static constexpr bool kLink = !std::is_same_v<L, NoLaw>;
+  static constexpr int D = Config::dimensions;
+  using Layout = FieldLayout<typename Config::Fields>;
+  static constexpr unsigned kExtra = Layout::extra;
+  static_assert(kExtra <= kMaxExtra, "at most 8 float components of extra fields");
+  using Cell = LawCell<kExtra>;
+  using Values = typename ValuesOf<Layout, std::make_index_sequence<Layout::n>>::type;
   G gen;
   P law;
   L link;
+
+  // field k of one cell from the library's arrays: its position (xyz), its
+  // polarity (p) or its extra components (ex)
+  template <std::size_t K>
+  __device__ static void load(typename Layout::template type<K>& v, const float* xyz, float2 p, const float* ex) {
+    if constexpr (Layout::role(K) == 0) {
+      for (int d = 0; d < D; ++d) v[d] = xyz[d];
+    } else if constexpr (Layout::role(K) == 1) {
+      v[0] = p.x;
+      v[1] = p.y;
+    } else {
+      constexpr unsigned o = Layout::offset(K);
+      if constexpr (FieldWidth<typename Layout::template type<K>>::scalar) v = ex[o];
+      else
+        for (unsigned c = 0; c < FieldWidth<typename Layout::template type<K>>::value; ++c) v[c] = ex[o + c];
+    }
+  }
+  // field k's delta back into the sums
+  template <std::size_t K>
+  __device__ static void store(const typename Layout::template type<K>& v, float* x, float* p, float* ex) {
+    if constexpr (Layout::role(K) == 0) {
+      for (int d = 0; d < D; ++d) x[d] = v[d];
+    } else if constexpr (Layout::role(K) == 1) {
+      p[0] = v[0];
+      p[1] = v[1];
+    } else {
+      constexpr unsigned o = Layout::offset(K);
+      if constexpr (FieldWidth<typename Layout::template type<K>>::scalar) ex[o] = v;
+      else
+        for (unsigned c = 0; c < FieldWidth<typename Layout::template type<K>>::value; ++c) ex[o + c] = v[c];
+    }
+  }
+  template <typename F, std::size_t... I>
+  __device__ static void each(F&& f, std::index_sequence<I...>) {
+    (f(std::integral_constant<std::size_t, I>{}), ...);
+  }
+  template <typename F>
+  __device__ static void each(F&& f) {
+    each(static_cast<F&&>(f), std::make_index_sequence<Layout::n>{});
+  }
+  // the extra components of slot j of the pass's input
+  __device__ static void load_extra(const PassArgs& a, unsigned j, float* ex) {
+    if constexpr (kExtra > 0)
+      for (unsigned k = 0; k < kExtra; ++k) ex[k] = a.EX[k * (size_t)a.capacity + j];
+  }
+
+  __device__ void generic(const PassArgs& a, unsigned idi, const float* xi, float2 pi, Acc& acc, const float* exi,
+                          float* exd) const {
+    if constexpr (kGeneric) {
+      using Fields = typename Config::template ForceFields<GenericFieldRef>;
+      Values self{}, delta{};
+      each([&](auto k) {
+        load<k>(tget<k>(self), xi, pi, exi);
+        load<k>(tget<k>(delta), acc.x, make_float2(acc.p[0], acc.p[1]), exd);
+      });
+      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 3u : 4u, idi, idi);
+      [&]<std::size_t... I>(std::index_sequence<I...>) {
+        const Fields ctx{GenericFieldRef<typename Layout::template type<I>>{tget<I>(self), tget<I>(delta)}...};
+        gen(a.full_step != 0, idi, rng, ctx);
+      }(std::make_index_sequence<Layout::n>{});
+      each([&](auto k) { store<k>(tget<k>(delta), acc.x, acc.p, exd); });
+    }
+  }
+
+  __device__ void operator()(const PassArgs& a, unsigned idi, unsigned idj, unsigned j, const float* xi,
+                             const float4& vj, const float* disp, float dist, float2 pi, float2 pj, Acc& acc,
+                             Cell& cell) const {
+    if constexpr (kPairwise) {
+      using Fields = typename Config::template ForceFields<PairwiseFieldRef>;
+      using Vector = VectorN<float, D>;
+      Values self{}, other{}, delta{};
+      const float xj[3] = {vj.x, vj.y, vj.z};
+      float exj[kExtra > 0 ? kExtra : 1];
+      load_extra(a, j, exj);
+      each([&](auto k) {
+        load<k>(tget<k>(self), xi, pi, cell.ex_self);
+        load<k>(tget<k>(other), xj, pj, exj);
+        load<k>(tget<k>(delta), acc.x, make_float2(acc.p[0], acc.p[1]), cell.ex_delta);
+      });
+      Vector displacement;
+      for (int d = 0; d < D; ++d) displacement[d] = disp[d];
+      float drag = 0.f;
+      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
+      [&]<std::size_t... I>(std::index_sequence<I...>) {
+        const Fields ctx{PairwiseFieldRef<typename Layout::template type<I>>{tget<I>(self), tget<I>(other),
+                                                                             tget<I>(delta)}...};
+        law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
+      }(std::make_index_sequence<Layout::n>{});
+      each([&](auto k) { store<k>(tget<k>(delta), acc.x, acc.p, cell.ex_delta); });
+      // total_drag += drag; total_velocity += drag * old_velocities(j)
+      // (binned_gabriel.hpp:225-226); a simulation that keeps no old
+      // velocities fails its next count or download when a law sets drag
+      if (a.old_vel) {
+        const float4 ov = a.old_vel[idj];
+        const float o[3] = {ov.x, ov.y, ov.z};
+        cell.drag = cell.drag + drag;
+        for (int d = 0; d < D; ++d) cell.v[d] = cell.v[d] + drag * o[d];
+      } else if (drag != 0.f) {
+        atomicOr(&a.ctr->error, 2u);
+      }
+    }
+  }
 
   // One of the cell's links (entry e of its link list) through the LINK_FORCE
   // law: the reference calls the law once per link with zeroed accumulators
@@ -73,117 +206,53 @@ struct PairLaw {
   // link order (integrators/base.hpp:196-233).  Here each end evaluates the
   // link and adds its own accumulator, so the law runs twice per link with
   // the same inputs and the same generator draws (keyed by the link's index).
-  template <int D>
+  template <int DD>
   __device__ void add(const PassArgs& a, unsigned n, unsigned id, const float* xs, float2 ps, unsigned e, float* s,
-                      float* sp) const {
+                      float* sp, float* se) const {
     if constexpr (kLink) {
-      using Vector = VectorN<float, D>;
       using Fields = typename Config::template ForceFields<LinkFieldRef>;
       const uint2 le = a.link_ent[e];
       const bool b_end = (le.y & 1u) != 0u;
-      // the other end's value: an id beyond the active cells reads an unused
+      // the other end's values: an id beyond the active cells reads an unused
       // view slot's zero
       float xo[3] = {0.f, 0.f, 0.f};
       float2 po = make_float2(0.f, 0.f);
+      float exo[kExtra > 0 ? kExtra : 1] = {};
+      float exs[kExtra > 0 ? kExtra : 1] = {};
+      const unsigned self_slot = a.slot_of ? a.slot_of[id] : id;
+      load_extra(a, self_slot, exs);
       if (le.x < n) {
         const unsigned so = a.slot_of ? a.slot_of[le.x] : le.x;
         const float4 v = a.X[so];
         xo[0] = v.x; xo[1] = v.y; xo[2] = v.z;
         if (a.P) po = a.P[so];
+        load_extra(a, so, exo);
       }
-      Vector self, other, da, db;
-      for (int d = 0; d < D; ++d) {
-        self[d] = xs[d];
-        other[d] = xo[d];
-        da[d] = 0.f;
-        db[d] = 0.f;
-      }
+      Values va{}, vb{}, da{}, db{};
+      const float zeros[3 + kMaxExtra] = {};
+      each([&](auto k) {
+        load<k>(tget<k>(va), b_end ? xo : xs, b_end ? po : ps, b_end ? exo : exs);
+        load<k>(tget<k>(vb), b_end ? xs : xo, b_end ? ps : po, b_end ? exs : exo);
+        load<k>(tget<k>(da), zeros, make_float2(0.f, 0.f), zeros);
+        load<k>(tget<k>(db), zeros, make_float2(0.f, 0.f), zeros);
+      });
       const Link lk{b_end ? le.x : id, b_end ? id : le.x};
       XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 5u : 6u, le.y >> 1, 0u);
-      const Vector& va = b_end ? other : self;
-      const Vector& vb = b_end ? self : other;
-      if constexpr (Simulation<Config>::has_polarity) {
-        const Polarity_<float> pself(ps.x, ps.y), pother(po.x, po.y);
-        Polarity_<float> qa(0.f, 0.f), qb(0.f, 0.f);
-        const Fields ctx{{va, vb, da, db}, {b_end ? pother : pself, b_end ? pself : pother, qa, qb}};
+      [&]<std::size_t... I>(std::index_sequence<I...>) {
+        const Fields ctx{LinkFieldRef<typename Layout::template type<I>>{tget<I>(va), tget<I>(vb),
+                                                                         tget<I>(da), tget<I>(db)}...};
         link(a.full_step != 0, lk, rng, ctx);
-        const Polarity_<float>& q = b_end ? qb : qa;
-        sp[0] = sp[0] + q[0];
-        sp[1] = sp[1] + q[1];
-      } else {
-        const Fields ctx{{va, vb, da, db}};
-        link(a.full_step != 0, lk, rng, ctx);
+      }(std::make_index_sequence<Layout::n>{});
+      // this end's accumulator added to its sums, in link order
+      float mx[3] = {0.f, 0.f, 0.f}, mp[2] = {0.f, 0.f}, me[kExtra > 0 ? kExtra : 1] = {};
+      each([&](auto k) { store<k>(b_end ? tget<k>(db) : tget<k>(da), mx, mp, me); });
+      for (int d = 0; d < DD; ++d) s[d] = s[d] + mx[d];
+      if (a.P) {
+        sp[0] = sp[0] + mp[0];
+        sp[1] = sp[1] + mp[1];
       }
-      const Vector& mine = b_end ? db : da;
-      for (int d = 0; d < D; ++d) s[d] = s[d] + mine[d];
-    }
-  }
-
-  __device__ void generic(const PassArgs& a, unsigned idi, const float* xi, float2 pi, Acc& acc) const {
-    if constexpr (kGeneric) {
-      constexpr int D = Config::dimensions;
-      using Vector = VectorN<float, D>;
-      using Fields = typename Config::template ForceFields<GenericFieldRef>;
-      Vector self, delta;
-      for (int d = 0; d < D; ++d) {
-        self[d] = xi[d];
-        delta[d] = acc.x[d];
-      }
-      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 3u : 4u, idi, idi);
-      if constexpr (Simulation<Config>::has_polarity) {
-        const Polarity_<float> ps(pi.x, pi.y);
-        Polarity_<float> pd(acc.p[0], acc.p[1]);
-        const Fields ctx{{self, delta}, {ps, pd}};
-        gen(a.full_step != 0, idi, rng, ctx);
-        acc.p[0] = pd[0];
-        acc.p[1] = pd[1];
-      } else {
-        const Fields ctx{{self, delta}};
-        gen(a.full_step != 0, idi, rng, ctx);
-      }
-      for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
-    }
-  }
-
-  __device__ void operator()(const PassArgs& a, unsigned idi, unsigned idj, const float* xi, const float4& vj,
-                             const float* disp, float dist, float2 pi, float2 pj, Acc& acc, DragAcc& dacc) const {
-    if constexpr (!std::is_same_v<P, NoLaw>) {
-      constexpr int D = Config::dimensions;
-      using Vector = VectorN<float, D>;
-      using Fields = typename Config::template ForceFields<PairwiseFieldRef>;
-      Vector self, other, displacement, delta;
-      const float xj[3] = {vj.x, vj.y, vj.z};
-      for (int d = 0; d < D; ++d) {
-        self[d] = xi[d];
-        other[d] = xj[d];
-        displacement[d] = disp[d];
-        delta[d] = acc.x[d];
-      }
-      float drag = 0.f;
-      XorShiftRandom rng = XorShiftRandom::for_call(a.seed, a.ctr->step, a.full_step ? 1u : 2u, idi, idj);
-      if constexpr (Simulation<Config>::has_polarity) {
-        const Polarity_<float> ps(pi.x, pi.y), po(pj.x, pj.y);
-        Polarity_<float> pd(acc.p[0], acc.p[1]);
-        const Fields ctx{{self, other, delta}, {ps, po, pd}};
-        law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
-        acc.p[0] = pd[0];
-        acc.p[1] = pd[1];
-      } else {
-        const Fields ctx{{self, other, delta}};
-        law(a.full_step != 0, idi, idj, displacement, dist, rng, drag, ctx);
-      }
-      for (int d = 0; d < D; ++d) acc.x[d] = delta[d];
-      // total_drag += drag; total_velocity += drag * old_velocities(j)
-      // (binned_gabriel.hpp:225-226); a simulation that keeps no old
-      // velocities fails its next count or download when a law sets drag
-      if (a.old_vel) {
-        const float4 ov = a.old_vel[idj];
-        const float o[3] = {ov.x, ov.y, ov.z};
-        dacc.drag = dacc.drag + drag;
-        for (int d = 0; d < D; ++d) dacc.v[d] = dacc.v[d] + drag * o[d];
-      } else if (drag != 0.f) {
-        atomicOr(&a.ctr->error, 2u);
-      }
+      if constexpr (kExtra > 0)
+        for (unsigned k = 0; k < kExtra; ++k) se[k] = se[k] + me[k];
     }
   }
 };

@@ -140,27 +140,46 @@ class Simulation {
   static_assert(dimensions == 2 || dimensions == 3, "2 or 3 dimensions");
 
  private:
+  // the fields as the library holds them (tecs/config.hpp: FieldLayout)
+  using Layout = detail::FieldLayout<Fields>;
+  static_assert(std::is_same_v<typename Layout::template type<0>, Vector>, "the first field must be a Vector");
+  static_assert(Layout::extra <= 8, "at most 8 float components of extra fields");
+  template <std::size_t K>
+  using FieldType = typename Layout::template type<K>;
+  // one view per field; the position's and the polarity's are positions_ and
+  // polarity_, the other fields' live here (their slots in this tuple for the
+  // position and the polarity stay empty)
+  using FieldViews = decltype([]<std::size_t... K>(std::index_sequence<K...>) {
+    return std::tuple<View<FieldType<K>>...>{};
+  }(std::make_index_sequence<Layout::n>{}));
+  template <typename F, std::size_t... K>
+  void each_extra(F&& f, std::index_sequence<K...>) {
+    (
+        [&] {
+          if constexpr (Layout::role(K) == 2) f(std::integral_constant<std::size_t, K>{}, std::get<K>(extras_));
+        }(),
+        ...);
+  }
+  // f(index, view) for every extra field
   template <typename F>
-  static constexpr bool is_position_field = std::is_same_v<typename F::value_type, Vector> && F::name == "position";
-  template <typename F>
-  static constexpr bool is_polarity_field = std::is_same_v<typename F::value_type, Polarity> && F::name == "polarity";
-
+  void each_extra(F&& f) {
+    each_extra(static_cast<F&&>(f), std::make_index_sequence<Layout::n>{});
+  }
+  template <typename Field, std::size_t... K>
+  static constexpr std::size_t index_of(std::index_sequence<K...>) {
+    std::size_t at = Layout::n;
+    ((at = std::is_same_v<Field, std::tuple_element_t<K, typename FieldListTuple<Fields>::type>> ? K : at), ...);
+    return at;
+  }
   template <typename L>
-  struct FieldShape;
-  template <typename F0, typename... Fs>
-  struct FieldShape<detail::FieldList<F0, Fs...>> {
-    static constexpr int n = 1 + static_cast<int>(sizeof...(Fs));
-    static constexpr bool first_is_position = is_position_field<F0>;
-    static constexpr bool polarity = (false || ... || is_polarity_field<Fs>);
-    static constexpr bool only_known = (true && ... && is_polarity_field<Fs>);
+  struct FieldListTuple;
+  template <typename... Fs>
+  struct FieldListTuple<detail::FieldList<Fs...>> {
+    using type = std::tuple<Fs...>;
   };
-  using Shape = FieldShape<Fields>;
-  static_assert(Shape::first_is_position, "the first field must be (Vector, position)");
-  static_assert(Shape::only_known && Shape::n <= 2,
-                "the GB300 path carries a (Vector, position) field and an optional (Polarity, polarity) field");
 
  public:
-  static constexpr bool has_polarity = Shape::polarity;
+  static constexpr bool has_polarity = Layout::has_polarity;
 
   struct Settings {
     Settings(unsigned agent_count_, const std::string& output_path_)
@@ -207,7 +226,7 @@ class Simulation {
     d.device = s.device;
     check(tecs_sim_create(&d, &handle_));
     desc_ = d;
-    positions_ = View<Vector>("position", s.agent_count, s.capacity);
+    positions_ = View<Vector>(std::string(field_name<0>()), s.agent_count, s.capacity);
     if constexpr (has_polarity) polarity_ = View<Polarity>("polarity", s.agent_count, s.capacity);
     links_ = View<Link>("links", s.link_active_count, s.link_capacity);
     // zero-initialised views are the first state, as Kokkos views are
@@ -215,6 +234,13 @@ class Simulation {
     auto refresh = [this]() { refresh_host(); };
     positions_.set_refresh(refresh);
     if constexpr (has_polarity) polarity_.set_refresh(refresh);
+    if constexpr (Layout::extra > 0) {
+      check(tecs_sim_set_extra_fields(handle_, Layout::extra, Layout::double_mask()));
+      each_extra([&](auto k, auto& v) {
+        v = View<FieldType<k>>(std::string(field_name<k>()), s.agent_count, s.capacity);
+        v.set_refresh(refresh);
+      });
+    }
   }
 
   Simulation(const Simulation&) = delete;
@@ -222,6 +248,7 @@ class Simulation {
   ~Simulation() {
     positions_.set_refresh(nullptr);
     if constexpr (has_polarity) polarity_.set_refresh(nullptr);
+    each_extra([&](auto, auto& v) { v.set_refresh(nullptr); });
     if (handle_) tecs_sim_destroy(handle_);
   }
 
@@ -307,8 +334,10 @@ class Simulation {
     capacity = value;
     positions_.resize(value);
     if constexpr (has_polarity) polarity_.resize(value);
+    each_extra([&](auto, auto& v) { v.resize(value); });
+    if constexpr (Layout::extra > 0) check(tecs_sim_set_extra_fields(handle_, Layout::extra, Layout::double_mask()));
     set_count(agent_count);
-    positions_.set_host_modified(true);
+    mark_fields_host_modified();
     lib_newer_dev_ = lib_newer_host_ = false;
     if (old_velocities_kept_) {
       old_velocities_kept_ = false;
@@ -549,8 +578,7 @@ class Simulation {
       initializer(i, g);
       pool_.free_state(g);
     }
-    positions_.set_host_modified(true);
-    if constexpr (has_polarity) polarity_.set_host_modified(true);
+    mark_fields_host_modified();
     if constexpr (sizeof...(init_functions) > 0) init(static_cast<InitFuncs&&>(init_functions)...);
   }
 
@@ -569,8 +597,7 @@ class Simulation {
       (functions(i, g), ...);
       pool_.free_state(g);
     }
-    positions_.set_host_modified(true);
-    if constexpr (has_polarity) polarity_.set_host_modified(true);
+    mark_fields_host_modified();
     links_dirty_ = true;
   }
   // over the agents, and over the active links
@@ -767,22 +794,32 @@ class Simulation {
     if constexpr (requires { p.rebuild_every_n; }) d.rebuild_every_n = p.rebuild_every_n;
   }
 
+  template <std::size_t K>
+  static constexpr std::string_view field_name() {
+    return std::tuple_element_t<K, typename FieldListTuple<Fields>::type>::name;
+  }
+  template <std::size_t K>
+  View<FieldType<K>>& view_at() {
+    if constexpr (Layout::role(K) == 0) return positions_;
+    else if constexpr (Layout::role(K) == 1) return polarity_;
+    else return std::get<K>(extras_);
+  }
   template <typename Field>
   View<typename Field::value_type>& view_of() {
-    if constexpr (is_position_field<Field>) {
-      return positions_;
-    } else {
-      static_assert(has_polarity && is_polarity_field<Field>, "no such field in this config");
-      return polarity_;
-    }
+    constexpr std::size_t K = index_of<Field>(std::make_index_sequence<Layout::n>{});
+    static_assert(K < Layout::n, "no such field in this config");
+    return view_at<K>();
   }
 
+  // every field in the config's order, then the extra views, then the links
+  // (the reference writes get_views() first, simulation.hpp:600-667)
   template <typename... Ts>
   void write_all(double time, const View<Ts>&... extra) {
     refresh_host();
     const unsigned step = current_step++;
-    if constexpr (has_polarity) writer_.write(time, step, positions_, polarity_, extra..., links_);
-    else writer_.write(time, step, positions_, extra..., links_);
+    [&]<std::size_t... K>(std::index_sequence<K...>) {
+      writer_.write(time, step, view_at<K>()..., extra..., links_);
+    }(std::make_index_sequence<Layout::n>{});
   }
 
   // The library's state after steps is newer than both arrays of the field views.
@@ -790,6 +827,11 @@ class Simulation {
     lib_newer_dev_ = lib_newer_host_ = true;
     positions_.set_stale(true);
     if constexpr (has_polarity) polarity_.set_stale(true);
+    each_extra([&](auto, auto& v) { v.set_stale(true); });
+  }
+  template <std::size_t K>
+  static constexpr unsigned width_of() {
+    return detail::FieldWidth<FieldType<K>>::value;
   }
   // library -> the field views' device arrays (cell-id order, on the device)
   void refresh_device() {
@@ -798,6 +840,12 @@ class Simulation {
     check(tecs_sim_download_device(handle_, reinterpret_cast<float*>(positions_.device_data()),
                                    has_polarity ? reinterpret_cast<float*>(polarity_.device_data()) : nullptr, &n));
     set_count(n);
+    each_extra([&](auto k, auto& v) {
+      unsigned m = 0;
+      check(tecs_sim_download_extra(handle_, Layout::offset(k), width_of<k>(), reinterpret_cast<float*>(v.device_data()),
+                                    &m));
+      v.clear_device_flag();
+    });
     lib_newer_dev_ = false;
     positions_.clear_device_flag();
     if constexpr (has_polarity) polarity_.clear_device_flag();
@@ -812,40 +860,75 @@ class Simulation {
     if constexpr (has_polarity) polarity_.set_stale(false);
     positions_.set_host_modified(false);
     if constexpr (has_polarity) polarity_.set_host_modified(false);
+    each_extra([&](auto, auto& v) {
+      v.copy_to_host();
+      v.set_stale(false);
+      v.set_host_modified(false);
+    });
     lib_newer_host_ = false;
   }
   void set_count(unsigned n) {
     agent_count = n;
     positions_.set_active_count(n);
     if constexpr (has_polarity) polarity_.set_active_count(n);
+    each_extra([&](auto, auto& v) { v.set_active_count(n); });
+  }
+  void mark_fields_host_modified() {
+    positions_.set_host_modified(true);
+    if constexpr (has_polarity) polarity_.set_host_modified(true);
+    each_extra([&](auto, auto& v) { v.set_host_modified(true); });
   }
   // field views written since the library last read them -> the library: the
   // host arrays when host code wrote them, else the device arrays when
   // device code did
   void sync_to_library() {
     const bool host = positions_.host_modified() || (has_polarity && polarity_.host_modified());
-    if (host) {
-      check(tecs_sim_upload(handle_, reinterpret_cast<const float*>(positions_.host_array()),
-                            has_polarity ? reinterpret_cast<const float*>(polarity_.host_array()) : nullptr,
-                            agent_count));
-      positions_.set_host_modified(false);
-      if constexpr (has_polarity) polarity_.set_host_modified(false);
+    bool host_extra = false;
+    each_extra([&](auto, auto& v) { host_extra = host_extra || v.host_modified(); });
+    if (host || host_extra) {
+      // the position upload keeps the library's extra fields (by cell id)
+      if (host) {
+        check(tecs_sim_upload(handle_, reinterpret_cast<const float*>(positions_.host_array()),
+                              has_polarity ? reinterpret_cast<const float*>(polarity_.host_array()) : nullptr,
+                              agent_count));
+        positions_.set_host_modified(false);
+        if constexpr (has_polarity) polarity_.set_host_modified(false);
+      }
+      each_extra([&](auto k, auto& v) {
+        if (!v.host_modified()) return;
+        check(tecs_sim_upload_extra(handle_, Layout::offset(k), width_of<k>(),
+                                    reinterpret_cast<const float*>(v.host_array()), agent_count));
+        v.set_host_modified(false);
+      });
       // the device arrays did not see these writes
       lib_newer_dev_ = true;
       return;
     }
     if (!user_code_ran_) return;
     user_code_ran_ = false;
+    if (lib_newer_dev_) return;
     const bool dev = positions_.device_flag() || (has_polarity && polarity_.device_flag());
-    if (dev && !lib_newer_dev_) {
+    bool changed = false;
+    if (dev) {
       check(tecs_sim_upload_device(handle_, reinterpret_cast<const float*>(positions_.device_data()),
                                    has_polarity ? reinterpret_cast<const float*>(polarity_.device_data()) : nullptr,
                                    agent_count));
       positions_.clear_device_flag();
       if constexpr (has_polarity) polarity_.clear_device_flag();
+      changed = true;
+    }
+    each_extra([&](auto k, auto& v) {
+      if (!v.device_flag()) return;
+      check(tecs_sim_upload_extra(handle_, Layout::offset(k), width_of<k>(),
+                                  reinterpret_cast<const float*>(v.device_data()), agent_count));
+      v.clear_device_flag();
+      changed = true;
+    });
+    if (changed) {
       lib_newer_host_ = true;
       positions_.set_stale(true);
       if constexpr (has_polarity) polarity_.set_stale(true);
+      each_extra([&](auto, auto& v) { v.set_stale(true); });
     }
   }
 
@@ -858,6 +941,7 @@ class Simulation {
   tecs_sim* handle_ = nullptr;
   View<Vector> positions_;
   View<Polarity> polarity_;
+  FieldViews extras_;
   View<Link> links_;
   bool links_dirty_ = false;        // the host links may differ from the device's
   unsigned links_on_device_ = 0;    // links active in the library

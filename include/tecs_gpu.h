@@ -148,6 +148,24 @@ int tecs_sim_old_velocities(tecs_sim* sim, float* out, unsigned* n);
 /* Sets the old velocities of cells 0 .. n-1 (v: n*dims floats). */
 int tecs_sim_set_old_velocities(tecs_sim* sim, const float* v, unsigned n);
 
+/* Extra fields: a config's fields beyond the position and the polarity
+ * (include/simulation_config.hpp:44-192 holds any list of fields), as
+ * `components` floats per cell (at most 8; Scalar 1, Polarity 2, Vector
+ * dims each), zeroed.  Bit k of double_mask marks component k as a Scalar
+ * field's, which the integrators update in double (float += delta * double
+ * dt, as the reference's integrators do for a float field).  Every step
+ * moves and integrates them with the cell; the built-in laws give them zero
+ * deltas, user laws (tecs_sim_set_pair_law) any.  Non-symmetric finders
+ * only.  Synchronises. */
+int tecs_sim_set_extra_fields(tecs_sim* sim, unsigned components, uint32_t double_mask);
+/* One extra field, components [offset, offset + width), of cells 0 .. n-1 in
+ * cell-id order (values: n rows of width floats, host or device memory);
+ * n <= the active cells. */
+int tecs_sim_upload_extra(tecs_sim* sim, unsigned offset, unsigned width, const float* values, unsigned n);
+/* The same field of the active cells into out (host or device memory), *n
+ * receiving the count. */
+int tecs_sim_download_extra(tecs_sim* sim, unsigned offset, unsigned width, float* out, unsigned* n);
+
 /* Device memory for the drop-in layer's views and device variables
  * (include/types/view.hpp:47-266, device_var.hpp:38-134 hold theirs in
  * Kokkos::View device allocations).  tecs_device_copy copies between any two

@@ -400,6 +400,66 @@ static int run(const Input& in, const std::string& out, int steps, double dt) {
 }
 }  // namespace upd_bg_heun_3
 
+// A config with fields beyond the position: a Scalar u and a Vector w.  The
+// pairwise law diffuses u and w between neighbours and drives w along the
+// displacement; the generic law adds to u from the position; every field is
+// integrated by the reference's integrators (a Scalar field in double).
+// Outputs <out>.pos, <out>.u, <out>.w.
+template <class Config, class Scalar, class Vector, class Random, class PairwiseForceFields, class GenericForceFields>
+static int tecs_driver_run_fields(const Input& in, const std::string& out, int steps, double dt) {
+  using namespace tecs;
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  const unsigned n = in.n;
+  Kokkos::View<unsigned*> pairs("pairs", 2);
+  DeviceVar<int> counter = 0;
+  const bool capture = false;
+  auto make_force = [&]() {
+    return PAIRWISE_FORCE(TECS_DRIVER_SPRING
+                          ctx.u.delta += (ctx.u.other - ctx.u.self) * Scalar(0.2);
+                          ctx.w.delta += (ctx.w.other - ctx.w.self) * Scalar(0.1) + displacement * Scalar(0.01);)();
+  };
+  auto make_generic = GENERIC_FORCE(ctx.u.delta += Scalar(0.05) * ctx.position.self[0];);
+  typename Simulation<Config>::Settings st(n, "unused");
+  fill_settings<Simulation<Config>>(st, in);
+  fill_finder_settings(st.pair_finder_settings, in);
+  Simulation<Config> sim(st);
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  auto& u = sim.template get_view<FIELD(Scalar, u)>();
+  auto& w = sim.template get_view<FIELD(Vector, w)>();
+  for (unsigned i = 0; i < n; ++i) {
+    for (unsigned d = 0; d < in.dims; ++d) pos(i)[d] = in.x[(size_t)i * in.dims + d];
+    u(i) = pos(i)[0] * Scalar(0.3) + Scalar(1);
+    w(i) = pos(i) * Scalar(0.5);
+  }
+  auto force = make_force();
+  auto generic = make_generic();
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, force, generic);
+  std::vector<float> fp((size_t)n * in.dims), fu(n), fw((size_t)n * in.dims);
+  for (unsigned i = 0; i < n; ++i) {
+    fu[i] = u(i);
+    for (unsigned d = 0; d < in.dims; ++d) {
+      fp[(size_t)i * in.dims + d] = pos(i)[d];
+      fw[(size_t)i * in.dims + d] = w(i)[d];
+    }
+  }
+  write_raw(out + ".pos", fp.data(), fp.size() * 4);
+  write_raw(out + ".u", fu.data(), fu.size() * 4);
+  write_raw(out + ".w", fw.data(), fw.size() * 4);
+  return 0;
+}
+
+#define TECS_FIELDS_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                         \
+  namespace NAME {                                                                                      \
+  CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
+                                       CONFIG_COM_FIXER(COMFIXER) CONFIG_WRITER(tecs::io::Dummy)        \
+                                           CONFIG_FIELDS((Vector, position), (Scalar, u), (Vector, w)))  \
+  EXTRACT_ALL_FROM_SIMULATION_CONFIG(Config)                                                            \
+  static int run(const Input& in, const std::string& out, int steps, double dt) {                       \
+    return tecs_driver_run_fields<Config, Scalar, Vector, Random, PairwiseForceFields, GenericForceFields>( \
+        in, out, steps, dt);                                                                            \
+  }                                                                                                     \
+  }
+
 #define TECS_DRAG_SCENARIO(NAME, FINDER, INTEGRATOR, COMFIXER)                                          \
   namespace NAME {                                                                                      \
   CREATE_SIMULATION_CONFIG(Config, CONFIG_PAIR_FINDER(FINDER) CONFIG_INTEGRATOR(INTEGRATOR)             \
@@ -500,6 +560,9 @@ static int run(const Input& in, const std::string& out, int steps, double dt) {
 }  // namespace gen_bg_heun_3
 
 TECS_DRAG_SCENARIO(drag_bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer)
+TECS_FIELDS_SCENARIO(fields_bg_heun_3, pair_finders::BinnedGabriel, integrators::Heun, com_fixers::NoComFixer)
+TECS_FIELDS_SCENARIO(fields_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler,
+                     com_fixers::GlobalComFixer)
 TECS_DRAG_SCENARIO(drag_ba_euler_com_3, pair_finders::BinnedAllPairs, integrators::Euler, com_fixers::GlobalComFixer)
 
 // Grid-query scenarios (names starting "grid_"): the reference's standalone
@@ -630,6 +693,7 @@ int main(int argc, char** argv) {
 #define DISPATCH(NAME) \
   if (sc == #NAME) rc = NAME::run(in, out, steps, dt);
   DISPATCH(drag_bg_heun_3) DISPATCH(drag_ba_euler_com_3) DISPATCH(upd_bg_heun_3)
+  DISPATCH(fields_bg_heun_3) DISPATCH(fields_ba_euler_com_3)
   DISPATCH(ba_euler_3) DISPATCH(ba_heun_com_3) DISPATCH(bg_heun_3) DISPATCH(bg_heun_com_3) DISPATCH(bg_euler_com_3)
   DISPATCH(na_heun_3) DISPATCH(ng_heun_3) DISPATCH(bgs_euler_com_3) DISPATCH(bas_heun_3) DISPATCH(ngs_euler_3)
   DISPATCH(nas_heun_3)

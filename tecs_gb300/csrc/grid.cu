@@ -110,7 +110,7 @@ int grid_rebuild_from_device(tecs_grid* G, const float* pts, unsigned n) {
   k_scan_apply<<<chunks, kScanThreads, 0, G->stream>>>(G->cnt, len, G->part, G->off);
   k_scatter<<<gb, 256, 0, G->stream>>>(G->ctr, G->key, G->rank, G->off, G->src, G->part, 0u);
   k_order_gather<<<gb, 256, 0, G->stream>>>(G->ctr, G->key, G->off, G->src, G->A, nullptr, G->B, nullptr, G->Bid,
-                                            nullptr);
+                                            nullptr, ExtraMove{0, 0, nullptr, nullptr});
   GCK(cudaGetLastError());
   GCK(cudaStreamSynchronize(G->stream));
   G->n = n;

@@ -193,6 +193,11 @@ struct tecs_sim {
   unsigned* slot_of = nullptr;
   // the integrator's old velocities by cell id (float4, capacity), when kept
   float4* ov = nullptr;
+  // extra fields: E components per cell, component-major ([k * capacity +
+  // slot]); EA in A's slot order, EB in B's, Et the predictor, ed1 / ed2 the
+  // passes' deltas; ex_dbl marks the components of Scalar fields
+  unsigned E = 0, ex_dbl = 0;
+  float *EA = nullptr, *EB = nullptr, *Et = nullptr, *ed1 = nullptr, *ed2 = nullptr;
   unsigned n_links = 0;
   float link_k = 0.f;
   // B and Bid hold a sort of the current cells (false from an upload until the
@@ -206,7 +211,7 @@ struct tecs_sim {
   int step_count = 0;
   bool use_graph = true;
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-  float gdt[2] = {0.f, 0.f};
+  double gdt[2] = {0.0, 0.0};
   int kernels[2] = {0, 0};
   int last_kernels = 0;
   // the next rebuild's bin count is done by the state-writing kernel
@@ -295,7 +300,10 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
 }
 
 
-PassArgs base_args(const tecs_sim* s, float dt) {
+// the extra fields moved with A -> B
+ExtraMove extra_move(const tecs_sim* s) { return ExtraMove{s->E, (size_t)s->d.capacity, s->EA, s->EB}; }
+
+PassArgs base_args(const tecs_sim* s, float dt, double dt64 = 0.0) {
   PassArgs a{};
   a.off = s->off;
   a.ctr = s->ctr;
@@ -327,6 +335,10 @@ PassArgs base_args(const tecs_sim* s, float dt) {
   a.link_k = s->link_k;
   a.full_step = 1;
   a.old_vel = s->ov;
+  a.dt64 = dt64;
+  a.E = s->E;
+  a.ex_dbl = s->ex_dbl;
+  a.EA = s->EA;
   return a;
 }
 
@@ -374,12 +386,12 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
     PROF_END(s, "k_scatter");
     PROF_BEGIN(s);
     k_order_gather<<<gb, 256, 0, s->stream>>>(s->ctr, s->key, s->off, s->src, s->A, PA, s->B, PB, s->Bid,
-                                              s->n_links ? s->slot_of : nullptr);
+                                              s->n_links ? s->slot_of : nullptr, extra_move(s));
     PROF_END(s, "k_order_gather");
     K += 3;
   } else {
     PROF_BEGIN(s);
-    k_id_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, PA, s->B, PB);
+    k_id_scatter<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, PA, s->B, PB, extra_move(s));
     PROF_END(s, "k_id_scatter");
     K += 1;
   }
@@ -436,12 +448,14 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
 }
 
 // One integrator step (plus division), queued on the stream.
-int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
+int enqueue_step(tecs_sim* s, double dt64, bool rebuild, int& K) {
+  const float dt = (float)dt64;  // VectorN * Scalar narrows dt (vector.hpp:264-267)
   const bool pol = s->d.has_polarity != 0;
   const bool sym = s->d.symmetric != 0;
   const bool com = s->d.com_fix != 0;
-  // the old velocities are written by k_finish, after every pass that reads them
-  const bool fused = !com && !sym && !s->ov;
+  // the old velocities are written by k_finish, after every pass that reads
+  // them; the extra fields are updated there (the built-in passes carry none)
+  const bool fused = !com && !sym && !s->ov && !s->E;
   const unsigned L = launch_count(s);
   const unsigned gb = ceil_div(L ? L : 1, 256);
   const int D = s->d.dims;
@@ -449,15 +463,18 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     if (enqueue_rebuild(s, K, !s->fuse_count)) return -1;
   } else {
     PROF_BEGIN(s);
-    k_refresh<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, pol ? s->PA : nullptr, s->B, pol ? s->PB : nullptr);
+    k_refresh<<<gb, 256, 0, s->stream>>>(s->ctr, s->A, pol ? s->PA : nullptr, s->B, pol ? s->PB : nullptr,
+                                         extra_move(s));
     PROF_END(s, "k_refresh");
     K += 1;
   }
-  PassArgs a = base_args(s, dt);
+  PassArgs a = base_args(s, dt, dt64);
   auto store_args = [&](PassArgs& p, float4* dout, float2* dpout, int slot) {
     p.mode = kStore;
     p.d_out = dout;
     p.dp_out = pol ? dpout : nullptr;
+    p.ed_out = slot == 0 ? s->ed1 : s->ed2;
+    p.EX = slot == 0 ? s->EB : s->Et;
     p.com_part = (com && !sym) ? s->com_part : nullptr;
     p.com_out = s->com + 4 * slot;
     p.com_slot = slot;
@@ -479,11 +496,15 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
     prof_mark(s, 1, "k_com");
     K += 1;
   };
-  PassArgs fin = base_args(s, dt);
+  PassArgs fin = base_args(s, dt, dt64);
   fin.Bx = s->B;
   fin.Bp = pol ? s->PB : nullptr;
   fin.d1 = s->d1;
   fin.dp1 = pol ? s->dp1 : nullptr;
+  fin.EBx = s->EB;
+  fin.ed1 = s->ed1;
+  fin.ed2 = s->d.integrator == TECS_HEUN ? s->ed2 : nullptr;
+  fin.Et = s->Et;
 
   if (s->d.integrator == TECS_EULER) {
     PassArgs p = a;
@@ -523,7 +544,7 @@ int enqueue_step(tecs_sim* s, float dt, bool rebuild, int& K) {
       sym_com(s->d1, 0);
       PROF_BEGIN(s);
       k_predict<<<gb, 256, 0, s->stream>>>(s->ctr, s->com, dt, s->B, pol ? s->PB : nullptr, s->d1,
-                                           pol ? s->dp1 : nullptr, s->Xt, pol ? s->Pt : nullptr);
+                                           pol ? s->dp1 : nullptr, s->Xt, pol ? s->Pt : nullptr, fin);
       PROF_END(s, "k_predict");
       K += 1;
     }
@@ -696,7 +717,8 @@ int tecs_sim_destroy(tecs_sim* s) {
   if (s->hctr) cudaFreeHost(s->hctr);
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
-                  s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of, s->ov};
+                  s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of, s->ov, s->EA, s->EB, s->Et,
+                  s->ed1, s->ed2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -707,7 +729,26 @@ int tecs_sim_destroy(tecs_sim* s) {
 // A new state from positions (and polarities) the device can read: one
 // k_upload pass.  The delta buffers need no reset: every pass writes the
 // deltas of all active cells before they are read.
+namespace {
+// the extra fields of the n_old current cells into cell-id order (the upload
+// puts cell i at slot i): EA -> Et by A's ids, then back
+__global__ void k_extra_to_id(const float4* __restrict__ A, unsigned n_old, unsigned E, size_t C,
+                              const float* __restrict__ EA, float* __restrict__ tmp) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n_old; s += gridDim.x * blockDim.x) {
+    const unsigned id = id_of(A[s]);
+    for (unsigned k = 0; k < E; ++k) tmp[k * C + id] = EA[k * C + s];
+  }
+}
+}  // namespace
+
 static int upload_common(tecs_sim* s, const float* pos, const float2* pol, unsigned n) {
+  if (s->E && s->n_host) {
+    // Xt is free between steps; its extras partner Et takes the copy
+    k_extra_to_id<<<ceil_div(s->n_host, 256), 256, 0, s->stream>>>(s->A, s->n_host, s->E, s->d.capacity, s->EA,
+                                                                   s->Et);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(s->EA, s->Et, (size_t)s->E * s->d.capacity * 4, cudaMemcpyDeviceToDevice, s->stream));
+  }
   // the first rebuild expects the bin counts of A, and their chunk totals,
   // to be made already
   const unsigned len = s->g.nbins + 1;
@@ -763,7 +804,6 @@ int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
   if (!s) return fail("null simulation");
   if (n_steps < 0) return fail("negative step count");
   CK(cudaSetDevice(s->d.device));
-  const float fdt = (float)dt;  // VectorN * Scalar narrows dt (vector.hpp:264-267)
   for (int it = 0; it < n_steps; ++it) {
     // binned_gabriel.hpp:83-89: rebuild when step_count == 0 || step_count >= rebuild_every_n;
     // division resets the counter every step (set_agent_count, :61-64)
@@ -775,20 +815,20 @@ int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
     if (!s->use_graph) {
       int K = 0;
       s->prof_n = 0;
-      if (enqueue_step(s, fdt, rebuild, K)) return -1;
+      if (enqueue_step(s, dt, rebuild, K)) return -1;
       s->last_kernels = K;
       s->prof_last = s->prof_n;
       if (rebuild) s->sorted = true;
       continue;
     }
-    if (!s->gexec[gk] || s->gdt[gk] != fdt) {
+    if (!s->gexec[gk] || s->gdt[gk] != dt) {
       if (s->gexec[gk]) { cudaGraphExecDestroy(s->gexec[gk]); s->gexec[gk] = nullptr; }
       cudaGraph_t graph;
       CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
       int K = 0;
       s->prof_n = 0;
       g_capturing = true;
-      int rc = enqueue_step(s, fdt, rebuild, K);
+      int rc = enqueue_step(s, dt, rebuild, K);
       g_capturing = false;
       s->prof_last = s->prof_n;
       cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
@@ -797,7 +837,7 @@ int tecs_sim_step(tecs_sim* s, double dt, int n_steps) {
       e = cudaGraphInstantiate(&s->gexec[gk], graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) return fail(std::string("graph instantiate: ") + cudaGetErrorString(e));
-      s->gdt[gk] = fdt;
+      s->gdt[gk] = dt;
       s->kernels[gk] = K;
     }
     CK(cudaGraphLaunch(s->gexec[gk], s->stream));
@@ -1005,6 +1045,96 @@ int tecs_sim_set_old_velocities(tecs_sim* s, const float* v, unsigned n) {
   return 0;
 }
 
+namespace {
+// one extra field (components [offset, offset + width)) of the n active
+// cells, by cell id: device block <-> AoS rows of width floats
+__global__ void k_extra_out(const float4* __restrict__ A, unsigned n, size_t C, const float* __restrict__ EA,
+                            unsigned offset, unsigned width, float* __restrict__ out) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const unsigned id = id_of(A[s]);
+    for (unsigned c = 0; c < width; ++c) out[(size_t)id * width + c] = EA[(offset + c) * C + s];
+  }
+}
+__global__ void k_extra_in(const float4* __restrict__ A, unsigned n, size_t C, float* __restrict__ EA,
+                           unsigned offset, unsigned width, const float* __restrict__ in) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const unsigned id = id_of(A[s]);
+    for (unsigned c = 0; c < width; ++c) EA[(offset + c) * C + s] = in[(size_t)id * width + c];
+  }
+}
+}  // namespace
+
+int tecs_sim_set_extra_fields(tecs_sim* s, unsigned components, uint32_t double_mask) {
+  if (!s) return fail("null simulation");
+  if (components > kMaxExtra) return fail("at most 8 extra components per cell");
+  if (components && s->d.symmetric) return fail("extra fields are carried with the non-symmetric finders");
+  if (components == s->E && double_mask == s->ex_dbl) return 0;
+  CK(cudaSetDevice(s->d.device));
+  CK(cudaStreamSynchronize(s->stream));
+  drop_graphs(s);
+  for (float** p : {&s->EA, &s->EB, &s->Et, &s->ed1, &s->ed2}) {
+    if (*p) CK(cudaFree(*p));
+    *p = nullptr;
+  }
+  s->E = components;
+  s->ex_dbl = components ? double_mask & ((1u << components) - 1u) : 0u;
+  if (!components) return 0;
+  const size_t bytes = (size_t)components * s->d.capacity * 4;
+  for (float** p : {&s->EA, &s->EB, &s->Et, &s->ed1, &s->ed2}) {
+    CK(cudaMalloc(p, bytes));
+    CK(cudaMemsetAsync(*p, 0, bytes, s->stream));
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+static int extra_check(tecs_sim* s, unsigned offset, unsigned width) {
+  if (!s) return fail("null simulation");
+  if (!width || offset + width > s->E) return fail("extra field outside the extra components");
+  return 0;
+}
+
+int tecs_sim_upload_extra(tecs_sim* s, unsigned offset, unsigned width, const float* values, unsigned n) {
+  if (extra_check(s, offset, width)) return -1;
+  if (!values && n) return fail("null argument");
+  if (n > s->n_host) return fail("more rows than active cells");
+  if (!n) return 0;
+  CK(cudaSetDevice(s->d.device));
+  const size_t bytes = (size_t)n * width * 4;
+  const float* src = values;
+  cudaPointerAttributes pa{};
+  const bool on_device = cudaPointerGetAttributes(&pa, values) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  if (!on_device) {
+    // the predictor's extras are free between steps (E x capacity floats)
+    CK(cudaMemcpyAsync(s->Et, values, bytes, cudaMemcpyHostToDevice, s->stream));
+    src = s->Et;
+  }
+  k_extra_in<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, n, s->d.capacity, s->EA, offset, width, src);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+int tecs_sim_download_extra(tecs_sim* s, unsigned offset, unsigned width, float* out, unsigned* n_out) {
+  if (extra_check(s, offset, width)) return -1;
+  if (!out) return fail("null argument");
+  CK(cudaSetDevice(s->d.device));
+  unsigned n = 0;
+  if (tecs_sim_count(s, &n)) return -1;
+  if (n_out) *n_out = n;
+  if (!n) return 0;
+  cudaPointerAttributes pa{};
+  const bool on_device = cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  float* dst = on_device ? out : s->Et;
+  k_extra_out<<<ceil_div(n, 256), 256, 0, s->stream>>>(s->A, n, s->d.capacity, s->EA, offset, width, dst);
+  CK(cudaGetLastError());
+  if (!on_device) CK(cudaMemcpyAsync(out, s->Et, (size_t)n * width * 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
 int tecs_device_alloc(int device, size_t bytes, void** out) {
   if (!out) return fail("null argument");
   *out = nullptr;
@@ -1070,6 +1200,12 @@ int tecs_sim_set_pair_law(tecs_sim* s, tecs_pair_law_fn fn, void* user) {
   s->law_fn = fn;
   s->law_user = fn ? user : nullptr;
   drop_graphs(s);
+  // the built-in passes write no extra deltas: clear the user law's
+  if (s->E) {
+    CK(cudaMemsetAsync(s->ed1, 0, (size_t)s->E * s->d.capacity * 4, s->stream));
+    CK(cudaMemsetAsync(s->ed2, 0, (size_t)s->E * s->d.capacity * 4, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
   return 0;
 }
 

@@ -34,6 +34,15 @@ CREATE_SIMULATION_CONFIG(BinnedAllPairsEulerCom,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
                          CONFIG_INTEGRATOR(integrators::Euler)
                          CONFIG_COM_FIXER(com_fixers::GlobalComFixer))
+CREATE_SIMULATION_CONFIG(FieldsGabrielHeun,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
+                         CONFIG_INTEGRATOR(integrators::Heun)
+                         CONFIG_FIELDS((Vector, position), (Scalar, u), (Vector, w)))
+CREATE_SIMULATION_CONFIG(FieldsAllPairsEulerCom,
+                         CONFIG_PAIR_FINDER(pair_finders::BinnedAllPairs)
+                         CONFIG_INTEGRATOR(integrators::Euler)
+                         CONFIG_COM_FIXER(com_fixers::GlobalComFixer)
+                         CONFIG_FIELDS((Vector, position), (Scalar, u), (Vector, w)))
 CREATE_SIMULATION_CONFIG(BinnedGabrielHeun,
                          CONFIG_PAIR_FINDER(pair_finders::BinnedGabriel)
                          CONFIG_INTEGRATOR(integrators::Heun))
@@ -268,6 +277,40 @@ static int run_link_lambda(const Input& in, const std::string& out, int steps, d
   return 0;
 }
 
+// a config with a Scalar field u and a Vector field w beyond the position:
+// the pairwise law diffuses them between neighbours and drives w along the
+// displacement, the generic law adds to u from the position; writes .pos,
+// .u and .w
+template <typename FieldsConfig>
+static int run_fields(const Input& in, const std::string& out, int steps, double dt) {
+  EXTRACT_TYPES_FROM_SIMULATION_CONFIG(FieldsConfig)
+  const Scalar k_rep = in.prm[8], r_rep = in.prm[9], k_adh = in.prm[10], r_adh = in.prm[11];
+  auto law = PAIRWISE_FORCE(
+    if (distance != Scalar(0)) {
+      const Scalar F = k_rep * fmaxf(r_rep - distance, Scalar(0)) - k_adh * fmaxf(distance - r_adh, Scalar(0));
+      ctx.position.delta += displacement * F / distance;
+    }
+    ctx.u.delta += (ctx.u.other - ctx.u.self) * Scalar(0.2);
+    ctx.w.delta += (ctx.w.other - ctx.w.self) * Scalar(0.1) + displacement * Scalar(0.01);
+  );
+  auto generic = GENERIC_FORCE(ctx.u.delta += Scalar(0.05) * ctx.position.self[0];);
+  Simulation<FieldsConfig> sim(settings_of<FieldsConfig>(in));
+  auto& pos = sim.template get_view<FIELD(Vector, position)>();
+  auto& u = sim.template get_view<FIELD(Scalar, u)>();
+  auto& w = sim.template get_view<FIELD(Vector, w)>();
+  for (unsigned i = 0; i < in.n; ++i) {
+    for (int d = 0; d < 3; ++d) pos(i)[d] = in.x[std::size_t(i) * 3 + d];
+    u(i) = pos(i)[0] * Scalar(0.3) + Scalar(1);
+    w(i) = pos(i) * Scalar(0.5);
+  }
+  for (int s = 0; s < steps; ++s) sim.take_step(dt, law(), generic());
+  const unsigned n = sim.get_agent_count();
+  write_raw(out + ".pos", pos.data(), std::size_t(n) * sizeof(Vector));
+  write_raw(out + ".u", u.data(), std::size_t(n) * sizeof(Scalar));
+  write_raw(out + ".w", w.data(), std::size_t(n) * sizeof(Vector));
+  return 0;
+}
+
 // a law that draws from rng: two simulations of the same input give the same run
 static int run_rng_twice(const Input& in, const std::string& out, int steps, double dt) {
   EXTRACT_TYPES_FROM_SIMULATION_CONFIG(BinnedGabrielHeun)
@@ -335,6 +378,8 @@ int main(int argc, char** argv) {
     if (scenario == "lk_lambda_ba_euler_com") return run_link_lambda<BinnedAllPairsEulerCom>(in, out, steps, dt);
     if (scenario == "rng_twice") return run_rng_twice(in, out, steps, dt);
     if (scenario == "drag_bg_heun") return run_drag<BinnedGabrielHeun>(in, out, steps, dt);
+    if (scenario == "fields_bg_heun") return run_fields<FieldsGabrielHeun>(in, out, steps, dt);
+    if (scenario == "fields_ba_euler_com") return run_fields<FieldsAllPairsEulerCom>(in, out, steps, dt);
     if (scenario == "drag_ba_euler_com") return run_drag<BinnedAllPairsEulerCom>(in, out, steps, dt);
   } catch (const Error& e) {
     std::fprintf(stderr, "tecs error: %s\n", e.what());

@@ -68,6 +68,9 @@ SCENARIOS = {
     "drag_ba_euler_com": ("drag_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
     # update functions between steps (run, run_links, init): positions, links, a DeviceVar count
     "upd_bg_heun": ("upd_bg_heun_3", 3, 0, 1, 0, 3, 0),
+    # a config with a Scalar and a Vector field beyond the position: pos, u, w
+    "fields_bg_heun": ("fields_bg_heun_3", 3, 0, 1, 0, 3, 0),
+    "fields_ba_euler_com": ("fields_ba_euler_com_3", 1, 0, 0, 1, 3, 0),
 }
 
 
@@ -169,6 +172,12 @@ def inputs(name):
         x = wl.ball(2000, 19)
         mn, mx = wl.bounds_for(x)
         steps, dt = 10, 0.05
+    elif name in ("fields_bg_heun", "fields_ba_euler_com"):
+        x = wl.ball(1500, 24 if name == "fields_bg_heun" else 25)
+        mn, mx = wl.bounds_for(x)
+        steps, dt = 10, 0.05
+        if name == "fields_ba_euler_com":
+            prm[13] = 1600
     elif name == "upd_bg_heun":
         x = wl.ball(800, 23)
         mn, mx = wl.bounds_for(x)
@@ -337,6 +346,9 @@ def run(name):
             pass
         elif scen.startswith("drag_"):
             res["ov"] = np.fromfile(f"{out}.ov", np.float32).reshape(-1, dims)
+        elif scen.startswith("fields_"):
+            res["u"] = np.fromfile(f"{out}.u", np.float32)
+            res["w"] = np.fromfile(f"{out}.w", np.float32).reshape(-1, dims)
         elif scen.startswith("upd_"):
             res["links"] = np.fromfile(f"{out}.links", np.uint32).reshape(-1, 2)
             res["hits"] = np.fromfile(f"{out}.hits", np.int32)

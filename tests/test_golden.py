@@ -48,7 +48,8 @@ WRITER = ["lk_writer", "lk_writer_nolinks"]
 # fixtures of a GENERIC_FORCE law with the spring: the reference's final state,
 # which the user-law program reproduces on a GPU (tests/test_user_laws.py);
 # the C restatement has built-in laws only
-USER_LAW = ["gen_bg_heun", "drag_bg_heun", "drag_ba_euler_com", "upd_bg_heun"]
+USER_LAW = ["gen_bg_heun", "drag_bg_heun", "drag_ba_euler_com", "upd_bg_heun", "fields_bg_heun",
+            "fields_ba_euler_com"]
 # fixtures of the reference's standalone acceleration::Grid queries
 GRID = ["grid_q_3d", "grid_q_2d"]
 # output of five of the reference's example programs run on its headers

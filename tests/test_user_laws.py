@@ -153,6 +153,27 @@ def test_link_force_lambda_reproduces_reference(driver, tmp_path, scenario, name
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name,exact", [("fields_bg_heun", True), ("fields_ba_euler_com", False)])
+def test_config_with_extra_fields_reproduces_reference(driver, tmp_path, name, exact):
+    """CONFIG_FIELDS((Vector, position), (Scalar, u), (Vector, w)): laws that read and write u and w through
+    ctx, and the integrators updating every field (the Scalar field in double, as the reference's float +=
+    float * double dt).  Ten steps bit for bit against the reference's run (within the COM tolerance with
+    the COM fix, which moves the positions and so the w term of the law)."""
+    g, out, r = run(driver, name, name, tmp_path)
+    assert r.returncode == 0, r.stderr
+    pos = np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3)
+    u = np.fromfile(f"{out}.u", np.float32)
+    w = np.fromfile(f"{out}.w", np.float32).reshape(-1, 3)
+    assert not np.array_equal(u, g["x0"][:, 0] * np.float32(0.3) + np.float32(1))  # u evolved
+    if exact:
+        np.testing.assert_array_equal(pos, g["pos"])
+        np.testing.assert_array_equal(u, g["u"])
+        np.testing.assert_array_equal(w, g["w"])
+    else:
+        assert close(pos, g["pos"]) and close(u, g["u"]) and close(w, g["w"])
+
+
+@pytest.mark.gpu
 def test_generic_law_with_pairwise_law_reproduces_reference(driver, tmp_path):
     """take_step(dt, PAIRWISE_FORCE(...)(), GENERIC_FORCE(...)()): the generic law (is_full_step-dependent,
     reading ctx.position.self) is added before the pair sums, as the reference fuses them; bit for bit."""
