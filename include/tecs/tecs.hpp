@@ -6,6 +6,8 @@
 
 #include "components.hpp"
 #include "config.hpp"
+#include "grid.hpp"
+#include "hdf5_reader.hpp"
 #include "kokkos_compat.hpp"
 #include "plane.hpp"
 #include "random.hpp"

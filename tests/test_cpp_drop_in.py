@@ -278,3 +278,29 @@ def test_update_functions_between_steps_reproduce_reference(driver, tmp_path):
     np.testing.assert_array_equal(np.fromfile(f"{out}.links", np.uint32).reshape(-1, 2), g["links"])
     np.testing.assert_array_equal(np.fromfile(f"{out}.hits", np.int32), g["hits"])
     np.testing.assert_array_equal(np.fromfile(f"{out}.pos", np.float32).reshape(-1, 3), g["pos"])
+
+
+@pytest.mark.parametrize("name,dims", [("grid_q_3d", 3), ("grid_q_2d", 2)])
+def test_host_grid_matches_reference_queries(name, dims, tmp_path):
+    """tecs::acceleration::Grid (include/tecs/grid.hpp, the host grid that update functions query) on the
+    reference's grid-query fixtures: every query result equal, with the fixtures' stub generator."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    g = dict(np.load(GOLDEN / f"{name}.npz"))
+    exe = tmp_path / "grid_host"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}",
+                        str(ROOT / "tests" / "cpp" / "grid_host.cpp"), *link_flags(), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(inp, "wb") as f:
+        np.array([len(g["x"]), len(g["q"])], np.uint32).tofile(f)
+        g["prm"].astype(np.float32).tofile(f)
+        g["x"].astype(np.float32).tofile(f)
+        g["q"].astype(np.float32).tofile(f)
+        g["draws"].astype(np.uint32).tofile(f)
+    r = subprocess.run([str(exe), str(dims), str(inp), str(out)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    res = np.fromfile(out, np.int32).reshape(-1, 5)
+    for k, key in enumerate(("near1", "near2", "rbins", "rrad", "rfilt")):
+        np.testing.assert_array_equal(res[:, k], g[key], err_msg=key)

@@ -172,3 +172,4 @@ def test_oracle_grid_queries_match_reference(name):
                             float(prm[1]))
     for k in ("near1", "near2", "rbins", "rrad", "rfilt"):
         np.testing.assert_array_equal(out[k], g[k], err_msg=k)
+

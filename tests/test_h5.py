@@ -276,3 +276,72 @@ def test_sink_append_keeps_earlier_snapshots_and_sidecar(tmp_path):
     two.close()
     for name in ("request_00009.h5", "request_00009.xmf"):
         assert (tmp_path / "two" / name).read_bytes() == (tmp_path / "one" / name).read_bytes()
+
+
+def _cpp_reader(tmp_path):
+    import shutil
+    import subprocess
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    import tecs_gb300 as tg
+
+    root = Path(__file__).resolve().parents[1]
+    lib = Path(tg.library_path())
+    exe = tmp_path / "h5_reader"
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}",
+                        str(root / "tests" / "cpp" / "h5_reader.cpp"), f"-L{lib.parent}", "-l" + lib.stem[3:],
+                        f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def _cpp_read(exe, path, name, kind, tmp_path):
+    import subprocess
+
+    out = tmp_path / f"{name.replace('/', '_')}.bin"
+    r = subprocess.run([str(exe), str(path), name, kind, str(out)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    dims = tuple(int(v) for v in r.stdout.split())
+    dtype = np.int32 if kind == "int" else np.float32
+    cols = {"vec3": 3, "polarity": 2, "float": 1, "int": 1}[kind]
+    return dims, np.fromfile(out, dtype).reshape(-1, cols) if cols > 1 else np.fromfile(out, dtype)
+
+
+def test_cpp_reader_reads_the_codecs_files(tmp_path):
+    """io::HDF5_Reader (include/tecs/hdf5_reader.hpp) against the Python codec's files: float32 rows,
+    int32 and uint32 datasets converted into float and int views, in nested groups."""
+    tg = pytest.importorskip("tecs_gb300")
+    del tg
+    exe = _cpp_reader(tmp_path)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((300, 3)).astype(np.float32)
+    p = rng.standard_normal((300, 2)).astype(np.float32)
+    t = rng.integers(-5, 5, 300).astype(np.int32)
+    u = rng.integers(0, 1000, 300).astype(np.uint32)
+    w = h5.H5Writer(tmp_path / "in.h5")
+    w.write_group("t0", {"position": x, "polarity": p, "cell_type": t, "ids": u})
+    w.close()
+    dims, got = _cpp_read(exe, tmp_path / "in.h5", "t0/position", "vec3", tmp_path)
+    assert dims == (300, 3)
+    np.testing.assert_array_equal(got, x)
+    np.testing.assert_array_equal(_cpp_read(exe, tmp_path / "in.h5", "t0/polarity", "polarity", tmp_path)[1], p)
+    np.testing.assert_array_equal(_cpp_read(exe, tmp_path / "in.h5", "t0/cell_type", "int", tmp_path)[1], t)
+    np.testing.assert_array_equal(_cpp_read(exe, tmp_path / "in.h5", "t0/cell_type", "float", tmp_path)[1],
+                                  t.astype(np.float32))
+    np.testing.assert_array_equal(_cpp_read(exe, tmp_path / "in.h5", "t0/ids", "int", tmp_path)[1], u.astype(np.int32))
+
+
+def test_cpp_reader_reads_library_written_fixture(tmp_path):
+    """The reference's library-written initial state (examples/data/sphere_ic.h5) through the C++ reader
+    equals the Python reader's."""
+    path = FIXTURES[0]
+    if not path.exists():
+        pytest.skip("reference fixtures not present")
+    exe = _cpp_reader(tmp_path)
+    f = h5.H5File(path)
+    for name, kind in (("POINTS", "vec3"), ("polarity", "polarity"), ("cell_type", "int")):
+        dims, got = _cpp_read(exe, path, name, kind, tmp_path)
+        ref = f.read(name)
+        assert dims == ref.shape
+        np.testing.assert_array_equal(got, ref)

@@ -2,7 +2,7 @@
 
 Two parts:
 
-  * compile: eighteen of the reference's own programs (COMPILED, from its
+  * compile: nineteen of the reference's own programs (COMPILED, from its
     examples/) are copied byte for byte into a directory examples/ next to a
     link include/ -> this repository's include/, so that their
     "../include/tecs.hpp" is the drop-in layer's, and compiled by nvcc
@@ -51,11 +51,12 @@ PROGRAMS = ["springs", "epithelium", "polarization", "growth_w_wall", "delaunay_
 # the five above, and programs using the other initialisers (line, cuboid,
 # hexagon, rectangle, disk, relaxed cuboid), LINK_FORCE and UPDATE_FUNC with
 # run / run_links, drag, set_capacity, extra int views, the polarity laws
-# (apical constriction, migration) and fields beyond the position and the
-# polarity (Scalar fields, a second polarity)
+# (apical constriction, migration), fields beyond the position and the
+# polarity (Scalar fields, a second polarity), the host grid's random
+# neighbour queries and the HDF5 reader
 COMPILED = PROGRAMS + ["apical_constriction", "bending", "branching", "delaunay", "delaunay_sheet",
                        "epithelia_double_polarity", "gradient", "growth_w_squeeze", "intercalation",
-                       "lineage_tracing", "migration", "passive_growth", "turing"]
+                       "intercalation_w_gradient", "lineage_tracing", "migration", "passive_growth", "turing"]
 
 
 def program_source(name):
