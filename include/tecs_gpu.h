@@ -271,6 +271,74 @@ int tecs_engine_kernels_per_step(tecs_engine* engine, int* kernels);
 void* tecs_engine_stream(tecs_engine* engine);
 
 /* ------------------------------------------------------------------------
+ * Served stream: a continuous-batching request loop over engines, run by a
+ * server thread of this library.  No counterpart in the reference (it runs
+ * one Simulation per program).  Requests (a tecs_sim_desc with its state and
+ * step count) are submitted from any thread; the server admits each as soon
+ * as its lane's engine has free cells and a free run of bins (first come,
+ * first served), steps every lane's resident simulations together (each lane
+ * on its own stream with at most in_flight step batches queued, never past a
+ * resident request's next snapshot or end), writes a snapshot every
+ * snapshot_every steps (unpacked on the device, copied to pinned memory on a
+ * side stream, written as HDF5 by a writer thread: <dir>/request_<tag>.h5,
+ * group t<step>, datasets position and polarity), and retires a request at
+ * its step count, keeping its final state for tecs_serve_fetch.
+ * ------------------------------------------------------------------------ */
+typedef struct tecs_serve_desc {
+  int device;
+  unsigned cell_capacity;        /* cells of all lanes together                      */
+  unsigned bin_capacity;         /* bins of all lanes together                       */
+  unsigned max_sims;             /* resident simulations per lane at most            */
+  double dt;                     /* the step of every request                        */
+  unsigned snapshot_every;       /* 0: no snapshots                                  */
+  const char* snapshot_dir;      /* NULL: snapshots are copied but not written       */
+  unsigned n_lanes;              /* 1 to 4 size classes                              */
+  unsigned lane_max_cells[4];    /* largest request of each lane (last lane: 0, any) */
+  float lane_share[4];           /* each lane's share of the capacities              */
+  unsigned steps_per_issue;      /* steps per engine call at most (>= 1)             */
+  unsigned in_flight;            /* step batches queued per lane at most (>= 1)      */
+} tecs_serve_desc;
+
+typedef struct tecs_serve_result {
+  uint64_t id;
+  uint64_t tag;                  /* the caller's name for the request (submit)       */
+  unsigned cells;
+  unsigned steps;                /* steps run (the request's, less its start step)   */
+  double arrival_s, admitted_s, completed_s;  /* seconds since tecs_serve_create     */
+} tecs_serve_result;
+
+typedef struct tecs_serve_stats {
+  unsigned long long cell_steps; /* cells x steps of every request so far            */
+  unsigned long long engine_steps;
+  unsigned long long snapshots_written;
+  unsigned long long snapshot_errors;
+  unsigned submitted, completed, resident, waiting;
+} tecs_serve_stats;
+
+typedef struct tecs_serve tecs_serve;
+
+int tecs_serve_desc_default(tecs_serve_desc* desc);
+int tecs_serve_create(const tecs_serve_desc* desc, tecs_serve** out);
+/* Queue a request: its state (host memory, copied), its step count and the
+ * step it starts from (a resumed request: its snapshots and its end fall on
+ * the same steps as in an uninterrupted run).  tag is the caller's name for
+ * it: its snapshots go to <snapshot_dir>/request_<tag, 5 digits>.h5 (a new
+ * file).  *id receives the server's name for it. */
+int tecs_serve_submit(tecs_serve* server, const tecs_sim_desc* desc, const float* positions, const float* polarity,
+                      unsigned n, unsigned steps, unsigned start_step, uint64_t tag, uint64_t* id);
+/* Results completed since the last call, up to capacity; *n receives the count. */
+int tecs_serve_poll(tecs_serve* server, tecs_serve_result* results, unsigned capacity, unsigned* n);
+/* A completed request's final state in cell-id order; fails for an unknown or
+ * unfinished request.  The state is released after the fetch. */
+int tecs_serve_fetch(tecs_serve* server, uint64_t id, float* positions, float* polarity, unsigned* n);
+/* Waits until every submitted request has completed and every snapshot is
+ * written, or timeout_s passes (then fails). */
+int tecs_serve_drain(tecs_serve* server, double timeout_s);
+int tecs_serve_stats_get(tecs_serve* server, tecs_serve_stats* stats);
+/* Stops the server thread (resident requests are dropped) and frees everything. */
+int tecs_serve_destroy(tecs_serve* server);
+
+/* ------------------------------------------------------------------------
  * Standalone bin grid: acceleration::Grid (include/utils/grid.hpp:29-638),
  * the grid user forces query for the nearest point or a random neighbour
  * (examples/tribolium/main.cpp:84-95, intercalation_w_gradient.cpp:73-91).

@@ -19,7 +19,7 @@ LIB = BUILD / "libtecs_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so the pair predicates and the
 # force sums keep the reference's rounding (Serial backend, no FMA).
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-shared"]
+NVCC_FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-shared"]
 
 
 def nvcc() -> str:

@@ -22,6 +22,7 @@ at their own rate while the large ones run alongside on the same GPU.
 from __future__ import annotations
 
 import collections
+import ctypes
 import json
 import math
 import os
@@ -355,6 +356,157 @@ class Server:
             lane.engine.close()
 
 
+class _ServeDesc(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("cell_capacity", ctypes.c_uint), ("bin_capacity", ctypes.c_uint),
+                ("max_sims", ctypes.c_uint), ("dt", ctypes.c_double), ("snapshot_every", ctypes.c_uint),
+                ("snapshot_dir", ctypes.c_char_p), ("n_lanes", ctypes.c_uint),
+                ("lane_max_cells", ctypes.c_uint * 4), ("lane_share", ctypes.c_float * 4),
+                ("steps_per_issue", ctypes.c_uint), ("in_flight", ctypes.c_uint)]
+
+
+class _ServeResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("tag", ctypes.c_uint64), ("cells", ctypes.c_uint), ("steps", ctypes.c_uint),
+                ("arrival_s", ctypes.c_double), ("admitted_s", ctypes.c_double), ("completed_s", ctypes.c_double)]
+
+
+class _ServeStats(ctypes.Structure):
+    _fields_ = [("cell_steps", ctypes.c_ulonglong), ("engine_steps", ctypes.c_ulonglong),
+                ("snapshots_written", ctypes.c_ulonglong), ("snapshot_errors", ctypes.c_ulonglong),
+                ("submitted", ctypes.c_uint), ("completed", ctypes.c_uint), ("resident", ctypes.c_uint),
+                ("waiting", ctypes.c_uint)]
+
+
+def _serve_lib():
+    L = tg.load()
+    if getattr(L, "_serve_bound", False):
+        return L
+    vp = ctypes.c_void_p
+    L.tecs_serve_desc_default.argtypes = [ctypes.POINTER(_ServeDesc)]
+    L.tecs_serve_create.argtypes = [ctypes.POINTER(_ServeDesc), ctypes.POINTER(vp)]
+    L.tecs_serve_submit.argtypes = [vp, ctypes.POINTER(tg.SimDesc), vp, vp, ctypes.c_uint, ctypes.c_uint,
+                                    ctypes.c_uint, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    L.tecs_serve_poll.argtypes = [vp, ctypes.POINTER(_ServeResult), ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]
+    L.tecs_serve_fetch.argtypes = [vp, ctypes.c_uint64, vp, vp, ctypes.POINTER(ctypes.c_uint)]
+    L.tecs_serve_drain.argtypes = [vp, ctypes.c_double]
+    L.tecs_serve_stats_get.argtypes = [vp, ctypes.POINTER(_ServeStats)]
+    L.tecs_serve_destroy.argtypes = [vp]
+    for name in ("tecs_serve_desc_default", "tecs_serve_create", "tecs_serve_submit", "tecs_serve_poll",
+                 "tecs_serve_fetch", "tecs_serve_drain", "tecs_serve_stats_get", "tecs_serve_destroy"):
+        getattr(L, name).restype = ctypes.c_int
+    L._serve_bound = True
+    return L
+
+
+class NativeServer:
+    """The served loop of the library (include/tecs_gpu.h, tecs_serve_*): the same admission, lanes,
+    multi-step issue, snapshots and retirement as Server, run by a server thread in the library, with
+    snapshots written as HDF5 by its own writer thread (<snapshot_dir>/request_<index>.h5, the request's
+    index in the list, as SnapshotSink names them; a resumed request starts a new file).  This thread only
+    submits requests at their arrival times and collects the results."""
+
+    def __init__(self, cell_capacity: int, bin_capacity: int, max_sims: int = 1024, snapshot_every: int = 100,
+                 dt: float = 0.05, snapshot_dir=None, keep_results: bool = False, device: int = 0,
+                 size_classes=None, steps_per_issue: int = 1, in_flight: int = IN_FLIGHT):
+        L = _serve_lib()
+        classes = size_classes or [(None, 1.0)]
+        if classes[-1][0] is not None:
+            raise ValueError("the last size class must take any request (None)")
+        d = _ServeDesc()
+        tg._check(L.tecs_serve_desc_default(ctypes.byref(d)))
+        d.device = device
+        d.cell_capacity = int(cell_capacity)
+        d.bin_capacity = int(bin_capacity)
+        d.max_sims = int(max_sims)
+        d.dt = float(dt)
+        d.snapshot_every = int(snapshot_every)
+        self._dir = None if snapshot_dir is None else str(snapshot_dir).encode()
+        d.snapshot_dir = self._dir
+        d.n_lanes = len(classes)
+        for k, (m, share) in enumerate(classes):
+            d.lane_max_cells[k] = 0 if m is None else int(m)
+            d.lane_share[k] = float(share)
+        d.steps_per_issue = int(steps_per_issue)
+        d.in_flight = int(in_flight)
+        h = ctypes.c_void_p()
+        tg._check(L.tecs_serve_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self.size_classes = classes
+        self.dt = dt
+        self.keep_results = keep_results
+        self.cell_steps = 0
+        self.steps = 0
+        self.makespan = 0.0
+        self.written = 0
+
+    def run(self, requests: List[wl.Request], time_scale: float = 1.0, max_cells: Optional[int] = None,
+            resume: Optional[Dict[int, tuple]] = None, timeout_s: float = 3600.0):
+        """Serve the requests (arrival times divided by time_scale); returns the results, as Server.run."""
+        L = _serve_lib()
+        resume = resume or {}
+        reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival_s)
+        built = {}
+        for idx, r in reqs:
+            x, p, d, _, _ = request_sim(r, max_cells)
+            start = 0
+            if idx in resume:
+                start, pos, pol = resume[idx]
+                if len(pos) != len(x) or (pol is None) != (p is None) or not 0 <= start <= r.steps:
+                    raise ValueError(f"resume state of request {idx} does not match the request")
+                x = np.ascontiguousarray(pos, np.float32)
+                p = None if pol is None else np.ascontiguousarray(pol, np.float32)
+            built[idx] = (np.ascontiguousarray(x, np.float32),
+                          None if p is None else np.ascontiguousarray(p, np.float32), d, start)
+        ids = {}
+        t0 = time.perf_counter()
+        for idx, r in reqs:
+            wait = r.arrival_s / time_scale - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            x, p, d, start = built[idx]
+            rid = ctypes.c_uint64()
+            tg._check(L.tecs_serve_submit(self._h, ctypes.byref(d), tg._ptr(x), tg._ptr(p), len(x), r.steps, start,
+                                          idx, ctypes.byref(rid)))
+            ids[rid.value] = idx
+        tg._check(L.tecs_serve_drain(self._h, float(timeout_s)))
+        self.makespan = time.perf_counter() - t0
+        results: List[Result] = []
+        buf = (_ServeResult * 256)()
+        n = ctypes.c_uint()
+        while True:
+            tg._check(L.tecs_serve_poll(self._h, buf, 256, ctypes.byref(n)))
+            if n.value == 0:
+                break
+            for k in range(n.value):
+                rr = buf[k]
+                idx = ids[rr.id]
+                res = Result(idx, rr.cells, requests[idx].steps, rr.arrival_s, rr.admitted_s, rr.completed_s)
+                if self.keep_results:
+                    x = np.empty((rr.cells, 3), np.float32)
+                    p = np.empty((rr.cells, 2), np.float32) if built[idx][1] is not None else None
+                    cnt = ctypes.c_uint()
+                    tg._check(L.tecs_serve_fetch(self._h, rr.id, tg._ptr(x), tg._ptr(p), ctypes.byref(cnt)))
+                    res.positions, res.polarity = x, p
+                results.append(res)
+        st = _ServeStats()
+        tg._check(L.tecs_serve_stats_get(self._h, ctypes.byref(st)))
+        self.cell_steps = st.cell_steps
+        self.steps = st.engine_steps
+        self.written = st.snapshots_written
+        self.request_of = ids
+        return sorted(results, key=lambda r: r.index)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _serve_lib().tecs_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def resume_points(directory, indices) -> Dict[int, tuple]:
     """{request index: (step, positions, polarity)} from the newest snapshots in `directory`, for the
     requests that have one."""
@@ -428,8 +580,6 @@ def bench_main(args):
     """bench.py --workload served: the served stream on one GPU."""
     import torch
 
-    from tecs_gb300 import h5
-
     rank, world, local = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(
         os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
@@ -439,9 +589,9 @@ def bench_main(args):
     out_dir = Path(os.environ.get("TECS_SNAPSHOT_DIR", "/tmp/tecs_snapshots"))
     out_dir.mkdir(parents=True, exist_ok=True)
     dt = 0.05
-    sink = h5.SnapshotSink(out_dir, dt=dt)  # HDF5 files and their XDMF sidecars
-    srv = Server(cells, bins, max_sims=4096, snapshot_every=100, dt=dt, sink=sink, size_classes=BENCH_SIZE_CLASSES,
-                 steps_per_issue=8)
+    # the library's own loop (tecs_serve_*): server and HDF5 writer threads in C++
+    srv = NativeServer(cells, bins, max_sims=4096, snapshot_every=100, dt=dt, snapshot_dir=out_dir,
+                       size_classes=BENCH_SIZE_CLASSES, steps_per_issue=8)
     res = srv.run(reqs, time_scale=args.time_scale)
     summ = summarize(res, srv.makespan, srv.cell_steps)
     small = [r for r in res if r.n <= BENCH_SIZE_CLASSES[0][0]]
@@ -449,14 +599,13 @@ def bench_main(args):
     by_class = {name: {"requests": len(rs), "p50_s": float(np.percentile([r.latency for r in rs], 50)),
                        "p99_s": float(np.percentile([r.latency for r in rs], 99))}
                 for name, rs in (("small", small), ("large", large)) if rs}
-    written = srv.writer.written
+    written = srv.written
     srv.close()
-    sink.close()
     plain_v, rows = plain_sample(reqs)
     plain_lat = plain_fcfs_latency(reqs, rows, args.time_scale)
     # capacity: the same stream with arrivals compressed 100 times (compute-bound)
-    cap_srv = Server(cells, bins, max_sims=4096, snapshot_every=10 ** 9, dt=dt, sink=None,
-                     size_classes=BENCH_SIZE_CLASSES, steps_per_issue=8)
+    cap_srv = NativeServer(cells, bins, max_sims=4096, snapshot_every=0, dt=dt, snapshot_dir=None,
+                           size_classes=BENCH_SIZE_CLASSES, steps_per_issue=8)
     cap_res = cap_srv.run(reqs, time_scale=100.0)
     cap = summarize(cap_res, cap_srv.makespan, cap_srv.cell_steps)
     cap_srv.close()
@@ -469,7 +618,7 @@ def bench_main(args):
                                "cells log-uniform [1e3, 1e6], steps U[100, 1000], spring|polarity x euler|heun, "
                                "snapshots every 100 steps", "engine_cells": cells, "engine_bins": bins,
                    "size_classes": [{"max_request_cells": m, "capacity_share": f} for m, f in BENCH_SIZE_CLASSES],
-                   "steps_per_issue": 8},
+                   "steps_per_issue": 8, "loop": "tecs_serve_* (server and HDF5 writer threads in the library)"},
         "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_s": summ["mean_s"],
                     "by_size_class": by_class},
         "capacity": {"value": cap["cell_steps_per_s"], "makespan_s": cap["makespan_s"],

@@ -12,17 +12,17 @@ import pytest
 import tecs_gb300 as tg
 from tecs_gb300 import h5
 from tecs_gb300 import workloads as wl
-from tecs_gb300.served import Server, request_sim, summarize
+from tecs_gb300.served import NativeServer, Server, request_sim, summarize
 
 pytestmark = pytest.mark.gpu
 
 
-def alone(req, max_cells):
+def alone(req, max_cells, steps=None):
     x, p, d, settings, force = request_sim(req, max_cells)
     s = tg.Simulation(settings, pair_finder="binned_gabriel", integrator=req.integrator, force=force,
                       polarity=p is not None)
     s.set_state(x, p)
-    s.take_step(0.05, req.steps)
+    s.take_step(0.05, req.steps if steps is None else steps)
     return s.get_state()
 
 
@@ -122,3 +122,60 @@ def test_resume_from_snapshots_gives_the_uninterrupted_results(tmp_path):
         np.testing.assert_array_equal(r.positions, full[r.index].positions)
         if full[r.index].polarity is not None:
             np.testing.assert_array_equal(r.polarity, full[r.index].polarity)
+
+
+@pytest.mark.parametrize("lanes,per_issue", [(None, 1), ([(3000, 0.3), (None, 0.7)], 8)])
+def test_native_server_results_and_snapshots(tmp_path, lanes, per_issue):
+    """The library's own served loop (tecs_serve_*: server and writer threads in C++): every request's result
+    equals the same simulation run alone, bit for bit, with one lane or two size-class lanes and multi-step
+    issue; the writer's HDF5 files hold one group per snapshot step, and a snapshot equals the plain run
+    stopped at that step."""
+    reqs = wl.served_stream(12, seed=9, rate_hz=300.0, lo=800, hi=12000, steps_lo=30, steps_hi=140)
+    srv = NativeServer(cell_capacity=40000, bin_capacity=240000, max_sims=16, snapshot_every=40,
+                       snapshot_dir=tmp_path, keep_results=True, size_classes=lanes, steps_per_issue=per_issue)
+    res = srv.run(reqs, time_scale=1.0)
+    srv.close()  # joins the writer: every file is closed
+    assert len(res) == len(reqs) and srv.written > 0
+    assert max(r.admitted for r in res) > min(r.completed for r in res)  # some admitted while others ran
+    for r in res:
+        req = reqs[r.index]
+        x_alone, p_alone = alone(req, None)
+        np.testing.assert_array_equal(r.positions, x_alone)
+        if p_alone is not None:
+            np.testing.assert_array_equal(r.polarity, p_alone)
+        want = [f"t{k}" for k in range(40, req.steps, 40)]
+        if not want:
+            continue
+        f = h5.H5File(tmp_path / f"request_{r.index:05d}.h5")
+        assert sorted(f.keys(), key=lambda g: int(g[1:])) == want
+        xs, ps = alone(req, None, steps=40)
+        np.testing.assert_array_equal(f.read("t40/position"), xs)
+        if ps is not None:
+            np.testing.assert_array_equal(f.read("t40/polarity"), ps)
+    s = summarize(res, srv.makespan, srv.cell_steps)
+    assert s["p99_s"] >= s["p50_s"] > 0
+
+
+def test_native_server_resume_ends_as_uninterrupted(tmp_path):
+    """A request submitted with a start step (the state of its snapshot at that step) runs only its
+    remaining steps and ends with the uninterrupted result."""
+    reqs = wl.served_stream(3, seed=10, rate_hz=1000.0, lo=2000, hi=6000, steps_lo=90, steps_hi=90)
+    (tmp_path / "a").mkdir()
+    srv = NativeServer(cell_capacity=30000, bin_capacity=200000, max_sims=8, snapshot_every=30,
+                       snapshot_dir=tmp_path / "a", keep_results=True)
+    full = srv.run(reqs)
+    srv.close()
+    resume = {}
+    for r in full:
+        f = h5.H5File(tmp_path / "a" / f"request_{r.index:05d}.h5")
+        pol = f.read("t60/polarity") if "polarity" in f.keys("t60") else None
+        resume[r.index] = (60, f.read("t60/position"), pol)
+    (tmp_path / "b").mkdir()
+    srv = NativeServer(cell_capacity=30000, bin_capacity=200000, max_sims=8, snapshot_every=30,
+                       snapshot_dir=tmp_path / "b", keep_results=True)
+    again = srv.run(reqs, resume=resume)
+    srv.close()
+    for a, b in zip(full, again):
+        np.testing.assert_array_equal(a.positions, b.positions)
+        if a.polarity is not None:
+            np.testing.assert_array_equal(a.polarity, b.polarity)
