@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "forces.cuh"
+#include "delaunay_star.cuh"
 
 namespace tecs {
 
@@ -28,7 +29,8 @@ struct Counters {
   unsigned n;           // active cells
   unsigned div_count;   // daughters requested this step
   unsigned done[2];     // last-block counters of the two COM reductions
-  unsigned error;       // bit 0: capacity overflow on division; bit 1: a user law set drag, no old velocities kept
+  unsigned error;       // bit 0: capacity overflow on division; bit 1: a user law set drag, no old velocities kept;
+                        // bit 2: a Delaunay cell search overflowed its arrays (more than kDlRow partners)
   unsigned done_div;    // last-block counter of the division fixup
   unsigned long long step;        // integrator steps taken (keys the division RNG)
   unsigned long long pair_count;  // pairs recorded by the capture hook
@@ -82,6 +84,10 @@ struct PassArgs {
   unsigned* part;       // scan chunk totals formed while counting (count_bin), or null
   // naive Delaunay: how many times each directed pair is applied, row i at i * capacity
   const unsigned short* dmult;
+  // Delaunay (any capacity): cell i's partners and their applications,
+  // dl_row[i * kDlRow + t] = (j, reps) for t < dl_len[i], ascending j
+  const uint2* dl_row;
+  const unsigned* dl_len;
   // links of each cell id, in link order: link_ent[link_off[id] .. link_off[id + 1])
   // = (other cell id, (link index << 1) | 1 when this cell is the link's b
   // end); slot_of maps an id to its slot in X (null when X is in id order)
@@ -646,9 +652,173 @@ k_delaunay_mult(const float4* __restrict__ X, const Counters* __restrict__ ctr, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Delaunay finder for any capacity (tecs/device/delaunay_star.cuh).  Before
+// each pass: the bounding box of the pass's positions, a bin grid of about
+// two cells per bin, a counting sort into it, then each cell's partners and
+// multiplicities (k_dl_mult, one thread per cell).  The pass applies each
+// listed pair reps times in ascending j, as FINDER 4 does.
+constexpr unsigned kDlRow = 64;  // partners per cell
+constexpr int kDlThreads = 64;
+
+struct DlState {
+  unsigned mm[6];  // ordered-integer min (0..2) and max (3..5) of the coordinates
+  double lo[3];
+  double h, inv;
+  int dims[3];
+  unsigned nbins;
+};
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+static __global__ void k_dl_reset(DlState* st) {
+  if (threadIdx.x < 3) { st->mm[threadIdx.x] = 0xffffffffu; st->mm[3 + threadIdx.x] = 0u; }
+}
+
+template <int D>
+static __global__ void k_dl_bounds(const float4* __restrict__ X, const Counters* __restrict__ ctr, DlState* st) {
+  const unsigned n = ctr->n;
+  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = X[i];
+    const float c[3] = {v.x, v.y, v.z};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const unsigned o = f2ord(c[d]);
+      lo[d] = min(lo[d], o);
+      hi[d] = max(hi[d], o);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    for (int sh = 16; sh > 0; sh >>= 1) {
+      lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], sh));
+      hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], sh));
+    }
+    if ((threadIdx.x & 31) == 0) { atomicMin(&st->mm[d], lo[d]); atomicMax(&st->mm[3 + d], hi[d]); }
+  }
+}
+
+template <int D>
+static __global__ void k_dl_plan(const Counters* __restrict__ ctr, unsigned max_bins, DlState* st) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned n = ctr->n;
+  double mn[3] = {0.0, 0.0, 0.0}, mx[3] = {0.0, 0.0, 0.0};
+  if (n > 0)
+    for (int d = 0; d < D; ++d) { mn[d] = ord2f(st->mm[d]); mx[d] = ord2f(st->mm[3 + d]); }
+  dl::Grid g{};
+  dl::plan_grid<D>(g, mn, mx, n, max_bins);
+  for (int d = 0; d < 3; ++d) { st->lo[d] = g.lo[d]; st->dims[d] = g.dims[d]; }
+  st->h = g.h;
+  st->inv = g.inv;
+  st->nbins = g.nbins;
+}
+
+__device__ __forceinline__ dl::Grid dl_view(const DlState* st) {
+  dl::Grid g{};
+  for (int d = 0; d < 3; ++d) { g.lo[d] = st->lo[d]; g.dims[d] = st->dims[d]; }
+  g.h = st->h;
+  g.inv = st->inv;
+  g.nbins = st->nbins;
+  return g;
+}
+
+template <int D>
+__device__ __forceinline__ unsigned dl_bin(const dl::Grid& g, const float4& v) {
+  const double q[3] = {v.x, v.y, v.z};
+  int b[3];
+  dl::bin_of<D>(g, q, b);
+  return dl::flat(g, b[0], b[1], b[2]);
+}
+
+template <int D>
+static __global__ void k_dl_count(const float4* __restrict__ X, const Counters* __restrict__ ctr,
+                                  const DlState* __restrict__ st, unsigned* __restrict__ cnt) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ctr->n) return;
+  const dl::Grid g = dl_view(st);
+  atomicAdd(&cnt[dl_bin<D>(g, X[i])], 1u);
+}
+
+// exclusive scan of the bin counts into off (off[nbins] = cells), one block;
+// the counts are cleared for the scatter's cursors
+static __global__ void __launch_bounds__(1024) k_dl_scan(const DlState* __restrict__ st, unsigned* __restrict__ cnt,
+                                                         unsigned* __restrict__ off) {
+  __shared__ unsigned part[1024];
+  const unsigned nb = st->nbins, t = threadIdx.x;
+  const unsigned per = (nb + 1023u) / 1024u, b0 = min(nb, t * per), b1 = min(nb, b0 + per);
+  unsigned sum = 0;
+  for (unsigned b = b0; b < b1; ++b) sum += cnt[b];
+  part[t] = sum;
+  __syncthreads();
+  for (unsigned sh = 1; sh < 1024u; sh <<= 1) {
+    const unsigned v = t >= sh ? part[t - sh] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  unsigned run = part[t] - sum;
+  for (unsigned b = b0; b < b1; ++b) {
+    const unsigned c = cnt[b];
+    off[b] = run;
+    run += c;
+    cnt[b] = 0u;
+  }
+  if (t == 1023u) off[nb] = part[1023];
+}
+
+template <int D>
+static __global__ void k_dl_scatter(const float4* __restrict__ X, const Counters* __restrict__ ctr,
+                                    const DlState* __restrict__ st, unsigned* __restrict__ cnt,
+                                    const unsigned* __restrict__ off, unsigned* __restrict__ idx,
+                                    float4* __restrict__ sp) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ctr->n) return;
+  const dl::Grid g = dl_view(st);
+  const float4 v = X[i];
+  const unsigned b = dl_bin<D>(g, v);
+  const unsigned at = off[b] + atomicAdd(&cnt[b], 1u);
+  idx[at] = i;
+  sp[at] = v;
+}
+
+template <int D>
+static __global__ void __launch_bounds__(kDlThreads) k_dl_mult(const float4* __restrict__ X, Counters* __restrict__ ctr,
+                                                               const DlState* __restrict__ st,
+                                                               const unsigned* __restrict__ off,
+                                                               const unsigned* __restrict__ idx,
+                                                               const float4* __restrict__ sp, float rc2,
+                                                               uint2* __restrict__ row, unsigned* __restrict__ len) {
+  const unsigned n = ctr->n;
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dl::Grid g = dl_view(st);
+  g.off = off;
+  g.idx = idx;
+  g.sp = reinterpret_cast<const dl::Pt*>(sp);
+  g.P = reinterpret_cast<const dl::Pt*>(X);
+  g.n = n;
+  g.rc2 = rc2;
+  dl::Star star;
+  unsigned oj[kDlRow], orp[kDlRow], err = 0;
+  const unsigned m = dl::cell_mult<D>(g, i, oj, orp, kDlRow, &err, star);
+  for (unsigned t = 0; t < m; ++t) row[(size_t)i * kDlRow + t] = make_uint2(oj[t], orp[t]);
+  len[i] = m;
+  // a full near-circle list keeps the points nearest the circle (no error);
+  // any other overflow leaves the row incomplete
+  if (err & (dl::kErrStar | dl::kErrPairs | dl::kErrList)) atomicOr(&ctr->error, 4u);
+}
+
 template <int D, int FINDER, int FORCE>
 __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
-                                      unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi) {
+                                      unsigned j, const float* xi, float2 pi, Acc& acc, unsigned idi,
+                                      unsigned reps5 = 1u) {
   const float4 vj = a.X[j];
   float disp[3];
   disp[0] = xi[0] - vj.x;
@@ -659,7 +829,7 @@ __device__ __forceinline__ void visit(const GridP& g, const ForceP& fp, const Pa
   if (d2 >= fp.rc2) return;
   if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
   if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
-  unsigned reps = 1;
+  unsigned reps = FINDER == 5 ? reps5 : 1u;
   if (FINDER == 4 && (reps = a.dmult[(size_t)i * a.capacity + j]) == 0u) return;
   if (a.pairs) {
     unsigned long long s = atomicAdd(&a.ctr->pair_count, (unsigned long long)reps);
@@ -1001,6 +1171,13 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
           }
         }
       }
+    } else if (FINDER == 5) {
+      // the cell's Delaunay partners, ascending j, each applied reps times
+      const unsigned m = a.dl_len[i];
+      for (unsigned t = 0; t < m; ++t) {
+        const uint2 e = a.dl_row[(size_t)i * kDlRow + t];
+        visit<D, FINDER, FORCE>(g, fp, a, n, i, e.x, xi, pi, acc, idi, e.y);
+      }
     } else {
       for (unsigned j = 0; j < n; ++j) {
         if (j == i) continue;
@@ -1028,7 +1205,8 @@ __device__ __forceinline__ void cell_general(const GridP& g, const ForceP& fp, c
 template <int D, int FINDER, class Law>
 __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned n, unsigned i,
                                           unsigned j, const float* xi, float2 pi, Acc& acc,
-                                          typename Law::Cell& dacc, unsigned idi, const Law& law) {
+                                          typename Law::Cell& dacc, unsigned idi, const Law& law,
+                                          unsigned reps5 = 1u) {
   const float4 vj = a.X[j];
   float disp[3] = {xi[0] - vj.x, xi[1] - vj.y, D >= 3 ? xi[2] - vj.z : 0.f};
   float d2 = disp[0] * disp[0] + disp[1] * disp[1];
@@ -1036,8 +1214,8 @@ __device__ __forceinline__ void visit_law(const GridP& g, const ForceP& fp, cons
   if (d2 >= fp.rc2) return;
   if (FINDER == 3 && gabriel_blocked<D>(g, fp, a.X, a.off, i, j, xi, disp, d2)) return;
   if (FINDER == 2 && gabriel_blocked_naive<D>(fp, a.X, n, i, j, xi, disp, d2)) return;
-  // naive Delaunay: the law is called once per accepted simplex, in j order
-  unsigned reps = 1;
+  // Delaunay: the law is called once per accepted simplex, in j order
+  unsigned reps = FINDER == 5 ? reps5 : 1u;
   if (FINDER == 4 && (reps = a.dmult[(size_t)i * a.capacity + j]) == 0u) return;
   const unsigned idj = id_at(a.X, a.Bid, j);
   if (a.pairs) {
@@ -1075,6 +1253,12 @@ __device__ __forceinline__ void cell_law(const GridP& g, const ForceP& fp, const
           visit_law<D, FINDER>(g, fp, a, n, i, j, xi, pi, acc, dacc, idi, law);
         }
       }
+    }
+  } else if (FINDER == 5) {
+    const unsigned m = a.dl_len[i];
+    for (unsigned t = 0; t < m; ++t) {
+      const uint2 e = a.dl_row[(size_t)i * kDlRow + t];
+      visit_law<D, FINDER>(g, fp, a, n, i, e.x, xi, pi, acc, dacc, idi, law, e.y);
     }
   } else {
     for (unsigned j = 0; j < n; ++j) {
@@ -1151,7 +1335,7 @@ struct UserPassCall {
   unsigned size;
   int device;           // the simulation's GPU
   int dims;
-  int finder;           // TECS_FINDER_NAIVE_ALL_PAIRS .. TECS_FINDER_BINNED_GABRIEL
+  int finder;           // TECS_FINDER_NAIVE_ALL_PAIRS .. TECS_FINDER_DELAUNAY
   unsigned blocks;      // of kPassThreads threads
   GridP g;
   ForceP fp;
@@ -1162,14 +1346,19 @@ struct UserPassCall {
 // for the finder and dimension count the program was compiled for.  0 on
 // success; 1 the call's layout differs; 2 a launch error; 3 the simulation's
 // finder or dimension count is not the program's.
+// A program compiled for the naive Delaunay finder runs with the Delaunay
+// finder of any capacity (FINDER 5) too: the library takes that one past the
+// naive finder's capacity.
 template <int D, int FINDER, class Law>
 int launch_user_pass(const UserPassCall* c, cudaStream_t stream, const Law* law) {
-  static_assert(FINDER >= 0 && FINDER <= 4, "user laws run with the all-pairs, Gabriel and Delaunay finders");
+  static_assert(FINDER >= 0 && FINDER <= 5, "user laws run with the all-pairs, Gabriel and Delaunay finders");
   if (!c || c->size != sizeof(UserPassCall)) return 1;
-  if (c->dims != D || c->finder != FINDER || c->a.E != Law::kExtra) return 3;
+  const bool dl5 = FINDER == 4 && c->finder == 5;
+  if (c->dims != D || (c->finder != FINDER && !dl5) || c->a.E != Law::kExtra) return 3;
   int cur = -1;
   if (cudaGetDevice(&cur) != cudaSuccess || (cur != c->device && cudaSetDevice(c->device) != cudaSuccess)) return 2;
-  k_pass_law<D, FINDER, Law><<<c->blocks, kPassThreads, 0, stream>>>(c->g, c->fp, c->a, law);
+  if (dl5) k_pass_law<D, 5, Law><<<c->blocks, kPassThreads, 0, stream>>>(c->g, c->fp, c->a, law);
+  else k_pass_law<D, FINDER, Law><<<c->blocks, kPassThreads, 0, stream>>>(c->g, c->fp, c->a, law);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
@@ -1179,6 +1368,7 @@ template <int D, int FINDER, class Law>
 int prepare_user_pass(int device) {
   cudaFuncAttributes fa;
   if (cudaSetDevice(device) != cudaSuccess) return 2;
+  if (FINDER == 4 && cudaFuncGetAttributes(&fa, k_pass_law<D, 5, Law>) != cudaSuccess) return 2;
   return cudaFuncGetAttributes(&fa, k_pass_law<D, FINDER, Law>) == cudaSuccess ? 0 : 2;
 }
 

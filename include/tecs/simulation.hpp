@@ -224,6 +224,7 @@ class Simulation {
     d.division_offset = s.division.offset;
     d.seed = s.seed;
     d.device = s.device;
+    delaunay_for_capacity(d);
     check(tecs_sim_create(&d, &handle_));
     desc_ = d;
     positions_ = View<Vector>(std::string(field_name<0>()), s.agent_count, s.capacity);
@@ -321,6 +322,7 @@ class Simulation {
     }
     tecs_sim_desc d = desc_;
     d.capacity = value;
+    delaunay_for_capacity(d);
     tecs_sim* next = nullptr;
     check(tecs_sim_create(&d, &next));
     check(tecs_sim_set_pair_law(handle_, nullptr, nullptr));
@@ -951,6 +953,13 @@ class Simulation {
   bool user_code_ran_ = false;      // user code ran on the device since the views were last checked
   bool old_velocities_kept_ = false;
   tecs_sim_desc desc_{};
+  // NaiveDelaunay takes the library's Delaunay finder of any capacity past
+  // the naive finder's 4096 cells (the same multiplicities in 2-D; the
+  // Delaunay tetrahedra in 3-D), and the naive one below
+  static void delaunay_for_capacity(tecs_sim_desc& d) {
+    if (PairFinder::finder_id != TECS_FINDER_NAIVE_DELAUNAY) return;
+    d.finder = d.capacity > 4096u ? TECS_FINDER_DELAUNAY : TECS_FINDER_NAIVE_DELAUNAY;
+  }
 
   void keep_old_velocities() {
     if (old_velocities_kept_) return;

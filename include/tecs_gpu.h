@@ -35,7 +35,11 @@ enum tecs_finder {
   TECS_FINDER_BINNED_ALL_PAIRS = 1,
   TECS_FINDER_NAIVE_GABRIEL = 2,
   TECS_FINDER_BINNED_GABRIEL = 3,
-  TECS_FINDER_NAIVE_DELAUNAY = 4    /* naive_delaunay.hpp:31-294; capacity <= 4096, non-symmetric */
+  TECS_FINDER_NAIVE_DELAUNAY = 4,   /* naive_delaunay.hpp:31-294; capacity <= 4096, non-symmetric */
+  TECS_FINDER_DELAUNAY = 5          /* the same finder for any capacity, from each cell's Delaunay star: in 2-D
+                                       the naive finder's multiplicities bit for bit; in 3-D the Delaunay
+                                       tetrahedra under its counting rule (its 3-D sphere is centred at
+                                       x_i + c, not at the circumcentre c); non-symmetric */
 };
 
 /* Integrators: include/integrators/euler.hpp, heun.hpp */

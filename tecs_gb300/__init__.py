@@ -17,7 +17,7 @@ import numpy as np
 
 from . import build as _build
 
-NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL, NAIVE_DELAUNAY = 0, 1, 2, 3, 4
+NAIVE_ALL_PAIRS, BINNED_ALL_PAIRS, NAIVE_GABRIEL, BINNED_GABRIEL, NAIVE_DELAUNAY, DELAUNAY = 0, 1, 2, 3, 4, 5
 EULER, HEUN = 0, 1
 FORCE_NONE, FORCE_SPRING2R, FORCE_POLARITY = 0, 1, 2
 
@@ -27,6 +27,7 @@ FINDERS = {
     "naive_gabriel": NAIVE_GABRIEL,
     "binned_gabriel": BINNED_GABRIEL,
     "naive_delaunay": NAIVE_DELAUNAY,
+    "delaunay": DELAUNAY,
 }
 INTEGRATORS = {"euler": EULER, "heun": HEUN}
 
@@ -227,7 +228,8 @@ def make_desc(settings: Settings, *, dims: int = 3, pair_finder: str = "binned_g
 class Simulation:
     """One simulation resident on a GB300: the reference's Simulation<Config>.
 
-    ``pair_finder``: naive_all_pairs | binned_all_pairs | naive_gabriel | binned_gabriel | naive_delaunay
+    ``pair_finder``: naive_all_pairs | binned_all_pairs | naive_gabriel | binned_gabriel | naive_delaunay |
+    delaunay (the Delaunay finder of any capacity, from each cell's star)
     ``integrator``:  euler | heun;  ``com_fixer``: None | "global"
     ``force``: Spring2R | PolaritySpring | None (pair capture only).
     """

@@ -187,6 +187,13 @@ struct tecs_sim {
   unsigned *div_parent = nullptr, *div_slot = nullptr;
   unsigned* Bid = nullptr;  // cell ids of B's slots (B.w holds the bin key)
   unsigned short* dmult = nullptr;  // naive Delaunay: applications per directed pair, capacity x capacity
+  // Delaunay of any capacity: the pass's bin grid (state, counts, offsets,
+  // sorted slots and positions) and each cell's partner row
+  DlState* dl_st = nullptr;
+  unsigned *dl_cnt = nullptr, *dl_off = nullptr, *dl_idx = nullptr, *dl_len = nullptr;
+  float4* dl_sp = nullptr;
+  uint2* dl_row = nullptr;
+  unsigned dl_maxbins = 0;
   // links: per-cell entries in link order, and the id -> slot map of the sorted copy
   unsigned* link_off = nullptr;
   uint2* link_ent = nullptr;
@@ -296,6 +303,13 @@ PassFn pass_fn(const tecs_sim* s, bool sym) {
     if (D == 2 && FO == 0) return k_pass<2, 4, 0>;
     if (D == 2 && FO == 1) return k_pass<2, 4, 1>;
   }
+  if (F == TECS_FINDER_DELAUNAY && !sym) {
+    if (D == 3 && FO == 0) return k_pass<3, 5, 0>;
+    if (D == 3 && FO == 1) return k_pass<3, 5, 1>;
+    if (D == 3 && FO == 2) return k_pass<3, 5, 2>;
+    if (D == 2 && FO == 0) return k_pass<2, 5, 0>;
+    if (D == 2 && FO == 1) return k_pass<2, 5, 1>;
+  }
   return nullptr;
 }
 
@@ -329,6 +343,8 @@ PassArgs base_args(const tecs_sim* s, float dt, double dt64 = 0.0) {
   a.cnt = s->cnt;
   a.part = s->fuse_part ? s->part : nullptr;
   a.dmult = s->dmult;
+  a.dl_row = s->dl_row;
+  a.dl_len = s->dl_len;
   a.link_off = s->n_links ? s->link_off : nullptr;
   a.link_ent = s->n_links ? s->link_ent : nullptr;
   a.slot_of = (s->n_links && s->binned) ? s->slot_of : nullptr;
@@ -399,7 +415,40 @@ int enqueue_rebuild(tecs_sim* s, int& K, bool run_count) {
   return 0;
 }
 
+// The Delaunay finder of any capacity: bin grid of the pass's positions, then
+// every cell's partner row.
+int enqueue_delaunay_star(tecs_sim* s, const PassArgs& a, int& K) {
+  const unsigned L = launch_count(s);
+  const unsigned gb = ceil_div(L ? L : 1, 256);
+  const bool d3 = s->d.dims == 3;
+  PROF_BEGIN(s);
+  CK(cudaMemsetAsync(s->dl_cnt, 0, (size_t)s->dl_maxbins * 4, s->stream));
+  k_dl_reset<<<1, 32, 0, s->stream>>>(s->dl_st);
+  if (d3) k_dl_bounds<3><<<std::min(gb, 1216u), 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st);
+  else k_dl_bounds<2><<<std::min(gb, 1216u), 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st);
+  if (d3) k_dl_plan<3><<<1, 32, 0, s->stream>>>(s->ctr, s->dl_maxbins, s->dl_st);
+  else k_dl_plan<2><<<1, 32, 0, s->stream>>>(s->ctr, s->dl_maxbins, s->dl_st);
+  if (d3) k_dl_count<3><<<gb, 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_cnt);
+  else k_dl_count<2><<<gb, 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_cnt);
+  k_dl_scan<<<1, 1024, 0, s->stream>>>(s->dl_st, s->dl_cnt, s->dl_off);
+  if (d3) k_dl_scatter<3><<<gb, 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_cnt, s->dl_off, s->dl_idx, s->dl_sp);
+  else k_dl_scatter<2><<<gb, 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_cnt, s->dl_off, s->dl_idx, s->dl_sp);
+  PROF_END(s, "k_dl_grid");
+  K += 6;
+  const unsigned mb = ceil_div(L ? L : 1, kDlThreads);
+  PROF_BEGIN(s);
+  if (d3) k_dl_mult<3><<<mb, kDlThreads, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_off, s->dl_idx, s->dl_sp,
+                                                         s->fp.rc2, s->dl_row, s->dl_len);
+  else k_dl_mult<2><<<mb, kDlThreads, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_off, s->dl_idx, s->dl_sp,
+                                                      s->fp.rc2, s->dl_row, s->dl_len);
+  PROF_END(s, "k_dl_mult");
+  K += 1;
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int enqueue_delaunay_mult(tecs_sim* s, const PassArgs& a, int& K) {
+  if (s->d.finder == TECS_FINDER_DELAUNAY) return enqueue_delaunay_star(s, a, K);
   const unsigned L = launch_count(s);
   // applications per pair on this pass's positions, before the pass
   PROF_BEGIN(s);
@@ -417,7 +466,7 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   const unsigned L = launch_count(s);
   const unsigned blocks = ceil_div(L ? L : 1, kPassThreads);
   if (s->law_fn) {
-    if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
+    if (s->d.finder >= TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
     UserPassCall c{};
     c.size = sizeof(UserPassCall);
     c.device = s->d.device;
@@ -437,7 +486,7 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
   }
   const PassFn fn = pass_fn(s, sym);
   if (!fn) return fail("unsupported finder/force/dims combination");
-  if (s->d.finder == TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
+  if (s->d.finder >= TECS_FINDER_NAIVE_DELAUNAY && enqueue_delaunay_mult(s, a, K)) return -1;
   PROF_BEGIN(s);
   fn<<<ceil_div(L ? L : 1, kPassThreads), kPassThreads, 0, s->stream>>>(s->g, s->fp, a);
   PROF_END(s, a.mode == kStore ? "k_pass_store" : a.mode == kEulerFused ? "k_pass_euler"
@@ -616,9 +665,11 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   *out = nullptr;
   if (desc->dims != 2 && desc->dims != 3) return fail("dims must be 2 or 3");
   if (desc->capacity == 0) return fail("capacity must be > 0");
-  if (desc->finder < 0 || desc->finder > TECS_FINDER_NAIVE_DELAUNAY) return fail("unknown finder");
-  if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY && desc->symmetric)
+  if (desc->finder < 0 || desc->finder > TECS_FINDER_DELAUNAY) return fail("unknown finder");
+  if (desc->finder >= TECS_FINDER_NAIVE_DELAUNAY && desc->symmetric)
     return fail("the Delaunay finder has no symmetric variant");
+  if (desc->finder == TECS_FINDER_DELAUNAY && desc->capacity >= (1u << 30))
+    return fail("the Delaunay finder holds fewer than 2^30 cells");
   if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY && desc->capacity > kDelaunayMaxCells)
     return fail("the naive Delaunay finder holds at most 4096 cells");
   if (desc->force < 0 || desc->force > 2) return fail("unknown force");
@@ -649,7 +700,10 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
     if (g.ext[k] < 1) { delete s; return fail("max_bounds must exceed min_bounds"); }
     nb *= (unsigned long long)g.ext[k];
   }
-  if (nb > (1ull << 31)) { delete s; return fail("bin grid too large"); }
+  // the naive and Delaunay finders do not use this grid
+  const bool binned_finder = desc->finder == TECS_FINDER_BINNED_ALL_PAIRS || desc->finder == TECS_FINDER_BINNED_GABRIEL;
+  if (binned_finder && nb > (1ull << 31)) { delete s; return fail("bin grid too large"); }
+  if (!binned_finder && nb > (1ull << 31)) nb = 1ull << 31;
   g.nbins = (unsigned)nb;
   grid_set_pow2(g);
   ForceP& f = s->fp;
@@ -682,6 +736,15 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   ok = ok && alloc((void**)&s->div_parent, cap * 4) && alloc((void**)&s->div_slot, cap * 4);
   if (s->binned) ok = ok && alloc((void**)&s->Bid, cap * 4);
   if (desc->finder == TECS_FINDER_NAIVE_DELAUNAY) ok = ok && alloc((void**)&s->dmult, cap * cap * 2);
+  if (desc->finder == TECS_FINDER_DELAUNAY) {
+    // about two cells per bin: capacity / 2 bins suffice (dl::plan_grid)
+    s->dl_maxbins = (unsigned)(cap / 2 + 64);
+    ok = ok && alloc((void**)&s->dl_st, sizeof(DlState)) && alloc((void**)&s->dl_cnt, (size_t)s->dl_maxbins * 4) &&
+         alloc((void**)&s->dl_off, ((size_t)s->dl_maxbins + 1) * 4) && alloc((void**)&s->dl_idx, cap * 4) &&
+         alloc((void**)&s->dl_sp, cap * 16) && alloc((void**)&s->dl_row, cap * kDlRow * 8) &&
+         alloc((void**)&s->dl_len, cap * 4);
+    if (ok) ok = cudaMemsetAsync(s->dl_len, 0, cap * 4, s->stream) == cudaSuccess;
+  }
   if (s->binned) {
     const size_t len = (size_t)g.nbins + 1;
     ok = ok && alloc((void**)&s->cnt, len * 4) && alloc((void**)&s->off, len * 4) &&
@@ -718,7 +781,7 @@ int tecs_sim_destroy(tecs_sim* s) {
   void* ptrs[] = {s->A, s->B, s->Xt, s->d1, s->d2, s->PA, s->PB, s->Pt, s->dp1, s->dp2, s->key, s->rank, s->src,
                   s->cnt, s->off, s->part, s->div_parent, s->div_slot, s->ctr, s->com_part, s->com, s->stage,
                   s->Bid, s->dmult, s->link_off, s->link_ent, s->slot_of, s->ov, s->EA, s->EB, s->Et,
-                  s->ed1, s->ed2};
+                  s->ed1, s->ed2, s->dl_st, s->dl_cnt, s->dl_off, s->dl_idx, s->dl_sp, s->dl_row, s->dl_len};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -859,6 +922,8 @@ int tecs_sim_count(tecs_sim* s, unsigned* n) {
   CK(cudaStreamSynchronize(s->stream));
   if (s->hctr->error & 1u) return fail("capacity exceeded by cell division");
   if (s->hctr->error & 2u) return fail("a user pairwise law set drag in a simulation that keeps no old velocities");
+  if (s->hctr->error & 4u)
+    return fail("the Delaunay finder met a cell with more partners or star simplices than its arrays hold");
   *n = s->hctr->n;
   return 0;
 }
