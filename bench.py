@@ -13,6 +13,10 @@ Workloads (--workload):
       alignment), Heun dt = 0.05.
   small: 1,000 cells in a ball of radius 5 (seed 0), binned all-pairs, spring,
       Euler dt = 0.1.
+  delaunay, delaunay3d: 100,000 cells uniform in a 2-D disk or a 3-D ball at
+      density 1, the Delaunay finder of any capacity (cutoff 1.0), spring,
+      Heun dt = 0.05 (no CPU leg: the reference's naive Delaunay finder does
+      O(N^3) work per cell).
   ensemble: 256 simulations in one engine vs the plain path one after another.
   served: the continuous-batching request loop (tecs_gb300.served).
 
@@ -79,6 +83,14 @@ def _sheet_workload(n):
     return x, p, mn, mx
 
 
+def _disk_workload(n):
+    from tecs_gb300 import workloads as wl
+
+    x = wl.disk(n, 1)
+    mn, mx = wl.bounds_for(x, margin=2.0)
+    return x, None, mn, mx
+
+
 def _small_workload(n):
     from tecs_gb300 import workloads as wl
 
@@ -107,6 +119,18 @@ WORKLOADS = {
         finder="binned_all_pairs", integrator="euler", com=False, division=0.0, polarity=False, dt=0.1,
         capacity=1.0, desc="ball {n} cells radius 5 (seed 0), binned all-pairs, spring, Euler dt 0.1",
         step_bytes=92),
+    # the Delaunay finder of any capacity; the reference's naive finder does
+    # O(N^3) work per cell, so no CPU leg runs at this size
+    "delaunay": dict(
+        metric="cell-steps/s, 100k-cell 2-D disk (Delaunay finder, spring, Heun)", cells=100_000,
+        make=_disk_workload, finder="delaunay", integrator="heun", com=False, division=0.0, polarity=False,
+        dt=0.05, capacity=1.0, dims=2, cpu=False,
+        desc="disk {n} cells (density 1, seed 1), Delaunay finder, spring, Heun dt 0.05", step_bytes=156),
+    "delaunay3d": dict(
+        metric="cell-steps/s, 100k-cell 3-D ball (Delaunay finder, spring, Heun)", cells=100_000,
+        make=_ball_workload, finder="delaunay", integrator="heun", com=False, division=0.0, polarity=False,
+        dt=0.05, capacity=1.0, dims=3, cpu=False,
+        desc="ball {n} cells (density 1, seed 1), Delaunay finder, spring, Heun dt 0.05", step_bytes=156),
 }
 
 
@@ -136,7 +160,7 @@ def make_sim(w, n, mn, mx, device=0, steps=0):
     cap = capacity_for(w, n, steps)
     force = tg.PolaritySpring(k_pol=0.2) if w["polarity"] else tg.Spring2R(k_rep=2.0, r_rep=0.7, k_adh=0.5, r_adh=0.8)
     return tg.Simulation(tg.Settings(agent_count=n, capacity=cap, cutoff_distance=1.0, seed=1, pair_finder_settings=pf),
-                         pair_finder=w["finder"], integrator=w["integrator"],
+                         dims=w.get("dims", 3), pair_finder=w["finder"], integrator=w["integrator"],
                          com_fixer="global" if w["com"] else None, force=force, polarity=w["polarity"],
                          division=tg.Division(probability=w["division"], offset=0.25), device=device)
 
@@ -293,6 +317,10 @@ def run_reference(args):
     if rank != 0:
         return 0
     w = WORKLOADS[args.workload]
+    if not w.get("cpu", True):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's naive Delaunay finder does O(N^3) "
+                                                              "work per cell; no bounded sample at this size"}))
+        return 0
     n = args.cells or w["cells"]
     threads = os.cpu_count() or 1
     x, p, mn, mx = w["make"](n)
@@ -396,7 +424,8 @@ def run_gb300(args):
     if not args.no_e2e:
         L = tg.load()
         cap = sim.desc.capacity
-        hx = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+        D = w.get("dims", 3)
+        hx = torch.empty((cap, D), dtype=torch.float32, pin_memory=True)
         hx.numpy()[:n] = x
         hp = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True) if pol else None
         if pol:
@@ -425,13 +454,13 @@ def run_gb300(args):
             tg._check(L.tecs_sim_upload(sim._h, ctypes.c_void_p(hx.data_ptr()),
                                         ctypes.c_void_p(hp.data_ptr()) if pol else None, m))
             tb = time.perf_counter()
-            h2d += m * (20 if pol else 12)
+            h2d += m * (4 * D + (8 if pol else 0))
             tg._check(L.tecs_sim_step(sim._h, dt, 1))
             tg._check(L.tecs_sim_download(sim._h, ctypes.c_void_p(hx.data_ptr()),
                                           ctypes.c_void_p(hp.data_ptr()) if pol else None, ctypes.byref(nn)))
             t_up += tb - ta
             t_rest += time.perf_counter() - tb
-            d2h += nn.value * (20 if pol else 12)
+            d2h += nn.value * (4 * D + (8 if pol else 0))
             cs += m
         t1 = time.perf_counter()
         e2e = {"value": cs / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
@@ -495,7 +524,7 @@ def run_gb300(args):
     kernel_table = {k: {"launches": len(v), "mean_ms": statistics.mean(v), "share": sum(v) / max(sum(prof_ms), 1e-9)}
                     for k, v in kern.items()}
     cpu = None
-    if not args.no_cpu_baseline and world == 1:
+    if not args.no_cpu_baseline and world == 1 and w.get("cpu", True):
         threads = os.cpu_count() or 1
         v, k, sec = cpu_steps(w, n, mn, mx, x, p, 1000, threads, 15.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
@@ -601,7 +630,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble comparison of the default run")
     ap.add_argument("--chunk", type=int, default=10,
                     help="simulation steps per timed step (the L2 is flushed between timed steps)")
-    ap.add_argument("--workload", default="spheroid", choices=["spheroid", "sheet", "small", "ensemble", "served"])
+    ap.add_argument("--workload", default="spheroid",
+                    choices=["spheroid", "sheet", "small", "delaunay", "delaunay3d", "ensemble", "served"])
     ap.add_argument("--sims", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--requests", type=int, default=200, help="served workload: number of requests")

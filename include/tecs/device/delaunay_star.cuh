@@ -96,6 +96,53 @@ constexpr int kMaxPairs = 320;   // accepted (j, k)
 constexpr double kInf = 1.0e300;
 constexpr double kEps = (double)FLT_EPSILON;
 
+// Lane policies.  Every search visits entries; Solo visits them in one
+// thread (the host), Warp in the 32 lanes of a warp, each lane taking every
+// 32nd entry.  Lanes keep identical copies of all other state: every result
+// of a visit is combined across the warp (a vote, a minimum, candidates
+// merged in lane order) before anything depends on it.
+struct Solo {
+  static constexpr unsigned width = 1;
+  TECS_DL_HD unsigned lane() const { return 0u; }
+  TECS_DL_HD bool any(bool b) const { return b; }
+  TECS_DL_HD unsigned ballot(bool b) const { return b ? 1u : 0u; }
+  TECS_DL_HD unsigned bcast(unsigned v, int) const { return v; }
+  TECS_DL_HD double bcast(double v, int) const { return v; }
+};
+
+#if defined(__CUDACC__)
+struct Warp {
+  static constexpr unsigned width = 32;
+  __device__ __forceinline__ unsigned lane() const { return threadIdx.x & 31u; }
+  __device__ __forceinline__ bool any(bool b) const { return __any_sync(0xffffffffu, b); }
+  __device__ __forceinline__ unsigned ballot(bool b) const { return __ballot_sync(0xffffffffu, b); }
+  __device__ __forceinline__ unsigned bcast(unsigned v, int src) const { return __shfl_sync(0xffffffffu, v, src); }
+  __device__ __forceinline__ double bcast(double v, int src) const { return __shfl_sync(0xffffffffu, v, src); }
+};
+#endif
+
+// the lowest set bit's index
+TECS_DL_HD int low_bit(unsigned m) {
+  int b = 0;
+  while (!(m & 1u)) { m >>= 1; ++b; }
+  return b;
+}
+
+// the least (key, id) over the lanes, in every lane
+template <class W>
+TECS_DL_HD void lane_min(const W& w, double& key, unsigned& id) {
+  for (unsigned sh = W::width / 2; sh > 0; sh >>= 1) {
+    const int src = (int)(w.lane() ^ sh);
+    const double k2 = w.bcast(key, src);
+    const unsigned i2 = w.bcast(id, src);
+    if (k2 < key || (k2 == key && i2 < id)) { key = k2; id = i2; }
+  }
+}
+
+struct NoRound {
+  TECS_DL_HD void operator()() const {}
+};
+
 TECS_DL_HD double dmax(double a, double b) { return a > b ? a : b; }
 TECS_DL_HD int imax(int a, int b) { return a > b ? a : b; }
 TECS_DL_HD int imin(int a, int b) { return a < b ? a : b; }
@@ -158,22 +205,51 @@ TECS_DL_HD unsigned flat(const Grid& g, int x, int y, int z) {
   return ((unsigned)z * (unsigned)g.dims[1] + (unsigned)y) * (unsigned)g.dims[0] + (unsigned)x;
 }
 
-// Every entry of the bins [b0, b1] (inclusive); f(slot, pos) returns false to stop.
-template <int D, class F>
-TECS_DL_HD bool visit_box(const Grid& g, const int* b0, const int* b1, F&& f) {
+// Every entry of the bins [b0, b1] (inclusive); f(slot, pos) returns false
+// to stop (the warp stops when any lane does).  round() runs in every lane
+// after each round of entries (one entry per lane), where the caller merges
+// what the lanes found.  One thread loads four entries at a time, to keep
+// several loads in flight.
+template <int D, class W, class F, class R = NoRound>
+TECS_DL_HD bool visit_box(const W& w, const Grid& g, const int* b0, const int* b1, F&& f, R&& round = R{}) {
   const int z0 = D >= 3 ? b0[2] : 0, z1 = D >= 3 ? b1[2] : 0;
   for (int z = z0; z <= z1; ++z)
     for (int y = b0[1]; y <= b1[1]; ++y) {
       const unsigned lo = g.off[flat(g, b0[0], y, z)], hi = g.off[flat(g, b1[0], y, z) + 1];
-      for (unsigned e = lo; e < hi; ++e)
-        if (!f(g.idx[e], g.sp[e])) return false;
+      if (W::width == 1) {
+        unsigned e = lo;
+        for (; e + 4 <= hi; e += 4) {
+          const unsigned i0 = g.idx[e], i1 = g.idx[e + 1], i2 = g.idx[e + 2], i3 = g.idx[e + 3];
+          const Pt p0 = g.sp[e], p1 = g.sp[e + 1], p2 = g.sp[e + 2], p3 = g.sp[e + 3];
+          if (!f(i0, p0)) return false;
+          round();
+          if (!f(i1, p1)) return false;
+          round();
+          if (!f(i2, p2)) return false;
+          round();
+          if (!f(i3, p3)) return false;
+          round();
+        }
+        for (; e < hi; ++e) {
+          if (!f(g.idx[e], g.sp[e])) return false;
+          round();
+        }
+      } else {
+        for (unsigned base = lo; base < hi; base += W::width) {
+          const unsigned e = base + w.lane();
+          bool stop = false;
+          if (e < hi) stop = !f(g.idx[e], g.sp[e]);
+          if (w.any(stop)) return false;
+          round();
+        }
+      }
     }
   return true;
 }
 
 // The bins at Chebyshev distance k from bc.
-template <int D, class F>
-TECS_DL_HD bool visit_shell(const Grid& g, const int* bc, int k, F&& f) {
+template <int D, class W, class F, class R = NoRound>
+TECS_DL_HD bool visit_shell(const W& w, const Grid& g, const int* bc, int k, F&& f, R&& round = R{}) {
   const int z0 = D >= 3 ? bc[2] - k : 0, z1 = D >= 3 ? bc[2] + k : 0;
   for (int z = z0; z <= z1; ++z) {
     if (z < 0 || z >= g.dims[2]) continue;
@@ -186,16 +262,124 @@ TECS_DL_HD bool visit_shell(const Grid& g, const int* bc, int k, F&& f) {
         const int a = imax(bc[0] - k, 0), b = imin(bc[0] + k, g.dims[0] - 1);
         if (a > b) continue;
         const int lo3[3] = {a, y, z}, hi3[3] = {b, y, z};
-        if (!visit_box<3>(g, lo3, hi3, f)) return false;
+        if (!visit_box<3>(w, g, lo3, hi3, f, round)) return false;
         continue;
       }
       if (bc[0] - k >= 0) xs[nx++] = bc[0] - k;
       if (k > 0 && bc[0] + k < g.dims[0]) xs[nx++] = bc[0] + k;
       for (int q = 0; q < nx; ++q) {
         const int c3[3] = {xs[q], y, z};
-        if (!visit_box<3>(g, c3, c3, f)) return false;
+        if (!visit_box<3>(w, g, c3, c3, f, round)) return false;
       }
     }
+  }
+  return true;
+}
+
+// Distance from v to the interval that bin b of dimension d covers (0
+// inside), shrunk by a margin so that rounding in bin1() cannot hide a point.
+TECS_DL_HD double gap_to_bin(const Grid& g, int d, int b, double v) {
+  const double m = 1.0e-9 * g.h;
+  const double lo = g.lo[d] + (double)b * g.h - m, hi = g.lo[d] + (double)(b + 1) * g.h + m;
+  return v < lo ? lo - v : (v > hi ? v - hi : 0.0);
+}
+
+// The bins [a, b] of row (y, z) that can hold a point p with w.(p - o) > 0.
+template <int D>
+TECS_DL_HD void half_range(const Grid& g, int y, int z, const double* o, const double* w, int& a, int& b) {
+  const double m = 1.0e-9 * g.h;
+  // the largest w1 (y - o1) + w2 (z - o2) over the row's box
+  double off = 0.0;
+  for (int d = 1; d < D; ++d) {
+    const int bb = d == 1 ? y : z;
+    const double lo = g.lo[d] + (double)bb * g.h - m, hi = g.lo[d] + (double)(bb + 1) * g.h + m;
+    off += w[d] > 0.0 ? w[d] * (hi - o[d]) : w[d] * (lo - o[d]);
+  }
+  // need w0 (x - o0) + off > 0
+  a = 0;
+  b = g.dims[0] - 1;
+  if (w[0] > 0.0) a = bin1(g, 0, o[0] - off / w[0] - m);
+  else if (w[0] < 0.0) b = bin1(g, 0, o[0] - off / w[0] + m);
+  else if (!(off >= 0.0)) { a = 1; b = 0; }
+}
+
+// Every entry within distance rad of c (and a few just outside): the rows
+// of bins (along x) that the ball touches, each cut to the ball's chord --
+// and, given a plane (o, w), to the bins that reach its open side.
+template <int D, class W, class F, class R = NoRound>
+TECS_DL_HD bool visit_ball(const W& ln, const Grid& g, const double* c, double rad, F&& f, const double* o = nullptr,
+                           const double* w = nullptr, R&& round = R{}) {
+  if (!(rad < 1.0e300)) {
+    const int b0[3] = {0, 0, 0}, b1[3] = {g.dims[0] - 1, g.dims[1] - 1, g.dims[2] - 1};
+    return visit_box<D>(ln, g, b0, b1, f, round);
+  }
+  const int z0 = D >= 3 ? bin1(g, 2, c[2] - rad) : 0, z1 = D >= 3 ? bin1(g, 2, c[2] + rad) : 0;
+  const int y0 = bin1(g, 1, c[1] - rad), y1 = bin1(g, 1, c[1] + rad);
+  const double r2 = rad * rad;
+  for (int z = z0; z <= z1; ++z) {
+    const double gz = D >= 3 ? gap_to_bin(g, 2, z, c[2]) : 0.0;
+    for (int y = y0; y <= y1; ++y) {
+      const double gy = gap_to_bin(g, 1, y, c[1]);
+      const double rem2 = r2 - gy * gy - gz * gz;
+      if (rem2 < 0.0) continue;
+      const double rem = sqrt(rem2) * (1.0 + 1.0e-12) + 1.0e-9 * g.h;
+      int a = bin1(g, 0, c[0] - rem), b = bin1(g, 0, c[0] + rem);
+      if (w) {
+        int ha, hb;
+        half_range<D>(g, y, z, o, w, ha, hb);
+        a = imax(a, ha);
+        b = imin(b, hb);
+        if (a > b) continue;
+      }
+      const int lo3[3] = {a, y, z}, hi3[3] = {b, y, z};
+      if (!visit_box<3>(ln, g, lo3, hi3, f, round)) return false;
+    }
+  }
+  return true;
+}
+
+// Every entry p with w.(p - o) > 0 (and a few on the boundary): each row of
+// bins cut to the part that can reach the open side.
+template <int D, class W, class F>
+TECS_DL_HD bool visit_half(const W& ln, const Grid& g, const double* o, const double* w, F&& f) {
+  const int z1 = D >= 3 ? g.dims[2] - 1 : 0;
+  for (int z = 0; z <= z1; ++z)
+    for (int y = 0; y < g.dims[1]; ++y) {
+      int a, b;
+      half_range<D>(g, y, z, o, w, a, b);
+      if (a > b) continue;
+      const int lo3[3] = {a, y, z}, hi3[3] = {b, y, z};
+      if (!visit_box<3>(ln, g, lo3, hi3, f)) return false;
+    }
+  return true;
+}
+
+// 2-D: every entry within distance del of the line through o with unit
+// normal nrm (and a few just outside): each row of bins cut to the band.
+template <class W, class F, class R>
+TECS_DL_HD bool visit_band(const W& w, const Grid& g, const double* o, const double* nrm, double del, F&& f,
+                           R&& round) {
+  const double m = 1.0e-9 * g.h;
+  for (int y = 0; y < g.dims[1]; ++y) {
+    const double ylo = g.lo[1] + (double)y * g.h - m, yhi = g.lo[1] + (double)(y + 1) * g.h + m;
+    int a = 0, b = g.dims[0] - 1;
+    if (fabs(nrm[0]) > 1.0e-12) {
+      // n0 (x - o0) + n1 (y - o1) in [-del, del] over the row's y interval
+      double xmn = kInf, xmx = -kInf;
+      for (int e = 0; e < 4; ++e) {
+        const double yy = (e & 1) ? yhi : ylo, sg = (e & 2) ? del : -del;
+        const double x = o[0] + (sg - nrm[1] * (yy - o[1])) / nrm[0];
+        xmn = x < xmn ? x : xmn;
+        xmx = x > xmx ? x : xmx;
+      }
+      a = bin1(g, 0, xmn - m);
+      b = bin1(g, 0, xmx + m);
+    } else {
+      const double half = del / fabs(nrm[1]);
+      if (yhi < o[1] - half || ylo > o[1] + half) continue;
+    }
+    const int lo3[3] = {a, y, 0}, hi3[3] = {b, y, 0};
+    if (!visit_box<3>(w, g, lo3, hi3, f, round)) return false;
   }
   return true;
 }
@@ -229,22 +413,9 @@ TECS_DL_HD bool in_cutoff(const Grid& g, const Pt& pi, const Pt& pj) {
   return d2 < g.rc2;
 }
 
-// Box of bins that holds every point a float test at (c, reach) can reach.
-template <int D>
-TECS_DL_HD void reach_bins(const Grid& g, const float* c, float reach, int* b0, int* b1) {
-  bool all = !(reach < 3.0e38f);
-  for (int d = 0; d < D; ++d) all = all || !(c[d] > -3.0e38f && c[d] < 3.0e38f);
-  for (int d = 0; d < 3; ++d) { b0[d] = 0; b1[d] = g.dims[d] - 1; }
-  if (all) return;
-  const double m = (double)reach * (1.0 + 8.0 * kEps) + 1.0e-30;
-  for (int d = 0; d < D; ++d) {
-    b0[d] = bin1(g, d, (double)c[d] - m);
-    b1[d] = bin1(g, d, (double)c[d] + m);
-  }
-}
-
 // naive_delaunay.hpp:62-99: triangle (i, j, k) accepted
-TECS_DL_HD bool tri_pass(const Grid& g, unsigned i, unsigned j, unsigned k) {
+template <class W>
+TECS_DL_HD bool tri_pass(const W& w, const Grid& g, unsigned i, unsigned j, unsigned k) {
   const Pt pi = g.P[i], pj = g.P[j], pk = g.P[k];
   const float den = 2.0f * (pi.x * (pj.y - pk.y) + pj.x * (pk.y - pi.y) + pk.x * (pi.y - pj.y));
   if (fabsf(den) <= FLT_EPSILON) return false;
@@ -254,9 +425,12 @@ TECS_DL_HD bool tri_pass(const Grid& g, unsigned i, unsigned j, unsigned k) {
   c[1] = (li * (pk.x - pj.x) + lj * (pi.x - pk.x) + lk * (pj.x - pi.x)) / den;
   const float e0 = pi.x - c[0], e1 = pi.y - c[1];
   const float r2 = e0 * e0 + e1 * e1;
-  int b0[3], b1[3];
-  reach_bins<2>(g, c, sqrtf(r2), b0, b1);
-  return visit_box<2>(g, b0, b1, [&](unsigned m, const Pt& pm) {
+  // every point the test can reach: float distance^2 <= r2 means a true
+  // distance within sqrt(r2) (1 + a few eps)
+  const double cc[3] = {c[0], c[1], 0.0};
+  const double reach = (double)sqrtf(r2) * (1.0 + 8.0 * kEps) + 1.0e-30;
+  const bool finite = cc[0] > -1.0e30 && cc[0] < 1.0e30 && cc[1] > -1.0e30 && cc[1] < 1.0e30;
+  return visit_ball<2>(w, g, cc, finite ? reach : kInf, [&](unsigned m, const Pt& pm) {
     if (m == i || m == j || m == k) return true;
     const float f0 = pm.x - c[0], f1 = pm.y - c[1];
     return !(f0 * f0 + f1 * f1 <= r2);
@@ -271,53 +445,86 @@ struct Hit {
   double s;
 };
 
-// The first point p (not in ex) that becomes as close to x0 + s w as i is.
-template <int D>
-TECS_DL_HD Hit shoot(const Grid& g, const double* x0, const double* w, const double* pi, const unsigned* ex,
-                     int nex) {
+// The first point p (not in ex) that becomes as close to x0 + s w as i is:
+// the least s = (|x0 - p|^2 - |x0 - i|^2) / (2 w.(p - i)) over w.(p - i) > 0.
+// Every point with parameter <= s lies in the ball B(s) about x0 + s w
+// through i (on the open side of the plane through i), and B(s) grows with
+// s.  So: the bins around x0 first; then balls of doubling s until one holds
+// a point, whose least parameter is then the answer (after one more ball at
+// that parameter, for points just outside the last ball's bins); past the
+// grid's size, every bin on the open side of the plane.
+template <int D, class W>
+TECS_DL_HD Hit shoot(const W& ln, const Grid& g, const double* x0, const double* w, const double* pi,
+                     const unsigned* ex, int nex) {
   double pow0 = 0.0;
   for (int d = 0; d < D; ++d) { const double v = x0[d] - pi[d]; pow0 += v * v; }
-  Hit best{~0u, kInf};
+  Hit best{~0u, kInf};  // this lane's, then the warp's after each visit
+  auto take = [&](unsigned id, const Pt& p) {
+    for (int e = 0; e < nex; ++e)
+      if (id == ex[e]) return true;
+    double q[3];
+    load(p, q);
+    double wp = 0.0, nn = 0.0, num = 0.0;
+    for (int d = 0; d < D; ++d) {
+      const double v = q[d] - pi[d], u = q[d] - x0[d];
+      wp += w[d] * v;
+      nn += v * v;
+      num += u * u;
+    }
+    if (!(wp > 0.0) || wp * wp <= 1.0e-18 * nn) return true;  // on or behind the plane through i
+    const double s = (num - pow0) / (2.0 * wp);
+    if (s < best.s || (s == best.s && id < best.id)) best = Hit{id, s};
+    return true;
+  };
+  auto reduce = [&]() { lane_min(ln, best.s, best.id); };
+  // visits B(s) (with a margin)
+  auto ball_at = [&](double s) {
+    double c[3] = {0.0, 0.0, 0.0}, r2 = 0.0;
+    for (int d = 0; d < D; ++d) {
+      c[d] = x0[d] + s * w[d];
+      const double v = c[d] - pi[d];
+      r2 += v * v;
+    }
+    visit_ball<D>(ln, g, c, sqrt(r2) * (1.0 + 1.0e-9) + 1.0e-9 * g.h, take, pi, w);
+    reduce();
+  };
   int bc[3];
   bin_of<D>(g, x0, bc);
-  const int kmax = shells_to_cover<D>(g, bc);
-  for (int k = 0; k <= kmax; ++k) {
-    visit_shell<D>(g, bc, k, [&](unsigned id, const Pt& p) {
-      for (int e = 0; e < nex; ++e)
-        if (id == ex[e]) return true;
-      double q[3];
-      load(p, q);
-      double wp = 0.0, nn = 0.0, num = 0.0;
-      for (int d = 0; d < D; ++d) {
-        const double v = q[d] - pi[d], u = q[d] - x0[d];
-        wp += w[d] * v;
-        nn += v * v;
-        num += u * u;
-      }
-      if (!(wp > 1.0e-9 * sqrt(nn))) return true;  // on or behind the plane through i
-      const double s = (num - pow0) / (2.0 * wp);
-      if (s < best.s || (s == best.s && id < best.id)) best = Hit{id, s};
-      return true;
-    });
+  const int kmax = imin(1, shells_to_cover<D>(g, bc));
+  for (int k = 0; k <= kmax; ++k) visit_shell<D>(ln, g, bc, k, take);
+  reduce();
+  if (best.id != ~0u) {
+    double r2 = 0.0;
+    for (int d = 0; d < D; ++d) { const double v = x0[d] + best.s * w[d] - pi[d]; r2 += v * v; }
+    if (kmax == 1 && (1.0 - 1.0e-3) * g.h >= fabs(best.s) + sqrt(r2)) return best;
+    ball_at(best.s);
+    return best;
+  }
+  double span2 = 0.0;
+  for (int d = 0; d < D; ++d) { const double e = (double)g.dims[d] * g.h; span2 += e * e; }
+  const double span = sqrt(span2);
+  for (double s = g.h; s < 4.0 * span; s *= 2.0) {
+    ball_at(s);
     if (best.id != ~0u) {
-      double r2 = 0.0;
-      for (int d = 0; d < D; ++d) { const double v = x0[d] + best.s * w[d] - pi[d]; r2 += v * v; }
-      if (((double)k - 1.0e-3) * g.h >= fabs(best.s) + sqrt(r2)) break;
+      if (best.s > s) ball_at(best.s);
+      return best;
     }
   }
+  visit_half<D>(ln, g, pi, w, take);
+  reduce();
   return best;
 }
 
 // i's nearest other cell at a non-zero distance (ties by index).
-template <int D>
-TECS_DL_HD unsigned nearest(const Grid& g, const double* pi, unsigned self) {
+template <int D, class W>
+TECS_DL_HD unsigned nearest(const W& ln, const Grid& g, const double* pi, unsigned self) {
   double bd = kInf;
   unsigned bid = ~0u;
   int bc[3];
   bin_of<D>(g, pi, bc);
   const int kmax = shells_to_cover<D>(g, bc);
   for (int k = 0; k <= kmax; ++k) {
-    visit_shell<D>(g, bc, k, [&](unsigned id, const Pt& p) {
+    visit_shell<D>(ln, g, bc, k, [&](unsigned id, const Pt& p) {
       if (id == self) return true;
       double q[3];
       load(p, q);
@@ -326,6 +533,7 @@ TECS_DL_HD unsigned nearest(const Grid& g, const double* pi, unsigned self) {
       if (d2 > 0.0 && (d2 < bd || (d2 == bd && id < bid))) { bd = d2; bid = id; }
       return true;
     });
+    lane_min(ln, bd, bid);
     if (bid != ~0u && ((double)k - 1.0e-3) * g.h >= sqrt(bd)) break;
   }
   return bid;
@@ -348,6 +556,8 @@ struct Star {
   Sph s[kMaxSph];
   int nt = 0, ns = 0;
   unsigned err = 0;
+  unsigned open_end[2];  // 2-D: the neighbours at which the walk left the grid (i on the hull)
+  int n_open = 0;
 };
 
 // Rounding of the reference's float circumcentre for a simplex of this shape
@@ -368,11 +578,18 @@ TECS_DL_HD double shell_tol(const double* pi, const double (*e)[3], double R) {
   const double den = dmax(2.0 * fabs(det), 1.0e-300);
   double hp = 1.0;
   for (int q = 0; q < D - 1; ++q) hp *= hm;
-  // centre error: the b terms (|p|^2 differences, absolute error ~ eps L^2)
-  // times cofactors of size h^(D-1), over the determinant
-  const double dc = 32.0 * kEps * (L * L + hm * hm) * hp / den + 8.0 * kEps * L;
+  // Centre error (u = eps/2, the unit roundoff): the |x|^2 terms carry about
+  // 3 u L^2 each, times cofactors of size h^(D-1), summed over D + 1 terms
+  // with as many roundings of partial sums of size L^2 h^(D-1); the
+  // determinant's own relative error (about 6 u L h^(D-1) / den) moves a
+  // centre of size L by as much again: about 21 u L^2 h^(D-1) / den in all,
+  // taken here with a factor 2 to spare.
+  const double u = 0.5 * kEps;
+  const double dc = 48.0 * u * (L * L + hm * hm) * hp / den + 8.0 * u * L;
+  // |p - c|^2 - R moves by 2 r dc + dc^2 with the centre; the distance
+  // test's own roundings add a few u (R + L r); a factor 4 over both
   const double r = sqrt(R);
-  return 16.0 * (2.0 * r * dc + dc * dc) + 64.0 * kEps * (R + L * r);
+  return 4.0 * (2.0 * r * dc + dc * dc) + 32.0 * u * (R + L * r);
 }
 
 template <int D>
@@ -450,10 +667,11 @@ TECS_DL_HD void cross3(const double* a, const double* b, double* c) {
 // from vertex to vertex, each time across the edge of the newest neighbour,
 // until the walk is back at a (closed) or leaves the grid (i on the hull);
 // then the same from the other side.
-TECS_DL_HD void star2(const Grid& g, unsigned i, Star& st) {
+template <class W>
+TECS_DL_HD void star2(const W& ln, const Grid& g, unsigned i, Star& st) {
   double pi[3];
   load(g.P[i], pi);
-  const unsigned a = nearest<2>(g, pi, i);
+  const unsigned a = nearest<2>(ln, g, pi, i);
   if (a == ~0u) return;
   double pa[3];
   load(g.P[a], pa);
@@ -463,8 +681,11 @@ TECS_DL_HD void star2(const Grid& g, unsigned i, Star& st) {
   for (int side = 0; side < 2; ++side) {
     const double w[3] = {side ? -u[0] : u[0], side ? -u[1] : u[1], 0.0};
     const unsigned ex[2] = {i, a};
-    const Hit h = shoot<2>(g, x0, w, pi, ex, 2);
-    if (h.id == ~0u) continue;
+    const Hit h = shoot<2>(ln, g, x0, w, pi, ex, 2);
+    if (h.id == ~0u) {
+      if (st.n_open < 2) st.open_end[st.n_open++] = a;  // (i, a) is a hull edge
+      continue;
+    }
     const double c[3] = {x0[0] + h.s * w[0], x0[1] + h.s * w[1], 0.0};
     const int nt0 = st.nt;
     int q = add_simplex<2>(g, st, pi, a, h.id, ~0u, c);
@@ -480,8 +701,11 @@ TECS_DL_HD void star2(const Grid& g, unsigned i, Star& st) {
       if (n[0] * (pp[0] - pi[0]) + n[1] * (pp[1] - pi[1]) > 0.0) { n[0] = -n[0]; n[1] = -n[1]; }
       normalize3(n, 2);
       const unsigned ex2[3] = {i, cur, prev};
-      const Hit h2 = shoot<2>(g, v, n, pi, ex2, 3);
-      if (h2.id == ~0u) break;  // open: i is on the hull
+      const Hit h2 = shoot<2>(ln, g, v, n, pi, ex2, 3);
+      if (h2.id == ~0u) {  // open: (i, cur) is a hull edge
+        if (st.n_open < 2) st.open_end[st.n_open++] = cur;
+        break;
+      }
       const double c2[3] = {v[0] + h2.s * n[0], v[1] + h2.s * n[1], 0.0};
       const int cur_sph = st.t[q].sph, ns0 = st.ns, nt1 = st.nt;
       const int q2 = add_simplex<2>(g, st, pi, cur, h2.id, ~0u, c2);
@@ -500,10 +724,11 @@ TECS_DL_HD void star2(const Grid& g, unsigned i, Star& st) {
 
 // 3-D: breadth-first over i's Voronoi vertices, crossing each face of each
 // star tetrahedron that contains i once.
-TECS_DL_HD void star3(const Grid& g, unsigned i, Star& st) {
+template <class W>
+TECS_DL_HD void star3(const W& ln, const Grid& g, unsigned i, Star& st) {
   double pi[3];
   load(g.P[i], pi);
-  const unsigned a = nearest<3>(g, pi, i);
+  const unsigned a = nearest<3>(ln, g, pi, i);
   if (a == ~0u) return;
   double pa[3];
   load(g.P[a], pa);
@@ -519,10 +744,10 @@ TECS_DL_HD void star3(const Grid& g, unsigned i, Star& st) {
   cross3(ea, unit, u);
   normalize3(u, 3);
   const unsigned ex[2] = {i, a};
-  Hit h = shoot<3>(g, x0, u, pi, ex, 2);
+  Hit h = shoot<3>(ln, g, x0, u, pi, ex, 2);
   if (h.id == ~0u) {
     for (int d = 0; d < 3; ++d) u[d] = -u[d];
-    h = shoot<3>(g, x0, u, pi, ex, 2);
+    h = shoot<3>(ln, g, x0, u, pi, ex, 2);
   }
   if (h.id == ~0u) return;  // every other point on the line through i and a
   const unsigned b = h.id;
@@ -538,7 +763,7 @@ TECS_DL_HD void star3(const Grid& g, unsigned i, Star& st) {
   unsigned apex[2] = {~0u, ~0u};
   for (int side = 0; side < 2; ++side) {
     double w[3] = {side ? -n[0] : n[0], side ? -n[1] : n[1], side ? -n[2] : n[2]};
-    const Hit hd = shoot<3>(g, x1, w, pi, ex3, 3);
+    const Hit hd = shoot<3>(ln, g, x1, w, pi, ex3, 3);
     if (hd.id == ~0u) continue;
     const double c[3] = {x1[0] + hd.s * w[0], x1[1] + hd.s * w[1], x1[2] + hd.s * w[2]};
     q0[side] = add_simplex<3>(g, st, pi, a, b, hd.id, c);
@@ -565,7 +790,7 @@ TECS_DL_HD void star3(const Grid& g, unsigned i, Star& st) {
       normalize3(w, 3);
       const Sph& S = st.s[st.t[q].sph];
       const unsigned exf[4] = {i, A, B, O};
-      const Hit hf = shoot<3>(g, S.c, w, pi, exf, 4);
+      const Hit hf = shoot<3>(ln, g, S.c, w, pi, exf, 4);
       if (hf.id == ~0u) continue;  // open face: i is on the hull
       const double c[3] = {S.c[0] + hf.s * w[0], S.c[1] + hf.s * w[1], S.c[2] + hf.s * w[2]};
       const int q2 = add_simplex<3>(g, st, pi, A, B, hf.id, c);
@@ -583,14 +808,15 @@ struct JK {
   unsigned j, k;
 };
 
-template <int D>
-TECS_DL_HD unsigned cell_mult(const Grid& g, unsigned i, unsigned* out_j, unsigned* out_r, unsigned cap,
+template <int D, class W>
+TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* out_j, unsigned* out_r, unsigned cap,
                               unsigned* err, Star& st) {
   st.nt = 0;
   st.ns = 0;
   st.err = 0;
-  if (D == 2) star2(g, i, st);
-  else star3(g, i, st);
+  st.n_open = 0;
+  if (D == 2) star2(ln, g, i, st);
+  else star3(ln, g, i, st);
   unsigned e = st.err;
   JK pairs[kMaxPairs];
   int np = 0;
@@ -613,8 +839,8 @@ TECS_DL_HD unsigned cell_mult(const Grid& g, unsigned i, unsigned* out_j, unsign
   } else {
     unsigned near[kMaxNear];
     double dev[kMaxNear];
-    for (int q = 0; q < st.ns; ++q) {
-      const Sph S = st.s[q];
+    // the star circles, then one group per hull edge at i
+    for (int q = 0; q < st.ns + st.n_open; ++q) {
       // the circle's own triangle points first (deviation -1: never dropped),
       // then every point on or near it, or inside; when the array is full
       // the point farthest from the circle gives way
@@ -629,21 +855,73 @@ TECS_DL_HD unsigned cell_mult(const Grid& g, unsigned i, unsigned* out_j, unsign
           if (dev[x] > dev[w]) w = x;
         if (f < dev[w]) { near[w] = id; dev[w] = f; }
       };
-      for (int t = 0; t < st.nt; ++t)
-        if (st.t[t].sph == q) { put(st.t[t].v[0], -1.0); put(st.t[t].v[1], -1.0); }
-      const double rad = sqrt(S.R + S.tol) * (1.0 + 1.0e-9) + 1.0e-200;
-      int b0[3], b1[3];
-      for (int d = 0; d < 3; ++d) {
-        b0[d] = d < 2 ? bin1(g, d, S.c[d] - rad) : 0;
-        b1[d] = d < 2 ? bin1(g, d, S.c[d] + rad) : 0;
+      // a lane's candidate of the current round, put by every lane in lane order
+      bool has = false;
+      unsigned cid = 0u;
+      double cdev = 0.0;
+      auto merge = [&]() {
+        unsigned m = ln.ballot(has);
+        while (m) {
+          const int src = low_bit(m);
+          m &= m - 1u;
+          put(ln.bcast(cid, src), ln.bcast(cdev, src));
+        }
+        has = false;
+      };
+      if (q < st.ns) {
+        const Sph S = st.s[q];
+        double pi2[3], hm = 0.0;
+        load(Pi, pi2);
+        for (int t = 0; t < st.nt; ++t)
+          if (st.t[t].sph == q)
+            for (int v = 0; v < 2; ++v) {
+              put(st.t[t].v[v], -1.0);
+              double pv[3];
+              load(g.P[st.t[t].v[v]], pv);
+              hm = dmax(hm, sqrt((pv[0] - pi2[0]) * (pv[0] - pi2[0]) + (pv[1] - pi2[1]) * (pv[1] - pi2[1])));
+            }
+        auto near_test = [&](unsigned id, const Pt& p) {
+          if (id == i) return true;
+          const double u0 = (double)p.x - S.c[0], u1 = (double)p.y - S.c[1];
+          const double f = u0 * u0 + u1 * u1 - S.R;
+          if (f <= S.tol) { has = true; cid = id; cdev = fabs(f); }
+          return true;
+        };
+        // An alternative triangle to the circle's own is local: its points
+        // lie within a few of the triangle's edges of i.  A circle much
+        // larger than its triangle (a hull triangle, bulging out of the
+        // hull) meets the other cells only along the hull, where a wide
+        // float tolerance would take in cells far from i whose triangles
+        // with i enclose the hull's interior; those are searched near i.
+        const double rad = sqrt(S.R + S.tol) * (1.0 + 1.0e-9) + 1.0e-9 * g.h;
+        const double local = 4.0 * hm + 4.0 * g.h;
+        if (local < rad) visit_ball<2>(ln, g, pi2, local, near_test, nullptr, nullptr, merge);
+        else visit_ball<2>(ln, g, S.c, rad, near_test, nullptr, nullptr, merge);
+      } else {
+        // A hull edge (i, e): three points that are collinear in exact
+        // arithmetic can still give the reference a determinant above
+        // FLT_EPSILON (it rounds products of size L h, L the coordinates'
+        // size), and the huge circle of such a triangle holds no point when
+        // it bulges out of the hull, along a supporting line of i.  So the
+        // points near the line of each hull edge form one more group.
+        const unsigned e_id = st.open_end[q - st.ns];
+        double pi2[3], pe[3];
+        load(Pi, pi2);
+        load(g.P[e_id], pe);
+        double nrm[3] = {-(pe[1] - pi2[1]), pe[0] - pi2[0], 0.0};
+        normalize3(nrm, 2);
+        const double L = dmax(dmax(fabs(g.lo[0]), fabs(g.lo[0] + g.dims[0] * g.h)),
+                              dmax(fabs(g.lo[1]), fabs(g.lo[1] + g.dims[1] * g.h)));
+        const double span = (double)(g.dims[0] + g.dims[1]) * g.h;
+        const double del = 64.0 * 0.5 * kEps * L * (1.0 + span) + (double)FLT_EPSILON;
+        put(e_id, -1.0);
+        visit_band(ln, g, pi2, nrm, del, [&](unsigned id, const Pt& p) {
+          if (id == i) return true;
+          const double f = fabs(((double)p.x - pi2[0]) * nrm[0] + ((double)p.y - pi2[1]) * nrm[1]);
+          if (f <= del) { has = true; cid = id; cdev = f; }
+          return true;
+        }, merge);
       }
-      visit_box<2>(g, b0, b1, [&](unsigned id, const Pt& p) {
-        if (id == i) return true;
-        const double u0 = (double)p.x - S.c[0], u1 = (double)p.y - S.c[1];
-        const double f = u0 * u0 + u1 * u1 - S.R;
-        if (f <= S.tol) put(id, fabs(f));
-        return true;
-      });
       // the reference's test on every choice of j (in cutoff) and k among them
       for (int a = 0; a < nn; ++a) {
         const unsigned j = near[a];
@@ -653,7 +931,7 @@ TECS_DL_HD unsigned cell_mult(const Grid& g, unsigned i, unsigned* out_j, unsign
           if (k == j) continue;
           bool have = false;
           for (int p = 0; p < np && !have; ++p) have = pairs[p].j == j && pairs[p].k == k;
-          if (!have && tri_pass(g, i, j, k)) record(j, k);
+          if (!have && tri_pass(ln, g, i, j, k)) record(j, k);
         }
       }
     }

@@ -788,6 +788,7 @@ static __global__ void k_dl_scatter(const float4* __restrict__ X, const Counters
   sp[at] = v;
 }
 
+// one warp per cell: the lanes share each search's entries (dl::Warp)
 template <int D>
 static __global__ void __launch_bounds__(kDlThreads) k_dl_mult(const float4* __restrict__ X, Counters* __restrict__ ctr,
                                                                const DlState* __restrict__ st,
@@ -796,7 +797,7 @@ static __global__ void __launch_bounds__(kDlThreads) k_dl_mult(const float4* __r
                                                                const float4* __restrict__ sp, float rc2,
                                                                uint2* __restrict__ row, unsigned* __restrict__ len) {
   const unsigned n = ctr->n;
-  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // the same in every lane of the warp
   if (i >= n) return;
   dl::Grid g = dl_view(st);
   g.off = off;
@@ -807,7 +808,9 @@ static __global__ void __launch_bounds__(kDlThreads) k_dl_mult(const float4* __r
   g.rc2 = rc2;
   dl::Star star;
   unsigned oj[kDlRow], orp[kDlRow], err = 0;
-  const unsigned m = dl::cell_mult<D>(g, i, oj, orp, kDlRow, &err, star);
+  const dl::Warp lanes;
+  const unsigned m = dl::cell_mult<D>(lanes, g, i, oj, orp, kDlRow, &err, star);
+  if (lanes.lane() != 0u) return;
   for (unsigned t = 0; t < m; ++t) row[(size_t)i * kDlRow + t] = make_uint2(oj[t], orp[t]);
   len[i] = m;
   // a full near-circle list keeps the points nearest the circle (no error);

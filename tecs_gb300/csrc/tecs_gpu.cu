@@ -435,7 +435,7 @@ int enqueue_delaunay_star(tecs_sim* s, const PassArgs& a, int& K) {
   else k_dl_scatter<2><<<gb, 256, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_cnt, s->dl_off, s->dl_idx, s->dl_sp);
   PROF_END(s, "k_dl_grid");
   K += 6;
-  const unsigned mb = ceil_div(L ? L : 1, kDlThreads);
+  const unsigned mb = ceil_div(L ? L : 1, kDlThreads / 32);  // one warp per cell
   PROF_BEGIN(s);
   if (d3) k_dl_mult<3><<<mb, kDlThreads, 0, s->stream>>>(a.X, s->ctr, s->dl_st, s->dl_off, s->dl_idx, s->dl_sp,
                                                          s->fp.rc2, s->dl_row, s->dl_len);

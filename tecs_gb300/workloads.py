@@ -30,6 +30,14 @@ def ball(n: int, seed: int, radius: float | None = None) -> np.ndarray:
     return (d * r[:, None]).astype(np.float32)
 
 
+def disk(n: int, seed: int, density: float = 1.0) -> np.ndarray:
+    """n cells uniform in a 2-D disk of the given density."""
+    rng = np.random.default_rng(seed)
+    r = np.sqrt(rng.random(n) * n / (math.pi * density))
+    t = rng.random(n) * 2.0 * math.pi
+    return np.stack([r * np.cos(t), r * np.sin(t)], axis=1).astype(np.float32)
+
+
 def sheet_radius(n: int) -> float:
     return math.sqrt(n / (4.0 * math.pi)) * 0.8
 
