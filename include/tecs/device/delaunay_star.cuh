@@ -90,7 +90,7 @@ enum : unsigned {
 };
 
 constexpr int kMaxTet = 192;     // star simplices (3-D tetrahedra, 2-D triangles)
-constexpr int kMaxSph = 128;     // distinct star spheres
+constexpr int kMaxSph = 192;     // distinct star spheres (3-D: one per tetrahedron)
 constexpr int kMaxNear = 48;     // points near one circle (2-D)
 constexpr int kMaxPairs = 320;   // accepted (j, k)
 constexpr double kInf = 1.0e300;
@@ -618,6 +618,20 @@ TECS_DL_HD int add_simplex(const Grid& g, Star& st, const double* pi, unsigned a
   if (st.nt >= kMaxTet) { st.err |= kErrStar; return -1; }
   double R = 0.0;
   for (int d = 0; d < D; ++d) { const double u = c[d] - pi[d]; R += u * u; }
+  if (D == 3) {
+    // 3-D counts come from the tetrahedra; their centres only start the
+    // next searches, so each keeps its own (no merging, no tolerance)
+    if (st.ns >= kMaxSph) { st.err |= kErrStar; return -1; }
+    const int sp3 = st.ns++;
+    for (int d = 0; d < 3; ++d) st.s[sp3].c[d] = c[d];
+    st.s[sp3].R = R;
+    st.s[sp3].tol = 0.0;
+    const int q = st.nt++;
+    st.t[q].v[0] = v[0]; st.t[q].v[1] = v[1]; st.t[q].v[2] = v[2];
+    st.t[q].sph = sp3;
+    st.t[q].done = 0u;
+    return q;
+  }
   double e[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   for (int q = 0; q < D; ++q) {
     double p[3];

@@ -61,6 +61,13 @@ struct BinnedGabrielHeun2D : public DefaultSimulationConfig {
   RESOLVE_TECS_CONFIG()
 };
 
+struct NaiveDelaunayEuler2D : public DefaultSimulationConfig {
+  CONFIG_PAIR_FINDER(pair_finders::NaiveDelaunay)
+  CONFIG_INTEGRATOR(integrators::Euler)
+  CONFIG_DIMENSIONS(2)
+  RESOLVE_TECS_CONFIG()
+};
+
 struct Input {
   unsigned n = 0, dims = 0, has_pol = 0;
   float prm[16] = {};
@@ -371,6 +378,9 @@ int main(int argc, char** argv) {
     if (scenario == "bg_heun_functor") return run<BinnedGabrielHeun>(in, out, steps, dt, true);
     if (scenario == "bg_heun_com") return run<BinnedGabrielHeunCom>(in, out, steps, dt, false);
     if (scenario == "bg_heun_2d") return run<BinnedGabrielHeun2D>(in, out, steps, dt, false);
+    // NaiveDelaunay: the naive finder up to 4096 cells of capacity, the
+    // library's Delaunay finder of any capacity past that
+    if (scenario == "nd_euler_2d") return run<NaiveDelaunayEuler2D>(in, out, steps, dt, false);
     if (scenario == "bg_heun_pol") return run_polarity(in, out, steps, dt);
     if (scenario == "gen_bg_heun") return run_generic(in, out, steps, dt);
     if (scenario == "lk_bg_heun") return run_links<BinnedGabrielHeun>(in, out, steps, dt);

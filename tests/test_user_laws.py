@@ -214,3 +214,40 @@ def test_user_law_setting_drag_reproduces_reference(driver, tmp_path, name, exac
         # weights up to 0.6), so they agree to ~1e-5 absolute
         assert close(pos, g["pos"])
         assert close(ov, g["ov"], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.gpu
+def test_naive_delaunay_program_past_4096_cells_of_capacity(driver, tmp_path):
+    """A 2-D NaiveDelaunay program with a user law: up to 4096 cells of capacity the library runs the naive
+    finder, past that its Delaunay finder of any capacity (the user law's pass for FINDER 5).  The same cells
+    give the same pairs with the same multiplicities, deltas and 5-step Euler run either way, bit for bit."""
+    rng = np.random.default_rng(12)
+    n = 1200
+    r = np.sqrt(rng.random(n) * n / np.pi)
+    t = rng.random(n) * 2 * np.pi
+    x0 = np.stack([r * np.cos(t), r * np.sin(t)], 1).astype(np.float32)
+    outs = []
+    for cap in (n, 5000):
+        prm = np.zeros(16, np.float32)
+        prm[0] = 1.0                      # cutoff
+        prm[8:12] = (2.0, 0.7, 0.5, 0.8)  # the spring
+        prm[13] = cap
+        prm[14] = 1.0
+        g = {"x0": x0, "prm": prm}
+        d = tmp_path / f"cap{cap}"
+        d.mkdir()
+        inp = d / "in.bin"
+        write_input(inp, g)
+        out = d / "out"
+        res = subprocess.run([str(driver), "nd_euler_2d", str(inp), str(out), "5", "0.05"], capture_output=True,
+                             text=True, timeout=600, cwd=d)
+        assert res.returncode == 0, res.stderr
+        outs.append({k: np.fromfile(f"{out}.{k}", np.uint32 if k == "pairs" else np.float32)
+                     for k in ("pairs", "dpos", "pos")})
+    a, b = outs
+    pa = np.sort(a["pairs"].reshape(-1, 2).view(np.uint64).ravel())
+    pb = np.sort(b["pairs"].reshape(-1, 2).view(np.uint64).ravel())
+    assert len(pa) > 2 * n and len(np.unique(pa)) < len(pa)  # pairs repeat once per accepted triangle
+    np.testing.assert_array_equal(pa, pb)
+    np.testing.assert_array_equal(a["dpos"], b["dpos"])
+    np.testing.assert_array_equal(a["pos"], b["pos"])
