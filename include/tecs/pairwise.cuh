@@ -47,6 +47,7 @@
 #endif
 
 #include <cstring>
+#include <new>
 #include <memory>
 #include <utility>
 
@@ -291,7 +292,16 @@ struct PairLawBinding {
   static void bind(tecs_sim* handle, int device, const G& g, const P& p, const L& l, std::shared_ptr<void>& holder,
                    tecs_pair_law_fn& bound) {
     const tecs_pair_law_fn fn = &pair_law_launcher<Config, Law>;
-    const Law law{g, p, l};
+    // built in zeroed storage, so that padding between the members compares
+    // equal from one step to the next (padding inside the captured closures
+    // is copied as it is; unequal padding only costs one more copy)
+    alignas(Law) unsigned char storage[sizeof(Law)];
+    std::memset(storage, 0, sizeof(Law));
+    struct Built {
+      Law* p;
+      ~Built() { p->~Law(); }
+    } built{::new (static_cast<void*>(storage)) Law{g, p, l}};
+    const Law& law = *built.p;
     Bound* b = (holder && bound == fn) ? static_cast<Bound*>(holder.get()) : nullptr;
     if (!b) {
       if (prepare_user_pass<Config::dimensions, FinderOf<Config>::finder_id, Law>(device))
