@@ -98,12 +98,16 @@ constexpr double kEps = (double)FLT_EPSILON;
 
 // Lane policies.  Every search visits entries; Solo visits them in one
 // thread (the host), Warp in the 32 lanes of a warp, each lane taking every
-// 32nd entry.  Lanes keep identical copies of all other state: every result
-// of a visit is combined across the warp (a vote, a minimum, candidates
-// merged in lane order) before anything depends on it.
+// 32nd entry.  Every result of a visit is combined across the warp (a vote,
+// a minimum, candidates merged in lane order) before anything depends on it.
+// The star and the candidate lists (Scratch) are one copy per warp, in
+// shared memory on the device: every lane reads them, the leader lane writes
+// them between two sync() calls.
 struct Solo {
   static constexpr unsigned width = 1;
   TECS_DL_HD unsigned lane() const { return 0u; }
+  TECS_DL_HD bool leader() const { return true; }
+  TECS_DL_HD void sync() const {}
   TECS_DL_HD bool any(bool b) const { return b; }
   TECS_DL_HD unsigned ballot(bool b) const { return b ? 1u : 0u; }
   TECS_DL_HD unsigned bcast(unsigned v, int) const { return v; }
@@ -114,6 +118,8 @@ struct Solo {
 struct Warp {
   static constexpr unsigned width = 32;
   __device__ __forceinline__ unsigned lane() const { return threadIdx.x & 31u; }
+  __device__ __forceinline__ bool leader() const { return (threadIdx.x & 31u) == 0u; }
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
   __device__ __forceinline__ bool any(bool b) const { return __any_sync(0xffffffffu, b); }
   __device__ __forceinline__ unsigned ballot(bool b) const { return __ballot_sync(0xffffffffu, b); }
   __device__ __forceinline__ unsigned bcast(unsigned v, int src) const { return __shfl_sync(0xffffffffu, v, src); }
@@ -554,10 +560,23 @@ struct Sph {
 struct Star {
   Tet t[kMaxTet];
   Sph s[kMaxSph];
-  int nt = 0, ns = 0;
-  unsigned err = 0;
+  int nt, ns;
+  unsigned err;
   unsigned open_end[2];  // 2-D: the neighbours at which the walk left the grid (i on the hull)
-  int n_open = 0;
+  int n_open;
+};
+
+struct JK {
+  unsigned j, k;
+};
+
+// One cell's working state: the star, the accepted (j, k), one circle's
+// candidate points.
+struct Scratch {
+  Star st;
+  JK pairs[kMaxPairs];
+  unsigned near[kMaxNear];
+  double dev[kMaxNear];
 };
 
 // Rounding of the reference's float circumcentre for a simplex of this shape
@@ -605,61 +624,84 @@ TECS_DL_HD int find_sphere(Star& st, const double* c, double R) {
 }
 
 // Adds the simplex (i, a, b[, d]) with circumcentre c; returns its index.
-template <int D>
-TECS_DL_HD int add_simplex(const Grid& g, Star& st, const double* pi, unsigned a, unsigned b, unsigned d3,
-                           const double* c) {
+// Every lane computes the same values from the same snapshot; the leader
+// writes them.
+template <int D, class W>
+TECS_DL_HD int add_simplex(const W& ln, const Grid& g, Star& st, const double* pi, unsigned a, unsigned b,
+                           unsigned d3, const double* c) {
   unsigned v[3] = {a, b, D == 3 ? d3 : ~0u};
   // ascending (three elements)
   for (int x = 0; x < 2; ++x)
     for (int y = 0; y < 2 - x; ++y)
       if (v[y] > v[y + 1]) { const unsigned t = v[y]; v[y] = v[y + 1]; v[y + 1] = t; }
-  for (int q = 0; q < st.nt; ++q)
+  const int nt = st.nt, ns = st.ns;
+  for (int q = 0; q < nt; ++q)
     if (st.t[q].v[0] == v[0] && st.t[q].v[1] == v[1] && st.t[q].v[2] == v[2]) return q;
-  if (st.nt >= kMaxTet) { st.err |= kErrStar; return -1; }
   double R = 0.0;
   for (int d = 0; d < D; ++d) { const double u = c[d] - pi[d]; R += u * u; }
-  if (D == 3) {
-    // 3-D counts come from the tetrahedra; their centres only start the
-    // next searches, so each keeps its own (no merging, no tolerance)
-    if (st.ns >= kMaxSph) { st.err |= kErrStar; return -1; }
-    const int sp3 = st.ns++;
-    for (int d = 0; d < 3; ++d) st.s[sp3].c[d] = c[d];
-    st.s[sp3].R = R;
-    st.s[sp3].tol = 0.0;
-    const int q = st.nt++;
-    st.t[q].v[0] = v[0]; st.t[q].v[1] = v[1]; st.t[q].v[2] = v[2];
-    st.t[q].sph = sp3;
-    st.t[q].done = 0u;
-    return q;
+  // 3-D counts come from the tetrahedra; their centres only start the next
+  // searches, so each keeps its own (no merging, no tolerance)
+  double tol = 0.0;
+  int sp = -1;
+  if (D == 2) {
+    double e[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int q = 0; q < D; ++q) {
+      double p[3];
+      load(g.P[v[q]], p);
+      for (int d = 0; d < D; ++d) e[q][d] = p[d] - pi[d];
+    }
+    tol = shell_tol<D>(pi, e, R);
+    sp = find_sphere<D>(st, c, R);
   }
-  double e[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int q = 0; q < D; ++q) {
-    double p[3];
-    load(g.P[v[q]], p);
-    for (int d = 0; d < D; ++d) e[q][d] = p[d] - pi[d];
+  const bool fresh = sp < 0;
+  const bool full = nt >= kMaxTet || (fresh && ns >= kMaxSph);
+  const double old_tol = fresh ? 0.0 : st.s[sp].tol;
+  ln.sync();  // every lane has read what the leader writes next
+  if (ln.leader()) {
+    if (full) {
+      st.err |= kErrStar;
+    } else {
+      const int spw = fresh ? ns : sp;
+      if (fresh) {
+        for (int d = 0; d < 3; ++d) st.s[spw].c[d] = d < D ? c[d] : 0.0;
+        st.s[spw].R = R;
+        st.s[spw].tol = tol;
+        st.ns = ns + 1;
+      } else if (tol > old_tol) {
+        st.s[spw].tol = tol;
+      }
+      st.t[nt].v[0] = v[0];
+      st.t[nt].v[1] = v[1];
+      st.t[nt].v[2] = v[2];
+      st.t[nt].sph = spw;
+      st.t[nt].done = 0u;
+      st.nt = nt + 1;
+    }
   }
-  const double tol = shell_tol<D>(pi, e, R);
-  int sp = find_sphere<D>(st, c, R);
-  if (sp < 0) {
-    if (st.ns >= kMaxSph) { st.err |= kErrStar; return -1; }
-    sp = st.ns++;
-    for (int d = 0; d < 3; ++d) st.s[sp].c[d] = d < D ? c[d] : 0.0;
-    st.s[sp].R = R;
-    st.s[sp].tol = tol;
-  } else if (tol > st.s[sp].tol) {
-    st.s[sp].tol = tol;
-  }
-  const int q = st.nt++;
-  st.t[q].v[0] = v[0]; st.t[q].v[1] = v[1]; st.t[q].v[2] = v[2];
-  st.t[q].sph = sp;
-  st.t[q].done = 0u;
-  return q;
+  ln.sync();
+  return full ? -1 : nt;
 }
 
-TECS_DL_HD void mark_face(Star& st, int q, unsigned opposite) {
+template <class W>
+TECS_DL_HD void mark_face(const W& ln, Star& st, int q, unsigned opposite) {
   if (q < 0) return;
+  unsigned bits = st.t[q].done;
   for (int f = 0; f < 3; ++f)
-    if (st.t[q].v[f] == opposite) st.t[q].done |= 1u << f;
+    if (st.t[q].v[f] == opposite) bits |= 1u << f;
+  ln.sync();
+  if (ln.leader()) st.t[q].done = bits;
+  ln.sync();
+}
+
+template <class W>
+TECS_DL_HD void add_open_end(const W& ln, Star& st, unsigned e) {
+  const int k = st.n_open;
+  ln.sync();
+  if (ln.leader() && k < 2) {
+    st.open_end[k] = e;
+    st.n_open = k + 1;
+  }
+  ln.sync();
 }
 
 TECS_DL_HD void normalize3(double* v, int D) {
@@ -697,12 +739,12 @@ TECS_DL_HD void star2(const W& ln, const Grid& g, unsigned i, Star& st) {
     const unsigned ex[2] = {i, a};
     const Hit h = shoot<2>(ln, g, x0, w, pi, ex, 2);
     if (h.id == ~0u) {
-      if (st.n_open < 2) st.open_end[st.n_open++] = a;  // (i, a) is a hull edge
+      add_open_end(ln, st, a);  // (i, a) is a hull edge
       continue;
     }
     const double c[3] = {x0[0] + h.s * w[0], x0[1] + h.s * w[1], 0.0};
     const int nt0 = st.nt;
-    int q = add_simplex<2>(g, st, pi, a, h.id, ~0u, c);
+    int q = add_simplex<2>(ln, g, st, pi, a, h.id, ~0u, c);
     if (q < 0 || (side == 1 && st.nt == nt0)) return;
     unsigned prev = a, cur = h.id;
     double v[3] = {c[0], c[1], 0.0};
@@ -717,12 +759,12 @@ TECS_DL_HD void star2(const W& ln, const Grid& g, unsigned i, Star& st) {
       const unsigned ex2[3] = {i, cur, prev};
       const Hit h2 = shoot<2>(ln, g, v, n, pi, ex2, 3);
       if (h2.id == ~0u) {  // open: (i, cur) is a hull edge
-        if (st.n_open < 2) st.open_end[st.n_open++] = cur;
+        add_open_end(ln, st, cur);
         break;
       }
       const double c2[3] = {v[0] + h2.s * n[0], v[1] + h2.s * n[1], 0.0};
       const int cur_sph = st.t[q].sph, ns0 = st.ns, nt1 = st.nt;
-      const int q2 = add_simplex<2>(g, st, pi, cur, h2.id, ~0u, c2);
+      const int q2 = add_simplex<2>(ln, g, st, pi, cur, h2.id, ~0u, c2);
       if (q2 < 0) return;
       // back at a, at a triangle met before, or at an earlier vertex: closed
       closed = h2.id == a || st.nt == nt1 || (st.ns == ns0 && st.t[q2].sph != cur_sph);
@@ -780,16 +822,19 @@ TECS_DL_HD void star3(const W& ln, const Grid& g, unsigned i, Star& st) {
     const Hit hd = shoot<3>(ln, g, x1, w, pi, ex3, 3);
     if (hd.id == ~0u) continue;
     const double c[3] = {x1[0] + hd.s * w[0], x1[1] + hd.s * w[1], x1[2] + hd.s * w[2]};
-    q0[side] = add_simplex<3>(g, st, pi, a, b, hd.id, c);
+    q0[side] = add_simplex<3>(ln, g, st, pi, a, b, hd.id, c);
     apex[side] = hd.id;
   }
   // the face (i, a, b) between the two first tetrahedra is crossed
-  mark_face(st, q0[0], apex[0]);
-  mark_face(st, q0[1], apex[1]);
+  mark_face(ln, st, q0[0], apex[0]);
+  mark_face(ln, st, q0[1], apex[1]);
   for (int q = 0; q < st.nt; ++q) {
     for (int f = 0; f < 3; ++f) {
-      if (st.t[q].done & (1u << f)) continue;
-      st.t[q].done |= 1u << f;
+      const unsigned done = st.t[q].done;
+      if (done & (1u << f)) continue;
+      ln.sync();
+      if (ln.leader()) st.t[q].done = done | (1u << f);
+      ln.sync();
       const unsigned O = st.t[q].v[f], A = st.t[q].v[(f + 1) % 3], B = st.t[q].v[(f + 2) % 3];
       double pA[3], pB[3], pO[3];
       load(g.P[A], pA);
@@ -807,9 +852,9 @@ TECS_DL_HD void star3(const W& ln, const Grid& g, unsigned i, Star& st) {
       const Hit hf = shoot<3>(ln, g, S.c, w, pi, exf, 4);
       if (hf.id == ~0u) continue;  // open face: i is on the hull
       const double c[3] = {S.c[0] + hf.s * w[0], S.c[1] + hf.s * w[1], S.c[2] + hf.s * w[2]};
-      const int q2 = add_simplex<3>(g, st, pi, A, B, hf.id, c);
+      const int q2 = add_simplex<3>(ln, g, st, pi, A, B, hf.id, c);
       if (q2 < 0) return;
-      mark_face(st, q2, hf.id);
+      mark_face(ln, st, q2, hf.id);
     }
   }
 }
@@ -818,28 +863,34 @@ TECS_DL_HD void star3(const W& ln, const Grid& g, unsigned i, Star& st) {
 // One cell: its partners and how often the reference applies each pair.
 // out[0..return) = (j, reps), ascending j; *err gets the error bits.
 
-struct JK {
-  unsigned j, k;
-};
-
 template <int D, class W>
 TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* out_j, unsigned* out_r, unsigned cap,
-                              unsigned* err, Star& st) {
-  st.nt = 0;
-  st.ns = 0;
-  st.err = 0;
-  st.n_open = 0;
+                              unsigned* err, Scratch& sc) {
+  Star& st = sc.st;
+  JK* pairs = sc.pairs;
+  unsigned* near = sc.near;
+  double* dev = sc.dev;
+  ln.sync();
+  if (ln.leader()) {
+    st.nt = 0;
+    st.ns = 0;
+    st.err = 0u;
+    st.n_open = 0;
+  }
+  ln.sync();
   if (D == 2) star2(ln, g, i, st);
   else star3(ln, g, i, st);
   unsigned e = st.err;
-  JK pairs[kMaxPairs];
   int np = 0;
   const Pt Pi = g.P[i];
   auto record = [&](unsigned j, unsigned k) {
     for (int p = 0; p < np; ++p)
       if (pairs[p].j == j && pairs[p].k == k) return;
     if (np >= kMaxPairs) { e |= kErrPairs; return; }
-    pairs[np++] = JK{j, k};
+    ln.sync();
+    if (ln.leader()) pairs[np] = JK{j, k};
+    ln.sync();
+    ++np;
   };
   if (D == 3) {
     // every star tetrahedron (i, a, b, c): j one of them, k the lesser other
@@ -851,8 +902,6 @@ TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* 
       }
     }
   } else {
-    unsigned near[kMaxNear];
-    double dev[kMaxNear];
     // the star circles, then one group per hull edge at i
     for (int q = 0; q < st.ns + st.n_open; ++q) {
       // the circle's own triangle points first (deviation -1: never dropped),
@@ -862,12 +911,18 @@ TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* 
       auto put = [&](unsigned id, double f) {
         for (int x = 0; x < nn; ++x)
           if (near[x] == id) return;
-        if (nn < kMaxNear) { near[nn] = id; dev[nn] = f; ++nn; return; }
-        e |= kErrNear;
-        int w = 0;
-        for (int x = 1; x < nn; ++x)
-          if (dev[x] > dev[w]) w = x;
-        if (f < dev[w]) { near[w] = id; dev[w] = f; }
+        int at = nn;
+        if (nn >= kMaxNear) {
+          e |= kErrNear;
+          at = 0;
+          for (int x = 1; x < nn; ++x)
+            if (dev[x] > dev[at]) at = x;
+          if (!(f < dev[at])) return;
+        }
+        ln.sync();
+        if (ln.leader()) { near[at] = id; dev[at] = f; }
+        ln.sync();
+        if (at == nn) ++nn;
       };
       // a lane's candidate of the current round, put by every lane in lane order
       bool has = false;
@@ -950,13 +1005,16 @@ TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* 
       }
     }
   }
-  // (j, number of distinct k), ascending j
-  for (int x = 1; x < np; ++x) {
-    const JK v = pairs[x];
-    int y = x - 1;
-    while (y >= 0 && (pairs[y].j > v.j || (pairs[y].j == v.j && pairs[y].k > v.k))) { pairs[y + 1] = pairs[y]; --y; }
-    pairs[y + 1] = v;
-  }
+  // (j, number of distinct k), ascending j: sorted by the leader
+  ln.sync();
+  if (ln.leader())
+    for (int x = 1; x < np; ++x) {
+      const JK v = pairs[x];
+      int y = x - 1;
+      while (y >= 0 && (pairs[y].j > v.j || (pairs[y].j == v.j && pairs[y].k > v.k))) { pairs[y + 1] = pairs[y]; --y; }
+      pairs[y + 1] = v;
+    }
+  ln.sync();
   unsigned len = 0;
   for (int x = 0; x < np;) {
     int y = x;

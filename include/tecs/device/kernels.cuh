@@ -806,10 +806,12 @@ static __global__ void __launch_bounds__(kDlThreads) k_dl_mult(const float4* __r
   g.P = reinterpret_cast<const dl::Pt*>(X);
   g.n = n;
   g.rc2 = rc2;
-  dl::Star star;
+  // the warp's star and candidate lists: one copy, in shared memory
+  __shared__ __align__(16) unsigned char scratch[(kDlThreads / 32) * sizeof(dl::Scratch)];
+  dl::Scratch& sc = reinterpret_cast<dl::Scratch*>(scratch)[threadIdx.x >> 5];
   unsigned oj[kDlRow], orp[kDlRow], err = 0;
   const dl::Warp lanes;
-  const unsigned m = dl::cell_mult<D>(lanes, g, i, oj, orp, kDlRow, &err, star);
+  const unsigned m = dl::cell_mult<D>(lanes, g, i, oj, orp, kDlRow, &err, sc);
   if (lanes.lane() != 0u) return;
   for (unsigned t = 0; t < m; ++t) row[(size_t)i * kDlRow + t] = make_uint2(oj[t], orp[t]);
   len[i] = m;

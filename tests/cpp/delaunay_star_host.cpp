@@ -51,11 +51,11 @@ static int run(unsigned n, float cutoff, std::vector<Pt>& P) {
   g.P = P.data();
   g.n = n;
   g.rc2 = cutoff * cutoff;
-  static Star st;
+  static Scratch sc;
   unsigned oj[64], orr[64], err_all = 0;
   for (unsigned i = 0; i < n; ++i) {
     unsigned err = 0;
-    const unsigned len = cell_mult<D>(Solo{}, g, i, oj, orr, 64, &err, st);
+    const unsigned len = cell_mult<D>(Solo{}, g, i, oj, orr, 64, &err, sc);
     err_all |= err;
     if (err) std::printf("cellerr %u %u\n", i, err);
     for (unsigned t = 0; t < len; ++t) std::printf("%u %u %u\n", i, oj[t], orr[t]);
