@@ -13,7 +13,9 @@
 //
 //  1. A counting-sorted copy of the positions on a uniform grid (about two
 //     cells per bin) answers every geometric search below exactly: a search
-//     visits every bin that a ball or box can touch, in growing shells.
+//     visits every row of bins that its region (the shells around a point, a
+//     ball, an open half-space, a band along a line) can touch, each row cut
+//     to the region.
 //  2. Star of cell i, in double.  From i's nearest neighbour a, the walk
 //     moves through i's Voronoi cell: from a point x on it along a direction
 //     w, the first point p that becomes as close to x + s w as i is the one
@@ -30,9 +32,11 @@
 //     rounding of the float circumcentre, from the coordinates' size and the
 //     triangle's shape, times a safety factor), and the reference's own float
 //     test (with its emptiness check over every point the test can reach,
-//     found through the grid) runs on every (j, k) drawn from that set.
-//     mult(i, j) is the number of distinct k accepted: the reference's
-//     multiplicities, bit for bit.
+//     found through the grid) runs on every (j, k) drawn from that set.  On
+//     the hull, the points near the line of each hull edge at i form one more
+//     set (three collinear points can pass the float test there).  mult(i, j)
+//     is the number of distinct k accepted: the reference's multiplicities,
+//     bit for bit.
 //  4. 3-D: the reference's quotients solve 2 (x_m - x_i).c = |x_m|^2 -
 //     |x_i|^2, so they are the circumcentre itself; it adds x_i once more, and
 //     its sphere (centre x_i + c, radius |c|) passes through i but not through
@@ -42,9 +46,10 @@
 //     the number of distinct k = min(k, l) over the star tetrahedra
 //     (i, j, k, l).
 //
-// The same code runs on the device (one thread per cell, k_dl_mult) and on
-// the host (the tests' driver), so the walk can be checked on the CPU against
-// the naive restatement (2-D) and an independent Delaunay triangulation (3-D).
+// The same code runs on the device (one warp per cell, k_dl_mult; Warp
+// below) and on the host (the tests' driver; Solo), so the walk can be
+// checked on the CPU against the naive restatement (2-D) and an independent
+// Delaunay triangulation (3-D).
 #pragma once
 
 #include <float.h>
