@@ -287,31 +287,64 @@ TECS_DL_HD bool visit_shell(const W& w, const Grid& g, const int* bc, int k, F&&
   return true;
 }
 
+// Row ranges in float.  A search region's rows are the same in every lane
+// of a warp, and FP64 is scarce on this part, so the bounds are formed in
+// float with a margin m far above float rounding (1e-3 of a bin plus the
+// rounding of bin numbers and coordinates of the grid's size): a range can
+// only grow, so no point is lost, and the tests on the points stay exact.
+struct GridF {
+  float lo[3], h, inv, m;
+  int dims[3];
+};
+
+TECS_DL_HD GridF grid_f(const Grid& g) {
+  GridF f;
+  double span = 0.0;
+  int dm = 1;
+  for (int d = 0; d < 3; ++d) {
+    f.lo[d] = (float)g.lo[d];
+    f.dims[d] = g.dims[d];
+    span = dmax(span, fabs(g.lo[d]) + (double)g.dims[d] * g.h);
+    dm = imax(dm, g.dims[d]);
+  }
+  f.h = (float)g.h;
+  f.inv = (float)g.inv;
+  f.m = (float)(g.h * (1.0e-3 + 1.0e-6 * (double)dm) + 2.0e-6 * span);
+  return f;
+}
+
+TECS_DL_HD int bin1f(const GridF& f, int d, float x) {
+  const float t = floorf((x - f.lo[d]) * f.inv);
+  if (!(t >= 0.0f)) return 0;  // also NaN
+  if (t >= (float)(f.dims[d] - 1)) return f.dims[d] - 1;
+  return (int)t;
+}
+
 // Distance from v to the interval that bin b of dimension d covers (0
-// inside), shrunk by a margin so that rounding in bin1() cannot hide a point.
-TECS_DL_HD double gap_to_bin(const Grid& g, int d, int b, double v) {
-  const double m = 1.0e-9 * g.h;
-  const double lo = g.lo[d] + (double)b * g.h - m, hi = g.lo[d] + (double)(b + 1) * g.h + m;
-  return v < lo ? lo - v : (v > hi ? v - hi : 0.0);
+// inside), the interval widened by the margin.
+TECS_DL_HD float gap_to_bin(const GridF& f, int d, int b, float v) {
+  const float lo = f.lo[d] + (float)b * f.h - f.m, hi = f.lo[d] + (float)(b + 1) * f.h + f.m;
+  return v < lo ? lo - v : (v > hi ? v - hi : 0.0f);
 }
 
 // The bins [a, b] of row (y, z) that can hold a point p with w.(p - o) > 0.
 template <int D>
-TECS_DL_HD void half_range(const Grid& g, int y, int z, const double* o, const double* w, int& a, int& b) {
-  const double m = 1.0e-9 * g.h;
-  // the largest w1 (y - o1) + w2 (z - o2) over the row's box
-  double off = 0.0;
+TECS_DL_HD void half_range(const GridF& f, int y, int z, const float* o, const float* w, int& a, int& b) {
+  // the largest w1 (y - o1) + w2 (z - o2) over the row's box, then its margin
+  float off = 0.0f, aw = 0.0f;
   for (int d = 1; d < D; ++d) {
     const int bb = d == 1 ? y : z;
-    const double lo = g.lo[d] + (double)bb * g.h - m, hi = g.lo[d] + (double)(bb + 1) * g.h + m;
-    off += w[d] > 0.0 ? w[d] * (hi - o[d]) : w[d] * (lo - o[d]);
+    const float lo = f.lo[d] + (float)bb * f.h - f.m, hi = f.lo[d] + (float)(bb + 1) * f.h + f.m;
+    off += w[d] > 0.0f ? w[d] * (hi - o[d]) : w[d] * (lo - o[d]);
+    aw += fabsf(w[d]);
   }
+  off += aw * f.m;
   // need w0 (x - o0) + off > 0
   a = 0;
-  b = g.dims[0] - 1;
-  if (w[0] > 0.0) a = bin1(g, 0, o[0] - off / w[0] - m);
-  else if (w[0] < 0.0) b = bin1(g, 0, o[0] - off / w[0] + m);
-  else if (!(off >= 0.0)) { a = 1; b = 0; }
+  b = f.dims[0] - 1;
+  if (w[0] > 0.0f) a = bin1f(f, 0, o[0] - off / w[0] - f.m);
+  else if (w[0] < 0.0f) b = bin1f(f, 0, o[0] - off / w[0] + f.m);
+  else if (!(off >= 0.0f)) { a = 1; b = 0; }
 }
 
 // Every entry within distance rad of c (and a few just outside): the rows
@@ -320,24 +353,30 @@ TECS_DL_HD void half_range(const Grid& g, int y, int z, const double* o, const d
 template <int D, class W, class F, class R = NoRound>
 TECS_DL_HD bool visit_ball(const W& ln, const Grid& g, const double* c, double rad, F&& f, const double* o = nullptr,
                            const double* w = nullptr, R&& round = R{}) {
-  if (!(rad < 1.0e300)) {
+  if (!(rad < 1.0e18)) {
     const int b0[3] = {0, 0, 0}, b1[3] = {g.dims[0] - 1, g.dims[1] - 1, g.dims[2] - 1};
     return visit_box<D>(ln, g, b0, b1, f, round);
   }
-  const int z0 = D >= 3 ? bin1(g, 2, c[2] - rad) : 0, z1 = D >= 3 ? bin1(g, 2, c[2] + rad) : 0;
-  const int y0 = bin1(g, 1, c[1] - rad), y1 = bin1(g, 1, c[1] + rad);
-  const double r2 = rad * rad;
+  const GridF gf = grid_f(g);
+  const float cf[3] = {(float)c[0], (float)c[1], (float)c[2]};
+  const float rf = (float)rad * 1.00001f + gf.m;
+  float of[3] = {0.f, 0.f, 0.f}, wf[3] = {0.f, 0.f, 0.f};
+  if (w)
+    for (int d = 0; d < 3; ++d) { of[d] = (float)o[d]; wf[d] = (float)w[d]; }
+  const int z0 = D >= 3 ? bin1f(gf, 2, cf[2] - rf) : 0, z1 = D >= 3 ? bin1f(gf, 2, cf[2] + rf) : 0;
+  const int y0 = bin1f(gf, 1, cf[1] - rf), y1 = bin1f(gf, 1, cf[1] + rf);
+  const float r2 = rf * rf;
   for (int z = z0; z <= z1; ++z) {
-    const double gz = D >= 3 ? gap_to_bin(g, 2, z, c[2]) : 0.0;
+    const float gz = D >= 3 ? gap_to_bin(gf, 2, z, cf[2]) : 0.0f;
     for (int y = y0; y <= y1; ++y) {
-      const double gy = gap_to_bin(g, 1, y, c[1]);
-      const double rem2 = r2 - gy * gy - gz * gz;
-      if (rem2 < 0.0) continue;
-      const double rem = sqrt(rem2) * (1.0 + 1.0e-12) + 1.0e-9 * g.h;
-      int a = bin1(g, 0, c[0] - rem), b = bin1(g, 0, c[0] + rem);
+      const float gy = gap_to_bin(gf, 1, y, cf[1]);
+      const float rem2 = r2 - gy * gy - gz * gz + 1.0e-5f * r2;
+      if (rem2 < 0.0f) continue;
+      const float rem = sqrtf(rem2) + gf.m;
+      int a = bin1f(gf, 0, cf[0] - rem), b = bin1f(gf, 0, cf[0] + rem);
       if (w) {
         int ha, hb;
-        half_range<D>(g, y, z, o, w, ha, hb);
+        half_range<D>(gf, y, z, of, wf, ha, hb);
         a = imax(a, ha);
         b = imin(b, hb);
         if (a > b) continue;
@@ -353,11 +392,13 @@ TECS_DL_HD bool visit_ball(const W& ln, const Grid& g, const double* c, double r
 // bins cut to the part that can reach the open side.
 template <int D, class W, class F>
 TECS_DL_HD bool visit_half(const W& ln, const Grid& g, const double* o, const double* w, F&& f) {
+  const GridF gf = grid_f(g);
+  const float of[3] = {(float)o[0], (float)o[1], (float)o[2]}, wf[3] = {(float)w[0], (float)w[1], (float)w[2]};
   const int z1 = D >= 3 ? g.dims[2] - 1 : 0;
   for (int z = 0; z <= z1; ++z)
     for (int y = 0; y < g.dims[1]; ++y) {
       int a, b;
-      half_range<D>(g, y, z, o, w, a, b);
+      half_range<D>(gf, y, z, of, wf, a, b);
       if (a > b) continue;
       const int lo3[3] = {a, y, z}, hi3[3] = {b, y, z};
       if (!visit_box<3>(ln, g, lo3, hi3, f)) return false;
