@@ -995,11 +995,17 @@ TECS_DL_HD unsigned cell_mult(const W& ln, const Grid& g, unsigned i, unsigned* 
               load(g.P[st.t[t].v[v]], pv);
               hm = dmax(hm, sqrt((pv[0] - pi2[0]) * (pv[0] - pi2[0]) + (pv[1] - pi2[1]) * (pv[1] - pi2[1])));
             }
+        // |p - c|^2 - R <= tol, in float with a margin above its rounding:
+        // the set may only grow (every member's triangles are tested by the
+        // reference's float test), so no double work is needed per point
+        const float cx = (float)S.c[0], cy = (float)S.c[1], Rf = (float)S.R, tf = (float)S.tol;
+        const float reach = sqrtf(fmaxf(Rf + tf, 0.0f));
+        const float slack = 1.0e-5f * (Rf + tf + 2.0f * reach * (fabsf(cx) + fabsf(cy) + reach)) + 1.0e-30f;
         auto near_test = [&](unsigned id, const Pt& p) {
           if (id == i) return true;
-          const double u0 = (double)p.x - S.c[0], u1 = (double)p.y - S.c[1];
-          const double f = u0 * u0 + u1 * u1 - S.R;
-          if (f <= S.tol) { has = true; cid = id; cdev = fabs(f); }
+          const float u0 = p.x - cx, u1 = p.y - cy;
+          const float f = u0 * u0 + u1 * u1 - Rf;
+          if (f <= tf + slack) { has = true; cid = id; cdev = fabs((double)f); }
           return true;
         };
         // An alternative triangle to the circle's own is local: its points
