@@ -501,10 +501,11 @@ struct Hit {
 // the least s = (|x0 - p|^2 - |x0 - i|^2) / (2 w.(p - i)) over w.(p - i) > 0.
 // Every point with parameter <= s lies in the ball B(s) about x0 + s w
 // through i (on the open side of the plane through i), and B(s) grows with
-// s.  So: the bins around x0 first; then balls of doubling s until one holds
-// a point, whose least parameter is then the answer (after one more ball at
-// that parameter, for points just outside the last ball's bins); past the
-// grid's size, every bin on the open side of the plane.
+// s.  So: balls of doubling s, each cut to the open side, from half the
+// radius of the empty ball about x0, until one holds a point; its least
+// parameter is then the answer (after one more ball at that parameter, for
+// points just outside the last ball's bins); past the grid's size, every
+// bin on the open side of the plane.
 template <int D, class W>
 TECS_DL_HD Hit shoot(const W& ln, const Grid& g, const double* x0, const double* w, const double* pi,
                      const unsigned* ex, int nex) {
@@ -540,22 +541,12 @@ TECS_DL_HD Hit shoot(const W& ln, const Grid& g, const double* x0, const double*
     visit_ball<D>(ln, g, c, sqrt(r2) * (1.0 + 1.0e-9) + 1.0e-9 * g.h, take, pi, w);
     reduce();
   };
-  int bc[3];
-  bin_of<D>(g, x0, bc);
-  const int kmax = imin(1, shells_to_cover<D>(g, bc));
-  for (int k = 0; k <= kmax; ++k) visit_shell<D>(ln, g, bc, k, take);
-  reduce();
-  if (best.id != ~0u) {
-    double r2 = 0.0;
-    for (int d = 0; d < D; ++d) { const double v = x0[d] + best.s * w[d] - pi[d]; r2 += v * v; }
-    if (kmax == 1 && (1.0 - 1.0e-3) * g.h >= fabs(best.s) + sqrt(r2)) return best;
-    ball_at(best.s);
-    return best;
-  }
+  // the first ball: half the distance from x0 to i (the radius of the
+  // empty ball the search starts from), at least a twentieth of a bin
   double span2 = 0.0;
   for (int d = 0; d < D; ++d) { const double e = (double)g.dims[d] * g.h; span2 += e * e; }
   const double span = sqrt(span2);
-  for (double s = g.h; s < 4.0 * span; s *= 2.0) {
+  for (double s = dmax(0.5 * sqrt(pow0), 0.05 * g.h); s < 4.0 * span; s *= 2.0) {
     ball_at(s);
     if (best.id != ~0u) {
       if (best.s > s) ball_at(best.s);
