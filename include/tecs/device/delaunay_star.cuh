@@ -501,8 +501,8 @@ struct Hit {
 // the least s = (|x0 - p|^2 - |x0 - i|^2) / (2 w.(p - i)) over w.(p - i) > 0.
 // Every point with parameter <= s lies in the ball B(s) about x0 + s w
 // through i (on the open side of the plane through i), and B(s) grows with
-// s.  So: balls of doubling s, each cut to the open side, from half the
-// radius of the empty ball about x0, until one holds a point; its least
+// s.  So: balls of doubling s, each cut to the open side, from the radius
+// of the empty ball about x0, until one holds a point; its least
 // parameter is then the answer (after one more ball at that parameter, for
 // points just outside the last ball's bins); past the grid's size, every
 // bin on the open side of the plane.
@@ -541,12 +541,12 @@ TECS_DL_HD Hit shoot(const W& ln, const Grid& g, const double* x0, const double*
     visit_ball<D>(ln, g, c, sqrt(r2) * (1.0 + 1.0e-9) + 1.0e-9 * g.h, take, pi, w);
     reduce();
   };
-  // the first ball: half the distance from x0 to i (the radius of the
-  // empty ball the search starts from), at least a twentieth of a bin
+  // the first ball: s = the distance from x0 to i (the radius of the empty
+  // ball the search starts from), at least a twentieth of a bin
   double span2 = 0.0;
   for (int d = 0; d < D; ++d) { const double e = (double)g.dims[d] * g.h; span2 += e * e; }
   const double span = sqrt(span2);
-  for (double s = dmax(0.5 * sqrt(pow0), 0.05 * g.h); s < 4.0 * span; s *= 2.0) {
+  for (double s = dmax(sqrt(pow0), 0.05 * g.h); s < 4.0 * span; s *= 2.0) {
     ball_at(s);
     if (best.id != ~0u) {
       if (best.s > s) ball_at(best.s);
