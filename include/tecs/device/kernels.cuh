@@ -1017,8 +1017,8 @@ constexpr int kPassThreads = 96;
 // most 31 slots) and masks the extra slots off.
 constexpr unsigned kRowPad = 64;
 
-// nb: room for MAXN neighbours at a stride of kPassThreads
-template <int D, int FORCE, int MAXN = kMaxNb>
+// nb: room for MAXN neighbours at a stride of STRIDE (the block size)
+template <int D, int FORCE, int MAXN = kMaxNb, int STRIDE = kPassThreads>
 __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& fp, const PassArgs& a, unsigned i,
                                                   const float* xi, float2 pi, unsigned idi, Acc& acc,
                                                   float4* nb) {
@@ -1050,7 +1050,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
         if (cnt == MAXN) return false;
         const int rx = x0 + (j >= o1 ? 1 : 0) + (j >= o2 ? 1 : 0) - bc[0];
         const unsigned code = (unsigned)(rx + 1) | ((unsigned)(dy + 1) << 2) | ((unsigned)(dz + 1) << 4);
-        nb[cnt * kPassThreads] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 6) | code));
+        nb[cnt * STRIDE] = make_float4(vj.x, vj.y, vj.z, __uint_as_float((j << 6) | code));
         ++cnt;
       }
     }
@@ -1058,7 +1058,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
   // pass over the pairs: Gabriel test against the other neighbours
   unsigned accepted = 0u;
   for (int q = 0; q < cnt; ++q) {
-    const float4 vj = nb[q * kPassThreads];
+    const float4 vj = nb[q * STRIDE];
     float disp[3];
     disp[0] = xi[0] - vj.x;
     disp[1] = xi[1] - vj.y;
@@ -1081,7 +1081,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
     bool blocked = false;
     for (int w = 0; w < cnt && !blocked; ++w) {
       if (w == q) continue;
-      const float4 vk = nb[w * kPassThreads];
+      const float4 vk = nb[w * STRIDE];
       const unsigned code = __float_as_uint(vk.w) & 63u;
       const int rx = (int)(code & 3u) - 1, ry = (int)((code >> 2) & 3u) - 1, rz = (int)((code >> 4) & 3u) - 1;
       if (rx < lo[0] || rx > hi[0] || ry < lo[1] || ry > hi[1]) continue;
@@ -1098,7 +1098,7 @@ __device__ __forceinline__ bool gabriel_cell_fast(const GridP& g, const ForceP& 
   while (accepted) {
     const int q = __ffs(accepted) - 1;
     accepted &= accepted - 1u;
-    const float4 vj = nb[q * kPassThreads];
+    const float4 vj = nb[q * STRIDE];
     const unsigned j = __float_as_uint(vj.w) >> 6;
     float disp[3];
     disp[0] = xi[0] - vj.x;

@@ -251,6 +251,9 @@ int tecs_engine_destroy(tecs_engine* engine);
 int tecs_engine_bins_needed(const tecs_sim_desc* desc, unsigned* nbins);
 /* Free cells and the largest free run of bins (admission by free capacity). */
 int tecs_engine_free(tecs_engine* engine, unsigned* free_cells, unsigned* largest_free_bins);
+/* Threads per block of the engine's force passes: 64, 96 (the default) or 128.
+ * Results do not depend on it; the autotuner (tecs_gb300/batched.py) picks it. */
+int tecs_engine_set_pass_threads(tecs_engine* engine, unsigned threads);
 /* Admit a simulation with its initial state (host memory); *slot names it. */
 int tecs_engine_add(tecs_engine* engine, const tecs_sim_desc* desc, const float* positions, const float* polarity,
                     unsigned n, int* slot);

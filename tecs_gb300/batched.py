@@ -59,12 +59,16 @@ def size_class(n: int) -> str:
 
 
 def build_engine(members: List[Member], scales: Optional[Dict[str, float]] = None, device: int = 0):
+    """One engine holding every member; scales: bin-size scale per size class, and optionally the
+    passes' threads per block under "pass_threads" (autotune's result)."""
     scales = scales or {}
     descs = [m.desc(scales.get(size_class(len(m.x)), 1.0)) for m in members]
     cells = sum(len(m.x) for m in members)
     bins = sum(bins_needed(d) for d in descs)
     eng = Engine(cell_capacity=cells + 1024, bin_capacity=bins + 1024, max_sims=len(members) + 8, device=device)
     slots = [eng.add(d, m.x) for d, m in zip(descs, members)]
+    if scales.get("pass_threads"):
+        eng.set_pass_threads(int(scales["pass_threads"]))
     return eng, slots
 
 
@@ -83,11 +87,15 @@ def time_engine_steps(eng: Engine, steps: int, warmup: int = 2, dt: float = 0.05
     return e0.elapsed_time(e1) / 1e3
 
 
-def autotune(members: List[Member], candidates=(1.0, 1.25, 1.5), steps: int = 4, use_cache: bool = True):
-    """Bin-size scale per size class that minimises the batched step time.
+def autotune(members: List[Member], candidates=(1.0, 1.25, 1.5), steps: int = 4, use_cache: bool = True,
+             thread_candidates=(64, 96, 128)):
+    """Bin-size scale per size class, then the force passes' threads per block, that minimise the
+    batched step time.
 
-    Each candidate is timed on a fresh engine holding the members of that size
-    class only; results are cached per (class, cell count bucket, finder mix).
+    Each scale is timed on a fresh engine holding the members of that size class
+    only; then the whole ensemble, at the chosen scales, is timed at each block
+    size (chosen["pass_threads"]).  Results are cached per (class, cell count
+    bucket, finder mix) and per ensemble.
     """
     key_of = lambda cls, ms: f"{cls}:{int(math.log2(max(1, sum(len(m.x) for m in ms))))}:" \
                              f"{sum(m.finder == 'binned_gabriel' for m in ms)}/{len(ms)}"
@@ -116,6 +124,22 @@ def autotune(members: List[Member], candidates=(1.0, 1.25, 1.5), steps: int = 4,
         chosen[cls] = float(best)
         timings[cls] = res
         cache[key] = {"scale": float(best), "timings": res}
+    if thread_candidates:
+        key = "threads:" + ",".join(f"{cls}={chosen[cls]}" for cls in sorted(chosen)) + ":" + key_of("all", members)
+        if key in cache:
+            chosen["pass_threads"] = cache[key]["threads"]
+            timings["pass_threads"] = cache[key]["timings"]
+        else:
+            eng, _ = build_engine(members, chosen)
+            res = {}
+            for t in thread_candidates:
+                eng.set_pass_threads(t)
+                res[str(t)] = time_engine_steps(eng, steps, warmup=1)
+            eng.close()
+            best = min(res, key=res.get)
+            chosen["pass_threads"] = int(best)
+            timings["pass_threads"] = res
+            cache[key] = {"threads": int(best), "timings": res}
     if use_cache:
         CACHE.parent.mkdir(parents=True, exist_ok=True)
         CACHE.write_text(json.dumps(cache, indent=1, sort_keys=True))

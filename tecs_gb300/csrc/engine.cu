@@ -147,19 +147,23 @@ static __global__ void k_eorder_gather(const unsigned* __restrict__ off, unsigne
 // POL: some resident simulation carries polarity; their cells then take the
 // cooperative path with the polarity law, its pair terms added in the ordered
 // sums -- spring-only engines use the instance without that branch.
-template <int PASS, bool POL>
-static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
+// TB: threads per block (64, 96 or 128; the autotuner's choice).
+template <int TB>
+__device__ __forceinline__ int ecix(int q, int c) { return q * TB + (c ^ q); }
+
+template <int PASS, bool POL, int TB>
+static __global__ void __launch_bounds__(TB) k_epass(EngArgs e) {
   constexpr int NB = kMaxNb;  // neighbour slots per cell (more: the per-thread path)
-  __shared__ float4 cand[NB * kPassThreads];
-  __shared__ float4 home[kPassThreads];
-  __shared__ unsigned short pinfo[NB * kPassThreads];
-  __shared__ unsigned short wcls[kPassThreads / 32][NB + 1];  // pairs per (warp, neighbour count)
-  __shared__ unsigned amask[kPassThreads];
-  __shared__ unsigned char ncnt[kPassThreads];
-  __shared__ unsigned hsim[kPassThreads];
+  __shared__ float4 cand[NB * TB];
+  __shared__ float4 home[TB];
+  __shared__ unsigned short pinfo[NB * TB];
+  __shared__ unsigned short wcls[TB / 32][NB + 1];  // pairs per (warp, neighbour count)
+  __shared__ unsigned amask[TB];
+  __shared__ unsigned char ncnt[TB];
+  __shared__ unsigned hsim[TB];
   const unsigned n = e.off[e.nb_total];
   const int t = threadIdx.x;
-  const unsigned i = blockIdx.x * kPassThreads + t;
+  const unsigned i = blockIdx.x * TB + t;
   const bool active = i < n;
   const unsigned sim = active ? e.Bsim[i] : 0u;
   const SimSlot& sl = e.table[sim];
@@ -241,7 +245,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
           mm &= mm - 1u;
           const float4 v = __ldg(&e.X[j]);
           const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
-          cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
+          cand[ecix<TB>(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
           ++cnt;
         }
       }
@@ -289,7 +293,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     const int c = (int)(info >> 4), q = (int)(info & 15u);
     const SimSlot& cs = e.table[hsim[c]];
     const float4 h = home[c];
-    const float4 vj = cand[cix(q, c)];
+    const float4 vj = cand[ecix<TB>(q, c)];
     const float hx[3] = {h.x, h.y, h.z};
     const float disp[3] = {hx[0] - vj.x, hx[1] - vj.y, hx[2] - vj.z};
     float d2 = disp[0] * disp[0] + disp[1] * disp[1];
@@ -302,7 +306,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     unsigned hits = 0u, bit = 1u;
     for (int w = 0; w < cc; w += 2) {
       const int w1 = min(w + 1, cc - 1);
-      const float4 vk0 = cand[cix(w, c)], vk1 = cand[cix(w1, c)];
+      const float4 vk0 = cand[ecix<TB>(w, c)], vk1 = cand[ecix<TB>(w1, c)];
       const float f0 = vk0.x - m[0], f1 = vk0.y - m[1], f2 = vk0.z - m[2];
       const float g0 = vk1.x - m[0], g1 = vk1.y - m[1], g2 = vk1.z - m[2];
       float sd0 = f0 * f0 + f1 * f1, sd1 = g0 * g0 + g1 * g1;
@@ -329,7 +333,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
       while (hits && !blocked) {
         const int w = __ffs(hits) - 1;
         hits &= hits - 1u;
-        const unsigned code = __float_as_uint(cand[cix(w, c)].w) & 31u;
+        const unsigned code = __float_as_uint(cand[ecix<TB>(w, c)].w) & 31u;
         const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
         bool inside = true;
 #pragma unroll
@@ -364,7 +368,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
     const SimSlot& cs = e.table[hsim[c]];
     const float4 h = home[c];
-    const float4 vj = cand[cix(q, c)];
+    const float4 vj = cand[ecix<TB>(q, c)];
     const float disp[3] = {h.x - vj.x, h.y - vj.y, h.z - vj.z};
     float d2 = disp[0] * disp[0] + disp[1] * disp[1];
     d2 = d2 + disp[2] * disp[2];
@@ -380,7 +384,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
         f.z = (disp[2] * F) / dist;
       }
     }
-    cand[cix(q, c)] = f;
+    cand[ecix<TB>(q, c)] = f;
   }
   __syncwarp();
   // ---- ordered per-cell sums
@@ -389,7 +393,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     const bool pol_law = POL && polar && sl.fp.force == TECS_FORCE_POLARITY;
     for (int q = 0; q < cnt; ++q) {
       if (!((amask[t] >> q) & 1u)) continue;
-      const float4 f = cand[cix(q, t)];
+      const float4 f = cand[ecix<TB>(q, t)];
       if (pol_law) {
         // this pair's spring, bending vector, bending and alignment terms, each
         // added to the sums in turn (polarity.hpp:131-198 as pair_force adds them)
@@ -419,7 +423,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_epass(EngArgs e) {
     const int force = sl.fp.force;
     if (gab) {
       if (force == TECS_FORCE_POLARITY) {
-        if (!(sl.gabriel_fast && gabriel_cell_fast<3, 2, NB>(sl.g, sl.fp, pa, i, xi, pi, idi, acc, &cand[t])))
+        if (!(sl.gabriel_fast && gabriel_cell_fast<3, 2, NB, TB>(sl.g, sl.fp, pa, i, xi, pi, idi, acc, &cand[t])))
           cell_general<3, 3, 2>(sl.g, sl.fp, pa, n, i, xi, pi, idi, acc);
       } else if (force == TECS_FORCE_SPRING2R) {
         cell_general<3, 3, 1>(sl.g, sl.fp, pa, n, i, xi, pi, idi, acc);
@@ -531,6 +535,8 @@ struct tecs_engine {
   unsigned gC = 0, gNB = 0;  // the extents the captured graph covers (cells, bins)
   bool gpol = false;         // the captured graph runs the polarity-capable pass
   int kernels = 7;
+  unsigned pass_threads = 96;  // threads per block of the force passes (64, 96 or 128)
+  unsigned gTB = 0;            // ... in the captured graph
 };
 
 namespace {
@@ -610,14 +616,20 @@ int enqueue_engine_step(tecs_engine* e, float dt) {
   EngArgs a2 = a;
   a2.X = e->Xt;
   a2.P = e->Pt;
-  const unsigned blocks = cdiv(e->gC, kPassThreads);
-  if (e->gpol) {
-    k_epass<1, true><<<blocks, kPassThreads, 0, e->stream>>>(a1);
-    k_epass<2, true><<<blocks, kPassThreads, 0, e->stream>>>(a2);
-  } else {
-    k_epass<1, false><<<blocks, kPassThreads, 0, e->stream>>>(a1);
-    k_epass<2, false><<<blocks, kPassThreads, 0, e->stream>>>(a2);
+  const unsigned TB = e->pass_threads;
+  const unsigned blocks = cdiv(e->gC, TB);
+#define EPASS(T)                                                    \
+  if (TB == T) {                                                    \
+    if (e->gpol) {                                                  \
+      k_epass<1, true, T><<<blocks, T, 0, e->stream>>>(a1);         \
+      k_epass<2, true, T><<<blocks, T, 0, e->stream>>>(a2);         \
+    } else {                                                        \
+      k_epass<1, false, T><<<blocks, T, 0, e->stream>>>(a1);        \
+      k_epass<2, false, T><<<blocks, T, 0, e->stream>>>(a2);        \
+    }                                                               \
   }
+  EPASS(64) EPASS(96) EPASS(128)
+#undef EPASS
   ECK(cudaGetLastError());
   return 0;
 }
@@ -703,6 +715,13 @@ int tecs_engine_destroy(tecs_engine* e) {
   if (e->stream) cudaStreamDestroy(e->stream);
   if (e->side) cudaStreamDestroy(e->side);
   delete e;
+  return 0;
+}
+
+int tecs_engine_set_pass_threads(tecs_engine* e, unsigned threads) {
+  if (!e) return fail("null engine");
+  if (threads != 64 && threads != 96 && threads != 128) return fail("pass threads must be 64, 96 or 128");
+  e->pass_threads = threads;  // the next step captures its graph again
   return 0;
 }
 
@@ -857,11 +876,13 @@ int tecs_engine_step(tecs_engine* e, double dt, int n_steps) {
         pol = pol || e->htable[k].has_pol;
       }
     const unsigned wantC = extent_class(e->n_resident, e->C), wantNB = extent_class(hwm, e->NB);
-    if (!e->graph || e->gdt != fdt || wantC != e->gC || wantNB != e->gNB || pol != e->gpol) {
+    if (!e->graph || e->gdt != fdt || wantC != e->gC || wantNB != e->gNB || pol != e->gpol ||
+        e->gTB != e->pass_threads) {
       if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
       e->gC = wantC;
       e->gNB = wantNB;
       e->gpol = pol;
+      e->gTB = e->pass_threads;
       cudaGraph_t g;
       ECK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_engine_step(e, fdt);

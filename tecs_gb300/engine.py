@@ -35,6 +35,7 @@ def _lib():
     L.tecs_engine_destroy.argtypes = [vp]
     L.tecs_engine_bins_needed.argtypes = [ctypes.POINTER(SimDesc), up]
     L.tecs_engine_free.argtypes = [vp, up, up]
+    L.tecs_engine_set_pass_threads.argtypes = [vp, ctypes.c_uint]
     L.tecs_engine_add.argtypes = [vp, ctypes.POINTER(SimDesc), vp, vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_int)]
     L.tecs_engine_remove.argtypes = [vp, ctypes.c_int]
     L.tecs_engine_step.argtypes = [vp, ctypes.c_double, ctypes.c_int]
@@ -50,7 +51,8 @@ def _lib():
     for name in ("tecs_engine_desc_default", "tecs_engine_create", "tecs_engine_destroy", "tecs_engine_bins_needed",
                  "tecs_engine_free", "tecs_engine_add", "tecs_engine_remove", "tecs_engine_step",
                  "tecs_engine_synchronize", "tecs_engine_count", "tecs_engine_download", "tecs_engine_snapshot_async",
-                 "tecs_engine_event_query", "tecs_engine_event_destroy", "tecs_engine_kernels_per_step"):
+                 "tecs_engine_event_query", "tecs_engine_event_destroy", "tecs_engine_kernels_per_step",
+                 "tecs_engine_set_pass_threads"):
         getattr(L, name).restype = ctypes.c_int
     _bound = True
     return L
@@ -84,6 +86,10 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+    def set_pass_threads(self, threads: int):
+        """Threads per block of the force passes: 64, 96 or 128 (results do not depend on it)."""
+        _check(_lib().tecs_engine_set_pass_threads(self._h, int(threads)))
 
     def free(self):
         c, b = ctypes.c_uint(), ctypes.c_uint()

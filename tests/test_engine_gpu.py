@@ -154,3 +154,29 @@ def test_engine_after_other_engines_closed_matches_plain_runs():
         np.testing.assert_array_equal(xe, s.get_state()[0])
         s.close()
     eng.close()
+
+
+@pytest.mark.parametrize("threads", [64, 128])
+def test_engine_block_size_changes_no_result(threads):
+    """The force passes at 64 or 128 threads per block (the autotuner's other choices) give the plain runs'
+    trajectories bit for bit, also with a polarity simulation resident; a change between steps recaptures
+    the step graph."""
+    cases = [(1500, 61, "binned_gabriel", "heun"), (900, 62, "binned_all_pairs", "euler"),
+             (4000, 63, "binned_gabriel", "euler")]
+    specs = [spec(n, sd, f, it) for n, sd, f, it in cases]
+    pol = spec(1200, 64, "binned_gabriel", "heun", polarity=True)
+    eng = Engine(cell_capacity=12000, bin_capacity=sum(bins_needed(s[2]) for s in specs + [pol]) + 100, max_sims=8)
+    slots = [eng.add(d, x, p) for x, p, d, _, _ in specs]
+    sp = eng.add(pol[2], pol[0], pol[1])
+    eng.step(0.05, 2)
+    eng.set_pass_threads(threads)
+    eng.step(0.05, 3)
+    for (x, p, d, settings, force), slot, case in zip(specs, slots, cases):
+        xe, _ = eng.download(slot)
+        np.testing.assert_array_equal(xe, plain_run(x, p, settings, case[2], case[3], force, False, 5)[0])
+    xe, pe = eng.download(sp)
+    xp, pp = plain_run(pol[0], pol[1], pol[3], "binned_gabriel", "heun", pol[4], True, 5)
+    np.testing.assert_array_equal(xe, xp)
+    np.testing.assert_array_equal(pe, pp)
+    with pytest.raises(tg.TecsError, match="64, 96 or 128"):
+        eng.set_pass_threads(100)
