@@ -154,14 +154,18 @@ void writer_loop(tecs_serve* s) {
       s->files.erase(sn.id);  // the file's superblock is written as it closes
       continue;
     }
-    for (;;) {
+    // the copy's event, waited for at most a minute (a copy that never
+    // completes loses its snapshot, not the writer)
+    bool ok = true;
+    for (int polls = 0;; ++polls) {
       int ready = 0;
-      if (tecs_engine_event_query(sn.event, &ready) != 0 || ready) break;
+      if (tecs_engine_event_query(sn.event, &ready) != 0) { ok = false; break; }
+      if (ready) break;
+      if (polls >= 300000) { ok = false; break; }
       std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
     tecs_engine_event_destroy(sn.event);
-    bool ok = true;
-    if (s->d.snapshot_dir) {
+    if (ok && s->d.snapshot_dir) {
       try {
         auto& f = s->files[sn.id];
         if (!f) {
@@ -182,6 +186,9 @@ void writer_loop(tecs_serve* s) {
     if (ok) ++s->snaps_written;
     else ++s->snaps_errors;
     --s->snaps_pending;
+    // taken and released so that a drain between its check and its wait
+    // cannot miss this notification
+    { std::lock_guard<std::mutex> lock(s->mu); }
     s->cv.notify_all();
   }
 }
