@@ -1398,8 +1398,11 @@ __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c 
 // FINDER 3: binned Gabriel; FINDER 1: binned all-pairs (i's bin by
 // multiplication, binned_all_pairs.hpp:103-109, and every in-cutoff pair
 // accepted: no phase 2).
+// One block's cells blk * kPassThreads .. (only warp-level synchronisation,
+// so a kernel may run several blocks' cells one after another).
 template <int D, int FORCE, int FINDER = 3>
-static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
+__device__ __forceinline__ void pass_gabriel_block(const GridP& g, const ForceP& fp, const PassArgs& a,
+                                                   const unsigned blk) {
   static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
   static_assert(FINDER == 1 || FINDER == 3, "the binned finders");
   constexpr bool POL = FORCE == 2;
@@ -1414,7 +1417,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
 
   const unsigned n = a.ctr->n;
   const int t = threadIdx.x;
-  const unsigned i = blockIdx.x * kPassThreads + t;
+  const unsigned i = blk * kPassThreads + t;
   const bool active = i < n;
   float xi[3] = {0.f, 0.f, 0.f};
   float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1640,7 +1643,7 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     if (D >= 3) d2 = d2 + disp[2] * disp[2];
     if (a.pairs) {
       const unsigned j = __float_as_uint(vj.w) >> 5;
-      const unsigned ci = blockIdx.x * kPassThreads + c;
+      const unsigned ci = blk * kPassThreads + c;
       unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
       if (s < a.pair_cap) a.pairs[s] = make_uint2(id_at(a.X, a.Bid, ci), id_at(a.X, a.Bid, j));
     }
@@ -1688,6 +1691,11 @@ static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, F
     }
   }
   pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
+}
+
+template <int D, int FORCE, int FINDER = 3>
+static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
+  pass_gabriel_block<D, FORCE, FINDER>(g, fp, a, blockIdx.x);
 }
 
 // Symmetric finders (…_symmetric.hpp): only j with a smaller id, +delta to the
@@ -1753,6 +1761,111 @@ static __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, Pas
     }
   } else {
     for (unsigned j = 0; j < n; ++j) one(j);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One step of a small simulation in one cluster of kSmallCtas blocks (up to
+// kSmallCells cells and kSmallBins bins; the binned finders on the geometry of
+// the cooperative pass, no COM fix, no division, no extra fields, built-in
+// laws): the bin counts (made by the previous step's epilogue, or here), their
+// scan, the scatter, the in-bin id order, then the pass (Euler) or both passes
+// (Heun) -- what the rebuild kernels and the fused passes do over the grid,
+// for a step whose launches would otherwise each cost more than their work.
+// The phases are separated by cluster barriers (release/acquire at cluster
+// scope); every block scans all the counts into its own shared memory, so the
+// scan needs no barrier of its own; each block runs the cooperative pass
+// (pass_gabriel_block) over blocks of cells blockIdx.x, + kSmallCtas, ...  The
+// arithmetic is that of the passes over the grid, so runs are bit-identical.
+// The cluster size is set at launch (16 blocks: past the portable 8, opted
+// into per kernel).
+constexpr int kSmallCtas = 16;
+constexpr unsigned kSmallCells = 4096;
+constexpr unsigned kSmallBins = 16384;
+constexpr size_t kSmallSmem = (kSmallBins + 1) * sizeof(unsigned);
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <int D, int FINDER, int FORCE>
+static __global__ void __launch_bounds__(kPassThreads)
+    k_step_small(GridP g, ForceP fp, PassArgs p1, PassArgs p2, int heun, int run_count, const float4* A,
+                 const float2* PA, float4* B, float2* PB, unsigned* Bid, unsigned* off, unsigned* src,
+                 unsigned part_words) {
+  extern __shared__ unsigned offs[];  // the exclusive scan of the counts, nbins + 1 words
+  __shared__ unsigned wsum[kPassThreads / 32];
+  const unsigned n = p1.ctr->n, t = threadIdx.x;
+  const unsigned g0 = blockIdx.x * kPassThreads + t, gs = kSmallCtas * kPassThreads;
+  const int lane = t & 31, warp = t >> 5;
+  const unsigned len = g.nbins + 1;
+  // 1. bin counts of A (the previous step's epilogue made them unless run_count)
+  if (run_count) {
+    for (unsigned c = g0; c < n; c += gs) {
+      const float4 v = A[c];
+      const float q[3] = {v.x, v.y, v.z};
+      int b3[3] = {0, 0, 0};
+      bin_coords_div<D>(g, q, b3);
+      const unsigned b = flatten<D>(g, b3);
+      p1.key[c] = b;
+      p1.rank[c] = atomicAdd(&p1.cnt[b], 1u);
+    }
+    cluster_barrier();
+  }
+  // 2. every block: the exclusive scan of all the counts (offs[nbins] = n);
+  // block 0 also writes it to off for the pass; then the scatter of the
+  // block's own cells
+  {
+    const unsigned per = (len + kPassThreads - 1) / kPassThreads;
+    const unsigned b0 = min(len, t * per), b1 = min(len, b0 + per);
+    unsigned sum = 0;
+    for (unsigned b = b0; b < b1; ++b) sum += p1.cnt[b];
+    unsigned incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    unsigned before = 0;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    unsigned run = before + incl - sum;
+    for (unsigned b = b0; b < b1; ++b) {
+      const unsigned c = p1.cnt[b];
+      offs[b] = run;
+      if (blockIdx.x == 0) off[b] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (unsigned c = g0; c < n; c += gs) src[offs[p1.key[c]] + p1.rank[c]] = c;
+  cluster_barrier();
+  // 3. the counts cleared for the next step's epilogue (and chunk totals that
+  // the counting formed on a sparse grid), each bin in ascending id
+  // (k_order_gather)
+  for (unsigned b = g0; b < len; b += gs) p1.cnt[b] = 0u;
+  for (unsigned w = g0; w < part_words; w += gs) p1.part[w] = 0u;
+  for (unsigned u = g0; u < n; u += gs) {
+    const unsigned c = src[u], b = p1.key[c], lo = offs[b], hi = offs[b + 1];
+    const float4 v = A[c];
+    unsigned dst = u;
+    if (hi - lo > 1u) {
+      const unsigned me = id_of(v);
+      unsigned r = 0;
+      for (unsigned k = lo; k < hi; ++k) r += id_of(A[src[k]]) < me ? 1u : 0u;
+      dst = lo + r;
+    }
+    B[dst] = make_float4(v.x, v.y, v.z, __uint_as_float(b));
+    Bid[dst] = id_of(v);
+    if (PB) PB[dst] = PA[c];
+  }
+  cluster_barrier();
+  // 4. the pass(es)
+  for (int k = 0; k <= heun; ++k) {
+    const PassArgs& a = k ? p2 : p1;
+    for (unsigned blk = blockIdx.x; blk * kPassThreads < n; blk += kSmallCtas)
+      pass_gabriel_block<D, FORCE, FINDER>(g, fp, a, blk);
+    if (k < heun) cluster_barrier();
   }
 }
 

@@ -223,6 +223,7 @@ struct tecs_sim {
   int last_kernels = 0;
   // the next rebuild's bin count is done by the state-writing kernel
   bool fuse_count = false;
+  bool small_ok = true;  // small steps may take k_step_small (TECS_NO_SMALL_STEP=1: never)
   // sparse grids (bins > 4 x capacity): the counting also forms the scan's
   // chunk totals, and the rebuild needs no reduction pass over the bins
   bool fuse_part = false;
@@ -269,12 +270,23 @@ int prof_mark(tecs_sim* s, int which, const char* name) {
   if (prof_mark((s), 1, (name))) return -1
 
 
+// The cooperative Gabriel pass needs the fast-path geometry and packs bin
+// coordinates in 10 bits and slots in 27 bits.
+bool coop_geometry(const tecs_sim* s) {
+  return s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 && s->g.ext[1] <= 1024 &&
+         s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27);
+}
+// The built-in binned pass over the grid is the cooperative one
+// (k_pass_gabriel): all-pairs on its geometry, Gabriel also with c <= 0.9.
+bool coop_pass(const tecs_sim* s) {
+  const bool geom = coop_geometry(s);
+  if (s->d.finder == TECS_FINDER_BINNED_ALL_PAIRS) return geom;
+  return s->d.finder == TECS_FINDER_BINNED_GABRIEL && geom && s->d.gabriel_coefficient <= 0.9f;
+}
+
 PassFn pass_fn(const tecs_sim* s, bool sym) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
-  // the cooperative Gabriel pass needs the fast-path geometry and packs
-  // bin coordinates in 10 bits and slots in 27 bits
-  const bool coop_geom = s->g.R == 1 && s->g.bin_size >= s->d.cutoff && s->g.ext[0] <= 1024 &&
-                         s->g.ext[1] <= 1024 && s->g.ext[2] <= 1024 && s->d.capacity < (1u << 27);
+  const bool coop_geom = coop_geometry(s);
   const bool coop = coop_geom && s->d.gabriel_coefficient <= 0.9f;
 #define PICK(DD, FF)                                                            \
   if (D == DD && F == FF) {                                                     \
@@ -497,6 +509,85 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
 }
 
 // One integrator step (plus division), queued on the stream.
+// A step small enough for one cluster (k_step_small): binned, non-symmetric,
+// built-in laws, no COM fix, no division, no links, no extra fields, no old
+// velocities.
+bool small_step_ok(const tecs_sim* s) {
+  return s->binned && !s->d.symmetric && !s->d.com_fix && s->d.division_probability <= 0.0 && !s->n_links &&
+         !s->E && !s->ov && !s->law_fn && s->small_ok && s->d.capacity <= kSmallCells && s->g.nbins <= kSmallBins &&
+         coop_pass(s);
+}
+
+using SmallFn = void (*)(GridP, ForceP, PassArgs, PassArgs, int, int, const float4*, const float2*, float4*, float2*,
+                         unsigned*, unsigned*, unsigned*, unsigned);
+
+SmallFn small_fn_of(const tecs_sim* s) {
+  const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
+  if (F != TECS_FINDER_BINNED_ALL_PAIRS && F != TECS_FINDER_BINNED_GABRIEL) return nullptr;
+  const bool gab = F == TECS_FINDER_BINNED_GABRIEL;
+  if (D == 3) {
+    if (FO == 0) return gab ? k_step_small<3, 3, 0> : k_step_small<3, 1, 0>;
+    if (FO == 1) return gab ? k_step_small<3, 3, 1> : k_step_small<3, 1, 1>;
+    if (FO == 2) return gab ? k_step_small<3, 3, 2> : k_step_small<3, 1, 2>;
+  } else {
+    if (FO == 0) return gab ? k_step_small<2, 3, 0> : k_step_small<2, 1, 0>;
+    if (FO == 1) return gab ? k_step_small<2, 3, 1> : k_step_small<2, 1, 1>;
+  }
+  return nullptr;
+}
+
+// The kernel, allowed a cluster of kSmallCtas blocks (past the portable 8)
+// and shared memory for the scan of up to kSmallBins + 1 counts past the
+// default 48 KB; set once, at creation, outside any stream capture.  False if
+// such a cluster cannot be placed on this GPU (the step then runs over the
+// grid).
+bool small_fn_prepare(const tecs_sim* s) {
+  const SmallFn fn = small_fn_of(s);
+  if (!fn) return false;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kSmallCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kSmallCtas);
+  cfg.blockDim = dim3(kPassThreads);
+  cfg.dynamicSmemBytes = kSmallSmem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return clusters >= 1;
+}
+
+int launch_small(tecs_sim* s, SmallFn fn, const PassArgs& p1, const PassArgs& p2, bool pol) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kSmallCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kSmallCtas);
+  cfg.blockDim = dim3(kPassThreads);
+  cfg.dynamicSmemBytes = (s->g.nbins + 1) * sizeof(unsigned);
+  cfg.stream = s->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const unsigned part_words = s->fuse_part ? (unsigned)scan_part_words(s->g.nbins + 1) : 0u;
+  CK(cudaLaunchKernelEx(&cfg, fn, s->g, s->fp, p1, p2, s->d.integrator == TECS_HEUN ? 1 : 0,
+                        s->fuse_count ? 0 : 1, (const float4*)s->A, (const float2*)(pol ? s->PA : nullptr), s->B,
+                        pol ? s->PB : nullptr, s->Bid, s->off, s->src, part_words));
+  return 0;
+}
+
 int enqueue_step(tecs_sim* s, double dt64, bool rebuild, int& K) {
   const float dt = (float)dt64;  // VectorN * Scalar narrows dt (vector.hpp:264-267)
   const bool pol = s->d.has_polarity != 0;
@@ -508,7 +599,9 @@ int enqueue_step(tecs_sim* s, double dt64, bool rebuild, int& K) {
   const unsigned L = launch_count(s);
   const unsigned gb = ceil_div(L ? L : 1, 256);
   const int D = s->d.dims;
-  if (rebuild || !s->binned) {
+  if (rebuild && small_step_ok(s)) {
+    // k_step_small below sorts the cells itself
+  } else if (rebuild || !s->binned) {
     if (enqueue_rebuild(s, K, !s->fuse_count)) return -1;
   } else {
     PROF_BEGIN(s);
@@ -518,6 +611,41 @@ int enqueue_step(tecs_sim* s, double dt64, bool rebuild, int& K) {
     K += 1;
   }
   PassArgs a = base_args(s, dt, dt64);
+  if (rebuild && small_step_ok(s)) {
+    // the whole step in one cluster (k_step_small)
+    PassArgs p1 = a, p2 = a;
+    p1.X = s->B;
+    p1.P = pol ? s->PB : nullptr;
+    p1.Bx = s->B;
+    p1.Bp = p1.P;
+    p1.count_next = 0;
+    if (s->d.integrator == TECS_EULER) {
+      p1.mode = kEulerFused;
+      p1.count_next = s->fuse_count ? 1 : 0;
+    } else {
+      p1.mode = kHeun1Fused;
+      p1.d_out = s->d1;
+      p1.dp_out = pol ? s->dp1 : nullptr;
+      p1.Xt = s->Xt;
+      p1.Pt = pol ? s->Pt : nullptr;
+      p2.X = s->Xt;
+      p2.P = pol ? s->Pt : nullptr;
+      p2.full_step = 0;  // heun.hpp:117
+      p2.mode = kHeun2Fused;
+      p2.Bx = s->B;
+      p2.Bp = pol ? s->PB : nullptr;
+      p2.d1 = s->d1;
+      p2.dp1 = pol ? s->dp1 : nullptr;
+      p2.count_next = s->fuse_count ? 1 : 0;
+    }
+    const SmallFn fn = small_fn_of(s);
+    if (!fn) return fail("unsupported finder/force/dims combination");
+    PROF_BEGIN(s);
+    if (launch_small(s, fn, p1, p2, pol)) return -1;
+    PROF_END(s, "k_step_small");
+    K += 1;
+    return 0;
+  }
   auto store_args = [&](PassArgs& p, float4* dout, float2* dpout, int slot) {
     p.mode = kStore;
     p.d_out = dout;
@@ -715,6 +843,10 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   s->binned = desc->finder == TECS_FINDER_BINNED_ALL_PAIRS || desc->finder == TECS_FINDER_BINNED_GABRIEL;
   s->fuse_count = s->binned && (desc->division_probability > 0.0 || desc->rebuild_every_n <= 1);
   s->fuse_part = s->binned && (double)g.nbins > 4.0 * (double)desc->capacity;
+  {
+    const char* e = std::getenv("TECS_NO_SMALL_STEP");
+    s->small_ok = !(e && e[0] == '1') && s->binned && small_fn_prepare(s);
+  }
 
   const size_t cap = desc->capacity;
   auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
