@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
@@ -536,14 +537,13 @@ SmallFn small_fn_of(const tecs_sim* s) {
   return nullptr;
 }
 
-// The kernel, allowed a cluster of kSmallCtas blocks (past the portable 8)
-// and shared memory for the scan of up to kSmallBins + 1 counts past the
-// default 48 KB; set once, at creation, outside any stream capture.  False if
-// such a cluster cannot be placed on this GPU (the step then runs over the
-// grid).
-bool small_fn_prepare(const tecs_sim* s) {
-  const SmallFn fn = small_fn_of(s);
-  if (!fn) return false;
+// Every instantiation of the kernel (the force may change after creation,
+// tecs_sim_set_force), allowed a cluster of kSmallCtas blocks (past the
+// portable 8) and shared memory for the scan of up to kSmallBins + 1 counts
+// past the default 48 KB; set once per device, at the first creation, outside
+// any stream capture.  False if such a cluster cannot be placed on the GPU
+// (steps then run over the grid).
+bool small_prepare_one(SmallFn fn) {
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem) != cudaSuccess) {
     cudaGetLastError();
@@ -566,6 +566,22 @@ bool small_fn_prepare(const tecs_sim* s) {
     return false;
   }
   return clusters >= 1;
+}
+
+constexpr int kMaxDevices = 64;
+
+bool small_prepare(int device) {
+  static std::atomic<int> state[kMaxDevices];  // 0 not yet, 1 ready, 2 unavailable
+  if (device < 0 || device >= kMaxDevices) return false;
+  if (const int v = state[device].load()) return v == 1;
+  const SmallFn fns[] = {k_step_small<3, 1, 0>, k_step_small<3, 1, 1>, k_step_small<3, 1, 2>,
+                         k_step_small<3, 3, 0>, k_step_small<3, 3, 1>, k_step_small<3, 3, 2>,
+                         k_step_small<2, 1, 0>, k_step_small<2, 1, 1>, k_step_small<2, 3, 0>,
+                         k_step_small<2, 3, 1>};
+  bool ok = true;
+  for (const SmallFn fn : fns) ok = ok && small_prepare_one(fn);
+  state[device].store(ok ? 1 : 2);
+  return ok;
 }
 
 int launch_small(tecs_sim* s, SmallFn fn, const PassArgs& p1, const PassArgs& p2, bool pol) {
@@ -845,7 +861,7 @@ int tecs_sim_create(const tecs_sim_desc* desc, tecs_sim** out) {
   s->fuse_part = s->binned && (double)g.nbins > 4.0 * (double)desc->capacity;
   {
     const char* e = std::getenv("TECS_NO_SMALL_STEP");
-    s->small_ok = !(e && e[0] == '1') && s->binned && small_fn_prepare(s);
+    s->small_ok = !(e && e[0] == '1') && s->binned && small_prepare(s->d.device);
   }
 
   const size_t cap = desc->capacity;

@@ -71,3 +71,18 @@ def test_one_block_step_equals_the_multi_kernel_step(finder, integrator, dims, p
     np.testing.assert_array_equal(a.get_state()[0], b.get_state()[0])
     if every == 0:
         assert a.kernels_per_step() == 1 and b.kernels_per_step() > 1
+
+
+def test_force_changed_after_creation_takes_the_one_launch_step():
+    # tecs_sim_set_force picks another instantiation of the kernel than the
+    # one the simulation was created with; each must be ready to launch
+    L = tg.load()
+    sims = [make("binned_all_pairs", "euler", 3, False, 0, 1000, small=f) for f in (True, False)]
+    for s in sims:
+        s.take_step(0.05, 2)
+        tg._check(L.tecs_sim_set_force(s._h, 0, 0.0, 0.0, 0.0, 0.0, 0.0))  # no force
+        s.take_step(0.05, 2)
+        tg._check(L.tecs_sim_set_force(s._h, 1, 1.5, 0.6, 0.4, 0.9, 0.0))
+        s.take_step(0.05, 3)
+    np.testing.assert_array_equal(sims[0].get_state()[0], sims[1].get_state()[0])
+    assert sims[0].kernels_per_step() == 1 and sims[1].kernels_per_step() > 1
