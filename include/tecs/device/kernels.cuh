@@ -1765,13 +1765,13 @@ static __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, Pas
 }
 
 // ---------------------------------------------------------------------------
-// One step of a small simulation in one cluster of kSmallCtas blocks (up to
-// kSmallCells cells and kSmallBins bins; the binned finders on the geometry of
-// the cooperative pass, no COM fix, no division, no extra fields, built-in
-// laws): the bin counts (made by the previous step's epilogue, or here), their
-// scan, the scatter, the in-bin id order, then the pass (Euler) or both passes
-// (Heun) -- what the rebuild kernels and the fused passes do over the grid,
-// for a step whose launches would otherwise each cost more than their work.
+// One Euler step of a small simulation in one cluster of kSmallCtas blocks
+// (up to kSmallCells = 1536 cells and kSmallBins bins; the binned finders on
+// the geometry of the cooperative pass, no COM fix, no division, no extra
+// fields, built-in laws): the bin counts (made by the previous step's
+// epilogue, or here), their scan, the scatter, the in-bin id order, then the
+// pass -- what the rebuild kernels and the fused pass do over the grid, for a
+// step whose launches would otherwise each cost more than their work.
 // The phases are separated by cluster barriers (release/acquire at cluster
 // scope); every block scans all the counts into its own shared memory, so the
 // scan needs no barrier of its own; each block runs the cooperative pass
@@ -1780,7 +1780,9 @@ static __global__ void __launch_bounds__(128) k_pass_sym(GridP g, ForceP fp, Pas
 // The cluster size is set at launch (16 blocks: past the portable 8, opted
 // into per kernel).
 constexpr int kSmallCtas = 16;
-constexpr unsigned kSmallCells = 4096;
+// one block of cells per block of the cluster: past that the blocks run
+// their cells' blocks in turn, and the grid path spreads them over more SMs
+constexpr unsigned kSmallCells = kSmallCtas * kPassThreads;
 constexpr unsigned kSmallBins = 16384;
 constexpr size_t kSmallSmem = (kSmallBins + 1) * sizeof(unsigned);
 
@@ -1790,9 +1792,8 @@ __device__ __forceinline__ void cluster_barrier() {
 
 template <int D, int FINDER, int FORCE>
 static __global__ void __launch_bounds__(kPassThreads)
-    k_step_small(GridP g, ForceP fp, PassArgs p1, PassArgs p2, int heun, int run_count, const float4* A,
-                 const float2* PA, float4* B, float2* PB, unsigned* Bid, unsigned* off, unsigned* src,
-                 unsigned part_words) {
+    k_step_small(GridP g, ForceP fp, PassArgs p1, int run_count, const float4* A, const float2* PA, float4* B,
+                 float2* PB, unsigned* Bid, unsigned* off, unsigned* src, unsigned part_words) {
   extern __shared__ unsigned offs[];  // the exclusive scan of the counts, nbins + 1 words
   __shared__ unsigned wsum[kPassThreads / 32];
   const unsigned n = p1.ctr->n, t = threadIdx.x;
@@ -1860,13 +1861,9 @@ static __global__ void __launch_bounds__(kPassThreads)
     if (PB) PB[dst] = PA[c];
   }
   cluster_barrier();
-  // 4. the pass(es)
-  for (int k = 0; k <= heun; ++k) {
-    const PassArgs& a = k ? p2 : p1;
-    for (unsigned blk = blockIdx.x; blk * kPassThreads < n; blk += kSmallCtas)
-      pass_gabriel_block<D, FORCE, FINDER>(g, fp, a, blk);
-    if (k < heun) cluster_barrier();
-  }
+  // 4. the Euler pass
+  for (unsigned blk = blockIdx.x; blk * kPassThreads < n; blk += kSmallCtas)
+    pass_gabriel_block<D, FORCE, FINDER>(g, fp, p1, blk);
 }
 
 // Plain COM reduction over a delta buffer (used after the symmetric pass).

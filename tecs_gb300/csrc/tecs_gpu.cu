@@ -510,17 +510,18 @@ int enqueue_pass(tecs_sim* s, PassArgs a, int& K) {
 }
 
 // One integrator step (plus division), queued on the stream.
-// A step small enough for one cluster (k_step_small): binned, non-symmetric,
-// built-in laws, no COM fix, no division, no links, no extra fields, no old
-// velocities.
+// A step small enough for one cluster (k_step_small): Euler, binned,
+// non-symmetric, built-in laws, no COM fix, no division, no links, no extra
+// fields, no old velocities.  (Heun's two passes in one cluster, with a
+// barrier between them, were slower than over the grid.)
 bool small_step_ok(const tecs_sim* s) {
-  return s->binned && !s->d.symmetric && !s->d.com_fix && s->d.division_probability <= 0.0 && !s->n_links &&
+  return s->d.integrator == TECS_EULER && s->binned && !s->d.symmetric && !s->d.com_fix && s->d.division_probability <= 0.0 && !s->n_links &&
          !s->E && !s->ov && !s->law_fn && s->small_ok && s->d.capacity <= kSmallCells && s->g.nbins <= kSmallBins &&
          coop_pass(s);
 }
 
-using SmallFn = void (*)(GridP, ForceP, PassArgs, PassArgs, int, int, const float4*, const float2*, float4*, float2*,
-                         unsigned*, unsigned*, unsigned*, unsigned);
+using SmallFn = void (*)(GridP, ForceP, PassArgs, int, const float4*, const float2*, float4*, float2*, unsigned*,
+                         unsigned*, unsigned*, unsigned);
 
 SmallFn small_fn_of(const tecs_sim* s) {
   const int D = s->d.dims, F = s->d.finder, FO = s->d.force;
@@ -584,7 +585,7 @@ bool small_prepare(int device) {
   return ok;
 }
 
-int launch_small(tecs_sim* s, SmallFn fn, const PassArgs& p1, const PassArgs& p2, bool pol) {
+int launch_small(tecs_sim* s, SmallFn fn, const PassArgs& p1, bool pol) {
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -598,8 +599,7 @@ int launch_small(tecs_sim* s, SmallFn fn, const PassArgs& p1, const PassArgs& p2
   cfg.attrs = at;
   cfg.numAttrs = 1;
   const unsigned part_words = s->fuse_part ? (unsigned)scan_part_words(s->g.nbins + 1) : 0u;
-  CK(cudaLaunchKernelEx(&cfg, fn, s->g, s->fp, p1, p2, s->d.integrator == TECS_HEUN ? 1 : 0,
-                        s->fuse_count ? 0 : 1, (const float4*)s->A, (const float2*)(pol ? s->PA : nullptr), s->B,
+  CK(cudaLaunchKernelEx(&cfg, fn, s->g, s->fp, p1, s->fuse_count ? 0 : 1, (const float4*)s->A, (const float2*)(pol ? s->PA : nullptr), s->B,
                         pol ? s->PB : nullptr, s->Bid, s->off, s->src, part_words));
   return 0;
 }
@@ -629,35 +629,17 @@ int enqueue_step(tecs_sim* s, double dt64, bool rebuild, int& K) {
   PassArgs a = base_args(s, dt, dt64);
   if (rebuild && small_step_ok(s)) {
     // the whole step in one cluster (k_step_small)
-    PassArgs p1 = a, p2 = a;
+    PassArgs p1 = a;
     p1.X = s->B;
     p1.P = pol ? s->PB : nullptr;
     p1.Bx = s->B;
     p1.Bp = p1.P;
-    p1.count_next = 0;
-    if (s->d.integrator == TECS_EULER) {
-      p1.mode = kEulerFused;
-      p1.count_next = s->fuse_count ? 1 : 0;
-    } else {
-      p1.mode = kHeun1Fused;
-      p1.d_out = s->d1;
-      p1.dp_out = pol ? s->dp1 : nullptr;
-      p1.Xt = s->Xt;
-      p1.Pt = pol ? s->Pt : nullptr;
-      p2.X = s->Xt;
-      p2.P = pol ? s->Pt : nullptr;
-      p2.full_step = 0;  // heun.hpp:117
-      p2.mode = kHeun2Fused;
-      p2.Bx = s->B;
-      p2.Bp = pol ? s->PB : nullptr;
-      p2.d1 = s->d1;
-      p2.dp1 = pol ? s->dp1 : nullptr;
-      p2.count_next = s->fuse_count ? 1 : 0;
-    }
+    p1.mode = kEulerFused;
+    p1.count_next = s->fuse_count ? 1 : 0;
     const SmallFn fn = small_fn_of(s);
     if (!fn) return fail("unsupported finder/force/dims combination");
     PROF_BEGIN(s);
-    if (launch_small(s, fn, p1, p2, pol)) return -1;
+    if (launch_small(s, fn, p1, pol)) return -1;
     PROF_END(s, "k_step_small");
     K += 1;
     return 0;
