@@ -63,6 +63,7 @@ PASS_BYTES = {
     "k_pass_euler": (32, 16),   # read x, write x'                (+ p, p')
     "k_pass_heun1": (48, 24),   # read x, write d1, x~            (+ p, dp1, p~)
     "k_pass_heun2": (64, 32),   # read x~, x, d1, write x'        (+ p~, p, dp1, p')
+    "k_step_small": (32, 16),   # the one-launch Euler step: read x, write x' (+ p, p')
 }
 
 
@@ -498,7 +499,9 @@ def run_gb300(args):
     tpc = traffic_per_pass(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": (tpc * n_avg if tpc else None),
-                "kernel": "force pass (k_pass_*: pair finding + force + fused integrator epilogue)",
+                "kernel": ("one-launch Euler step (k_step_small: bin sort + pair finding + force + integrator)"
+                           if "k_step_small" in kern else
+                           "force pass (k_pass_*: pair finding + force + fused integrator epilogue)"),
                 "bytes_per_launch": bytes_per_launch * n_avg / n_prof,
                 "peak_kind": f"{peak_kind} hbm_gbs", "avg_launch_ms": 1e3 * pass_launch_s,
                 "avg_launch_ms_basis": "the pass's share of the profiled step (per-kernel CUDA events) times "
