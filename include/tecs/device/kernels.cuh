@@ -1398,304 +1398,22 @@ __device__ __forceinline__ int cix(int q, int c) { return q * kPassThreads + (c 
 // FINDER 3: binned Gabriel; FINDER 1: binned all-pairs (i's bin by
 // multiplication, binned_all_pairs.hpp:103-109, and every in-cutoff pair
 // accepted: no phase 2).
+// The grid pass: block blockIdx.x's cells.
+template <int D, int FORCE, int FINDER = 3>
+static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
+#define TECS_PASS_BLOCK blockIdx.x
+#include "pass_gabriel_body.inc"
+#undef TECS_PASS_BLOCK
+}
+
 // One block's cells blk * kPassThreads .. (only warp-level synchronisation,
 // so a kernel may run several blocks' cells one after another).
 template <int D, int FORCE, int FINDER = 3>
 __device__ __forceinline__ void pass_gabriel_block(const GridP& g, const ForceP& fp, const PassArgs& a,
                                                    const unsigned blk) {
-  static_assert(FORCE <= 1 || (FORCE == 2 && D == 3), "spring laws, or the 3-D polarity law");
-  static_assert(FINDER == 1 || FINDER == 3, "the binned finders");
-  constexpr bool POL = FORCE == 2;
-  constexpr int NB = kMaxNb;  // neighbour slots per cell (more: the per-thread path)
-  __shared__ float4 cand[NB * kPassThreads];           // [q][t]: position, w = (slot << 5) | bin code
-  __shared__ float4 home[kPassThreads];                // position, w = packed bin coords
-  __shared__ unsigned short pinfo[NB * kPassThreads];  // each warp's pairs: (t << 4) | q
-  __shared__ unsigned short wcls[kPassThreads / 32][NB + 1];  // pairs per (warp, neighbour count)
-  __shared__ unsigned amask[kPassThreads];             // accepted pairs of each cell, bit q
-  __shared__ unsigned char ncnt[kPassThreads];
-  __shared__ unsigned char fallback[kPassThreads];
-
-  const unsigned n = a.ctr->n;
-  const int t = threadIdx.x;
-  const unsigned i = blk * kPassThreads + t;
-  const bool active = i < n;
-  float xi[3] = {0.f, 0.f, 0.f};
-  float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
-  float2 pi = make_float2(0.f, 0.f);
-  int bc[3] = {0, 0, 0};
-  int cnt = 0;
-  bool fb = false;
-  // ---- phase 1: in-cutoff neighbours of this thread's cell.  The row
-  // offsets of all 3x3 neighbour rows are fetched first, then the three rows
-  // of each z-plane are scanned together two candidates at a time, so each
-  // thread keeps several loads in flight; a candidate's bin comes with its
-  // position (B.w holds the bin key).
-  if (active) {
-    vi = __ldg(&a.X[i]);
-    xi[0] = vi.x; xi[1] = vi.y; xi[2] = vi.z;
-    if (a.P) pi = a.P[i];
-    if (FINDER == 1) bin_coords_mul<D>(g, xi, bc);
-    else bin_coords_div<D>(g, xi, bc);
-    constexpr int kRows = D >= 3 ? 9 : 3;
-    unsigned rlo[kRows], rhi[kRows], rb0[kRows];
-    const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, g.ext[0] - 1);
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      const int dy = r % 3 - 1, dz = D >= 3 ? r / 3 - 1 : 0;
-      const int cy = bc[1] + dy, cz = D >= 3 ? bc[2] + dz : 0;
-      const bool ok = cy >= 0 && cy < g.ext[1] && (D < 3 || (cz >= 0 && cz < g.ext[2]));
-      int c0[3] = {x0, ok ? cy : 0, ok ? cz : 0};
-      const unsigned b0 = flatten<D>(g, c0);
-      rb0[r] = b0;
-      rlo[r] = ok ? __ldg(&a.off[b0]) : 0u;
-      rhi[r] = ok ? __ldg(&a.off[b0 + (unsigned)(x1 - x0) + 1u]) : 0u;
-    }
-    // 1: test the candidates three rows (one z-plane) at a time and append
-    // the in-cutoff ones at once: rows are visited in the reference's task
-    // order and positions ascend within a row, so the list is in candidate order
-    const int rxo = x0 - bc[0] + 1;
-#pragma unroll
-    for (int g0 = 0; g0 < kRows; g0 += 3) {
-      unsigned len[3];
-      unsigned lmax = 0u;
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        len[q] = rhi[g0 + q] - rlo[g0 + q];
-        lmax = max(lmax, len[q]);
-      }
-      if (lmax > 32u) fb = true;
-      if (fb) continue;
-      unsigned m[3] = {0u, 0u, 0u};
-      // whole rounds of two slots per row; a slot past its row's end reads
-      // the cells that follow (padded arrays) and is masked off below
-      for (unsigned o = 0; o < lmax; o += 2u) {
-        float4 v[3][2];
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-#pragma unroll
-          for (int k = 0; k < 2; ++k) v[q][k] = __ldg(&a.X[rlo[g0 + q] + o + k]);
-        const unsigned bit[2] = {1u << o, 2u << o};  // o <= 30
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            const float e0 = xi[0] - v[q][k].x, e1 = xi[1] - v[q][k].y;
-            float d2 = e0 * e0 + e1 * e1;
-            if (D >= 3) { const float e2 = xi[2] - v[q][k].z; d2 = d2 + e2 * e2; }
-            if (d2 < fp.rc2) m[q] |= bit[k];
-          }
-      }
-      // the row's own slots only, and never the cell itself
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        m[q] &= len[q] >= 32u ? 0xffffffffu : (1u << len[q]) - 1u;
-        const unsigned self = i - rlo[g0 + q];
-        if (self < len[q]) m[q] &= ~(1u << self);
-      }
-      // append this plane's rows in order
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const int r = g0 + q;
-        const unsigned rowcode = 3u * (unsigned)(r % 3) + 9u * (unsigned)(D >= 3 ? r / 3 : 1);
-        unsigned mm = m[q];
-        if (cnt + __popc(mm) > NB) { fb = true; break; }
-        while (mm) {
-          const unsigned j = rlo[r] + (unsigned)(__ffs(mm) - 1);
-          mm &= mm - 1u;
-          const float4 v = __ldg(&a.X[j]);
-          const unsigned rx = (unsigned)((int)(__float_as_uint(v.w) - rb0[r]) + rxo);
-          cand[cix(cnt, t)] = make_float4(v.x, v.y, v.z, __uint_as_float((j << 5) | (rowcode + rx)));
-          ++cnt;
-        }
-      }
-    }
-  }
-  if (fb) cnt = 0;
-  home[t] = make_float4(xi[0], xi[1], xi[2],
-                        __uint_as_float((unsigned)bc[0] | ((unsigned)bc[1] << 10) | ((unsigned)bc[2] << 20)));
-  ncnt[t] = (unsigned char)cnt;
-  fallback[t] = fb ? 1 : 0;
-  // Phases 2-4 run per warp over the warp's own 32 cells (no block
-  // barrier).  Pair offsets: the warp's pairs sorted by their cell's
-  // neighbour count, so that the Gabriel loops of a round of pairs run the
-  // same length.  The cells of one count are ranked (match_any), the first
-  // records the class's pairs, and lane v forms class v's base.
-  const int lane = t & 31, warp = t >> 5;
-  unsigned short* const wp = pinfo + warp * 32 * NB;
-  int P = 0, P1 = 0;
-  {
-    if (lane <= NB) wcls[warp][lane] = 0;
-    __syncwarp();
-    const unsigned same = __match_any_sync(0xffffffffu, cnt);
-    const int rank = __popc(same & ((1u << lane) - 1u));
-    if (rank == 0) wcls[warp][cnt] = (unsigned short)(__popc(same) * (unsigned)cnt);
-    // a single neighbour has no witness: accepted (cnt <= 16)
-    amask[t] = FINDER == 1 ? (1u << cnt) - 1u : (cnt == 1 ? 1u : 0u);
-    __syncwarp();
-    const unsigned tot = lane <= NB ? (unsigned)wcls[warp][lane] : 0u;
-    unsigned incl = tot;
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    P = (int)__shfl_sync(0xffffffffu, incl, NB);
-    P1 = (int)__shfl_sync(0xffffffffu, incl, 1);  // the pairs of single-neighbour cells come first
-    const int base = (int)__shfl_sync(0xffffffffu, incl - tot, cnt) + rank * cnt;
-    for (int q = 0; q < cnt; ++q) wp[base + q] = (unsigned short)((t << 4) | q);
-  }
-  __syncwarp();
-
-  // ---- phase 2: Gabriel test, one pair per thread at a time.  A witness k
-  // blocks (i, j) when it is inside the ball (|x_k - m|^2 < r^2) and its bin
-  // lies in the ball's bin range; the range (sqrt + floors) is only worked out
-  // for the rare k that pass the distance test.
-  for (int p = P1 + lane; p < (FINDER == 3 ? P : 0); p += 32) {
-    const unsigned info = wp[p];
-    const int c = (int)(info >> 4), q = (int)(info & 15u);
-    const float4 h = home[c];
-    const float4 vj = cand[cix(q, c)];
-    const float hx[3] = {h.x, h.y, h.z};
-    float disp[3];
-    disp[0] = hx[0] - vj.x;
-    disp[1] = hx[1] - vj.y;
-    disp[2] = D >= 3 ? hx[2] - vj.z : 0.f;
-    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
-    if (D >= 3) d2 = d2 + disp[2] * disp[2];
-    float m[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int d = 0; d < D; ++d) m[d] = hx[d] - disp[d] * 0.5f;
-    const float rsq = d2 * fp.gab_factor;
-    const int cc = ncnt[c];
-    // every witness, two per round and without branches: bit w of hits is a
-    // witness inside the ball (an odd count's last round tests one twice)
-    unsigned hits = 0u, bit = 1u;
-    for (int w = 0; w < cc; w += 2) {
-      const int w1 = min(w + 1, cc - 1);
-      const float4 vk0 = cand[cix(w, c)], vk1 = cand[cix(w1, c)];
-      const float f0 = vk0.x - m[0], f1 = vk0.y - m[1];
-      const float g0 = vk1.x - m[0], g1 = vk1.y - m[1];
-      float sd0 = f0 * f0 + f1 * f1, sd1 = g0 * g0 + g1 * g1;
-      if (D >= 3) {
-        const float f2 = vk0.z - m[2], g2 = vk1.z - m[2];
-        sd0 = sd0 + f2 * f2;
-        sd1 = sd1 + g2 * g2;
-      }
-      if (sd0 < rsq) hits |= bit;
-      if (sd1 < rsq) hits |= bit << 1;
-      bit <<= 2;
-    }
-    hits &= ((1u << cc) - 1u) & ~(1u << q);
-    bool blocked = false;
-    if (hits) {
-      // binned_gabriel.hpp:142-153: a witness in the ball blocks only from a
-      // bin overlapping the ball, [lo, hi] per axis relative to the cell's bin
-      const unsigned hb = __float_as_uint(h.w);
-      const int hbc[3] = {(int)(hb & 1023u), (int)((hb >> 10) & 1023u), (int)(hb >> 20)};
-      const float r = sqrtf(rsq);
-      int lo[3] = {-1, -1, -1}, hi[3] = {1, 1, 1};
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        lo[d] = clampi((int)floorf((m[d] - r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-        hi[d] = clampi((int)floorf((m[d] + r - g.mn[d]) * g.inv_bin), g.ext[d] - 1) - hbc[d];
-      }
-      while (hits && !blocked) {
-        const int w = __ffs(hits) - 1;
-        hits &= hits - 1u;
-        const unsigned code = __float_as_uint(cand[cix(w, c)].w) & 31u;
-        const int rel[3] = {(int)(code % 3u) - 1, (int)((code / 3u) % 3u) - 1, (int)(code / 9u) - 1};
-        bool inside = true;
-#pragma unroll
-        for (int d = 0; d < D; ++d) inside = inside && rel[d] >= lo[d] && rel[d] <= hi[d];
-        blocked = inside;
-      }
-    }
-    if (!blocked) atomicOr(&amask[c], 1u << q);
-  }
-  __syncwarp();
-  // the warp's accepted pairs, cell by cell, written over the pair list
-  // (phase 2 has finished reading it)
-  int PA = 0;
-  {
-    const unsigned acc_bits = fallback[t] ? 0u : amask[t];
-    const int na = __popc(acc_bits);
-    int incl = na;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    PA = __shfl_sync(0xffffffffu, incl, 31);
-    int base = incl - na;
-    __syncwarp();
-    for (unsigned b = acc_bits; b; b &= b - 1u) wp[base++] = (unsigned short)((t << 4) | (__ffs(b) - 1));
-  }
-  __syncwarp();
-  // ---- phase 3: forces of the accepted pairs, written over the candidate slot
-  for (int p = lane; p < PA; p += 32) {
-    const unsigned info = wp[p];
-    const int c = (int)((info >> 4) & 127u), q = (int)(info & 15u);
-    const float4 h = home[c];
-    const float4 vj = cand[cix(q, c)];
-    float disp[3];
-    disp[0] = h.x - vj.x;
-    disp[1] = h.y - vj.y;
-    disp[2] = D >= 3 ? h.z - vj.z : 0.f;
-    float d2 = disp[0] * disp[0] + disp[1] * disp[1];
-    if (D >= 3) d2 = d2 + disp[2] * disp[2];
-    if (a.pairs) {
-      const unsigned j = __float_as_uint(vj.w) >> 5;
-      const unsigned ci = blk * kPassThreads + c;
-      unsigned long long s = atomicAdd(&a.ctr->pair_count, 1ull);
-      if (s < a.pair_cap) a.pairs[s] = make_uint2(id_at(a.X, a.Bid, ci), id_at(a.X, a.Bid, j));
-    }
-    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float dist = sqrtf(d2);
-    if (FORCE == 1 && dist != 0.0f) {
-      // (displacement * F) / distance, forces/predefined.hpp:134-143; a zero
-      // F gives +-0 terms, which leave the cell's sum (never -0) unchanged,
-      // so the +0 left in f adds the same
-      const float F = fp.k_rep * fmaxf(fp.r_rep - dist, 0.0f) - fp.k_adh * fmaxf(dist - fp.r_adh, 0.0f);
-      if (F != 0.0f) {
-        f.x = (disp[0] * F) / dist;
-        f.y = (disp[1] * F) / dist;
-        if (D >= 3) f.z = (disp[2] * F) / dist;
-      }
-    }
-    // the polarity law's pairs are summed term by term in phase 4: the
-    // candidate keeps its position
-    if (!POL) cand[cix(q, c)] = f;
-  }
-  __syncwarp();
-  // ---- phase 4: ordered per-cell sums
-  Acc acc = {{0.f, 0.f, 0.f}, {0.f, 0.f}};
-  if (active) {
-    if (fallback[t]) {
-      cell_general<D, FINDER, FORCE>(g, fp, a, n, i, xi, pi, id_at(a.X, a.Bid, i), acc);
-    } else {
-      for (int q = 0; q < cnt; ++q) {
-        if (!((amask[t] >> q) & 1u)) continue;
-        const float4 f = cand[cix(q, t)];
-        if (POL) {
-          // the pair's spring, bending vector, bending and alignment terms,
-          // each added to the sums in turn (polarity.hpp:131-198)
-          const float disp[3] = {xi[0] - f.x, xi[1] - f.y, xi[2] - f.z};
-          float d2 = disp[0] * disp[0] + disp[1] * disp[1];
-          d2 = d2 + disp[2] * disp[2];
-          const float2 pj = __ldg(&a.P[__float_as_uint(f.w) >> 5]);
-          pair_force<3, 2>(fp, disp, sqrtf(d2), pi, pj, acc);
-          continue;
-        }
-        acc.x[0] = acc.x[0] + f.x;
-        acc.x[1] = acc.x[1] + f.y;
-        if (D >= 3) acc.x[2] = acc.x[2] + f.z;
-      }
-    }
-  }
-  pass_epilogue<D>(g, a, active, n, i, xi, vi, pi, acc);
-}
-
-template <int D, int FORCE, int FINDER = 3>
-static __global__ void __launch_bounds__(kPassThreads) k_pass_gabriel(GridP g, ForceP fp, PassArgs a) {
-  pass_gabriel_block<D, FORCE, FINDER>(g, fp, a, blockIdx.x);
+#define TECS_PASS_BLOCK blk
+#include "pass_gabriel_body.inc"
+#undef TECS_PASS_BLOCK
 }
 
 // Symmetric finders (…_symmetric.hpp): only j with a smaller id, +delta to the

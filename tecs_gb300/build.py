@@ -34,7 +34,7 @@ DEVICE_HEADERS = PKG.parent / "include" / "tecs" / "device"
 
 def sources():
     return (sorted(CSRC.glob("*.cu")) + sorted(DEVICE_HEADERS.glob("*.cuh")) +
-            [PKG.parent / "include" / "tecs_gpu.h"])
+            sorted(DEVICE_HEADERS.glob("*.inc")) + [PKG.parent / "include" / "tecs_gpu.h"])
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
